@@ -1,0 +1,458 @@
+"""CPU restatement of lyspeq's per-chunk QMLE path (test infrastructure).
+
+This module is the oracle that travels: it re-states, in numpy with the same
+LAPACK/BLAS routines (through scipy's bundled OpenBLAS), what lyspeq's C++
+does for one Newton-Raphson iteration.  It is imported only by the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``, always as
+the checker or the reported CPU baseline, never as the product path.
+
+Parity of this restatement is pinned against the reference itself, compiled
+from its own sources (oracle/refbuild), on identical inputs; the reference
+build is in turn pinned against lyspeq's golden files
+(tests/truth/test_it1_*.dat).
+
+Each step cites the reference lines it follows.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+from scipy.linalg import lapack
+
+C_KMS = 299792.458
+LYA_REST = 1215.67
+DOUBLE_EPSILON = 1e-15
+MIN_PIXELS_IN_FILE = 100          # core/one_qso_estimate.cpp:14
+
+
+@dataclasses.dataclass
+class Settings:
+    """The config values the per-chunk path reads (core/global_numbers.cpp:93-173)."""
+    max_forest_length: float = 3.5e4
+    number_of_chunks: int = 1
+    max_pixel_length_v: float = 150.0
+    cont_logl_order: int = 1
+    cont_l_order: int = -1
+    turn_off_sfid: bool = False
+
+    @property
+    def max_forest_length_v(self):
+        return self.max_forest_length / max(1, self.number_of_chunks)
+
+    @property
+    def min_forest_length_v(self):
+        return 0.90 / 2 * self.max_forest_length_v
+
+    @property
+    def cont_nvecs(self):
+        # core/global_numbers.cpp:78-90
+        if self.cont_logl_order >= 0 or self.cont_l_order >= 0:
+            n = 1
+            if self.cont_logl_order > 0:
+                n += self.cont_logl_order
+            if self.cont_l_order > 0:
+                n += self.cont_l_order
+            return n
+        return 0
+
+
+@dataclasses.dataclass
+class ChunkData:
+    """Host-side chunk, as Chunk::Chunk leaves it (core/chunk_estimate.cpp:141-257)."""
+    wave: np.ndarray           # lambda / LYA_REST
+    delta: np.ndarray
+    ivar: np.ndarray
+    r_fwhm: int
+    dv: float
+    res_index: int
+    kbin_upp: int
+    zbin_low: int
+    zbin_upp: int
+    nq: int
+    fisher_index_start: int
+
+    @property
+    def n(self):
+        return len(self.wave)
+
+
+def _median_sorted(a):
+    n = len(a)
+    return (a[n // 2 - 1] + a[n // 2]) / 2 if n % 2 == 0 else a[n // 2]
+
+
+def _median(v):
+    return _median_sorted(np.sort(v))
+
+
+def _c_round(x):
+    return math.floor(x + 0.5) if x >= 0 else math.ceil(x - 0.5)
+
+
+def find_redshift_bin(bins, z):
+    """core/global_numbers.cpp:344-355."""
+    if z < bins.z_lower:
+        return -1
+    r = int((z - bins.z_lower) / bins.dz)
+    return min(r, bins.nz)
+
+
+def cut_masked_boundary(ivar):
+    """QSOFile::_cutMaskedBoundary, io/qso_file.cpp:139-157: (start, stop)."""
+    nz = np.flatnonzero(ivar != 0)
+    if len(nz) == 0:
+        raise ValueError("Empty spectrum when masked pixels at boundary are removed!")
+    return int(nz[0]), int(nz[-1]) + 1
+
+
+def preprocess_spectrum(spec, bins):
+    """Reading and cleaning of one binary spectrum: io/qso_file.cpp:352-369
+    (sigma -> ivar), :189-230 (maskOutliers), :159-187 (cutBoundary) and
+    core/one_qso_estimate.cpp:52-100.  Returns (wave, delta, ivar) in
+    Angstrom, or raises ValueError when the reference would drop the file."""
+    wave = np.array(spec.wave, dtype=np.float64)
+    delta = np.array(spec.delta, dtype=np.float64)
+    ivar = 1.0 / (np.asarray(spec.sigma, dtype=np.float64) ** 2)
+    ivar[ivar < DOUBLE_EPSILON] = 0.0
+    # maskOutliers (factor 5)
+    good = ivar != 0
+    realsize = int(good.sum())
+    tmp = delta[good]
+    med = _median(tmp.copy())
+    mad = 1.4826 * (1.0 + 1.0 / math.sqrt(realsize)) * _median(np.abs(tmp - med))
+    mad = max(1.0, mad)
+    for i in np.flatnonzero(good):
+        s = 5.0 * max(1.0 / math.sqrt(ivar[i]), mad)
+        fup = math.exp(1.663e-03 * (wave[i] / LYA_REST) ** 4.107)
+        if delta[i] < (-1.0 - s) or delta[i] > (fup + s):
+            delta[i] = 0.0
+            ivar[i] = 0.0
+    # cutBoundary
+    l1, l2 = LYA_REST * (1 + bins.z_lower), LYA_REST * (1 + bins.z_upper)
+    wi1 = int(np.searchsorted(wave, l1, side="left"))
+    wi2 = int(np.searchsorted(wave, l2, side="right"))
+    if wi1 == len(wave) or wi2 == 0:
+        raise ValueError("Empty spectrum when redshift boundary is applied!")
+    wave, delta, ivar = wave[wi1:wi2], delta[wi1:wi2], ivar[wi1:wi2]
+    a, b = cut_masked_boundary(ivar)
+    wave, delta, ivar = wave[a:b], delta[a:b], ivar[a:b]
+    if int((ivar != 0).sum()) < MIN_PIXELS_IN_FILE:
+        raise ValueError("Short file")
+    return wave, delta, ivar
+
+
+def decide_indices(wave, settings):
+    """OneQSOEstimate::decideIndices, core/one_qso_estimate.cpp:17-50."""
+    vel = C_KMS * np.log(wave / wave[0])
+    vmax = vel[-1]
+    nchunks = 1
+    if settings.number_of_chunks > 1:
+        nchunks += int(vmax / settings.max_forest_length_v)
+        vmax = min(settings.max_forest_length_v, vmax / nchunks)
+    idx = [0]
+    vl = 0
+    vel = vel.copy()
+    for _ in range(nchunks):
+        jj = vl + int(np.searchsorted(vel[vl:], vmax, side="right"))
+        idx.append(jj)
+        if jj == len(wave):
+            break
+        vl = jj
+        vel[vl:] -= vel[vl]
+    return idx
+
+
+def make_chunk(wave, delta, ivar, r_fwhm, bins, table_keys, settings):
+    """Chunk::Chunk, core/chunk_estimate.cpp:141-257 (raises ValueError where
+    the reference throws).  table_keys maps (R, dv rounded to 0.1) -> index."""
+    a, b = cut_masked_boundary(ivar)
+    wave, delta, ivar = wave[a:b].copy(), delta[a:b].copy(), ivar[a:b].copy()
+    n = len(wave)
+    realsize = int((ivar != 0).sum())
+    dv = _median(np.log(wave[1:] / wave[:-1]) * C_KMS) if n > 1 else -1.0
+    lenv = C_KMS * math.log(wave[-1] / wave[0]) if n else 0.0
+    minnopix = int(lenv / settings.max_pixel_length_v)
+    if realsize < minnopix or lenv < settings.min_forest_length_v:
+        raise ValueError("Short chunk")
+    rounded = _c_round(dv * 10) / 10
+    res_index = -1
+    for (r, tdv), idx in table_keys.items():
+        if r == r_fwhm and abs(rounded - tdv) < 0.01:
+            res_index = idx
+            break
+    if res_index < 0:
+        raise KeyError(f"SpecRes R: {r_fwhm}, dv: {dv} not found in tables!")
+    zmin, zmax = wave[0] / LYA_REST - 1, wave[-1] / LYA_REST - 1
+    kbin_upp = int(np.searchsorted(bins.k_centers, 0.85 * (math.pi / dv), side="left"))
+    zlow, zupp = find_redshift_bin(bins, zmin), find_redshift_bin(bins, zmax)
+    nq = zupp - zlow + 1
+    fis = zlow * bins.nk
+    if bins.triangular:
+        if zmin < bins.z_centers[zlow] and zlow != 0:
+            nq += 1
+            fis -= bins.nk
+        if bins.z_centers[zupp] < zmax and zupp < bins.nz - 1:
+            nq += 1
+    nq *= bins.nk
+    return ChunkData(wave / LYA_REST, delta, ivar, int(r_fwhm), float(dv), res_index, kbin_upp,
+                     zlow, zupp, nq, fis)
+
+
+def chunks_from_spectra(spectra, bins, table_keys, settings):
+    """OneQSOEstimate construction for every spectrum; chunks the reference
+    would reject are skipped, as OneQSOEstimate::OneQSOEstimate does."""
+    out = []
+    for s in spectra:
+        try:
+            wave, delta, ivar = preprocess_spectrum(s, bins)
+        except ValueError:
+            continue
+        idx = decide_indices(wave, settings)
+        for i1, i2 in zip(idx[:-1], idx[1:]):
+            try:
+                out.append(make_chunk(wave[i1:i2], delta[i1:i2], ivar[i1:i2], s.r_fwhm, bins,
+                                      table_keys, settings))
+            except (ValueError, KeyError):
+                continue
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Per-chunk QMLE (core/chunk_estimate.cpp:384-914)
+
+def interp1d(y, x1, dx, x):
+    """DiscreteInterpolation1D::evaluate, mathtools/discrete_interpolation.cpp:61-72."""
+    xx = (x - x1) / dx
+    n = np.trunc(xx).astype(np.int64)
+    n = np.clip(n, 0, len(y) - 2)
+    dn = xx - n
+    return y[n] * (1 - dn) + y[n + 1] * dn
+
+
+def interp2d(zarr, nx, ny, x1, dx, y1, dy, x, y):
+    """DiscreteInterpolation2D::evaluate, mathtools/discrete_interpolation.cpp:221-242;
+    zarr is flat with x fastest (index nx + Nx * ny)."""
+    xx, yy = (x - x1) / dx, (y - y1) / dy
+    ix = np.clip(np.trunc(xx).astype(np.int64), 0, nx - 2)
+    iy = np.clip(np.trunc(yy).astype(np.int64), 0, ny - 2)
+    ind = ix + nx * iy
+    dnx, dny = xx - ix, yy - iy
+    return (zarr[ind] * (1 - dnx) * (1 - dny) + zarr[ind + 1] * dnx * (1 - dny)
+            + zarr[ind + nx] * (1 - dnx) * dny + zarr[ind + nx + 1] * dnx * dny)
+
+
+def zbin_weight(bins, zm, z):
+    """Redshift weights of bin zm, element-wise form of
+    core/global_numbers.cpp:393-471 (the reference applies them along sorted
+    rows; on a sorted row these conditions select the same elements)."""
+    zc, dz = bins.z_centers[zm], bins.dz
+    out = np.zeros_like(z)
+    if (not bins.triangular) or bins.nz == 1:
+        out[(z >= zc - dz / 2) & (z <= zc + dz / 2)] = 1.0
+        return out
+    inside = (z >= zc - dz) & (z <= zc + dz)
+    out[inside] = 1.0 - np.abs(z[inside] - zc) / dz
+    if zm == 0:
+        out[z < zc] = 1.0
+    if zm == bins.nz - 1:
+        out[z > zc] = 1.0
+    return out
+
+
+def _sym_upper(a):
+    return np.triu(a) + np.triu(a, 1).T
+
+
+def lu_inverse(a):
+    """LAPACKE_InvertMatrixLU, mathtools/matrix_helper.cpp:184-204."""
+    lu, piv, info = lapack.dgetrf(a)
+    if info != 0:
+        raise np.linalg.LinAlgError("ERROR in LU decomposition.")
+    inv, info = lapack.dgetri(lu, piv)
+    if info != 0:
+        raise np.linalg.LinAlgError("ERROR in LU invert.")
+    return inv
+
+
+@dataclasses.dataclass
+class TableView:
+    """The interpolation grids SQLookupTable builds (core/sq_table.cpp:148-175, 325-368)."""
+    deriv: np.ndarray      # nk x nv
+    signal: np.ndarray     # nv x nz (z fastest)
+    v1: float
+    dv: float
+    z1: float
+    dz: float
+
+
+def table_view(table, bins, nv, lenv, nzp):
+    lenz = bins.dz * (bins.nz + 1)
+    return TableView(np.asarray(table.deriv), np.asarray(table.signal), 0.0, lenv / (nv - 1.0),
+                     bins.z_centers[0] - bins.dz, lenz / (nzp - 1.0))
+
+
+def build_matrices(ch: ChunkData, bins, tv: TableView):
+    """v/z matrices, stored Q_k with redshift weights, and S_fid
+    (core/chunk_estimate.cpp:384-536, :861-882).  Returns (stored i_kz list,
+    Q stack [ns, n, n], S)."""
+    n = ch.n
+    li, lj = ch.wave[:, None], ch.wave[None, :]
+    vmat = C_KMS * np.log(lj / li)
+    zmat = np.sqrt(li * lj) - 1.0
+    iu = np.triu_indices(n)
+    stored = [i for i in range(ch.nq) if (i + ch.fisher_index_start) % bins.nk < ch.kbin_upp]
+    ns = len(stored)
+    q = np.empty((ns, n, n))
+    vu = vmat[iu]
+    for kn in range(ch.kbin_upp):
+        m = np.empty((n, n))
+        m[iu] = interp1d(tv.deriv[kn], tv.v1, tv.dv, vu)
+        q[kn] = _sym_upper_fill(m)
+    for s in range(ch.kbin_upp, ns):
+        q[s] = q[stored[s] % bins.nk]
+    nzp = tv.signal.shape[1]
+    sm = np.empty((n, n))
+    sm[iu] = interp2d(tv.signal.ravel(), nzp, tv.signal.shape[0], tv.z1, tv.dz, tv.v1, tv.dv,
+                      zmat[iu], vu)
+    sm = _sym_upper_fill(sm)
+    zu = zmat[iu]
+    nzb = ns // ch.kbin_upp
+    for iz in range(nzb):
+        zm = ch.fisher_index_start // bins.nk + iz
+        w = np.zeros((n, n))
+        w[iu] = zbin_weight(bins, zm, zu)
+        w = _sym_upper_fill(w)
+        q[iz * ch.kbin_upp:(iz + 1) * ch.kbin_upp] *= w[None]
+    return stored, q, sm
+
+
+def _sym_upper_fill(m):
+    """mxhelp::copyUpperToLower (mathtools/matrix_helper.cpp:81-94)."""
+    il = np.tril_indices(m.shape[0], -1)
+    m[il] = m.T[il]
+    return m
+
+
+def inverse_covariance(ch: ChunkData, stored, q, sm, theta, settings):
+    """Chunk::setInvertCovarianceMatrix, core/chunk_estimate.cpp:668-719, with
+    _addMarginalizations :576-665."""
+    n = ch.n
+    cov = np.zeros((n, n)) if settings.turn_off_sfid else sm.copy()
+    for s, ikz in enumerate(stored):
+        cov += theta[ch.fisher_index_start + ikz] * q[s]
+    cov *= ch.ivar[:, None]
+    cov[np.diag_indices(n)] += 1.0
+    cinv = lu_inverse(cov)
+    cinv *= ch.ivar[None, :]
+    nvec = settings.cont_nvecs
+    if nvec > 0:
+        vecs = [np.full(n, 1.0 / math.sqrt(n))]
+        for cmo in range(1, settings.cont_logl_order + 1):
+            v = np.log(ch.wave) ** cmo
+            vecs.append(v * (1.0 / np.linalg.norm(v)))
+        for cmo in range(1, settings.cont_l_order + 1):
+            v = ch.wave ** cmo
+            vecs.append(v * (1.0 / np.linalg.norm(v)))
+        a = np.stack(vecs, axis=1)                 # n x nvec, column-major view of marg_mat
+        u, svals, _vt, info = lapack.dgesvd(a, compute_uv=1, full_matrices=0)
+        if info != 0:
+            raise np.linalg.LinAlgError("ERROR in SVD.")
+        nuse = nvec
+        while nuse > 0 and not (svals[nuse - 1] / svals[0] > DOUBLE_EPSILON):
+            nuse -= 1
+        for i in range(nuse):
+            v = u[:, i]
+            y = _sym_upper(cinv) @ v
+            norm = -1.0 / np.dot(v, y)
+            cinv += norm * np.outer(y, y)
+    return cinv
+
+
+def chunk_iteration(ch: ChunkData, bins, tv: TableView, theta, settings, compute_fisher=True):
+    """Chunk::oneQSOiteration for one chunk: returns (d, b, t, F) with
+    F (nq x nq) upper triangle filled and not halved (core/chunk_estimate.cpp:738-914)."""
+    stored, q, sm = build_matrices(ch, bins, tv)
+    cinv = inverse_covariance(ch, stored, q, sm, theta, settings)
+    n, nq, ns = ch.n, ch.nq, len(stored)
+    d, b, t = np.zeros(nq), np.zeros(nq), np.zeros(nq)
+    y = _sym_upper(cinv) @ ch.delta
+    for s, ikz in enumerate(stored):
+        d[ikz] = y @ (_sym_upper(q[s]) @ y)
+    a = np.matmul(cinv[None], q)                   # C^-1 Q_k, :721-736
+    wn = np.zeros((n, n))
+    good = ch.ivar != 0
+    wn[good] = (1.0 / ch.ivar[good])[:, None] * cinv[good]
+    a2 = a.reshape(ns, -1)
+    b[stored] = a2 @ wn.ravel()
+    if not settings.turn_off_sfid:
+        ws = sm @ cinv
+        t[stored] = a2 @ ws.ravel()
+    fisher = np.zeros((nq, nq))
+    if compute_fisher:
+        at = np.ascontiguousarray(a.transpose(0, 2, 1)).reshape(ns, -1)
+        f = at @ a2.T                              # F_ij = <A_i^T, A_j>
+        idx = np.array(stored)
+        fu = np.triu(f)
+        fisher[np.ix_(idx, idx)] = fu
+    return d, b, t, fisher
+
+
+# ---------------------------------------------------------------------------
+# Global step (core/quadratic_estimate.cpp:456-457, 261-318;
+# mathtools/matrix_helper.cpp:220-358)
+
+def accumulate(nkz, results):
+    """Sum per-chunk (fisher_index_start, d, b, t, F) into the global arrays
+    (core/chunk_estimate.cpp:893-903)."""
+    fsum = np.zeros((nkz, nkz))
+    dbt = np.zeros((3, nkz))
+    for fis, d, b, t, f in results:
+        nq = len(d)
+        fsum[fis:fis + nq, fis:fis + nq] += np.triu(f)
+        dbt[0, fis:fis + nq] += d
+        dbt[1, fis:fis + nq] += b
+        dbt[2, fis:fis + nq] += t
+    return fsum, dbt
+
+
+def stable_invert_sym(s):
+    """mxhelp::stableInvertSym: returns (solver matrix, inverse, warn, dof, damp)."""
+    s = s.copy()
+    nkz = s.shape[0]
+    empty = [i for i in range(nkz) if s[i, i] == 0]
+    for i in empty:
+        s[i, i] = 1.0
+    svals = lapack.dgesvd(s.copy(), compute_uv=0)[1]
+    damp = 0.0
+    for i in range(nkz - 1, 0, -1):
+        if svals[i - 1] / svals[i] > 8.0:
+            damp = svals[i]
+        else:
+            break
+    if damp != 0:
+        sinv = lu_inverse(s.copy())
+        amat = s @ s
+        amat[np.diag_indices(nkz)] += damp
+        solver = lu_inverse(amat) @ s
+        warn = 1
+    else:
+        solver = lu_inverse(s.copy())
+        sinv = solver.copy()
+        warn = 0
+    for i in empty:
+        solver[i, i] = 0.0
+        sinv[i, i] = 0.0
+    return solver, sinv, warn, nkz - len(empty), damp
+
+
+def newton_raphson_step(fsum, dbt):
+    """F *= 1/2, symmetrise, invert, theta = 1/2 F^-1 (d - b - t)."""
+    f = 0.5 * fsum
+    f = _sym_upper_fill(f)
+    solver, sinv, warn, dof, damp = stable_invert_sym(f)
+    w = 0.5 * (solver @ dbt.T).T
+    theta = w[0] - w[1] - w[2]
+    return dict(fisher=f, solver=solver, inverse=sinv, theta=theta, warn=warn, dof=dof, damp=damp,
+                weighted=w)

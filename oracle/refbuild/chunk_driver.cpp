@@ -1,0 +1,181 @@
+// Oracle driver (test infrastructure).  Links lyspeq's own translation units,
+// compiled unmodified from the reference sources, and runs its per-chunk QMLE
+// path on every chunk of a config's spectra, then the global Newton-Raphson
+// step, dumping every intermediate result in a flat little-endian binary file
+// that the tests read.
+//
+// Set-up follows LyaPowerEstimate.cpp:21-121 (config, bins, specifics,
+// conversion, fiducial cosmology, SQ tables, smoother).  Each chunk's
+// contribution is obtained from Chunk::oneQSOiteration
+// (core/chunk_estimate.cpp:837-914) with zeroed accumulators, so the dump
+// holds the per-chunk d, b, t and Fisher exactly as the reference computes
+// them.  The global step repeats core/quadratic_estimate.cpp:456-457
+// (F *= 0.5, copyUpperToLower), :261-288 (stableInvertSym) and :290-318
+// (theta = 0.5 F^-1 (d - b - t)) with the reference's own mxhelp routines.
+//
+// Usage: chunk_driver <config> <out.bin> [--no-pixels]
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "core/chunk_estimate.hpp"
+#include "core/fiducial_cosmology.hpp"
+#include "core/global_numbers.hpp"
+#include "core/one_qso_estimate.hpp"
+#include "core/sq_table.hpp"
+#include "io/config_file.hpp"
+#include "io/io_helper_functions.hpp"
+#include "io/logger.hpp"
+#include "mathtools/matrix_helper.hpp"
+#include "mathtools/smoother.hpp"
+
+namespace {
+void putI(FILE *f, int v) { std::fwrite(&v, sizeof v, 1, f); }
+void putD(FILE *f, const double *v, size_t n) { if (n) std::fwrite(v, sizeof(double), n, f); }
+}
+
+int main(int argc, char *argv[]) {
+    if (argc < 3) {
+        std::fprintf(stderr, "usage: %s <config> <out.bin> [--no-pixels]\n", argv[0]);
+        return 2;
+    }
+    bool dump_pixels = !(argc > 3 && std::strcmp(argv[3], "--no-pixels") == 0);
+
+    ConfigFile config;
+    config.readFile(argv[1]);
+    LOG::LOGGER.open(config.get("OutputDir", "."), 0);
+    process::readProcess(config);
+    bins::readBins(config);
+    specifics::readSpecifics(config);
+    conv::readConversion(config);
+    fidcosmo::readFiducialCosmo(config);
+
+    process::sq_private_table = std::make_unique<SQLookupTable>(config);
+    process::sq_private_table->readTables();
+    process::updateMemory(-process::sq_private_table->getMaxMemUsage());
+    process::smoother = std::make_unique<Smoother>(config);
+
+    // Keys OneDQuadraticPowerEstimate consumes; read here so checkUnusedKeys passes.
+    config.getInteger("NumberOfIterations", 1);
+    std::string flist = config.get("FileNameList"), findir = config.get("FileInputDir");
+    config.get("Targetids2Ignore");
+    config.checkUnusedKeys();
+    if (findir.back() != '/') findir += '/';
+
+    std::vector<std::string> fpaths;
+    ioh::readList(flist.c_str(), fpaths);
+
+    std::vector<std::unique_ptr<OneQSOEstimate>> qsos;
+    qsos.reserve(fpaths.size());
+    for (auto &fp : fpaths)
+        qsos.push_back(std::make_unique<OneQSOEstimate>(findir + fp));
+
+    glmemory::allocMemory();
+
+    const int nkz = bins::TOTAL_KZ_BINS;
+    std::vector<double> ps(nkz, 0.0);          // powerspectra_fits: zero on the first iteration
+    std::vector<std::unique_ptr<double[]>> dbt_sum;
+    for (int i = 0; i < 3; ++i) dbt_sum.push_back(std::make_unique<double[]>(nkz));
+    auto fisher_sum = std::make_unique<double[]>((size_t) nkz * nkz);
+
+    FILE *out = std::fopen(argv[2], "wb");
+    if (!out) { std::perror("fopen"); return 1; }
+    std::fwrite("LQGREF01", 1, 8, out);
+    putI(out, nkz);
+    putI(out, bins::NUMBER_OF_K_BANDS);
+    putI(out, bins::NUMBER_OF_Z_BINS);
+    int nchunks_total = 0;
+    for (auto &q : qsos) nchunks_total += (int) q->chunks.size();
+    putI(out, nchunks_total);
+
+    double t_chunks = 0;
+    for (size_t iq = 0; iq < qsos.size(); ++iq) {
+        for (size_t ic = 0; ic < qsos[iq]->chunks.size(); ++ic) {
+            Chunk &ch = *qsos[iq]->chunks[ic];
+            const int n = ch.size(), nq = ch.N_Q_MATRICES;
+            // Copy the chunk's inputs before the iteration: wave is already lambda/LYA_REST.
+            std::vector<double> w(ch.qFile->wave(), ch.qFile->wave() + n),
+                d(ch.qFile->delta(), ch.qFile->delta() + n),
+                iv(ch.qFile->ivar(), ch.qFile->ivar() + n);
+
+            std::vector<std::unique_ptr<double[]>> dbt_local;
+            for (int i = 0; i < 3; ++i) dbt_local.push_back(std::make_unique<double[]>(nkz));
+            auto fisher_local = std::make_unique<double[]>((size_t) nkz * nkz);
+
+            auto t0 = std::chrono::steady_clock::now();
+            ch.oneQSOiteration(ps.data(), dbt_local, fisher_local.get());
+            t_chunks += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+            // A chunk whose inversion threw contributes nothing (chunk_estimate.cpp:905-913).
+            int status = 0;
+            bool any = false;
+            for (int i = 0; i < 3 && !any; ++i)
+                for (int k = 0; k < nkz; ++k) if (dbt_local[i][k] != 0) { any = true; break; }
+            if (!any) status = 1;
+
+            for (int i = 0; i < 3; ++i)
+                for (int k = 0; k < nkz; ++k) dbt_sum[i][k] += dbt_local[i][k];
+            for (size_t k = 0; k < (size_t) nkz * nkz; ++k) fisher_sum[k] += fisher_local[k];
+
+            putI(out, (int) iq); putI(out, (int) ic); putI(out, n);
+            putI(out, ch.fisher_index_start); putI(out, nq); putI(out, ch.KBIN_UPP);
+            putI(out, ch.qFile->R_fwhm); putI(out, status);
+            double dv = ch.qFile->dv_kms;
+            putD(out, &dv, 1);
+            putI(out, dump_pixels ? 1 : 0);
+            if (dump_pixels) { putD(out, w.data(), n); putD(out, d.data(), n); putD(out, iv.data(), n); }
+            for (int i = 0; i < 3; ++i) putD(out, ch.dbt_estimate_before_fisher_vector[i].get(), nq);
+            putD(out, ch.fisher_matrix.get(), (size_t) nq * nq);
+        }
+    }
+
+    // Global NR step, quadratic_estimate.cpp:456-457 then :261-318.
+    auto t1 = std::chrono::steady_clock::now();
+    cblas_dscal(nkz * nkz, 0.5, fisher_sum.get(), 1);
+    mxhelp::copyUpperToLower(fisher_sum.get(), nkz);
+    std::vector<double> fisher_halved(fisher_sum.get(), fisher_sum.get() + (size_t) nkz * nkz);
+
+    auto solver = std::make_unique<double[]>((size_t) nkz * nkz);
+    auto invf = std::make_unique<double[]>((size_t) nkz * nkz);
+    std::copy_n(fisher_sum.get(), (size_t) nkz * nkz, solver.get());
+    int dof = nkz;
+    double damp = 0;
+    int warn = mxhelp::stableInvertSym(solver, invf, nkz, dof, damp);
+
+    std::vector<std::vector<double>> weighted(3, std::vector<double>(nkz));
+    for (int i = 0; i < 3; ++i)
+        cblas_dgemv(CblasRowMajor, CblasNoTrans, nkz, nkz, 0.5, solver.get(), nkz,
+                    dbt_sum[i].get(), 1, 0, weighted[i].data(), 1);
+    std::vector<double> theta(weighted[0]);
+    cblas_daxpy(nkz, -1, weighted[1].data(), 1, theta.data(), 1);
+    cblas_daxpy(nkz, -1, weighted[2].data(), 1, theta.data(), 1);
+    double t_global = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+
+    std::fwrite("GLOBAL01", 1, 8, out);
+    putD(out, fisher_halved.data(), fisher_halved.size());
+    for (int i = 0; i < 3; ++i) putD(out, dbt_sum[i].get(), nkz);
+    putD(out, solver.get(), (size_t) nkz * nkz);
+    putD(out, invf.get(), (size_t) nkz * nkz);
+    putD(out, theta.data(), nkz);
+    putI(out, warn); putI(out, dof);
+    putD(out, &damp, 1);
+    std::vector<double> pfid(nkz);
+    for (int i = 0; i < nkz; ++i) {
+        int kn, zm;
+        bins::getFisherMatrixBinNoFromIndex(i, kn, zm);
+        pfid[i] = fidcosmo::fiducialPowerSpectrum(bins::KBAND_CENTERS[kn], bins::ZBIN_CENTERS[zm],
+                                                  &fidpd13::FIDUCIAL_PD13_PARAMS);
+    }
+    putD(out, pfid.data(), nkz);
+    putD(out, &t_chunks, 1);
+    putD(out, &t_global, 1);
+    std::fclose(out);
+
+    glmemory::dealloc();
+    std::printf("chunks=%d t_chunks=%.6f s t_global=%.6f s damped=%d\n", nchunks_total, t_chunks,
+                t_global, warn);
+    return 0;
+}

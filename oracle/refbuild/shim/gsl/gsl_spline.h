@@ -1,0 +1,2 @@
+/* Oracle-build shim: see gsl_shim_common.h. */
+#include "gsl/gsl_shim_common.h"

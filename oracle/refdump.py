@@ -1,0 +1,129 @@
+"""Reader for the oracle driver's dump (test infrastructure only).
+
+The dump is written by ``oracle/refbuild/chunk_driver.cpp``, which runs
+lyspeq's own ``Chunk::oneQSOiteration`` (core/chunk_estimate.cpp:837-914) on
+every chunk of a config and then the global Newton-Raphson step
+(core/quadratic_estimate.cpp:456-457, 261-318).  Layout: little-endian,
+``LQGREF01`` magic, four int32 (nkz, nk, nz, nchunks), one record per chunk,
+then a ``GLOBAL01`` block.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+DRIVER = os.path.join(REF_DIR, "chunk_driver")
+LYAPOWER = os.path.join(REF_DIR, "LyaPowerEstimate")
+
+
+@dataclasses.dataclass
+class RefChunk:
+    qso: int
+    index: int
+    n: int
+    fisher_index_start: int
+    nq: int
+    kbin_upp: int
+    r_fwhm: int
+    status: int
+    dv: float
+    wave: np.ndarray | None   # lambda / LYA_REST (= 1 + z), as the chunk holds it
+    delta: np.ndarray | None
+    ivar: np.ndarray | None
+    d: np.ndarray
+    b: np.ndarray
+    t: np.ndarray
+    fisher: np.ndarray        # nq x nq, upper triangle filled, not halved
+
+
+@dataclasses.dataclass
+class RefDump:
+    nkz: int
+    nk: int
+    nz: int
+    chunks: list
+    fisher: np.ndarray        # global, halved and symmetrised
+    dbt: np.ndarray           # 3 x nkz sums before Fisher weighting
+    solver_invfisher: np.ndarray
+    inverse_fisher: np.ndarray
+    theta: np.ndarray
+    damped: int
+    dof: int
+    damp: float
+    pfid: np.ndarray
+    t_chunks: float
+    t_global: float
+
+
+class _Reader:
+    def __init__(self, buf: bytes):
+        self.buf = buf
+        self.pos = 0
+
+    def i(self, n=1):
+        v = np.frombuffer(self.buf, dtype="<i4", count=n, offset=self.pos)
+        self.pos += 4 * n
+        return int(v[0]) if n == 1 else v.copy()
+
+    def d(self, n):
+        v = np.frombuffer(self.buf, dtype="<f8", count=n, offset=self.pos)
+        self.pos += 8 * n
+        return v.copy()
+
+    def magic(self, want: bytes):
+        got = self.buf[self.pos:self.pos + 8]
+        if got != want:
+            raise ValueError(f"bad dump: expected {want!r}, got {got!r}")
+        self.pos += 8
+
+
+def read_dump(path: str) -> RefDump:
+    with open(path, "rb") as f:
+        r = _Reader(f.read())
+    r.magic(b"LQGREF01")
+    nkz, nk, nz, nch = (r.i() for _ in range(4))
+    chunks = []
+    for _ in range(nch):
+        qso, idx, n, fis, nq, kup, rf, st = (r.i() for _ in range(8))
+        dv = float(r.d(1)[0])
+        has_pix = r.i()
+        w = dl = iv = None
+        if has_pix:
+            w, dl, iv = r.d(n), r.d(n), r.d(n)
+        d, b, t = r.d(nq), r.d(nq), r.d(nq)
+        fm = r.d(nq * nq).reshape(nq, nq)
+        chunks.append(RefChunk(qso, idx, n, fis, nq, kup, rf, st, dv, w, dl, iv, d, b, t, fm))
+    r.magic(b"GLOBAL01")
+    fisher = r.d(nkz * nkz).reshape(nkz, nkz)
+    dbt = np.stack([r.d(nkz) for _ in range(3)])
+    solver = r.d(nkz * nkz).reshape(nkz, nkz)
+    invf = r.d(nkz * nkz).reshape(nkz, nkz)
+    theta = r.d(nkz)
+    damped, dof = r.i(), r.i()
+    damp = float(r.d(1)[0])
+    pfid = r.d(nkz)
+    t_chunks, t_global = float(r.d(1)[0]), float(r.d(1)[0])
+    return RefDump(nkz, nk, nz, chunks, fisher, dbt, solver, invf, theta, damped, dof, damp,
+                   pfid, t_chunks, t_global)
+
+
+def available() -> bool:
+    return os.path.exists(DRIVER)
+
+
+def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None) -> RefDump:
+    env = dict(os.environ)
+    env.setdefault("OPENBLAS_NUM_THREADS", "1")
+    # One OpenMP thread: with more, Chunk::_applyRedshiftInterp races on the
+    # shared `low`/`tmp` bounds (core/chunk_estimate.cpp:486, 512-516) and the
+    # redshift weights of some rows come out wrong from run to run.
+    env["OMP_NUM_THREADS"] = str(threads or 1)
+    args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"])
+    subprocess.run(args, check=True, env=env, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
+    return read_dump(out)
