@@ -1,0 +1,175 @@
+/*
+ * lqg.h - C ABI of the GB300 per-chunk QMLE engine (lyspeq's hot path).
+ *
+ * lyspeq has no C ABI of its own: the per-chunk path is the C++ API
+ *   Chunk::Chunk(const qio::QSOFile&, int i1, int i2)       core/chunk_estimate.cpp:141-167
+ *   Chunk::oneQSOiteration(ps, dbt_sum, fisher_sum)           core/chunk_estimate.cpp:837-914
+ *   OneQSOEstimate::oneQSOiteration(...)                      core/one_qso_estimate.cpp:176-197
+ *   OneDQuadraticPowerEstimate::iterate()                     core/quadratic_estimate.cpp:398-546
+ *   OneDQuadraticPowerEstimate::invertTotalFisherMatrix()     core/quadratic_estimate.cpp:261-288
+ *   OneDQuadraticPowerEstimate::computePowerSpectrumEstimates() :290-318
+ * The entry points below are what a binding of that API binds: plain
+ * pointers and sizes, integer status codes, no C++ or torch types.  The C++
+ * facade in lyspeq_gb300/csrc/lyspeq_api.hpp keeps the reference's class
+ * names on top of them.
+ *
+ * Conventions
+ *  - All arrays are row-major IEEE double unless noted.
+ *  - Every function returns LQG_OK (0) or a negative LQG_ERR_* code; the
+ *    message of the last error of a context is lqg_last_error(ctx).
+ *  - A chunk that the reference would reject or skip gets a positive
+ *    LQG_CHUNK_* status and contributes nothing, as the reference logs and
+ *    drops it (core/one_qso_estimate.cpp:117-124, chunk_estimate.cpp:905-913).
+ *  - One context per host thread.  Work is enqueued on the context's CUDA
+ *    stream; functions that return host data synchronise that stream.
+ */
+#ifndef LQG_H
+#define LQG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LQG_ABI_VERSION 1
+
+/* status codes */
+#define LQG_OK 0
+#define LQG_ERR_ARG -1          /* invalid argument */
+#define LQG_ERR_CUDA -2         /* CUDA runtime error */
+#define LQG_ERR_NOMEM -3        /* device or host allocation failed */
+#define LQG_ERR_STATE -4        /* call out of order (e.g. no batch) */
+#define LQG_ERR_TIMEOUT -5      /* a bounded device wait gave up */
+#define LQG_ERR_UNSUPPORTED -6  /* option not implemented on this path */
+#define LQG_ERR_SINGULAR -7     /* global Fisher matrix could not be inverted */
+
+/* per-chunk status */
+#define LQG_CHUNK_OK 0
+#define LQG_CHUNK_SHORT 1       /* Chunk::_copyQSOFile short chunk, chunk_estimate.cpp:173-187 */
+#define LQG_CHUNK_NO_TABLE 2    /* no (R, dv) table, chunk_estimate.cpp:197-206 */
+#define LQG_CHUNK_EMPTY 3       /* all pixels masked (QSOFile::_cutMaskedBoundary) */
+#define LQG_CHUNK_OUT_OF_RANGE 4 /* no redshift bin touched */
+#define LQG_CHUNK_NOT_SPD 5     /* covariance not positive definite ("not invertable") */
+#define LQG_CHUNK_BAD_INPUT 6   /* non-finite pixel values */
+#define LQG_CHUNK_TOO_LARGE 7   /* more pixels than the engine's maximum */
+
+/* arithmetic of the per-chunk products */
+#define LQG_PRECISION_FP64 0    /* everything in IEEE binary64 */
+#define LQG_PRECISION_MIXED 1   /* FP64 factorisation; C^-1 Q_k, Fisher and bias traces
+                                   on tensor cores as fp16 hi/lo split products (3 terms),
+                                   fp32 accumulation, fp64 reduction of partial sums */
+
+typedef struct lqg_ctx lqg_ctx;
+
+/* k and z binning: bins::setUpBins, core/global_numbers.cpp:209-251 */
+typedef struct {
+    int nk;                     /* NUMBER_OF_K_BANDS */
+    int nz;                     /* NUMBER_OF_Z_BINS */
+    const double *k_edges;      /* KBAND_EDGES [nk + 1] */
+    const double *z_centers;    /* ZBIN_CENTERS [nz] */
+    double z_bin_width;         /* Z_BIN_WIDTH */
+    int triangular;             /* 1: RedshiftBinningMethod 1, 0: top hat */
+} lqg_bins;
+
+/* S/Q lookup tables: SQLookupTable, core/sq_table.cpp:148-175, 325-368.
+ * All tables share the v grid [0, v_length] with nv points and the z grid
+ * [z_c0 - dz, z_c0 - dz + dz (nz + 1)] with nzp points. */
+typedef struct {
+    int n_tables;               /* number of (R, dv) pairs (FileNameRList) */
+    const int *r_fwhm;          /* [n_tables] spectrograph resolution R */
+    const double *dv;           /* [n_tables] pixel width, km/s */
+    int nv;                     /* NumberVPoints */
+    double v_length;            /* VelocityLength */
+    int nzp;                    /* NumberZPoints */
+    const double *deriv;        /* [n_tables][nk][nv]   Q_k(v) */
+    const double *signal;       /* [n_tables][nv][nzp]  S(z, v), z fastest; NULL if
+                                   turn_off_sfid */
+} lqg_tables;
+
+typedef struct {
+    double max_forest_length;   /* MaximumForestLength (already divided by the
+                                   DynamicChunkNumber, i.e. MAX_FOREST_LENGTH_V) */
+    double max_mean_pixel_size; /* MaximumMeanPixelSize */
+    int cont_logl_order;        /* ContinuumLogLambdaMargOrder */
+    int cont_l_order;           /* ContinuumLambdaMargOrder */
+    int turn_off_sfid;          /* TurnOffBaseline > 0 */
+    int skip_fisher;            /* PrecomputedFisher given: Fisher not computed */
+    size_t workspace_bytes;     /* device workspace cap; 0 = 60% of free memory */
+} lqg_opts;
+
+/* Create a context on CUDA device `device`; bins and tables are copied.
+ * Replaces SQLookupTable::readTables + glmemory::allocMemory. */
+int lqg_ctx_create(lqg_ctx **ctx, const lqg_bins *bins, const lqg_tables *tables,
+                   const lqg_opts *opts, int device);
+int lqg_ctx_destroy(lqg_ctx *ctx);
+const char *lqg_last_error(const lqg_ctx *ctx);
+int lqg_abi_version(void);
+
+/* Add chunks, each given as the pixel range of one spectrum after lyspeq's
+ * reading and cleaning (qio::QSOFile after cutBoundary / maskOutliers and
+ * OneQSOEstimate::decideIndices).  lambda is the observed wavelength in
+ * Angstrom, ivar the inverse variance (0 = masked).  For each chunk this does
+ * what Chunk::Chunk does (core/chunk_estimate.cpp:141-257): trims masked
+ * edges, takes the median dv, applies the short-chunk rule, finds the table,
+ * KBIN_UPP, the redshift bins, N_Q_MATRICES and fisher_index_start.
+ * status_out[n_chunks] receives LQG_CHUNK_* per chunk; rejected chunks are
+ * kept out of the batch.  Pixel data are copied to the device. */
+int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
+                  const double *lambda, const double *delta, const double *ivar,
+                  const int *r_fwhm, int *status_out);
+int lqg_batch_clear(lqg_ctx *ctx);
+int lqg_batch_size(const lqg_ctx *ctx);
+
+/* Metadata of batch chunk i (in insertion order of accepted chunks):
+ * info[0..7] = n, fisher_index_start, n_q_matrices, kbin_upp, res_index,
+ * zbin_low, zbin_upp, input index (position in the lqg_batch_add call). */
+int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info);
+
+/* One Newton-Raphson iteration over the whole batch: for every chunk build
+ * S and Q_k from the tables, C = S + sum theta_k Q_k + N, invert, continuum
+ * marginalisation, then d_k, b_k, t_k and the chunk Fisher matrix, summed
+ * into the global accumulators exactly as Chunk::oneQSOiteration does
+ * (core/chunk_estimate.cpp:837-914): F upper triangle, NOT halved.
+ * theta: TOTAL_KZ_BINS values (powerspectra_fits) or NULL for zeros.
+ * Enqueued on the context stream; results stay on the device. */
+int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision);
+
+/* Copy the accumulated results of the last iteration to host memory (any
+ * pointer may be NULL): d, b, t [nkz] and fisher [nkz * nkz] (upper, not
+ * halved) and chunk_status [batch size].  Synchronises the stream. */
+int lqg_download(lqg_ctx *ctx, double *d, double *b, double *t, double *fisher,
+                 int *chunk_status);
+
+/* Per-chunk results of the last iteration for batch chunk i: d, b, t
+ * [n_q_matrices] and fisher [n_q * n_q] (upper triangle filled), the
+ * Chunk::dbt_estimate_before_fisher_vector / fisher_matrix members. */
+int lqg_chunk_result(lqg_ctx *ctx, int i, double *d, double *b, double *t, double *fisher);
+
+/* Global Newton-Raphson update, OneDQuadraticPowerEstimate::iterate tail
+ * (core/quadratic_estimate.cpp:456-457, 261-318, mathtools/matrix_helper.cpp:330-358):
+ * F <- F/2 symmetrised; zero-diagonal bins are set to 1 for the inversion;
+ * if the singular values of F show a jump > 8 the damped solver
+ * (F^2 + s I)^-1 F is used; theta = 1/2 F_solver (d - b - t).
+ * In: fisher_sum [nkz^2] (upper, unhalved), dbt [3][nkz].
+ * Out (any may be NULL): fisher [nkz^2] halved and symmetric, solver and
+ * inverse [nkz^2], weighted [3][nkz] (0.5 F_solver d, b, t), theta [nkz],
+ * damped (0/1), dof, damp.  Runs in FP64 on the device. */
+int lqg_fisher_solve(lqg_ctx *ctx, const double *fisher_sum, const double *dbt,
+                     double *fisher, double *solver, double *inverse, double *weighted,
+                     double *theta, int *damped, int *dof, double *damp);
+
+/* Device time (ms) of the phases of the last iteration, CUDA events on the
+ * context stream: [0] build + factorisation, [1] C^-1 Q_k products,
+ * [2] traces / Fisher, [3] total.  Returns the number of values written. */
+int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n);
+
+/* Number of kernel launches the last lqg_nr_iteration enqueued. */
+int lqg_last_launch_count(const lqg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LQG_H */

@@ -1,0 +1,115 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/lqg.h"
+
+namespace lqg {
+
+constexpr double kSpeedOfLight = 299792.458;   // core/global_numbers.hpp:17-22
+constexpr double kLyaRest = 1215.67;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kDoubleEpsilon = 1e-15;
+
+constexpr int kPad = 64;          // matrices are stored with a leading dimension that is a multiple of 64
+constexpr int kMaxPixels = 8192;  // largest chunk the engine accepts
+constexpr int kMaxContVecs = 4;
+
+// One chunk of the batch: what Chunk::Chunk computes (core/chunk_estimate.cpp:141-257)
+// plus the device offsets of its data and workspace.
+struct ChunkDesc {
+    int n;                // pixels (size())
+    int ld;               // leading dimension of its N x N matrices (n rounded up to kPad)
+    int nq;               // N_Q_MATRICES
+    int ns;               // number of stored derivative matrices (kn < KBIN_UPP)
+    int kbin_upp;         // KBIN_UPP
+    int fis;              // fisher_index_start
+    int res;              // table index (RES_INDEX)
+    int zb0;              // first redshift bin of the chunk's matrices = fis / nk
+    int64_t pix;          // offset of the pixel arrays
+    int64_t res_off;      // offset of the per-chunk results (3 nq + nq^2 doubles)
+    // Workspace offsets (bytes, relative to the wave workspace base)
+    int64_t o_s, o_c, o_y, o_q, o_r, o_p, o_part, o_dpart, o_split_c;
+    int slot_q, slot_r, slot_p;  // first matrix slot of this chunk in the stacked operand buffers
+    int n_tiles;          // number of 64x64 tiles of its matrix (ld/64)^2
+    int status;
+};
+
+struct DeviceBins {
+    int nk, nz, nkz, triangular;
+    double dz;
+    double z_centers[64];
+};
+
+struct TableGrid {
+    int nv, nzp, n_tables;
+    double v1, dv, z1, dz;
+};
+
+// Thin RAII for device allocations owned by the context.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t n) {
+        if (p && bytes >= n) return cudaSuccess;
+        if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+inline int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+// ---- kernel launchers (defined in the .cu files) ----
+struct WaveArgs {
+    const ChunkDesc *chunks;     // device
+    int n_chunks;
+    int max_ld;
+    char *ws;                    // wave workspace base
+    const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
+    const double *deriv, *signal, *qmax;             // tables
+    const double *theta;                             // device, nkz
+    double *results;                                 // per-chunk results
+    int *status;                                     // per-chunk status (wave-local)
+    TableGrid grid;
+    DeviceBins *bins;                                // device pointer
+    int cont_logl, cont_l, turn_off_sfid, skip_fisher;
+    int precision;
+    int total_slots_q, total_slots_r, total_slots_p;
+    __half *q_hi, *q_lo, *r_hi, *r_lo, *p_hi, *p_lo, *c_hi, *c_lo;  // mixed operand planes
+    float *gram_part;
+    int gram_splits;
+    double *scales;              // per-slot scales (mixed): q [slots], r, p and c
+    int launches;
+};
+
+void launch_build_s_c(WaveArgs &a, cudaStream_t st);
+void launch_factor(WaveArgs &a, cudaStream_t st);
+void launch_build_q(WaveArgs &a, cudaStream_t st);
+void launch_products_fp64(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs);
+void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs);
+void launch_scales_mixed(WaveArgs &a, cudaStream_t st);
+void launch_finish(WaveArgs &a, cudaStream_t st);
+
+bool tc_available();
+
+}  // namespace lqg
+
+#define LQG_CUDA_CHECK_RET(expr)                                               \
+    do {                                                                       \
+        cudaError_t _e = (expr);                                               \
+        if (_e != cudaSuccess) {                                               \
+            ctx->err = std::string(#expr) + ": " + cudaGetErrorString(_e);     \
+            return LQG_ERR_CUDA;                                               \
+        }                                                                      \
+    } while (0)

@@ -1,0 +1,211 @@
+"""ctypes binding of the engine's C ABI (include/lqg.h).
+
+The engine is the compiled library lyspeq_gb300/liblqg.so; there is no
+fallback: if the library is missing or a call fails, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblqg.so")
+
+LQG_OK = 0
+PRECISION = {"fp64": 0, "mixed": 1}
+CHUNK_STATUS = {0: "ok", 1: "short", 2: "no_table", 3: "empty", 4: "out_of_range",
+                5: "not_spd", 6: "bad_input", 7: "too_large"}
+
+EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_error",
+           "lqg_batch_add", "lqg_batch_clear", "lqg_batch_size", "lqg_chunk_info",
+           "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
+           "lqg_last_timings", "lqg_last_launch_count"]
+
+
+class LqgBins(C.Structure):
+    _fields_ = [("nk", C.c_int), ("nz", C.c_int), ("k_edges", C.POINTER(C.c_double)),
+                ("z_centers", C.POINTER(C.c_double)), ("z_bin_width", C.c_double),
+                ("triangular", C.c_int)]
+
+
+class LqgTables(C.Structure):
+    _fields_ = [("n_tables", C.c_int), ("r_fwhm", C.POINTER(C.c_int)),
+                ("dv", C.POINTER(C.c_double)), ("nv", C.c_int), ("v_length", C.c_double),
+                ("nzp", C.c_int), ("deriv", C.POINTER(C.c_double)),
+                ("signal", C.POINTER(C.c_double))]
+
+
+class LqgOpts(C.Structure):
+    _fields_ = [("max_forest_length", C.c_double), ("max_mean_pixel_size", C.c_double),
+                ("cont_logl_order", C.c_int), ("cont_l_order", C.c_int),
+                ("turn_off_sfid", C.c_int), ("skip_fisher", C.c_int),
+                ("workspace_bytes", C.c_size_t)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load liblqg.so and declare the signatures; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built: run `python -m lyspeq_gb300.build`")
+    lib = C.CDLL(path)
+    dp, ip, vp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
+    lib.lqg_abi_version.restype = C.c_int
+    lib.lqg_ctx_create.argtypes = [C.POINTER(vp), C.POINTER(LqgBins), C.POINTER(LqgTables),
+                                   C.POINTER(LqgOpts), C.c_int]
+    lib.lqg_ctx_destroy.argtypes = [vp]
+    lib.lqg_last_error.argtypes = [vp]
+    lib.lqg_last_error.restype = C.c_char_p
+    lib.lqg_batch_add.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), dp, dp, dp, ip, ip]
+    lib.lqg_batch_clear.argtypes = [vp]
+    lib.lqg_batch_size.argtypes = [vp]
+    lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
+    lib.lqg_nr_iteration.argtypes = [vp, dp, C.c_int]
+    lib.lqg_download.argtypes = [vp, dp, dp, dp, dp, ip]
+    lib.lqg_chunk_result.argtypes = [vp, C.c_int, dp, dp, dp, dp]
+    lib.lqg_fisher_solve.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, dp]
+    lib.lqg_last_timings.argtypes = [vp, dp, C.c_int]
+    lib.lqg_last_launch_count.argtypes = [vp]
+    _lib = lib
+    return lib
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
+
+
+class Engine:
+    """One engine context on one GPU: the lookup tables, the binning and a
+    batch of chunks (Chunk objects of the reference, kept on the device)."""
+
+    def __init__(self, bins, tables, nv, lenv, nzp, max_forest_length, max_mean_pixel_size=150.0,
+                 cont=(-1, -1), turn_off_sfid=False, skip_fisher=False, device=0,
+                 workspace_bytes=0):
+        self.lib = load_library()
+        self.bins = bins
+        self.nkz = bins.nk * bins.nz
+        self._k_edges = np.ascontiguousarray(bins.k_edges, dtype=np.float64)
+        self._z = np.ascontiguousarray(bins.z_centers, dtype=np.float64)
+        self._r = np.ascontiguousarray([t.r_fwhm for t in tables], dtype=np.int32)
+        self._dv = np.ascontiguousarray([t.dv for t in tables], dtype=np.float64)
+        self._deriv = np.ascontiguousarray(np.stack([t.deriv for t in tables]), dtype=np.float64)
+        self._signal = np.ascontiguousarray(np.stack([t.signal for t in tables]), dtype=np.float64)
+        b = LqgBins(bins.nk, bins.nz, _dptr(self._k_edges), _dptr(self._z), bins.dz,
+                    1 if bins.triangular else 0)
+        t = LqgTables(len(tables), _iptr(self._r), _dptr(self._dv), nv, lenv, nzp,
+                      _dptr(self._deriv), None if turn_off_sfid else _dptr(self._signal))
+        o = LqgOpts(max_forest_length, max_mean_pixel_size, cont[0], cont[1], int(turn_off_sfid),
+                    int(skip_fisher), workspace_bytes)
+        h = C.c_void_p()
+        rc = self.lib.lqg_ctx_create(C.byref(h), C.byref(b), C.byref(t), C.byref(o), device)
+        if rc != LQG_OK:
+            raise RuntimeError(f"lqg_ctx_create failed with {rc}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lqg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != LQG_OK:
+            raise RuntimeError(f"{what} failed ({rc}): {self.lib.lqg_last_error(self.h).decode()}")
+
+    def add_chunks(self, lam, delta, ivar, offsets, r_fwhm):
+        """Add chunks given as concatenated arrays; returns the per-chunk status."""
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        delta = np.ascontiguousarray(delta, dtype=np.float64)
+        ivar = np.ascontiguousarray(ivar, dtype=np.float64)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        r_fwhm = np.ascontiguousarray(r_fwhm, dtype=np.int32)
+        n = len(offsets) - 1
+        status = np.zeros(max(n, 1), dtype=np.int32)
+        rc = self.lib.lqg_batch_add(self.h, n, offsets.ctypes.data_as(C.POINTER(C.c_int64)),
+                                    _dptr(lam), _dptr(delta), _dptr(ivar), _iptr(r_fwhm),
+                                    _iptr(status))
+        self._check(rc, "lqg_batch_add")
+        return status[:n]
+
+    def add_chunk_list(self, chunks):
+        """chunks: iterable of (lambda_angstrom, delta, ivar, r_fwhm)."""
+        chunks = list(chunks)
+        offs = np.zeros(len(chunks) + 1, dtype=np.int64)
+        for i, c in enumerate(chunks):
+            offs[i + 1] = offs[i] + len(c[0])
+        cat = lambda j: np.concatenate([np.asarray(c[j], dtype=np.float64) for c in chunks]) \
+            if chunks else np.zeros(0)
+        return self.add_chunks(cat(0), cat(1), cat(2), offs, [c[3] for c in chunks])
+
+    def clear(self):
+        self._check(self.lib.lqg_batch_clear(self.h), "lqg_batch_clear")
+
+    @property
+    def size(self):
+        return self.lib.lqg_batch_size(self.h)
+
+    def chunk_info(self, i):
+        info = np.zeros(8, dtype=np.int32)
+        self._check(self.lib.lqg_chunk_info(self.h, i, _iptr(info)), "lqg_chunk_info")
+        keys = ("n", "fisher_index_start", "nq", "kbin_upp", "res_index", "zbin_low", "zbin_upp",
+                "input_index")
+        return dict(zip(keys, (int(x) for x in info)))
+
+    def iterate(self, theta=None, precision="fp64"):
+        th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+        rc = self.lib.lqg_nr_iteration(self.h, _dptr(th), PRECISION[precision])
+        self._check(rc, "lqg_nr_iteration")
+
+    def download(self):
+        d, b, t = (np.zeros(self.nkz) for _ in range(3))
+        f = np.zeros((self.nkz, self.nkz))
+        st = np.zeros(max(self.size, 1), dtype=np.int32)
+        rc = self.lib.lqg_download(self.h, _dptr(d), _dptr(b), _dptr(t), _dptr(f), _iptr(st))
+        self._check(rc, "lqg_download")
+        return dict(d=d, b=b, t=t, fisher=f, status=st[:self.size])
+
+    def chunk_result(self, i):
+        nq = self.chunk_info(i)["nq"]
+        d, b, t = (np.zeros(nq) for _ in range(3))
+        f = np.zeros((nq, nq))
+        rc = self.lib.lqg_chunk_result(self.h, i, _dptr(d), _dptr(b), _dptr(t), _dptr(f))
+        self._check(rc, "lqg_chunk_result")
+        return d, b, t, f
+
+    def fisher_solve(self, fisher_sum, dbt):
+        n = self.nkz
+        fs = np.ascontiguousarray(fisher_sum, dtype=np.float64)
+        db = np.ascontiguousarray(dbt, dtype=np.float64)
+        out = {k: np.zeros((n, n)) for k in ("fisher", "solver", "inverse")}
+        w = np.zeros((3, n))
+        th = np.zeros(n)
+        damped, dof, damp = C.c_int(), C.c_int(), C.c_double()
+        rc = self.lib.lqg_fisher_solve(self.h, _dptr(fs), _dptr(db), _dptr(out["fisher"]),
+                                       _dptr(out["solver"]), _dptr(out["inverse"]), _dptr(w),
+                                       _dptr(th), C.byref(damped), C.byref(dof), C.byref(damp))
+        self._check(rc, "lqg_fisher_solve")
+        out.update(weighted=w, theta=th, damped=damped.value, dof=dof.value, damp=damp.value)
+        return out
+
+    def timings(self):
+        ms = np.zeros(4)
+        self.lib.lqg_last_timings(self.h, _dptr(ms), 4)
+        return ms
+
+    def launch_count(self):
+        return self.lib.lqg_last_launch_count(self.h)

@@ -1,0 +1,106 @@
+"""Generate the golden fixtures of the parity tests.
+
+Each fixture holds a seeded synthetic workload (binning, lookup-table keys
+and the chunks exactly as lyspeq hands them to Chunk::oneQSOiteration; the
+tables themselves are rebuilt by lyspeq_gb300.synth.build_table) together
+with the outputs of lyspeq itself on those inputs: per-chunk d, b, t and
+Fisher matrices and the global Newton-Raphson results.  The outputs come from
+the reference compiled from its own sources (oracle/refbuild, run through
+oracle/_ref/chunk_driver with one OpenMP thread), so the fixtures travel to
+machines where the reference sources are absent.
+
+Run (needs the oracle built: make -C oracle/refbuild):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from lyspeq_gb300 import synth  # noqa: E402
+from oracle import refdump  # noqa: E402
+
+LYA_REST = synth.LYA_REST
+
+# name -> (workload, n_chunks, (logl, lam) marginalisation orders, masked-pixel fraction,
+#          chunks kept in the fixture)
+CASES = {
+    "tiny_nomarg": ("tiny", None, (-1, -1), 0.0, None),
+    "tiny_marg1": ("tiny", None, (1, -1), 0.0, None),
+    "tiny_marg3": ("tiny", None, (2, 1), 0.0, None),
+    "tiny_masked": ("tiny", None, (1, -1), 0.04, None),
+    "small_cfg": ("small", None, (-1, -1), 0.0, 12),
+    "desi_sub": ("desi", 6, (1, -1), 0.0, None),
+}
+
+
+def _mask(w, frac, seed):
+    if frac <= 0:
+        return
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for s in w.spectra:
+        n = len(s.wave)
+        idx = rng.choice(np.arange(1, n - 1), size=max(1, int(frac * n)), replace=False)
+        s.sigma = s.sigma.copy()
+        s.sigma[idx] = 1e10      # ivar = 1/sigma^2 < 1e-15 -> masked by the reader
+
+
+def make_case(name, spec):
+    wl, nch, marg, mask, keep = spec
+    w = synth.make_workload(wl, n_chunks=nch)
+    w.cont_logl_order, w.cont_l_order = marg
+    _mask(w, mask, 99)
+    with tempfile.TemporaryDirectory() as tmp:
+        cfg = synth.write_reference_inputs(w, tmp)
+        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"))
+    chunks = dump.chunks
+    if keep is not None:
+        chunks = chunks[:keep]
+    out = dict(
+        bins=np.array([w.bins.k0, w.bins.nklin, w.bins.dklin, w.bins.nklog, w.bins.dklog,
+                       w.bins.z0, w.bins.dz, w.bins.nz, float(w.bins.triangular)]),
+        grid=np.array([w.nv, w.lenv, w.nzp, w.max_forest_length, marg[0], marg[1]], dtype=float),
+        table_r=np.array([t.r_fwhm for t in w.tables], dtype=np.int32),
+        table_dv=np.array([t.dv for t in w.tables]),
+        # tables are rebuilt from their definition by the tests; these sums detect drift
+        table_sums=np.array([[np.abs(t.deriv).sum(), np.abs(t.signal).sum()] for t in w.tables]),
+        n_chunks=np.array(len(chunks)),
+        g_fisher=dump.fisher, g_dbt=dump.dbt, g_theta=dump.theta, g_solver=dump.solver_invfisher,
+        g_inverse=dump.inverse_fisher, g_damped=np.array(dump.damped),
+        g_complete=np.array(keep is None),
+    )
+    for i, c in enumerate(chunks):
+        # the chunk is a contiguous slice of its spectrum; keep the wavelengths in
+        # Angstrom as read from the file so that lambda / LYA_REST is bit-identical
+        full = w.spectra[c.qso].wave
+        start = int(np.flatnonzero(full / LYA_REST == c.wave[0])[0])
+        lam = full[start:start + c.n]
+        assert np.array_equal(lam / LYA_REST, c.wave), "chunk is not a slice of its spectrum"
+        out[f"c{i}_meta"] = np.array([c.n, c.fisher_index_start, c.nq, c.kbin_upp, c.r_fwhm,
+                                      c.status], dtype=np.int64)
+        out[f"c{i}_lam"] = lam
+        out[f"c{i}_delta"] = c.delta
+        out[f"c{i}_ivar"] = c.ivar
+        out[f"c{i}_dbt"] = np.stack([c.d, c.b, c.t])
+        out[f"c{i}_fisher"] = c.fisher
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {len(chunks)} chunks -> {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+def main():
+    if not refdump.available():
+        raise SystemExit("oracle not built: make -C oracle/refbuild")
+    for name, spec in CASES.items():
+        make_case(name, spec)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,77 @@
+"""Loader of the golden fixtures written by tests/golden/make_golden.py."""
+from __future__ import annotations
+
+import dataclasses
+import os
+
+import numpy as np
+
+from lyspeq_gb300 import synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub"]
+
+
+@dataclasses.dataclass
+class GoldenCase:
+    name: str
+    bins: synth.Bins
+    tables: list
+    nv: int
+    lenv: float
+    nzp: int
+    max_forest_length: float
+    marg: tuple
+    chunks: list          # (lambda_angstrom, delta, ivar, r_fwhm)
+    meta: list            # (n, fisher_index_start, nq, kbin_upp, r_fwhm, status)
+    dbt: list             # per chunk 3 x nq
+    fisher: list          # per chunk nq x nq
+    g: dict               # global reference results
+    complete: bool
+
+
+_cache = {}
+
+
+def load(name: str) -> GoldenCase:
+    if name in _cache:
+        return _cache[name]
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    b = z["bins"]
+    bins = synth.Bins(b[0], int(b[1]), b[2], int(b[3]), b[4], b[5], b[6], int(b[7]), bool(b[8]))
+    nv, lenv, nzp, mfl, m0, m1 = z["grid"]
+    nv, nzp = int(nv), int(nzp)
+    tables = [synth.build_table(bins, int(r), float(dv), nv, float(lenv), nzp)
+              for r, dv in zip(z["table_r"], z["table_dv"])]
+    sums = np.array([[np.abs(t.deriv).sum(), np.abs(t.signal).sum()] for t in tables])
+    np.testing.assert_allclose(sums, z["table_sums"], rtol=1e-12)
+    n = int(z["n_chunks"])
+    chunks, meta, dbt, fis = [], [], [], []
+    for i in range(n):
+        m = z[f"c{i}_meta"]
+        chunks.append((z[f"c{i}_lam"], z[f"c{i}_delta"], z[f"c{i}_ivar"], int(m[4])))
+        meta.append(tuple(int(x) for x in m))
+        dbt.append(z[f"c{i}_dbt"])
+        fis.append(z[f"c{i}_fisher"])
+    g = {k[2:]: z[k] for k in z.files if k.startswith("g_")}
+    case = GoldenCase(name, bins, tables, nv, float(lenv), nzp, float(mfl), (int(m0), int(m1)),
+                      chunks, meta, dbt, fis, g, bool(z["g_complete"]))
+    _cache[name] = case
+    return case
+
+
+def rel_err(x, ref):
+    """max |x - ref| / max |ref|, the error measure of the parity tests."""
+    x, ref = np.asarray(x), np.asarray(ref)
+    scale = np.max(np.abs(ref))
+    if scale == 0:
+        return float(np.max(np.abs(x)))
+    return float(np.max(np.abs(x - ref)) / scale)
+
+
+def fisher_err(f, ref):
+    """Per-element error of a Fisher matrix normalised by sqrt(F_ii F_jj)."""
+    d = np.sqrt(np.abs(np.diag(ref)))
+    den = np.outer(d, d)
+    den[den == 0] = 1.0
+    return float(np.max(np.abs(np.asarray(f) - ref) / den))

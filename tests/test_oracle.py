@@ -1,0 +1,106 @@
+"""The oracle: pinned against lyspeq's own golden files, then used as checker.
+
+* The reference compiled from its own sources (oracle/refbuild) reproduces
+  lyspeq's truth files tests/truth/test_it1_* on tests/input/test.config.
+* The table builder reproduces the truth lookup table signal_R70000_dv20.0.fits.
+* The numpy restatement (oracle/qmle_port.py) reproduces the compiled
+  reference's outputs stored in the golden fixtures.
+The first two need the reference sources and run only where they exist.
+"""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+from lyspeq_gb300 import synth
+from oracle import qmle_port as P
+from oracle import refdump
+
+REFERENCE = "/root/reference"
+have_ref = pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference sources absent")
+
+
+def _read_detailed(path):
+    with open(path) as f:
+        lines = [ln for ln in f if not ln.startswith("#")]
+    return np.loadtxt(lines, skiprows=1, usecols=(4, 5, 7), unpack=True)
+
+
+def _close(a, b):
+    # tests/compareTestResults.py:8-9, 47-63
+    diff = np.abs(a - b)
+    mag = np.maximum(np.abs(a), np.abs(b))
+    return bool(np.all(diff < 1e-8 + 1e-5 * mag))
+
+
+@have_ref
+def test_reference_build_reproduces_truth(tmp_path):
+    if not os.path.exists(refdump.LYAPOWER):
+        subprocess.run(["make", "-s", "-j8", "-C", os.path.join(G.GOLDEN, "..", "..", "oracle", "refbuild")],
+                       check=True)
+    out = tmp_path / "out"
+    out.mkdir()
+    shutil.copy(f"{REFERENCE}/tests/truth/signal_R70000_dv20.0.fits", out)
+    cfg = open(f"{REFERENCE}/tests/input/test.config").read()
+    cfg = cfg.replace("./tests/input/flist.txt", f"{REFERENCE}/tests/input/flist.txt")
+    cfg = cfg.replace("./tests/input/slist.txt", f"{REFERENCE}/tests/input/slist.txt")
+    cfg = cfg.replace("FileInputDir ./tests/input/", f"FileInputDir {REFERENCE}/tests/input/")
+    cfg = cfg.replace("./tests/output/", f"{out}/").replace("TemporaryFolder ./tests/output",
+                                                            f"TemporaryFolder {out}")
+    (tmp_path / "test.config").write_text(cfg)
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+    subprocess.run([refdump.LYAPOWER, str(tmp_path / "test.config")], check=True, env=env,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    t = _read_detailed(f"{REFERENCE}/tests/truth/test_it1_quadratic_power_estimate_detailed.dat")
+    r = _read_detailed(out / "test_it1_quadratic_power_estimate_detailed.txt")
+    for a, b in zip(t, r):
+        assert _close(a, b)
+    ft = np.loadtxt(f"{REFERENCE}/tests/truth/test_it1_fisher_matrix.dat", skiprows=1)
+    fr = np.loadtxt(out / "test_it1_fisher_matrix.txt", skiprows=1)
+    assert _close(ft, fr)
+
+
+@have_ref
+def test_table_builder_reproduces_truth_table():
+    bins = synth.Bins(0.0, 3, 7e-4, 2, 0.5, 1.8, 0.2, 2)
+    t = synth.build_table(bins, 70000, 20.0, 1401, 14000.0, 10, fid=(0.06, -2.6, -0.1, 1.0, 0.0, 0.0))
+    tr = synth.read_table_fits(f"{REFERENCE}/tests/truth/signal_R70000_dv20.0.fits")
+    for mine, ref in ((t.deriv, tr["deriv"]), (t.signal, tr["signal"])):
+        assert _close(mine, ref)
+        assert np.max(np.abs(mine - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+# The (2, 1)-order continuum templates of tiny_marg3 are nearly collinear on
+# these short chunks: the singular values of the template matrix span
+# s_min / s_max ~ 3e-9, so any FP64 orthonormalisation (the reference's
+# dgesvd included) fixes the projected C^-1 only to ~1e-16 / 3e-9 relative.
+TOL = {"tiny_marg3": 1e-7}
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_port_matches_reference(name):
+    c = G.load(name)
+    tol = TOL.get(name, 1e-12)
+    s = P.Settings(max_forest_length=c.max_forest_length, cont_logl_order=c.marg[0],
+                   cont_l_order=c.marg[1])
+    keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
+    tvs = [P.table_view(t, c.bins, c.nv, c.lenv, c.nzp) for t in c.tables]
+    results = []
+    for (lam, delta, ivar, r), meta, dbt, fis in zip(c.chunks, c.meta, c.dbt, c.fisher):
+        ch = P.make_chunk(lam, delta, ivar, r, c.bins, keys, s)
+        assert (ch.n, ch.fisher_index_start, ch.nq, ch.kbin_upp) == meta[:4]
+        d, b, t, f = P.chunk_iteration(ch, c.bins, tvs[ch.res_index], np.zeros(c.bins.nkz), s)
+        assert G.rel_err(d, dbt[0]) < tol
+        assert G.rel_err(b, dbt[1]) < tol
+        assert G.rel_err(t, dbt[2]) < tol
+        assert G.fisher_err(f, fis) < tol
+        results.append((ch.fisher_index_start, d, b, t, f))
+    if c.complete:
+        fsum, dbtsum = P.accumulate(c.bins.nkz, results)
+        g = P.newton_raphson_step(fsum, dbtsum)
+        assert G.rel_err(g["fisher"], c.g["fisher"]) < tol
+        assert G.rel_err(dbtsum, c.g["dbt"]) < tol
+        assert G.rel_err(g["theta"], c.g["theta"]) < max(tol, 1e-10)
