@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Benchmark: chunks/s of one Newton-Raphson iteration of lyspeq's per-chunk
+QMLE on one GB300, mixed precision vs FP64, with the CPU baseline beside it.
+
+Workload (BASELINE "DESI-like" configuration): 4096 synthetic chunks, N_pix
+log-uniform in [200, 1200], dv = 50 km/s, R uniform in [2000, 5000], 35 k bins,
+13 triangular z bins, S/N per pixel lognormal(ln 1, 0.8), continuum
+marginalisation of amplitude + slope.  Inputs are seeded synthetic data of
+those shapes (lyspeq_gb300.synth); the per-iteration working set (tens of GB
+of operand planes) is far larger than L2, so no L2 flush is needed.
+
+A step is one lqg_nr_iteration over the whole batch (table interpolation ->
+C -> FP64 Cholesky/inverse -> C^-1 Q_k on tensor cores -> traces) plus the
+global Fisher inversion and theta update.  `value` times steps with the
+chunks resident on the device; `e2e` times the same through the C ABI from
+host buffers (chunk upload, iteration, result download, solve).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "chunks/s per NR iteration (mixed precision, one GB300)"
+UNIT = "chunks/s"
+PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
+FP64_PEAK_TFLOPS = 1.191   # DFMA throughput measured on this machine's GB300 (see profiles/)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def chunk_arrays(w):
+    """Chunks as lqg_batch_add takes them: lambda (A), delta, ivar, R."""
+    return [(s.wave, s.delta, 1.0 / np.asarray(s.sigma) ** 2, s.r_fwhm) for s in w.spectra]
+
+
+def pack(chunks):
+    offs = np.zeros(len(chunks) + 1, dtype=np.int64)
+    for i, c in enumerate(chunks):
+        offs[i + 1] = offs[i] + len(c[0])
+    cat = lambda j: np.ascontiguousarray(np.concatenate([np.asarray(c[j], np.float64) for c in chunks]))
+    return cat(0), cat(1), cat(2), offs, np.array([c[3] for c in chunks], dtype=np.int32)
+
+
+def flop_counts(ns_list, n_list):
+    """Algorithmic FLOPs of the per-chunk work (the same for every precision):
+    factorisation n^3 (Cholesky + triangular inverse + C^-1 assembly, n^3/3
+    each), products 2 (ns + 1) n^3, traces 2 (ns + 2) ns n^2."""
+    n = np.asarray(n_list, dtype=np.float64)
+    ns = np.asarray(ns_list, dtype=np.float64)
+    return dict(factor=float(np.sum(n ** 3)), products=float(np.sum(2 * (ns + 1) * n ** 3)),
+                traces=float(np.sum(2 * (ns + 2) * ns * n ** 2)))
+
+
+def cpu_port_rate(w, chunks, budget_s=15.0, max_chunks=None):
+    """Chunks/s of the CPU restatement of lyspeq's per-chunk path (numpy +
+    scipy's OpenBLAS, all host threads) on a bounded sample of the workload."""
+    from oracle import qmle_port as P
+    s = P.Settings(max_forest_length=w.max_forest_length, cont_logl_order=w.cont_logl_order,
+                   cont_l_order=w.cont_l_order)
+    keys = w.table_index()
+    tvs = {}
+    t0 = time.perf_counter()
+    done = 0
+    for lam, delta, ivar, r in chunks:
+        try:
+            ch = P.make_chunk(lam, delta, ivar, r, w.bins, keys, s)
+        except (ValueError, KeyError):
+            continue
+        if ch.res_index not in tvs:
+            tvs[ch.res_index] = P.table_view(w.tables[ch.res_index], w.bins, w.nv, w.lenv, w.nzp)
+        P.chunk_iteration(ch, w.bins, tvs[ch.res_index], np.zeros(w.bins.nkz), s)
+        done += 1
+        if time.perf_counter() - t0 > budget_s or (max_chunks and done >= max_chunks):
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from lyspeq_gb300 import synth
+    w = synth.make_workload(args.workload)
+    chunks = chunk_arrays(w)
+    rng = np.random.default_rng(1)
+    rates, times, counts = [], [], []
+    for step in range(args.warmup + args.steps):
+        order = rng.permutation(len(chunks))
+        rate, done, dt = cpu_port_rate(w, [chunks[i] for i in order], budget_s=args.cpu_budget)
+        if step >= args.warmup:
+            rates.append(rate)
+            times.append(dt)
+            counts.append(done)
+    value = float(np.mean(rates))
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times) * 1e3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded, DESI-like shapes)",
+        "config": {"workload": f"{args.workload}: 4096 chunks, N 200-1200, dv 50, 35 k x 13 z bins",
+                   "sample": f"{int(np.mean(counts))} random chunks per step (~{args.cpu_budget:.0f} s)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{int(np.mean(counts))} chunks/step of the {args.workload} workload"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="desi")
+    ap.add_argument("--chunks", type=int, default=None)
+    ap.add_argument("--fp64-chunks", type=int, default=96)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from lyspeq_gb300 import build, lqg, synth
+    build.build()
+    seed = None if world == 1 else 20240602 + 7919 * rank
+    w = synth.make_workload(args.workload, seed=seed, n_chunks=args.chunks)
+    chunks = chunk_arrays(w)
+    lam, delta, ivar, offs, rr = pack(chunks)
+    lam_p, delta_p, ivar_p = (torch.from_numpy(x).pin_memory().numpy() for x in (lam, delta, ivar))
+    eng = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
+                     cont=(w.cont_logl_order, w.cont_l_order), device=local)
+    st = eng.add_chunks(lam_p, delta_p, ivar_p, offs, rr)
+    n_ok = int((st == 0).sum())
+    infos = [eng.chunk_info(i) for i in range(eng.size)]
+    ns_list = [(i["nq"] // w.bins.nk) * i["kbin_upp"] for i in infos]
+    n_list = [i["n"] for i in infos]
+    nkz = w.bins.nkz
+
+    def allreduce(out):
+        if world == 1:
+            return out
+        import torch.distributed as dist
+        buf = torch.from_numpy(np.concatenate([out["fisher"].ravel(), out["d"], out["b"], out["t"]])).cuda()
+        dist.all_reduce(buf)
+        v = buf.cpu().numpy()
+        return dict(fisher=v[:nkz * nkz].reshape(nkz, nkz), d=v[nkz * nkz:nkz * nkz + nkz],
+                    b=v[nkz * nkz + nkz:nkz * nkz + 2 * nkz], t=v[nkz * nkz + 2 * nkz:], status=out["status"])
+
+    def step_resident():
+        eng.iterate(precision="mixed")
+        out = allreduce(eng.download())
+        return eng.fisher_solve(out["fisher"], np.stack([out["d"], out["b"], out["t"]]))
+
+    def step_e2e():
+        eng.clear()
+        eng.add_chunks(lam_p, delta_p, ivar_p, offs, rr)
+        return step_resident()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_resident()
+    phase = np.zeros(8)
+    launches = 0
+    barrier()
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            step_resident()
+            phase += eng.timings()
+            launches += eng.launch_count()
+        e1.record()
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n_ok * world / (ms / 1e3)
+    phase /= args.steps
+
+    # end to end through the C ABI from pinned host buffers
+    barrier()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    for _ in range(args.steps):
+        step_e2e()
+    e3.record()
+    barrier()
+    ms_e2e = e2.elapsed_time(e3) / args.steps
+    e2e_value = n_ok * world / (ms_e2e / 1e3)
+    h2d = int(lam.nbytes + delta.nbytes + ivar.nbytes + 8 * nkz)
+    d2h = int(8 * (nkz * nkz + 3 * nkz))
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return 0
+
+    # FP64 GPU path on a subset of the same chunks, and accuracy of mixed vs FP64 there
+    sub = chunks[:args.fp64_chunks]
+    e64 = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
+                     cont=(w.cont_logl_order, w.cont_l_order), device=local)
+    e64.add_chunk_list(sub)
+    e64.iterate(precision="fp64")
+    t0 = time.perf_counter()
+    e64.iterate(precision="fp64")
+    fp64_ms = e64.timings()[7]
+    ref = e64.download()
+    g_ref = e64.fisher_solve(ref["fisher"], np.stack([ref["d"], ref["b"], ref["t"]]))
+    fp64_rate = int((ref["status"] == 0).sum()) / (fp64_ms / 1e3)
+    e64.iterate(precision="mixed")
+    mix = e64.download()
+    g_mix = e64.fisher_solve(mix["fisher"], np.stack([mix["d"], mix["b"], mix["t"]]))
+    dg = np.sqrt(np.abs(np.diag(g_ref["fisher"])))
+    den = np.outer(dg, dg)
+    den[den == 0] = 1
+    err_f = float(np.max(np.abs(g_mix["fisher"] - g_ref["fisher"]) / den))
+    dbt_ref = np.stack([ref["d"], ref["b"], ref["t"]])
+    dbt_mix = np.stack([mix["d"], mix["b"], mix["t"]])
+    err_dbt = float(np.max(np.abs(dbt_mix - dbt_ref) / np.max(np.abs(dbt_ref), axis=1, keepdims=True)))
+    pfid = synth.pd13_power(np.tile(w.bins.k_centers, w.bins.nz),
+                            np.repeat(w.bins.z_centers, w.bins.nk))
+    p_ref, p_mix = pfid + g_ref["theta"], pfid + g_mix["theta"]
+    used = np.diag(g_ref["fisher"]) > 0
+    err_p1d = float(np.max(np.abs(p_mix - p_ref)[used] / np.abs(p_ref)[used]))
+    e64.close()
+
+    # roofline of the dominant kernel
+    fl = flop_counts(ns_list, n_list)
+    names = ["build_s_c", "factor_fp64", "build_q", "products_tc", "traces_tc", "finish", "accumulate"]
+    shares = {nm: float(phase[i] / phase[7]) for i, nm in enumerate(names)}
+    dom = max(range(7), key=lambda i: phase[i])
+    peaks = {}
+    if os.path.exists(PEAKS_FILE):
+        peaks = json.load(open(PEAKS_FILE))
+    if names[dom] == "factor_fp64":
+        achieved = fl["factor"] / (phase[1] / 1e3) / 1e12
+        roof = {"kernel": "k_factor", "bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
+                "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                "peak_source": "DFMA throughput probe on GB300 (MEASURED_PEAKS.json has no FP64 figure)"}
+    else:
+        key = "products" if names[dom] == "products_tc" else "traces"
+        achieved = fl[key] / (phase[dom] / 1e3) / 1e12
+        pk = peaks.get("bf16_tflops", 1900.0)
+        roof = {"kernel": "k_tc_gemm" if key == "products" else "k_tc_gram", "bound": "tensor",
+                "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
+                "traffic": None, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}
+    tensor_tf = fl["products"] / (phase[3] / 1e3) / 1e12 if phase[3] > 0 else None
+    fp64_tf = fl["factor"] / (phase[1] / 1e3) / 1e12 if phase[1] > 0 else None
+
+    cpu = None
+    if not args.no_cpu:
+        rate, done, dt = cpu_port_rate(w, chunks, budget_s=args.cpu_budget)
+        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"first {done} chunks of the workload, {dt:.1f} s, numpy + scipy OpenBLAS"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16x3 products / f64 factorisation", "data": "synthetic (seeded)",
+        "config": {"workload": f"{args.workload}: {n_ok} chunks, N log-uniform 200-1200, dv 50 km/s, "
+                               "R 2000-5000, 35 k x 13 z bins, amplitude+slope marginalisation",
+                   "l2": "working set of tens of GB per iteration (>> 129 MB L2); no flush"},
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": ms_e2e},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "fp64_gpu": {"value": fp64_rate, "unit": UNIT, "chunks": len(sub), "ms": fp64_ms},
+        "mixed_over_fp64": value / fp64_rate if fp64_rate else None,
+        "mixed_rel_err": {"fisher": err_f, "dbt": err_dbt, "p1d": err_p1d},
+        "phase_ms": {nm: float(phase[i]) for i, nm in enumerate(names)},
+        "phase_share": shares,
+        "achieved_tflops": {"fp64_factor": fp64_tf, "tensor_products": tensor_tf},
+    }
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    eng.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -54,6 +54,7 @@ extern "C" {
 #define LQG_CHUNK_NOT_SPD 5     /* covariance not positive definite ("not invertable") */
 #define LQG_CHUNK_BAD_INPUT 6   /* non-finite pixel values */
 #define LQG_CHUNK_TOO_LARGE 7   /* more pixels than the engine's maximum */
+#define LQG_CHUNK_TIMEOUT 8     /* a bounded device wait gave up; results dropped */
 
 /* arithmetic of the per-chunk products */
 #define LQG_PRECISION_FP64 0    /* everything in IEEE binary64 */
@@ -155,14 +156,16 @@ int lqg_chunk_result(lqg_ctx *ctx, int i, double *d, double *b, double *t, doubl
  * In: fisher_sum [nkz^2] (upper, unhalved), dbt [3][nkz].
  * Out (any may be NULL): fisher [nkz^2] halved and symmetric, solver and
  * inverse [nkz^2], weighted [3][nkz] (0.5 F_solver d, b, t), theta [nkz],
- * damped (0/1), dof, damp.  Runs in FP64 on the device. */
+ * damped (0/1), dof, damp.  FP64, O(nkz^3), on the host CPU. */
 int lqg_fisher_solve(lqg_ctx *ctx, const double *fisher_sum, const double *dbt,
                      double *fisher, double *solver, double *inverse, double *weighted,
                      double *theta, int *damped, int *dof, double *damp);
 
 /* Device time (ms) of the phases of the last iteration, CUDA events on the
- * context stream: [0] build + factorisation, [1] C^-1 Q_k products,
- * [2] traces / Fisher, [3] total.  Returns the number of values written. */
+ * context stream, summed over the size-bucketed waves: [0] S and C build,
+ * [1] FP64 factorisation, inverse and marginalisation, [2] Q_k build,
+ * [3] C^-1 Q_k products, [4] Fisher / bias traces, [5] per-chunk reduction,
+ * [6] global accumulation, [7] whole iteration.  Returns the number written. */
 int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n);
 
 /* Number of kernel launches the last lqg_nr_iteration enqueued. */

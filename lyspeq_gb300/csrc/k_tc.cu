@@ -1,11 +1,519 @@
-// Tensor-core (tcgen05) kernels of the mixed-precision path.
+// Tensor-core kernels of the mixed-precision path (sm_103a, tcgen05 + TMA).
+//
+// Every FP64 operand X is stored as two fp16 planes, hi = fp16(s X) and
+// lo = fp16(s X - hi), with a power-of-two scale s chosen so |s X| <= 2^14;
+// hi + lo carries 22 significant bits.  A product is taken as
+//     A B ~= A_hi B_hi + A_hi B_lo + A_lo B_hi
+// (three tcgen05.mma kind::f16 per K step, fp32 accumulation in tensor
+// memory); the dropped A_lo B_lo term is below 2^-22 relative.
+//
+// k_tc_gemm:  A_s = C^-1 Q_s for every stored derivative matrix and A_S = C^-1 S
+//             (Chunk::_getWeightedMatrix, core/chunk_estimate.cpp:721-736, and
+//             the S_fid C^-1 product at :796-799).  The epilogue writes A_s as
+//             hi/lo planes twice: row-major into R and transposed into P.
+// k_tc_gram:  G = P R^T over K = ld^2, split over K; per-split fp32 partial
+//             tiles are reduced in FP64 by k_finish.  Rows of P are A_s^T,
+//             A_S^T = S C^-1 and N C^-1, so G holds F_ij = <A_i^T, A_j>,
+//             t_j and b_j (core/chunk_estimate.cpp:783-832).
+//
+// Warp roles (192 threads): warp 0 issues TMA loads, warp 1 owns tensor memory
+// and issues the MMAs, warps 2-5 drain the accumulator.  Every wait on an
+// mbarrier is bounded by a wall-clock limit; on timeout the kernel records an
+// error in the chunk status and leaves after its own work has drained.
 #include "lqg_internal.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 namespace lqg {
 
-bool tc_available() { return false; }
+namespace {
 
-void launch_scales_mixed(WaveArgs &, cudaStream_t) {}
-void launch_products_mixed(WaveArgs &, cudaStream_t, const int *, int) {}
+constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait for the phase of the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    uint64_t t0 = 0;
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        uint64_t t = now_ns();
+        if (t0 == 0) t0 = t;
+        else if (t - t0 > kWaitLimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
+                                            int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+        "%4, %5}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
+                                            int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+        "%4}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with
+// 128-byte swizzle: rows of 64 fp16 (128 B), 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(const void *tile) {
+    uint64_t addr = smem_u32(tile);
+    uint64_t d = (addr & 0x3FFFF) >> 4;      // start address
+    d |= (uint64_t) 1 << 16;                  // leading byte offset (unused with this swizzle)
+    d |= (uint64_t) (1024 >> 4) << 32;        // stride byte offset
+    d |= (uint64_t) 1 << 46;                  // descriptor version
+    d |= (uint64_t) 2 << 61;                  // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: fp16 A and B (K-major), fp32 D.
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
+    return (1u << 4) | ((uint32_t) (n >> 3) << 17) | ((uint32_t) (m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive fp32 columns of this warp's 32 lanes.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+        "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+        "%30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+          "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+          "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ double pow2_floor(double x) {
+    if (!(x > 0) || !isfinite(x)) return 1.0;
+    int e;
+    frexp(x, &e);
+    return ldexp(1.0, e - 1);
+}
+
+constexpr int BK = 64;                      // fp16 elements per K step (128 bytes)
+constexpr int G_BM = 128, G_BN = 256, G_STAGES = 2;
+constexpr int G_TILE_A = G_BM * BK * 2, G_TILE_B = G_BN * BK * 2;
+constexpr int G_STAGE_BYTES = 2 * G_TILE_A + 2 * G_TILE_B;
+constexpr int G_SMEM = G_STAGES * G_STAGE_BYTES + 1024 + 256;
+constexpr int R_BM = 128, R_BN = 128, R_STAGES = 3;
+constexpr int R_TILE = R_BM * BK * 2;
+constexpr int R_STAGE_BYTES = 4 * R_TILE;
+constexpr int R_SMEM = R_STAGES * R_STAGE_BYTES + 1024 + 256;
+constexpr int kGramK = 8192;                // K elements per Gram split
+
+struct TcMaps {
+    CUtensorMap c_hi, c_lo, q_hi, q_lo;     // GEMM operands (3D: k, row, matrix)
+    CUtensorMap p_hi, p_lo, r_hi, r_lo;     // Gram operands (2D: k, slot)
+};
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(192, 1)
+k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
+          const __grid_constant__ CUtensorMap mc_lo, const __grid_constant__ CUtensorMap mq_hi,
+          const __grid_constant__ CUtensorMap mq_lo) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + G_STAGES * G_STAGE_BYTES);
+    uint64_t *empty = full + G_STAGES;
+    uint64_t *accum = empty + G_STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+
+    const int job = blockIdx.y;
+    if (job >= njobs) return;
+    const int c = jobs[2 * job], s = jobs[2 * job + 1];
+    const ChunkDesc &ch = a.chunks[c];
+    const int ld = ch.ld;
+    const int mt = (ld + G_BM - 1) / G_BM, nt = (ld + G_BN - 1) / G_BN;
+    if ((int) blockIdx.x >= mt * nt || a.status[c] != LQG_CHUNK_OK) return;
+    const int m0 = (blockIdx.x % mt) * G_BM, n0 = (blockIdx.x / mt) * G_BN;
+    const int kblocks = ld / BK;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < G_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+        mbar_init(accum, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, G_BN);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // TMA producer
+        const int qslot = ch.slot_q + s;
+        int issued = 0;
+        for (int kb = 0; kb < kblocks; ++kb) {
+            const int st = kb % G_STAGES;
+            if (!mbar_wait(&empty[st], ((kb / G_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
+            unsigned char *sb = smem + st * G_STAGE_BYTES;
+            mbar_expect_tx(&full[st], G_STAGE_BYTES);
+            tma_load_3d(sb, &mc_hi, &full[st], kb * BK, m0, c);
+            tma_load_3d(sb + G_TILE_A, &mc_lo, &full[st], kb * BK, m0, c);
+            tma_load_3d(sb + 2 * G_TILE_A, &mq_hi, &full[st], kb * BK, n0, qslot);
+            tma_load_3d(sb + 2 * G_TILE_A + G_TILE_B, &mq_lo, &full[st], kb * BK, n0, qslot);
+            ++issued;
+        }
+        // drain: every issued stage must land before the CTA may leave
+        for (int kb = (issued > G_STAGES ? issued - G_STAGES : 0); kb < issued; ++kb)
+            mbar_wait(&full[kb % G_STAGES], (kb / G_STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t idesc = idesc_f16(G_BM, G_BN);
+        bool ok = true;
+        for (int kb = 0; kb < kblocks && ok; ++kb) {
+            const int st = kb % G_STAGES;
+            if (!mbar_wait(&full[st], (kb / G_STAGES) & 1)) { *abort_flag = 1; ok = false; break; }
+            fence_after();
+            unsigned char *sb = smem + st * G_STAGE_BYTES;
+            const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + G_TILE_A);
+            const uint64_t bh = sw128_desc(sb + 2 * G_TILE_A), bl = sw128_desc(sb + 2 * G_TILE_A + G_TILE_B);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t adv = (uint64_t) (kk * 32) >> 4;
+                umma_f16(tmem, ah + adv, bh + adv, idesc, (kb | kk) != 0);
+                umma_f16(tmem, ah + adv, bl + adv, idesc, 1);
+                umma_f16(tmem, al + adv, bh + adv, idesc, 1);
+            }
+            umma_commit(&empty[st]);
+        }
+        umma_commit(accum);
+    } else if (warp >= 2) {
+        // epilogue: TMEM -> scaled fp16 hi/lo planes, row-major (R) and transposed (P)
+        const bool got = mbar_wait(accum, 0);
+        fence_after();
+        if (got && !*abort_flag) {
+            const int sub = warp % 4;
+            const int row = m0 + sub * 32 + lane;
+            const int nq4 = 4 * a.n_chunks;
+            const double sc = a.scales[4 * c + 2];
+            const double qs = a.scales[nq4 + ch.slot_q + s];
+            const double ps = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
+            const float mult = (float) (ps / (sc * qs));
+            const size_t plane = (size_t) ld * ld;
+            __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
+            __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
+            const bool write_r = s < ch.ns;
+            for (int jc = 0; jc < G_BN / 32; ++jc) {
+                const int col0 = n0 + jc * 32;
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t) (sub * 32) << 16) + jc * 32, v);
+                if (col0 >= ld) continue;
+                __align__(16) __half hi[32], lo[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    float x = v[j] * mult;
+                    hi[j] = __float2half_rn(x);
+                    lo[j] = __float2half_rn(x - __half2float(hi[j]));
+                }
+                if (row < ld) {
+                    if (write_r) {
+                        uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + col0);
+                        uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + col0);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            dh[q] = reinterpret_cast<const uint4 *>(hi)[q];
+                            dl[q] = reinterpret_cast<const uint4 *>(lo)[q];
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        Ph[(size_t) (col0 + j) * ld + row] = hi[j];
+                        Pl[(size_t) (col0 + j) * ld + row] = lo[j];
+                    }
+                }
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        tmem_dealloc(tmem, G_BN);
+    }
+    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[c], LQG_CHUNK_TIMEOUT);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(192, 1)
+k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_constant__ CUtensorMap mp_lo,
+          const __grid_constant__ CUtensorMap mr_hi, const __grid_constant__ CUtensorMap mr_lo) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + R_STAGES * R_STAGE_BYTES);
+    uint64_t *empty = full + R_STAGES;
+    uint64_t *accum = empty + R_STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+
+    const int c = blockIdx.y, sp = blockIdx.x;
+    const ChunkDesc &ch = a.chunks[c];
+    if (a.status[c] != LQG_CHUNK_OK || sp >= a.gram_splits) return;
+    const int64_t K = (int64_t) ch.ld * ch.ld;
+    const int64_t kper = ((K + a.gram_splits - 1) / a.gram_splits + BK - 1) / BK * BK;
+    const int64_t k_lo = sp * kper, k_hi = min(K, k_lo + kper);
+    const int kblocks = k_hi > k_lo ? (int) ((k_hi - k_lo) / BK) : 0;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < R_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+        mbar_init(accum, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, R_BN);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        int issued = 0;
+        for (int kb = 0; kb < kblocks; ++kb) {
+            const int st = kb % R_STAGES;
+            if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
+            unsigned char *sb = smem + st * R_STAGE_BYTES;
+            const int x = (int) (k_lo + (int64_t) kb * BK);
+            mbar_expect_tx(&full[st], R_STAGE_BYTES);
+            tma_load_2d(sb, &mp_hi, &full[st], x, ch.slot_p);
+            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], x, ch.slot_p);
+            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], x, ch.slot_r);
+            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], x, ch.slot_r);
+            ++issued;
+        }
+        for (int kb = (issued > R_STAGES ? issued - R_STAGES : 0); kb < issued; ++kb)
+            mbar_wait(&full[kb % R_STAGES], (kb / R_STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = idesc_f16(R_BM, R_BN);
+        for (int kb = 0; kb < kblocks; ++kb) {
+            const int st = kb % R_STAGES;
+            if (!mbar_wait(&full[st], (kb / R_STAGES) & 1)) { *abort_flag = 1; break; }
+            fence_after();
+            unsigned char *sb = smem + st * R_STAGE_BYTES;
+            const uint64_t ph = sw128_desc(sb), pl = sw128_desc(sb + R_TILE);
+            const uint64_t rh = sw128_desc(sb + 2 * R_TILE), rl = sw128_desc(sb + 3 * R_TILE);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t adv = (uint64_t) (kk * 32) >> 4;
+                umma_f16(tmem, ph + adv, rh + adv, idesc, (kb | kk) != 0);
+                umma_f16(tmem, ph + adv, rl + adv, idesc, 1);
+                umma_f16(tmem, pl + adv, rh + adv, idesc, 1);
+            }
+            umma_commit(&empty[st]);
+        }
+        umma_commit(accum);
+    } else if (warp >= 2) {
+        const bool got = mbar_wait(accum, 0);
+        fence_after();
+        if (got && !*abort_flag) {
+            const int sub = warp % 4;
+            const int row = sub * 32 + lane;
+            float *out = a.gram_part + ((size_t) c * a.gram_splits + sp) * R_BM * R_BN + (size_t) row * R_BN;
+            for (int jc = 0; jc < R_BN / 32; ++jc) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t) (sub * 32) << 16) + jc * 32, v);
+                if (kblocks == 0)
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) v[j] = 0.f;
+                float4 *o = reinterpret_cast<float4 *>(out + jc * 32);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        tmem_dealloc(tmem, R_BN);
+    }
+    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[c], LQG_CHUNK_TIMEOUT);
+}
+
+// Operand scales of the mixed path (powers of two), from the FP64 bounds the
+// factorisation left in scales[4c + 0..1]: max |C^-1| and the largest row sum.
+__global__ void k_scales(WaveArgs a) {
+    const int c = blockIdx.x;
+    const ChunkDesc &ch = a.chunks[c];
+    if (a.status[c] != LQG_CHUNK_OK) return;
+    __shared__ double red[32];
+    double mx = 0;
+    const double *iv = a.ivar + ch.pix;
+    for (int i = threadIdx.x; i < ch.n; i += blockDim.x)
+        if (iv[i] != 0) mx = fmax(mx, 1.0 / iv[i]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = mx;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int i = 1; i < (int) blockDim.x / 32; ++i) mx = fmax(mx, red[i]);
+    double *sc = a.scales + 4 * c;
+    const double maxc = sc[0], rowsum = sc[1];
+    const double target = 16384.0;
+    sc[2] = pow2_floor(target / maxc);
+    sc[3] = pow2_floor(target / (maxc * mx));
+    const int nq4 = 4 * a.n_chunks;
+    double *qsc = a.scales + nq4 + ch.slot_q;
+    double *psc = a.scales + nq4 + a.total_slots_q + ch.slot_p;
+    double *rsc = a.scales + nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r;
+    for (int s = 0; s <= ch.ns; ++s) {
+        // |C^-1 B| <= rowsum * max|B| and max|B| <= target / (B scale)
+        double r = pow2_floor(qsc[s] / rowsum);
+        psc[s] = r;
+        if (s < ch.ns) rsc[s] = r;
+    }
+    psc[ch.ns + 1] = sc[3];
+}
+
+// cuTensorMapEncodeTiled is resolved through the runtime so that the library
+// does not link libcuda (it then also loads on machines without a driver).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+CUtensorMap make_map(void *base, int rank, const cuuint64_t *dims, const cuuint64_t *strides,
+                     const cuuint32_t *box, bool *ok) {
+    CUtensorMap m;
+    cuuint32_t es[3] = {1, 1, 1};
+    auto enc = encode_fn();
+    if (!enc) { *ok = false; return m; }
+    CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, rank, base, dims, strides, box,
+                                        es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) *ok = false;
+    return m;
+}
+
+}  // namespace
+
+bool tc_available() { return true; }
+
+void launch_scales_mixed(WaveArgs &a, cudaStream_t st) {
+    k_scales<<<a.n_chunks, 256, 0, st>>>(a);
+    a.launches++;
+}
+
+void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, R_SMEM);
+        attr = true;
+    }
+    const int ld = a.max_ld;
+    const cuuint64_t plane = (cuuint64_t) ld * ld;
+    bool ok = true;
+    cuuint64_t d3c[3] = {(cuuint64_t) ld, (cuuint64_t) ld, (cuuint64_t) a.n_chunks};
+    cuuint64_t d3q[3] = {(cuuint64_t) ld, (cuuint64_t) ld, (cuuint64_t) a.total_slots_q};
+    cuuint64_t s3[2] = {(cuuint64_t) ld * 2, plane * 2};
+    cuuint32_t boxa[3] = {BK, G_BM, 1}, boxb[3] = {BK, G_BN, 1};
+    CUtensorMap mch = make_map(a.c_hi, 3, d3c, s3, boxa, &ok);
+    CUtensorMap mcl = make_map(a.c_lo, 3, d3c, s3, boxa, &ok);
+    CUtensorMap mqh = make_map(a.q_hi, 3, d3q, s3, boxb, &ok);
+    CUtensorMap mql = make_map(a.q_lo, 3, d3q, s3, boxb, &ok);
+    cuuint64_t d2p[2] = {plane, (cuuint64_t) a.total_slots_p};
+    cuuint64_t d2r[2] = {plane, (cuuint64_t) a.total_slots_r};
+    cuuint64_t s2[1] = {plane * 2};
+    cuuint32_t box2[2] = {BK, R_BM};
+    CUtensorMap mph = make_map(a.p_hi, 2, d2p, s2, box2, &ok);
+    CUtensorMap mpl = make_map(a.p_lo, 2, d2p, s2, box2, &ok);
+    CUtensorMap mrh = make_map(a.r_hi, 2, d2r, s2, box2, &ok);
+    CUtensorMap mrl = make_map(a.r_lo, 2, d2r, s2, box2, &ok);
+    if (!ok) {
+        fprintf(stderr, "lqg: cuTensorMapEncodeTiled failed\n");
+        return;
+    }
+    const int tiles = ((ld + G_BM - 1) / G_BM) * ((ld + G_BN - 1) / G_BN);
+    k_tc_gemm<<<dim3(tiles, njobs), 192, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
+    if (a.mid_event) cudaEventRecord(a.mid_event, st);
+    k_tc_gram<<<dim3(a.gram_splits, a.n_chunks), 192, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
+    a.launches += 2;
+}
+
+int gram_splits_mixed(int ld) {
+    int64_t K = (int64_t) ld * ld;
+    return (int) ((K + kGramK - 1) / kGramK);
+}
 
 }  // namespace lqg

@@ -37,9 +37,9 @@ struct lqg_ctx {
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
-    DevBuf d_ws, d_desc, d_jobs, d_scales, d_halves, d_gram;
+    DevBuf d_ws, d_desc, d_jobs, d_scales, d_halves, d_gram, d_wstat;
     std::vector<int> last_status;
-    double timings[4] = {0, 0, 0, 0};
+    double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int launches = 0;
     cudaEvent_t ev[8] = {};
 };
@@ -351,7 +351,8 @@ int64_t chunk_ws_bytes(const lqg_ctx::HostChunk &h, int precision, int splits) {
     return base;
 }
 
-int gram_splits_for(int ld) {
+int gram_splits_for(int ld, int precision) {
+    if (precision == LQG_PRECISION_MIXED) return gram_splits_mixed(ld);
     int64_t K = (int64_t) ld * ld;
     int64_t s = (K + 32767) / 32768;
     return (int) std::max<int64_t>(1, std::min<int64_t>(s, 256));
@@ -361,7 +362,7 @@ int run_wave(lqg_ctx *ctx, const WavePlan &w, int precision, bool use_theta) {
     cudaStream_t st = ctx->stream;
     const int nch = (int) w.members.size();
     const int ld = w.ld;
-    const int splits = gram_splits_for(ld);
+    const int splits = gram_splits_for(ld, precision);
     std::vector<ChunkDesc> desc(nch);
     int64_t off = 0;
     int slot_q = 0, slot_r = 0, slot_p = 0;
@@ -421,9 +422,8 @@ int run_wave(lqg_ctx *ctx, const WavePlan &w, int precision, bool use_theta) {
     if (ctx->d_jobs.alloc(jobs.size() * 4)) return set_err(ctx, LQG_ERR_NOMEM, "jobs");
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_jobs.p, jobs.data(), jobs.size() * 4, cudaMemcpyHostToDevice, st));
     // wave-local status: starts OK
-    DevBuf wstat;
-    if (wstat.alloc(nch * 4)) return set_err(ctx, LQG_ERR_NOMEM, "status");
-    LQG_CUDA_CHECK_RET(cudaMemsetAsync(wstat.p, 0, nch * 4, st));
+    if (ctx->d_wstat.alloc(nch * 4)) return set_err(ctx, LQG_ERR_NOMEM, "status");
+    LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_wstat.p, 0, nch * 4, st));
 
     WaveArgs a{};
     a.chunks = ctx->d_desc.as<ChunkDesc>();
@@ -436,7 +436,7 @@ int run_wave(lqg_ctx *ctx, const WavePlan &w, int precision, bool use_theta) {
     a.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
     a.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
     a.results = ctx->d_results.as<double>();
-    a.status = wstat.as<int>();
+    a.status = ctx->d_wstat.as<int>();
     a.grid = ctx->grid;
     a.bins = ctx->d_bins.as<DeviceBins>();
     a.cont_logl = ctx->opts.cont_logl_order;
@@ -460,30 +460,35 @@ int run_wave(lqg_ctx *ctx, const WavePlan &w, int precision, bool use_theta) {
         a.p_lo = hb; hb += pl * slot_p;
         a.gram_part = ctx->d_gram.as<float>();
     }
+    a.mid_event = ctx->ev[4];
     cudaEventRecord(ctx->ev[0], st);
     launch_build_s_c(a, st);
+    cudaEventRecord(ctx->ev[1], st);
     launch_factor(a, st);
+    cudaEventRecord(ctx->ev[2], st);
     if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(a, st);
     launch_build_q(a, st);
-    cudaEventRecord(ctx->ev[1], st);
+    cudaEventRecord(ctx->ev[3], st);
     if (precision == LQG_PRECISION_MIXED)
         launch_products_mixed(a, st, ctx->d_jobs.as<int>(), (int) jobs.size() / 2);
     else
         launch_products_fp64(a, st, ctx->d_jobs.as<int>(), (int) jobs.size() / 2);
-    cudaEventRecord(ctx->ev[2], st);
+    cudaEventRecord(ctx->ev[5], st);
     launch_finish(a, st);
-    cudaEventRecord(ctx->ev[3], st);
+    cudaEventRecord(ctx->ev[6], st);
     // scatter wave status into the batch status array
     std::vector<int> ws_host(nch);
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ws_host.data(), wstat.p, nch * 4, cudaMemcpyDeviceToHost, st));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ws_host.data(), ctx->d_wstat.p, nch * 4, cudaMemcpyDeviceToHost, st));
     LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, std::string("wave kernels: ") + cudaGetErrorString(e));
-    float t01 = 0, t12 = 0, t23 = 0;
-    cudaEventElapsedTime(&t01, ctx->ev[0], ctx->ev[1]);
-    cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
-    cudaEventElapsedTime(&t23, ctx->ev[2], ctx->ev[3]);
-    ctx->timings[0] += t01; ctx->timings[1] += t12; ctx->timings[2] += t23;
+    // [0] S/C build, [1] factorisation, [2] Q build, [3] C^-1 Q products, [4] Gram, [5] finish
+    static const int from[6] = {0, 1, 2, 3, 4, 5}, to[6] = {1, 2, 3, 4, 5, 6};
+    for (int k = 0; k < 6; ++k) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[from[k]], ctx->ev[to[k]]);
+        ctx->timings[k] += ms;
+    }
     for (int i = 0; i < nch; ++i) ctx->last_status[w.members[i]] = ws_host[i];
     ctx->launches += a.launches;
     return LQG_OK;
@@ -507,7 +512,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     }
     const int nb = (int) ctx->chunks.size();
     ctx->last_status.assign(nb, LQG_CHUNK_OK);
-    std::fill(ctx->timings, ctx->timings + 4, 0.0);
+    std::fill(ctx->timings, ctx->timings + 8, 0.0);
     ctx->launches = 0;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
@@ -528,7 +533,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     int64_t used = 0;
     for (int idx : order) {
         const auto &h = ctx->chunks[idx];
-        int64_t need = chunk_ws_bytes(h, precision, gram_splits_for(h.ld));
+        int64_t need = chunk_ws_bytes(h, precision, gram_splits_for(h.ld, precision));
         if (waves.empty() || waves.back().ld != h.ld || used + need > (int64_t) budget) {
             waves.push_back(WavePlan{});
             waves.back().ld = h.ld;
@@ -542,14 +547,17 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
         if (rc) return rc;
     }
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_status.p, ctx->last_status.data(), nb * 4, cudaMemcpyHostToDevice, ctx->stream));
+    cudaEventRecord(ctx->ev[7], ctx->stream);
     launch_accumulate(ctx->d_meta.as<ChunkDesc>(), nb, ctx->d_results.as<double>(), ctx->d_status.as<int>(),
                       ctx->nkz, ctx->d_fisher.as<double>(), ctx->d_dbt.as<double>(), ctx->stream);
     ctx->launches++;
     cudaEventRecord(t1, ctx->stream);
     LQG_CUDA_CHECK_RET(cudaStreamSynchronize(ctx->stream));
-    float tt = 0;
+    float tt = 0, ta = 0;
     cudaEventElapsedTime(&tt, t0, t1);
-    ctx->timings[3] = tt;
+    cudaEventElapsedTime(&ta, ctx->ev[7], t1);
+    ctx->timings[6] = ta;
+    ctx->timings[7] = tt;
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     cudaError_t e = cudaGetLastError();
@@ -587,7 +595,7 @@ extern "C" int lqg_chunk_result(lqg_ctx *ctx, int i, double *d, double *b, doubl
 
 extern "C" int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n) {
     if (!ctx || !ms) return 0;
-    int k = std::min(n, 4);
+    int k = std::min(n, 8);
     for (int i = 0; i < k; ++i) ms[i] = ctx->timings[i];
     return k;
 }

@@ -91,6 +91,7 @@ struct WaveArgs {
     int gram_splits;
     double *scales;              // per-slot scales (mixed): q [slots], r, p and c
     int launches;
+    cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
 };
 
 void launch_build_s_c(WaveArgs &a, cudaStream_t st);
@@ -102,6 +103,7 @@ void launch_scales_mixed(WaveArgs &a, cudaStream_t st);
 void launch_finish(WaveArgs &a, cudaStream_t st);
 
 bool tc_available();
+int gram_splits_mixed(int ld);
 
 }  // namespace lqg
 

@@ -203,8 +203,10 @@ class Engine:
         return out
 
     def timings(self):
-        ms = np.zeros(4)
-        self.lib.lqg_last_timings(self.h, _dptr(ms), 4)
+        """Device ms of the last iteration: build S/C, factorisation, build Q,
+        C^-1 Q products, traces, per-chunk reduction, accumulation, total."""
+        ms = np.zeros(8)
+        self.lib.lqg_last_timings(self.h, _dptr(ms), 8)
         return ms
 
     def launch_count(self):

@@ -1,0 +1,64 @@
+"""Mixed-precision path (fp16 hi/lo split products on tcgen05 tensor cores).
+
+Bar: d, b, t and the Fisher matrix within 1e-5 relative of lyspeq's own FP64
+results (Fisher elements normalised by sqrt(F_ii F_jj); d, b, t by the largest
+magnitude of the vector), and the same for the global sums and theta.
+"""
+import numpy as np
+import pytest
+
+import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 1e-5
+CASES = ["tiny_nomarg", "tiny_marg1", "tiny_masked", "small_cfg", "desi_sub"]
+
+
+def make_engine(c):
+    from lyspeq_gb300 import lqg
+    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg)
+    st = eng.add_chunk_list(c.chunks)
+    assert (st == 0).all(), st
+    return eng
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_matches_reference(engine_lib, name):
+    c = G.load(name)
+    eng = make_engine(c)
+    eng.iterate(precision="mixed")
+    out = eng.download()
+    assert (out["status"] == 0).all(), out["status"]
+    worst = 0.0
+    for i, (dbt, fis) in enumerate(zip(c.dbt, c.fisher)):
+        d, b, t, f = eng.chunk_result(i)
+        errs = (G.rel_err(d, dbt[0]), G.rel_err(b, dbt[1]), G.rel_err(t, dbt[2]), G.fisher_err(f, fis))
+        worst = max(worst, *errs)
+        assert max(errs) < MIXED_TOL, (i, errs)
+    if c.complete:
+        g = eng.fisher_solve(out["fisher"], np.stack([out["d"], out["b"], out["t"]]))
+        assert G.fisher_err(g["fisher"], c.g["fisher"]) < MIXED_TOL
+        pfid_free = np.abs(g["theta"] - c.g["theta"]) / np.max(np.abs(c.g["theta"]))
+        assert np.max(pfid_free) < 1e-4
+    eng.close()
+
+
+def test_mixed_matches_fp64_on_desi_like_chunks(engine_lib):
+    from lyspeq_gb300 import lqg, synth
+    w = synth.make_workload("desi", n_chunks=24)
+    eng = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length, cont=(1, -1))
+    chunks = [(s.wave, s.delta, 1.0 / s.sigma ** 2, s.r_fwhm) for s in w.spectra]
+    st = eng.add_chunk_list(chunks)
+    eng.iterate(precision="fp64")
+    ref = eng.download()
+    per = [eng.chunk_result(i) for i in range(eng.size)]
+    eng.iterate(precision="mixed")
+    mix = eng.download()
+    assert (mix["status"] == ref["status"]).all()
+    for i in range(eng.size):
+        d, b, t, f = eng.chunk_result(i)
+        assert G.fisher_err(f, per[i][3]) < MIXED_TOL
+        assert G.rel_err(b, per[i][1]) < MIXED_TOL and G.rel_err(t, per[i][2]) < MIXED_TOL
+        assert G.rel_err(d, per[i][0]) < MIXED_TOL
+    assert G.fisher_err(mix["fisher"], ref["fisher"]) < MIXED_TOL
+    eng.close()
