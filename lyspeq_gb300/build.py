@@ -16,6 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblqg.so")
+# Self-checking variant (-DLQG_CHECKED): device index checks that count and skip
+# out-of-bounds accesses instead of performing them.
+CHECKED_BUILD = os.path.join(HERE, "_build_checked")
+CHECKED_LIB = os.path.join(HERE, "liblqg_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["lqg_api.cu", "lqg_fisher.cu", "k_fp64.cu", "k_accum.cu", "k_tc.cu"]
 
@@ -27,8 +31,8 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: str, nvcc: str, extra: list) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src: str, nvcc: str, extra: list, build_dir: str = BUILD) -> str:
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
         os.path.join(HERE, "..", "include", "lqg.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
@@ -41,22 +45,24 @@ def _compile(src: str, nvcc: str, extra: list) -> str:
     return obj
 
 
-def build(verbose: bool = False, extra: list | None = None) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, extra: list | None = None, checked: bool = False) -> str:
+    bdir, lib = (CHECKED_BUILD, CHECKED_LIB) if checked else (BUILD, LIB)
+    os.makedirs(bdir, exist_ok=True)
     nvcc = nvcc_path()
-    extra = extra or []
+    extra = list(extra or []) + (["-DLQG_CHECKED"] if checked else [])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, nvcc, extra), SOURCES))
+        objs = list(ex.map(lambda s: _compile(s, nvcc, extra, bdir), SOURCES))
     newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs]
+    if not os.path.exists(lib) or os.path.getmtime(lib) < newest:
+        cmd = [nvcc, *ARCH, "-shared", "-o", lib, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True, extra=sys.argv[1:])
+    args = [a for a in sys.argv[1:] if a != "--checked"]
+    build(verbose=True, extra=args, checked="--checked" in sys.argv[1:])

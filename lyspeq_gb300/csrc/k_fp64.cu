@@ -437,6 +437,10 @@ __global__ void __launch_bounds__(FT) k_factor(WaveArgs a) {
     const int c = blockIdx.x;
     const ChunkDesc &ch = chunk_of(a, c);
     if (a.status[c] != LQG_CHUNK_OK) return;
+    if (!LQG_IN_BOUNDS(a, ch.o_c + (int64_t) ch.ld * ch.ld * 8 <= a.ws_bytes &&
+                              ch.o_part + 40 * (int64_t) ch.ld * 8 <= a.ws_bytes &&
+                              ch.o_y + (int64_t) ch.ld * 8 <= a.ws_bytes, 7, c, ch.o_part))
+        return;
     const int ld = ch.ld, n = ch.n, n32 = (n + NB - 1) / NB * NB;
     double *A = ws_ptr<double>(a, ch.o_c);
     double *scratch = ws_ptr<double>(a, ch.o_part);   // >= 32 * ld + (kMaxContVecs + 2) * ld doubles
@@ -533,6 +537,7 @@ __global__ void k_build_q(WaveArgs a) {
             }
             size_t off = (size_t) (ch.slot_q + s) * ld * ld + (size_t) ii[u] * ld + jj[u];
             if (MIXED) {
+                if (!LQG_IN_BOUNDS(a, off < (size_t) a.total_slots_q * ld * ld, 5, c, off)) continue;
                 float xs = (float) (q * qs);
                 __half h = __float2half_rn(xs);
                 a.q_hi[off] = h;
@@ -565,6 +570,11 @@ __global__ void k_prep_mixed(WaveArgs a) {
         float x = (float) (cv * cs);
         __half h = __float2half_rn(x);
         size_t coff = (size_t) c * ld * ld + idx;
+        if (!LQG_IN_BOUNDS(a, coff < (size_t) a.n_chunks * ld * ld &&
+                                  (size_t) (ch.slot_q + ch.ns) * ld * ld + idx < (size_t) a.total_slots_q * ld * ld &&
+                                  (size_t) (ch.slot_p + ch.ns + 1) * ld * ld + idx < (size_t) a.total_slots_p * ld * ld,
+                           6, c, coff))
+            continue;
         a.c_hi[coff] = h;
         a.c_lo[coff] = __float2half_rn(x - __half2float(h));
         float xs = (float) (S[idx] * ss);
@@ -710,8 +720,10 @@ __global__ void k_finish(WaveArgs a, int mixed) {
     const int c = blockIdx.x;
     const ChunkDesc &ch = chunk_of(a, c);
     const DeviceBins &bins = *a.bins;
-    double *res = a.results + ch.res_off;
     const int nq = ch.nq;
+    if (!LQG_IN_BOUNDS(a, ch.res_off + 3 * nq + (int64_t) nq * nq <= a.results_elems, 8, c, ch.res_off)) return;
+    if (mixed && !LQG_IN_BOUNDS(a, (int64_t) (c + 1) * a.gram_splits * GR * GR <= a.gram_elems, 9, c, c)) return;
+    double *res = a.results + ch.res_off;
     double *d = res, *b = res + nq, *t = res + 2 * nq, *F = res + 3 * nq;
     for (int e = threadIdx.x; e < 3 * nq + nq * nq; e += blockDim.x) res[e] = 0.0;
     __syncthreads();

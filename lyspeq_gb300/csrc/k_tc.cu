@@ -120,13 +120,18 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
                  : "memory");
 }
 
+// The .sync.aligned tcgen05 instructions below must be executed by all 32
+// lanes of a converged warp; callers reach them after divergent waits and
+// branches, so each helper re-converges the warp first.
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
                  "r"(ncols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
 }
 
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
 }
 
@@ -136,6 +141,7 @@ __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::aft
 // 32 consecutive fp32 columns of this warp's 32 lanes.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     uint32_t r[32];
+    __syncwarp();
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
         "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
@@ -215,7 +221,10 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         // TMA producer
         const int qslot = ch.slot_q + s;
         int issued = 0;
-        for (int kb = 0; kb < kblocks; ++kb) {
+        if (!LQG_IN_BOUNDS(a, c < a.n_chunks && qslot >= 0 && qslot < a.total_slots_q && m0 < ld && n0 < ld,
+                           1, c, qslot))
+            *abort_flag = 1;
+        for (int kb = 0; kb < kblocks && !*abort_flag; ++kb) {
             const int st = kb % G_STAGES;
             if (!mbar_wait(&empty[st], ((kb / G_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
             unsigned char *sb = smem + st * G_STAGE_BYTES;
@@ -252,9 +261,10 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         umma_commit(accum);
     } else if (warp >= 2) {
         // epilogue: TMEM -> scaled fp16 hi/lo planes, row-major (R) and transposed (P)
-        const bool got = mbar_wait(accum, 0);
+        // warp-uniform outcome, so that the aligned TMEM loads run in whole warps
+        const bool got = __all_sync(0xffffffffu, mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
-        if (got && !*abort_flag) {
+        if (got) {
             const int sub = warp % 4;
             const int row = m0 + sub * 32 + lane;
             const int nq4 = 4 * a.n_chunks;
@@ -266,7 +276,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
             __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
             const bool write_r = s < ch.ns;
-            for (int jc = 0; jc < G_BN / 32; ++jc) {
+            const bool slots_ok = LQG_IN_BOUNDS(a, (!write_r || ch.slot_r + s < a.total_slots_r) &&
+                                                     ch.slot_p + s < a.total_slots_p, 2, c, s);
+            for (int jc = 0; jc < G_BN / 32 && slots_ok; ++jc) {
                 const int col0 = n0 + jc * 32;
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t) (sub * 32) << 16) + jc * 32, v);
@@ -342,7 +354,10 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 
     if (warp == 0 && lane == 0) {
         int issued = 0;
-        for (int kb = 0; kb < kblocks; ++kb) {
+        if (!LQG_IN_BOUNDS(a, ch.slot_p >= 0 && ch.slot_p < a.total_slots_p && ch.slot_r >= 0 &&
+                                  ch.slot_r < a.total_slots_r && k_hi <= K, 3, c, ch.slot_p))
+            *abort_flag = 1;
+        for (int kb = 0; kb < kblocks && !*abort_flag; ++kb) {
             const int st = kb % R_STAGES;
             if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
             unsigned char *sb = smem + st * R_STAGE_BYTES;
@@ -376,13 +391,16 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         }
         umma_commit(accum);
     } else if (warp >= 2) {
-        const bool got = mbar_wait(accum, 0);
+        // warp-uniform outcome, so that the aligned TMEM loads run in whole warps
+        const bool got = __all_sync(0xffffffffu, mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
-        if (got && !*abort_flag) {
+        if (got) {
             const int sub = warp % 4;
             const int row = sub * 32 + lane;
-            float *out = a.gram_part + ((size_t) c * a.gram_splits + sp) * R_BM * R_BN + (size_t) row * R_BN;
-            for (int jc = 0; jc < R_BN / 32; ++jc) {
+            const size_t obase = ((size_t) c * a.gram_splits + sp) * R_BM * R_BN + (size_t) row * R_BN;
+            float *out = a.gram_part + obase;
+            const bool out_ok = LQG_IN_BOUNDS(a, (int64_t) (obase + R_BN) <= a.gram_elems, 4, c, obase);
+            for (int jc = 0; jc < R_BN / 32 && out_ok; ++jc) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t) (sub * 32) << 16) + jc * 32, v);
                 if (kblocks == 0)

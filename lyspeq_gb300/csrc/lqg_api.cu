@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -37,7 +38,7 @@ struct lqg_ctx {
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
-    DevBuf d_ws, d_desc, d_jobs, d_scales, d_halves, d_gram, d_wstat;
+    DevBuf d_ws, d_desc, d_jobs, d_scales, d_halves, d_gram, d_wstat, d_check;
     std::vector<int> last_status;
     double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int launches = 0;
@@ -461,27 +462,56 @@ int run_wave(lqg_ctx *ctx, const WavePlan &w, int precision, bool use_theta) {
         a.gram_part = ctx->d_gram.as<float>();
     }
     a.mid_event = ctx->ev[4];
+    a.ws_bytes = fp64_bytes;
+    a.results_elems = ctx->results_size;
+    a.gram_elems = precision == LQG_PRECISION_MIXED ? (int64_t) nch * splits * 128 * 128 : 0;
+    if (ctx->d_check.alloc(4 * sizeof(unsigned long long))) return set_err(ctx, LQG_ERR_NOMEM, "check");
+    LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_check.p, 0, 4 * sizeof(unsigned long long), st));
+    a.check = ctx->d_check.as<unsigned long long>();
+    // LQG_SYNC_EACH=1: synchronise after every kernel and name the one that failed
+    static const bool sync_each = getenv("LQG_SYNC_EACH") && getenv("LQG_SYNC_EACH")[0] == '1';
+    auto step = [&](const char *what) -> int {
+        if (!sync_each) return LQG_OK;
+        cudaError_t se = cudaStreamSynchronize(st);
+        if (se == cudaSuccess) se = cudaGetLastError();
+        if (se != cudaSuccess)
+            return set_err(ctx, LQG_ERR_CUDA, std::string(what) + " (ld " + std::to_string(ld) + ", " +
+                                                  std::to_string(nch) + " chunks): " + cudaGetErrorString(se));
+        return LQG_OK;
+    };
+    int rc = LQG_OK;
     cudaEventRecord(ctx->ev[0], st);
     launch_build_s_c(a, st);
+    if ((rc = step("build_s_c"))) return rc;
     cudaEventRecord(ctx->ev[1], st);
     launch_factor(a, st);
+    if ((rc = step("factor"))) return rc;
     cudaEventRecord(ctx->ev[2], st);
     if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(a, st);
     launch_build_q(a, st);
+    if ((rc = step("build_q"))) return rc;
     cudaEventRecord(ctx->ev[3], st);
     if (precision == LQG_PRECISION_MIXED)
         launch_products_mixed(a, st, ctx->d_jobs.as<int>(), (int) jobs.size() / 2);
     else
         launch_products_fp64(a, st, ctx->d_jobs.as<int>(), (int) jobs.size() / 2);
+    if ((rc = step("products"))) return rc;
     cudaEventRecord(ctx->ev[5], st);
     launch_finish(a, st);
+    if ((rc = step("finish"))) return rc;
     cudaEventRecord(ctx->ev[6], st);
+    unsigned long long chk[4] = {0, 0, 0, 0};
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(chk, ctx->d_check.p, sizeof chk, cudaMemcpyDeviceToHost, st));
     // scatter wave status into the batch status array
     std::vector<int> ws_host(nch);
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ws_host.data(), ctx->d_wstat.p, nch * 4, cudaMemcpyDeviceToHost, st));
     LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, std::string("wave kernels: ") + cudaGetErrorString(e));
+    if (chk[0] != 0)
+        return set_err(ctx, LQG_ERR_STATE, "index check failed " + std::to_string(chk[0]) + " times: code " +
+                                               std::to_string(chk[1]) + " chunk " + std::to_string(chk[2]) +
+                                               " index " + std::to_string(chk[3]) + " (ld " + std::to_string(ld) + ")");
     // [0] S/C build, [1] factorisation, [2] Q build, [3] C^-1 Q products, [4] Gram, [5] finish
     static const int from[6] = {0, 1, 2, 3, 4, 5}, to[6] = {1, 2, 3, 4, 5, 6};
     for (int k = 0; k < 6; ++k) {

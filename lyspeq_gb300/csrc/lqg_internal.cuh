@@ -92,7 +92,29 @@ struct WaveArgs {
     double *scales;              // per-slot scales (mixed): q [slots], r, p and c
     int launches;
     cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
+    // extents of the buffers above, used by the LQG_CHECKED build to validate indices
+    int64_t ws_bytes, results_elems, gram_elems;
+    unsigned long long *check;   // [0] violations, [1] first code, [2] first chunk, [3] first index
 };
+
+// Self-checking build (-DLQG_CHECKED): an index that would leave its buffer is
+// counted and the access skipped, so that a bad launch reports instead of faulting.
+#ifdef LQG_CHECKED
+__device__ __forceinline__ bool lqg_in_bounds(const WaveArgs &a, bool ok, int code, int chunk,
+                                              long long idx) {
+    if (!ok && a.check) {
+        if (atomicAdd(&a.check[0], 1ull) == 0ull) {
+            a.check[1] = (unsigned long long) code;
+            a.check[2] = (unsigned long long) chunk;
+            a.check[3] = (unsigned long long) idx;
+        }
+    }
+    return ok;
+}
+#define LQG_IN_BOUNDS(a, cond, code, chunk, idx) lqg_in_bounds((a), (cond), (code), (chunk), (long long) (idx))
+#else
+#define LQG_IN_BOUNDS(a, cond, code, chunk, idx) true
+#endif
 
 void launch_build_s_c(WaveArgs &a, cudaStream_t st);
 void launch_factor(WaveArgs &a, cudaStream_t st);

@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "liblqg.so")
+# LQG_LIB selects another build of the same ABI (e.g. liblqg_checked.so)
+LIB_PATH = os.environ.get("LQG_LIB", os.path.join(HERE, "liblqg.so"))
 
 LQG_OK = 0
 PRECISION = {"fp64": 0, "mixed": 1}
