@@ -1,0 +1,478 @@
+// FP64 factorisation of every chunk's covariance, one CTA per chunk, all
+// chunks of the batch in one launch (largest first):
+//   C~ = L L^T (blocked right-looking Cholesky),  X = L^-1 (blocked, row block
+//   by row block),  C~^-1 = X^T X,  C^-1 = D C~^-1 D  (D = diag(sqrt(ivar))),
+// then the continuum marginalisation (Chunk::_addMarginalizations,
+// core/chunk_estimate.cpp:576-665) and y = C^-1 delta (:747-750).
+// The reference inverts N^-1 C + I by LU instead (mathtools/matrix_helper.cpp:184-204);
+// both give the same C^-1 (see k_fp64.cu).
+//
+// Every O(n^3) step is a sequence of 64 x 64 x 64 tile products staged in
+// shared memory (two K-major tiles), 256 threads with a 4 x 4 register block
+// each; rows {ti + 16u}, columns {tj + 16w} per thread keep shared-memory
+// reads conflict-free.
+#include "lqg_internal.cuh"
+
+namespace lqg {
+
+namespace {
+
+constexpr int FB = 64;             // tile edge
+constexpr int FP = FB + 1;         // padded row of a shared tile
+constexpr int FTH = 256;           // threads per CTA
+
+__device__ __forceinline__ double block_sum_all(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+    for (int i = 0; i < FTH / 32; ++i) s += red[i];
+    __syncthreads();
+    return s;
+}
+
+__device__ __forceinline__ double block_max_all(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+    for (int i = 0; i < FTH / 32; ++i) s = fmax(s, red[i]);
+    __syncthreads();
+    return s;
+}
+
+// Shared tile loaders.  K-major layout: t[k * FP + m].
+// direct: t[k][m] = G[(r0 + k) * ld + c0 + m]  (rows of G are k)
+__device__ __forceinline__ void load_direct(double *t, const double *G, int ld, int r0, int c0) {
+    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+        int k = e / FB, m = e % FB;
+        t[k * FP + m] = G[(size_t) (r0 + k) * ld + c0 + m];
+    }
+}
+// transposed: t[k][m] = G[(r0 + m) * ld + c0 + k]  (rows of G are m)
+__device__ __forceinline__ void load_trans(double *t, const double *G, int ld, int r0, int c0) {
+    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+        int m = e / FB, k = e % FB;
+        t[k * FP + m] = G[(size_t) (r0 + m) * ld + c0 + k];
+    }
+}
+
+// acc[u][w] += sum_k A[k][ti + 16u] * B[k][tj + 16w]
+__device__ __forceinline__ void tile_mma(double (&acc)[4][4], const double *A, const double *B, int klen) {
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+#pragma unroll 4
+    for (int k = 0; k < klen; ++k) {
+        double a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { a[u] = A[k * FP + ti + 16 * u]; b[u] = B[k * FP + tj + 16 * u]; }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int w = 0; w < 4; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
+    }
+}
+
+__device__ __forceinline__ void zero_acc(double (&acc)[4][4]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) acc[u][w] = 0.0;
+}
+
+// In-shared-memory Cholesky of a 64 x 64 block stored row-major in d[r * FP + c]
+// (lower triangle is used); returns false if a pivot is not positive.
+__device__ bool chol_block(double *d, int *flag) {
+    if (threadIdx.x == 0) *flag = 0;
+    __syncthreads();
+    for (int j = 0; j < FB; ++j) {
+        const double piv = d[j * FP + j];
+        if (threadIdx.x == 0 && (!(piv > 0.0) || !isfinite(piv))) *flag = 1;
+        const double ljj = sqrt(piv > 0.0 ? piv : 1.0);
+        __syncthreads();
+        // column j below the diagonal
+        for (int i = j + 1 + threadIdx.x; i < FB; i += FTH) d[i * FP + j] /= ljj;
+        __syncthreads();
+        if (threadIdx.x == 0) d[j * FP + j] = ljj;
+        // rank-1 update of the trailing lower triangle
+        const int m = FB - j - 1;
+        for (int e = threadIdx.x; e < m * m; e += FTH) {
+            int i = j + 1 + e / m, l = j + 1 + e % m;
+            if (l <= i) d[i * FP + l] -= d[i * FP + j] * d[l * FP + j];
+        }
+        __syncthreads();
+    }
+    return *flag == 0;
+}
+
+// Inverse of the lower-triangular 64 x 64 block d (row-major) into x (row-major,
+// zero above the diagonal).  Column c is solved by thread c.
+__device__ void tri_inv_block(const double *d, double *x) {
+    if (threadIdx.x < FB) {
+        const int c = threadIdx.x;
+        for (int r = 0; r < FB; ++r) {
+            double s = (r == c) ? 1.0 : 0.0;
+            if (r >= c) {
+                for (int l = c; l < r; ++l) s -= d[r * FP + l] * x[l * FP + c];
+                s /= d[r * FP + r];
+            } else {
+                s = 0.0;
+            }
+            x[r * FP + c] = s;
+        }
+    }
+    __syncthreads();
+}
+
+struct FactorSmem {
+    double a[FB * FP];
+    double b[FB * FP];
+    double red[FTH / 32];
+    int flag;
+};
+
+// Blocked Cholesky in place (lower triangle of A, ld x ld, first nb*64 rows).
+__device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
+    for (int kb = 0; kb < nb; ++kb) {
+        const int k0 = kb * FB;
+        // diagonal block
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            s.a[(e / FB) * FP + e % FB] = A[(size_t) (k0 + e / FB) * ld + k0 + e % FB];
+        __syncthreads();
+        if (!chol_block(s.a, &s.flag)) return false;
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            A[(size_t) (k0 + e / FB) * ld + k0 + e % FB] = s.a[(e / FB) * FP + e % FB];
+        // b = (L_kk^-1)^T in K-major form: b[k][j] = Linv[j][k]
+        tri_inv_block(s.a, s.b);           // s.b row-major inverse
+        // transpose in place into K-major (b[k * FP + j] = Linv[j][k])
+        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+            int r = e / FB, c = e % FB;
+            if (c < r) {
+                double t = s.b[r * FP + c];
+                s.b[r * FP + c] = s.b[c * FP + r];
+                s.b[c * FP + r] = t;
+            }
+        }
+        __syncthreads();
+        // panel: L_ik = A_ik L_kk^-T, tile by tile
+        for (int ib = kb + 1; ib < nb; ++ib) {
+            const int i0 = ib * FB;
+            load_trans(s.a, A, ld, i0, k0);     // a[k][m] = A[i0 + m][k0 + k]
+            __syncthreads();
+            double acc[4][4];
+            zero_acc(acc);
+            // acc[m][j] = sum_k A[m][k] Linv[j][k]  with b[k][j] = Linv[j][k]
+            tile_mma(acc, s.a, s.b, FB);
+            __syncthreads();
+            const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w)
+                    A[(size_t) (i0 + ti + 16 * u) * ld + k0 + tj + 16 * w] = acc[u][w];
+            __syncthreads();
+        }
+        // trailing update: A_ij -= L_ik L_jk^T for kb < jb <= ib
+        for (int ib = kb + 1; ib < nb; ++ib)
+            for (int jb = kb + 1; jb <= ib; ++jb) {
+                const int i0 = ib * FB, j0 = jb * FB;
+                load_trans(s.a, A, ld, i0, k0);
+                load_trans(s.b, A, ld, j0, k0);
+                __syncthreads();
+                double acc[4][4];
+                zero_acc(acc);
+                tile_mma(acc, s.a, s.b, FB);
+                const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w)
+                        A[(size_t) (i0 + ti + 16 * u) * ld + j0 + tj + 16 * w] -= acc[u][w];
+                __syncthreads();
+            }
+    }
+    return true;
+}
+
+// In-place X = L^-1 (lower), row block by row block:
+//   X_II = L_II^-1;  X_IC = -X_II sum_{J=C}^{I-1} L_IJ X_JC   for C < I.
+// T = sum_J L_IJ X_JC is accumulated per column block into scratch (64 x ld).
+__device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &s) {
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    for (int ib = 0; ib < nb; ++ib) {
+        const int i0 = ib * FB;
+        // T[:, C] for every C < I (reads L_I* and already inverted X rows above)
+        for (int cb = 0; cb < ib; ++cb) {
+            double acc[4][4];
+            zero_acc(acc);
+            for (int jb = cb; jb < ib; ++jb) {
+                load_trans(s.a, A, ld, i0, jb * FB);       // a[k][m] = L[i0+m][j0+k]
+                load_direct(s.b, A, ld, jb * FB, cb * FB);  // b[k][c] = X[j0+k][c0+c]
+                __syncthreads();
+                tile_mma(acc, s.a, s.b, FB);
+                __syncthreads();
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w) T[(size_t) (ti + 16 * u) * ld + cb * FB + tj + 16 * w] = acc[u][w];
+        }
+        __syncthreads();
+        // X_II = L_II^-1 in s.b (row-major), then as K-major operand
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            s.a[(e / FB) * FP + e % FB] = A[(size_t) (i0 + e / FB) * ld + i0 + e % FB];
+        __syncthreads();
+        tri_inv_block(s.a, s.b);
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            A[(size_t) (i0 + e / FB) * ld + i0 + e % FB] = s.b[(e / FB) * FP + e % FB];
+        // a[k][m] = X_II[m][k]
+        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+            int m = e / FB, k = e % FB;
+            s.a[k * FP + m] = s.b[m * FP + k];
+        }
+        __syncthreads();
+        // X_IC = -X_II T_C
+        for (int cb = 0; cb < ib; ++cb) {
+            load_direct(s.b, T, ld, 0, cb * FB);           // b[k][c] = T[k][c0+c]
+            __syncthreads();
+            double acc[4][4];
+            zero_acc(acc);
+            tile_mma(acc, s.a, s.b, FB);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w)
+                    A[(size_t) (i0 + ti + 16 * u) * ld + cb * FB + tj + 16 * w] = -acc[u][w];
+            __syncthreads();
+        }
+    }
+}
+
+// In place: M = X^T X (lower tiles, row block by row block; within a row block the
+// off-diagonal tiles first), then C^-1 = D M D symmetric in the full ld x ld.
+__device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *ivar, FactorSmem &s) {
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    for (int ib = 0; ib < nb; ++ib) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const int jlo = pass == 0 ? 0 : ib, jhi = pass == 0 ? ib : ib + 1;
+            for (int jb = jlo; jb < jhi; ++jb) {
+                double acc[4][4];
+                zero_acc(acc);
+                for (int lb = ib; lb < nb; ++lb) {
+                    load_direct(s.a, A, ld, lb * FB, ib * FB);   // a[l][i] = X[l0+l][i0+i]
+                    load_direct(s.b, A, ld, lb * FB, jb * FB);   // b[l][j] = X[l0+l][j0+j]
+                    __syncthreads();
+                    // X is lower triangular: zero its upper part inside the diagonal tiles
+                    if (lb == ib)
+                        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+                            int l = e / FB, i = e % FB;
+                            if (l < i) s.a[l * FP + i] = 0.0;
+                        }
+                    if (lb == jb)
+                        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+                            int l = e / FB, j = e % FB;
+                            if (l < j) s.b[l * FP + j] = 0.0;
+                        }
+                    __syncthreads();
+                    tile_mma(acc, s.a, s.b, FB);
+                    __syncthreads();
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w)
+                        A[(size_t) (ib * FB + ti + 16 * u) * ld + jb * FB + tj + 16 * w] = acc[u][w];
+                __syncthreads();
+            }
+        }
+    }
+    for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
+        int i = (int) (e / ld), j = (int) (e % ld);
+        if (j > i) continue;
+        double v = 0.0;
+        if (i < n && j < n) v = sqrt(ivar[i]) * A[e] * sqrt(ivar[j]);
+        A[e] = v;
+        A[(size_t) j * ld + i] = v;
+    }
+    __syncthreads();
+}
+
+// x^m for integer m >= 1 by repeated multiplication
+__device__ __forceinline__ double ipow(double x, int m) {
+    double r = x;
+    for (int i = 1; i < m; ++i) r *= x;
+    return r;
+}
+
+// Continuum marginalisation: templates [1/sqrt(n), (ln w)^m, w^m] (each of unit
+// norm), their left singular vectors by one-sided Jacobi on the n x nv matrix,
+// vectors with s_i / s_0 <= 1e-15 dropped, then sequential rank-1 removal
+// C^-1 <- C^-1 - (C^-1 v)(C^-1 v)^T / (v^T C^-1 v).
+__device__ void marginalize_all(double *A, int ld, int n, const double *wave, int logl, int lord,
+                                double *V /* (2 kMaxContVecs + 1) * ld */, FactorSmem &s) {
+    double *y = V + kMaxContVecs * ld, *U = y + ld;
+    __shared__ double sv[kMaxContVecs], rot[2];
+    __shared__ int order[kMaxContVecs], nuse_s, changed;
+    int nv = 0;
+    for (int i = threadIdx.x; i < n; i += FTH) V[i] = 1.0 / sqrt((double) n);
+    nv = 1;
+    for (int kind = 0; kind < 2; ++kind) {
+        const int ordr = kind == 0 ? logl : lord;
+        for (int cmo = 1; cmo <= ordr && nv < kMaxContVecs; ++cmo) {
+            double part = 0;
+            for (int i = threadIdx.x; i < n; i += FTH) {
+                double x = ipow(kind == 0 ? log(wave[i]) : wave[i], cmo);
+                V[nv * ld + i] = x;
+                part += x * x;
+            }
+            const double inv = 1.0 / sqrt(block_sum_all(part, s.red));
+            for (int i = threadIdx.x; i < n; i += FTH) V[nv * ld + i] *= inv;
+            ++nv;
+            __syncthreads();
+        }
+    }
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        if (threadIdx.x == 0) changed = 0;
+        __syncthreads();
+        for (int p = 0; p < nv; ++p)
+            for (int q = p + 1; q < nv; ++q) {
+                double app = 0, aqq = 0, apq = 0;
+                for (int i = threadIdx.x; i < n; i += FTH) {
+                    double x = V[p * ld + i], z = V[q * ld + i];
+                    app += x * x; aqq += z * z; apq += x * z;
+                }
+                app = block_sum_all(app, s.red);
+                aqq = block_sum_all(aqq, s.red);
+                apq = block_sum_all(apq, s.red);
+                if (threadIdx.x == 0) {
+                    rot[0] = 1.0; rot[1] = 0.0;
+                    if (fabs(apq) > 1e-15 * sqrt(app * aqq)) {
+                        double zeta = (aqq - app) / (2.0 * apq);
+                        double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                        double cs = 1.0 / sqrt(1.0 + t * t);
+                        rot[0] = cs; rot[1] = cs * t;
+                        changed = 1;
+                    }
+                }
+                __syncthreads();
+                const double cs = rot[0], sn = rot[1];
+                if (sn != 0.0)
+                    for (int i = threadIdx.x; i < n; i += FTH) {
+                        double x = V[p * ld + i], z = V[q * ld + i];
+                        V[p * ld + i] = cs * x - sn * z;
+                        V[q * ld + i] = sn * x + cs * z;
+                    }
+                __syncthreads();
+            }
+        if (!changed) break;
+    }
+    for (int p = 0; p < nv; ++p) {
+        double part = 0;
+        for (int i = threadIdx.x; i < n; i += FTH) part += V[p * ld + i] * V[p * ld + i];
+        double ss = block_sum_all(part, s.red);
+        if (threadIdx.x == 0) sv[p] = sqrt(ss);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int p = 0; p < nv; ++p) order[p] = p;
+        for (int p = 0; p < nv; ++p)
+            for (int q = p + 1; q < nv; ++q)
+                if (sv[order[q]] > sv[order[p]]) { int t = order[p]; order[p] = order[q]; order[q] = t; }
+        int nuse = nv;
+        while (nuse > 0 && !(sv[order[nuse - 1]] / sv[order[0]] > kDoubleEpsilon)) --nuse;
+        nuse_s = nuse;
+    }
+    __syncthreads();
+    const int nuse = nuse_s;
+    for (int u = 0; u < nuse; ++u) {
+        const int p = order[u];
+        const double inv = 1.0 / sv[p];
+        for (int i = threadIdx.x; i < n; i += FTH) U[u * ld + i] = V[p * ld + i] * inv;
+    }
+    __syncthreads();
+    for (int u = 0; u < nuse; ++u) {
+        const double *vv = U + u * ld;
+        for (int i = threadIdx.x; i < n; i += FTH) {
+            double acc = 0;
+            const double *Ai = A + (size_t) i * ld;
+            for (int j = 0; j < n; ++j) acc += Ai[j] * vv[j];
+            y[i] = acc;
+        }
+        __syncthreads();
+        double part = 0;
+        for (int i = threadIdx.x; i < n; i += FTH) part += vv[i] * y[i];
+        const double cnorm = -1.0 / block_sum_all(part, s.red);
+        for (size_t e = threadIdx.x; e < (size_t) n * ld; e += FTH) {
+            int i = (int) (e / ld), j = (int) (e % ld);
+            if (j < n) A[e] += cnorm * y[i] * y[j];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(FTH) k_factor_tiled(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FactorSmem &s = *reinterpret_cast<FactorSmem *>(smem_raw);
+    const int c = blockIdx.x;
+    const ChunkDesc &ch = a.chunks[c];
+    if (a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    const int ld = ch.ld, n = ch.n, nb = (n + FB - 1) / FB;
+    if (!LQG_IN_BOUNDS(a, ch.o_c + (int64_t) ld * ld * 8 <= a.fws_bytes &&
+                              ch.o_fscr + (int64_t) FB * ld * 8 <= a.fws_bytes &&
+                              ch.o_y + (int64_t) ld * 8 <= a.fws_bytes && nb * FB <= ld, 10, c, ch.o_fscr))
+        return;
+    double *A = reinterpret_cast<double *>(a.fws + ch.o_c);
+    double *scratch = reinterpret_cast<double *>(a.fws + ch.o_fscr);
+    const double *iv = a.ivar + ch.pix;
+    if (!potrf_blocked(A, ld, nb, s)) {
+        if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_NOT_SPD;
+        return;
+    }
+    __syncthreads();
+    trtri_blocked(A, ld, nb, scratch, s);
+    __syncthreads();
+    lauum_blocked(A, ld, nb, n, iv, s);
+    if (a.cont_logl >= 0 || a.cont_l >= 0)
+        marginalize_all(A, ld, n, a.wave + ch.pix, a.cont_logl, a.cont_l, scratch, s);
+    double *y = reinterpret_cast<double *>(a.fws + ch.o_y);
+    const double *dl = a.delta + ch.pix;
+    for (int i = threadIdx.x; i < ld; i += FTH) {
+        double acc = 0;
+        if (i < n) {
+            const double *Ai = A + (size_t) i * ld;
+            for (int j = 0; j < n; ++j) acc += Ai[j] * dl[j];
+        }
+        y[i] = acc;
+    }
+    double mx = 0, rs = 0;
+    for (int i = threadIdx.x; i < n; i += FTH) {
+        const double *Ai = A + (size_t) i * ld;
+        double r = 0;
+        for (int j = 0; j < n; ++j) { double v = fabs(Ai[j]); r += v; mx = fmax(mx, v); }
+        rs = fmax(rs, r);
+    }
+    mx = block_max_all(mx, s.red);
+    rs = block_max_all(rs, s.red);
+    if (threadIdx.x == 0) {
+        a.fbounds[2 * ch.gidx] = mx;
+        a.fbounds[2 * ch.gidx + 1] = rs;
+    }
+}
+
+}  // namespace
+
+size_t factor_smem_bytes() { return sizeof(FactorSmem); }
+
+void launch_factor_all(WaveArgs &a, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_factor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int) sizeof(FactorSmem));
+        attr = true;
+    }
+    k_factor_tiled<<<a.n_chunks, FTH, sizeof(FactorSmem), st>>>(a);
+    a.launches++;
+}
+
+}  // namespace lqg

@@ -173,12 +173,15 @@ constexpr int R_BM = 128, R_BN = 128, R_STAGES = 3;
 constexpr int R_TILE = R_BM * BK * 2;
 constexpr int R_STAGE_BYTES = 4 * R_TILE;
 constexpr int R_SMEM = R_STAGES * R_STAGE_BYTES + 1024 + 256;
-constexpr int kGramK = 8192;                // K elements per Gram split
+constexpr int R_THREADS = 320;              // producer, MMA, 8 epilogue warps
+constexpr int kGramK = 32768;               // K elements per Gram split
+constexpr int kDrain = 4;                   // K blocks per drained hi*hi partial
 
-struct TcMaps {
-    CUtensorMap c_hi, c_lo, q_hi, q_lo;     // GEMM operands (3D: k, row, matrix)
-    CUtensorMap p_hi, p_lo, r_hi, r_lo;     // Gram operands (2D: k, slot)
-};
+// Accumulation: the tensor cores round every fp32 accumulation of an MMA, with a
+// bias that grows with the number of accumulations into one accumulator.  The
+// hi*hi products and the (2^11 times smaller) cross products therefore go to
+// separate TMEM accumulators, and the Gram drains its hi*hi accumulator every
+// kDrain K blocks into Kahan-compensated fp32 sums held in registers.
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(192, 1)
@@ -200,7 +203,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     const ChunkDesc &ch = a.chunks[c];
     const int ld = ch.ld;
     const int mt = (ld + G_BM - 1) / G_BM, nt = (ld + G_BN - 1) / G_BN;
-    if ((int) blockIdx.x >= mt * nt || a.status[c] != LQG_CHUNK_OK) return;
+    if ((int) blockIdx.x >= mt * nt || a.status[ch.gidx] != LQG_CHUNK_OK) return;
     const int m0 = (blockIdx.x % mt) * G_BM, n0 = (blockIdx.x / mt) * G_BN;
     const int kblocks = ld / BK;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -211,7 +214,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) tmem_alloc(tmem_slot, G_BN);
+    if (warp == 1) tmem_alloc(tmem_slot, 2 * G_BN);   // hi*hi in [0, 256), cross in [256, 512)
     fence_before();
     __syncthreads();
     fence_after();
@@ -241,10 +244,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         constexpr uint32_t idesc = idesc_f16(G_BM, G_BN);
-        bool ok = true;
-        for (int kb = 0; kb < kblocks && ok; ++kb) {
+        for (int kb = 0; kb < kblocks; ++kb) {
             const int st = kb % G_STAGES;
-            if (!mbar_wait(&full[st], (kb / G_STAGES) & 1)) { *abort_flag = 1; ok = false; break; }
+            if (!mbar_wait(&full[st], (kb / G_STAGES) & 1)) { *abort_flag = 1; break; }
             fence_after();
             unsigned char *sb = smem + st * G_STAGE_BYTES;
             const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + G_TILE_A);
@@ -252,9 +254,10 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
                 const uint64_t adv = (uint64_t) (kk * 32) >> 4;
-                umma_f16(tmem, ah + adv, bh + adv, idesc, (kb | kk) != 0);
-                umma_f16(tmem, ah + adv, bl + adv, idesc, 1);
-                umma_f16(tmem, al + adv, bh + adv, idesc, 1);
+                const uint32_t acc = (kb | kk) != 0;
+                umma_f16(tmem, ah + adv, bh + adv, idesc, acc);
+                umma_f16(tmem + G_BN, ah + adv, bl + adv, idesc, acc);
+                umma_f16(tmem + G_BN, al + adv, bh + adv, idesc, 1);
             }
             umma_commit(&empty[st]);
         }
@@ -280,15 +283,17 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
                                                      ch.slot_p + s < a.total_slots_p, 2, c, s);
             for (int jc = 0; jc < G_BN / 32 && slots_ok; ++jc) {
                 const int col0 = n0 + jc * 32;
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t) (sub * 32) << 16) + jc * 32, v);
+                float v[32], x[32];
+                const uint32_t lane_addr = (uint32_t) (sub * 32) << 16;
+                tmem_ld32(tmem + lane_addr + jc * 32, v);
+                tmem_ld32(tmem + lane_addr + G_BN + jc * 32, x);
                 if (col0 >= ld) continue;
                 __align__(16) __half hi[32], lo[32];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    float x = v[j] * mult;
-                    hi[j] = __float2half_rn(x);
-                    lo[j] = __float2half_rn(x - __half2float(hi[j]));
+                    const float val = (v[j] + x[j]) * mult;
+                    hi[j] = __float2half_rn(val);
+                    lo[j] = __float2half_rn(val - __half2float(hi[j]));
                 }
                 if (row < ld) {
                     if (write_r) {
@@ -313,13 +318,18 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     __syncthreads();
     if (warp == 1) {
         fence_after();
-        tmem_dealloc(tmem, G_BN);
+        tmem_dealloc(tmem, 2 * G_BN);
     }
-    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[c], LQG_CHUNK_TIMEOUT);
+    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[ch.gidx], LQG_CHUNK_TIMEOUT);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(192, 1)
+// Gram block (bi, bj) of one chunk over one K split.
+__global__ void __launch_bounds__(R_THREADS, 1)
 k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_constant__ CUtensorMap mp_lo,
           const __grid_constant__ CUtensorMap mr_hi, const __grid_constant__ CUtensorMap mr_lo) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -327,26 +337,33 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + R_STAGES * R_STAGE_BYTES);
     uint64_t *empty = full + R_STAGES;
-    uint64_t *accum = empty + R_STAGES;
+    uint64_t *dfull = empty + R_STAGES;      // [2] hi*hi buffer ready to drain
+    uint64_t *dempty = dfull + 2;            // [2] hi*hi buffer drained
+    uint64_t *accum = dempty + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
 
-    const int c = blockIdx.y, sp = blockIdx.x;
+    const int c = blockIdx.y, sp = blockIdx.x, blk = blockIdx.z;
     const ChunkDesc &ch = a.chunks[c];
-    if (a.status[c] != LQG_CHUNK_OK || sp >= a.gram_splits) return;
+    if (a.status[ch.gidx] != LQG_CHUNK_OK || sp >= a.gram_splits) return;
+    const int bi = blk / a.gt, bj = blk % a.gt;
+    if (bi * R_BM >= ch.ns + 2 || bj * R_BN >= ch.ns) return;
     const int64_t K = (int64_t) ch.ld * ch.ld;
     const int64_t kper = ((K + a.gram_splits - 1) / a.gram_splits + BK - 1) / BK * BK;
     const int64_t k_lo = sp * kper, k_hi = min(K, k_lo + kper);
     const int kblocks = k_hi > k_lo ? (int) ((k_hi - k_lo) / BK) : 0;
+    const int nchunk = (kblocks + kDrain - 1) / kDrain;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int prow = ch.slot_p + bi * R_BM, rrow = ch.slot_r + bj * R_BN;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < R_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+        for (int i = 0; i < 2; ++i) { mbar_init(&dfull[i], 1); mbar_init(&dempty[i], 8); }
         mbar_init(accum, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) tmem_alloc(tmem_slot, R_BN);
+    if (warp == 1) tmem_alloc(tmem_slot, 512);   // hi*hi ping [0,128), pong [128,256), cross [256,384)
     fence_before();
     __syncthreads();
     fence_after();
@@ -354,8 +371,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 
     if (warp == 0 && lane == 0) {
         int issued = 0;
-        if (!LQG_IN_BOUNDS(a, ch.slot_p >= 0 && ch.slot_p < a.total_slots_p && ch.slot_r >= 0 &&
-                                  ch.slot_r < a.total_slots_r && k_hi <= K, 3, c, ch.slot_p))
+        if (!LQG_IN_BOUNDS(a, prow >= 0 && prow < a.total_slots_p && rrow >= 0 && rrow < a.total_slots_r &&
+                                  k_hi <= K, 3, c, prow))
             *abort_flag = 1;
         for (int kb = 0; kb < kblocks && !*abort_flag; ++kb) {
             const int st = kb % R_STAGES;
@@ -363,52 +380,95 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             unsigned char *sb = smem + st * R_STAGE_BYTES;
             const int x = (int) (k_lo + (int64_t) kb * BK);
             mbar_expect_tx(&full[st], R_STAGE_BYTES);
-            tma_load_2d(sb, &mp_hi, &full[st], x, ch.slot_p);
-            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], x, ch.slot_p);
-            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], x, ch.slot_r);
-            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], x, ch.slot_r);
+            tma_load_2d(sb, &mp_hi, &full[st], x, prow);
+            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], x, prow);
+            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], x, rrow);
+            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], x, rrow);
             ++issued;
         }
         for (int kb = (issued > R_STAGES ? issued - R_STAGES : 0); kb < issued; ++kb)
             mbar_wait(&full[kb % R_STAGES], (kb / R_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
         constexpr uint32_t idesc = idesc_f16(R_BM, R_BN);
-        for (int kb = 0; kb < kblocks; ++kb) {
-            const int st = kb % R_STAGES;
-            if (!mbar_wait(&full[st], (kb / R_STAGES) & 1)) { *abort_flag = 1; break; }
+        bool ok = true;
+        for (int g = 0; g < nchunk && ok; ++g) {
+            const int b = g & 1;
+            if (g >= 2 && !mbar_wait(&dempty[b], ((g >> 1) - 1) & 1)) { *abort_flag = 1; ok = false; break; }
             fence_after();
-            unsigned char *sb = smem + st * R_STAGE_BYTES;
-            const uint64_t ph = sw128_desc(sb), pl = sw128_desc(sb + R_TILE);
-            const uint64_t rh = sw128_desc(sb + 2 * R_TILE), rl = sw128_desc(sb + 3 * R_TILE);
+            const uint32_t thh = tmem + b * R_BN, tx = tmem + 2 * R_BN;
+            const int kb_end = min(kblocks, (g + 1) * kDrain);
+            for (int kb = g * kDrain; kb < kb_end; ++kb) {
+                const int st = kb % R_STAGES;
+                if (!mbar_wait(&full[st], (kb / R_STAGES) & 1)) { *abort_flag = 1; ok = false; break; }
+                fence_after();
+                unsigned char *sb = smem + st * R_STAGE_BYTES;
+                const uint64_t ph = sw128_desc(sb), pl = sw128_desc(sb + R_TILE);
+                const uint64_t rh = sw128_desc(sb + 2 * R_TILE), rl = sw128_desc(sb + 3 * R_TILE);
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-                const uint64_t adv = (uint64_t) (kk * 32) >> 4;
-                umma_f16(tmem, ph + adv, rh + adv, idesc, (kb | kk) != 0);
-                umma_f16(tmem, ph + adv, rl + adv, idesc, 1);
-                umma_f16(tmem, pl + adv, rh + adv, idesc, 1);
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint64_t adv = (uint64_t) (kk * 32) >> 4;
+                    umma_f16(thh, ph + adv, rh + adv, idesc, (kb > g * kDrain || kk > 0));
+                    umma_f16(tx, ph + adv, rl + adv, idesc, (kb | kk) != 0);
+                    umma_f16(tx, pl + adv, rh + adv, idesc, 1);
+                }
+                umma_commit(&empty[st]);
             }
-            umma_commit(&empty[st]);
+            umma_commit(&dfull[b]);
         }
         umma_commit(accum);
     } else if (warp >= 2) {
-        // warp-uniform outcome, so that the aligned TMEM loads run in whole warps
-        const bool got = __all_sync(0xffffffffu, mbar_wait(accum, 0)) && !*abort_flag;
+        // 8 epilogue warps: lane quadrant warp % 4, columns 64 * ((warp - 2) / 4) + [0, 64)
+        const int quad = warp % 4, half = (warp - 2) / 4;
+        const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
+        float sum[64], comp[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) { sum[j] = 0.f; comp[j] = 0.f; }
+        bool alive = true;
+        for (int g = 0; g < nchunk; ++g) {
+            const int b = g & 1;
+            alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g >> 1) & 1)) && !*abort_flag;
+            if (!alive) break;
+            fence_after();
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float v[32];
+                tmem_ld32(tmem + lane_addr + b * R_BN + half * 64 + h * 32, v);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    // Kahan: sum + comp carries the drained partials without rounding loss
+                    const float yv = v[j] - comp[h * 32 + j];
+                    const float t = sum[h * 32 + j] + yv;
+                    comp[h * 32 + j] = (t - sum[h * 32 + j]) - yv;
+                    sum[h * 32 + j] = t;
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&dempty[b]);
+        }
+        const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
-            const int sub = warp % 4;
-            const int row = sub * 32 + lane;
-            const size_t obase = ((size_t) c * a.gram_splits + sp) * R_BM * R_BN + (size_t) row * R_BN;
-            float *out = a.gram_part + obase;
-            const bool out_ok = LQG_IN_BOUNDS(a, (int64_t) (obase + R_BN) <= a.gram_elems, 4, c, obase);
-            for (int jc = 0; jc < R_BN / 32 && out_ok; ++jc) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t) (sub * 32) << 16) + jc * 32, v);
-                if (kblocks == 0)
+            const int row = quad * 32 + lane;
+            const size_t obase = (((size_t) c * a.gt * a.gt + blk) * a.gram_splits + sp) * R_BM * R_BN +
+                                 (size_t) row * R_BN + half * 64;
+            const bool out_ok = LQG_IN_BOUNDS(a, (int64_t) (obase + 64) <= a.gram_elems, 4, c, obase);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) v[j] = 0.f;
-                float4 *o = reinterpret_cast<float4 *>(out + jc * 32);
+            for (int h = 0; h < 2; ++h) {
+                float x[32];
+                tmem_ld32(tmem + lane_addr + 2 * R_BN + half * 64 + h * 32, x);
+                if (!out_ok) continue;
+                float4 *o = reinterpret_cast<float4 *>(a.gram_part + obase + h * 32);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                for (int q = 0; q < 8; ++q) {
+                    float r4[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int j = h * 32 + 4 * q + e;
+                        r4[e] = kblocks == 0 ? 0.f : (sum[j] - comp[j]) + x[4 * q + e];
+                    }
+                    o[q] = make_float4(r4[0], r4[1], r4[2], r4[3]);
+                }
             }
         }
     }
@@ -416,17 +476,17 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     __syncthreads();
     if (warp == 1) {
         fence_after();
-        tmem_dealloc(tmem, R_BN);
+        tmem_dealloc(tmem, 512);
     }
-    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[c], LQG_CHUNK_TIMEOUT);
+    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[ch.gidx], LQG_CHUNK_TIMEOUT);
 }
 
 // Operand scales of the mixed path (powers of two), from the FP64 bounds the
-// factorisation left in scales[4c + 0..1]: max |C^-1| and the largest row sum.
+// factorisation left per chunk: max |C^-1| and the largest row sum of |C^-1|.
 __global__ void k_scales(WaveArgs a) {
     const int c = blockIdx.x;
     const ChunkDesc &ch = a.chunks[c];
-    if (a.status[c] != LQG_CHUNK_OK) return;
+    if (a.status[ch.gidx] != LQG_CHUNK_OK) return;
     __shared__ double red[32];
     double mx = 0;
     const double *iv = a.ivar + ch.pix;
@@ -438,8 +498,10 @@ __global__ void k_scales(WaveArgs a) {
     if (threadIdx.x != 0) return;
     for (int i = 1; i < (int) blockDim.x / 32; ++i) mx = fmax(mx, red[i]);
     double *sc = a.scales + 4 * c;
-    const double maxc = sc[0], rowsum = sc[1];
+    const double maxc = a.fbounds[2 * ch.gidx], rowsum = a.fbounds[2 * ch.gidx + 1];
     const double target = 16384.0;
+    sc[0] = maxc;
+    sc[1] = rowsum;
     sc[2] = pow2_floor(target / maxc);
     sc[3] = pow2_floor(target / (maxc * mx));
     const int nq4 = 4 * a.n_chunks;
@@ -455,8 +517,8 @@ __global__ void k_scales(WaveArgs a) {
     psc[ch.ns + 1] = sc[3];
 }
 
-// cuTensorMapEncodeTiled is resolved through the runtime so that the library
-// does not link libcuda (it then also loads on machines without a driver).
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so that the
+// library links without libcuda.
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -472,7 +534,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 CUtensorMap make_map(void *base, int rank, const cuuint64_t *dims, const cuuint64_t *strides,
                      const cuuint32_t *box, bool *ok) {
-    CUtensorMap m;
+    CUtensorMap m{};
     cuuint32_t es[3] = {1, 1, 1};
     auto enc = encode_fn();
     if (!enc) { *ok = false; return m; }
@@ -525,7 +587,7 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     const int tiles = ((ld + G_BM - 1) / G_BM) * ((ld + G_BN - 1) / G_BN);
     k_tc_gemm<<<dim3(tiles, njobs), 192, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
     if (a.mid_event) cudaEventRecord(a.mid_event, st);
-    k_tc_gram<<<dim3(a.gram_splits, a.n_chunks), 192, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
+    k_tc_gram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), R_THREADS, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
     a.launches += 2;
 }
 

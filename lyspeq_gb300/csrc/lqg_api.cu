@@ -38,11 +38,13 @@ struct lqg_ctx {
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
-    DevBuf d_ws, d_desc, d_jobs, d_scales, d_halves, d_gram, d_wstat, d_check;
+    DevBuf d_fws, d_ws, d_fbounds, d_desc, d_jobs, d_scales, d_halves, d_gram, d_check;
+    void *h_stage = nullptr;   // pinned staging of the per-iteration descriptors
+    size_t h_stage_bytes = 0;
     std::vector<int> last_status;
     double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int launches = 0;
-    cudaEvent_t ev[8] = {};
+    std::vector<cudaEvent_t> evpool;
 };
 
 namespace {
@@ -104,7 +106,6 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     if (cudaSetDevice(device) != cudaSuccess) return LQG_ERR_CUDA;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         return LQG_ERR_CUDA;
-    for (auto &e : ctx->ev) cudaEventCreate(&e);
     ctx->nk = bins->nk;
     ctx->nz = bins->nz;
     ctx->nkz = bins->nk * bins->nz;
@@ -176,8 +177,8 @@ extern "C" int lqg_ctx_destroy(lqg_ctx *ctx) {
     if (!ctx) return LQG_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (auto &e : ctx->ev)
-        if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->evpool) cudaEventDestroy(e);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return LQG_OK;
@@ -260,7 +261,7 @@ extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
                 hc.res = res;
                 hc.zlow = zl;
                 hc.zupp = zu;
-                if (st == LQG_CHUNK_OK && hc.ns + 2 > 128)
+                if (st == LQG_CHUNK_OK && hc.ns + 2 > 128 * kMaxGramBlocks)
                     st = LQG_CHUNK_TOO_LARGE;
             }
         }
@@ -299,11 +300,6 @@ void launch_accumulate(const ChunkDesc *chunks, int n_chunks, const double *resu
 
 namespace {
 
-struct WavePlan {
-    std::vector<int> members;   // batch chunk indices
-    int ld = 0;
-};
-
 int upload_pixels(lqg_ctx *ctx) {
     if (!ctx->pix_dirty) return LQG_OK;
     size_t np = ctx->h_wave.size();
@@ -337,21 +333,6 @@ int upload_pixels(lqg_ctx *ctx) {
     return LQG_OK;
 }
 
-// Bytes of wave workspace one chunk needs (see the offsets set in run_wave).
-int64_t chunk_ws_bytes(const lqg_ctx::HostChunk &h, int precision, int splits) {
-    int64_t ld = h.ld, m = ld * ld * 8;
-    int64_t tiles = (ld / 64) * (ld / 64);
-    int64_t part = std::max<int64_t>((int64_t) splits * 128 * 128 * 8, 40 * ld * 8);
-    int64_t base = align_up(m, 256) * 2 + align_up(ld * 8, 256) + align_up(tiles * h.ns * 8, 256) +
-                   align_up(part, 256);
-    if (precision == LQG_PRECISION_FP64)
-        base += align_up(m * h.ns, 256) * 2 + align_up(m * (h.ns + 2), 256);
-    else
-        // halves: C (2 planes), Q (ns+1 slots), R (ns), P (ns+2), each 2 planes of ld^2 halves
-        base += (int64_t) ld * ld * 2 * 2 * (1 + (h.ns + 1) + h.ns + (h.ns + 2)) + (int64_t) splits * 128 * 128 * 4;
-    return base;
-}
-
 int gram_splits_for(int ld, int precision) {
     if (precision == LQG_PRECISION_MIXED) return gram_splits_mixed(ld);
     int64_t K = (int64_t) ld * ld;
@@ -359,168 +340,180 @@ int gram_splits_for(int ld, int precision) {
     return (int) std::max<int64_t>(1, std::min<int64_t>(s, 256));
 }
 
-int run_wave(lqg_ctx *ctx, const WavePlan &w, int precision, bool use_theta) {
-    cudaStream_t st = ctx->stream;
-    const int nch = (int) w.members.size();
-    const int ld = w.ld;
-    const int splits = gram_splits_for(ld, precision);
-    std::vector<ChunkDesc> desc(nch);
-    int64_t off = 0;
-    int slot_q = 0, slot_r = 0, slot_p = 0;
-    const int64_t m = (int64_t) ld * ld * 8;
-    const int64_t tiles = (ld / 64) * (ld / 64);
-    for (int i = 0; i < nch; ++i) {
-        const auto &h = ctx->chunks[w.members[i]];
-        ChunkDesc &d = desc[i];
-        d.n = h.n; d.ld = ld; d.nq = h.nq; d.ns = h.ns; d.kbin_upp = h.kbin_upp; d.fis = h.fis;
-        d.res = h.res; d.zb0 = h.fis / ctx->nk; d.pix = h.pix; d.res_off = h.res_off;
-        d.n_tiles = (int) tiles;
-        d.o_s = off; off += align_up(m, 256);
-        d.o_c = off; off += align_up(m, 256);
-        d.o_y = off; off += align_up((int64_t) ld * 8, 256);
-        d.o_dpart = off; off += align_up(tiles * h.ns * 8, 256);
-        d.o_part = off; off += align_up(std::max<int64_t>((int64_t) splits * 128 * 128 * 8, 40 * (int64_t) ld * 8), 256);
-        if (precision == LQG_PRECISION_FP64) {
-            d.o_q = off; off += align_up(m * h.ns, 256);
-            d.o_r = off; off += align_up(m * h.ns, 256);
-            d.o_p = off; off += align_up(m * (h.ns + 2), 256);
-        }
-        d.slot_q = slot_q; slot_q += h.ns + 1;
-        d.slot_r = slot_r; slot_r += h.ns;
-        d.slot_p = slot_p; slot_p += h.ns + 2;
-    }
-    const int64_t fp64_bytes = off;
-    int64_t half_bytes = 0;
-    const int64_t plane = (int64_t) ld * ld * 2;
-    if (precision == LQG_PRECISION_MIXED)
-        half_bytes = plane * 2 * ((int64_t) nch + slot_q + slot_r + slot_p);
-    if (ctx->d_ws.alloc(std::max<int64_t>(fp64_bytes, 256)))
-        return set_err(ctx, LQG_ERR_NOMEM, "workspace");
-    if (precision == LQG_PRECISION_MIXED) {
-        if (ctx->d_halves.alloc(half_bytes + 1024) ||
-            ctx->d_gram.alloc((int64_t) nch * splits * 128 * 128 * 4))
-            return set_err(ctx, LQG_ERR_NOMEM, "mixed workspace");
-    }
-    int nscales = 4 * nch + slot_q + slot_p + slot_r;
-    std::vector<double> scales(nscales, 1.0);
-    if (precision == LQG_PRECISION_MIXED) {
-        for (int i = 0; i < nch; ++i) {
-            const auto &h = ctx->chunks[w.members[i]];
-            for (int s = 0; s < h.ns; ++s)
-                scales[4 * nch + desc[i].slot_q + s] =
-                    pow2_scale(ctx->qmax[(size_t) h.res * ctx->nk + s % h.kbin_upp], 16384.0);
-            scales[4 * nch + desc[i].slot_q + h.ns] = pow2_scale(ctx->smax[h.res], 16384.0);
-        }
-    }
-    if (ctx->d_desc.alloc(nch * sizeof(ChunkDesc)) || ctx->d_scales.alloc(nscales * 8))
-        return set_err(ctx, LQG_ERR_NOMEM, "descriptors");
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_desc.p, desc.data(), nch * sizeof(ChunkDesc), cudaMemcpyHostToDevice, st));
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_scales.p, scales.data(), nscales * 8, cudaMemcpyHostToDevice, st));
-    // jobs: (chunk, s) for s in [0, ns]
-    std::vector<int> jobs;
-    for (int i = 0; i < nch; ++i)
-        for (int s = 0; s <= desc[i].ns; ++s) { jobs.push_back(i); jobs.push_back(s); }
-    if (ctx->d_jobs.alloc(jobs.size() * 4)) return set_err(ctx, LQG_ERR_NOMEM, "jobs");
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_jobs.p, jobs.data(), jobs.size() * 4, cudaMemcpyHostToDevice, st));
-    // wave-local status: starts OK
-    if (ctx->d_wstat.alloc(nch * 4)) return set_err(ctx, LQG_ERR_NOMEM, "status");
-    LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_wstat.p, 0, nch * 4, st));
+int gram_blocks(int ns) { return (ns + 2 + 127) / 128; }
 
-    WaveArgs a{};
-    a.chunks = ctx->d_desc.as<ChunkDesc>();
-    a.n_chunks = nch;
-    a.max_ld = ld;
-    a.ws = ctx->d_ws.as<char>();
-    a.wave = ctx->d_wave.as<double>(); a.delta = ctx->d_delta.as<double>(); a.ivar = ctx->d_ivar.as<double>();
-    a.logw = ctx->d_logw.as<double>(); a.sqw = ctx->d_sqw.as<double>();
-    a.deriv = ctx->d_deriv.as<double>();
-    a.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
-    a.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
-    a.results = ctx->d_results.as<double>();
-    a.status = ctx->d_wstat.as<int>();
-    a.grid = ctx->grid;
-    a.bins = ctx->d_bins.as<DeviceBins>();
-    a.cont_logl = ctx->opts.cont_logl_order;
-    a.cont_l = ctx->opts.cont_l_order;
-    a.turn_off_sfid = ctx->opts.turn_off_sfid;
-    a.skip_fisher = ctx->opts.skip_fisher;
-    a.precision = precision;
-    a.total_slots_q = slot_q; a.total_slots_r = slot_r; a.total_slots_p = slot_p;
-    a.gram_splits = splits;
-    a.scales = ctx->d_scales.as<double>();
-    if (precision == LQG_PRECISION_MIXED) {
-        __half *hb = ctx->d_halves.as<__half>();
-        int64_t pl = (int64_t) ld * ld;
-        a.c_hi = hb; hb += pl * nch;
-        a.c_lo = hb; hb += pl * nch;
-        a.q_hi = hb; hb += pl * slot_q;
-        a.q_lo = hb; hb += pl * slot_q;
-        a.r_hi = hb; hb += pl * slot_r;
-        a.r_lo = hb; hb += pl * slot_r;
-        a.p_hi = hb; hb += pl * slot_p;
-        a.p_lo = hb; hb += pl * slot_p;
-        a.gram_part = ctx->d_gram.as<float>();
-    }
-    a.mid_event = ctx->ev[4];
-    a.ws_bytes = fp64_bytes;
-    a.results_elems = ctx->results_size;
-    a.gram_elems = precision == LQG_PRECISION_MIXED ? (int64_t) nch * splits * 128 * 128 : 0;
-    if (ctx->d_check.alloc(4 * sizeof(unsigned long long))) return set_err(ctx, LQG_ERR_NOMEM, "check");
-    LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_check.p, 0, 4 * sizeof(unsigned long long), st));
-    a.check = ctx->d_check.as<unsigned long long>();
-    // LQG_SYNC_EACH=1: synchronise after every kernel and name the one that failed
-    static const bool sync_each = getenv("LQG_SYNC_EACH") && getenv("LQG_SYNC_EACH")[0] == '1';
-    auto step = [&](const char *what) -> int {
-        if (!sync_each) return LQG_OK;
-        cudaError_t se = cudaStreamSynchronize(st);
-        if (se == cudaSuccess) se = cudaGetLastError();
-        if (se != cudaSuccess)
-            return set_err(ctx, LQG_ERR_CUDA, std::string(what) + " (ld " + std::to_string(ld) + ", " +
-                                                  std::to_string(nch) + " chunks): " + cudaGetErrorString(se));
-        return LQG_OK;
-    };
-    int rc = LQG_OK;
-    cudaEventRecord(ctx->ev[0], st);
-    launch_build_s_c(a, st);
-    if ((rc = step("build_s_c"))) return rc;
-    cudaEventRecord(ctx->ev[1], st);
-    launch_factor(a, st);
-    if ((rc = step("factor"))) return rc;
-    cudaEventRecord(ctx->ev[2], st);
-    if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(a, st);
-    launch_build_q(a, st);
-    if ((rc = step("build_q"))) return rc;
-    cudaEventRecord(ctx->ev[3], st);
-    if (precision == LQG_PRECISION_MIXED)
-        launch_products_mixed(a, st, ctx->d_jobs.as<int>(), (int) jobs.size() / 2);
+// Factor workspace of one chunk: S_fid, C~ (becomes C^-1), y and 64 ld of scratch.
+int64_t chunk_fws_bytes(int64_t ld) {
+    return align_up(ld * ld * 8, 256) * 2 + align_up(ld * 8, 256) + align_up(64 * ld * 8, 256);
+}
+
+// Wave workspace of one chunk in a wave with the given Gram blocking.
+int64_t chunk_ws_bytes(int64_t ld, int ns, int precision, int splits, int gt) {
+    const int64_t m = ld * ld * 8, tiles = (ld / 64) * (ld / 64);
+    int64_t b = align_up(tiles * 8 * ns * 8, 256);
+    const int64_t gblk = (int64_t) gt * gt * splits * 128 * 128;
+    if (precision == LQG_PRECISION_FP64)
+        b += align_up(gblk * 8, 256) + align_up(m * ns, 256) * 2 + align_up(m * (ns + 2), 256);
     else
-        launch_products_fp64(a, st, ctx->d_jobs.as<int>(), (int) jobs.size() / 2);
-    if ((rc = step("products"))) return rc;
-    cudaEventRecord(ctx->ev[5], st);
-    launch_finish(a, st);
-    if ((rc = step("finish"))) return rc;
-    cudaEventRecord(ctx->ev[6], st);
-    unsigned long long chk[4] = {0, 0, 0, 0};
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(chk, ctx->d_check.p, sizeof chk, cudaMemcpyDeviceToHost, st));
-    // scatter wave status into the batch status array
-    std::vector<int> ws_host(nch);
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ws_host.data(), ctx->d_wstat.p, nch * 4, cudaMemcpyDeviceToHost, st));
-    LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, std::string("wave kernels: ") + cudaGetErrorString(e));
-    if (chk[0] != 0)
-        return set_err(ctx, LQG_ERR_STATE, "index check failed " + std::to_string(chk[0]) + " times: code " +
-                                               std::to_string(chk[1]) + " chunk " + std::to_string(chk[2]) +
-                                               " index " + std::to_string(chk[3]) + " (ld " + std::to_string(ld) + ")");
-    // [0] S/C build, [1] factorisation, [2] Q build, [3] C^-1 Q products, [4] Gram, [5] finish
-    static const int from[6] = {0, 1, 2, 3, 4, 5}, to[6] = {1, 2, 3, 4, 5, 6};
-    for (int k = 0; k < 6; ++k) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev[from[k]], ctx->ev[to[k]]);
-        ctx->timings[k] += ms;
+        // fp16 hi/lo planes of C^-1, Q (ns + 1 slots), R (ns) and P (ns + 2), and fp32 Gram partials
+        b += ld * ld * 2 * 2 * (int64_t) (1 + (ns + 1) + ns + (ns + 2)) + gblk * 4;
+    return b;
+}
+
+struct WavePlan {
+    std::vector<int> members;   // batch chunk indices
+    int ld = 0, gt = 1, splits = 1;
+    int slot_q = 0, slot_r = 0, slot_p = 0;
+    int64_t ws_bytes = 0, half_bytes = 0;
+    size_t desc_off = 0, jobs_off = 0, scales_off = 0;
+    int njobs = 0, nscales = 0;
+};
+
+struct GroupPlan {
+    std::vector<int> members;   // batch chunk indices, largest first
+    int max_ld = 0;
+    int64_t fws_bytes = 0;
+    size_t desc_off = 0;
+    std::vector<WavePlan> waves;
+};
+
+cudaEvent_t pool_event(lqg_ctx *ctx, size_t i) {
+    while (ctx->evpool.size() <= i) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ctx->evpool.push_back(e);
     }
-    for (int i = 0; i < nch; ++i) ctx->last_status[w.members[i]] = ws_host[i];
-    ctx->launches += a.launches;
+    return ctx->evpool[i];
+}
+
+// Plans the iteration: groups of chunks whose factor workspaces fit together
+// (phase A: S, C~ and the factorisation of every chunk of the group), each
+// split into waves of equal padded size (phase B: Q_s, products, traces).
+// Descriptors, jobs and host-known scales of every launch are packed into
+// single arrays, uploaded once.
+int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, std::vector<ChunkDesc> &desc,
+                   std::vector<int> &jobs, std::vector<double> &scales, int64_t &max_fws, int64_t &max_ws,
+                   int64_t &max_half, int64_t &max_gram) {
+    const int nb = (int) ctx->chunks.size();
+    size_t budget = ctx->opts.workspace_bytes;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = (size_t) (0.6 * (double) fr);
+    }
+    std::vector<int> order(nb);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const auto &a = ctx->chunks[x], &b = ctx->chunks[y];
+        if (a.ld != b.ld) return a.ld > b.ld;
+        return gram_blocks(a.ns) > gram_blocks(b.ns);
+    });
+    const int64_t fws_limit = (int64_t) (0.35 * (double) budget);
+    int64_t fsum = 0;
+    for (int idx : order) {
+        const int64_t need = chunk_fws_bytes(ctx->chunks[idx].ld);
+        // gridDim.y carries the chunk index of a launch: at most 65535 per launch
+        if (groups.empty() || fsum + need > fws_limit || groups.back().members.size() >= 65535) {
+            groups.emplace_back();
+            fsum = 0;
+        }
+        groups.back().members.push_back(idx);
+        fsum += need;
+        groups.back().fws_bytes = fsum;
+    }
+    max_fws = max_ws = max_half = max_gram = 0;
+    for (auto &g : groups) {
+        max_fws = std::max(max_fws, g.fws_bytes);
+        g.desc_off = desc.size();
+        int64_t off = 0;
+        for (int idx : g.members) {
+            const auto &h = ctx->chunks[idx];
+            ChunkDesc d{};
+            d.n = h.n; d.ld = h.ld; d.nq = h.nq; d.ns = h.ns; d.kbin_upp = h.kbin_upp; d.fis = h.fis;
+            d.res = h.res; d.zb0 = h.fis / ctx->nk; d.pix = h.pix; d.res_off = h.res_off; d.gidx = idx;
+            const int64_t m = (int64_t) h.ld * h.ld * 8;
+            d.o_s = off; off += align_up(m, 256);
+            d.o_c = off; off += align_up(m, 256);
+            d.o_y = off; off += align_up((int64_t) h.ld * 8, 256);
+            d.o_fscr = off; off += align_up(64 * (int64_t) h.ld * 8, 256);
+            g.max_ld = std::max(g.max_ld, h.ld);
+            desc.push_back(d);
+        }
+    }
+    // the wave budget is what the largest factor workspace leaves
+    const int64_t wlimit = std::max<int64_t>((int64_t) budget - max_fws, 1);
+    for (auto &g : groups) {
+        for (size_t k = 0; k < g.members.size(); ++k) {
+            const int idx = g.members[k];
+            const auto &h = ctx->chunks[idx];
+            const int gt = gram_blocks(h.ns), splits = gram_splits_for(h.ld, precision);
+            const int64_t need = chunk_ws_bytes(h.ld, h.ns, precision, splits, gt);
+            bool fresh = g.waves.empty() || g.waves.back().ld != h.ld || g.waves.back().gt != gt;
+            if (!fresh) {
+                const auto &w = g.waves.back();
+                fresh = w.ws_bytes + need > wlimit || w.slot_q + h.ns + 1 > 65535;
+            }
+            if (fresh) {
+                g.waves.emplace_back();
+                g.waves.back().ld = h.ld;
+                g.waves.back().gt = gt;
+                g.waves.back().splits = splits;
+            }
+            WavePlan &w = g.waves.back();
+            w.members.push_back((int) k);   // index within the group
+            w.ws_bytes += need;             // refined below
+            w.slot_q += h.ns + 1;           // product jobs, one launch row each (reset below)
+        }
+        for (auto &w : g.waves) {
+            const int ld = w.ld;
+            w.slot_q = 0;
+            const int64_t m = (int64_t) ld * ld * 8, tiles = (ld / 64) * (ld / 64);
+            const int64_t gblk = (int64_t) w.gt * w.gt * w.splits * 128 * 128;
+            w.desc_off = desc.size();
+            int64_t off = 0;
+            for (int k : w.members) {
+                ChunkDesc d = desc[g.desc_off + k];
+                d.o_dpart = off; off += align_up(tiles * 8 * d.ns * 8, 256);
+                if (precision == LQG_PRECISION_FP64) {
+                    d.o_part = off; off += align_up(gblk * 8, 256);
+                    d.o_q = off; off += align_up(m * d.ns, 256);
+                    d.o_r = off; off += align_up(m * d.ns, 256);
+                    d.o_p = off; off += align_up(m * (d.ns + 2), 256);
+                }
+                d.slot_q = w.slot_q; w.slot_q += d.ns + 1;
+                d.slot_r = w.slot_r; w.slot_r += d.ns;
+                d.slot_p = w.slot_p; w.slot_p += d.ns + 2;
+                desc.push_back(d);
+            }
+            const int nch = (int) w.members.size();
+            w.ws_bytes = std::max<int64_t>(off, 256);
+            w.half_bytes = 0;
+            int64_t gram = 0;
+            if (precision == LQG_PRECISION_MIXED) {
+                w.half_bytes = (int64_t) ld * ld * 2 * 2 * ((int64_t) nch + w.slot_q + w.slot_r + w.slot_p);
+                gram = (int64_t) nch * gblk;
+            }
+            max_ws = std::max(max_ws, w.ws_bytes);
+            max_half = std::max(max_half, w.half_bytes);
+            max_gram = std::max(max_gram, gram);
+            w.jobs_off = jobs.size();
+            for (int i = 0; i < nch; ++i)
+                for (int s = 0; s <= desc[w.desc_off + i].ns; ++s) { jobs.push_back(i); jobs.push_back(s); }
+            w.njobs = (int) (jobs.size() - w.jobs_off) / 2;
+            w.scales_off = scales.size();
+            w.nscales = 4 * nch + w.slot_q + w.slot_p + w.slot_r;
+            scales.resize(scales.size() + w.nscales, 1.0);
+            if (precision == LQG_PRECISION_MIXED) {
+                for (int i = 0; i < nch; ++i) {
+                    const ChunkDesc &d = desc[w.desc_off + i];
+                    double *q = scales.data() + w.scales_off + 4 * nch + d.slot_q;
+                    for (int s = 0; s < d.ns; ++s)
+                        q[s] = pow2_scale(ctx->qmax[(size_t) d.res * ctx->nk + s % d.kbin_upp], 16384.0);
+                    q[d.ns] = pow2_scale(ctx->smax[d.res], 16384.0);
+                }
+            }
+        }
+    }
     return LQG_OK;
 }
 
@@ -535,63 +528,192 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     cudaSetDevice(ctx->device);
     int rc = upload_pixels(ctx);
     if (rc) return rc;
+    cudaStream_t st = ctx->stream;
     bool use_theta = false;
     if (theta) {
         for (int i = 0; i < ctx->nkz; ++i) use_theta |= theta[i] != 0.0;
-        LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_theta.p, theta, ctx->nkz * 8, cudaMemcpyHostToDevice, ctx->stream));
+        LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_theta.p, theta, ctx->nkz * 8, cudaMemcpyHostToDevice, st));
     }
     const int nb = (int) ctx->chunks.size();
     ctx->last_status.assign(nb, LQG_CHUNK_OK);
     std::fill(ctx->timings, ctx->timings + 8, 0.0);
     ctx->launches = 0;
-    cudaEvent_t t0, t1;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
-    cudaEventRecord(t0, ctx->stream);
-    // Size-bucketed waves: chunks grouped by their padded size, largest first,
-    // each wave limited by the workspace budget.
-    size_t budget = ctx->opts.workspace_bytes;
-    if (budget == 0) {
-        size_t fr = 0, tot = 0;
-        cudaMemGetInfo(&fr, &tot);
-        budget = (size_t) (0.6 * (double) fr);
+
+    std::vector<GroupPlan> groups;
+    std::vector<ChunkDesc> desc;
+    std::vector<int> jobs;
+    std::vector<double> scales;
+    int64_t max_fws = 0, max_ws = 0, max_half = 0, max_gram = 0;
+    if ((rc = plan_iteration(ctx, precision, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram)))
+        return rc;
+    if (ctx->d_fws.alloc(std::max<int64_t>(max_fws, 256)) || ctx->d_ws.alloc(std::max<int64_t>(max_ws, 256)) ||
+        ctx->d_fbounds.alloc(std::max(2 * nb, 1) * 8))
+        return set_err(ctx, LQG_ERR_NOMEM, "workspace");
+    if (precision == LQG_PRECISION_MIXED &&
+        (ctx->d_halves.alloc(max_half + 1024) || ctx->d_gram.alloc(std::max<int64_t>(max_gram, 1) * 4)))
+        return set_err(ctx, LQG_ERR_NOMEM, "mixed workspace");
+    if (ctx->d_desc.alloc(std::max<size_t>(desc.size(), 1) * sizeof(ChunkDesc)) ||
+        ctx->d_jobs.alloc(std::max<size_t>(jobs.size(), 1) * 4) ||
+        ctx->d_scales.alloc(std::max<size_t>(scales.size(), 1) * 8) ||
+        ctx->d_check.alloc(4 * sizeof(unsigned long long)))
+        return set_err(ctx, LQG_ERR_NOMEM, "descriptors");
+    // pinned staging, so that the uploads below are asynchronous
+    const size_t stage = desc.size() * sizeof(ChunkDesc) + jobs.size() * 4 + scales.size() * 8;
+    if (ctx->h_stage_bytes < stage) {
+        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        ctx->h_stage = nullptr;
+        ctx->h_stage_bytes = 0;
+        LQG_CUDA_CHECK_RET(cudaMallocHost(&ctx->h_stage, stage));
+        ctx->h_stage_bytes = stage;
     }
-    std::vector<int> order(nb);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ctx->chunks[x].ld > ctx->chunks[y].ld; });
-    std::vector<WavePlan> waves;
-    int64_t used = 0;
-    for (int idx : order) {
-        const auto &h = ctx->chunks[idx];
-        int64_t need = chunk_ws_bytes(h, precision, gram_splits_for(h.ld, precision));
-        if (waves.empty() || waves.back().ld != h.ld || used + need > (int64_t) budget) {
-            waves.push_back(WavePlan{});
-            waves.back().ld = h.ld;
-            used = 0;
+    // the previous iteration's uploads must have left the staging buffer
+    LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
+    char *hs = static_cast<char *>(ctx->h_stage);
+    std::memcpy(hs, desc.data(), desc.size() * sizeof(ChunkDesc));
+    std::memcpy(hs + desc.size() * sizeof(ChunkDesc), jobs.data(), jobs.size() * 4);
+    std::memcpy(hs + desc.size() * sizeof(ChunkDesc) + jobs.size() * 4, scales.data(), scales.size() * 8);
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_desc.p, hs, desc.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice, st));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_jobs.p, hs + desc.size() * sizeof(ChunkDesc), jobs.size() * 4,
+                                       cudaMemcpyHostToDevice, st));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_scales.p, hs + desc.size() * sizeof(ChunkDesc) + jobs.size() * 4,
+                                       scales.size() * 8, cudaMemcpyHostToDevice, st));
+    LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_status.p, 0, std::max(nb, 1) * 4, st));
+    LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_check.p, 0, 4 * sizeof(unsigned long long), st));
+
+    WaveArgs base{};
+    base.fws = ctx->d_fws.as<char>();
+    base.ws = ctx->d_ws.as<char>();
+    base.fbounds = ctx->d_fbounds.as<double>();
+    base.wave = ctx->d_wave.as<double>(); base.delta = ctx->d_delta.as<double>(); base.ivar = ctx->d_ivar.as<double>();
+    base.logw = ctx->d_logw.as<double>(); base.sqw = ctx->d_sqw.as<double>();
+    base.deriv = ctx->d_deriv.as<double>();
+    base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
+    base.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
+    base.results = ctx->d_results.as<double>();
+    base.status = ctx->d_status.as<int>();
+    base.grid = ctx->grid;
+    base.bins = ctx->d_bins.as<DeviceBins>();
+    base.cont_logl = ctx->opts.cont_logl_order;
+    base.cont_l = ctx->opts.cont_l_order;
+    base.turn_off_sfid = ctx->opts.turn_off_sfid;
+    base.skip_fisher = ctx->opts.skip_fisher;
+    base.precision = precision;
+    base.results_elems = ctx->results_size;
+    base.check = ctx->d_check.as<unsigned long long>();
+
+    // LQG_SYNC_EACH=1: synchronise after every kernel and name the one that failed
+    static const bool sync_each = getenv("LQG_SYNC_EACH") && getenv("LQG_SYNC_EACH")[0] == '1';
+    auto step = [&](const char *what, int ld, int nch) -> int {
+        if (!sync_each) return LQG_OK;
+        cudaError_t se = cudaStreamSynchronize(st);
+        if (se == cudaSuccess) se = cudaGetLastError();
+        if (se != cudaSuccess)
+            return set_err(ctx, LQG_ERR_CUDA, std::string(what) + " (ld " + std::to_string(ld) + ", " +
+                                                  std::to_string(nch) + " chunks): " + cudaGetErrorString(se));
+        return LQG_OK;
+    };
+    // events: [0] start, then 3 per group and 5 per wave, [1] end
+    std::vector<std::pair<size_t, int>> spans;   // (first event, timing slot) of each measured span
+    size_t nev = 2;
+    cudaEvent_t ev_start = pool_event(ctx, 0), ev_end = pool_event(ctx, 1);
+    cudaEventRecord(ev_start, st);
+    for (auto &g : groups) {
+        WaveArgs a = base;
+        a.chunks = ctx->d_desc.as<ChunkDesc>() + g.desc_off;
+        a.n_chunks = (int) g.members.size();
+        a.max_ld = g.max_ld;
+        a.fws_bytes = g.fws_bytes;
+        const size_t e0 = nev;
+        nev += 3;
+        cudaEventRecord(pool_event(ctx, e0), st);
+        launch_build_s_c(a, st);
+        if ((rc = step("build_s_c", g.max_ld, a.n_chunks))) return rc;
+        cudaEventRecord(pool_event(ctx, e0 + 1), st);
+        launch_factor_all(a, st);
+        if ((rc = step("factor", g.max_ld, a.n_chunks))) return rc;
+        cudaEventRecord(pool_event(ctx, e0 + 2), st);
+        spans.push_back({e0, 0});
+        spans.push_back({e0 + 1, 1});
+        ctx->launches += a.launches;
+        for (auto &w : g.waves) {
+            WaveArgs b = base;
+            const int nch = (int) w.members.size();
+            b.chunks = ctx->d_desc.as<ChunkDesc>() + w.desc_off;
+            b.n_chunks = nch;
+            b.max_ld = w.ld;
+            b.gt = w.gt;
+            b.fws_bytes = g.fws_bytes;
+            b.ws_bytes = w.ws_bytes;
+            b.total_slots_q = w.slot_q; b.total_slots_r = w.slot_r; b.total_slots_p = w.slot_p;
+            b.gram_splits = w.splits;
+            b.scales = ctx->d_scales.as<double>() + w.scales_off;
+            if (precision == LQG_PRECISION_MIXED) {
+                __half *hb = ctx->d_halves.as<__half>();
+                const int64_t pl = (int64_t) w.ld * w.ld;
+                b.c_hi = hb; hb += pl * nch;
+                b.c_lo = hb; hb += pl * nch;
+                b.q_hi = hb; hb += pl * w.slot_q;
+                b.q_lo = hb; hb += pl * w.slot_q;
+                b.r_hi = hb; hb += pl * w.slot_r;
+                b.r_lo = hb; hb += pl * w.slot_r;
+                b.p_hi = hb; hb += pl * w.slot_p;
+                b.p_lo = hb; hb += pl * w.slot_p;
+                b.gram_part = ctx->d_gram.as<float>();
+                b.gram_elems = (int64_t) nch * w.gt * w.gt * w.splits * 128 * 128;
+            }
+            const size_t w0 = nev;
+            nev += 5;
+            b.mid_event = pool_event(ctx, w0 + 2);
+            const int *d_jobs = ctx->d_jobs.as<int>() + w.jobs_off;
+            cudaEventRecord(pool_event(ctx, w0), st);
+            if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(b, st);
+            launch_build_q(b, st);
+            if ((rc = step("build_q", w.ld, nch))) return rc;
+            cudaEventRecord(pool_event(ctx, w0 + 1), st);
+            if (precision == LQG_PRECISION_MIXED)
+                launch_products_mixed(b, st, d_jobs, w.njobs);
+            else
+                launch_products_fp64(b, st, d_jobs, w.njobs);
+            if ((rc = step("products", w.ld, nch))) return rc;
+            cudaEventRecord(pool_event(ctx, w0 + 3), st);
+            launch_finish(b, st);
+            if ((rc = step("finish", w.ld, nch))) return rc;
+            cudaEventRecord(pool_event(ctx, w0 + 4), st);
+            spans.push_back({w0, 2});
+            spans.push_back({w0 + 1, 3});
+            spans.push_back({w0 + 2, 4});
+            spans.push_back({w0 + 3, 5});
+            ctx->launches += b.launches;
         }
-        waves.back().members.push_back(idx);
-        used += need;
     }
-    for (auto &w : waves) {
-        rc = run_wave(ctx, w, precision, use_theta);
-        if (rc) return rc;
-    }
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_status.p, ctx->last_status.data(), nb * 4, cudaMemcpyHostToDevice, ctx->stream));
-    cudaEventRecord(ctx->ev[7], ctx->stream);
+    const size_t eacc = nev++;
+    cudaEventRecord(pool_event(ctx, eacc), st);
     launch_accumulate(ctx->d_meta.as<ChunkDesc>(), nb, ctx->d_results.as<double>(), ctx->d_status.as<int>(),
-                      ctx->nkz, ctx->d_fisher.as<double>(), ctx->d_dbt.as<double>(), ctx->stream);
+                      ctx->nkz, ctx->d_fisher.as<double>(), ctx->d_dbt.as<double>(), st);
     ctx->launches++;
-    cudaEventRecord(t1, ctx->stream);
-    LQG_CUDA_CHECK_RET(cudaStreamSynchronize(ctx->stream));
-    float tt = 0, ta = 0;
-    cudaEventElapsedTime(&tt, t0, t1);
-    cudaEventElapsedTime(&ta, ctx->ev[7], t1);
+    cudaEventRecord(ev_end, st);
+    unsigned long long *chk = reinterpret_cast<unsigned long long *>(hs);
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(chk, ctx->d_check.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->last_status.data(), ctx->d_status.p, nb * 4, cudaMemcpyDeviceToHost, st));
+    LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, std::string("iteration kernels: ") + cudaGetErrorString(e));
+    if (chk[0] != 0)
+        return set_err(ctx, LQG_ERR_STATE, "index check failed " + std::to_string(chk[0]) + " times: code " +
+                                               std::to_string(chk[1]) + " chunk " + std::to_string(chk[2]) +
+                                               " index " + std::to_string(chk[3]));
+    // [0] S/C build, [1] factorisation, [2] Q build, [3] products, [4] Gram, [5] finish,
+    // [6] accumulation, [7] whole iteration
+    for (auto &sp : spans) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->evpool[sp.first], ctx->evpool[sp.first + 1]);
+        ctx->timings[sp.second] += ms;
+    }
+    float ta = 0, tt = 0;
+    cudaEventElapsedTime(&ta, ctx->evpool[eacc], ev_end);
+    cudaEventElapsedTime(&tt, ev_start, ev_end);
     ctx->timings[6] = ta;
     ctx->timings[7] = tt;
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, cudaGetErrorString(e));
     return LQG_OK;
 }
 

@@ -20,6 +20,7 @@ constexpr double kDoubleEpsilon = 1e-15;
 constexpr int kPad = 64;          // matrices are stored with a leading dimension that is a multiple of 64
 constexpr int kMaxPixels = 8192;  // largest chunk the engine accepts
 constexpr int kMaxContVecs = 4;
+constexpr int kMaxGramBlocks = 4; // ns + 2 <= 128 kMaxGramBlocks stored matrices per chunk
 
 // One chunk of the batch: what Chunk::Chunk computes (core/chunk_estimate.cpp:141-257)
 // plus the device offsets of its data and workspace.
@@ -34,10 +35,14 @@ struct ChunkDesc {
     int zb0;              // first redshift bin of the chunk's matrices = fis / nk
     int64_t pix;          // offset of the pixel arrays
     int64_t res_off;      // offset of the per-chunk results (3 nq + nq^2 doubles)
-    // Workspace offsets (bytes, relative to the wave workspace base)
-    int64_t o_s, o_c, o_y, o_q, o_r, o_p, o_part, o_dpart, o_split_c;
+    // Factor workspace (bytes, relative to WaveArgs::fws): S_fid, C~ -> C^-1, y and
+    // the factorisation scratch (64 ld doubles), kept for the whole iteration.
+    int64_t o_s, o_c, o_y, o_fscr;
+    // Wave workspace (bytes, relative to WaveArgs::ws): FP64 product stacks, per-tile
+    // d partials and FP64 Gram partials.
+    int64_t o_q, o_r, o_p, o_part, o_dpart;
     int slot_q, slot_r, slot_p;  // first matrix slot of this chunk in the stacked operand buffers
-    int n_tiles;          // number of 64x64 tiles of its matrix (ld/64)^2
+    int gidx;             // index of the chunk in the batch (factor bounds, status)
     int status;
 };
 
@@ -76,6 +81,9 @@ struct WaveArgs {
     int n_chunks;
     int max_ld;
     char *ws;                    // wave workspace base
+    char *fws;                   // factor workspace base
+    double *fbounds;             // per batch chunk: max |C^-1|, largest row sum of |C^-1|
+    int gt;                      // Gram blocks of 128 per dimension (ns + 2 <= 128 gt)
     const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
     const double *deriv, *signal, *qmax;             // tables
     const double *theta;                             // device, nkz
@@ -93,7 +101,7 @@ struct WaveArgs {
     int launches;
     cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
     // extents of the buffers above, used by the LQG_CHECKED build to validate indices
-    int64_t ws_bytes, results_elems, gram_elems;
+    int64_t ws_bytes, fws_bytes, results_elems, gram_elems;
     unsigned long long *check;   // [0] violations, [1] first code, [2] first chunk, [3] first index
 };
 
@@ -116,8 +124,11 @@ __device__ __forceinline__ bool lqg_in_bounds(const WaveArgs &a, bool ok, int co
 #define LQG_IN_BOUNDS(a, cond, code, chunk, idx) true
 #endif
 
+// Phase A (all chunks of a group): S_fid and C~, then the FP64 factorisation.
 void launch_build_s_c(WaveArgs &a, cudaStream_t st);
-void launch_factor(WaveArgs &a, cudaStream_t st);
+void launch_factor_all(WaveArgs &a, cudaStream_t st);
+size_t factor_smem_bytes();
+// Phase B (per wave): Q_k, products, traces, per-chunk results.
 void launch_build_q(WaveArgs &a, cudaStream_t st);
 void launch_products_fp64(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs);
 void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs);
