@@ -16,8 +16,8 @@
 //             A_S^T = S C^-1 and N C^-1, so G holds F_ij = <A_i^T, A_j>,
 //             t_j and b_j (core/chunk_estimate.cpp:783-832).
 //
-// Warp roles (192 threads): warp 0 issues TMA loads, warp 1 owns tensor memory
-// and issues the MMAs, warps 2-5 drain the accumulator.  Every wait on an
+// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 owns tensor memory
+// and issues the MMAs, warps 2-9 drain the accumulators.  Every wait on an
 // mbarrier is bounded by a wall-clock limit; on timeout the kernel records an
 // error in the chunk status and leaves after its own work has drained.
 #include "lqg_internal.cuh"
@@ -165,7 +165,7 @@ __device__ __forceinline__ double pow2_floor(double x) {
 }
 
 constexpr int BK = 64;                      // fp16 elements per K step (128 bytes)
-constexpr int G_BM = 128, G_BN = 256, G_STAGES = 2;
+constexpr int G_BM = 128, G_BN = 128, G_STAGES = 3;
 constexpr int G_TILE_A = G_BM * BK * 2, G_TILE_B = G_BN * BK * 2;
 constexpr int G_STAGE_BYTES = 2 * G_TILE_A + 2 * G_TILE_B;
 constexpr int G_SMEM = G_STAGES * G_STAGE_BYTES + 1024 + 256;
@@ -173,18 +173,101 @@ constexpr int R_BM = 128, R_BN = 128, R_STAGES = 3;
 constexpr int R_TILE = R_BM * BK * 2;
 constexpr int R_STAGE_BYTES = 4 * R_TILE;
 constexpr int R_SMEM = R_STAGES * R_STAGE_BYTES + 1024 + 256;
-constexpr int R_THREADS = 320;              // producer, MMA, 8 epilogue warps
+constexpr int TC_THREADS = 320;             // producer, MMA, 8 epilogue warps
+constexpr int R_THREADS = TC_THREADS;
 constexpr int kGramK = 32768;               // K elements per Gram split
-constexpr int kDrain = 4;                   // K blocks per drained hi*hi partial
+constexpr int kDrain = 2;                   // K blocks per drained hi*hi partial
 
 // Accumulation: the tensor cores round every fp32 accumulation of an MMA, with a
 // bias that grows with the number of accumulations into one accumulator.  The
 // hi*hi products and the (2^11 times smaller) cross products therefore go to
-// separate TMEM accumulators, and the Gram drains its hi*hi accumulator every
-// kDrain K blocks into Kahan-compensated fp32 sums held in registers.
+// separate TMEM accumulators, and the hi*hi accumulator is drained every kDrain
+// K blocks (8 MMAs of K = 16) into fp32 sums held in registers: a ping-pong pair
+// of hi*hi accumulators lets the MMAs continue while one is drained.
+//
+// TMEM columns: hi*hi ping [0, 128), pong [128, 256), cross [256, 384).
+// Epilogue warps 2..9: warp w reads TMEM lanes 32 (w % 4) .. +31 and the 64
+// columns 64 ((w - 2) / 4) .. +63 of each accumulator.
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// MMA issuer of both kernels: for drain group g (kDrain K blocks), accumulate
+// hi*hi into buffer g & 1 (fresh per group) and the cross terms into the third
+// buffer (fresh at the first K block).  Stage layout: A hi, A lo, B hi, B lo.
+template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN>
+__device__ __forceinline__ void mma_drained(uint32_t tmem, unsigned char *smem, uint64_t *full, uint64_t *empty,
+                                            uint64_t *dfull, uint64_t *dempty, uint64_t *accum, int kblocks,
+                                            uint32_t idesc, int *abort_flag) {
+    const int ngroups = (kblocks + kDrain - 1) / kDrain;
+    bool ok = true;
+    for (int g = 0; g < ngroups && ok; ++g) {
+        const int b = g & 1;
+        if (g >= 2 && !mbar_wait(&dempty[b], ((g >> 1) - 1) & 1)) { *abort_flag = 1; break; }
+        fence_after();
+        const uint32_t thh = tmem + b * BN, tx = tmem + 2 * BN;
+        const int kb_end = min(kblocks, (g + 1) * kDrain);
+        for (int kb = g * kDrain; kb < kb_end; ++kb) {
+            const int st = kb % STAGES;
+            if (!mbar_wait(&full[st], (kb / STAGES) & 1)) { *abort_flag = 1; ok = false; break; }
+            fence_after();
+            unsigned char *sb = smem + st * STAGE_BYTES;
+            const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + TILE_A);
+            const uint64_t bh = sw128_desc(sb + 2 * TILE_A), bl = sw128_desc(sb + 2 * TILE_A + TILE_B);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t adv = (uint64_t) (kk * 32) >> 4;
+                umma_f16(thh, ah + adv, bh + adv, idesc, (kb > g * kDrain || kk > 0));
+                umma_f16(tx, ah + adv, bl + adv, idesc, (kb | kk) != 0);
+                umma_f16(tx, al + adv, bh + adv, idesc, 1);
+            }
+            umma_commit(&empty[st]);
+        }
+        umma_commit(&dfull[b]);
+    }
+    umma_commit(accum);
+}
+
+// Epilogue side of the drain: adds every drained hi*hi partial of this warp's
+// 32 lanes x 64 columns into sum (plain fp32, or Kahan-compensated with comp).
+// Returns false (warp-uniform) if a wait timed out or the CTA aborted.
+template <bool KAHAN>
+__device__ __forceinline__ bool drain_all(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
+                                          uint64_t *dempty, int kblocks, float (&sum)[64], float (&comp)[64],
+                                          int *abort_flag) {
+    const int ngroups = (kblocks + kDrain - 1) / kDrain;
+    bool alive = true;
+    for (int g = 0; g < ngroups; ++g) {
+        const int b = g & 1;
+        alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g >> 1) & 1)) && !*abort_flag;
+        if (!alive) break;
+        fence_after();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float v[32];
+            tmem_ld32(tmem + lane_addr + b * 128 + col0 + h * 32, v);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (KAHAN) {
+                    const float yv = v[j] - comp[h * 32 + j];
+                    const float t = sum[h * 32 + j] + yv;
+                    comp[h * 32 + j] = (t - sum[h * 32 + j]) - yv;
+                    sum[h * 32 + j] = t;
+                } else {
+                    sum[h * 32 + j] += v[j];
+                }
+            }
+        }
+        fence_before();
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) mbar_arrive(&dempty[b]);
+    }
+    return alive;
+}
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(192, 1)
+__global__ void __maxnreg__(200)
 k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
           const __grid_constant__ CUtensorMap mc_lo, const __grid_constant__ CUtensorMap mq_hi,
           const __grid_constant__ CUtensorMap mq_lo) {
@@ -193,7 +276,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + G_STAGES * G_STAGE_BYTES);
     uint64_t *empty = full + G_STAGES;
-    uint64_t *accum = empty + G_STAGES;
+    uint64_t *dfull = empty + G_STAGES;
+    uint64_t *dempty = dfull + 2;
+    uint64_t *accum = dempty + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
 
@@ -210,11 +295,12 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < G_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+        for (int i = 0; i < 2; ++i) { mbar_init(&dfull[i], 1); mbar_init(&dempty[i], 8); }
         mbar_init(accum, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) tmem_alloc(tmem_slot, 2 * G_BN);   // hi*hi in [0, 256), cross in [256, 512)
+    if (warp == 1) tmem_alloc(tmem_slot, 512);
     fence_before();
     __syncthreads();
     fence_after();
@@ -242,34 +328,21 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         for (int kb = (issued > G_STAGES ? issued - G_STAGES : 0); kb < issued; ++kb)
             mbar_wait(&full[kb % G_STAGES], (kb / G_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        constexpr uint32_t idesc = idesc_f16(G_BM, G_BN);
-        for (int kb = 0; kb < kblocks; ++kb) {
-            const int st = kb % G_STAGES;
-            if (!mbar_wait(&full[st], (kb / G_STAGES) & 1)) { *abort_flag = 1; break; }
-            fence_after();
-            unsigned char *sb = smem + st * G_STAGE_BYTES;
-            const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + G_TILE_A);
-            const uint64_t bh = sw128_desc(sb + 2 * G_TILE_A), bl = sw128_desc(sb + 2 * G_TILE_A + G_TILE_B);
-#pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-                const uint64_t adv = (uint64_t) (kk * 32) >> 4;
-                const uint32_t acc = (kb | kk) != 0;
-                umma_f16(tmem, ah + adv, bh + adv, idesc, acc);
-                umma_f16(tmem + G_BN, ah + adv, bl + adv, idesc, acc);
-                umma_f16(tmem + G_BN, al + adv, bh + adv, idesc, 1);
-            }
-            umma_commit(&empty[st]);
-        }
-        umma_commit(accum);
+        mma_drained<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN>(tmem, smem, full, empty, dfull, dempty, accum,
+                                                                     kblocks, idesc_f16(G_BM, G_BN), abort_flag);
     } else if (warp >= 2) {
-        // epilogue: TMEM -> scaled fp16 hi/lo planes, row-major (R) and transposed (P)
-        // warp-uniform outcome, so that the aligned TMEM loads run in whole warps
-        const bool got = __all_sync(0xffffffffu, mbar_wait(accum, 0)) && !*abort_flag;
+        // epilogue: drained sums + cross terms -> scaled fp16 hi/lo planes,
+        // row-major (R) and transposed (P)
+        const int quad = warp % 4, col0 = 64 * ((warp - 2) / 4);
+        const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
+        float sum[64], comp[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) sum[j] = 0.f;
+        bool got = drain_all<false>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, comp, abort_flag);
+        got = __all_sync(0xffffffffu, got && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
-            const int sub = warp % 4;
-            const int row = m0 + sub * 32 + lane;
+            const int row = m0 + quad * 32 + lane;
             const int nq4 = 4 * a.n_chunks;
             const double sc = a.scales[4 * c + 2];
             const double qs = a.scales[nq4 + ch.slot_q + s];
@@ -281,35 +354,41 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const bool write_r = s < ch.ns;
             const bool slots_ok = LQG_IN_BOUNDS(a, (!write_r || ch.slot_r + s < a.total_slots_r) &&
                                                      ch.slot_p + s < a.total_slots_p, 2, c, s);
-            for (int jc = 0; jc < G_BN / 32 && slots_ok; ++jc) {
-                const int col0 = n0 + jc * 32;
-                float v[32], x[32];
-                const uint32_t lane_addr = (uint32_t) (sub * 32) << 16;
-                tmem_ld32(tmem + lane_addr + jc * 32, v);
-                tmem_ld32(tmem + lane_addr + G_BN + jc * 32, x);
-                if (col0 >= ld) continue;
-                __align__(16) __half hi[32], lo[32];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float val = (v[j] + x[j]) * mult;
-                    hi[j] = __float2half_rn(val);
-                    lo[j] = __float2half_rn(val - __half2float(hi[j]));
+            for (int h = 0; h < 2; ++h) {
+                const int cb = n0 + col0 + h * 32;
+                float x[32];
+                tmem_ld32(tmem + lane_addr + 2 * G_BN + col0 + h * 32, x);
+                if (!slots_ok || cb >= ld || row >= ld) continue;
+                // hi/lo pairs packed in registers (two halves per 32-bit word)
+                uint32_t hp[16], lp[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const float v0 = (sum[h * 32 + 2 * j] + x[2 * j]) * mult;
+                    const float v1 = (sum[h * 32 + 2 * j + 1] + x[2 * j + 1]) * mult;
+                    const __half2 hv = __floats2half2_rn(v0, v1);
+                    const float2 hf = __half22float2(hv);
+                    const __half2 lv = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
+                    hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
+                    lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
                 }
-                if (row < ld) {
-                    if (write_r) {
-                        uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + col0);
-                        uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + col0);
+                if (write_r) {
+                    uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
+                    uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            dh[q] = reinterpret_cast<const uint4 *>(hi)[q];
-                            dl[q] = reinterpret_cast<const uint4 *>(lo)[q];
-                        }
+                    for (int q = 0; q < 4; ++q) {
+                        dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+                        dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
                     }
+                }
+                unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
+                unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        Ph[(size_t) (col0 + j) * ld + row] = hi[j];
-                        Pl[(size_t) (col0 + j) * ld + row] = lo[j];
-                    }
+                for (int j = 0; j < 16; ++j) {
+                    ph[(size_t) (cb + 2 * j) * ld] = (unsigned short) (hp[j] & 0xffffu);
+                    ph[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (hp[j] >> 16);
+                    pl[(size_t) (cb + 2 * j) * ld] = (unsigned short) (lp[j] & 0xffffu);
+                    pl[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (lp[j] >> 16);
                 }
             }
         }
@@ -318,18 +397,15 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     __syncthreads();
     if (warp == 1) {
         fence_after();
-        tmem_dealloc(tmem, 2 * G_BN);
+        tmem_dealloc(tmem, 512);
     }
     if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[ch.gidx], LQG_CHUNK_TIMEOUT);
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 
 // ---------------------------------------------------------------------------
 // Gram block (bi, bj) of one chunk over one K split.
-__global__ void __launch_bounds__(R_THREADS, 1)
+__global__ void __maxnreg__(200)
 k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_constant__ CUtensorMap mp_lo,
           const __grid_constant__ CUtensorMap mr_hi, const __grid_constant__ CUtensorMap mr_lo) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -352,7 +428,6 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     const int64_t kper = ((K + a.gram_splits - 1) / a.gram_splits + BK - 1) / BK * BK;
     const int64_t k_lo = sp * kper, k_hi = min(K, k_lo + kper);
     const int kblocks = k_hi > k_lo ? (int) ((k_hi - k_lo) / BK) : 0;
-    const int nchunk = (kblocks + kDrain - 1) / kDrain;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int prow = ch.slot_p + bi * R_BM, rrow = ch.slot_r + bj * R_BN;
 
@@ -389,33 +464,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         for (int kb = (issued > R_STAGES ? issued - R_STAGES : 0); kb < issued; ++kb)
             mbar_wait(&full[kb % R_STAGES], (kb / R_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
-        constexpr uint32_t idesc = idesc_f16(R_BM, R_BN);
-        bool ok = true;
-        for (int g = 0; g < nchunk && ok; ++g) {
-            const int b = g & 1;
-            if (g >= 2 && !mbar_wait(&dempty[b], ((g >> 1) - 1) & 1)) { *abort_flag = 1; ok = false; break; }
-            fence_after();
-            const uint32_t thh = tmem + b * R_BN, tx = tmem + 2 * R_BN;
-            const int kb_end = min(kblocks, (g + 1) * kDrain);
-            for (int kb = g * kDrain; kb < kb_end; ++kb) {
-                const int st = kb % R_STAGES;
-                if (!mbar_wait(&full[st], (kb / R_STAGES) & 1)) { *abort_flag = 1; ok = false; break; }
-                fence_after();
-                unsigned char *sb = smem + st * R_STAGE_BYTES;
-                const uint64_t ph = sw128_desc(sb), pl = sw128_desc(sb + R_TILE);
-                const uint64_t rh = sw128_desc(sb + 2 * R_TILE), rl = sw128_desc(sb + 3 * R_TILE);
-#pragma unroll
-                for (int kk = 0; kk < BK / 16; ++kk) {
-                    const uint64_t adv = (uint64_t) (kk * 32) >> 4;
-                    umma_f16(thh, ph + adv, rh + adv, idesc, (kb > g * kDrain || kk > 0));
-                    umma_f16(tx, ph + adv, rl + adv, idesc, (kb | kk) != 0);
-                    umma_f16(tx, pl + adv, rh + adv, idesc, 1);
-                }
-                umma_commit(&empty[st]);
-            }
-            umma_commit(&dfull[b]);
-        }
-        umma_commit(accum);
+        mma_drained<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN>(tmem, smem, full, empty, dfull, dempty, accum,
+                                                                  kblocks, idesc_f16(R_BM, R_BN), abort_flag);
     } else if (warp >= 2) {
         // 8 epilogue warps: lane quadrant warp % 4, columns 64 * ((warp - 2) / 4) + [0, 64)
         const int quad = warp % 4, half = (warp - 2) / 4;
@@ -423,29 +473,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         float sum[64], comp[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) { sum[j] = 0.f; comp[j] = 0.f; }
-        bool alive = true;
-        for (int g = 0; g < nchunk; ++g) {
-            const int b = g & 1;
-            alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g >> 1) & 1)) && !*abort_flag;
-            if (!alive) break;
-            fence_after();
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float v[32];
-                tmem_ld32(tmem + lane_addr + b * R_BN + half * 64 + h * 32, v);
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    // Kahan: sum + comp carries the drained partials without rounding loss
-                    const float yv = v[j] - comp[h * 32 + j];
-                    const float t = sum[h * 32 + j] + yv;
-                    comp[h * 32 + j] = (t - sum[h * 32 + j]) - yv;
-                    sum[h * 32 + j] = t;
-                }
-            }
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&dempty[b]);
-        }
+        const bool alive = drain_all<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, comp, abort_flag);
         const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
@@ -585,7 +613,7 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         return;
     }
     const int tiles = ((ld + G_BM - 1) / G_BM) * ((ld + G_BN - 1) / G_BN);
-    k_tc_gemm<<<dim3(tiles, njobs), 192, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
+    k_tc_gemm<<<dim3(tiles, njobs), TC_THREADS, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
     if (a.mid_event) cudaEventRecord(a.mid_event, st);
     k_tc_gram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), R_THREADS, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
     a.launches += 2;

@@ -397,9 +397,11 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
     const int nb = (int) ctx->chunks.size();
     size_t budget = ctx->opts.workspace_bytes;
     if (budget == 0) {
+        // 60 % of the memory that is free or already held as workspace
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        budget = (size_t) (0.6 * (double) fr);
+        const size_t held = ctx->d_fws.bytes + ctx->d_ws.bytes + ctx->d_halves.bytes + ctx->d_gram.bytes;
+        budget = (size_t) (0.6 * (double) (fr + held));
     }
     std::vector<int> order(nb);
     std::iota(order.begin(), order.end(), 0);
