@@ -128,15 +128,16 @@ __global__ void k_build_s_c(WaveArgs a) {
 
 // ---------------------------------------------------------------------------
 // Phase B, K1b: stored derivative matrices Q_s (Chunk::_setQiMatrix and
-// _applyRedshiftInterp, core/chunk_estimate.cpp:429-536), written as FP64 or
-// as fp16 hi/lo planes, and per-warp partial sums of d_s = y^T Q_s y
-// (computePSbeforeFvector, :754-759).  Each thread owns 16 elements of a
-// 64 x 64 tile; the interpolation index and the redshift weights of an element
-// are computed once and reused by every k band.
+// _applyRedshiftInterp, core/chunk_estimate.cpp:429-536) and per-warp partial
+// sums of d_s = y^T Q_s y (computePSbeforeFvector, :754-759).  Q_s at
+// (i, j) is the k-band row of the derivative table interpolated at v_ij times
+// the redshift weight of bin iz at z_ij; the interpolation index and the
+// interpolated row value are computed once per element and k band and reused
+// by every redshift bin.
+//
+// FP64 variant: each thread owns 16 elements of a 64 x 64 tile.
 constexpr int QEPT = T64 * T64 / 256;
-constexpr int kMaxZb = 8;
 
-template <bool MIXED>
 __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
     const int c = blockIdx.y;
     const ChunkDesc &ch = a.chunks[c];
@@ -148,7 +149,6 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
     const double *y = fws_d(a, ch.o_y);
     const int nzb = ch.ns / ch.kbin_upp;
     int nidx[QEPT];
-    float dnf[QEPT], yyf[QEPT];
     double dn[QEPT], yy[QEPT], zz[QEPT];
     size_t off[QEPT];
     bool valid[QEPT];
@@ -167,64 +167,126 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
             zz[u] = z;
             yy[u] = y[i] * y[j];
         }
-        dnf[u] = (float) dn[u];
-        yyf[u] = (float) yy[u];
     }
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
     const size_t plane = (size_t) ld * ld;
     const double *rows = a.deriv + (size_t) ch.res * bins.nk * a.grid.nv;
-    if (MIXED) {
-        // Operands of fp16 hi/lo splits (22 bits) need no FP64 here: the
-        // per-slot arithmetic is FP32 (GB300's FP64 rate is 1/60 of FP32).
+    for (int kn = 0; kn < ch.kbin_upp; ++kn) {
+        const double *row = rows + (size_t) kn * a.grid.nv;
+        double base[QEPT];
+#pragma unroll
+        for (int u = 0; u < QEPT; ++u)
+            base[u] = valid[u] ? row[nidx[u]] * (1 - dn[u]) + row[nidx[u] + 1] * dn[u] : 0.0;
         for (int iz = 0; iz < nzb; ++iz) {
-            const int zm = ch.zb0 + iz;
-            float w[QEPT];
+            const int s = iz * ch.kbin_upp + kn, zm = ch.zb0 + iz;
+            double *Q = ws_d(a, ch.o_q) + (size_t) s * plane;
+            double part = 0.0;
 #pragma unroll
-            for (int u = 0; u < QEPT; ++u) w[u] = valid[u] ? (float) zweight(bins, zm, zz[u]) : 0.f;
-            for (int kn = 0; kn < ch.kbin_upp; ++kn) {
-                const int s = iz * ch.kbin_upp + kn;
-                const double *row = rows + (size_t) kn * a.grid.nv;
-                const float qs = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + s];
-                __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
-                __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
-                float fpart = 0.f;
+            for (int u = 0; u < QEPT; ++u) {
+                const double q = valid[u] ? base[u] * zweight(bins, zm, zz[u]) : 0.0;
+                part += yy[u] * q;
+                Q[off[u]] = q;
+            }
+            part = warp_sum(part);
+            if (lane == 0) dpart[s] = part;
+        }
+    }
+}
+
+// Mixed variant: Q_s straight to fp16 hi/lo planes with the slot's power-of-two
+// scale.  The operands of a 22-bit split need no FP64: interpolation and
+// weights run in FP32 (GB300's FP64 rate is 1/60 of its FP32 rate) from a
+// float copy of the derivative table.  Each thread owns 4 column pairs of a
+// 32 x 64 half tile (one row per warp and pair step, stores of 128 B per warp);
+// redshift bins are taken kZGroup at a time with their weights in registers.
+constexpr int QM_PAIRS = 4;
+constexpr int kZGroup = 4;
+
+__device__ __forceinline__ float zweight_f(const DeviceBins &b, int zm, float z) {
+    const float zc = (float) b.z_centers[zm], dz = (float) b.dz;
+    if (!b.triangular || b.nz == 1) return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.f : 0.f;
+    if (zm == 0 && z < zc) return 1.f;
+    if (zm == b.nz - 1 && z > zc) return 1.f;
+    if (z >= zc - dz && z <= zc + dz) return 1.f - fabsf(z - zc) / dz;
+    return 0.f;
+}
+
+__global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    const int ld = ch.ld, n = ch.n, tpr = ld / T64;
+    const int tile = blockIdx.x >> 1, hrow = (blockIdx.x & 1) * 32;
+    if (tile >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    const int ti = tile / tpr, tj = tile % tpr;
+    const DeviceBins &bins = *a.bins;
+    const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix;
+    const double *y = fws_d(a, ch.o_y);
+    const int nzb = ch.ns / ch.kbin_upp;
+    constexpr int E = 2 * QM_PAIRS;
+    int nidx[E];
+    float dnf[E], yyf[E], zf[E];
+    size_t off[QM_PAIRS];    // element offset of each pair's first element
 #pragma unroll
-                for (int u = 0; u < QEPT; ++u) {
-                    const float r0 = (float) row[nidx[u]], r1 = (float) row[nidx[u] + 1];
-                    const float q = (r0 * (1.f - dnf[u]) + r1 * dnf[u]) * w[u];
-                    fpart = fmaf(yyf[u], q, fpart);
-                    if (!LQG_IN_BOUNDS(a, (size_t) (ch.slot_q + s) * plane + off[u] <
-                                              (size_t) a.total_slots_q * plane, 5, c, off[u]))
-                        continue;
-                    const float xs = q * qs;
-                    const __half h = __float2half_rn(xs);
-                    qh[off[u]] = h;
-                    ql[off[u]] = __float2half_rn(xs - __half2float(h));
-                }
-                const double part = warp_sum((double) fpart);
-                if (lane == 0) dpart[s] = part;
+    for (int u = 0; u < QM_PAIRS; ++u) {
+        const int p = threadIdx.x + 256 * u;
+        const int i = ti * T64 + hrow + p / 32, j0 = tj * T64 + 2 * (p % 32);
+        off[u] = (size_t) i * ld + j0;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int k = 2 * u + e, j = j0 + e;
+            nidx[k] = 0; dnf[k] = 0.f; yyf[k] = 0.f; zf[k] = -1e30f;
+            if (i < n && j < n) {
+                const int lo = i < j ? i : j, hi = i < j ? j : i;
+                double v, z, dn;
+                vz_of(logw, sqw, lo, hi, v, z);
+                vindex(a.grid, v, nidx[k], dn);
+                dnf[k] = (float) dn;
+                zf[k] = (float) z;
+                yyf[k] = (float) (y[i] * y[j]);
             }
         }
-    } else {
+    }
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
+    const size_t plane = (size_t) ld * ld;
+    const float *rows = a.deriv_f + (size_t) ch.res * bins.nk * a.grid.nv;
+    const double *qscale = a.scales + (size_t) 4 * a.n_chunks + ch.slot_q;
+    for (int z0 = 0; z0 < nzb; z0 += kZGroup) {
+        float w[kZGroup][E];
+#pragma unroll
+        for (int g = 0; g < kZGroup; ++g)
+#pragma unroll
+            for (int k = 0; k < E; ++k)
+                w[g][k] = (z0 + g < nzb && zf[k] > -1e29f) ? zweight_f(bins, ch.zb0 + z0 + g, zf[k]) : 0.f;
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
-            const double *row = rows + (size_t) kn * a.grid.nv;
-            double base[QEPT];
+            const float *row = rows + (size_t) kn * a.grid.nv;
+            float base[E];
 #pragma unroll
-            for (int u = 0; u < QEPT; ++u)
-                base[u] = valid[u] ? row[nidx[u]] * (1 - dn[u]) + row[nidx[u] + 1] * dn[u] : 0.0;
-            for (int iz = 0; iz < nzb; ++iz) {
-                const int s = iz * ch.kbin_upp + kn, zm = ch.zb0 + iz;
-                double *Q = ws_d(a, ch.o_q) + (size_t) s * plane;
-                double part = 0.0;
+            for (int k = 0; k < E; ++k) base[k] = fmaf(row[nidx[k] + 1] - row[nidx[k]], dnf[k], row[nidx[k]]);
 #pragma unroll
-                for (int u = 0; u < QEPT; ++u) {
-                    const double q = valid[u] ? base[u] * zweight(bins, zm, zz[u]) : 0.0;
-                    part += yy[u] * q;
-                    Q[off[u]] = q;
+            for (int g = 0; g < kZGroup; ++g) {
+                if (z0 + g >= nzb) break;
+                const int s = (z0 + g) * ch.kbin_upp + kn;
+                const float qs = (float) qscale[s];
+                uint32_t *qh = reinterpret_cast<uint32_t *>(a.q_hi + (size_t) (ch.slot_q + s) * plane);
+                uint32_t *ql = reinterpret_cast<uint32_t *>(a.q_lo + (size_t) (ch.slot_q + s) * plane);
+                float fpart = 0.f;
+#pragma unroll
+                for (int u = 0; u < QM_PAIRS; ++u) {
+                    const float q0 = base[2 * u] * w[g][2 * u], q1 = base[2 * u + 1] * w[g][2 * u + 1];
+                    fpart = fmaf(yyf[2 * u], q0, fmaf(yyf[2 * u + 1], q1, fpart));
+                    if (!LQG_IN_BOUNDS(a, (size_t) (ch.slot_q + s) * plane + off[u] + 1 <
+                                              (size_t) a.total_slots_q * plane, 5, c, off[u]))
+                        continue;
+                    const __half2 hv = __floats2half2_rn(q0 * qs, q1 * qs);
+                    const float2 hf = __half22float2(hv);
+                    const __half2 lv = __floats2half2_rn(q0 * qs - hf.x, q1 * qs - hf.y);
+                    qh[off[u] / 2] = *reinterpret_cast<const uint32_t *>(&hv);
+                    ql[off[u] / 2] = *reinterpret_cast<const uint32_t *>(&lv);
                 }
-                part = warp_sum(part);
-                if (lane == 0) dpart[s] = part;
+                for (int o = 16; o > 0; o >>= 1) fpart += __shfl_down_sync(0xffffffffu, fpart, o);
+                if (lane == 0) dpart[s] = (double) fpart;
             }
         }
     }
@@ -403,7 +465,8 @@ __global__ void k_finish(WaveArgs a, int mixed) {
     for (int e = threadIdx.x; e < 3 * nq + nq * nq; e += blockDim.x) res[e] = 0.0;
     __syncthreads();
     if (a.status[ch.gidx] != LQG_CHUNK_OK) return;
-    const int ns = ch.ns, parts = (ch.ld / T64) * (ch.ld / T64) * 8;
+    // d partials: 8 warps per 64 x 64 tile (FP64 build) or per 32 x 64 half tile (mixed)
+    const int ns = ch.ns, parts = (ch.ld / T64) * (ch.ld / T64) * 8 * (mixed ? 2 : 1);
     const double *dpart = ws_d(a, ch.o_dpart);
     for (int s = threadIdx.x; s < ns; s += blockDim.x) {
         double acc = 0;
@@ -450,9 +513,9 @@ void launch_build_q(WaveArgs &a, cudaStream_t st) {
     int tiles = (a.max_ld / T64) * (a.max_ld / T64);
     if (a.precision == LQG_PRECISION_MIXED) {
         k_prep_mixed<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
-        k_build_q<true><<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
+        k_build_q_mixed<<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
     } else {
-        k_build_q<false><<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
+        k_build_q<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
         k_wn_fp64<<<dim3(64, a.n_chunks), 256, 0, st>>>(a);
     }
     a.launches += 2;

@@ -157,6 +157,28 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Store 32 consecutive fp32 columns of this warp's 32 lanes (waits for completion).
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
+    __syncwarp();
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+        "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+        "%30, %31, %32};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
+        "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
+        "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
+        "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
+        "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+        : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ double pow2_floor(double x) {
     if (!(x > 0) || !isfinite(x)) return 1.0;
     int e;
@@ -230,12 +252,13 @@ __device__ __forceinline__ void mma_drained(uint32_t tmem, unsigned char *smem, 
 }
 
 // Epilogue side of the drain: adds every drained hi*hi partial of this warp's
-// 32 lanes x 64 columns into sum (plain fp32, or Kahan-compensated with comp).
-// Returns false (warp-uniform) if a wait timed out or the CTA aborted.
+// 32 lanes x 64 columns into sum, in plain fp32 or Kahan-compensated with the
+// compensation kept in TMEM columns [384, 512) (registers are the limit: ten
+// warps leave 168 per thread).  Returns false (warp-uniform) if a wait timed
+// out or the CTA aborted.
 template <bool KAHAN>
 __device__ __forceinline__ bool drain_all(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
-                                          uint64_t *dempty, int kblocks, float (&sum)[64], float (&comp)[64],
-                                          int *abort_flag) {
+                                          uint64_t *dempty, int kblocks, float (&sum)[64], int *abort_flag) {
     const int ngroups = (kblocks + kDrain - 1) / kDrain;
     bool alive = true;
     for (int g = 0; g < ngroups; ++g) {
@@ -247,16 +270,26 @@ __device__ __forceinline__ bool drain_all(uint32_t tmem, uint32_t lane_addr, int
         for (int h = 0; h < 2; ++h) {
             float v[32];
             tmem_ld32(tmem + lane_addr + b * 128 + col0 + h * 32, v);
+            if (KAHAN) {
+                const uint32_t ca = tmem + lane_addr + 384 + col0 + h * 32;
+                float cp[32];
+                if (g == 0) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                if (KAHAN) {
-                    const float yv = v[j] - comp[h * 32 + j];
-                    const float t = sum[h * 32 + j] + yv;
-                    comp[h * 32 + j] = (t - sum[h * 32 + j]) - yv;
-                    sum[h * 32 + j] = t;
+                    for (int j = 0; j < 32; ++j) cp[j] = 0.f;
                 } else {
-                    sum[h * 32 + j] += v[j];
+                    tmem_ld32(ca, cp);
                 }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float yv = v[j] - cp[j];
+                    const float t = sum[h * 32 + j] + yv;
+                    cp[j] = (t - sum[h * 32 + j]) - yv;
+                    sum[h * 32 + j] = t;
+                }
+                tmem_st32(ca, cp);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) sum[h * 32 + j] += v[j];
             }
         }
         fence_before();
@@ -267,7 +300,7 @@ __device__ __forceinline__ bool drain_all(uint32_t tmem, uint32_t lane_addr, int
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __maxnreg__(200)
+__global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
           const __grid_constant__ CUtensorMap mc_lo, const __grid_constant__ CUtensorMap mq_hi,
           const __grid_constant__ CUtensorMap mq_lo) {
@@ -335,10 +368,10 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         // row-major (R) and transposed (P)
         const int quad = warp % 4, col0 = 64 * ((warp - 2) / 4);
         const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
-        float sum[64], comp[64];
+        float sum[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-        bool got = drain_all<false>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, comp, abort_flag);
+        bool got = drain_all<false>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, abort_flag);
         got = __all_sync(0xffffffffu, got && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
@@ -405,7 +438,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
 
 // ---------------------------------------------------------------------------
 // Gram block (bi, bj) of one chunk over one K split.
-__global__ void __maxnreg__(200)
+__global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_constant__ CUtensorMap mp_lo,
           const __grid_constant__ CUtensorMap mr_hi, const __grid_constant__ CUtensorMap mr_lo) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -470,10 +503,10 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         // 8 epilogue warps: lane quadrant warp % 4, columns 64 * ((warp - 2) / 4) + [0, 64)
         const int quad = warp % 4, half = (warp - 2) / 4;
         const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
-        float sum[64], comp[64];
+        float sum[64];
 #pragma unroll
-        for (int j = 0; j < 64; ++j) { sum[j] = 0.f; comp[j] = 0.f; }
-        const bool alive = drain_all<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, comp, abort_flag);
+        for (int j = 0; j < 64; ++j) sum[j] = 0.f;
+        const bool alive = drain_all<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, abort_flag);
         const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
@@ -483,8 +516,14 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             const bool out_ok = LQG_IN_BOUNDS(a, (int64_t) (obase + 64) <= a.gram_elems, 4, c, obase);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                float x[32];
+                float x[32], cp[32];
                 tmem_ld32(tmem + lane_addr + 2 * R_BN + half * 64 + h * 32, x);
+                if (kblocks > 0) {
+                    tmem_ld32(tmem + lane_addr + 384 + half * 64 + h * 32, cp);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) { x[j] = 0.f; cp[j] = 0.f; }
+                }
                 if (!out_ok) continue;
                 float4 *o = reinterpret_cast<float4 *>(a.gram_part + obase + h * 32);
 #pragma unroll
@@ -493,7 +532,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const int j = h * 32 + 4 * q + e;
-                        r4[e] = kblocks == 0 ? 0.f : (sum[j] - comp[j]) + x[4 * q + e];
+                        r4[e] = (sum[j] - cp[4 * q + e]) + x[4 * q + e];
                     }
                     o[q] = make_float4(r4[0], r4[1], r4[2], r4[3]);
                 }

@@ -24,7 +24,7 @@ struct lqg_ctx {
     std::vector<int> r_fwhm;
     std::vector<double> tdv, qmax, smax;
     TableGrid grid{};
-    DevBuf d_deriv, d_signal, d_bins;
+    DevBuf d_deriv, d_deriv_f, d_signal, d_bins;
     lqg_opts opts{};
     // batch
     struct HostChunk {
@@ -135,6 +135,11 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     lqg_ctx *c = ctx.get();
     if (ctx->d_deriv.alloc(nd * 8) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "tables");
     cudaMemcpy(ctx->d_deriv.p, tables->deriv, nd * 8, cudaMemcpyHostToDevice);
+    {
+        std::vector<float> df(tables->deriv, tables->deriv + nd);
+        if (ctx->d_deriv_f.alloc(nd * 4) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "tables");
+        cudaMemcpy(ctx->d_deriv_f.p, df.data(), nd * 4, cudaMemcpyHostToDevice);
+    }
     ctx->qmax.assign((size_t) tables->n_tables * bins->nk, 0.0);
     for (int t = 0; t < tables->n_tables; ++t)
         for (int k = 0; k < bins->nk; ++k) {
@@ -350,7 +355,7 @@ int64_t chunk_fws_bytes(int64_t ld) {
 // Wave workspace of one chunk in a wave with the given Gram blocking.
 int64_t chunk_ws_bytes(int64_t ld, int ns, int precision, int splits, int gt) {
     const int64_t m = ld * ld * 8, tiles = (ld / 64) * (ld / 64);
-    int64_t b = align_up(tiles * 8 * ns * 8, 256);
+    int64_t b = align_up(tiles * 16 * ns * 8, 256);
     const int64_t gblk = (int64_t) gt * gt * splits * 128 * 128;
     if (precision == LQG_PRECISION_FP64)
         b += align_up(gblk * 8, 256) + align_up(m * ns, 256) * 2 + align_up(m * (ns + 2), 256);
@@ -475,7 +480,7 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             int64_t off = 0;
             for (int k : w.members) {
                 ChunkDesc d = desc[g.desc_off + k];
-                d.o_dpart = off; off += align_up(tiles * 8 * d.ns * 8, 256);
+                d.o_dpart = off; off += align_up(tiles * 16 * d.ns * 8, 256);
                 if (precision == LQG_PRECISION_FP64) {
                     d.o_part = off; off += align_up(gblk * 8, 256);
                     d.o_q = off; off += align_up(m * d.ns, 256);
@@ -589,6 +594,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.wave = ctx->d_wave.as<double>(); base.delta = ctx->d_delta.as<double>(); base.ivar = ctx->d_ivar.as<double>();
     base.logw = ctx->d_logw.as<double>(); base.sqw = ctx->d_sqw.as<double>();
     base.deriv = ctx->d_deriv.as<double>();
+    base.deriv_f = ctx->d_deriv_f.as<float>();
     base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
     base.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
     base.results = ctx->d_results.as<double>();

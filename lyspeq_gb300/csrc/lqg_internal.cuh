@@ -86,6 +86,7 @@ struct WaveArgs {
     int gt;                      // Gram blocks of 128 per dimension (ns + 2 <= 128 gt)
     const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
     const double *deriv, *signal, *qmax;             // tables
+    const float *deriv_f;                            // float copy of deriv (mixed path)
     const double *theta;                             // device, nkz
     double *results;                                 // per-chunk results
     int *status;                                     // per-chunk status (wave-local)
