@@ -197,20 +197,14 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
 // Mixed variant: Q_s straight to fp16 hi/lo planes with the slot's power-of-two
 // scale.  The operands of a 22-bit split need no FP64: interpolation and
 // weights run in FP32 (GB300's FP64 rate is 1/60 of its FP32 rate) from a
-// float copy of the derivative table.  Each thread owns 4 column pairs of a
+// float copy of the derivative table.  The redshift weights are evaluated from
+// the FP64 z_ij (once per element and bin): a float z carries 2.4e-7 absolute
+// error, which is 1e-4 relative on the small weights near a bin's edge.
+// Each thread owns 4 column pairs of a
 // 32 x 64 half tile (one row per warp and pair step, stores of 128 B per warp);
 // redshift bins are taken kZGroup at a time with their weights in registers.
 constexpr int QM_PAIRS = 4;
 constexpr int kZGroup = 4;
-
-__device__ __forceinline__ float zweight_f(const DeviceBins &b, int zm, float z) {
-    const float zc = (float) b.z_centers[zm], dz = (float) b.dz;
-    if (!b.triangular || b.nz == 1) return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.f : 0.f;
-    if (zm == 0 && z < zc) return 1.f;
-    if (zm == b.nz - 1 && z > zc) return 1.f;
-    if (z >= zc - dz && z <= zc + dz) return 1.f - fabsf(z - zc) / dz;
-    return 0.f;
-}
 
 __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
     const int c = blockIdx.y;
@@ -225,7 +219,8 @@ __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
     const int nzb = ch.ns / ch.kbin_upp;
     constexpr int E = 2 * QM_PAIRS;
     int nidx[E];
-    float dnf[E], yyf[E], zf[E];
+    float dnf[E], yyf[E];
+    double zd[E];
     size_t off[QM_PAIRS];    // element offset of each pair's first element
 #pragma unroll
     for (int u = 0; u < QM_PAIRS; ++u) {
@@ -235,14 +230,14 @@ __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
             const int k = 2 * u + e, j = j0 + e;
-            nidx[k] = 0; dnf[k] = 0.f; yyf[k] = 0.f; zf[k] = -1e30f;
+            nidx[k] = 0; dnf[k] = 0.f; yyf[k] = 0.f; zd[k] = -1e30;
             if (i < n && j < n) {
                 const int lo = i < j ? i : j, hi = i < j ? j : i;
                 double v, z, dn;
                 vz_of(logw, sqw, lo, hi, v, z);
                 vindex(a.grid, v, nidx[k], dn);
                 dnf[k] = (float) dn;
-                zf[k] = (float) z;
+                zd[k] = z;
                 yyf[k] = (float) (y[i] * y[j]);
             }
         }
@@ -258,7 +253,7 @@ __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
         for (int g = 0; g < kZGroup; ++g)
 #pragma unroll
             for (int k = 0; k < E; ++k)
-                w[g][k] = (z0 + g < nzb && zf[k] > -1e29f) ? zweight_f(bins, ch.zb0 + z0 + g, zf[k]) : 0.f;
+                w[g][k] = (z0 + g < nzb && zd[k] > -1e29) ? (float) zweight(bins, ch.zb0 + z0 + g, zd[k]) : 0.f;
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
             const float *row = rows + (size_t) kn * a.grid.nv;
             float base[E];
