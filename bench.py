@@ -219,12 +219,9 @@ def main():
     def allreduce(out):
         if world == 1:
             return out
-        import torch.distributed as dist
-        buf = torch.from_numpy(np.concatenate([out["fisher"].ravel(), out["d"], out["b"], out["t"]])).cuda()
-        dist.all_reduce(buf)
-        v = buf.cpu().numpy()
-        return dict(fisher=v[:nkz * nkz].reshape(nkz, nkz), d=v[nkz * nkz:nkz * nkz + nkz],
-                    b=v[nkz * nkz + nkz:nkz * nkz + 2 * nkz], t=v[nkz * nkz + 2 * nkz:], status=out["status"])
+        from lyspeq_gb300.distributed import allreduce_sums
+        f, d, b, t = allreduce_sums(out["fisher"], out["d"], out["b"], out["t"], device=f"cuda:{local}")
+        return dict(fisher=f, d=d, b=b, t=t, status=out["status"])
 
     def step_resident():
         eng.iterate(precision="mixed")
