@@ -44,6 +44,7 @@ extern "C" {
 #define LQG_ERR_TIMEOUT -5      /* a bounded device wait gave up */
 #define LQG_ERR_UNSUPPORTED -6  /* option not implemented on this path */
 #define LQG_ERR_SINGULAR -7     /* global Fisher matrix could not be inverted */
+#define LQG_ERR_TOO_LARGE -8    /* size beyond a fixed limit of the entry point */
 
 /* per-chunk status */
 #define LQG_CHUNK_OK 0
@@ -170,6 +171,36 @@ int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n);
 
 /* Number of kernel launches the last lqg_nr_iteration enqueued. */
 int lqg_last_launch_count(const lqg_ctx *ctx);
+
+/* Factorisation of one chunk's covariance without allocating: no counterpart
+ * in the reference (there it is part of Chunk::setInvertCovarianceMatrix,
+ * _addMarginalizations and computePSbeforeFvector, core/chunk_estimate.cpp:
+ * 668-719, 576-665, 746-750, which use the glmemory pool).  For callers that
+ * cannot let a library call cudaMalloc/cudaFree (which may synchronise the
+ * device) or allocate from their memory pool: all buffers are the caller's
+ * device memory, and the only scratch is a fixed 2 MiB static device array per
+ * device.  Enqueued on `stream` (a cudaStream_t; NULL = legacy default stream);
+ * nothing is copied from or to the host and nothing is synchronised.
+ *   n, ld       pixels and leading dimension: ld % 64 == 0, n <= ld <= 4096
+ *               (larger: LQG_ERR_TOO_LARGE, checked before any device work)
+ *   cov         in: C = S + sum theta_k Q_k, symmetric n x n in an ld x ld
+ *               row-major buffer (padding ignored); out: C^-1 (ld x ld, zero
+ *               padding; masked pixels give zero rows and columns)
+ *   wave        lambda / lambda_Lya per pixel (the marginalisation templates)
+ *   delta, ivar flux contrast and inverse variance per pixel
+ *   cont_*      ContinuumLogLambdaMargOrder / ContinuumLambdaMargOrder
+ *               (at most 4 template vectors, else LQG_ERR_UNSUPPORTED)
+ *   y           out: C^-1 delta, ld values
+ *   status      device int, out: LQG_CHUNK_OK or LQG_CHUNK_NOT_SPD.  The call
+ *               sets it to LQG_CHUNK_OK first: nothing needs to start at zero.
+ * The static scratch is shared by every call on a device: two calls in flight
+ * at the same time (other streams, other host threads) race on it and give
+ * wrong results; order them (one stream, or events).  The first call on each
+ * device looks up the scratch address and sets a kernel attribute; make it
+ * before any stream capture. */
+int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave, const double *delta,
+                       const double *ivar, int cont_logl_order, int cont_l_order, double *y,
+                       int *status, void *stream);
 
 #ifdef __cplusplus
 }
