@@ -10,7 +10,8 @@
 // Every O(n^3) step is a sequence of 64 x 64 x 64 tile products staged in
 // shared memory (two K-major tiles), 256 threads with a 4 x 4 register block
 // each; rows {ti + 16u}, columns {tj + 16w} per thread keep shared-memory
-// reads conflict-free.
+// reads conflict-free.  The tile products run in FP64 for the FP64 path and
+// in double-float (df64, 48 bits) on the FP32 pipe for the mixed path.
 #include "lqg_internal.cuh"
 
 namespace lqg {
@@ -43,35 +44,97 @@ __device__ __forceinline__ double block_max_all(double v, double *red) {
     return s;
 }
 
-// Shared tile loaders.  K-major layout: t[k * FP + m].
+// Double-float (df64) form of a double: hi = fl32(v), lo = fl32(v - hi), 48
+// significant bits.  The mixed-precision path runs the O(n^3) tile products in
+// this form on the FP32 pipe (GB300's FP32 rate is 60x its FP64 rate).
+__device__ __forceinline__ float2 to_df(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double) h));
+}
+
+// Shared tile loaders.  K-major layout: t[k * FP + m] (a double, or a df64
+// float2 in the same 8 bytes when DF).
+template <bool DF>
+__device__ __forceinline__ void put(double *t, int idx, double v) {
+    if (DF) reinterpret_cast<float2 *>(t)[idx] = to_df(v);
+    else t[idx] = v;
+}
 // direct: t[k][m] = G[(r0 + k) * ld + c0 + m]  (rows of G are k)
+template <bool DF>
 __device__ __forceinline__ void load_direct(double *t, const double *G, int ld, int r0, int c0) {
     for (int e = threadIdx.x; e < FB * FB; e += FTH) {
         int k = e / FB, m = e % FB;
-        t[k * FP + m] = G[(size_t) (r0 + k) * ld + c0 + m];
+        put<DF>(t, k * FP + m, G[(size_t) (r0 + k) * ld + c0 + m]);
     }
 }
 // transposed: t[k][m] = G[(r0 + m) * ld + c0 + k]  (rows of G are m)
+template <bool DF>
 __device__ __forceinline__ void load_trans(double *t, const double *G, int ld, int r0, int c0) {
     for (int e = threadIdx.x; e < FB * FB; e += FTH) {
         int m = e / FB, k = e % FB;
-        t[k * FP + m] = G[(size_t) (r0 + m) * ld + c0 + k];
+        put<DF>(t, k * FP + m, G[(size_t) (r0 + m) * ld + c0 + k]);
+    }
+}
+// A tile of doubles already in shared memory, to df64 in place.
+__device__ __forceinline__ void tile_to_df(double *t) {
+    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+        const int idx = (e / FB) * FP + e % FB;
+        const double v = t[idx];
+        reinterpret_cast<float2 *>(t)[idx] = to_df(v);
     }
 }
 
 // acc[u][w] += sum_k A[k][ti + 16u] * B[k][tj + 16w]
+template <bool DF>
 __device__ __forceinline__ void tile_mma(double (&acc)[4][4], const double *A, const double *B, int klen) {
     const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    if (!DF) {
 #pragma unroll 4
-    for (int k = 0; k < klen; ++k) {
-        double a[4], b[4];
+        for (int k = 0; k < klen; ++k) {
+            double a[4], b[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) { a[u] = A[k * FP + ti + 16 * u]; b[u] = B[k * FP + tj + 16 * u]; }
+            for (int u = 0; u < 4; ++u) { a[u] = A[k * FP + ti + 16 * u]; b[u] = B[k * FP + tj + 16 * u]; }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
+        }
+        return;
+    }
+    // df64: each product a*b = p + e exactly up to the dropped lo*lo term
+    // (p = fl(hi*hi), e from an FMA), added to the running (hi, lo) sum by
+    // Knuth's two-sum; lo is renormalised once per call.  The _rn intrinsics
+    // keep the compiler from contracting the error-free transformations.
+    const float2 *A2 = reinterpret_cast<const float2 *>(A), *B2 = reinterpret_cast<const float2 *>(B);
+    float hi[4][4], lo[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) { hi[u][w] = 0.f; lo[u][w] = 0.f; }
+#pragma unroll 2
+    for (int k = 0; k < klen; ++k) {
+        float2 a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { a[u] = A2[k * FP + ti + 16 * u]; b[u] = B2[k * FP + tj + 16 * u]; }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int w = 0; w < 4; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
+            for (int w = 0; w < 4; ++w) {
+                const float p = __fmul_rn(a[u].x, b[w].x);
+                float e = __fmaf_rn(a[u].x, b[w].x, -p);
+                e = __fmaf_rn(a[u].x, b[w].y, e);
+                e = __fmaf_rn(a[u].y, b[w].x, e);
+                const float sum = __fadd_rn(hi[u][w], p);
+                const float bb = __fsub_rn(sum, hi[u][w]);
+                const float err = __fadd_rn(__fsub_rn(hi[u][w], __fsub_rn(sum, bb)), __fsub_rn(p, bb));
+                hi[u][w] = sum;
+                lo[u][w] = __fadd_rn(lo[u][w], __fadd_rn(err, e));
+            }
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) acc[u][w] += (double) hi[u][w] + (double) lo[u][w];
 }
 
 __device__ __forceinline__ void zero_acc(double (&acc)[4][4]) {
@@ -133,6 +196,7 @@ struct FactorSmem {
 };
 
 // Blocked Cholesky in place (lower triangle of A, ld x ld, first nb*64 rows).
+template <bool DF>
 __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
     for (int kb = 0; kb < nb; ++kb) {
         const int k0 = kb * FB;
@@ -155,15 +219,19 @@ __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
             }
         }
         __syncthreads();
+        if (DF) {
+            tile_to_df(s.b);
+            __syncthreads();
+        }
         // panel: L_ik = A_ik L_kk^-T, tile by tile
         for (int ib = kb + 1; ib < nb; ++ib) {
             const int i0 = ib * FB;
-            load_trans(s.a, A, ld, i0, k0);     // a[k][m] = A[i0 + m][k0 + k]
+            load_trans<DF>(s.a, A, ld, i0, k0);     // a[k][m] = A[i0 + m][k0 + k]
             __syncthreads();
             double acc[4][4];
             zero_acc(acc);
             // acc[m][j] = sum_k A[m][k] Linv[j][k]  with b[k][j] = Linv[j][k]
-            tile_mma(acc, s.a, s.b, FB);
+            tile_mma<DF>(acc, s.a, s.b, FB);
             __syncthreads();
             const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
 #pragma unroll
@@ -177,12 +245,12 @@ __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
         for (int ib = kb + 1; ib < nb; ++ib)
             for (int jb = kb + 1; jb <= ib; ++jb) {
                 const int i0 = ib * FB, j0 = jb * FB;
-                load_trans(s.a, A, ld, i0, k0);
-                load_trans(s.b, A, ld, j0, k0);
+                load_trans<DF>(s.a, A, ld, i0, k0);
+                load_trans<DF>(s.b, A, ld, j0, k0);
                 __syncthreads();
                 double acc[4][4];
                 zero_acc(acc);
-                tile_mma(acc, s.a, s.b, FB);
+                tile_mma<DF>(acc, s.a, s.b, FB);
                 const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
@@ -198,6 +266,7 @@ __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
 // In-place X = L^-1 (lower), row block by row block:
 //   X_II = L_II^-1;  X_IC = -X_II sum_{J=C}^{I-1} L_IJ X_JC   for C < I.
 // T = sum_J L_IJ X_JC is accumulated per column block into scratch (64 x ld).
+template <bool DF>
 __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &s) {
     const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
     for (int ib = 0; ib < nb; ++ib) {
@@ -207,10 +276,10 @@ __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &
             double acc[4][4];
             zero_acc(acc);
             for (int jb = cb; jb < ib; ++jb) {
-                load_trans(s.a, A, ld, i0, jb * FB);       // a[k][m] = L[i0+m][j0+k]
-                load_direct(s.b, A, ld, jb * FB, cb * FB);  // b[k][c] = X[j0+k][c0+c]
+                load_trans<DF>(s.a, A, ld, i0, jb * FB);       // a[k][m] = L[i0+m][j0+k]
+                load_direct<DF>(s.b, A, ld, jb * FB, cb * FB);  // b[k][c] = X[j0+k][c0+c]
                 __syncthreads();
-                tile_mma(acc, s.a, s.b, FB);
+                tile_mma<DF>(acc, s.a, s.b, FB);
                 __syncthreads();
             }
 #pragma unroll
@@ -229,16 +298,16 @@ __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &
         // a[k][m] = X_II[m][k]
         for (int e = threadIdx.x; e < FB * FB; e += FTH) {
             int m = e / FB, k = e % FB;
-            s.a[k * FP + m] = s.b[m * FP + k];
+            put<DF>(s.a, k * FP + m, s.b[m * FP + k]);
         }
         __syncthreads();
         // X_IC = -X_II T_C
         for (int cb = 0; cb < ib; ++cb) {
-            load_direct(s.b, T, ld, 0, cb * FB);           // b[k][c] = T[k][c0+c]
+            load_direct<DF>(s.b, T, ld, 0, cb * FB);           // b[k][c] = T[k][c0+c]
             __syncthreads();
             double acc[4][4];
             zero_acc(acc);
-            tile_mma(acc, s.a, s.b, FB);
+            tile_mma<DF>(acc, s.a, s.b, FB);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -251,6 +320,7 @@ __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &
 
 // In place: M = X^T X (lower tiles, row block by row block; within a row block the
 // off-diagonal tiles first), then C^-1 = D M D symmetric in the full ld x ld.
+template <bool DF>
 __device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *ivar, FactorSmem &s) {
     const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
     for (int ib = 0; ib < nb; ++ib) {
@@ -260,8 +330,8 @@ __device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *iv
                 double acc[4][4];
                 zero_acc(acc);
                 for (int lb = ib; lb < nb; ++lb) {
-                    load_direct(s.a, A, ld, lb * FB, ib * FB);   // a[l][i] = X[l0+l][i0+i]
-                    load_direct(s.b, A, ld, lb * FB, jb * FB);   // b[l][j] = X[l0+l][j0+j]
+                    load_direct<DF>(s.a, A, ld, lb * FB, ib * FB);   // a[l][i] = X[l0+l][i0+i]
+                    load_direct<DF>(s.b, A, ld, lb * FB, jb * FB);   // b[l][j] = X[l0+l][j0+j]
                     __syncthreads();
                     // X is lower triangular: zero its upper part inside the diagonal tiles
                     if (lb == ib)
@@ -275,7 +345,7 @@ __device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *iv
                             if (l < j) s.b[l * FP + j] = 0.0;
                         }
                     __syncthreads();
-                    tile_mma(acc, s.a, s.b, FB);
+                    tile_mma<DF>(acc, s.a, s.b, FB);
                     __syncthreads();
                 }
 #pragma unroll
@@ -365,7 +435,11 @@ __device__ void marginalize_all(double *A, int ld, int n, const double *wave, in
                     }
                 __syncthreads();
             }
-        if (!changed) break;
+        // every thread takes the flag before thread 0 may reset it for the
+        // next sweep: all threads must leave the loop at the same sweep
+        const int again = changed;
+        __syncthreads();
+        if (!again) break;
     }
     for (int p = 0; p < nv; ++p) {
         double part = 0;
@@ -411,6 +485,7 @@ __device__ void marginalize_all(double *A, int ld, int n, const double *wave, in
     }
 }
 
+template <bool DF>
 __global__ void __launch_bounds__(FTH) k_factor_tiled(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FactorSmem &s = *reinterpret_cast<FactorSmem *>(smem_raw);
@@ -420,19 +495,21 @@ __global__ void __launch_bounds__(FTH) k_factor_tiled(WaveArgs a) {
     const int ld = ch.ld, n = ch.n, nb = (n + FB - 1) / FB;
     if (!LQG_IN_BOUNDS(a, ch.o_c + (int64_t) ld * ld * 8 <= a.fws_bytes &&
                               ch.o_fscr + (int64_t) FB * ld * 8 <= a.fws_bytes &&
-                              ch.o_y + (int64_t) ld * 8 <= a.fws_bytes && nb * FB <= ld, 10, c, ch.o_fscr))
+                              ch.o_y + (int64_t) ld * 8 <= a.fws_bytes && nb * FB <= ld && ch.o_c >= 0 &&
+                              ch.o_fscr >= 0 && ch.o_y >= 0 && ch.pix >= 0 && ch.pix + n <= a.n_pix,
+                       10, c, ch.o_fscr))
         return;
     double *A = reinterpret_cast<double *>(a.fws + ch.o_c);
     double *scratch = reinterpret_cast<double *>(a.fws + ch.o_fscr);
     const double *iv = a.ivar + ch.pix;
-    if (!potrf_blocked(A, ld, nb, s)) {
+    if (!potrf_blocked<DF>(A, ld, nb, s)) {
         if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_NOT_SPD;
         return;
     }
     __syncthreads();
-    trtri_blocked(A, ld, nb, scratch, s);
+    trtri_blocked<DF>(A, ld, nb, scratch, s);
     __syncthreads();
-    lauum_blocked(A, ld, nb, n, iv, s);
+    lauum_blocked<DF>(A, ld, nb, n, iv, s);
     if (a.cont_logl >= 0 || a.cont_l >= 0)
         marginalize_all(A, ld, n, a.wave + ch.pix, a.cont_logl, a.cont_l, scratch, s);
     double *y = reinterpret_cast<double *>(a.fws + ch.o_y);
@@ -464,14 +541,22 @@ __global__ void __launch_bounds__(FTH) k_factor_tiled(WaveArgs a) {
 
 size_t factor_smem_bytes() { return sizeof(FactorSmem); }
 
+// The FP64 path factors in FP64 throughout; the mixed path runs the tile
+// products in df64 on the FP32 pipe (the diagonal-block Cholesky and inverse,
+// the scaling and the marginalisation stay FP64).
 void launch_factor_all(WaveArgs &a, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_factor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_factor_tiled<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int) sizeof(FactorSmem));
+        cudaFuncSetAttribute(k_factor_tiled<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int) sizeof(FactorSmem));
         attr = true;
     }
-    k_factor_tiled<<<a.n_chunks, FTH, sizeof(FactorSmem), st>>>(a);
+    if (a.precision == LQG_PRECISION_MIXED)
+        k_factor_tiled<true><<<a.n_chunks, FTH, sizeof(FactorSmem), st>>>(a);
+    else
+        k_factor_tiled<false><<<a.n_chunks, FTH, sizeof(FactorSmem), st>>>(a);
     a.launches++;
 }
 

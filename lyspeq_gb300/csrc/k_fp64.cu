@@ -89,6 +89,11 @@ __global__ void k_build_s_c(WaveArgs a) {
     const int tpr = ld / T64;
     if ((int) blockIdx.x >= tpr * tpr) return;
     const int ti = blockIdx.x / tpr, tj = blockIdx.x % tpr;
+    if (!LQG_IN_BOUNDS(a, ch.o_s >= 0 && ch.o_c >= 0 && ch.o_s + (int64_t) ld * ld * 8 <= a.fws_bytes &&
+                              ch.o_c + (int64_t) ld * ld * 8 <= a.fws_bytes && ch.pix >= 0 &&
+                              ch.pix + n <= a.n_pix && ld % T64 == 0 && n <= ld,
+                       11, c, ch.o_c))
+        return;
     double *S = fws_d(a, ch.o_s), *C = fws_d(a, ch.o_c);
     const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix, *iv = a.ivar + ch.pix;
     const double *stab = a.signal ? a.signal + (size_t) ch.res * a.grid.nv * a.grid.nzp : nullptr;

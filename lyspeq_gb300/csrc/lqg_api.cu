@@ -607,6 +607,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.skip_fisher = ctx->opts.skip_fisher;
     base.precision = precision;
     base.results_elems = ctx->results_size;
+    base.n_pix = (int64_t) ctx->h_wave.size();
     base.check = ctx->d_check.as<unsigned long long>();
 
     // LQG_SYNC_EACH=1: synchronise after every kernel and name the one that failed

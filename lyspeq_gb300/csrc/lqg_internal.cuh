@@ -102,7 +102,7 @@ struct WaveArgs {
     int launches;
     cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
     // extents of the buffers above, used by the LQG_CHECKED build to validate indices
-    int64_t ws_bytes, fws_bytes, results_elems, gram_elems;
+    int64_t ws_bytes, fws_bytes, results_elems, gram_elems, n_pix;
     unsigned long long *check;   // [0] violations, [1] first code, [2] first chunk, [3] first index
 };
 

@@ -119,6 +119,7 @@ extern "C" int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave
     a.cont_logl = cont_logl_order;
     a.cont_l = cont_l_order;
     a.precision = LQG_PRECISION_FP64;
+    a.n_pix = n;
     a.check = nullptr;
     launch_factor_all(a, st);
     return cudaGetLastError() == cudaSuccess ? LQG_OK : LQG_ERR_CUDA;
