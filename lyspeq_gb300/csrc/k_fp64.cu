@@ -75,6 +75,25 @@ __device__ __forceinline__ void vindex(const TableGrid &g, double v, int &n, dou
     dn = xx - n;
 }
 
+// Mixed-path variants: multiplication by precomputed reciprocals instead of
+// FP64 divisions (one rounding more, far below the 22-bit operands).
+__device__ __forceinline__ void vindex_rcp(const TableGrid &g, double inv_dv, double v, int &n, double &dn) {
+    double xx = (v - g.v1) * inv_dv;
+    n = (int) xx;
+    n = n < 0 ? 0 : (n >= g.nv - 1 ? g.nv - 2 : n);
+    dn = xx - n;
+}
+
+__device__ __forceinline__ double zweight_rcp(const DeviceBins &b, double inv_dz, int zm, double z) {
+    const double zc = b.z_centers[zm], dz = b.dz;
+    if (!b.triangular || b.nz == 1)
+        return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.0 : 0.0;
+    if (zm == 0 && z < zc) return 1.0;
+    if (zm == b.nz - 1 && z > zc) return 1.0;
+    const double u = fabs(z - zc);
+    return u <= dz ? 1.0 - u * inv_dz : 0.0;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
@@ -211,7 +230,7 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
 constexpr int QM_PAIRS = 4;
 constexpr int kZGroup = 4;
 
-__global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
+__global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     const int c = blockIdx.y;
     const ChunkDesc &ch = a.chunks[c];
     const int ld = ch.ld, n = ch.n, tpr = ld / T64;
@@ -222,6 +241,7 @@ __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
     const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix;
     const double *y = fws_d(a, ch.o_y);
     const int nzb = ch.ns / ch.kbin_upp;
+    const double inv_dv = 1.0 / a.grid.dv, inv_dz = 1.0 / bins.dz;
     constexpr int E = 2 * QM_PAIRS;
     int nidx[E];
     float dnf[E], yyf[E];
@@ -240,7 +260,7 @@ __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
                 const int lo = i < j ? i : j, hi = i < j ? j : i;
                 double v, z, dn;
                 vz_of(logw, sqw, lo, hi, v, z);
-                vindex(a.grid, v, nidx[k], dn);
+                vindex_rcp(a.grid, inv_dv, v, nidx[k], dn);
                 dnf[k] = (float) dn;
                 zd[k] = z;
                 yyf[k] = (float) (y[i] * y[j]);
@@ -258,7 +278,8 @@ __global__ void __launch_bounds__(256) k_build_q_mixed(WaveArgs a) {
         for (int g = 0; g < kZGroup; ++g)
 #pragma unroll
             for (int k = 0; k < E; ++k)
-                w[g][k] = (z0 + g < nzb && zd[k] > -1e29) ? (float) zweight(bins, ch.zb0 + z0 + g, zd[k]) : 0.f;
+                w[g][k] = (z0 + g < nzb && zd[k] > -1e29) ? (float) zweight_rcp(bins, inv_dz, ch.zb0 + z0 + g, zd[k])
+                                                          : 0.f;
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
             const float *row = rows + (size_t) kn * a.grid.nv;
             float base[E];
@@ -325,8 +346,9 @@ __global__ void k_prep_mixed(WaveArgs a) {
         double nw = (i < n && iv[i] != 0.0) ? 1.0 / iv[i] : 0.0;
         float xw = (float) (nw * cv * wsc);
         __half hw = __float2half_rn(xw);
-        a.p_hi[(size_t) (ch.slot_p + ch.ns + 1) * plane + idx] = hw;
-        a.p_lo[(size_t) (ch.slot_p + ch.ns + 1) * plane + idx] = __float2half_rn(xw - __half2float(hw));
+        const size_t pidx = kblocked(idx, ch.slot_p + ch.ns + 1, a.total_slots_p);
+        a.p_hi[pidx] = hw;
+        a.p_lo[pidx] = __float2half_rn(xw - __half2float(hw));
     }
 }
 

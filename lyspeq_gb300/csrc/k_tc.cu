@@ -382,8 +382,8 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const double ps = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
             const float mult = (float) (ps / (sc * qs));
             const size_t plane = (size_t) ld * ld;
-            __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
-            __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
+            (void) plane;
+            const int rslot = ch.slot_r + s, pslot = ch.slot_p + s;
             const bool write_r = s < ch.ns;
             const bool slots_ok = LQG_IN_BOUNDS(a, (!write_r || ch.slot_r + s < a.total_slots_r) &&
                                                      ch.slot_p + s < a.total_slots_p, 2, c, s);
@@ -406,22 +406,28 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
                     lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
                 }
                 if (write_r) {
-                    uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
-                    uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
+                    // 32 consecutive k of one slot: contiguous in the K-blocked layout
+                    const size_t o = kblocked((size_t) row * ld + cb, rslot, a.total_slots_r);
+                    uint4 *dh = reinterpret_cast<uint4 *>(a.r_hi + o);
+                    uint4 *dl = reinterpret_cast<uint4 *>(a.r_lo + o);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
                         dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
                     }
                 }
-                unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
-                unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
+                // transposed: element (col, row) of A_s^T; the warp's 32 rows are 32
+                // consecutive k of one K block
+                unsigned short *ph = reinterpret_cast<unsigned short *>(a.p_hi);
+                unsigned short *pl = reinterpret_cast<unsigned short *>(a.p_lo);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    ph[(size_t) (cb + 2 * j) * ld] = (unsigned short) (hp[j] & 0xffffu);
-                    ph[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (hp[j] >> 16);
-                    pl[(size_t) (cb + 2 * j) * ld] = (unsigned short) (lp[j] & 0xffffu);
-                    pl[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (lp[j] >> 16);
+                    const size_t o0 = kblocked((size_t) (cb + 2 * j) * ld + row, pslot, a.total_slots_p);
+                    const size_t o1 = kblocked((size_t) (cb + 2 * j + 1) * ld + row, pslot, a.total_slots_p);
+                    ph[o0] = (unsigned short) (hp[j] & 0xffffu);
+                    ph[o1] = (unsigned short) (hp[j] >> 16);
+                    pl[o0] = (unsigned short) (lp[j] & 0xffffu);
+                    pl[o1] = (unsigned short) (lp[j] >> 16);
                 }
             }
         }
@@ -486,12 +492,15 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             const int st = kb % R_STAGES;
             if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
             unsigned char *sb = smem + st * R_STAGE_BYTES;
-            const int x = (int) (k_lo + (int64_t) kb * BK);
+            // K block kg of 128 consecutive slots: rows kg * total_slots + slot of
+            // the K-blocked stacks (rows past the chunk's slots are not used)
+            const int64_t kg = k_lo / BK + kb;
+            const int yp = (int) (kg * a.total_slots_p + prow), yr = (int) (kg * a.total_slots_r + rrow);
             mbar_expect_tx(&full[st], R_STAGE_BYTES);
-            tma_load_2d(sb, &mp_hi, &full[st], x, prow);
-            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], x, prow);
-            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], x, rrow);
-            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], x, rrow);
+            tma_load_2d(sb, &mp_hi, &full[st], 0, yp);
+            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], 0, yp);
+            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], 0, yr);
+            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], 0, yr);
             ++issued;
         }
         for (int kb = (issued > R_STAGES ? issued - R_STAGES : 0); kb < issued; ++kb)
@@ -639,9 +648,10 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     CUtensorMap mcl = make_map(a.c_lo, 3, d3c, s3, boxa, &ok);
     CUtensorMap mqh = make_map(a.q_hi, 3, d3q, s3, boxb, &ok);
     CUtensorMap mql = make_map(a.q_lo, 3, d3q, s3, boxb, &ok);
-    cuuint64_t d2p[2] = {plane, (cuuint64_t) a.total_slots_p};
-    cuuint64_t d2r[2] = {plane, (cuuint64_t) a.total_slots_r};
-    cuuint64_t s2[1] = {plane * 2};
+    // K-blocked stacks: rows of 64 halves, (ld^2 / 64) * total_slots rows
+    cuuint64_t d2p[2] = {(cuuint64_t) BK, plane / BK * (cuuint64_t) a.total_slots_p};
+    cuuint64_t d2r[2] = {(cuuint64_t) BK, plane / BK * (cuuint64_t) a.total_slots_r};
+    cuuint64_t s2[1] = {(cuuint64_t) BK * 2};
     cuuint32_t box2[2] = {BK, R_BM};
     CUtensorMap mph = make_map(a.p_hi, 2, d2p, s2, box2, &ok);
     CUtensorMap mpl = make_map(a.p_lo, 2, d2p, s2, box2, &ok);
