@@ -343,7 +343,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f16x3 products / f64 factorisation", "data": "synthetic (seeded)",
+        "vs_baseline": None, "dtype": "f16x3 products / df64 factorisation", "data": "synthetic (seeded)",
         "config": {"workload": f"{args.workload}: {n_ok} chunks, N log-uniform 200-1200, dv 50 km/s, "
                                "R 2000-5000, 35 k x 13 z bins, amplitude+slope marginalisation",
                    "l2": "working set of tens of GB per iteration (>> 129 MB L2); no flush"},

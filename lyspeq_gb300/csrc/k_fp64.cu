@@ -346,9 +346,8 @@ __global__ void k_prep_mixed(WaveArgs a) {
         double nw = (i < n && iv[i] != 0.0) ? 1.0 / iv[i] : 0.0;
         float xw = (float) (nw * cv * wsc);
         __half hw = __float2half_rn(xw);
-        const size_t pidx = kblocked(idx, ch.slot_p + ch.ns + 1, a.total_slots_p);
-        a.p_hi[pidx] = hw;
-        a.p_lo[pidx] = __float2half_rn(xw - __half2float(hw));
+        a.p_hi[(size_t) (ch.slot_p + ch.ns + 1) * plane + idx] = hw;
+        a.p_lo[(size_t) (ch.slot_p + ch.ns + 1) * plane + idx] = __float2half_rn(xw - __half2float(hw));
     }
 }
 

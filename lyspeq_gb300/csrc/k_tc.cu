@@ -22,6 +22,7 @@
 // error in the chunk status and leaves after its own work has drained.
 #include "lqg_internal.cuh"
 
+#include <algorithm>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -215,24 +216,27 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// MMA issuer of both kernels: for drain group g (kDrain K blocks), accumulate
-// hi*hi into buffer g & 1 (fresh per group) and the cross terms into the third
-// buffer (fresh at the first K block).  Stage layout: A hi, A lo, B hi, B lo.
+// MMA issuer, one output tile: for each drain group (kDrain K blocks)
+// accumulate hi*hi into hi*hi buffer (g_all & 1) of [thh, thh + 2 BN), fresh
+// per group, and the cross terms into tx, fresh at the tile's first K block.
+// kb_all (shared-memory stage ring) and g_all (hi*hi buffers) run on across
+// the tiles of a persistent CTA.  Commits `done` after the tile's last MMA.
+// Returns false after a timed-out wait (abort flag set).
+// Stage layout: A hi, A lo, B hi, B lo.
 template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN>
-__device__ __forceinline__ void mma_drained(uint32_t tmem, unsigned char *smem, uint64_t *full, uint64_t *empty,
-                                            uint64_t *dfull, uint64_t *dempty, uint64_t *accum, int kblocks,
-                                            uint32_t idesc, int *abort_flag) {
+__device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned char *smem, uint64_t *full,
+                                         uint64_t *empty, uint64_t *dfull, uint64_t *dempty, uint64_t *done,
+                                         int kblocks, uint32_t idesc, int &kb_all, int &g_all, int *abort_flag) {
     const int ngroups = (kblocks + kDrain - 1) / kDrain;
-    bool ok = true;
-    for (int g = 0; g < ngroups && ok; ++g) {
-        const int b = g & 1;
-        if (g >= 2 && !mbar_wait(&dempty[b], ((g >> 1) - 1) & 1)) { *abort_flag = 1; break; }
+    for (int g = 0; g < ngroups; ++g) {
+        const int b = g_all & 1;
+        if (g_all >= 2 && !mbar_wait(&dempty[b], ((g_all >> 1) - 1) & 1)) { *abort_flag = 1; return false; }
         fence_after();
-        const uint32_t thh = tmem + b * BN, tx = tmem + 2 * BN;
+        const uint32_t th = thh + b * BN;
         const int kb_end = min(kblocks, (g + 1) * kDrain);
         for (int kb = g * kDrain; kb < kb_end; ++kb) {
-            const int st = kb % STAGES;
-            if (!mbar_wait(&full[st], (kb / STAGES) & 1)) { *abort_flag = 1; ok = false; break; }
+            const int st = kb_all % STAGES;
+            if (!mbar_wait(&full[st], (kb_all / STAGES) & 1)) { *abort_flag = 1; return false; }
             fence_after();
             unsigned char *sb = smem + st * STAGE_BYTES;
             const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + TILE_A);
@@ -240,30 +244,35 @@ __device__ __forceinline__ void mma_drained(uint32_t tmem, unsigned char *smem, 
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
                 const uint64_t adv = (uint64_t) (kk * 32) >> 4;
-                umma_f16(thh, ah + adv, bh + adv, idesc, (kb > g * kDrain || kk > 0));
+                umma_f16(th, ah + adv, bh + adv, idesc, (kb > g * kDrain || kk > 0));
                 umma_f16(tx, ah + adv, bl + adv, idesc, (kb | kk) != 0);
                 umma_f16(tx, al + adv, bh + adv, idesc, 1);
             }
             umma_commit(&empty[st]);
+            ++kb_all;
         }
         umma_commit(&dfull[b]);
+        ++g_all;
     }
-    umma_commit(accum);
+    umma_commit(done);
+    return true;
 }
 
-// Epilogue side of the drain: adds every drained hi*hi partial of this warp's
-// 32 lanes x 64 columns into sum, in plain fp32 or Kahan-compensated with the
-// compensation kept in TMEM columns [384, 512) (registers are the limit: ten
-// warps leave 168 per thread).  Returns false (warp-uniform) if a wait timed
-// out or the CTA aborted.
+// Epilogue side of the drains of one tile: adds every drained hi*hi partial
+// of this warp's 32 lanes x 64 columns into sum, in plain fp32 or
+// Kahan-compensated with the compensation kept in TMEM columns [384, 512)
+// (registers are the limit: ten warps leave 168 per thread).  g_all runs on
+// across tiles like the issuer's.  Returns false (warp-uniform) if a wait
+// timed out or the CTA aborted.
 template <bool KAHAN>
-__device__ __forceinline__ bool drain_all(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
-                                          uint64_t *dempty, int kblocks, float (&sum)[64], int *abort_flag) {
+__device__ __forceinline__ bool drain_tile(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
+                                           uint64_t *dempty, int kblocks, float (&sum)[64], int &g_all,
+                                           int *abort_flag) {
     const int ngroups = (kblocks + kDrain - 1) / kDrain;
     bool alive = true;
     for (int g = 0; g < ngroups; ++g) {
-        const int b = g & 1;
-        alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g >> 1) & 1)) && !*abort_flag;
+        const int b = g_all & 1;
+        alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g_all >> 1) & 1)) && !*abort_flag;
         if (!alive) break;
         fence_after();
 #pragma unroll
@@ -295,11 +304,29 @@ __device__ __forceinline__ bool drain_all(uint32_t tmem, uint32_t lane_addr, int
         fence_before();
         __syncwarp();
         if ((threadIdx.x & 31) == 0) mbar_arrive(&dempty[b]);
+        ++g_all;
     }
     return alive;
 }
 
 // ---------------------------------------------------------------------------
+// Persistent GEMM: one CTA per SM walks the tiles t = blockIdx.x + i gridDim.x
+// of the wave (tile t: job t / tiles_per_job, i.e. (chunk, slot), and one
+// 128 x 128 output tile of A_s).  The TMA ring, the hi*hi drain groups and
+// their barrier parities run on across tiles; the cross-term accumulator
+// alternates between two TMEM buffers, so that the epilogue of tile t
+// (conversion and stores) overlaps the MMAs of tile t + 1.
+// TMEM: hi*hi ping [0, 128), pong [128, 256), cross [256, 384) and [384, 512).
+struct GemmTile {
+    int c, s, m0, n0;
+};
+
+__device__ __forceinline__ GemmTile gemm_tile(const int *jobs, long long t, int mt) {
+    const long long tpj = (long long) mt * mt;
+    const int job = (int) (t / tpj), tix = (int) (t % tpj);
+    return GemmTile{jobs[2 * job], jobs[2 * job + 1], (tix % mt) * G_BM, (tix / mt) * G_BN};
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
           const __grid_constant__ CUtensorMap mc_lo, const __grid_constant__ CUtensorMap mq_hi,
@@ -311,25 +338,27 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     uint64_t *empty = full + G_STAGES;
     uint64_t *dfull = empty + G_STAGES;
     uint64_t *dempty = dfull + 2;
-    uint64_t *accum = dempty + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
+    uint64_t *xfull = dempty + 2;
+    uint64_t *xempty = xfull + 2;
+    uint64_t *mdone = xempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
 
-    const int job = blockIdx.y;
-    if (job >= njobs) return;
-    const int c = jobs[2 * job], s = jobs[2 * job + 1];
-    const ChunkDesc &ch = a.chunks[c];
-    const int ld = ch.ld;
-    const int mt = (ld + G_BM - 1) / G_BM, nt = (ld + G_BN - 1) / G_BN;
-    if ((int) blockIdx.x >= mt * nt || a.status[ch.gidx] != LQG_CHUNK_OK) return;
-    const int m0 = (blockIdx.x % mt) * G_BM, n0 = (blockIdx.x / mt) * G_BN;
+    const int ld = a.max_ld;
+    const int mt = (ld + G_BM - 1) / G_BM;
+    const long long total = (long long) njobs * mt * mt;
     const int kblocks = ld / BK;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < G_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
-        for (int i = 0; i < 2; ++i) { mbar_init(&dfull[i], 1); mbar_init(&dempty[i], 8); }
-        mbar_init(accum, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&dfull[i], 1);
+            mbar_init(&dempty[i], 8);
+            mbar_init(&xfull[i], 1);
+            mbar_init(&xempty[i], 8);
+        }
+        mbar_init(mdone, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -341,64 +370,88 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
 
     if (warp == 0 && lane == 0) {
         // TMA producer
-        const int qslot = ch.slot_q + s;
-        int issued = 0;
-        if (!LQG_IN_BOUNDS(a, c < a.n_chunks && qslot >= 0 && qslot < a.total_slots_q && m0 < ld && n0 < ld,
-                           1, c, qslot))
-            *abort_flag = 1;
-        for (int kb = 0; kb < kblocks && !*abort_flag; ++kb) {
-            const int st = kb % G_STAGES;
-            if (!mbar_wait(&empty[st], ((kb / G_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
-            unsigned char *sb = smem + st * G_STAGE_BYTES;
-            mbar_expect_tx(&full[st], G_STAGE_BYTES);
-            tma_load_3d(sb, &mc_hi, &full[st], kb * BK, m0, c);
-            tma_load_3d(sb + G_TILE_A, &mc_lo, &full[st], kb * BK, m0, c);
-            tma_load_3d(sb + 2 * G_TILE_A, &mq_hi, &full[st], kb * BK, n0, qslot);
-            tma_load_3d(sb + 2 * G_TILE_A + G_TILE_B, &mq_lo, &full[st], kb * BK, n0, qslot);
-            ++issued;
+        int kb_all = 0;
+        for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+            const GemmTile tl = gemm_tile(jobs, t, mt);
+            const int qslot = a.chunks[tl.c].slot_q + tl.s;
+            if (!LQG_IN_BOUNDS(a, tl.c >= 0 && tl.c < a.n_chunks && qslot >= 0 && qslot < a.total_slots_q &&
+                                      tl.m0 < ld && tl.n0 < ld && a.chunks[tl.c].ld == ld,
+                               1, tl.c, qslot)) {
+                *abort_flag = 1;
+                break;
+            }
+            for (int kb = 0; kb < kblocks; ++kb) {
+                const int st = kb_all % G_STAGES;
+                if (!mbar_wait(&empty[st], ((kb_all / G_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
+                unsigned char *sb = smem + st * G_STAGE_BYTES;
+                mbar_expect_tx(&full[st], G_STAGE_BYTES);
+                tma_load_3d(sb, &mc_hi, &full[st], kb * BK, tl.m0, tl.c);
+                tma_load_3d(sb + G_TILE_A, &mc_lo, &full[st], kb * BK, tl.m0, tl.c);
+                tma_load_3d(sb + 2 * G_TILE_A, &mq_hi, &full[st], kb * BK, tl.n0, qslot);
+                tma_load_3d(sb + 2 * G_TILE_A + G_TILE_B, &mq_lo, &full[st], kb * BK, tl.n0, qslot);
+                ++kb_all;
+            }
         }
-        // drain: every issued stage must land before the CTA may leave
-        for (int kb = (issued > G_STAGES ? issued - G_STAGES : 0); kb < issued; ++kb)
-            mbar_wait(&full[kb % G_STAGES], (kb / G_STAGES) & 1);
+        // every issued stage must land before the CTA may leave
+        for (int k = (kb_all > G_STAGES ? kb_all - G_STAGES : 0); k < kb_all; ++k)
+            mbar_wait(&full[k % G_STAGES], (k / G_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
-        mma_drained<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN>(tmem, smem, full, empty, dfull, dempty, accum,
-                                                                     kblocks, idesc_f16(G_BM, G_BN), abort_flag);
+        // MMA issuer
+        int kb_all = 0, g_all = 0, lt = 0;
+        for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x, ++lt) {
+            const int x = lt & 1;
+            if (lt >= 2 && !mbar_wait(&xempty[x], ((lt >> 1) - 1) & 1)) { *abort_flag = 1; break; }
+            fence_after();
+            if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN>(
+                    tmem, tmem + 2 * G_BN + x * G_BN, smem, full, empty, dfull, dempty, &xfull[x], kblocks,
+                    idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag))
+                break;
+        }
+        // every MMA of this CTA completes before its tensor memory is freed
+        umma_commit(mdone);
+        mbar_wait(mdone, 0);
     } else if (warp >= 2) {
         // epilogue: drained sums + cross terms -> scaled fp16 hi/lo planes,
         // row-major (R) and transposed (P)
         const int quad = warp % 4, col0 = 64 * ((warp - 2) / 4);
         const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
-        float sum[64];
+        const size_t plane = (size_t) ld * ld;
+        const int nq4 = 4 * a.n_chunks;
+        int g_all = 0, lt = 0;
+        for (long long t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
+            const GemmTile tl = gemm_tile(jobs, t, mt);
+            const ChunkDesc &ch = a.chunks[tl.c];
+            float sum[64];
 #pragma unroll
-        for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-        bool got = drain_all<false>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, abort_flag);
-        got = __all_sync(0xffffffffu, got && mbar_wait(accum, 0)) && !*abort_flag;
-        fence_after();
-        if (got) {
-            const int row = m0 + quad * 32 + lane;
-            const int nq4 = 4 * a.n_chunks;
-            const double sc = a.scales[4 * c + 2];
+            for (int j = 0; j < 64; ++j) sum[j] = 0.f;
+            bool got = drain_tile<false>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, g_all, abort_flag);
+            const int x = lt & 1;
+            got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1)) && !*abort_flag;
+            if (!got) break;
+            fence_after();
+            const int row = tl.m0 + quad * 32 + lane;
+            const int s = tl.s;
+            const double sc = a.scales[4 * tl.c + 2];
             const double qs = a.scales[nq4 + ch.slot_q + s];
             const double ps = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
             const float mult = (float) (ps / (sc * qs));
-            const size_t plane = (size_t) ld * ld;
-            (void) plane;
-            const int rslot = ch.slot_r + s, pslot = ch.slot_p + s;
+            __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
+            __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
             const bool write_r = s < ch.ns;
             const bool slots_ok = LQG_IN_BOUNDS(a, (!write_r || ch.slot_r + s < a.total_slots_r) &&
-                                                     ch.slot_p + s < a.total_slots_p, 2, c, s);
+                                                     ch.slot_p + s < a.total_slots_p, 2, tl.c, s);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int cb = n0 + col0 + h * 32;
-                float x[32];
-                tmem_ld32(tmem + lane_addr + 2 * G_BN + col0 + h * 32, x);
+                const int cb = tl.n0 + col0 + h * 32;
+                float xv[32];
+                tmem_ld32(tmem + lane_addr + 2 * G_BN + x * G_BN + col0 + h * 32, xv);
                 if (!slots_ok || cb >= ld || row >= ld) continue;
                 // hi/lo pairs packed in registers (two halves per 32-bit word)
                 uint32_t hp[16], lp[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    const float v0 = (sum[h * 32 + 2 * j] + x[2 * j]) * mult;
-                    const float v1 = (sum[h * 32 + 2 * j + 1] + x[2 * j + 1]) * mult;
+                    const float v0 = (sum[h * 32 + 2 * j] + xv[2 * j]) * mult;
+                    const float v1 = (sum[h * 32 + 2 * j + 1] + xv[2 * j + 1]) * mult;
                     const __half2 hv = __floats2half2_rn(v0, v1);
                     const float2 hf = __half22float2(hv);
                     const __half2 lv = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
@@ -406,30 +459,28 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
                     lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
                 }
                 if (write_r) {
-                    // 32 consecutive k of one slot: contiguous in the K-blocked layout
-                    const size_t o = kblocked((size_t) row * ld + cb, rslot, a.total_slots_r);
-                    uint4 *dh = reinterpret_cast<uint4 *>(a.r_hi + o);
-                    uint4 *dl = reinterpret_cast<uint4 *>(a.r_lo + o);
+                    uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
+                    uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
                         dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
                     }
                 }
-                // transposed: element (col, row) of A_s^T; the warp's 32 rows are 32
-                // consecutive k of one K block
-                unsigned short *ph = reinterpret_cast<unsigned short *>(a.p_hi);
-                unsigned short *pl = reinterpret_cast<unsigned short *>(a.p_lo);
+                unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
+                unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    const size_t o0 = kblocked((size_t) (cb + 2 * j) * ld + row, pslot, a.total_slots_p);
-                    const size_t o1 = kblocked((size_t) (cb + 2 * j + 1) * ld + row, pslot, a.total_slots_p);
-                    ph[o0] = (unsigned short) (hp[j] & 0xffffu);
-                    ph[o1] = (unsigned short) (hp[j] >> 16);
-                    pl[o0] = (unsigned short) (lp[j] & 0xffffu);
-                    pl[o1] = (unsigned short) (lp[j] >> 16);
+                    ph[(size_t) (cb + 2 * j) * ld] = (unsigned short) (hp[j] & 0xffffu);
+                    ph[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (hp[j] >> 16);
+                    pl[(size_t) (cb + 2 * j) * ld] = (unsigned short) (lp[j] & 0xffffu);
+                    pl[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (lp[j] >> 16);
                 }
             }
+            // this cross buffer may now be taken by tile lt + 2
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&xempty[x]);
         }
     }
     fence_before();
@@ -438,9 +489,10 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         fence_after();
         tmem_dealloc(tmem, 512);
     }
-    if (threadIdx.x == 0 && *abort_flag) atomicExch(&a.status[ch.gidx], LQG_CHUNK_TIMEOUT);
+    if (threadIdx.x == 0 && *abort_flag)
+        for (long long t = blockIdx.x; t < total; t += gridDim.x)
+            atomicExch(&a.status[a.chunks[gemm_tile(jobs, t, mt).c].gidx], LQG_CHUNK_TIMEOUT);
 }
-
 
 // ---------------------------------------------------------------------------
 // Gram block (bi, bj) of one chunk over one K split.
@@ -455,7 +507,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     uint64_t *dfull = empty + R_STAGES;      // [2] hi*hi buffer ready to drain
     uint64_t *dempty = dfull + 2;            // [2] hi*hi buffer drained
     uint64_t *accum = dempty + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
+    uint64_t *mdone = accum + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
 
     const int c = blockIdx.y, sp = blockIdx.x, blk = blockIdx.z;
@@ -474,6 +527,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         for (int i = 0; i < R_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
         for (int i = 0; i < 2; ++i) { mbar_init(&dfull[i], 1); mbar_init(&dempty[i], 8); }
         mbar_init(accum, 1);
+        mbar_init(mdone, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -492,22 +546,24 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             const int st = kb % R_STAGES;
             if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
             unsigned char *sb = smem + st * R_STAGE_BYTES;
-            // K block kg of 128 consecutive slots: rows kg * total_slots + slot of
-            // the K-blocked stacks (rows past the chunk's slots are not used)
-            const int64_t kg = k_lo / BK + kb;
-            const int yp = (int) (kg * a.total_slots_p + prow), yr = (int) (kg * a.total_slots_r + rrow);
+            const int x = (int) (k_lo + (int64_t) kb * BK);
             mbar_expect_tx(&full[st], R_STAGE_BYTES);
-            tma_load_2d(sb, &mp_hi, &full[st], 0, yp);
-            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], 0, yp);
-            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], 0, yr);
-            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], 0, yr);
+            tma_load_2d(sb, &mp_hi, &full[st], x, prow);
+            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], x, prow);
+            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], x, rrow);
+            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], x, rrow);
             ++issued;
         }
         for (int kb = (issued > R_STAGES ? issued - R_STAGES : 0); kb < issued; ++kb)
             mbar_wait(&full[kb % R_STAGES], (kb / R_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
-        mma_drained<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN>(tmem, smem, full, empty, dfull, dempty, accum,
-                                                                  kblocks, idesc_f16(R_BM, R_BN), abort_flag);
+        int kb_all = 0, g_all = 0;
+        mma_tile<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN>(tmem, tmem + 2 * R_BN, smem, full, empty, dfull,
+                                                               dempty, accum, kblocks, idesc_f16(R_BM, R_BN),
+                                                               kb_all, g_all, abort_flag);
+        // every MMA completes before the tensor memory is freed
+        umma_commit(mdone);
+        mbar_wait(mdone, 0);
     } else if (warp >= 2) {
         // 8 epilogue warps: lane quadrant warp % 4, columns 64 * ((warp - 2) / 4) + [0, 64)
         const int quad = warp % 4, half = (warp - 2) / 4;
@@ -515,7 +571,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         float sum[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-        const bool alive = drain_all<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, abort_flag);
+        int g_all = 0;
+        const bool alive = drain_tile<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, g_all, abort_flag);
         const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
@@ -648,10 +705,9 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     CUtensorMap mcl = make_map(a.c_lo, 3, d3c, s3, boxa, &ok);
     CUtensorMap mqh = make_map(a.q_hi, 3, d3q, s3, boxb, &ok);
     CUtensorMap mql = make_map(a.q_lo, 3, d3q, s3, boxb, &ok);
-    // K-blocked stacks: rows of 64 halves, (ld^2 / 64) * total_slots rows
-    cuuint64_t d2p[2] = {(cuuint64_t) BK, plane / BK * (cuuint64_t) a.total_slots_p};
-    cuuint64_t d2r[2] = {(cuuint64_t) BK, plane / BK * (cuuint64_t) a.total_slots_r};
-    cuuint64_t s2[1] = {(cuuint64_t) BK * 2};
+    cuuint64_t d2p[2] = {plane, (cuuint64_t) a.total_slots_p};
+    cuuint64_t d2r[2] = {plane, (cuuint64_t) a.total_slots_r};
+    cuuint64_t s2[1] = {plane * 2};
     cuuint32_t box2[2] = {BK, R_BM};
     CUtensorMap mph = make_map(a.p_hi, 2, d2p, s2, box2, &ok);
     CUtensorMap mpl = make_map(a.p_lo, 2, d2p, s2, box2, &ok);
@@ -661,8 +717,17 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         fprintf(stderr, "lqg: cuTensorMapEncodeTiled failed\n");
         return;
     }
-    const int tiles = ((ld + G_BM - 1) / G_BM) * ((ld + G_BN - 1) / G_BN);
-    k_tc_gemm<<<dim3(tiles, njobs), TC_THREADS, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
+    static int n_sm = 0;
+    if (!n_sm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (n_sm <= 0) n_sm = 1;
+    }
+    // persistent: one CTA per SM (one fits: 197 KB of shared memory)
+    const long long tiles = (long long) ((ld + G_BM - 1) / G_BM) * ((ld + G_BN - 1) / G_BN) * njobs;
+    const int grid = (int) std::min<long long>(tiles, n_sm);
+    k_tc_gemm<<<grid, TC_THREADS, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
     if (a.mid_event) cudaEventRecord(a.mid_event, st);
     k_tc_gram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), R_THREADS, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
     a.launches += 2;

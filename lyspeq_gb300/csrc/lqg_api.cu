@@ -458,11 +458,7 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             bool fresh = g.waves.empty() || g.waves.back().ld != h.ld || g.waves.back().gt != gt;
             if (!fresh) {
                 const auto &w = g.waves.back();
-                // gridDim.y of the product launch (slot jobs) <= 65535, and the
-                // K-blocked trace operands address (ld^2 / 64) * slots rows with
-                // 32-bit TMA coordinates
-                fresh = w.ws_bytes + need > wlimit || w.slot_q + h.ns + 1 > 65535 ||
-                        (int64_t) h.ld * h.ld / 64 * (w.slot_p + h.ns + 2) >= ((int64_t) 1 << 31);
+                fresh = w.ws_bytes + need > wlimit || w.slot_q + h.ns + 1 > 65535;
             }
             if (fresh) {
                 g.waves.emplace_back();
@@ -474,12 +470,10 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             w.members.push_back((int) k);   // index within the group
             w.ws_bytes += need;             // refined below
             w.slot_q += h.ns + 1;           // product jobs, one launch row each (reset below)
-            w.slot_p += h.ns + 2;           // trace operand rows (reset below)
         }
         for (auto &w : g.waves) {
             const int ld = w.ld;
             w.slot_q = 0;
-            w.slot_p = 0;
             const int64_t m = (int64_t) ld * ld * 8, tiles = (ld / 64) * (ld / 64);
             const int64_t gblk = (int64_t) w.gt * w.gt * w.splits * 128 * 128;
             w.desc_off = desc.size();

@@ -106,14 +106,6 @@ struct WaveArgs {
     unsigned long long *check;   // [0] violations, [1] first code, [2] first chunk, [3] first index
 };
 
-// Trace-Gram operand layout of the mixed path (R and P stacks): element k of
-// the flattened ld x ld matrix of stack slot `slot` lives at
-// ((k / 64) * total_slots + slot) * 64 + k % 64, so that the 64-element K block
-// of 128 consecutive slots (one TMA box) is one contiguous 16 KB run.
-__host__ __device__ __forceinline__ size_t kblocked(size_t k, int slot, int total_slots) {
-    return ((k >> 6) * (size_t) total_slots + (size_t) slot) * 64 + (k & 63);
-}
-
 // Self-checking build (-DLQG_CHECKED): an index that would leave its buffer is
 // counted and the access skipped, so that a bad launch reports instead of faulting.
 #ifdef LQG_CHECKED
