@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     }
 }
 
-// Mixed path: C^-1 and S to fp16 hi/lo planes, W_N = N C^-1 into its P slot.
+// Mixed path: C^-1 and S to fp16 hi/lo planes, C^-1 N into its R slot.
 __global__ void k_prep_mixed(WaveArgs a) {
     const int c = blockIdx.y;
     const ChunkDesc &ch = a.chunks[c];
@@ -331,7 +331,7 @@ __global__ void k_prep_mixed(WaveArgs a) {
         size_t idx = (size_t) i * ld + j;
         if (!LQG_IN_BOUNDS(a, (size_t) c * plane + idx < (size_t) a.n_chunks * plane &&
                                   (size_t) (ch.slot_q + ch.ns) * plane + idx < (size_t) a.total_slots_q * plane &&
-                                  (size_t) (ch.slot_p + ch.ns + 1) * plane + idx < (size_t) a.total_slots_p * plane,
+                                  (size_t) (ch.slot_r + ch.ns + 1) * plane + idx < (size_t) a.total_slots_r * plane,
                            6, c, idx))
             continue;
         double cv = A[idx];
@@ -343,11 +343,12 @@ __global__ void k_prep_mixed(WaveArgs a) {
         __half hs = __float2half_rn(xs);
         a.q_hi[(size_t) (ch.slot_q + ch.ns) * plane + idx] = hs;
         a.q_lo[(size_t) (ch.slot_q + ch.ns) * plane + idx] = __float2half_rn(xs - __half2float(hs));
-        double nw = (i < n && iv[i] != 0.0) ? 1.0 / iv[i] : 0.0;
-        float xw = (float) (nw * cv * wsc);
+        // C^-1 N (column j scaled by 1 / ivar_j) into R slot ns + 1
+        double nw = (j < n && iv[j] != 0.0) ? 1.0 / iv[j] : 0.0;
+        float xw = (float) (cv * nw * wsc);
         __half hw = __float2half_rn(xw);
-        a.p_hi[(size_t) (ch.slot_p + ch.ns + 1) * plane + idx] = hw;
-        a.p_lo[(size_t) (ch.slot_p + ch.ns + 1) * plane + idx] = __float2half_rn(xw - __half2float(hw));
+        a.r_hi[(size_t) (ch.slot_r + ch.ns + 1) * plane + idx] = hw;
+        a.r_lo[(size_t) (ch.slot_r + ch.ns + 1) * plane + idx] = __float2half_rn(xw - __half2float(hw));
     }
 }
 
@@ -494,22 +495,42 @@ __global__ void k_finish(WaveArgs a, int mixed) {
         for (int p = 0; p < parts; ++p) acc += dpart[(size_t) p * ns + s];
         d[(s / ch.kbin_upp) * bins.nk + s % ch.kbin_upp] = acc;
     }
-    const int rows = ns + 2;
     const size_t blkstride = (size_t) a.gram_splits * GR * GR;
+    if (mixed) {
+        // G = P R^T: P rows = A_i^T (i < ns), R rows = A_j (j < ns), C^-1 S, C^-1 N;
+        // blocks bi <= bj only.  F_ij = G_ij (i <= j), t_i = G_{i,ns}, b_i = G_{i,ns+1}.
+        const double *psc = a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + ch.slot_p;
+        const double *rsc = a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + a.total_slots_p + ch.slot_r;
+        auto gram = [&](int i, int j) {
+            const int blk = (i / GR) * a.gt + j / GR, li = i % GR, lj = j % GR;
+            const float *gp = a.gram_part + ((size_t) c * a.gt * a.gt + blk) * blkstride;
+            double acc = 0;
+            for (int sp = 0; sp < a.gram_splits; ++sp) acc += (double) gp[(size_t) sp * GR * GR + li * GR + lj];
+            return acc / (psc[i] * rsc[j]);
+        };
+        for (int e = threadIdx.x; e < ns * (ns + 2); e += blockDim.x) {
+            const int i = e / (ns + 2), j = e % (ns + 2);
+            if (j < ns && j < i) continue;
+            const double g = gram(i, j);
+            const int ikz = (i / ch.kbin_upp) * bins.nk + i % ch.kbin_upp;
+            if (j < ns) {
+                const int jkz = (j / ch.kbin_upp) * bins.nk + j % ch.kbin_upp;
+                if (!a.skip_fisher) F[(size_t) ikz * nq + jkz] = g;
+            } else if (j == ns) {
+                if (!a.turn_off_sfid) t[ikz] = g;
+            } else {
+                b[ikz] = g;
+            }
+        }
+        return;
+    }
+    const int rows = ns + 2;
     for (int e = threadIdx.x; e < rows * ns; e += blockDim.x) {
         const int i = e / ns, j = e % ns;
         const int blk = (i / GR) * a.gt + j / GR, li = i % GR, lj = j % GR;
         double acc = 0;
-        if (mixed) {
-            const float *gp = a.gram_part + ((size_t) c * a.gt * a.gt + blk) * blkstride;
-            for (int sp = 0; sp < a.gram_splits; ++sp) acc += (double) gp[(size_t) sp * GR * GR + li * GR + lj];
-            double si = a.scales[(size_t) 4 * a.n_chunks + a.total_slots_q + ch.slot_p + i];
-            double sj = a.scales[(size_t) 4 * a.n_chunks + a.total_slots_q + a.total_slots_p + ch.slot_r + j];
-            acc /= (si * sj);
-        } else {
-            const double *gp = ws_d(a, ch.o_part) + blk * blkstride;
-            for (int sp = 0; sp < a.gram_splits; ++sp) acc += gp[(size_t) sp * GR * GR + li * GR + lj];
-        }
+        const double *gp = ws_d(a, ch.o_part) + blk * blkstride;
+        for (int sp = 0; sp < a.gram_splits; ++sp) acc += gp[(size_t) sp * GR * GR + li * GR + lj];
         const int jkz = (j / ch.kbin_upp) * bins.nk + j % ch.kbin_upp;
         if (i < ns) {
             const int ikz = (i / ch.kbin_upp) * bins.nk + i % ch.kbin_upp;

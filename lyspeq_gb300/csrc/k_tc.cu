@@ -433,13 +433,15 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const int s = tl.s;
             const double sc = a.scales[4 * tl.c + 2];
             const double qs = a.scales[nq4 + ch.slot_q + s];
-            const double ps = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
+            // R scale (equal to the P scale of the same slot for s < ns)
+            const double ps = a.scales[nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r + s];
             const float mult = (float) (ps / (sc * qs));
             __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
             __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
-            const bool write_r = s < ch.ns;
-            const bool slots_ok = LQG_IN_BOUNDS(a, (!write_r || ch.slot_r + s < a.total_slots_r) &&
-                                                     ch.slot_p + s < a.total_slots_p, 2, tl.c, s);
+            // A_s (s < ns) goes to R and, transposed, to P; C^-1 S (s = ns) to R only
+            const bool write_p = s < ch.ns;
+            const bool slots_ok = LQG_IN_BOUNDS(a, ch.slot_r + s < a.total_slots_r &&
+                                                     (!write_p || ch.slot_p + s < a.total_slots_p), 2, tl.c, s);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int cb = tl.n0 + col0 + h * 32;
@@ -458,7 +460,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
                     hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
                     lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
                 }
-                if (write_r) {
+                {
                     uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
                     uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
 #pragma unroll
@@ -467,6 +469,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
                         dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
                     }
                 }
+                if (!write_p) continue;
                 unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
                 unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
 #pragma unroll
@@ -514,8 +517,11 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     const int c = blockIdx.y, sp = blockIdx.x, blk = blockIdx.z;
     const ChunkDesc &ch = a.chunks[c];
     if (a.status[ch.gidx] != LQG_CHUNK_OK || sp >= a.gram_splits) return;
+    // P rows: the ns A_s^T; R rows: ns A_s, C^-1 S, C^-1 N.  F is symmetric, so
+    // only blocks bi <= bj are formed (they hold every F_ij with i <= j and the
+    // t, b columns ns and ns + 1).
     const int bi = blk / a.gt, bj = blk % a.gt;
-    if (bi * R_BM >= ch.ns + 2 || bj * R_BN >= ch.ns) return;
+    if (bi > bj || bi * R_BM >= ch.ns || bj * R_BN >= ch.ns + 2) return;
     const int64_t K = (int64_t) ch.ld * ch.ld;
     const int64_t kper = ((K + a.gram_splits - 1) / a.gram_splits + BK - 1) / BK * BK;
     const int64_t k_lo = sp * kper, k_hi = min(K, k_lo + kper);
@@ -644,10 +650,10 @@ __global__ void k_scales(WaveArgs a) {
     for (int s = 0; s <= ch.ns; ++s) {
         // |C^-1 B| <= rowsum * max|B| and max|B| <= target / (B scale)
         double r = pow2_floor(qsc[s] / rowsum);
-        psc[s] = r;
-        if (s < ch.ns) rsc[s] = r;
+        rsc[s] = r;
+        if (s < ch.ns) psc[s] = r;
     }
-    psc[ch.ns + 1] = sc[3];
+    rsc[ch.ns + 1] = sc[3];   // C^-1 N
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point, so that the

@@ -488,8 +488,11 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
                     d.o_p = off; off += align_up(m * (d.ns + 2), 256);
                 }
                 d.slot_q = w.slot_q; w.slot_q += d.ns + 1;
-                d.slot_r = w.slot_r; w.slot_r += d.ns;
-                d.slot_p = w.slot_p; w.slot_p += d.ns + 2;
+                // trace-Gram operand stacks.  FP64: P = [A_s^T, (C^-1 S)^T, N C^-1],
+                // R = [A_s].  Mixed: P = [A_s^T], R = [A_s, C^-1 S, C^-1 N].
+                const bool mixed = precision == LQG_PRECISION_MIXED;
+                d.slot_r = w.slot_r; w.slot_r += mixed ? d.ns + 2 : d.ns;
+                d.slot_p = w.slot_p; w.slot_p += mixed ? d.ns : d.ns + 2;
                 desc.push_back(d);
             }
             const int nch = (int) w.members.size();
