@@ -158,6 +158,31 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 64 consecutive fp32 columns of this warp's 32 lanes: one load, one wait.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
+    uint32_t r[64];
+    __syncwarp();
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, "
+        "%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, "
+        "%51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]),
+          "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]),
+          "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]),
+          "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
+          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // Store 32 consecutive fp32 columns of this warp's 32 lanes (waits for completion).
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
     __syncwarp();
@@ -199,12 +224,13 @@ constexpr int R_SMEM = R_STAGES * R_STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 320;             // producer, MMA, 8 epilogue warps
 constexpr int R_THREADS = TC_THREADS;
 constexpr int kGramK = 32768;               // K elements per Gram split
-constexpr int kDrain = 2;                   // K blocks per drained hi*hi partial
+constexpr int kGemmDrain = 4;               // K blocks per drained hi*hi partial: products
+constexpr int kGramDrain = 2;               // and traces
 
 // Accumulation: the tensor cores round every fp32 accumulation of an MMA, with a
 // bias that grows with the number of accumulations into one accumulator.  The
 // hi*hi products and the (2^11 times smaller) cross products therefore go to
-// separate TMEM accumulators, and the hi*hi accumulator is drained every kDrain
+// separate TMEM accumulators, and the hi*hi accumulator is drained every DRAIN
 // K blocks (8 MMAs of K = 16) into fp32 sums held in registers: a ping-pong pair
 // of hi*hi accumulators lets the MMAs continue while one is drained.
 //
@@ -216,25 +242,25 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// MMA issuer, one output tile: for each drain group (kDrain K blocks)
+// MMA issuer, one output tile: for each drain group (DRAIN K blocks)
 // accumulate hi*hi into hi*hi buffer (g_all & 1) of [thh, thh + 2 BN), fresh
 // per group, and the cross terms into tx, fresh at the tile's first K block.
 // kb_all (shared-memory stage ring) and g_all (hi*hi buffers) run on across
 // the tiles of a persistent CTA.  Commits `done` after the tile's last MMA.
 // Returns false after a timed-out wait (abort flag set).
 // Stage layout: A hi, A lo, B hi, B lo.
-template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN>
+template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN, int DRAIN>
 __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned char *smem, uint64_t *full,
                                          uint64_t *empty, uint64_t *dfull, uint64_t *dempty, uint64_t *done,
                                          int kblocks, uint32_t idesc, int &kb_all, int &g_all, int *abort_flag) {
-    const int ngroups = (kblocks + kDrain - 1) / kDrain;
+    const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
     for (int g = 0; g < ngroups; ++g) {
         const int b = g_all & 1;
         if (g_all >= 2 && !mbar_wait(&dempty[b], ((g_all >> 1) - 1) & 1)) { *abort_flag = 1; return false; }
         fence_after();
         const uint32_t th = thh + b * BN;
-        const int kb_end = min(kblocks, (g + 1) * kDrain);
-        for (int kb = g * kDrain; kb < kb_end; ++kb) {
+        const int kb_end = min(kblocks, (g + 1) * DRAIN);
+        for (int kb = g * DRAIN; kb < kb_end; ++kb) {
             const int st = kb_all % STAGES;
             if (!mbar_wait(&full[st], (kb_all / STAGES) & 1)) { *abort_flag = 1; return false; }
             fence_after();
@@ -244,7 +270,7 @@ __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned cha
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
                 const uint64_t adv = (uint64_t) (kk * 32) >> 4;
-                umma_f16(th, ah + adv, bh + adv, idesc, (kb > g * kDrain || kk > 0));
+                umma_f16(th, ah + adv, bh + adv, idesc, (kb > g * DRAIN || kk > 0));
                 umma_f16(tx, ah + adv, bl + adv, idesc, (kb | kk) != 0);
                 umma_f16(tx, al + adv, bh + adv, idesc, 1);
             }
@@ -264,22 +290,28 @@ __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned cha
 // (registers are the limit: ten warps leave 168 per thread).  g_all runs on
 // across tiles like the issuer's.  Returns false (warp-uniform) if a wait
 // timed out or the CTA aborted.
-template <bool KAHAN>
+template <bool KAHAN, int DRAIN>
 __device__ __forceinline__ bool drain_tile(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
                                            uint64_t *dempty, int kblocks, float (&sum)[64], int &g_all,
                                            int *abort_flag) {
-    const int ngroups = (kblocks + kDrain - 1) / kDrain;
+    const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
     bool alive = true;
     for (int g = 0; g < ngroups; ++g) {
         const int b = g_all & 1;
         alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g_all >> 1) & 1)) && !*abort_flag;
         if (!alive) break;
         fence_after();
+        if (!KAHAN) {
+            float v[64];
+            tmem_ld64(tmem + lane_addr + b * 128 + col0, v);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+            for (int j = 0; j < 64; ++j) sum[j] += v[j];
+        }
+#pragma unroll
+        for (int h = 0; h < 2 && KAHAN; ++h) {
             float v[32];
             tmem_ld32(tmem + lane_addr + b * 128 + col0 + h * 32, v);
-            if (KAHAN) {
+            {
                 const uint32_t ca = tmem + lane_addr + 384 + col0 + h * 32;
                 float cp[32];
                 if (g == 0) {
@@ -296,9 +328,6 @@ __device__ __forceinline__ bool drain_tile(uint32_t tmem, uint32_t lane_addr, in
                     sum[h * 32 + j] = t;
                 }
                 tmem_st32(ca, cp);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; ++j) sum[h * 32 + j] += v[j];
             }
         }
         fence_before();
@@ -402,7 +431,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const int x = lt & 1;
             if (lt >= 2 && !mbar_wait(&xempty[x], ((lt >> 1) - 1) & 1)) { *abort_flag = 1; break; }
             fence_after();
-            if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN>(
+            if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN, kGemmDrain>(
                     tmem, tmem + 2 * G_BN + x * G_BN, smem, full, empty, dfull, dempty, &xfull[x], kblocks,
                     idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag))
                 break;
@@ -424,7 +453,8 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             float sum[64];
 #pragma unroll
             for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-            bool got = drain_tile<false>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, g_all, abort_flag);
+            bool got = drain_tile<false, kGemmDrain>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, g_all,
+                                                     abort_flag);
             const int x = lt & 1;
             got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1)) && !*abort_flag;
             if (!got) break;
@@ -447,7 +477,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
                 const int cb = tl.n0 + col0 + h * 32;
                 float xv[32];
                 tmem_ld32(tmem + lane_addr + 2 * G_BN + x * G_BN + col0 + h * 32, xv);
-                if (!slots_ok || cb >= ld || row >= ld) continue;
+                // warp-uniform: ld is a multiple of 64, so a warp's 32 rows are all
+                // inside the matrix or all padding
+                if (!slots_ok || cb >= ld || tl.m0 + quad * 32 >= ld) continue;
                 // hi/lo pairs packed in registers (two halves per 32-bit word)
                 uint32_t hp[16], lp[16];
 #pragma unroll
@@ -564,7 +596,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             mbar_wait(&full[kb % R_STAGES], (kb / R_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
         int kb_all = 0, g_all = 0;
-        mma_tile<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN>(tmem, tmem + 2 * R_BN, smem, full, empty, dfull,
+        mma_tile<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN, kGramDrain>(tmem, tmem + 2 * R_BN, smem, full, empty, dfull,
                                                                dempty, accum, kblocks, idesc_f16(R_BM, R_BN),
                                                                kb_all, g_all, abort_flag);
         // every MMA completes before the tensor memory is freed
@@ -578,7 +610,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 #pragma unroll
         for (int j = 0; j < 64; ++j) sum[j] = 0.f;
         int g_all = 0;
-        const bool alive = drain_tile<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, g_all, abort_flag);
+        const bool alive = drain_tile<true, kGramDrain>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, g_all,
+                                                        abort_flag);
         const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
