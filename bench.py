@@ -307,8 +307,14 @@ def main():
     pfid = synth.pd13_power(np.tile(w.bins.k_centers, w.bins.nz),
                             np.repeat(w.bins.z_centers, w.bins.nk))
     p_ref, p_mix = pfid + g_ref["theta"], pfid + g_mix["theta"]
-    used = np.diag(g_ref["fisher"]) > 0
-    err_p1d = float(np.max(np.abs(p_mix - p_ref)[used] / np.abs(p_ref)[used]))
+    # P1D error on the bins the subset measures: P_ref at least 5 sigma from 0
+    # (sigma = sqrt(diag F^-1)); on the others the estimate is noise and a
+    # relative error says nothing.  Also the largest |dP| in units of sigma.
+    sig = np.sqrt(np.abs(np.diag(g_ref["inverse"])))
+    used = (np.diag(g_ref["fisher"]) > 0) & (sig > 0)
+    good = used & (np.abs(p_ref) > 5 * sig)
+    err_p1d = float(np.max(np.abs(p_mix - p_ref)[good] / np.abs(p_ref)[good])) if good.any() else None
+    err_p1d_sigma = float(np.max(np.abs(p_mix - p_ref)[used] / sig[used])) if used.any() else None
     e64.close()
 
     # roofline of the dominant kernel
@@ -355,7 +361,8 @@ def main():
         "clocks": clk.summary(),
         "fp64_gpu": {"value": fp64_rate, "unit": UNIT, "chunks": len(sub), "ms": fp64_ms},
         "mixed_over_fp64": value / fp64_rate if fp64_rate else None,
-        "mixed_rel_err": {"fisher": err_f, "dbt": err_dbt, "p1d": err_p1d},
+        "mixed_rel_err": {"fisher": err_f, "dbt": err_dbt, "p1d": err_p1d, "p1d_bins": int(good.sum()),
+                          "p1d_in_sigma": err_p1d_sigma},
         "phase_ms": {nm: float(phase[i]) for i, nm in enumerate(names)},
         "phase_share": shares,
         "achieved_tflops": {"fp64_factor": fp64_tf, "tensor_products": tensor_tf},

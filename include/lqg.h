@@ -10,7 +10,7 @@
  *   OneDQuadraticPowerEstimate::computePowerSpectrumEstimates() :290-318
  * The entry points below are what a binding of that API binds: plain
  * pointers and sizes, integer status codes, no C++ or torch types.  The C++
- * facade in lyspeq_gb300/csrc/lyspeq_api.hpp keeps the reference's class
+ * facade in include/lyspeq_api.hpp keeps the reference's class
  * names on top of them.
  *
  * Conventions

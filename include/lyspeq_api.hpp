@@ -1,0 +1,356 @@
+// lyspeq_api.hpp - C++ facade of the GB300 engine with lyspeq's class names.
+//
+// lyspeq's per-chunk path is a C++ class API (no FFI).  This header keeps its
+// shape on top of the C ABI of lqg.h, so that a lyspeq-style driver reads the
+// same with the engine underneath:
+//
+//   lyspeq                                            here
+//   qio::QSOFile (after reading)                      QSOSpectrum
+//   OneQSOEstimate(const std::string &fname)          OneQSOEstimate(estimator, spectrum)
+//     (core/one_qso_estimate.cpp:52-121)
+//   Chunk(const qio::QSOFile&, int i1, int i2)        Chunk (made by OneQSOEstimate)
+//     (core/chunk_estimate.cpp:141-257)
+//   Chunk::dbt_estimate_before_fisher_vector,         same members, filled after iterate()
+//     Chunk::fisher_matrix                              (fetchResults())
+//   OneDQuadraticPowerEstimate::iterate()             same name; one batched NR iteration per
+//     (core/quadratic_estimate.cpp:398-546)             iteration on the GPU
+//   ::invertTotalFisherMatrix / ::computePowerSpectrumEstimates (:261-318)
+//   fisher_matrix_sum, inverse_fisher_matrix_sum,     same members
+//     solver_invfisher_matrix,
+//     dbt_estimate_sum_before_fisher_vector,
+//     dbt_estimate_fisher_weighted_vector,
+//     current_power_estimate_vector, powerspectra_fits
+//
+// Errors follow the reference: a spectrum or chunk the reference rejects
+// with an exception is skipped (logged through the optional log callback),
+// and a failure of the engine throws std::runtime_error.
+//
+// Header-only; link with -llqg (lyspeq_gb300/liblqg.so).
+#ifndef LYSPEQ_API_HPP
+#define LYSPEQ_API_HPP
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "lqg.h"
+
+namespace lyspeq_gb300 {
+
+constexpr double SPEED_OF_LIGHT = 299792.458;   // core/global_numbers.hpp
+constexpr double LYA_REST = 1215.67;
+constexpr int MIN_PIXELS_IN_FILE = 100;         // core/one_qso_estimate.cpp:14
+
+enum class Precision { FP64 = LQG_PRECISION_FP64, Mixed = LQG_PRECISION_MIXED };
+
+// bins:: (core/global_numbers.cpp:209-251)
+struct Binning {
+    std::vector<double> k_edges;    // NUMBER_OF_K_BANDS + 1
+    std::vector<double> z_centers;  // NUMBER_OF_Z_BINS
+    double z_bin_width = 0.2;
+    bool triangular = true;         // RedshiftBinningMethod 1
+    int nk() const { return (int) k_edges.size() - 1; }
+    int nz() const { return (int) z_centers.size(); }
+    int nkz() const { return nk() * nz(); }
+    double z_lower() const { return z_centers.front() - z_bin_width / 2; }
+    double z_upper() const { return z_centers.back() + z_bin_width / 2; }
+};
+
+// One (R, dv) pair of SQ lookup tables (SQLookupTable, core/sq_table.cpp):
+// deriv[k][v] (nk x nv) and signal[v][z] (nv x nzp).
+struct SQTable {
+    int r_fwhm = 0;
+    double dv = 0;
+    std::vector<double> deriv, signal;
+};
+
+struct SQGrid {
+    int nv = 0;           // NumberVPoints
+    double v_length = 0;  // VelocityLength
+    int nzp = 0;          // NumberZPoints
+};
+
+// The specifics:: values of the path (core/global_numbers.cpp:93-173).
+struct Specifics {
+    double max_forest_length = 35000;   // MaximumForestLength
+    int number_of_chunks = 1;           // DynamicChunkNumber
+    double max_mean_pixel_size = 150;   // MaximumMeanPixelSize (MAX_PIXEL_LENGTH_V)
+    int cont_logl_order = 1;            // ContinuumLogLambdaMargOrder
+    int cont_l_order = -1;              // ContinuumLambdaMargOrder
+    bool turn_off_sfid = false;         // TurnOffBaseline
+    bool precomputed_fisher = false;    // PrecomputedFisher given
+    double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
+};
+
+// A spectrum as qio::QSOFile holds it after reading: observed wavelength in
+// Angstrom, flux contrast and inverse variance (0 = masked), resolution R.
+struct QSOSpectrum {
+    std::vector<double> wave, delta, ivar;
+    int r_fwhm = 0;
+};
+
+class OneDQuadraticPowerEstimate;
+
+// One chunk of a spectrum in the estimator's batch (Chunk).
+class Chunk {
+public:
+    int fisher_index_start = 0, N_Q_MATRICES = 0;
+    int ZBIN_LOW = 0, ZBIN_UPP = 0, KBIN_UPP = 0, RES_INDEX = 0;
+    // filled by OneDQuadraticPowerEstimate::fetchResults after an iteration
+    std::vector<std::unique_ptr<double[]>> dbt_estimate_before_fisher_vector;
+    std::unique_ptr<double[]> fisher_matrix;   // N_Q x N_Q, upper triangle, not halved
+    int status = LQG_CHUNK_OK;
+
+    int size() const { return n_pix; }
+
+private:
+    friend class OneDQuadraticPowerEstimate;
+    int n_pix = 0, batch_index = -1;
+};
+
+// One spectrum cut into chunks (OneQSOEstimate).
+class OneQSOEstimate {
+public:
+    std::vector<std::unique_ptr<Chunk>> chunks;
+
+    // OneQSOEstimate::decideIndices, core/one_qso_estimate.cpp:17-50
+    static std::vector<int> decideIndices(int size, const double *wave, const Specifics &sp) {
+        std::vector<double> vel(size);
+        for (int i = 0; i < size; ++i) vel[i] = SPEED_OF_LIGHT * std::log(wave[i] / wave[0]);
+        double vmax = vel[size - 1];
+        int nchunks = 1;
+        if (sp.number_of_chunks > 1) {
+            nchunks += (int) (vmax / sp.max_forest_length_v());
+            vmax = std::min(sp.max_forest_length_v(), vmax / nchunks);
+        }
+        std::vector<int> idx{0};
+        int vl = 0;
+        for (int i = 0; i < nchunks; ++i) {
+            int jj = (int) (std::upper_bound(vel.begin() + vl, vel.end(), vmax) - vel.begin());
+            idx.push_back(jj);
+            if (jj == size) break;
+            vl = jj;
+            const double v0 = vel[vl];
+            for (int k = vl; k < size; ++k) vel[k] -= v0;
+        }
+        return idx;
+    }
+};
+
+class OneDQuadraticPowerEstimate {
+public:
+    // 3 x TOTAL_KZ_BINS
+    std::vector<std::unique_ptr<double[]>> dbt_estimate_sum_before_fisher_vector,
+        dbt_estimate_fisher_weighted_vector;
+    // TOTAL_KZ_BINS
+    std::unique_ptr<double[]> current_power_estimate_vector, powerspectra_fits;
+    // TOTAL_KZ_BINS^2
+    std::unique_ptr<double[]> fisher_matrix_sum, inverse_fisher_matrix_sum, solver_invfisher_matrix;
+    std::vector<std::unique_ptr<OneQSOEstimate>> local_queue;
+    int damped = 0, dof = 0;
+    double damp = 0;
+
+    std::function<void(const std::string &)> log = [](const std::string &) {};
+
+    OneDQuadraticPowerEstimate(const Binning &bins, const SQGrid &grid, const std::vector<SQTable> &tables,
+                               const Specifics &sp, int device = 0)
+        : bins_(bins), sp_(sp) {
+        nkz_ = bins.nkz();
+        std::vector<int> r;
+        std::vector<double> dv, deriv, signal;
+        for (const auto &t : tables) {
+            r.push_back(t.r_fwhm);
+            dv.push_back(t.dv);
+            deriv.insert(deriv.end(), t.deriv.begin(), t.deriv.end());
+            signal.insert(signal.end(), t.signal.begin(), t.signal.end());
+        }
+        lqg_bins b{bins.nk(), bins.nz(), bins.k_edges.data(), bins.z_centers.data(), bins.z_bin_width,
+                   bins.triangular ? 1 : 0};
+        lqg_tables tb{(int) tables.size(), r.data(), dv.data(), grid.nv, grid.v_length, grid.nzp,
+                      deriv.data(), sp.turn_off_sfid ? nullptr : signal.data()};
+        lqg_opts o{sp.max_forest_length_v(), sp.max_mean_pixel_size, sp.cont_logl_order, sp.cont_l_order,
+                   sp.turn_off_sfid ? 1 : 0, sp.precomputed_fisher ? 1 : 0, 0};
+        lqg_ctx *c = nullptr;
+        if (lqg_ctx_create(&c, &b, &tb, &o, device) != LQG_OK)
+            throw std::runtime_error("lqg_ctx_create failed (tables, binning or CUDA device)");
+        ctx_.reset(c);
+        for (int i = 0; i < 3; ++i) {
+            dbt_estimate_sum_before_fisher_vector.emplace_back(new double[nkz_]());
+            dbt_estimate_fisher_weighted_vector.emplace_back(new double[nkz_]());
+        }
+        current_power_estimate_vector.reset(new double[nkz_]());
+        powerspectra_fits.reset(new double[nkz_]());
+        fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
+        inverse_fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
+        solver_invfisher_matrix.reset(new double[(size_t) nkz_ * nkz_]());
+    }
+
+    int numberOfChunks() const { return lqg_batch_size(ctx_.get()); }
+
+    // OneQSOEstimate(fname): cleaning of the spectrum (QSOFile::maskOutliers,
+    // io/qso_file.cpp:189-230; cutBoundary :159-187; _cutMaskedBoundary
+    // :139-157), decideIndices, then one Chunk per pixel range.  A spectrum or
+    // chunk the reference rejects is skipped and logged.
+    OneQSOEstimate &addQSO(const QSOSpectrum &q) {
+        auto est = std::make_unique<OneQSOEstimate>();
+        std::vector<double> w = q.wave, d = q.delta, iv = q.ivar;
+        const size_t n0 = w.size();
+        if (d.size() != n0 || iv.size() != n0) throw std::invalid_argument("QSOSpectrum arrays differ in size");
+        for (auto &x : iv)
+            if (x < 1e-15) x = 0;
+        maskOutliers(w, d, iv, 5.0);
+        const double l1 = LYA_REST * (1 + bins_.z_lower()), l2 = LYA_REST * (1 + bins_.z_upper());
+        size_t a = std::lower_bound(w.begin(), w.end(), l1) - w.begin();
+        size_t b = std::upper_bound(w.begin(), w.end(), l2) - w.begin();
+        while (a < b && iv[a] == 0) ++a;
+        while (b > a && iv[b - 1] == 0) --b;
+        const int real = (int) std::count_if(iv.begin() + a, iv.begin() + b, [](double x) { return x != 0; });
+        if (b <= a || real < MIN_PIXELS_IN_FILE) {
+            log("spectrum skipped: short or empty after the redshift and mask cuts");
+            local_queue.push_back(std::move(est));
+            return *local_queue.back();
+        }
+        const int size = (int) (b - a);
+        std::vector<int> idx = OneQSOEstimate::decideIndices(size, w.data() + a, sp_);
+        const int nch = (int) idx.size() - 1;
+        std::vector<int64_t> offs(nch + 1, 0);
+        for (int i = 0; i < nch; ++i) offs[i + 1] = offs[i] + (idx[i + 1] - idx[i]);
+        std::vector<int> rr(nch, q.r_fwhm), st(nch, 0);
+        const int before = lqg_batch_size(ctx_.get());
+        check(lqg_batch_add(ctx_.get(), nch, offs.data(), w.data() + a, d.data() + a, iv.data() + a, rr.data(),
+                            st.data()),
+              "lqg_batch_add");
+        int next = before;
+        for (int i = 0; i < nch; ++i) {
+            if (st[i] != LQG_CHUNK_OK) {
+                log("chunk skipped: status " + std::to_string(st[i]));
+                continue;
+            }
+            auto ch = std::make_unique<Chunk>();
+            int info[8];
+            check(lqg_chunk_info(ctx_.get(), next, info), "lqg_chunk_info");
+            ch->n_pix = info[0];
+            ch->fisher_index_start = info[1];
+            ch->N_Q_MATRICES = info[2];
+            ch->KBIN_UPP = info[3];
+            ch->RES_INDEX = info[4];
+            ch->ZBIN_LOW = info[5];
+            ch->ZBIN_UPP = info[6];
+            ch->batch_index = next++;
+            est->chunks.push_back(std::move(ch));
+        }
+        local_queue.push_back(std::move(est));
+        return *local_queue.back();
+    }
+
+    // iterate(): for each iteration, every chunk's d, b, t and Fisher matrix
+    // (one batched lqg_nr_iteration with powerspectra_fits as the fiducial
+    // offset), the sums, invertTotalFisherMatrix and
+    // computePowerSpectrumEstimates.
+    void iterate(int number_of_iterations = 1, Precision precision = Precision::FP64) {
+        for (int it = 0; it < number_of_iterations; ++it) {
+            check(lqg_nr_iteration(ctx_.get(), powerspectra_fits.get(), (int) precision), "lqg_nr_iteration");
+            check(lqg_download(ctx_.get(), dbt_estimate_sum_before_fisher_vector[0].get(),
+                               dbt_estimate_sum_before_fisher_vector[1].get(),
+                               dbt_estimate_sum_before_fisher_vector[2].get(), fisher_matrix_sum.get(), nullptr),
+                  "lqg_download");
+            invertTotalFisherMatrix();
+        }
+    }
+
+    // invertTotalFisherMatrix + computePowerSpectrumEstimates
+    // (core/quadratic_estimate.cpp:261-318): F/2, stableInvertSym, theta.
+    void invertTotalFisherMatrix() {
+        std::vector<double> dbt(3 * (size_t) nkz_), w(3 * (size_t) nkz_), fh((size_t) nkz_ * nkz_);
+        for (int i = 0; i < 3; ++i)
+            std::copy(dbt_estimate_sum_before_fisher_vector[i].get(),
+                      dbt_estimate_sum_before_fisher_vector[i].get() + nkz_, dbt.begin() + (size_t) i * nkz_);
+        int rc = lqg_fisher_solve(ctx_.get(), fisher_matrix_sum.get(), dbt.data(), fh.data(),
+                                  solver_invfisher_matrix.get(), inverse_fisher_matrix_sum.get(), w.data(),
+                                  current_power_estimate_vector.get(), &damped, &dof, &damp);
+        if (rc != LQG_OK) throw std::runtime_error(std::string("Fisher matrix inversion: ") + lqg_last_error(ctx_.get()));
+        for (int i = 0; i < 3; ++i)
+            std::copy(w.begin() + (size_t) i * nkz_, w.begin() + (size_t) (i + 1) * nkz_,
+                      dbt_estimate_fisher_weighted_vector[i].get());
+    }
+
+    // Copies every chunk's own results of the last iteration into its
+    // dbt_estimate_before_fisher_vector and fisher_matrix members.
+    void fetchResults() {
+        for (auto &q : local_queue)
+            for (auto &ch : q->chunks) {
+                const int nq = ch->N_Q_MATRICES;
+                ch->dbt_estimate_before_fisher_vector.clear();
+                for (int i = 0; i < 3; ++i) ch->dbt_estimate_before_fisher_vector.emplace_back(new double[nq]());
+                ch->fisher_matrix.reset(new double[(size_t) nq * nq]());
+                check(lqg_chunk_result(ctx_.get(), ch->batch_index, ch->dbt_estimate_before_fisher_vector[0].get(),
+                                       ch->dbt_estimate_before_fisher_vector[1].get(),
+                                       ch->dbt_estimate_before_fisher_vector[2].get(), ch->fisher_matrix.get()),
+                      "lqg_chunk_result");
+            }
+        std::vector<int> st(numberOfChunks());
+        if (!st.empty()) {
+            check(lqg_download(ctx_.get(), nullptr, nullptr, nullptr, nullptr, st.data()), "lqg_download");
+            for (auto &q : local_queue)
+                for (auto &ch : q->chunks) ch->status = st[ch->batch_index];
+        }
+    }
+
+    // Device time of the last iteration's phases (ms), lqg_last_timings.
+    std::vector<double> timings() const {
+        std::vector<double> t(8);
+        lqg_last_timings(ctx_.get(), t.data(), 8);
+        return t;
+    }
+
+private:
+    struct CtxDel {
+        void operator()(lqg_ctx *c) const { lqg_ctx_destroy(c); }
+    };
+    std::unique_ptr<lqg_ctx, CtxDel> ctx_;
+    Binning bins_;
+    Specifics sp_;
+    int nkz_ = 0;
+
+    void check(int rc, const char *what) {
+        if (rc != LQG_OK) throw std::runtime_error(std::string(what) + ": " + lqg_last_error(ctx_.get()));
+    }
+
+    static double median(std::vector<double> v) {
+        std::sort(v.begin(), v.end());
+        const size_t n = v.size();
+        return n % 2 == 0 ? (v[n / 2 - 1] + v[n / 2]) / 2 : v[n / 2];
+    }
+
+    // QSOFile::maskOutliers (io/qso_file.cpp:189-230)
+    static void maskOutliers(const std::vector<double> &w, std::vector<double> &d, std::vector<double> &iv,
+                             double factor) {
+        std::vector<double> tmp;
+        for (size_t i = 0; i < d.size(); ++i)
+            if (iv[i] != 0) tmp.push_back(d[i]);
+        if (tmp.empty()) return;
+        const double med = median(tmp);
+        for (auto &x : tmp) x = std::fabs(x - med);
+        double mad = 1.4826 * (1.0 + 1.0 / std::sqrt((double) tmp.size())) * median(tmp);
+        mad = std::max(1.0, mad);
+        for (size_t i = 0; i < d.size(); ++i) {
+            if (iv[i] == 0) continue;
+            const double s = factor * std::max(1.0 / std::sqrt(iv[i]), mad);
+            const double fup = std::exp(1.663e-03 * std::pow(w[i] / LYA_REST, 4.107));
+            if (d[i] < (-1.0 - s) || d[i] > (fup + s)) {
+                d[i] = 0;
+                iv[i] = 0;
+            }
+        }
+    }
+};
+
+}  // namespace lyspeq_gb300
+
+#endif  // LYSPEQ_API_HPP

@@ -1,0 +1,86 @@
+"""C++ facade (include/lyspeq_api.hpp) driven by a C++ test program
+(tests/cpp/test_facade.cpp) the way lyspeq's own tests drive its classes: the
+tiny workload's spectra go through OneQSOEstimate chunking and one FP64
+Newton-Raphson iteration, compared with the CPU restatement of lyspeq's path
+(global Fisher matrix, d/b/t sums, theta and every chunk's own results)."""
+import os
+import shutil
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _write(path, w, s, chunks, results, g):
+    from oracle import qmle_port as P
+    out = open(path, "wb")
+    i64 = lambda v: out.write(struct.pack("<q", int(v)))
+    f64 = lambda v: out.write(struct.pack("<d", float(v)))
+
+    def vec(a):
+        a = np.ascontiguousarray(a, dtype="<f8").ravel()
+        i64(a.size)
+        out.write(a.tobytes())
+
+    vec(w.bins.k_edges); vec(w.bins.z_centers); f64(w.bins.dz); i64(1 if w.bins.triangular else 0)
+    i64(w.nv); f64(w.lenv); i64(w.nzp)
+    i64(len(w.tables))
+    for t in w.tables:
+        i64(t.r_fwhm); f64(t.dv); vec(t.deriv); vec(t.signal)
+    f64(s.max_forest_length); i64(s.cont_logl_order); i64(s.cont_l_order)
+    i64(len(w.spectra))
+    for sp in w.spectra:
+        i64(sp.r_fwhm); vec(sp.wave); vec(sp.delta); vec(1.0 / np.asarray(sp.sigma, dtype=np.float64) ** 2)
+    i64(len(chunks))
+    fsum = g["fsum"]
+    vec(fsum); vec(g["dbt"]); vec(g["theta"])
+    for d, b, t, f in results:
+        vec(np.concatenate([d, b, t])); vec(f)
+    out.close()
+
+
+def test_cpp_program_compiles_against_the_header():
+    """Host-only: the facade and the test program compile and link."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    from lyspeq_gb300 import build
+    lib = build.build()
+    exe = os.path.join(HERE, "cpp", "test_facade")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(HERE, "cpp", "test_facade.cpp"), "-L", os.path.dirname(lib), "-llqg",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", exe], check=True)
+    assert os.path.exists(exe)
+
+
+@pytest.mark.gpu
+def test_cpp_facade_one_iteration_matches_the_oracle(tmp_path):
+    from lyspeq_gb300 import build, synth
+    from oracle import qmle_port as P
+
+    gxx = shutil.which("g++")
+    lib = build.build()
+    exe = os.path.join(HERE, "cpp", "test_facade")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(HERE, "cpp", "test_facade.cpp"), "-L", os.path.dirname(lib), "-llqg",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", exe], check=True)
+    w = synth.make_workload("tiny")
+    s = P.Settings(max_forest_length=w.max_forest_length, cont_logl_order=1, cont_l_order=-1)
+    chunks = P.chunks_from_spectra(w.spectra, w.bins, w.table_index(), s)
+    tvs = [P.table_view(t, w.bins, w.nv, w.lenv, w.nzp) for t in w.tables]
+    results, acc = [], []
+    for ch in chunks:
+        d, b, t, f = P.chunk_iteration(ch, w.bins, tvs[ch.res_index], np.zeros(w.bins.nkz), s)
+        results.append((d, b, t, f))
+        acc.append((ch.fisher_index_start, d, b, t, f))
+    fsum, dbt = P.accumulate(w.bins.nkz, acc)
+    nr = P.newton_raphson_step(fsum, dbt)
+    path = str(tmp_path / "case.bin")
+    _write(path, w, s, chunks, results, dict(fsum=fsum, dbt=dbt, theta=nr["theta"]))
+    r = subprocess.run([exe, path, "1e-9"], capture_output=True, text=True)
+    print(r.stdout, r.stderr)
+    assert r.returncode == 0, r.stdout + r.stderr
