@@ -75,23 +75,52 @@ __device__ __forceinline__ void vindex(const TableGrid &g, double v, int &n, dou
     dn = xx - n;
 }
 
-// Mixed-path variants: multiplication by precomputed reciprocals instead of
-// FP64 divisions (one rounding more, far below the 22-bit operands).
-__device__ __forceinline__ void vindex_rcp(const TableGrid &g, double inv_dv, double v, int &n, double &dn) {
-    double xx = (v - g.v1) * inv_dv;
-    n = (int) xx;
-    n = n < 0 ? 0 : (n >= g.nv - 1 ? g.nv - 2 : n);
-    dn = xx - n;
+// Mixed-path element math on the FP32 pipe in double-float arithmetic (a
+// value is hi + lo, two floats).  Differences of close operands are exact
+// (Sterbenz), so v_ij, the interpolation fraction and the redshift weights
+// keep ~1e-7 relative accuracy, down to the small weights at a bin's edge.
+
+// a * b for double-float a, b: p + e (the lo * lo term is below 2^-46)
+__device__ __forceinline__ void two_prod_ff(float2 a, float2 b, float &p, float &e) {
+    p = __fmul_rn(a.x, b.x);
+    e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
 }
 
-__device__ __forceinline__ double zweight_rcp(const DeviceBins &b, double inv_dz, int zm, double z) {
-    const double zc = b.z_centers[zm], dz = b.dz;
-    if (!b.triangular || b.nz == 1)
-        return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.0 : 0.0;
-    if (zm == 0 && z < zc) return 1.0;
-    if (zm == b.nz - 1 && z > zc) return 1.0;
-    const double u = fabs(z - zc);
-    return u <= dz ? 1.0 - u * inv_dz : 0.0;
+// Table index and fraction at v = c (ln w_hi - ln w_lo): xx = v / dv as p + e,
+// then the reference's clamped linear-interpolation index
+// (mathtools/discrete_interpolation.cpp:61-72, v1 = 0).
+__device__ __forceinline__ void vindex_ff(const TableGrid &g, float2 lwh, float2 lwl, int &n, float &dn) {
+    const float2 d = make_float2(__fsub_rn(lwh.x, lwl.x), __fsub_rn(lwh.y, lwl.y));
+    float p, e;
+    two_prod_ff(d, make_float2(g.kv_hi, g.kv_lo), p, e);
+    int nn = (int) floorf(p);
+    float f = __fadd_rn(__fsub_rn(p, (float) nn), e);
+    if (f < 0.f) { --nn; f = __fadd_rn(f, 1.f); }
+    else if (f >= 1.f) { ++nn; f = __fsub_rn(f, 1.f); }
+    if (nn > g.nv - 2) { nn = g.nv - 2; f = __fadd_rn(__fsub_rn(p, (float) nn), e); }
+    if (nn < 0) { nn = 0; f = __fadd_rn(p, e); }
+    n = nn;
+    dn = f;
+}
+
+// Redshift weight of bin zm at 1 + z = P + E (zweight's rules): u = z - z_c
+// as u_hi (exact) + u_lo, and dz - |u| formed before any rounding.
+__device__ __forceinline__ float zweight_ff(const DeviceBins &b, int zm, float P, float E) {
+    const float u_hi = __fsub_rn(P, b.zc1_hi[zm]);
+    const float u_lo = __fsub_rn(E, b.zc1_lo[zm]);
+    const float u = __fadd_rn(u_hi, u_lo);
+    const float au_hi = fabsf(u_hi);
+    const float au_lo = u_hi > 0.f ? u_lo : (u_hi < 0.f ? -u_lo : fabsf(u_lo));
+    if (!b.triangular || b.nz == 1) {
+        const float r = __fadd_rn(__fsub_rn(b.dzh_hi, au_hi), __fsub_rn(b.dzh_lo, au_lo));
+        return r >= 0.f ? 1.f : 0.f;
+    }
+    if (zm == 0 && u < 0.f) return 1.f;
+    if (zm == b.nz - 1 && u > 0.f) return 1.f;
+    const float r = __fadd_rn(__fsub_rn(b.dz_hi, au_hi), __fsub_rn(b.dz_lo, au_lo));
+    return r >= 0.f ? r * b.inv_dz : 0.f;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -238,32 +267,32 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     if (tile >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK) return;
     const int ti = tile / tpr, tj = tile % tpr;
     const DeviceBins &bins = *a.bins;
-    const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix;
+    const float2 *lw2 = a.logw2 + ch.pix, *sw2 = a.sqw2 + ch.pix;
     const double *y = fws_d(a, ch.o_y);
     const int nzb = ch.ns / ch.kbin_upp;
-    const double inv_dv = 1.0 / a.grid.dv, inv_dz = 1.0 / bins.dz;
     constexpr int E = 2 * QM_PAIRS;
     int nidx[E];
     float dnf[E], yyf[E];
-    double zd[E];
+    float zp[E], ze[E];      // 1 + z_ij as double-float; zp = 0 marks padding
     size_t off[QM_PAIRS];    // element offset of each pair's first element
+    // y of this thread's two columns (the same for its four rows)
+    const int jc = tj * T64 + 2 * (threadIdx.x % 32);
+    const float yc0 = jc < n ? (float) y[jc] : 0.f, yc1 = jc + 1 < n ? (float) y[jc + 1] : 0.f;
 #pragma unroll
     for (int u = 0; u < QM_PAIRS; ++u) {
         const int p = threadIdx.x + 256 * u;
         const int i = ti * T64 + hrow + p / 32, j0 = tj * T64 + 2 * (p % 32);
         off[u] = (size_t) i * ld + j0;
+        const float yr = i < n ? (float) y[i] : 0.f;
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
             const int k = 2 * u + e, j = j0 + e;
-            nidx[k] = 0; dnf[k] = 0.f; yyf[k] = 0.f; zd[k] = -1e30;
+            nidx[k] = 0; dnf[k] = 0.f; yyf[k] = 0.f; zp[k] = 0.f; ze[k] = 0.f;
             if (i < n && j < n) {
                 const int lo = i < j ? i : j, hi = i < j ? j : i;
-                double v, z, dn;
-                vz_of(logw, sqw, lo, hi, v, z);
-                vindex_rcp(a.grid, inv_dv, v, nidx[k], dn);
-                dnf[k] = (float) dn;
-                zd[k] = z;
-                yyf[k] = (float) (y[i] * y[j]);
+                vindex_ff(a.grid, lw2[hi], lw2[lo], nidx[k], dnf[k]);
+                two_prod_ff(sw2[i], sw2[j], zp[k], ze[k]);
+                yyf[k] = yr * (e == 0 ? yc0 : yc1);
             }
         }
     }
@@ -278,8 +307,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
         for (int g = 0; g < kZGroup; ++g)
 #pragma unroll
             for (int k = 0; k < E; ++k)
-                w[g][k] = (z0 + g < nzb && zd[k] > -1e29) ? (float) zweight_rcp(bins, inv_dz, ch.zb0 + z0 + g, zd[k])
-                                                          : 0.f;
+                w[g][k] = (z0 + g < nzb && zp[k] > 0.f) ? zweight_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k]) : 0.f;
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
             const float *row = rows + (size_t) kn * a.grid.nv;
             float base[E];

@@ -33,8 +33,9 @@ struct lqg_ctx {
     };
     std::vector<HostChunk> chunks;
     std::vector<double> h_wave, h_delta, h_ivar, h_logw, h_sqw;
+    std::vector<float2> h_logw2, h_sqw2;
     bool pix_dirty = true;
-    DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw;
+    DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw, d_logw2, d_sqw2;
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
@@ -67,6 +68,12 @@ int find_redshift_bin(const lqg_ctx *ctx, double z) {
     if (z < zlow) return -1;
     int r = (int) ((z - zlow) / ctx->dz);
     return std::min(r, ctx->nz);
+}
+
+// x as a double-float pair: hi = fl32(x), lo = fl32(x - hi)
+float2 split_ff(double x) {
+    const float h = (float) x;
+    return make_float2(h, (float) (x - (double) h));
 }
 
 double pow2_scale(double bound, double target) {
@@ -130,6 +137,11 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     ctx->grid.dv = tables->v_length / (tables->nv - 1.);
     ctx->grid.z1 = ctx->z_centers[0] - ctx->dz;
     ctx->grid.dz = ctx->dz * (ctx->nz + 1) / (tables->nzp - 1.);
+    {
+        const float2 kv = split_ff(kSpeedOfLight / ctx->grid.dv);
+        ctx->grid.kv_hi = kv.x;
+        ctx->grid.kv_lo = kv.y;
+    }
     size_t nd = (size_t) tables->n_tables * bins->nk * tables->nv;
     size_t ns = (size_t) tables->n_tables * tables->nv * tables->nzp;
     lqg_ctx *c = ctx.get();
@@ -165,7 +177,17 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     db.nkz = ctx->nkz;
     db.triangular = ctx->triangular;
     db.dz = ctx->dz;
-    for (int z = 0; z < ctx->nz; ++z) db.z_centers[z] = ctx->z_centers[z];
+    for (int z = 0; z < ctx->nz; ++z) {
+        db.z_centers[z] = ctx->z_centers[z];
+        const float2 c1 = split_ff(1.0 + ctx->z_centers[z]);
+        db.zc1_hi[z] = c1.x;
+        db.zc1_lo[z] = c1.y;
+    }
+    {
+        const float2 d = split_ff(ctx->dz), dh = split_ff(ctx->dz / 2);
+        db.dz_hi = d.x; db.dz_lo = d.y; db.dzh_hi = dh.x; db.dzh_lo = dh.y;
+        db.inv_dz = (float) (1.0 / ctx->dz);
+    }
     if (ctx->d_bins.alloc(sizeof(DeviceBins)) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "bins");
     cudaMemcpy(ctx->d_bins.p, &db, sizeof db, cudaMemcpyHostToDevice);
     if (ctx->d_fisher.alloc((size_t) ctx->nkz * ctx->nkz * 8) != cudaSuccess ||
@@ -194,6 +216,7 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
     ctx->chunks.clear();
     ctx->h_wave.clear(); ctx->h_delta.clear(); ctx->h_ivar.clear();
     ctx->h_logw.clear(); ctx->h_sqw.clear();
+    ctx->h_logw2.clear(); ctx->h_sqw2.clear();
     ctx->results_size = 0;
     ctx->pix_dirty = true;
     return LQG_OK;
@@ -281,6 +304,8 @@ extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
             ctx->h_wave.push_back(w);
             ctx->h_logw.push_back(std::log(w));
             ctx->h_sqw.push_back(std::sqrt(w));
+            ctx->h_logw2.push_back(split_ff(ctx->h_logw.back()));
+            ctx->h_sqw2.push_back(split_ff(ctx->h_sqw.back()));
             ctx->h_delta.push_back(delta[i]);
             ctx->h_ivar.push_back(ivar[i]);
         }
@@ -310,7 +335,8 @@ int upload_pixels(lqg_ctx *ctx) {
     size_t np = ctx->h_wave.size();
     size_t bytes = std::max<size_t>(np, 1) * 8;
     if (ctx->d_wave.alloc(bytes) || ctx->d_delta.alloc(bytes) || ctx->d_ivar.alloc(bytes) ||
-        ctx->d_logw.alloc(bytes) || ctx->d_sqw.alloc(bytes))
+        ctx->d_logw.alloc(bytes) || ctx->d_sqw.alloc(bytes) || ctx->d_logw2.alloc(bytes) ||
+        ctx->d_sqw2.alloc(bytes))
         return set_err(ctx, LQG_ERR_NOMEM, "pixel arrays");
     cudaStream_t s = ctx->stream;
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_wave.p, ctx->h_wave.data(), np * 8, cudaMemcpyHostToDevice, s));
@@ -318,6 +344,8 @@ int upload_pixels(lqg_ctx *ctx) {
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_ivar.p, ctx->h_ivar.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_logw.p, ctx->h_logw.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqw.p, ctx->h_sqw.data(), np * 8, cudaMemcpyHostToDevice, s));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_logw2.p, ctx->h_logw2.data(), np * 8, cudaMemcpyHostToDevice, s));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqw2.p, ctx->h_sqw2.data(), np * 8, cudaMemcpyHostToDevice, s));
     if (ctx->d_results.alloc(std::max<int64_t>(ctx->results_size, 1) * 8) ||
         ctx->d_status.alloc(std::max<size_t>(ctx->chunks.size(), 1) * 4))
         return set_err(ctx, LQG_ERR_NOMEM, "results");
@@ -596,6 +624,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.fbounds = ctx->d_fbounds.as<double>();
     base.wave = ctx->d_wave.as<double>(); base.delta = ctx->d_delta.as<double>(); base.ivar = ctx->d_ivar.as<double>();
     base.logw = ctx->d_logw.as<double>(); base.sqw = ctx->d_sqw.as<double>();
+    base.logw2 = ctx->d_logw2.as<float2>(); base.sqw2 = ctx->d_sqw2.as<float2>();
     base.deriv = ctx->d_deriv.as<double>();
     base.deriv_f = ctx->d_deriv_f.as<float>();
     base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;

@@ -50,11 +50,16 @@ struct DeviceBins {
     int nk, nz, nkz, triangular;
     double dz;
     double z_centers[64];
+    // double-float (hi + lo) forms for the FP32-pipe element math of the
+    // mixed path: 1 + z_c per bin, dz, dz / 2, and 1 / dz
+    float zc1_hi[64], zc1_lo[64];
+    float dz_hi, dz_lo, dzh_hi, dzh_lo, inv_dz;
 };
 
 struct TableGrid {
     int nv, nzp, n_tables;
     double v1, dv, z1, dz;
+    float kv_hi, kv_lo;   // speed of light / dv as double-float
 };
 
 // Thin RAII for device allocations owned by the context.
@@ -85,6 +90,7 @@ struct WaveArgs {
     double *fbounds;             // per batch chunk: max |C^-1|, largest row sum of |C^-1|
     int gt;                      // Gram blocks of 128 per dimension (ns + 2 <= 128 gt)
     const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
+    const float2 *logw2, *sqw2;                      // ln w and sqrt w as double-float (hi, lo)
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
     const double *theta;                             // device, nkz
