@@ -44,37 +44,63 @@ __device__ __forceinline__ double block_max_all(double v, double *red) {
     return s;
 }
 
-// Double-float (df64) form of a double: hi = fl32(v), lo = fl32(v - hi), 48
-// significant bits.  The mixed-precision path runs the O(n^3) tile products in
-// this form on the FP32 pipe (GB300's FP32 rate is 60x its FP64 rate).
+// Shared tile loaders.  K-major layout: t[k * FP + m].
+// direct: t[k][m] = G[(r0 + k) * ld + c0 + m]  (rows of G are k)
+template <class T>
+__device__ __forceinline__ void load_direct(T *t, const T *G, int ld, int r0, int c0) {
+    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+        int k = e / FB, m = e % FB;
+        t[k * FP + m] = G[(size_t) (r0 + k) * ld + c0 + m];
+    }
+}
+// transposed: t[k][m] = G[(r0 + m) * ld + c0 + k]  (rows of G are m)
+template <class T>
+__device__ __forceinline__ void load_trans(T *t, const T *G, int ld, int r0, int c0) {
+    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+        int m = e / FB, k = e % FB;
+        t[k * FP + m] = G[(size_t) (r0 + m) * ld + c0 + k];
+    }
+}
+
+// acc[u][w] += sum_k A[k][ti + 16u] * B[k][tj + 16w]
+__device__ __forceinline__ void tile_mma(double (&acc)[4][4], const double *A, const double *B, int klen) {
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+#pragma unroll 4
+    for (int k = 0; k < klen; ++k) {
+        double a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { a[u] = A[k * FP + ti + 16 * u]; b[u] = B[k * FP + tj + 16 * u]; }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int w = 0; w < 4; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Double-float (df64) arithmetic for the mixed path: a value is hi + lo (two
+// floats, 48 significant bits), the matrix is kept in this form in memory
+// between the steps, and the O(n^3) tile products run on the FP32 pipe
+// (GB300's FP32 rate is 60x its FP64 rate).  The _rn intrinsics keep the
+// compiler from contracting the error-free transformations.
 __device__ __forceinline__ float2 to_df(double v) {
     const float h = __double2float_rn(v);
     return make_float2(h, __double2float_rn(v - (double) h));
 }
+__device__ __forceinline__ double df_to_d(float2 v) { return (double) v.x + (double) v.y; }
 
-// Shared tile loaders.  K-major layout: t[k * FP + m] (a double, or a df64
-// float2 in the same 8 bytes when DF).
-template <bool DF>
-__device__ __forceinline__ void put(double *t, int idx, double v) {
-    if (DF) reinterpret_cast<float2 *>(t)[idx] = to_df(v);
-    else t[idx] = v;
+// Knuth's two-sum: a + b = s + e exactly
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
 }
-// direct: t[k][m] = G[(r0 + k) * ld + c0 + m]  (rows of G are k)
-template <bool DF>
-__device__ __forceinline__ void load_direct(double *t, const double *G, int ld, int r0, int c0) {
-    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
-        int k = e / FB, m = e % FB;
-        put<DF>(t, k * FP + m, G[(size_t) (r0 + k) * ld + c0 + m]);
-    }
+// a - (bh + bl), renormalised
+__device__ __forceinline__ float2 df_sub(float2 a, float bh, float bl) {
+    const float2 s = df_two_sum(a.x, -bh);
+    return df_two_sum(s.x, __fadd_rn(s.y, __fsub_rn(a.y, bl)));
 }
-// transposed: t[k][m] = G[(r0 + m) * ld + c0 + k]  (rows of G are m)
-template <bool DF>
-__device__ __forceinline__ void load_trans(double *t, const double *G, int ld, int r0, int c0) {
-    for (int e = threadIdx.x; e < FB * FB; e += FTH) {
-        int m = e / FB, k = e % FB;
-        put<DF>(t, k * FP + m, G[(size_t) (r0 + m) * ld + c0 + k]);
-    }
-}
+
 // A tile of doubles already in shared memory, to df64 in place.
 __device__ __forceinline__ void tile_to_df(double *t) {
     for (int e = threadIdx.x; e < FB * FB; e += FTH) {
@@ -84,35 +110,23 @@ __device__ __forceinline__ void tile_to_df(double *t) {
     }
 }
 
-// acc[u][w] += sum_k A[k][ti + 16u] * B[k][tj + 16w]
-template <bool DF>
-__device__ __forceinline__ void tile_mma(double (&acc)[4][4], const double *A, const double *B, int klen) {
-    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
-    if (!DF) {
-#pragma unroll 4
-        for (int k = 0; k < klen; ++k) {
-            double a[4], b[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) { a[u] = A[k * FP + ti + 16 * u]; b[u] = B[k * FP + tj + 16 * u]; }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int w = 0; w < 4; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
-        }
-        return;
-    }
-    // df64: each product a*b = p + e exactly up to the dropped lo*lo term
-    // (p = fl(hi*hi), e from an FMA), added to the running (hi, lo) sum by
-    // Knuth's two-sum; lo is renormalised once per call.  The _rn intrinsics
-    // keep the compiler from contracting the error-free transformations.
-    const float2 *A2 = reinterpret_cast<const float2 *>(A), *B2 = reinterpret_cast<const float2 *>(B);
-    float hi[4][4], lo[4][4];
+struct DfAcc {
+    float h[4][4], l[4][4];
+};
+__device__ __forceinline__ void df_zero(DfAcc &c) {
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int w = 0; w < 4; ++w) { hi[u][w] = 0.f; lo[u][w] = 0.f; }
+        for (int w = 0; w < 4; ++w) { c.h[u][w] = 0.f; c.l[u][w] = 0.f; }
+}
+
+// c[u][w] += sum_k A[k][ti + 16u] * B[k][tj + 16w] in df64: each product
+// a * b = p + e up to the dropped lo * lo term (p = fl(hi * hi), e from FMAs),
+// p added to the running hi by two-sum, the errors summed in lo.
+__device__ __forceinline__ void tile_mma_df(DfAcc &c, const float2 *A2, const float2 *B2) {
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
 #pragma unroll 2
-    for (int k = 0; k < klen; ++k) {
+    for (int k = 0; k < FB; ++k) {
         float2 a[4], b[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) { a[u] = A2[k * FP + ti + 16 * u]; b[u] = B2[k * FP + tj + 16 * u]; }
@@ -124,17 +138,11 @@ __device__ __forceinline__ void tile_mma(double (&acc)[4][4], const double *A, c
                 float e = __fmaf_rn(a[u].x, b[w].x, -p);
                 e = __fmaf_rn(a[u].x, b[w].y, e);
                 e = __fmaf_rn(a[u].y, b[w].x, e);
-                const float sum = __fadd_rn(hi[u][w], p);
-                const float bb = __fsub_rn(sum, hi[u][w]);
-                const float err = __fadd_rn(__fsub_rn(hi[u][w], __fsub_rn(sum, bb)), __fsub_rn(p, bb));
-                hi[u][w] = sum;
-                lo[u][w] = __fadd_rn(lo[u][w], __fadd_rn(err, e));
+                const float2 s2 = df_two_sum(c.h[u][w], p);
+                c.h[u][w] = s2.x;
+                c.l[u][w] = __fadd_rn(c.l[u][w], __fadd_rn(s2.y, e));
             }
     }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int w = 0; w < 4; ++w) acc[u][w] += (double) hi[u][w] + (double) lo[u][w];
 }
 
 __device__ __forceinline__ void zero_acc(double (&acc)[4][4]) {
@@ -196,7 +204,6 @@ struct FactorSmem {
 };
 
 // Blocked Cholesky in place (lower triangle of A, ld x ld, first nb*64 rows).
-template <bool DF>
 __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
     for (int kb = 0; kb < nb; ++kb) {
         const int k0 = kb * FB;
@@ -219,19 +226,15 @@ __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
             }
         }
         __syncthreads();
-        if (DF) {
-            tile_to_df(s.b);
-            __syncthreads();
-        }
         // panel: L_ik = A_ik L_kk^-T, tile by tile
         for (int ib = kb + 1; ib < nb; ++ib) {
             const int i0 = ib * FB;
-            load_trans<DF>(s.a, A, ld, i0, k0);     // a[k][m] = A[i0 + m][k0 + k]
+            load_trans(s.a, A, ld, i0, k0);     // a[k][m] = A[i0 + m][k0 + k]
             __syncthreads();
             double acc[4][4];
             zero_acc(acc);
             // acc[m][j] = sum_k A[m][k] Linv[j][k]  with b[k][j] = Linv[j][k]
-            tile_mma<DF>(acc, s.a, s.b, FB);
+            tile_mma(acc, s.a, s.b, FB);
             __syncthreads();
             const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
 #pragma unroll
@@ -245,12 +248,12 @@ __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
         for (int ib = kb + 1; ib < nb; ++ib)
             for (int jb = kb + 1; jb <= ib; ++jb) {
                 const int i0 = ib * FB, j0 = jb * FB;
-                load_trans<DF>(s.a, A, ld, i0, k0);
-                load_trans<DF>(s.b, A, ld, j0, k0);
+                load_trans(s.a, A, ld, i0, k0);
+                load_trans(s.b, A, ld, j0, k0);
                 __syncthreads();
                 double acc[4][4];
                 zero_acc(acc);
-                tile_mma<DF>(acc, s.a, s.b, FB);
+                tile_mma(acc, s.a, s.b, FB);
                 const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
@@ -266,7 +269,6 @@ __device__ bool potrf_blocked(double *A, int ld, int nb, FactorSmem &s) {
 // In-place X = L^-1 (lower), row block by row block:
 //   X_II = L_II^-1;  X_IC = -X_II sum_{J=C}^{I-1} L_IJ X_JC   for C < I.
 // T = sum_J L_IJ X_JC is accumulated per column block into scratch (64 x ld).
-template <bool DF>
 __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &s) {
     const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
     for (int ib = 0; ib < nb; ++ib) {
@@ -276,10 +278,10 @@ __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &
             double acc[4][4];
             zero_acc(acc);
             for (int jb = cb; jb < ib; ++jb) {
-                load_trans<DF>(s.a, A, ld, i0, jb * FB);       // a[k][m] = L[i0+m][j0+k]
-                load_direct<DF>(s.b, A, ld, jb * FB, cb * FB);  // b[k][c] = X[j0+k][c0+c]
+                load_trans(s.a, A, ld, i0, jb * FB);       // a[k][m] = L[i0+m][j0+k]
+                load_direct(s.b, A, ld, jb * FB, cb * FB);  // b[k][c] = X[j0+k][c0+c]
                 __syncthreads();
-                tile_mma<DF>(acc, s.a, s.b, FB);
+                tile_mma(acc, s.a, s.b, FB);
                 __syncthreads();
             }
 #pragma unroll
@@ -298,16 +300,16 @@ __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &
         // a[k][m] = X_II[m][k]
         for (int e = threadIdx.x; e < FB * FB; e += FTH) {
             int m = e / FB, k = e % FB;
-            put<DF>(s.a, k * FP + m, s.b[m * FP + k]);
+            s.a[k * FP + m] = s.b[m * FP + k];
         }
         __syncthreads();
         // X_IC = -X_II T_C
         for (int cb = 0; cb < ib; ++cb) {
-            load_direct<DF>(s.b, T, ld, 0, cb * FB);           // b[k][c] = T[k][c0+c]
+            load_direct(s.b, T, ld, 0, cb * FB);           // b[k][c] = T[k][c0+c]
             __syncthreads();
             double acc[4][4];
             zero_acc(acc);
-            tile_mma<DF>(acc, s.a, s.b, FB);
+            tile_mma(acc, s.a, s.b, FB);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -320,8 +322,7 @@ __device__ void trtri_blocked(double *A, int ld, int nb, double *T, FactorSmem &
 
 // In place: M = X^T X (lower tiles, row block by row block; within a row block the
 // off-diagonal tiles first), then C^-1 = D M D symmetric in the full ld x ld.
-template <bool DF>
-__device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *ivar, FactorSmem &s) {
+__device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *ivar, double *sq, FactorSmem &s) {
     const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
     for (int ib = 0; ib < nb; ++ib) {
         for (int pass = 0; pass < 2; ++pass) {
@@ -330,8 +331,8 @@ __device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *iv
                 double acc[4][4];
                 zero_acc(acc);
                 for (int lb = ib; lb < nb; ++lb) {
-                    load_direct<DF>(s.a, A, ld, lb * FB, ib * FB);   // a[l][i] = X[l0+l][i0+i]
-                    load_direct<DF>(s.b, A, ld, lb * FB, jb * FB);   // b[l][j] = X[l0+l][j0+j]
+                    load_direct(s.a, A, ld, lb * FB, ib * FB);   // a[l][i] = X[l0+l][i0+i]
+                    load_direct(s.b, A, ld, lb * FB, jb * FB);   // b[l][j] = X[l0+l][j0+j]
                     __syncthreads();
                     // X is lower triangular: zero its upper part inside the diagonal tiles
                     if (lb == ib)
@@ -345,7 +346,7 @@ __device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *iv
                             if (l < j) s.b[l * FP + j] = 0.0;
                         }
                     __syncthreads();
-                    tile_mma<DF>(acc, s.a, s.b, FB);
+                    tile_mma(acc, s.a, s.b, FB);
                     __syncthreads();
                 }
 #pragma unroll
@@ -357,11 +358,185 @@ __device__ void lauum_blocked(double *A, int ld, int nb, int n, const double *iv
             }
         }
     }
+    for (int i = threadIdx.x; i < n; i += FTH) sq[i] = sqrt(ivar[i]);
+    __syncthreads();
     for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
         int i = (int) (e / ld), j = (int) (e % ld);
         if (j > i) continue;
         double v = 0.0;
-        if (i < n && j < n) v = sqrt(ivar[i]) * A[e] * sqrt(ivar[j]);
+        if (i < n && j < n) v = sq[i] * A[e] * sq[j];
+        A[e] = v;
+        A[(size_t) j * ld + i] = v;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// The same three steps with the matrix held as df64 pairs (A2, the same bytes
+// as the FP64 matrix).  The 64 x 64 diagonal-block Cholesky and inverse run in
+// FP64 (O(64^3) per block) and are converted at their boundaries; every tile
+// product, load and store is FP32-pipe work.
+
+__device__ bool potrf_df(float2 *A2, int ld, int nb, FactorSmem &s) {
+    float2 *sa2 = reinterpret_cast<float2 *>(s.a), *sb2 = reinterpret_cast<float2 *>(s.b);
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    for (int kb = 0; kb < nb; ++kb) {
+        const int k0 = kb * FB;
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            s.a[(e / FB) * FP + e % FB] = df_to_d(A2[(size_t) (k0 + e / FB) * ld + k0 + e % FB]);
+        __syncthreads();
+        if (!chol_block(s.a, &s.flag)) return false;
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            A2[(size_t) (k0 + e / FB) * ld + k0 + e % FB] = to_df(s.a[(e / FB) * FP + e % FB]);
+        tri_inv_block(s.a, s.b);           // s.b row-major inverse
+        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+            int r = e / FB, c = e % FB;
+            if (c < r) {
+                double t = s.b[r * FP + c];
+                s.b[r * FP + c] = s.b[c * FP + r];
+                s.b[c * FP + r] = t;
+            }
+        }
+        __syncthreads();
+        tile_to_df(s.b);                   // b[k][j] = Linv[j][k] as df64
+        __syncthreads();
+        for (int ib = kb + 1; ib < nb; ++ib) {
+            const int i0 = ib * FB;
+            load_trans(sa2, A2, ld, i0, k0);
+            __syncthreads();
+            DfAcc c;
+            df_zero(c);
+            tile_mma_df(c, sa2, sb2);
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w)
+                    A2[(size_t) (i0 + ti + 16 * u) * ld + k0 + tj + 16 * w] = df_two_sum(c.h[u][w], c.l[u][w]);
+            __syncthreads();
+        }
+        for (int ib = kb + 1; ib < nb; ++ib)
+            for (int jb = kb + 1; jb <= ib; ++jb) {
+                const int i0 = ib * FB, j0 = jb * FB;
+                load_trans(sa2, A2, ld, i0, k0);
+                load_trans(sb2, A2, ld, j0, k0);
+                __syncthreads();
+                DfAcc c;
+                df_zero(c);
+                tile_mma_df(c, sa2, sb2);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w) {
+                        float2 &dst = A2[(size_t) (i0 + ti + 16 * u) * ld + j0 + tj + 16 * w];
+                        dst = df_sub(dst, c.h[u][w], c.l[u][w]);
+                    }
+                __syncthreads();
+            }
+    }
+    return true;
+}
+
+__device__ void trtri_df(float2 *A2, int ld, int nb, float2 *T2, FactorSmem &s) {
+    float2 *sa2 = reinterpret_cast<float2 *>(s.a), *sb2 = reinterpret_cast<float2 *>(s.b);
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    for (int ib = 0; ib < nb; ++ib) {
+        const int i0 = ib * FB;
+        for (int cb = 0; cb < ib; ++cb) {
+            DfAcc c;
+            df_zero(c);
+            for (int jb = cb; jb < ib; ++jb) {
+                load_trans(sa2, A2, ld, i0, jb * FB);
+                load_direct(sb2, A2, ld, jb * FB, cb * FB);
+                __syncthreads();
+                tile_mma_df(c, sa2, sb2);
+                __syncthreads();
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w)
+                    T2[(size_t) (ti + 16 * u) * ld + cb * FB + tj + 16 * w] = df_two_sum(c.h[u][w], c.l[u][w]);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            s.a[(e / FB) * FP + e % FB] = df_to_d(A2[(size_t) (i0 + e / FB) * ld + i0 + e % FB]);
+        __syncthreads();
+        tri_inv_block(s.a, s.b);
+        for (int e = threadIdx.x; e < FB * FB; e += FTH)
+            A2[(size_t) (i0 + e / FB) * ld + i0 + e % FB] = to_df(s.b[(e / FB) * FP + e % FB]);
+        // a[k][m] = X_II[m][k]: s.a is free (tri_inv_block ended with a barrier)
+        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+            int m = e / FB, k = e % FB;
+            sa2[k * FP + m] = to_df(s.b[m * FP + k]);
+        }
+        __syncthreads();
+        for (int cb = 0; cb < ib; ++cb) {
+            load_direct(sb2, T2, ld, 0, cb * FB);
+            __syncthreads();
+            DfAcc c;
+            df_zero(c);
+            tile_mma_df(c, sa2, sb2);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    const float2 v = df_two_sum(c.h[u][w], c.l[u][w]);
+                    A2[(size_t) (i0 + ti + 16 * u) * ld + cb * FB + tj + 16 * w] = make_float2(-v.x, -v.y);
+                }
+            __syncthreads();
+        }
+    }
+}
+
+// M = X^T X, then C^-1 = D M D symmetric as FP64 (the matrix leaves df64 form).
+__device__ void lauum_df(float2 *A2, int ld, int nb, int n, const double *ivar, double *sq, FactorSmem &s) {
+    float2 *sa2 = reinterpret_cast<float2 *>(s.a), *sb2 = reinterpret_cast<float2 *>(s.b);
+    const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    for (int ib = 0; ib < nb; ++ib) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const int jlo = pass == 0 ? 0 : ib, jhi = pass == 0 ? ib : ib + 1;
+            for (int jb = jlo; jb < jhi; ++jb) {
+                DfAcc c;
+                df_zero(c);
+                for (int lb = ib; lb < nb; ++lb) {
+                    load_direct(sa2, A2, ld, lb * FB, ib * FB);
+                    load_direct(sb2, A2, ld, lb * FB, jb * FB);
+                    __syncthreads();
+                    if (lb == ib)
+                        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+                            int l = e / FB, i = e % FB;
+                            if (l < i) sa2[l * FP + i] = make_float2(0.f, 0.f);
+                        }
+                    if (lb == jb)
+                        for (int e = threadIdx.x; e < FB * FB; e += FTH) {
+                            int l = e / FB, j = e % FB;
+                            if (l < j) sb2[l * FP + j] = make_float2(0.f, 0.f);
+                        }
+                    __syncthreads();
+                    tile_mma_df(c, sa2, sb2);
+                    __syncthreads();
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w)
+                        A2[(size_t) (ib * FB + ti + 16 * u) * ld + jb * FB + tj + 16 * w] =
+                            df_two_sum(c.h[u][w], c.l[u][w]);
+                __syncthreads();
+            }
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += FTH) sq[i] = sqrt(ivar[i]);
+    __syncthreads();
+    double *A = reinterpret_cast<double *>(A2);
+    // lower elements are read (as df64) and written (as FP64) by the same
+    // thread; upper elements are only written
+    for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
+        int i = (int) (e / ld), j = (int) (e % ld);
+        if (j > i) continue;
+        double v = 0.0;
+        if (i < n && j < n) v = sq[i] * df_to_d(A2[e]) * sq[j];
         A[e] = v;
         A[(size_t) j * ld + i] = v;
     }
@@ -486,7 +661,7 @@ __device__ void marginalize_all(double *A, int ld, int n, const double *wave, in
 }
 
 template <bool DF>
-__global__ void __launch_bounds__(FTH) k_factor_tiled(WaveArgs a) {
+__global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FactorSmem &s = *reinterpret_cast<FactorSmem *>(smem_raw);
     const int c = blockIdx.x;
@@ -502,32 +677,59 @@ __global__ void __launch_bounds__(FTH) k_factor_tiled(WaveArgs a) {
     double *A = reinterpret_cast<double *>(a.fws + ch.o_c);
     double *scratch = reinterpret_cast<double *>(a.fws + ch.o_fscr);
     const double *iv = a.ivar + ch.pix;
-    if (!potrf_blocked<DF>(A, ld, nb, s)) {
-        if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_NOT_SPD;
-        return;
+    if (DF) {
+        // C~ to df64 in place (the pair occupies the double's 8 bytes)
+        for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
+            const double v = A[e];
+            reinterpret_cast<float2 *>(A)[e] = to_df(v);
+        }
+        __syncthreads();
+        float2 *A2 = reinterpret_cast<float2 *>(A);
+        if (!potrf_df(A2, ld, nb, s)) {
+            if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_NOT_SPD;
+            return;
+        }
+        __syncthreads();
+        trtri_df(A2, ld, nb, reinterpret_cast<float2 *>(scratch), s);
+        __syncthreads();
+        lauum_df(A2, ld, nb, n, iv, scratch, s);
+    } else {
+        if (!potrf_blocked(A, ld, nb, s)) {
+            if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_NOT_SPD;
+            return;
+        }
+        __syncthreads();
+        trtri_blocked(A, ld, nb, scratch, s);
+        __syncthreads();
+        lauum_blocked(A, ld, nb, n, iv, scratch, s);
     }
-    __syncthreads();
-    trtri_blocked<DF>(A, ld, nb, scratch, s);
-    __syncthreads();
-    lauum_blocked<DF>(A, ld, nb, n, iv, s);
     if (a.cont_logl >= 0 || a.cont_l >= 0)
         marginalize_all(A, ld, n, a.wave + ch.pix, a.cont_logl, a.cont_l, scratch, s);
+    // y = C^-1 delta, and the bounds max |C^-1| and max row sum of |C^-1|:
+    // one warp per row, lanes along the row (coalesced)
     double *y = reinterpret_cast<double *>(a.fws + ch.o_y);
     const double *dl = a.delta + ch.pix;
-    for (int i = threadIdx.x; i < ld; i += FTH) {
-        double acc = 0;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    double mx = 0, rs = 0;
+    for (int i = warp; i < ld; i += FTH / 32) {
+        double acc = 0, r = 0;
         if (i < n) {
             const double *Ai = A + (size_t) i * ld;
-            for (int j = 0; j < n; ++j) acc += Ai[j] * dl[j];
+            for (int j = lane; j < n; j += 32) {
+                const double v = Ai[j];
+                acc += v * dl[j];
+                r += fabs(v);
+                mx = fmax(mx, fabs(v));
+            }
         }
-        y[i] = acc;
-    }
-    double mx = 0, rs = 0;
-    for (int i = threadIdx.x; i < n; i += FTH) {
-        const double *Ai = A + (size_t) i * ld;
-        double r = 0;
-        for (int j = 0; j < n; ++j) { double v = fabs(Ai[j]); r += v; mx = fmax(mx, v); }
-        rs = fmax(rs, r);
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_down_sync(0xffffffffu, acc, o);
+            r += __shfl_down_sync(0xffffffffu, r, o);
+        }
+        if (lane == 0) {
+            y[i] = acc;
+            rs = fmax(rs, r);
+        }
     }
     mx = block_max_all(mx, s.red);
     rs = block_max_all(rs, s.red);

@@ -143,7 +143,7 @@ __global__ void k_build_s_c(WaveArgs a) {
                        11, c, ch.o_c))
         return;
     double *S = fws_d(a, ch.o_s), *C = fws_d(a, ch.o_c);
-    const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix, *iv = a.ivar + ch.pix;
+    const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix, *sq = a.sqiv + ch.pix;
     const double *stab = a.signal ? a.signal + (size_t) ch.res * a.grid.nv * a.grid.nzp : nullptr;
     const DeviceBins &bins = *a.bins;
     for (int e = threadIdx.x; e < T64 * T64; e += blockDim.x) {
@@ -174,7 +174,7 @@ __global__ void k_build_s_c(WaveArgs a) {
                 cv += th * q;
             }
         }
-        double di = sqrt(iv[i]), dj = sqrt(iv[j]);
+        const double di = sq[i], dj = sq[j];
         C[idx] = di * cv * dj + (i == j ? 1.0 : 0.0);
     }
 }
@@ -300,7 +300,11 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
     const size_t plane = (size_t) ld * ld;
     const float *rows = a.deriv_f + (size_t) ch.res * bins.nk * a.grid.nv;
-    const double *qscale = a.scales + (size_t) 4 * a.n_chunks + ch.slot_q;
+    // slot scales as floats, converted once per block
+    __shared__ float qscale[kMaxGramBlocks * 128];
+    for (int t = threadIdx.x; t < ch.ns; t += blockDim.x)
+        qscale[t] = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + t];
+    __syncthreads();
     for (int z0 = 0; z0 < nzb; z0 += kZGroup) {
         float w[kZGroup][E];
 #pragma unroll
@@ -317,7 +321,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
             for (int g = 0; g < kZGroup; ++g) {
                 if (z0 + g >= nzb) break;
                 const int s = (z0 + g) * ch.kbin_upp + kn;
-                const float qs = (float) qscale[s];
+                const float qs = qscale[s];
                 uint32_t *qh = reinterpret_cast<uint32_t *>(a.q_hi + (size_t) (ch.slot_q + s) * plane);
                 uint32_t *ql = reinterpret_cast<uint32_t *>(a.q_lo + (size_t) (ch.slot_q + s) * plane);
                 float fpart = 0.f;
@@ -349,7 +353,6 @@ __global__ void k_prep_mixed(WaveArgs a) {
     if ((int) blockIdx.x >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK) return;
     const int ti = blockIdx.x / tpr, tj = blockIdx.x % tpr;
     const double *A = fws_d(a, ch.o_c), *S = fws_d(a, ch.o_s);
-    const double *iv = a.ivar + ch.pix;
     const double *sc = a.scales + 4 * c;
     const double cs = sc[2], wsc = sc[3];
     const double ss = a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + ch.ns];
@@ -372,7 +375,7 @@ __global__ void k_prep_mixed(WaveArgs a) {
         a.q_hi[(size_t) (ch.slot_q + ch.ns) * plane + idx] = hs;
         a.q_lo[(size_t) (ch.slot_q + ch.ns) * plane + idx] = __float2half_rn(xs - __half2float(hs));
         // C^-1 N (column j scaled by 1 / ivar_j) into R slot ns + 1
-        double nw = (j < n && iv[j] != 0.0) ? 1.0 / iv[j] : 0.0;
+        const double nw = j < n ? a.niv[ch.pix + j] : 0.0;
         float xw = (float) (cv * nw * wsc);
         __half hw = __float2half_rn(xw);
         a.r_hi[(size_t) (ch.slot_r + ch.ns + 1) * plane + idx] = hw;
@@ -387,12 +390,11 @@ __global__ void k_wn_fp64(WaveArgs a) {
     const int ld = ch.ld, n = ch.n;
     if (a.status[ch.gidx] != LQG_CHUNK_OK) return;
     const double *A = fws_d(a, ch.o_c);
-    const double *iv = a.ivar + ch.pix;
     double *P = ws_d(a, ch.o_p) + (size_t) (ch.ns + 1) * ld * ld;
     for (size_t e = (size_t) blockIdx.x * blockDim.x + threadIdx.x; e < (size_t) ld * ld;
          e += (size_t) gridDim.x * blockDim.x) {
         int i = (int) (e / ld);
-        double nw = (i < n && iv[i] != 0.0) ? 1.0 / iv[i] : 0.0;
+        const double nw = i < n ? a.niv[ch.pix + i] : 0.0;
         P[e] = nw * A[e];
     }
 }

@@ -661,9 +661,9 @@ __global__ void k_scales(WaveArgs a) {
     if (a.status[ch.gidx] != LQG_CHUNK_OK) return;
     __shared__ double red[32];
     double mx = 0;
-    const double *iv = a.ivar + ch.pix;
+    const double *iv = a.niv + ch.pix;
     for (int i = threadIdx.x; i < ch.n; i += blockDim.x)
-        if (iv[i] != 0) mx = fmax(mx, 1.0 / iv[i]);
+        mx = fmax(mx, iv[i]);   // 1 / ivar, 0 where masked
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
     if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = mx;
     __syncthreads();

@@ -34,8 +34,9 @@ struct lqg_ctx {
     std::vector<HostChunk> chunks;
     std::vector<double> h_wave, h_delta, h_ivar, h_logw, h_sqw;
     std::vector<float2> h_logw2, h_sqw2;
+    std::vector<double> h_sqiv, h_niv;
     bool pix_dirty = true;
-    DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw, d_logw2, d_sqw2;
+    DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw, d_logw2, d_sqw2, d_sqiv, d_niv;
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
@@ -217,6 +218,7 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
     ctx->h_wave.clear(); ctx->h_delta.clear(); ctx->h_ivar.clear();
     ctx->h_logw.clear(); ctx->h_sqw.clear();
     ctx->h_logw2.clear(); ctx->h_sqw2.clear();
+    ctx->h_sqiv.clear(); ctx->h_niv.clear();
     ctx->results_size = 0;
     ctx->pix_dirty = true;
     return LQG_OK;
@@ -308,6 +310,8 @@ extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
             ctx->h_sqw2.push_back(split_ff(ctx->h_sqw.back()));
             ctx->h_delta.push_back(delta[i]);
             ctx->h_ivar.push_back(ivar[i]);
+            ctx->h_sqiv.push_back(std::sqrt(ivar[i]));
+            ctx->h_niv.push_back(ivar[i] != 0 ? 1.0 / ivar[i] : 0.0);
         }
         ctx->chunks.push_back(hc);
     }
@@ -336,7 +340,7 @@ int upload_pixels(lqg_ctx *ctx) {
     size_t bytes = std::max<size_t>(np, 1) * 8;
     if (ctx->d_wave.alloc(bytes) || ctx->d_delta.alloc(bytes) || ctx->d_ivar.alloc(bytes) ||
         ctx->d_logw.alloc(bytes) || ctx->d_sqw.alloc(bytes) || ctx->d_logw2.alloc(bytes) ||
-        ctx->d_sqw2.alloc(bytes))
+        ctx->d_sqw2.alloc(bytes) || ctx->d_sqiv.alloc(bytes) || ctx->d_niv.alloc(bytes))
         return set_err(ctx, LQG_ERR_NOMEM, "pixel arrays");
     cudaStream_t s = ctx->stream;
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_wave.p, ctx->h_wave.data(), np * 8, cudaMemcpyHostToDevice, s));
@@ -345,6 +349,8 @@ int upload_pixels(lqg_ctx *ctx) {
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_logw.p, ctx->h_logw.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqw.p, ctx->h_sqw.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_logw2.p, ctx->h_logw2.data(), np * 8, cudaMemcpyHostToDevice, s));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqiv.p, ctx->h_sqiv.data(), np * 8, cudaMemcpyHostToDevice, s));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_niv.p, ctx->h_niv.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqw2.p, ctx->h_sqw2.data(), np * 8, cudaMemcpyHostToDevice, s));
     if (ctx->d_results.alloc(std::max<int64_t>(ctx->results_size, 1) * 8) ||
         ctx->d_status.alloc(std::max<size_t>(ctx->chunks.size(), 1) * 4))
@@ -625,6 +631,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.wave = ctx->d_wave.as<double>(); base.delta = ctx->d_delta.as<double>(); base.ivar = ctx->d_ivar.as<double>();
     base.logw = ctx->d_logw.as<double>(); base.sqw = ctx->d_sqw.as<double>();
     base.logw2 = ctx->d_logw2.as<float2>(); base.sqw2 = ctx->d_sqw2.as<float2>();
+    base.sqiv = ctx->d_sqiv.as<double>(); base.niv = ctx->d_niv.as<double>();
     base.deriv = ctx->d_deriv.as<double>();
     base.deriv_f = ctx->d_deriv_f.as<float>();
     base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;

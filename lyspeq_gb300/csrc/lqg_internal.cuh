@@ -91,6 +91,7 @@ struct WaveArgs {
     int gt;                      // Gram blocks of 128 per dimension (ns + 2 <= 128 gt)
     const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
     const float2 *logw2, *sqw2;                      // ln w and sqrt w as double-float (hi, lo)
+    const double *sqiv, *niv;                        // sqrt(ivar), and 1 / ivar (0 where ivar = 0)
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
     const double *theta;                             // device, nkz
