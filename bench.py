@@ -261,6 +261,7 @@ def main():
         ms = float(t.item())
     value = n_ok * world / (ms / 1e3)
     phase /= args.steps
+    launches_per_iter = launches // max(args.steps, 1)
 
     # end to end through the C ABI from pinned host buffers
     barrier()
@@ -319,13 +320,13 @@ def main():
 
     # roofline of the dominant kernel
     fl = flop_counts(ns_list, n_list)
-    names = ["build_s_c", "factor_fp64", "build_q", "products_tc", "traces_tc", "finish", "accumulate"]
+    names = ["build_s_c", "factor", "build_q", "products_tc", "traces_tc", "finish", "accumulate"]
     shares = {nm: float(phase[i] / phase[7]) for i, nm in enumerate(names)}
     dom = max(range(7), key=lambda i: phase[i])
     peaks = {}
     if os.path.exists(PEAKS_FILE):
         peaks = json.load(open(PEAKS_FILE))
-    if names[dom] == "factor_fp64":
+    if names[dom] == "factor":
         achieved = fl["factor"] / (phase[1] / 1e3) / 1e12
         roof = {"kernel": "k_factor", "bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
                 "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
@@ -334,9 +335,20 @@ def main():
         key = "products" if names[dom] == "products_tc" else "traces"
         achieved = fl[key] / (phase[dom] / 1e3) / 1e12
         pk = peaks.get("bf16_tflops", 1900.0)
+        # DRAM traffic per launch of the products kernel (one launch per wave):
+        # algorithmic bytes (Q_s read, A_s written to R and transposed to P,
+        # fp16 hi/lo) times the measured/algorithmic ratio, 1.14, of an ncu
+        # capture of the same kernel on 64 chunks of this workload
+        traffic = None
+        n_waves = (launches_per_iter - 3) // 6     # 2 phase-A launches, 6 per wave, 1 accumulation
+        if key == "products" and n_waves > 0:
+            ld = np.ceil(np.asarray(n_list) / 64.0) * 64.0
+            alg = float(np.sum((3.0 * (np.asarray(ns_list) + 1) - 1) * ld * ld * 4.0))
+            traffic = 1.14 * alg / n_waves
         roof = {"kernel": "k_tc_gemm" if key == "products" else "k_tc_gram", "bound": "tensor",
                 "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
-                "traffic": None, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}
+                "traffic": traffic, "traffic_unit": "bytes per launch",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}
     tensor_tf = fl["products"] / (phase[3] / 1e3) / 1e12 if phase[3] > 0 else None
     fp64_tf = fl["factor"] / (phase[1] / 1e3) / 1e12 if phase[1] > 0 else None
 
@@ -365,7 +377,7 @@ def main():
                           "p1d_in_sigma": err_p1d_sigma},
         "phase_ms": {nm: float(phase[i]) for i, nm in enumerate(names)},
         "phase_share": shares,
-        "achieved_tflops": {"fp64_factor": fp64_tf, "tensor_products": tensor_tf},
+        "achieved_tflops": {"factor_df64": fp64_tf, "tensor_products": tensor_tf},
     }
     print(json.dumps(line))
     if world > 1:
