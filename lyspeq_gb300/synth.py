@@ -16,6 +16,16 @@ with the shapes, sizes and value distributions of the named configurations:
                  (rounded to 0.1), R ~ U[30000, 50000], 40 k bins (10 x 5e-4
                  linear, 30 log to 0.2 s/km), 6 z bins centred 2.0 ... 3.0,
                  sigma ~ lognormal(ln 0.05, 0.5).
+* ``desi_reso``: 16384 chunks, N log-uniform in [150, 1000] on a grid linear
+                 in wavelength with dv = 50 km/s at its first pixel, each with an
+                 11-diagonal resolution matrix (Gaussian rows whose width varies
+                 by +-10 % smoothly along the spectrum, R ~ U[2000, 5000]),
+                 deconvolved (m = 1) and oversampled x 3 by the reader; the k/z
+                 binning of ``small``; S/N per pixel ~ lognormal(ln 1, 0.8).
+                 One signal table (R = 100000, dv = 16.7) serves every chunk.
+* ``tiny_reso`` and ``tiny_reso_dia``: 6 such spectra of 110-180 pixels,
+                 oversampled x 3 and deconvolved, or used as diagonal matrices
+                 on the pixel grid.
 
 The lookup tables follow the definitions lyspeq tabulates
 (core/sq_table.cpp:201-323 with core/fiducial_cosmology.cpp:273-331):
@@ -184,6 +194,9 @@ class Spectrum:
     r_fwhm: int
     dv: float
     z_qso: float = 3.0
+    # resolution matrix in lyspeq's DiaMatrix layout: ndiags x n, diagonal d
+    # holds offset ndiags/2 - d, the element of column c at [d, c]
+    resomat: np.ndarray | None = None
 
 
 @dataclasses.dataclass
@@ -200,6 +213,9 @@ class Workload:
     cont_logl_order: int = -1
     cont_l_order: int = -1
     fid: tuple = PD13_DEFAULT
+    reso: bool = False          # UseResoMatrix
+    oversample: int = -1        # OversampleRmat
+    deconv_m: float = 0.0       # ResoMatDeconvolutionM
 
     def table_index(self):
         return {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(self.tables)}
@@ -215,11 +231,70 @@ def _gaussian_field(rng, n, dv, r_kms, z, fid):
     return field[:n]
 
 
+def gaussian_resomat(n: int, sigma_pix: np.ndarray, ndiags: int = 11) -> np.ndarray:
+    """Resolution matrix with Gaussian rows of width sigma_pix[i] (pixels),
+    each row normalised to unit sum over its ndiags entries, in lyspeq's
+    DiaMatrix layout (mathtools/matrix_helper.cpp:503-520): values[d, c] is
+    the element of row c - off(d), column c, off(d) = ndiags/2 - d; entries
+    whose row falls outside the spectrum are zero."""
+    noff = ndiags // 2
+    offs = np.arange(noff, -noff - 1, -1)
+    rows = np.exp(-0.5 * (offs[None, :] / sigma_pix[:, None]) ** 2)   # [row i, d]
+    rows /= rows.sum(axis=1, keepdims=True)
+    vals = np.zeros((ndiags, n))
+    for d, off in enumerate(offs):
+        r = np.arange(n) - off          # row of column c on this diagonal
+        ok = (r >= 0) & (r < n)
+        vals[d, ok] = rows[r[ok], d]
+    return vals
+
+
+def _make_reso_workload(name, rng, seed, nch):
+    """The resolution-matrix workloads (see the module docstring)."""
+    bins = Bins(0.0, 20, 2e-3, 0, 0.0, 2.2, 0.2, 3)
+    dv = 50.0
+    if name == "desi_reso":
+        npix = np.exp(rng.uniform(math.log(150), math.log(1000), size=nch)).astype(int)
+    else:
+        npix = rng.integers(110, 181, size=nch)
+    span = 1.0 + npix * dv / C_KMS
+    lmin, lmax = LYA_REST * (1 + bins.z_lower) * 1.0005, LYA_REST * (1 + bins.z_upper) * 0.9995
+    lam0 = rng.uniform(lmin, lmax / span)
+    rs = (np.round(rng.uniform(2000, 5000, size=nch) / 100) * 100).astype(int)
+    spectra = []
+    for i in range(nch):
+        n = int(npix[i])
+        dlam = lam0[i] * dv / C_KMS
+        wave = lam0[i] + dlam * np.arange(n)
+        zmed = float(np.median(wave)) / LYA_REST - 1.0
+        r_kms = C_KMS / rs[i] / ONE_SIGMA_2_FWHM
+        sig = 1.0 / np.exp(rng.normal(0.0, 0.8, size=n))
+        delta = _gaussian_field(rng, n, dv, r_kms, zmed, PD13_DEFAULT) + sig * rng.standard_normal(n)
+        sigma_pix = wave / rs[i] / ONE_SIGMA_2_FWHM / dlam
+        phase = rng.uniform(0.0, 2.0 * math.pi)
+        sigma_pix = sigma_pix * (1.0 + 0.1 * np.sin(2.0 * math.pi * np.arange(n) / n + phase))
+        spectra.append(Spectrum(wave, delta, sig, int(rs[i]), dv, resomat=gaussian_resomat(n, sigma_pix)))
+    osamp = -1 if name == "tiny_reso_dia" else 3
+    table_dv = round(dv / 3.0, 1)
+    longest = max(float(np.log(s.wave[-1] / s.wave[0]) * C_KMS) for s in spectra)
+    mfl = 20000.0 if name == "desi_reso" else 6000.0
+    lenv = float(math.ceil(max(longest + 12 * dv, mfl) * 1.02 / 100.0) * 100.0)
+    nv = int(math.ceil(lenv / (table_dv / 2.0))) + 1
+    nzp = max(10, bins.nz + 2)
+    tables = [build_table(bins, 100000, table_dv, nv, lenv, nzp)]
+    return Workload(name, seed, bins, tables, spectra, nv, lenv, nzp, mfl, -1, -1,
+                    reso=True, oversample=osamp, deconv_m=1.0)
+
+
 def make_workload(name: str, seed: int | None = None, n_chunks: int | None = None) -> Workload:
     """Build one of the named synthetic workloads."""
-    seeds = {"small": 20240601, "desi": 20240602, "echelle": 20240604, "tiny": 20240605}
+    seeds = {"small": 20240601, "desi": 20240602, "echelle": 20240604, "tiny": 20240605,
+             "desi_reso": 20240606, "tiny_reso": 20240607, "tiny_reso_dia": 20240607}
     seed = seeds[name] if seed is None else seed
     rng = np.random.Generator(np.random.PCG64(seed))
+    if name in ("desi_reso", "tiny_reso", "tiny_reso_dia"):
+        nch = (16384 if name == "desi_reso" else 6) if n_chunks is None else n_chunks
+        return _make_reso_workload(name, rng, seed, nch)
     if name in ("small", "tiny"):
         bins = Bins(0.0, 20, 2e-3, 0, 0.0, 2.2, 0.2, 3)
         nch = 64 if name == "small" else 6
@@ -301,6 +376,15 @@ def write_dat(path: str, s: Spectrum):
         f.write(np.ascontiguousarray(s.wave, dtype="<f8").tobytes())
         f.write(np.ascontiguousarray(s.delta, dtype="<f8").tobytes())
         f.write(np.ascontiguousarray(s.sigma, dtype="<f8").tobytes())
+
+
+def write_resomat(path: str, values: np.ndarray):
+    """Side file of a binary spectrum holding its resolution matrix for the
+    oracle driver: int32 n, int32 ndiags, then values[ndiags][n] as doubles."""
+    nd, n = values.shape
+    with open(path, "wb") as f:
+        f.write(struct.pack("<ii", n, nd))
+        f.write(np.ascontiguousarray(values, dtype="<f8").tobytes())
 
 
 def read_dat(path: str) -> Spectrum:
@@ -396,6 +480,8 @@ def write_reference_inputs(w: Workload, outdir: str, marg=None) -> str:
     for i, s in enumerate(w.spectra):
         nm = f"chunk{i:05d}.dat"
         write_dat(os.path.join(spec_dir, nm), s)
+        if w.reso:
+            write_resomat(os.path.join(spec_dir, nm + ".rmat"), s.resomat)
         names.append(nm)
     with open(os.path.join(outdir, "flist.txt"), "w") as f:
         f.write(f"{len(names)}\n" + "\n".join(names) + "\n")
@@ -442,6 +528,8 @@ NumberOfBoots 0
 SmoothNoiseWeights -1
 AllocatedMemoryMB 200000.
 TemporaryFolder {outdir}
+OversampleRmat {w.oversample}
+ResoMatDeconvolutionM {w.deconv_m!r}
 """
     path = os.path.join(outdir, "qmle.config")
     with open(path, "w") as f:

@@ -72,6 +72,11 @@ class ChunkData:
     zbin_upp: int
     nq: int
     fisher_index_start: int
+    # resolution matrix (UseResoMatrix): dense R (n x ncols) and the grid the
+    # signal and derivative matrices are evaluated on before R . M . R^T
+    # (lambda / LYA_REST, ncols points); None without a resolution matrix
+    rmat: np.ndarray | None = None
+    fine_wave: np.ndarray | None = None
 
     @property
     def n(self):
@@ -107,11 +112,16 @@ def cut_masked_boundary(ivar):
     return int(nz[0]), int(nz[-1]) + 1
 
 
-def preprocess_spectrum(spec, bins):
+def preprocess_spectrum(spec, bins, reso=None):
     """Reading and cleaning of one binary spectrum: io/qso_file.cpp:352-369
     (sigma -> ivar), :189-230 (maskOutliers), :159-187 (cutBoundary) and
     core/one_qso_estimate.cpp:52-100.  Returns (wave, delta, ivar) in
-    Angstrom, or raises ValueError when the reference would drop the file."""
+    Angstrom, or raises ValueError when the reference would drop the file.
+    With reso = (oversampling, deconvolution m) the spectrum's resolution
+    matrix is deconvolved and oversampled before the cut
+    (core/one_qso_estimate.cpp:75-89) and a fourth item, the matrix cut with
+    the pixels (rows [n][nelem] when oversampled, else values[ndiags][n]),
+    is returned."""
     wave = np.array(spec.wave, dtype=np.float64)
     delta = np.array(spec.delta, dtype=np.float64)
     ivar = 1.0 / (np.asarray(spec.sigma, dtype=np.float64) ** 2)
@@ -129,6 +139,17 @@ def preprocess_spectrum(spec, bins):
         if delta[i] < (-1.0 - s) or delta[i] > (fup + s):
             delta[i] = 0.0
             ivar[i] = 0.0
+    rm = None
+    if reso is not None:
+        osamp, m = reso
+        vals = np.array(spec.resomat, dtype=np.float64)
+        if m > 0:
+            vals = dia_deconvolve(vals, m)
+        if osamp > 0:
+            dlam = _median(np.diff(wave))          # QSOFile::readData, io/qso_file.cpp:124-128
+            rm = dia_oversample(vals, osamp, dlam)
+        else:
+            rm = vals
     # cutBoundary
     l1, l2 = LYA_REST * (1 + bins.z_lower), LYA_REST * (1 + bins.z_upper)
     wi1 = int(np.searchsorted(wave, l1, side="left"))
@@ -140,7 +161,138 @@ def preprocess_spectrum(spec, bins):
     wave, delta, ivar = wave[a:b], delta[a:b], ivar[a:b]
     if int((ivar != 0).sum()) < MIN_PIXELS_IN_FILE:
         raise ValueError("Short file")
-    return wave, delta, ivar
+    if reso is None:
+        return wave, delta, ivar
+    lo, hi = wi1 + a, wi1 + b
+    rm = rm[lo:hi] if reso[0] > 0 else rm[:, lo:hi]
+    return wave, delta, ivar, rm
+
+
+# ---------------------------------------------------------------------------
+# Resolution matrices (mathtools/matrix_helper.cpp:503-1095, real_field.cpp:78-110)
+
+def dia_row_indices(i, n, ndiags):
+    """DiaMatrix::_getRowIndices, mathtools/matrix_helper.cpp:608-620: flat
+    indices into values[ndiags][n] of row i's entries, columns i - noff ..
+    i + noff; entries beyond an edge repeat the mirrored entry of the row."""
+    noff = ndiags // 2
+    idx = [j * n + (noff - j) + i for j in range(ndiags - 1, -1, -1)]
+    if i < noff:
+        for j in range(noff - i):
+            idx[j] = idx[ndiags - 1 - j]
+    elif i > n - noff - 1:
+        for j in range(i - n + noff + 1):
+            idx[ndiags - 1 - j] = idx[j]
+    return idx
+
+
+def dia_deconvolve(values, m):
+    """DiaMatrix::deconvolve (mathtools/matrix_helper.cpp:653-682) with
+    RealField::deconvolveSinc (real_field.cpp:78-110): each row, zero-padded by
+    5 on both sides, is divided by sinc(pi m i / size) in Fourier space."""
+    nd, n = values.shape
+    flat = values.ravel()
+    pad = 5
+    size = nd + 2 * pad
+    for i in range(n):
+        idx = dia_row_indices(i, n, nd)
+        x = np.zeros(size)
+        x[pad:pad + nd] = flat[idx]
+        fk = np.fft.rfft(x)
+        for k in range(1, size // 2 + 1):
+            a = math.pi * m * k / size
+            fk[k] /= math.sin(a) / a
+        out = np.fft.irfft(fk, n=size)
+        for p_ in range(nd):
+            flat[idx[p_]] = out[p_ + pad]
+    return flat.reshape(nd, n)
+
+
+def natural_cspline(x, y):
+    """Second derivatives M of the natural cubic spline through (x, y)."""
+    n = len(x)
+    mm = np.zeros(n)
+    if n < 3:
+        return mm
+    h = np.diff(x)
+    k = n - 2
+    diag = 2.0 * (h[:-1] + h[1:])
+    upper = h[1:].copy()
+    rhs = 6.0 * ((y[2:] - y[1:-1]) / h[1:] - (y[1:-1] - y[:-2]) / h[:-1])
+    for j in range(1, k):
+        f = h[j] / diag[j - 1]
+        diag[j] -= f * upper[j - 1]
+        rhs[j] -= f * rhs[j - 1]
+    mm[k] = rhs[k - 1] / diag[k - 1]
+    for j in range(k - 2, -1, -1):
+        mm[j + 1] = (rhs[j] - upper[j] * mm[j + 2]) / diag[j]
+    return mm
+
+
+def cspline_eval(x, y, mm, t):
+    """Natural cubic spline at t (x[0] <= t <= x[-1])."""
+    i = min(max(int(np.searchsorted(x, t, side="right")) - 1, 0), len(x) - 2)
+    h = x[i + 1] - x[i]
+    t1, t0 = x[i + 1] - t, t - x[i]
+    return ((mm[i] * t1 ** 3 + mm[i + 1] * t0 ** 3) / (6.0 * h)
+            + (y[i] / h - mm[i] * h / 6.0) * t1 + (y[i + 1] / h - mm[i + 1] * h / 6.0) * t0)
+
+
+def _nonzero_min_element(row):
+    """nonzero_min_element, mathtools/matrix_helper.cpp:20-39."""
+    smallest = abs(row[0])
+    for v in row[1:]:
+        tmp = abs(v)
+        if smallest < 1e-15:
+            smallest = tmp
+        elif tmp < smallest and tmp > 1e-15:
+            smallest = tmp
+    return max(smallest, 1e-15)
+
+
+def dia_oversample(values, osamp, dlambda):
+    """Resolution::oversample, mathtools/matrix_helper.cpp:1008-1073: each row's
+    ndiags entries, shifted positive and log-transformed, go through a natural
+    cubic spline evaluated at osamp x finer spacing; rows renormalised to unit
+    sum.  Returns rows [n][2 noff osamp + 1]."""
+    nd, n = values.shape
+    flat = values.ravel()
+    noff = nd // 2
+    nelem = 2 * noff * osamp + 1
+    win = np.array([(i - noff) * dlambda for i in range(nd)])
+    wout = np.array([(i * 1. / osamp - noff) * dlambda for i in range(nelem)])
+    out = np.empty((n, nelem))
+    for i in range(n):
+        row = flat[dia_row_indices(i, n, nd)].copy()
+        shift = float(np.min(row)) - _nonzero_min_element(row)
+        lrow = np.log(row - shift)
+        mm = natural_cspline(win, lrow)
+        new = np.array([shift + math.exp(cspline_eval(win, lrow, mm, t)) for t in wout])
+        out[i] = new * (1.0 / new.sum())
+    return out
+
+
+def resolution_dense(rows, oversampled, n):
+    """Dense R of a chunk: oversampled rows (n x nelem) sit at columns
+    i * osamp .. (OversampledMatrix, matrix_helper.cpp:859-920); a diagonal
+    matrix values[ndiags][n] gives R[c - off][c] = values[d][c]."""
+    if oversampled is not None:
+        nelem = rows.shape[1]
+        ncols = n * oversampled + nelem - 1
+        r = np.zeros((n, ncols))
+        for i in range(n):
+            r[i, i * oversampled:i * oversampled + nelem] = rows[i]
+        return r
+    nd = rows.shape[0]
+    noff = nd // 2
+    r = np.zeros((n, n))
+    for d in range(nd):
+        off = noff - d
+        for c in range(n):
+            row = c - off
+            if 0 <= row < n:
+                r[row, c] = rows[d, c]
+    return r
 
 
 def decide_indices(wave, settings):
@@ -164,11 +316,15 @@ def decide_indices(wave, settings):
     return idx
 
 
-def make_chunk(wave, delta, ivar, r_fwhm, bins, table_keys, settings):
+def make_chunk(wave, delta, ivar, r_fwhm, bins, table_keys, settings, reso=None, rm=None):
     """Chunk::Chunk, core/chunk_estimate.cpp:141-257 (raises ValueError where
-    the reference throws).  table_keys maps (R, dv rounded to 0.1) -> index."""
+    the reference throws).  table_keys maps (R, dv rounded to 0.1) -> index.
+    With a resolution matrix (reso = (oversampling, m), rm its slice for these
+    pixels) the table is the first one (RES_INDEX = 0, :189-193)."""
     a, b = cut_masked_boundary(ivar)
     wave, delta, ivar = wave[a:b].copy(), delta[a:b].copy(), ivar[a:b].copy()
+    if rm is not None:
+        rm = rm[a:b] if reso[0] > 0 else rm[:, a:b]
     n = len(wave)
     realsize = int((ivar != 0).sum())
     dv = _median(np.log(wave[1:] / wave[:-1]) * C_KMS) if n > 1 else -1.0
@@ -178,7 +334,11 @@ def make_chunk(wave, delta, ivar, r_fwhm, bins, table_keys, settings):
         raise ValueError("Short chunk")
     rounded = _c_round(dv * 10) / 10
     res_index = -1
+    if reso is not None:
+        res_index = 0
     for (r, tdv), idx in table_keys.items():
+        if res_index >= 0:
+            break
         if r == r_fwhm and abs(rounded - tdv) < 0.01:
             res_index = idx
             break
@@ -196,24 +356,45 @@ def make_chunk(wave, delta, ivar, r_fwhm, bins, table_keys, settings):
         if bins.z_centers[zupp] < zmax and zupp < bins.nz - 1:
             nq += 1
     nq *= bins.nk
+    rmat = fine = None
+    if reso is not None:
+        osamp = reso[0]
+        rmat = resolution_dense(rm, osamp if osamp > 0 else None, n)
+        w0 = wave[0] / LYA_REST
+        if osamp > 0:
+            # Chunk::_initMatrices, core/chunk_estimate.cpp:927-938; dlambda is
+            # the chunk's median pixel width (QSOFile copy, io/qso_file.cpp:86-88)
+            dlam = _median(np.diff(wave)) if n > 1 else -1.0
+            fine_dl = dlam / LYA_REST / osamp
+            disp = rm.shape[1] // 2
+            fine = np.array([w0 + (i - disp) * fine_dl for i in range(rmat.shape[1])])
+        else:
+            fine = wave / LYA_REST
     return ChunkData(wave / LYA_REST, delta, ivar, int(r_fwhm), float(dv), res_index, kbin_upp,
-                     zlow, zupp, nq, fis)
+                     zlow, zupp, nq, fis, rmat, fine)
 
 
-def chunks_from_spectra(spectra, bins, table_keys, settings):
+def chunks_from_spectra(spectra, bins, table_keys, settings, reso=None):
     """OneQSOEstimate construction for every spectrum; chunks the reference
-    would reject are skipped, as OneQSOEstimate::OneQSOEstimate does."""
+    would reject are skipped, as OneQSOEstimate::OneQSOEstimate does.
+    reso = (oversampling, deconvolution m) uses each spectrum's resolution
+    matrix (UseResoMatrix)."""
     out = []
     for s in spectra:
         try:
-            wave, delta, ivar = preprocess_spectrum(s, bins)
+            pre = preprocess_spectrum(s, bins, reso)
         except ValueError:
             continue
+        wave, delta, ivar = pre[:3]
+        rm = pre[3] if reso is not None else None
         idx = decide_indices(wave, settings)
         for i1, i2 in zip(idx[:-1], idx[1:]):
+            sl = None
+            if rm is not None:
+                sl = rm[i1:i2] if reso[0] > 0 else rm[:, i1:i2]
             try:
                 out.append(make_chunk(wave[i1:i2], delta[i1:i2], ivar[i1:i2], s.r_fwhm, bins,
-                                      table_keys, settings))
+                                      table_keys, settings, reso, sl))
             except (ValueError, KeyError):
                 continue
     return out
@@ -306,17 +487,43 @@ def build_matrices(ch: ChunkData, bins, tv: TableView):
     ns = len(stored)
     q = np.empty((ns, n, n))
     vu = vmat[iu]
-    for kn in range(ch.kbin_upp):
-        m = np.empty((n, n))
-        m[iu] = interp1d(tv.deriv[kn], tv.v1, tv.dv, vu)
-        q[kn] = _sym_upper_fill(m)
+    nzp = tv.signal.shape[1]
+    if ch.rmat is None:
+        for kn in range(ch.kbin_upp):
+            m = np.empty((n, n))
+            m[iu] = interp1d(tv.deriv[kn], tv.v1, tv.dv, vu)
+            q[kn] = _sym_upper_fill(m)
+        sm = np.empty((n, n))
+        sm[iu] = interp2d(tv.signal.ravel(), nzp, tv.signal.shape[0], tv.z1, tv.dz, tv.v1, tv.dv,
+                          zmat[iu], vu)
+        sm = _sym_upper_fill(sm)
+    else:
+        # UseResoMatrix: S and Q_k on the resolution matrix's grid, then
+        # R . M . R^T (core/chunk_estimate.cpp:400-480); Q_k is the analytic
+        # band (dk / pi) cos(k_c v) sinc(dk v / 2) (:444-454)
+        nf = len(ch.fine_wave)
+        fi, fj = ch.fine_wave[:, None], ch.fine_wave[None, :]
+        iuf = np.triu_indices(nf)
+        vf = (C_KMS * np.log(fj / fi))[iuf]
+        zf = (np.sqrt(fi * fj) - 1.0)[iuf]
+        r = ch.rmat
+        for kn in range(ch.kbin_upp):
+            kc = bins.k_centers[kn]
+            dk = bins.k_edges[kn + 1] - bins.k_edges[kn]
+            x = dk * vf / 2
+            with np.errstate(invalid="ignore", divide="ignore"):
+                val = np.where(vf == 0, dk / math.pi, (dk / math.pi) * np.cos(kc * vf) * (np.sin(x) / x))
+            m = np.empty((nf, nf))
+            m[iuf] = val
+            m = _sym_upper_fill(m)
+            q[kn] = _sym_upper_fill(r @ m @ r.T)
+        m = np.empty((nf, nf))
+        m[iuf] = interp2d(tv.signal.ravel(), nzp, tv.signal.shape[0], tv.z1, tv.dz, tv.v1, tv.dv,
+                          zf, vf)
+        m = _sym_upper_fill(m)
+        sm = _sym_upper_fill(r @ m @ r.T)
     for s in range(ch.kbin_upp, ns):
         q[s] = q[stored[s] % bins.nk]
-    nzp = tv.signal.shape[1]
-    sm = np.empty((n, n))
-    sm[iu] = interp2d(tv.signal.ravel(), nzp, tv.signal.shape[0], tv.z1, tv.dz, tv.v1, tv.dv,
-                      zmat[iu], vu)
-    sm = _sym_upper_fill(sm)
     zu = zmat[iu]
     nzb = ns // ch.kbin_upp
     for iz in range(nzb):

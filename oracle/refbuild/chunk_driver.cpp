@@ -13,7 +13,18 @@
 // (F *= 0.5, copyUpperToLower), :261-288 (stableInvertSym) and :290-318
 // (theta = 0.5 F^-1 (d - b - t)) with the reference's own mxhelp routines.
 //
-// Usage: chunk_driver <config> <out.bin> [--no-pixels]
+// With --reso, every spectrum X.dat comes with X.dat.rmat, its resolution
+// matrix in the reference's DiaMatrix layout (int32 n, int32 ndiags, then
+// ndiags x n doubles, diagonal d holding offset ndiags/2 - d, element of
+// column c at [d][c]).  The reference reads such matrices only from picca FITS
+// files (io/qso_file.cpp:652-677); the driver attaches them to the binary
+// spectrum instead and then follows OneQSOEstimate::_readQsoFile
+// (core/one_qso_estimate.cpp:52-100) step by step: deconvolution, oversampling,
+// boundary cut, chunking by decideIndices and Chunk::Chunk.  The config's
+// OversampleRmat and ResoMatDeconvolutionM keys apply;
+// specifics::USE_RESOLUTION_MATRIX is switched on after the config is read.
+//
+// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso]
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +37,7 @@
 #include "core/global_numbers.hpp"
 #include "core/one_qso_estimate.hpp"
 #include "core/sq_table.hpp"
+#include "io/qso_file.hpp"
 #include "io/config_file.hpp"
 #include "io/io_helper_functions.hpp"
 #include "io/logger.hpp"
@@ -35,14 +47,63 @@
 namespace {
 void putI(FILE *f, int v) { std::fwrite(&v, sizeof v, 1, f); }
 void putD(FILE *f, const double *v, size_t n) { if (n) std::fwrite(v, sizeof(double), n, f); }
+
+// One spectrum with its resolution matrix, read as OneQSOEstimate::_readQsoFile
+// does (core/one_qso_estimate.cpp:52-100), the matrix coming from X.rmat.
+std::unique_ptr<OneQSOEstimate> read_with_resomat(const std::string &path) {
+    auto q = std::make_unique<OneQSOEstimate>();
+    try {
+        auto qFile = std::make_unique<qio::QSOFile>(path, qio::Binary);
+        qFile->readParameters();
+        if (qFile->snr < specifics::MIN_SNR_CUT) throw std::runtime_error("Low SNR");
+        qFile->readData();
+        conv::convertFluxToDeltaF(qFile->wave(), qFile->delta(), qFile->ivar(), qFile->size());
+        qFile->maskOutliers();
+
+        FILE *rf = std::fopen((path + ".rmat").c_str(), "rb");
+        if (!rf) throw std::runtime_error("missing resolution matrix file");
+        int hdr[2] = {0, 0};
+        if (std::fread(hdr, sizeof(int), 2, rf) != 2 || hdr[0] != qFile->size()) {
+            std::fclose(rf);
+            throw std::runtime_error("resolution matrix size mismatch");
+        }
+        qFile->Rmat = std::make_unique<mxhelp::Resolution>(hdr[0], hdr[1]);
+        size_t nval = (size_t) hdr[0] * hdr[1];
+        size_t got = std::fread(qFile->Rmat->matrix(), sizeof(double), nval, rf);
+        std::fclose(rf);
+        if (got != nval) throw std::runtime_error("short resolution matrix file");
+        if (specifics::RESOMAT_DECONVOLUTION_M > 0)
+            qFile->Rmat->deconvolve(specifics::RESOMAT_DECONVOLUTION_M);
+        if (specifics::OVERSAMPLING_FACTOR > 0)
+            qFile->Rmat->oversample(specifics::OVERSAMPLING_FACTOR, qFile->dlambda);
+        qFile->closeFile();
+        qFile->cutBoundary(bins::Z_LOWER_EDGE, bins::Z_UPPER_EDGE);
+        if (qFile->realSize() < 100) throw std::runtime_error("Short file");
+
+        std::vector<int> indices = OneQSOEstimate::decideIndices(qFile->size(), qFile->wave());
+        for (size_t nc = 0; nc + 1 < indices.size(); ++nc) {
+            try {
+                q->chunks.push_back(std::make_unique<Chunk>(*qFile, indices[nc], indices[nc + 1]));
+            } catch (std::exception &) {
+            }
+        }
+    } catch (std::exception &e) {
+        std::fprintf(stderr, "%s: %s\n", path.c_str(), e.what());
+    }
+    return q;
+}
 }
 
 int main(int argc, char *argv[]) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s <config> <out.bin> [--no-pixels]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <config> <out.bin> [--no-pixels] [--reso]\n", argv[0]);
         return 2;
     }
-    bool dump_pixels = !(argc > 3 && std::strcmp(argv[3], "--no-pixels") == 0);
+    bool dump_pixels = true, reso = false;
+    for (int a = 3; a < argc; ++a) {
+        if (std::strcmp(argv[a], "--no-pixels") == 0) dump_pixels = false;
+        else if (std::strcmp(argv[a], "--reso") == 0) reso = true;
+    }
 
     ConfigFile config;
     config.readFile(argv[1]);
@@ -51,6 +112,7 @@ int main(int argc, char *argv[]) {
     bins::readBins(config);
     specifics::readSpecifics(config);
     conv::readConversion(config);
+    if (reso) specifics::USE_RESOLUTION_MATRIX = true;
     fidcosmo::readFiducialCosmo(config);
 
     process::sq_private_table = std::make_unique<SQLookupTable>(config);
@@ -71,7 +133,8 @@ int main(int argc, char *argv[]) {
     std::vector<std::unique_ptr<OneQSOEstimate>> qsos;
     qsos.reserve(fpaths.size());
     for (auto &fp : fpaths)
-        qsos.push_back(std::make_unique<OneQSOEstimate>(findir + fp));
+        qsos.push_back(reso ? read_with_resomat(findir + fp)
+                            : std::make_unique<OneQSOEstimate>(findir + fp));
 
     glmemory::allocMemory();
 
@@ -83,7 +146,7 @@ int main(int argc, char *argv[]) {
 
     FILE *out = std::fopen(argv[2], "wb");
     if (!out) { std::perror("fopen"); return 1; }
-    std::fwrite("LQGREF01", 1, 8, out);
+    std::fwrite("LQGREF02", 1, 8, out);
     putI(out, nkz);
     putI(out, bins::NUMBER_OF_K_BANDS);
     putI(out, bins::NUMBER_OF_Z_BINS);
@@ -100,6 +163,13 @@ int main(int argc, char *argv[]) {
             std::vector<double> w(ch.qFile->wave(), ch.qFile->wave() + n),
                 d(ch.qFile->delta(), ch.qFile->delta() + n),
                 iv(ch.qFile->ivar(), ch.qFile->ivar() + n);
+            std::vector<double> rm;
+            int rm_dia = 0, rm_nelem = 0;
+            if (reso && ch.qFile->Rmat) {
+                rm.assign(ch.qFile->Rmat->matrix(), ch.qFile->Rmat->matrix() + ch.qFile->Rmat->getSize());
+                rm_dia = ch.qFile->Rmat->isDiaMatrix() ? 1 : 0;
+                rm_nelem = ch.qFile->Rmat->getNElemPerRow();
+            }
 
             std::vector<std::unique_ptr<double[]>> dbt_local;
             for (int i = 0; i < 3; ++i) dbt_local.push_back(std::make_unique<double[]>(nkz));
@@ -127,6 +197,10 @@ int main(int argc, char *argv[]) {
             putD(out, &dv, 1);
             putI(out, dump_pixels ? 1 : 0);
             if (dump_pixels) { putD(out, w.data(), n); putD(out, d.data(), n); putD(out, iv.data(), n); }
+            // the chunk's resolution matrix: diagonal (values[ndiags][n]) or
+            // oversampled (rows[n][nelem]), as the chunk holds it
+            putI(out, (int) rm.size()); putI(out, rm_dia); putI(out, rm_nelem);
+            putD(out, rm.data(), rm.size());
             for (int i = 0; i < 3; ++i) putD(out, ch.dbt_estimate_before_fisher_vector[i].get(), nq);
             putD(out, ch.fisher_matrix.get(), (size_t) nq * nq);
         }

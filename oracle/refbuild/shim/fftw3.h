@@ -1,9 +1,9 @@
 /* Test-infrastructure shim (oracle build only).
  *
- * FFTW is not installed in this image.  lyspeq uses FFTs only to build the
- * signal lookup table and to deconvolve resolution matrices, both off the
- * per-chunk QMLE path.  The prototypes below let those translation units
- * compile; the definitions in gsl_fftw_stubs.cpp throw if reached.
+ * FFTW is not installed in this image.  lyspeq uses FFTs to build the
+ * signal lookup table (not reached here) and to deconvolve resolution-matrix
+ * rows (RealField::deconvolveSinc).  gsl_fftw_stubs.cpp defines the 1-D
+ * real-to-complex and complex-to-real transforms by their definition.
  */
 #ifndef LQG_ORACLE_SHIM_FFTW3_H
 #define LQG_ORACLE_SHIM_FFTW3_H

@@ -1,11 +1,11 @@
 /* Test-infrastructure shim (oracle build only).
  *
- * GSL is not installed in this image.  The GSL routines that lyspeq calls are
- * all off the per-chunk QMLE path: QAWO integration and FFTs build the S/Q
- * lookup tables, cubic splines read tabulated fiducial power or mean flux and
- * oversample resolution matrices.  This header declares the types and
- * prototypes those translation units use so that they compile; every function
- * is defined in gsl_fftw_stubs.cpp and throws if it is ever reached.
+ * GSL is not installed in this image.  Most GSL routines that lyspeq calls
+ * are off the per-chunk QMLE path (QAWO integration and FFTs build the S/Q
+ * lookup tables).  This header declares the types and prototypes those
+ * translation units use so that they compile.  gsl_fftw_stubs.cpp implements
+ * the 1-D interpolators (natural cubic spline, linear), which oversample
+ * resolution matrices, and throws for everything else.
  */
 #ifndef LQG_ORACLE_SHIM_GSL_COMMON_H
 #define LQG_ORACLE_SHIM_GSL_COMMON_H

@@ -4,7 +4,8 @@ The dump is written by ``oracle/refbuild/chunk_driver.cpp``, which runs
 lyspeq's own ``Chunk::oneQSOiteration`` (core/chunk_estimate.cpp:837-914) on
 every chunk of a config and then the global Newton-Raphson step
 (core/quadratic_estimate.cpp:456-457, 261-318).  Layout: little-endian,
-``LQGREF01`` magic, four int32 (nkz, nk, nz, nchunks), one record per chunk,
+``LQGREF02`` magic, four int32 (nkz, nk, nz, nchunks), one record per chunk
+(with the chunk's resolution matrix when the driver ran with ``--reso``),
 then a ``GLOBAL01`` block.
 """
 from __future__ import annotations
@@ -39,6 +40,8 @@ class RefChunk:
     b: np.ndarray
     t: np.ndarray
     fisher: np.ndarray        # nq x nq, upper triangle filled, not halved
+    rmat: np.ndarray | None = None   # values[ndiags][n] (diagonal) or rows[n][nelem]
+    rmat_dia: bool = False
 
 
 @dataclasses.dataclass
@@ -85,7 +88,7 @@ class _Reader:
 def read_dump(path: str) -> RefDump:
     with open(path, "rb") as f:
         r = _Reader(f.read())
-    r.magic(b"LQGREF01")
+    r.magic(b"LQGREF02")
     nkz, nk, nz, nch = (r.i() for _ in range(4))
     chunks = []
     for _ in range(nch):
@@ -95,9 +98,15 @@ def read_dump(path: str) -> RefDump:
         w = dl = iv = None
         if has_pix:
             w, dl, iv = r.d(n), r.d(n), r.d(n)
+        nrm, rdia, nelem = r.i(), r.i(), r.i()
+        rm = None
+        if nrm:
+            rm = r.d(nrm)
+            rm = rm.reshape(nelem, n) if rdia else rm.reshape(n, nelem)
         d, b, t = r.d(nq), r.d(nq), r.d(nq)
         fm = r.d(nq * nq).reshape(nq, nq)
-        chunks.append(RefChunk(qso, idx, n, fis, nq, kup, rf, st, dv, w, dl, iv, d, b, t, fm))
+        chunks.append(RefChunk(qso, idx, n, fis, nq, kup, rf, st, dv, w, dl, iv, d, b, t, fm,
+                               rm, bool(rdia)))
     r.magic(b"GLOBAL01")
     fisher = r.d(nkz * nkz).reshape(nkz, nkz)
     dbt = np.stack([r.d(nkz) for _ in range(3)])
@@ -116,14 +125,15 @@ def available() -> bool:
     return os.path.exists(DRIVER)
 
 
-def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None) -> RefDump:
+def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None,
+               reso: bool = False) -> RefDump:
     env = dict(os.environ)
     env.setdefault("OPENBLAS_NUM_THREADS", "1")
     # One OpenMP thread: with more, Chunk::_applyRedshiftInterp races on the
     # shared `low`/`tmp` bounds (core/chunk_estimate.cpp:486, 512-516) and the
     # redshift weights of some rows come out wrong from run to run.
     env["OMP_NUM_THREADS"] = str(threads or 1)
-    args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"])
+    args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else [])
     subprocess.run(args, check=True, env=env, stdout=subprocess.DEVNULL,
                    stderr=subprocess.DEVNULL)
     return read_dump(out)

@@ -38,6 +38,8 @@ CASES = {
     "tiny_masked": ("tiny", None, (1, -1), 0.04, None),
     "small_cfg": ("small", None, (-1, -1), 0.0, 12),
     "desi_sub": ("desi", 6, (1, -1), 0.0, None),
+    "tiny_reso": ("tiny_reso", None, (-1, -1), 0.0, None),
+    "tiny_reso_dia": ("tiny_reso_dia", None, (-1, -1), 0.0, None),
 }
 
 
@@ -59,7 +61,7 @@ def make_case(name, spec):
     _mask(w, mask, 99)
     with tempfile.TemporaryDirectory() as tmp:
         cfg = synth.write_reference_inputs(w, tmp)
-        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"))
+        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso)
     chunks = dump.chunks
     if keep is not None:
         chunks = chunks[:keep]
@@ -76,6 +78,16 @@ def make_case(name, spec):
         g_inverse=dump.inverse_fisher, g_damped=np.array(dump.damped),
         g_complete=np.array(keep is None),
     )
+    if w.reso:
+        # resolution-matrix case: the reader's options, every spectrum's raw
+        # matrix and wavelengths (for the preprocessing parity) and, per chunk,
+        # the matrix as the reference's chunk holds it after deconvolution,
+        # oversampling and the cuts
+        out["reso"] = np.array([w.oversample, w.deconv_m])
+        out["n_spectra"] = np.array(len(w.spectra))
+        for j, sp in enumerate(w.spectra):
+            out[f"s{j}_lam"] = sp.wave
+            out[f"s{j}_resomat"] = sp.resomat
     for i, c in enumerate(chunks):
         # the chunk is a contiguous slice of its spectrum; keep the wavelengths in
         # Angstrom as read from the file so that lambda / LYA_REST is bit-identical
@@ -90,6 +102,9 @@ def make_case(name, spec):
         out[f"c{i}_ivar"] = c.ivar
         out[f"c{i}_dbt"] = np.stack([c.d, c.b, c.t])
         out[f"c{i}_fisher"] = c.fisher
+        if w.reso:
+            out[f"c{i}_rmat"] = c.rmat
+            out[f"c{i}_src"] = np.array([c.qso, start], dtype=np.int64)
     path = os.path.join(HERE, f"{name}.npz")
     np.savez_compressed(path, **out)
     print(f"{name}: {len(chunks)} chunks -> {os.path.getsize(path) / 1024:.0f} KiB")
@@ -98,8 +113,9 @@ def make_case(name, spec):
 def main():
     if not refdump.available():
         raise SystemExit("oracle not built: make -C oracle/refbuild")
-    for name, spec in CASES.items():
-        make_case(name, spec)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        make_case(name, CASES[name])
 
 
 if __name__ == "__main__":

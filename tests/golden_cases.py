@@ -9,7 +9,9 @@ import numpy as np
 from lyspeq_gb300 import synth
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub"]
+CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub",
+         "tiny_reso", "tiny_reso_dia"]
+RESO_CASES = ["tiny_reso", "tiny_reso_dia"]
 
 
 @dataclasses.dataclass
@@ -28,6 +30,13 @@ class GoldenCase:
     fisher: list          # per chunk nq x nq
     g: dict               # global reference results
     complete: bool
+    # resolution-matrix cases: (oversampling, deconvolution m), per chunk the
+    # matrix as the reference's chunk holds it and (spectrum, first pixel),
+    # per spectrum (lambda, raw DiaMatrix values)
+    reso: tuple | None = None
+    rmats: list | None = None
+    src: list | None = None
+    spectra: list | None = None
 
 
 _cache = {}
@@ -56,6 +65,11 @@ def load(name: str) -> GoldenCase:
     g = {k[2:]: z[k] for k in z.files if k.startswith("g_")}
     case = GoldenCase(name, bins, tables, nv, float(lenv), nzp, float(mfl), (int(m0), int(m1)),
                       chunks, meta, dbt, fis, g, bool(z["g_complete"]))
+    if "reso" in z.files:
+        case.reso = (int(z["reso"][0]), float(z["reso"][1]))
+        case.rmats = [z[f"c{i}_rmat"] for i in range(n)]
+        case.src = [tuple(int(x) for x in z[f"c{i}_src"]) for i in range(n)]
+        case.spectra = [(z[f"s{j}_lam"], z[f"s{j}_resomat"]) for j in range(int(z["n_spectra"]))]
     _cache[name] = case
     return case
 

@@ -89,8 +89,11 @@ def test_port_matches_reference(name):
     keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
     tvs = [P.table_view(t, c.bins, c.nv, c.lenv, c.nzp) for t in c.tables]
     results = []
-    for (lam, delta, ivar, r), meta, dbt, fis in zip(c.chunks, c.meta, c.dbt, c.fisher):
-        ch = P.make_chunk(lam, delta, ivar, r, c.bins, keys, s)
+    for i, ((lam, delta, ivar, r), meta, dbt, fis) in enumerate(zip(c.chunks, c.meta, c.dbt, c.fisher)):
+        if c.reso is None:
+            ch = P.make_chunk(lam, delta, ivar, r, c.bins, keys, s)
+        else:
+            ch = P.make_chunk(lam, delta, ivar, r, c.bins, keys, s, c.reso, c.rmats[i])
         assert (ch.n, ch.fisher_index_start, ch.nq, ch.kbin_upp) == meta[:4]
         d, b, t, f = P.chunk_iteration(ch, c.bins, tvs[ch.res_index], np.zeros(c.bins.nkz), s)
         assert G.rel_err(d, dbt[0]) < tol
@@ -104,3 +107,33 @@ def test_port_matches_reference(name):
         assert G.rel_err(g["fisher"], c.g["fisher"]) < tol
         assert G.rel_err(dbtsum, c.g["dbt"]) < tol
         assert G.rel_err(g["theta"], c.g["theta"]) < max(tol, 1e-10)
+
+
+@pytest.mark.parametrize("name", G.RESO_CASES)
+def test_port_resolution_preprocessing_matches_reference(name):
+    """Deconvolution and oversampling of each spectrum's resolution matrix
+    (core/one_qso_estimate.cpp:75-89), cut to a chunk's pixels, give the
+    matrix the reference's chunk holds."""
+    c = G.load(name)
+    osamp, m = c.reso
+    prepared = {}
+    for i, (qso, start) in enumerate(c.src):
+        if qso not in prepared:
+            lam, vals = c.spectra[qso]
+            v = P.dia_deconvolve(np.array(vals), m) if m > 0 else np.array(vals)
+            prepared[qso] = P.dia_oversample(v, osamp, P._median(np.diff(lam))) if osamp > 0 else v
+        n = c.meta[i][0]
+        mine = prepared[qso][start:start + n] if osamp > 0 else prepared[qso][:, start:start + n]
+        assert np.max(np.abs(mine - c.rmats[i])) < 1e-12
+
+
+def test_natural_cspline_matches_scipy():
+    from scipy.interpolate import CubicSpline
+    rng = np.random.Generator(np.random.PCG64(5))
+    x = np.sort(rng.uniform(-3, 3, size=11))
+    y = rng.normal(size=11)
+    mm = P.natural_cspline(x, y)
+    ref = CubicSpline(x, y, bc_type="natural")
+    t = np.linspace(x[0], x[-1], 97)
+    mine = np.array([P.cspline_eval(x, y, mm, u) for u in t])
+    assert np.max(np.abs(mine - ref(t))) < 1e-12
