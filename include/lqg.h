@@ -121,6 +121,43 @@ int lqg_abi_version(void);
 int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
                   const double *lambda, const double *delta, const double *ivar,
                   const int *r_fwhm, int *status_out);
+/* Add chunks that carry a resolution matrix (UseResoMatrix): lyspeq then
+ * evaluates S and the band derivatives Q_k on the matrix's grid and uses
+ * R S R^T and R Q_k R^T (Chunk::_setFiducialSignalMatrix, _setQiMatrix,
+ * core/chunk_estimate.cpp:400-480, with Resolution::sandwich,
+ * mathtools/matrix_helper.cpp:815-821, 877-903).  Q_k is the analytic band
+ * (dk / pi) cos(k_c v) sinc(dk v / 2) (:444-454), S comes from table 0
+ * (RES_INDEX = 0, :189-193); the redshift weights apply after the sandwich.
+ * lambda, delta, ivar and offsets are as for lqg_batch_add.  resomat holds
+ * nelem doubles per pixel, aligned with lambda:
+ *  - oversampling > 0: the pixel's row of the oversampled matrix
+ *    (Resolution::oversample, mathtools/matrix_helper.cpp:1008-1073, i.e. the
+ *    output of lqg_resomat_oversample), nelem = 2 (ndiags / 2) oversampling + 1;
+ *    the row's weights sit at grid points i * oversampling + a of the grid
+ *    lambda_0 / LYA + (p - nelem / 2) dlambda / LYA / oversampling, dlambda the
+ *    chunk's median pixel width (core/chunk_estimate.cpp:927-938);
+ *  - oversampling <= 0: the diagonal matrix, the pixel's column on each of the
+ *    nelem = ndiags diagonals (entry d is DiaMatrix values[d][pixel], diagonal
+ *    d holding offset ndiags / 2 - d); S and Q_k stay on the pixel grid.
+ * Limits of the engine's tiles: nelem <= 48 and 31 * max(oversampling, 1) +
+ * nelem <= 128 (else LQG_ERR_UNSUPPORTED).  No table lookup by (R, dv) is
+ * made; every other rule of lqg_batch_add applies. */
+int lqg_batch_add_reso(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
+                       const double *lambda, const double *delta, const double *ivar,
+                       int oversampling, int nelem, const double *resomat, int *status_out);
+/* Resolution-matrix preprocessing of one spectrum (before chunking, as
+ * OneQSOEstimate::_readQsoFile does, core/one_qso_estimate.cpp:75-89).
+ * values: DiaMatrix layout values[ndiags][n] (diagonal d holds offset
+ * ndiags / 2 - d, its entry of column c at [d][c]; rows at the spectrum's
+ * edges mirror their missing entries, DiaMatrix::_getRowIndices).
+ * lqg_resomat_deconvolve: DiaMatrix::deconvolve(m) in place
+ *   (mathtools/matrix_helper.cpp:653-682, real_field.cpp:95-110).
+ * lqg_resomat_oversample: Resolution::oversample(osamp, dlambda)
+ *   (mathtools/matrix_helper.cpp:1008-1073); rows[n][2 (ndiags / 2) osamp + 1].
+ * Host only: neither touches the device nor needs a context. */
+int lqg_resomat_deconvolve(int n, int ndiags, double *values, double m);
+int lqg_resomat_oversample(int n, int ndiags, const double *values, int osamp, double dlambda,
+                           double *rows);
 int lqg_batch_clear(lqg_ctx *ctx);
 int lqg_batch_size(const lqg_ctx *ctx);
 

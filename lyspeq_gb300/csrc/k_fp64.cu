@@ -135,7 +135,7 @@ __global__ void k_build_s_c(WaveArgs a) {
     const ChunkDesc &ch = a.chunks[c];
     const int ld = ch.ld, n = ch.n;
     const int tpr = ld / T64;
-    if ((int) blockIdx.x >= tpr * tpr) return;
+    if ((int) blockIdx.x >= tpr * tpr || ch.nelem > 0) return;
     const int ti = blockIdx.x / tpr, tj = blockIdx.x % tpr;
     if (!LQG_IN_BOUNDS(a, ch.o_s >= 0 && ch.o_c >= 0 && ch.o_s + (int64_t) ld * ld * 8 <= a.fws_bytes &&
                               ch.o_c + (int64_t) ld * ld * 8 <= a.fws_bytes && ch.pix >= 0 &&
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
     const int c = blockIdx.y;
     const ChunkDesc &ch = a.chunks[c];
     const int ld = ch.ld, n = ch.n, tpr = ld / T64;
-    if ((int) blockIdx.x >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    if ((int) blockIdx.x >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK || ch.nelem > 0) return;
     const int ti = blockIdx.x / tpr, tj = blockIdx.x % tpr;
     const DeviceBins &bins = *a.bins;
     const double *logw = a.logw + ch.pix, *sqw = a.sqw + ch.pix;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     const ChunkDesc &ch = a.chunks[c];
     const int ld = ch.ld, n = ch.n, tpr = ld / T64;
     const int tile = blockIdx.x >> 1, hrow = (blockIdx.x & 1) * 32;
-    if (tile >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    if (tile >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK || ch.nelem > 0) return;
     const int ti = tile / tpr, tj = tile % tpr;
     const DeviceBins &bins = *a.bins;
     const float2 *lw2 = a.logw2 + ch.pix, *sw2 = a.sqw2 + ch.pix;

@@ -30,13 +30,19 @@ struct lqg_ctx {
     struct HostChunk {
         int n, ld, nq, ns, kbin_upp, fis, res, zlow, zupp, input_index;
         int64_t pix, res_off;
+        int nelem, os, sh, nf;     // resolution matrix (nelem = 0: none)
+        int64_t fpix, rw_off;
+        double rw_sum;
     };
     std::vector<HostChunk> chunks;
     std::vector<double> h_wave, h_delta, h_ivar, h_logw, h_sqw;
     std::vector<float2> h_logw2, h_sqw2;
     std::vector<double> h_sqiv, h_niv;
+    std::vector<double> h_flogw, h_fsqw, h_rw;   // resolution-matrix grids and weights
+    bool has_reso = false;
     bool pix_dirty = true;
     DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw, d_logw2, d_sqw2, d_sqiv, d_niv;
+    DevBuf d_flogw, d_fsqw, d_rw;
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
@@ -94,7 +100,7 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
                               const lqg_opts *opts, int device) {
     if (!out || !bins || !tables || !opts) return LQG_ERR_ARG;
     *out = nullptr;
-    if (bins->nk <= 0 || bins->nz <= 0 || bins->nz > 64 || !bins->k_edges || !bins->z_centers ||
+    if (bins->nk <= 0 || bins->nk > kMaxKBands || bins->nz <= 0 || bins->nz > 64 || !bins->k_edges || !bins->z_centers ||
         !(bins->z_bin_width > 0))
         return LQG_ERR_ARG;
     if (tables->n_tables <= 0 || tables->nv < 2 || tables->nzp < 2 || !tables->deriv ||
@@ -178,6 +184,7 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     db.nkz = ctx->nkz;
     db.triangular = ctx->triangular;
     db.dz = ctx->dz;
+    for (int k = 0; k <= ctx->nk; ++k) db.k_edges[k] = ctx->k_edges[k];
     for (int z = 0; z < ctx->nz; ++z) {
         db.z_centers[z] = ctx->z_centers[z];
         const float2 c1 = split_ff(1.0 + ctx->z_centers[z]);
@@ -219,6 +226,8 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
     ctx->h_logw.clear(); ctx->h_sqw.clear();
     ctx->h_logw2.clear(); ctx->h_sqw2.clear();
     ctx->h_sqiv.clear(); ctx->h_niv.clear();
+    ctx->h_flogw.clear(); ctx->h_fsqw.clear(); ctx->h_rw.clear();
+    ctx->has_reso = false;
     ctx->results_size = 0;
     ctx->pix_dirty = true;
     return LQG_OK;
@@ -226,12 +235,17 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
 
 extern "C" int lqg_batch_size(const lqg_ctx *ctx) { return ctx ? (int) ctx->chunks.size() : 0; }
 
-extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
-                             const double *lambda, const double *delta, const double *ivar,
-                             const int *r_fwhm, int *status_out) {
-    if (!ctx || n_chunks < 0 || (n_chunks > 0 && (!offsets || !lambda || !delta || !ivar || !r_fwhm)))
-        return set_err(ctx, LQG_ERR_ARG, "lqg_batch_add: bad arguments");
+namespace {
+
+// Chunk::Chunk for every chunk of an lqg_batch_add / lqg_batch_add_reso call.
+// resomat == NULL: table lookup by (R, dv).  Otherwise the chunk's resolution
+// matrix, per pixel: nelem weights of its oversampled row (reso_os > 0) or
+// its column's entries on the ndiags = nelem diagonals (reso_os <= 0).
+int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double *lambda,
+               const double *delta, const double *ivar, const int *r_fwhm, int reso_os, int reso_nelem,
+               const double *resomat, int *status_out) {
     const double max_v = ctx->opts.max_forest_length, min_v = 0.90 / 2 * max_v;
+    const bool reso = resomat != nullptr;
     for (int c = 0; c < n_chunks; ++c) {
         int64_t a = offsets[c], b = offsets[c + 1];
         int st = LQG_CHUNK_OK;
@@ -259,9 +273,10 @@ extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
             double lenv = kSpeedOfLight * std::log(lambda[b - 1] / lambda[a]);
             int minnopix = (int) (lenv / ctx->opts.max_mean_pixel_size);
             if (realsize < minnopix || lenv < min_v) st = LQG_CHUNK_SHORT;
-            // SQLookupTable::findSpecResIndex (core/sq_table.cpp:388-397)
-            int res = -1;
-            if (st == LQG_CHUNK_OK) {
+            // SQLookupTable::findSpecResIndex (core/sq_table.cpp:388-397); with a
+            // resolution matrix RES_INDEX = 0 (core/chunk_estimate.cpp:189-193)
+            int res = reso ? 0 : -1;
+            if (st == LQG_CHUNK_OK && !reso) {
                 double rounded = std::round(dv * 10) / 10;
                 for (int t = 0; t < ctx->n_tables; ++t)
                     if (ctx->r_fwhm[t] == r_fwhm[c] && std::fabs(rounded - ctx->tdv[t]) < 0.01) { res = t; break; }
@@ -295,8 +310,65 @@ extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
                     st = LQG_CHUNK_TOO_LARGE;
             }
         }
+        // resolution matrix of the chunk: weights per coarse row and its grid
+        std::vector<double> rw, fgrid;
+        if (st == LQG_CHUNK_OK && reso) {
+            const int nel = reso_nelem;
+            hc.nelem = nel;
+            if (reso_os > 0) {
+                // OversampledMatrix rows; grid of Chunk::_initMatrices
+                // (core/chunk_estimate.cpp:927-938): w_0 + (p - nelem/2) dlambda / LYA / os,
+                // dlambda the chunk's median pixel width (io/qso_file.cpp:86-88, 325-329)
+                hc.os = reso_os;
+                hc.sh = 0;
+                hc.nf = n * reso_os + nel - 1;
+                rw.assign(resomat + a * nel, resomat + b * nel);
+                std::vector<double> dl(n - 1);
+                for (int i = 0; i < n - 1; ++i) dl[i] = lambda[a + i + 1] - lambda[a + i];
+                const double fine = median_of(dl) / kLyaRest / reso_os, w0 = lambda[a] / kLyaRest;
+                const int disp = nel / 2;
+                fgrid.resize(hc.nf);
+                for (int p = 0; p < hc.nf; ++p) fgrid[p] = w0 + (p - disp) * fine;
+            } else {
+                // DiaMatrix: row r has entries at columns r + off, off = a - nel/2,
+                // held on diagonal d = nel - 1 - a (mathtools/matrix_helper.cpp:503-520,
+                // 684-813); columns outside the chunk drop out
+                hc.os = 1;
+                hc.sh = nel / 2;
+                hc.nf = n;
+                rw.assign((size_t) n * nel, 0.0);
+                for (int r = 0; r < n; ++r)
+                    for (int k = 0; k < nel; ++k) {
+                        const int col = r - hc.sh + k;
+                        if (col >= 0 && col < n) rw[(size_t) r * nel + k] = resomat[(a + col) * nel + (nel - 1 - k)];
+                    }
+                for (int64_t i = a; i < b; ++i) fgrid.push_back(lambda[i] / kLyaRest);
+            }
+            hc.rw_sum = 0;
+            for (int r = 0; r < n; ++r) {
+                double sum = 0;
+                for (int k = 0; k < nel; ++k) {
+                    const double w = rw[(size_t) r * nel + k];
+                    if (!std::isfinite(w)) st = LQG_CHUNK_BAD_INPUT;
+                    sum += std::fabs(w);
+                }
+                hc.rw_sum = std::max(hc.rw_sum, sum);
+            }
+            for (double w : fgrid)
+                if (!(w > 0) || !std::isfinite(w)) st = LQG_CHUNK_BAD_INPUT;
+        }
         if (status_out) status_out[c] = st;
         if (st != LQG_CHUNK_OK) continue;
+        if (reso) {
+            ctx->has_reso = true;
+            hc.fpix = (int64_t) ctx->h_flogw.size();
+            hc.rw_off = (int64_t) ctx->h_rw.size();
+            for (double w : fgrid) {
+                ctx->h_flogw.push_back(std::log(w));
+                ctx->h_fsqw.push_back(std::sqrt(w));
+            }
+            ctx->h_rw.insert(ctx->h_rw.end(), rw.begin(), rw.end());
+        }
         hc.input_index = c;
         hc.pix = (int64_t) ctx->h_wave.size();
         hc.res_off = ctx->results_size;
@@ -317,6 +389,31 @@ extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
     }
     ctx->pix_dirty = true;
     return LQG_OK;
+}
+
+}  // namespace
+
+extern "C" int lqg_batch_add(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
+                             const double *lambda, const double *delta, const double *ivar,
+                             const int *r_fwhm, int *status_out) {
+    if (!ctx || n_chunks < 0 || (n_chunks > 0 && (!offsets || !lambda || !delta || !ivar || !r_fwhm)))
+        return set_err(ctx, LQG_ERR_ARG, "lqg_batch_add: bad arguments");
+    return add_chunks(ctx, n_chunks, offsets, lambda, delta, ivar, r_fwhm, 0, 0, nullptr, status_out);
+}
+
+extern "C" int lqg_batch_add_reso(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
+                                  const double *lambda, const double *delta, const double *ivar,
+                                  int oversampling, int nelem, const double *resomat, int *status_out) {
+    if (!ctx || n_chunks < 0 || (n_chunks > 0 && (!offsets || !lambda || !delta || !ivar || !resomat)))
+        return set_err(ctx, LQG_ERR_ARG, "lqg_batch_add_reso: bad arguments");
+    if (nelem < 1 || nelem % 2 == 0)
+        return set_err(ctx, LQG_ERR_ARG, "lqg_batch_add_reso: nelem must be odd and positive");
+    const int os = oversampling > 0 ? oversampling : 1;
+    if (nelem > kResoMaxElem || (kResoTile - 1) * os + nelem > kResoMaxFine)
+        return set_err(ctx, LQG_ERR_UNSUPPORTED, "lqg_batch_add_reso: resolution matrix wider than the "
+                                                 "engine's tile (31 oversampling + nelem <= 128, nelem <= 48)");
+    return add_chunks(ctx, n_chunks, offsets, lambda, delta, ivar, nullptr, oversampling, nelem, resomat,
+                      status_out);
 }
 
 extern "C" int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info) {
@@ -352,6 +449,15 @@ int upload_pixels(lqg_ctx *ctx) {
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqiv.p, ctx->h_sqiv.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_niv.p, ctx->h_niv.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqw2.p, ctx->h_sqw2.data(), np * 8, cudaMemcpyHostToDevice, s));
+    const size_t nfp = ctx->h_flogw.size(), nrw = ctx->h_rw.size();
+    if (ctx->d_flogw.alloc(std::max<size_t>(nfp, 1) * 8) || ctx->d_fsqw.alloc(std::max<size_t>(nfp, 1) * 8) ||
+        ctx->d_rw.alloc(std::max<size_t>(nrw, 1) * 8))
+        return set_err(ctx, LQG_ERR_NOMEM, "resolution-matrix arrays");
+    if (nfp) {
+        LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_flogw.p, ctx->h_flogw.data(), nfp * 8, cudaMemcpyHostToDevice, s));
+        LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_fsqw.p, ctx->h_fsqw.data(), nfp * 8, cudaMemcpyHostToDevice, s));
+    }
+    if (nrw) LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_rw.p, ctx->h_rw.data(), nrw * 8, cudaMemcpyHostToDevice, s));
     if (ctx->d_results.alloc(std::max<int64_t>(ctx->results_size, 1) * 8) ||
         ctx->d_status.alloc(std::max<size_t>(ctx->chunks.size(), 1) * 4))
         return set_err(ctx, LQG_ERR_NOMEM, "results");
@@ -472,6 +578,8 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             ChunkDesc d{};
             d.n = h.n; d.ld = h.ld; d.nq = h.nq; d.ns = h.ns; d.kbin_upp = h.kbin_upp; d.fis = h.fis;
             d.res = h.res; d.zb0 = h.fis / ctx->nk; d.pix = h.pix; d.res_off = h.res_off; d.gidx = idx;
+            d.nelem = h.nelem; d.os = h.os; d.sh = h.sh; d.nf = h.nf; d.fpix = h.fpix; d.rw_off = h.rw_off;
+            d.rw_sum = h.rw_sum;
             const int64_t m = (int64_t) h.ld * h.ld * 8;
             d.o_s = off; off += align_up(m, 256);
             d.o_c = off; off += align_up(m, 256);
@@ -551,9 +659,20 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
                 for (int i = 0; i < nch; ++i) {
                     const ChunkDesc &d = desc[w.desc_off + i];
                     double *q = scales.data() + w.scales_off + 4 * nch + d.slot_q;
-                    for (int s = 0; s < d.ns; ++s)
-                        q[s] = pow2_scale(ctx->qmax[(size_t) d.res * ctx->nk + s % d.kbin_upp], 16384.0);
-                    q[d.ns] = pow2_scale(ctx->smax[d.res], 16384.0);
+                    if (d.nelem > 0) {
+                        // |R M R^T| <= max|M| (largest row sum of |R|)^2; the
+                        // resolution-matrix Q_k peaks at dk / pi (v = 0)
+                        const double r2 = d.rw_sum * d.rw_sum;
+                        for (int s = 0; s < d.ns; ++s) {
+                            const int kn = s % d.kbin_upp;
+                            q[s] = pow2_scale((ctx->k_edges[kn + 1] - ctx->k_edges[kn]) / kPi * r2, 16384.0);
+                        }
+                        q[d.ns] = pow2_scale(ctx->smax[d.res] * r2, 16384.0);
+                    } else {
+                        for (int s = 0; s < d.ns; ++s)
+                            q[s] = pow2_scale(ctx->qmax[(size_t) d.res * ctx->nk + s % d.kbin_upp], 16384.0);
+                        q[d.ns] = pow2_scale(ctx->smax[d.res], 16384.0);
+                    }
                 }
             }
         }
@@ -632,6 +751,9 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.logw = ctx->d_logw.as<double>(); base.sqw = ctx->d_sqw.as<double>();
     base.logw2 = ctx->d_logw2.as<float2>(); base.sqw2 = ctx->d_sqw2.as<float2>();
     base.sqiv = ctx->d_sqiv.as<double>(); base.niv = ctx->d_niv.as<double>();
+    base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
+    base.n_fpix = (int64_t) ctx->h_flogw.size();
+    base.n_rw = (int64_t) ctx->h_rw.size();
     base.deriv = ctx->d_deriv.as<double>();
     base.deriv_f = ctx->d_deriv_f.as<float>();
     base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
@@ -675,6 +797,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
         nev += 3;
         cudaEventRecord(pool_event(ctx, e0), st);
         launch_build_s_c(a, st);
+        if (ctx->has_reso) launch_build_s_c_reso(a, st);
         if ((rc = step("build_s_c", g.max_ld, a.n_chunks))) return rc;
         cudaEventRecord(pool_event(ctx, e0 + 1), st);
         launch_factor_all(a, st);
@@ -716,6 +839,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
             cudaEventRecord(pool_event(ctx, w0), st);
             if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(b, st);
             launch_build_q(b, st);
+            if (ctx->has_reso) launch_build_q_reso(b, st);
             if ((rc = step("build_q", w.ld, nch))) return rc;
             cudaEventRecord(pool_event(ctx, w0 + 1), st);
             if (precision == LQG_PRECISION_MIXED)

@@ -44,12 +44,22 @@ struct ChunkDesc {
     int slot_q, slot_r, slot_p;  // first matrix slot of this chunk in the stacked operand buffers
     int gidx;             // index of the chunk in the batch (factor bounds, status)
     int status;
+    // Resolution matrix (UseResoMatrix; nelem = 0 without one).  Coarse row r
+    // has weights rw[rw_off + r * nelem + a] at grid point r * os + a - sh of
+    // a grid of nf points (the oversampled grid, or the pixels themselves for
+    // a diagonal matrix), whose ln(lambda) and sqrt(lambda) start at fpix.
+    int nelem, os, sh, nf;
+    int64_t fpix, rw_off;
+    double rw_sum;        // largest sum of |weights| of a row (bound of R M R^T)
 };
+
+constexpr int kMaxKBands = 256;   // largest NUMBER_OF_K_BANDS
 
 struct DeviceBins {
     int nk, nz, nkz, triangular;
     double dz;
     double z_centers[64];
+    double k_edges[kMaxKBands + 1];
     // double-float (hi + lo) forms for the FP32-pipe element math of the
     // mixed path: 1 + z_c per bin, dz, dz / 2, and 1 / dz
     float zc1_hi[64], zc1_lo[64];
@@ -92,6 +102,7 @@ struct WaveArgs {
     const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
     const float2 *logw2, *sqw2;                      // ln w and sqrt w as double-float (hi, lo)
     const double *sqiv, *niv;                        // sqrt(ivar), and 1 / ivar (0 where ivar = 0)
+    const double *flogw, *fsqw, *rw;                 // resolution-matrix grids and weights
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
     const double *theta;                             // device, nkz
@@ -109,7 +120,7 @@ struct WaveArgs {
     int launches;
     cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
     // extents of the buffers above, used by the LQG_CHECKED build to validate indices
-    int64_t ws_bytes, fws_bytes, results_elems, gram_elems, n_pix;
+    int64_t ws_bytes, fws_bytes, results_elems, gram_elems, n_pix, n_fpix, n_rw;
     unsigned long long *check;   // [0] violations, [1] first code, [2] first chunk, [3] first index
 };
 
@@ -134,6 +145,13 @@ __device__ __forceinline__ bool lqg_in_bounds(const WaveArgs &a, bool ok, int co
 
 // Phase A (all chunks of a group): S_fid and C~, then the FP64 factorisation.
 void launch_build_s_c(WaveArgs &a, cudaStream_t st);
+// The same two matrix builds for chunks with a resolution matrix (lqg_reso.cu);
+// each kind of kernel skips the chunks of the other kind.
+void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st);
+void launch_build_q_reso(WaveArgs &a, cudaStream_t st);
+constexpr int kResoTile = 32;     // coarse tile edge of the resolution-matrix kernels
+constexpr int kResoMaxFine = 128; // largest fine extent of a tile: (kResoTile - 1) os + nelem
+constexpr int kResoMaxElem = 48;  // largest number of weights per row
 void launch_factor_all(WaveArgs &a, cudaStream_t st);
 size_t factor_smem_bytes();
 // Phase B (per wave): Q_k, products, traces, per-chunk results.

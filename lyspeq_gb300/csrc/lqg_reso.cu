@@ -1,0 +1,513 @@
+// Resolution-matrix path (UseResoMatrix): lyspeq evaluates the fiducial signal
+// and the derivative matrices on the resolution matrix's grid and sandwiches
+// them, M -> R M R^T (Chunk::_setFiducialSignalMatrix and _setQiMatrix,
+// core/chunk_estimate.cpp:400-480; Resolution::sandwich,
+// mathtools/matrix_helper.cpp:815-821, 877-903, 1075-1084).  The grid is the
+// pixel grid for a diagonal (banded) matrix, or an oversampled grid linear in
+// wavelength (Chunk::_initMatrices, core/chunk_estimate.cpp:927-938) for a
+// matrix that Resolution::oversample has resampled.
+//
+// Host side: the per-spectrum preprocessing of the matrix (deconvolution and
+// oversampling, core/one_qso_estimate.cpp:75-89).
+// Device side: the S / C~ build of phase A and the Q_s build of phase B for
+// chunks with a resolution matrix.  R is banded, row r having nelem weights at
+// grid points r os + a - sh, so one 32 x 32 tile of R M R^T needs a block of
+// at most 128 x 128 grid points of M.  The block is evaluated slab by slab into
+// shared memory and contracted twice (T = M_block R_J^T, then R_I T): about
+// 150 multiply-adds per output element for an x3-oversampled 11-diagonal
+// matrix, and each grid point of M is evaluated once per tile.  Only tiles on
+// or above the diagonal are computed; each writes its mirror tile too.
+#include "lqg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+// ---------------------------------------------------------------------------
+// Host preprocessing
+
+namespace {
+
+// DiaMatrix::_getRowIndices (mathtools/matrix_helper.cpp:608-620): flat
+// indices into values[ndiags][n] of row i, columns i - noff .. i + noff;
+// entries beyond the matrix edge repeat the row's mirrored entry.
+void dia_row_indices(int i, int n, int nd, std::vector<int> &idx) {
+    const int noff = nd / 2;
+    idx.clear();
+    for (int j = nd - 1; j >= 0; --j) idx.push_back(j * n + (noff - j) + i);
+    if (i < noff) {
+        for (int j = 0; j < noff - i; ++j) idx[j] = idx[nd - 1 - j];
+    } else if (i > n - noff - 1) {
+        for (int j = 0; j < i - n + noff + 1; ++j) idx[nd - 1 - j] = idx[j];
+    }
+}
+
+// Second derivatives of the natural cubic spline through (x, y).
+void natural_spline(const std::vector<double> &x, const std::vector<double> &y, std::vector<double> &m) {
+    const size_t n = x.size();
+    m.assign(n, 0.0);
+    if (n < 3) return;
+    const size_t k = n - 2;
+    std::vector<double> diag(k), upper(k), rhs(k);
+    for (size_t j = 0; j < k; ++j) {
+        const size_t i = j + 1;
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        diag[j] = 2.0 * (h0 + h1);
+        upper[j] = h1;
+        rhs[j] = 6.0 * ((y[i + 1] - y[i]) / h1 - (y[i] - y[i - 1]) / h0);
+    }
+    for (size_t j = 1; j < k; ++j) {
+        const double f = (x[j + 1] - x[j]) / diag[j - 1];
+        diag[j] -= f * upper[j - 1];
+        rhs[j] -= f * rhs[j - 1];
+    }
+    m[k] = rhs[k - 1] / diag[k - 1];
+    for (size_t j = k - 1; j-- > 0;) m[j + 1] = (rhs[j] - upper[j] * m[j + 2]) / diag[j];
+}
+
+double spline_eval(const std::vector<double> &x, const std::vector<double> &y, const std::vector<double> &m,
+                   double t) {
+    size_t lo = 0, hi = x.size() - 1;
+    while (hi - lo > 1) {
+        const size_t mid = (lo + hi) / 2;
+        if (x[mid] > t) hi = mid; else lo = mid;
+    }
+    const size_t i = lo;
+    const double h = x[i + 1] - x[i], t1 = x[i + 1] - t, t0 = t - x[i];
+    return (m[i] * t1 * t1 * t1 + m[i + 1] * t0 * t0 * t0) / (6.0 * h)
+         + (y[i] / h - m[i] * h / 6.0) * t1 + (y[i + 1] / h - m[i + 1] * h / 6.0) * t0;
+}
+
+// nonzero_min_element (mathtools/matrix_helper.cpp:20-39): the smallest |x|
+// above 1e-15 in the reference's scan order, at least 1e-15.
+double nonzero_min_abs(const std::vector<double> &row) {
+    double smallest = std::fabs(row[0]);
+    for (size_t i = 1; i < row.size(); ++i) {
+        const double tmp = std::fabs(row[i]);
+        if (smallest < 1e-15) smallest = tmp;
+        else if (tmp < smallest && tmp > 1e-15) smallest = tmp;
+    }
+    return smallest < 1e-15 ? 1e-15 : smallest;
+}
+
+}  // namespace
+
+// DiaMatrix::deconvolve (mathtools/matrix_helper.cpp:653-682) with
+// RealField::deconvolveSinc (mathtools/real_field.cpp:78-110): every row,
+// zero-padded by 5 on each side, is divided by sinc(pi m k / size) in Fourier
+// space (k >= 1).  The 21-point transforms are direct sums.
+extern "C" int lqg_resomat_deconvolve(int n, int ndiags, double *values, double m) {
+    if (n < 1 || ndiags < 1 || ndiags % 2 == 0 || !values || !(m > 0)) return LQG_ERR_ARG;
+    const int pad = 5, size = ndiags + 2 * pad, nh = size / 2 + 1;
+    std::vector<double> x(size), re(nh), im(nh), cs(size), sn(size);
+    for (int j = 0; j < size; ++j) {
+        cs[j] = std::cos(2.0 * lqg::kPi * j / size);
+        sn[j] = std::sin(2.0 * lqg::kPi * j / size);
+    }
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i) {
+        dia_row_indices(i, n, ndiags, idx);
+        std::fill(x.begin(), x.end(), 0.0);
+        for (int p = 0; p < ndiags; ++p) x[p + pad] = values[idx[p]];
+        for (int k = 0; k < nh; ++k) {
+            double r = 0.0, s = 0.0;
+            for (int j = 0; j < size; ++j) {
+                const int w = (int) (((long long) j * k) % size);
+                r += x[j] * cs[w];
+                s -= x[j] * sn[w];
+            }
+            if (k >= 1) {
+                const double a = lqg::kPi * m * k / size, sinc = std::sin(a) / a;
+                r /= sinc;
+                s /= sinc;
+            }
+            re[k] = r;
+            im[k] = s;
+        }
+        for (int j = 0; j < size; ++j) {
+            double v = re[0];
+            for (int k = 1; k < nh; ++k) {
+                const int w = (int) (((long long) j * k) % size);
+                if (2 * k == size) v += re[k] * cs[w];
+                else v += 2.0 * (re[k] * cs[w] - im[k] * sn[w]);
+            }
+            x[j] = v / size;
+        }
+        for (int p = 0; p < ndiags; ++p) values[idx[p]] = x[p + pad];
+    }
+    return LQG_OK;
+}
+
+// Resolution::oversample (mathtools/matrix_helper.cpp:1008-1073): each row's
+// ndiags entries are shifted positive, log-transformed, passed through a
+// natural cubic spline on the pixel offsets and evaluated osamp times finer;
+// the exponentiated row is shifted back and normalised to unit sum.
+extern "C" int lqg_resomat_oversample(int n, int ndiags, const double *values, int osamp, double dlambda,
+                                      double *rows) {
+    if (n < 1 || ndiags < 3 || ndiags % 2 == 0 || !values || !rows || osamp < 1 || !(dlambda > 0))
+        return LQG_ERR_ARG;
+    const int noff = ndiags / 2, nelem = 2 * noff * osamp + 1;
+    std::vector<double> win(ndiags), wout(nelem), row(ndiags), m;
+    for (int i = 0; i < ndiags; ++i) win[i] = (i - noff) * dlambda;
+    for (int i = 0; i < nelem; ++i) wout[i] = (i * 1. / osamp - noff) * dlambda;
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i) {
+        dia_row_indices(i, n, ndiags, idx);
+        double mn = values[idx[0]];
+        for (int p = 0; p < ndiags; ++p) {
+            row[p] = values[idx[p]];
+            mn = std::min(mn, row[p]);
+        }
+        const double shift = mn - nonzero_min_abs(row);
+        for (auto &f : row) f = std::log(f - shift);
+        natural_spline(win, row, m);
+        double *out = rows + (size_t) i * nelem;
+        double sum = 0.0;
+        for (int jj = 0; jj < nelem; ++jj) {
+            out[jj] = shift + std::exp(spline_eval(win, row, m, wout[jj]));
+            sum += out[jj];
+        }
+        const double isum = 1. / sum;
+        for (int jj = 0; jj < nelem; ++jj) out[jj] *= isum;
+    }
+    return LQG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device side
+
+namespace lqg {
+
+namespace {
+
+constexpr int RT = kResoTile, RLF = kResoMaxFine, RME = kResoMaxElem;
+constexpr int RSLAB = 32;          // grid rows of M evaluated per pass
+constexpr int RTH = 256;           // threads; each owns 4 rows of one column of the tile
+
+struct ResoShared {
+    double wi[RT][RME + 1];        // weights of the tile's coarse rows
+    double wj[RT][RME + 1];        // ... and columns
+    double f[RSLAB][RLF + 1];      // a slab of M on the tile's grid block
+    double t[RLF][RT + 1];         // T = M_block R_J^T
+    double lwr[RLF], swr[RLF];     // ln w and sqrt w of the block's grid rows
+    double lwc[RLF], swc[RLF];     // ... and grid columns
+};
+
+struct ResoGeom {
+    int lf;                        // grid points spanned by the tile: (RT - 1) os + nelem
+    int r0, c0;                    // first grid row / column of the block (may be < 0)
+    int os, nelem, nf;
+};
+
+__device__ __forceinline__ double *fws_d(const WaveArgs &a, int64_t off) {
+    return reinterpret_cast<double *>(a.fws + off);
+}
+__device__ __forceinline__ double *ws_d(const WaveArgs &a, int64_t off) {
+    return reinterpret_cast<double *>(a.ws + off);
+}
+
+// Weights and grid values of tile (I, J) of chunk ch into shared memory.
+__device__ ResoGeom reso_load(ResoShared &sm, const WaveArgs &a, const ChunkDesc &ch, int I, int J) {
+    ResoGeom g;
+    g.os = ch.os;
+    g.nelem = ch.nelem;
+    g.nf = ch.nf;
+    g.lf = (RT - 1) * ch.os + ch.nelem;
+    g.r0 = I * RT * ch.os - ch.sh;
+    g.c0 = J * RT * ch.os - ch.sh;
+    for (int e = threadIdx.x; e < RT * ch.nelem; e += blockDim.x) {
+        const int r = e / ch.nelem, k = e % ch.nelem;
+        const int ri = I * RT + r, rj = J * RT + r;
+        sm.wi[r][k] = ri < ch.n ? a.rw[ch.rw_off + (int64_t) ri * ch.nelem + k] : 0.0;
+        sm.wj[r][k] = rj < ch.n ? a.rw[ch.rw_off + (int64_t) rj * ch.nelem + k] : 0.0;
+    }
+    for (int e = threadIdx.x; e < g.lf; e += blockDim.x) {
+        const int pr = g.r0 + e, pc = g.c0 + e;
+        const bool okr = pr >= 0 && pr < ch.nf, okc = pc >= 0 && pc < ch.nf;
+        sm.lwr[e] = okr ? a.flogw[ch.fpix + pr] : 0.0;
+        sm.swr[e] = okr ? a.fsqw[ch.fpix + pr] : 0.0;
+        sm.lwc[e] = okc ? a.flogw[ch.fpix + pc] : 0.0;
+        sm.swc[e] = okc ? a.fsqw[ch.fpix + pc] : 0.0;
+    }
+    __syncthreads();
+    return g;
+}
+
+// Velocity and redshift separations of grid points (block row fr, block
+// column fc): v = c ln(w_hi / w_lo) >= 0 and z = sqrt(w_lo w_hi) - 1, the
+// upper-triangle values the reference copies to the lower triangle
+// (core/chunk_estimate.cpp:384-398, 414-416).  False outside the grid.
+__device__ __forceinline__ bool grid_vz(const ResoShared &sm, const ResoGeom &g, int fr, int fc, double &v,
+                                        double &z) {
+    const int p = g.r0 + fr, q = g.c0 + fc;
+    if (p < 0 || q < 0 || p >= g.nf || q >= g.nf) return false;
+    if (p <= q) {
+        v = kSpeedOfLight * (sm.lwc[fc] - sm.lwr[fr]);
+        z = sm.swr[fr] * sm.swc[fc] - 1.0;
+    } else {
+        v = kSpeedOfLight * (sm.lwr[fr] - sm.lwc[fc]);
+        z = sm.swc[fc] * sm.swr[fr] - 1.0;
+    }
+    return true;
+}
+
+// Tile of R M R^T: out[u] = (R M R^T)[I*RT + r8 + 8u][J*RT + j] for the
+// calling thread (j = threadIdx.x % 32, r8 = threadIdx.x / 32), M given at
+// block coordinates by ev(fr, fc).
+template <class Eval>
+__device__ void reso_sandwich(ResoShared &sm, const ResoGeom &g, Eval ev, double out[4]) {
+    const int j = threadIdx.x % 32, r8 = threadIdx.x / 32;
+    for (int s0 = 0; s0 < g.lf; s0 += RSLAB) {
+        const int rows = min(RSLAB, g.lf - s0);
+        for (int e = threadIdx.x; e < rows * g.lf; e += RTH) {
+            const int fr = e / g.lf, fc = e % g.lf;
+            sm.f[fr][fc] = ev(s0 + fr, fc);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < RSLAB / 8; ++u) {
+            const int fr = r8 + 8 * u;
+            if (fr < rows) {
+                const double *frow = &sm.f[fr][j * g.os];
+                double acc = 0.0;
+                for (int b = 0; b < g.nelem; ++b) acc = fma(frow[b], sm.wj[j][b], acc);
+                sm.t[s0 + fr][j] = acc;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int i = r8 + 8 * u;
+        double acc = 0.0;
+        for (int a = 0; a < g.nelem; ++a) acc = fma(sm.wi[i][a], sm.t[i * g.os + a][j], acc);
+        out[u] = acc;
+    }
+    __syncthreads();
+}
+
+// Redshift weight of bin zm at z (bins::zBin*, core/global_numbers.cpp:393-471),
+// the element-wise form used by the plain Q build.
+__device__ __forceinline__ double zweight_r(const DeviceBins &b, int zm, double z) {
+    const double zc = b.z_centers[zm], dz = b.dz;
+    if (!b.triangular || b.nz == 1) return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.0 : 0.0;
+    if (zm == 0 && z < zc) return 1.0;
+    if (zm == b.nz - 1 && z > zc) return 1.0;
+    if (z >= zc - dz && z <= zc + dz) return 1.0 - fabs(z - zc) / dz;
+    return 0.0;
+}
+
+// DiscreteInterpolation2D::evaluate (mathtools/discrete_interpolation.cpp:221-242).
+__device__ __forceinline__ double signal_at_r(const double *tab, const TableGrid &gr, double z, double v) {
+    const double xx = (z - gr.z1) / gr.dz, yy = (v - gr.v1) / gr.dv;
+    int nx = (int) xx, ny = (int) yy;
+    nx = nx < 0 ? 0 : (nx >= gr.nzp - 1 ? gr.nzp - 2 : nx);
+    ny = ny < 0 ? 0 : (ny >= gr.nv - 1 ? gr.nv - 2 : ny);
+    const size_t ind = (size_t) nx + (size_t) gr.nzp * ny;
+    const double dnx = xx - nx, dny = yy - ny;
+    return tab[ind] * (1 - dnx) * (1 - dny) + tab[ind + 1] * dnx * (1 - dny)
+         + tab[ind + gr.nzp] * (1 - dnx) * dny + tab[ind + gr.nzp + 1] * dnx * dny;
+}
+
+// Analytic band power derivative with a resolution matrix
+// (core/chunk_estimate.cpp:444-454): (dk / pi) cos(k_c v) sin(x) / x, x = dk v / 2.
+__device__ __forceinline__ double qband(double kc, double dk, double v) {
+    if (v == 0) return dk / kPi;
+    const double x = dk * v / 2;
+    return (dk / kPi) * cos(kc * v) * (sin(x) / x);
+}
+
+// Phase A: S = R S_grid R^T into o_s and C~ = D (S + sum_s theta_s Q_s) D + I
+// into o_c.  With theta, the Q_s term is formed per redshift bin m as
+// w_m(z_ij) (R G_m R^T)_ij with G_m = sum_k theta_{k,m} Q_k on the grid (the
+// sandwich is linear and the redshift weights act on the pixel grid after it,
+// core/chunk_estimate.cpp:483-536).
+__global__ void __launch_bounds__(RTH) k_build_s_c_reso(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    ResoShared &sm = *reinterpret_cast<ResoShared *>(smraw);
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    if (ch.nelem <= 0) return;
+    const int ld = ch.ld, n = ch.n, nt = ld / RT;
+    if ((int) blockIdx.x >= nt * nt) return;
+    const int I = blockIdx.x / nt, J = blockIdx.x % nt;
+    if (I > J) return;
+    const ResoGeom g = reso_load(sm, a, ch, I, J);
+    const DeviceBins &bins = *a.bins;
+    const double *stab = (a.signal && !a.turn_off_sfid) ? a.signal + (size_t) ch.res * a.grid.nv * a.grid.nzp : nullptr;
+    double s_out[4] = {0, 0, 0, 0}, c_out[4] = {0, 0, 0, 0};
+    if (stab) {
+        reso_sandwich(sm, g, [&](int fr, int fc) {
+            double v, z;
+            return grid_vz(sm, g, fr, fc, v, z) ? signal_at_r(stab, a.grid, z, v) : 0.0;
+        }, s_out);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c_out[u] = s_out[u];
+    }
+    const int j = threadIdx.x % 32, r8 = threadIdx.x / 32;
+    const int gj = J * RT + j;
+    if (a.theta) {
+        const int nzb = ch.ns / ch.kbin_upp;
+        for (int iz = 0; iz < nzb; ++iz) {
+            const double *th = a.theta + ch.fis + iz * bins.nk;
+            bool any = false;
+            for (int kn = 0; kn < ch.kbin_upp; ++kn) any |= th[kn] != 0.0;
+            if (!any) continue;
+            double gm[4];
+            reso_sandwich(sm, g, [&](int fr, int fc) {
+                double v, z;
+                if (!grid_vz(sm, g, fr, fc, v, z)) return 0.0;
+                double acc = 0.0;
+                for (int kn = 0; kn < ch.kbin_upp; ++kn) {
+                    if (th[kn] == 0.0) continue;
+                    const double k1 = bins.k_edges[kn], k2 = bins.k_edges[kn + 1];
+                    acc += th[kn] * qband((k1 + k2) / 2., k2 - k1, v);
+                }
+                return acc;
+            }, gm);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int gi = I * RT + r8 + 8 * u;
+                if (gi < n && gj < n) {
+                    const int lo = min(gi, gj), hi = max(gi, gj);
+                    const double z = a.sqw[ch.pix + lo] * a.sqw[ch.pix + hi] - 1.0;
+                    c_out[u] += gm[u] * zweight_r(bins, ch.zb0 + iz, z);
+                }
+            }
+        }
+    }
+    double *S = fws_d(a, ch.o_s), *C = fws_d(a, ch.o_c);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int gi = I * RT + r8 + 8 * u;
+        double sv = 0.0, cv = (gi == gj) ? 1.0 : 0.0;
+        if (gi < n && gj < n) {
+            sv = a.turn_off_sfid ? 0.0 : s_out[u];
+            cv += a.sqiv[ch.pix + gi] * c_out[u] * a.sqiv[ch.pix + gj];
+        }
+        S[(size_t) gi * ld + gj] = sv;
+        C[(size_t) gi * ld + gj] = cv;
+        if (I != J) {
+            S[(size_t) gj * ld + gi] = sv;
+            C[(size_t) gj * ld + gi] = cv;
+        }
+    }
+}
+
+// Phase B: Q_s = w_m(z_ij) (R Q_k R^T)_ij for the chunk's stored (k, m) and the
+// per-block partial sums of d_s = y^T Q_s y.  FP64 slots (ws o_q) or, MIXED,
+// fp16 hi/lo planes with the slot scale.  d partial rows: each 64 x 64 tile of
+// the plain build owns `parts` rows; this tile's sub-tile writes its sum into
+// the first of its share and zeros into the rest (lower tiles only zeros).
+template <bool MIXED>
+__global__ void __launch_bounds__(RTH) k_build_q_reso(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    ResoShared &sm = *reinterpret_cast<ResoShared *>(smraw);
+    __shared__ double red[RTH / 32];
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    if (ch.nelem <= 0 || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    const int ld = ch.ld, n = ch.n, nt = ld / RT, t64 = ld / 64;
+    if ((int) blockIdx.x >= nt * nt) return;
+    const int I = blockIdx.x / nt, J = blockIdx.x % nt;
+    const int parts = MIXED ? 16 : 8, share = parts / 4;
+    double *dpart = ws_d(a, ch.o_dpart) +
+                    ((size_t) ((I / 2) * t64 + J / 2) * parts + ((I % 2) * 2 + (J % 2)) * share) * ch.ns;
+    if (I > J) {
+        for (int e = threadIdx.x; e < share * ch.ns; e += blockDim.x) dpart[e] = 0.0;
+        return;
+    }
+    const ResoGeom g = reso_load(sm, a, ch, I, J);
+    const DeviceBins &bins = *a.bins;
+    const int j = threadIdx.x % 32, r8 = threadIdx.x / 32, gj = J * RT + j;
+    const int nzb = ch.ns / ch.kbin_upp;
+    const double *y = fws_d(a, ch.o_y);
+    // z_ij and y_i y_j of the thread's four elements
+    double zz[4], yy[4];
+    bool valid[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int gi = I * RT + r8 + 8 * u;
+        valid[u] = gi < n && gj < n;
+        yy[u] = valid[u] ? y[gi] * y[gj] : 0.0;
+        const int lo = min(gi, gj), hi = max(gi, gj);
+        zz[u] = valid[u] ? a.sqw[ch.pix + lo] * a.sqw[ch.pix + hi] - 1.0 : 0.0;
+    }
+    const double mult = (I == J) ? 1.0 : 2.0;   // the mirror tile's share of y^T Q y
+    const size_t plane = (size_t) ld * ld;
+    for (int kn = 0; kn < ch.kbin_upp; ++kn) {
+        const double k1 = bins.k_edges[kn], k2 = bins.k_edges[kn + 1], kc = (k1 + k2) / 2., dk = k2 - k1;
+        double b[4];
+        reso_sandwich(sm, g, [&](int fr, int fc) {
+            double v, z;
+            return grid_vz(sm, g, fr, fc, v, z) ? qband(kc, dk, v) : 0.0;
+        }, b);
+        for (int iz = 0; iz < nzb; ++iz) {
+            const int s = iz * ch.kbin_upp + kn;
+            double part = 0.0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int gi = I * RT + r8 + 8 * u;
+                const double q = valid[u] ? b[u] * zweight_r(bins, ch.zb0 + iz, zz[u]) : 0.0;
+                part += yy[u] * q;
+                const size_t e1 = (size_t) gi * ld + gj, e2 = (size_t) gj * ld + gi;
+                if (MIXED) {
+                    const float qs = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + s];
+                    const float x = (float) q * qs;
+                    const __half h = __float2half_rn(x);
+                    const __half l = __float2half_rn(x - __half2float(h));
+                    __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
+                    __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
+                    qh[e1] = h; ql[e1] = l;
+                    if (I != J) { qh[e2] = h; ql[e2] = l; }
+                } else {
+                    double *Q = ws_d(a, ch.o_q) + (size_t) s * plane;
+                    Q[e1] = q;
+                    if (I != J) Q[e2] = q;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+            if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = part;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double acc = 0.0;
+                for (int w = 0; w < RTH / 32; ++w) acc += red[w];
+                dpart[s] = mult * acc;
+                for (int r = 1; r < share; ++r) dpart[(size_t) r * ch.ns + s] = 0.0;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+bool reso_attr_set = false;
+
+void set_reso_attrs() {
+    if (reso_attr_set) return;
+    const int bytes = (int) sizeof(ResoShared);
+    cudaFuncSetAttribute(k_build_s_c_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_build_q_reso<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_build_q_reso<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    reso_attr_set = true;
+}
+
+}  // namespace
+
+void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st) {
+    set_reso_attrs();
+    const int nt = a.max_ld / RT;
+    k_build_s_c_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
+    a.launches++;
+}
+
+void launch_build_q_reso(WaveArgs &a, cudaStream_t st) {
+    set_reso_attrs();
+    const int nt = a.max_ld / RT;
+    if (a.precision == LQG_PRECISION_MIXED)
+        k_build_q_reso<true><<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
+    else
+        k_build_q_reso<false><<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
+    a.launches++;
+}
+
+}  // namespace lqg

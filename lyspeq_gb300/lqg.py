@@ -22,7 +22,8 @@ CHUNK_STATUS = {0: "ok", 1: "short", 2: "no_table", 3: "empty", 4: "out_of_range
 EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_error",
            "lqg_batch_add", "lqg_batch_clear", "lqg_batch_size", "lqg_chunk_info",
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
-           "lqg_last_timings", "lqg_last_launch_count"]
+           "lqg_last_timings", "lqg_last_launch_count", "lqg_batch_add_reso",
+           "lqg_resomat_deconvolve", "lqg_resomat_oversample"]
 
 
 class LqgBins(C.Structure):
@@ -64,6 +65,10 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_last_error.argtypes = [vp]
     lib.lqg_last_error.restype = C.c_char_p
     lib.lqg_batch_add.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), dp, dp, dp, ip, ip]
+    lib.lqg_batch_add_reso.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), dp, dp, dp, C.c_int, C.c_int,
+                                       dp, ip]
+    lib.lqg_resomat_deconvolve.argtypes = [C.c_int, C.c_int, dp, C.c_double]
+    lib.lqg_resomat_oversample.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_double, dp]
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
@@ -153,6 +158,36 @@ class Engine:
             if chunks else np.zeros(0)
         return self.add_chunks(cat(0), cat(1), cat(2), offs, [c[3] for c in chunks])
 
+    def add_chunks_reso(self, lam, delta, ivar, offsets, oversampling, resomat):
+        """Add chunks with resolution matrices: resomat has one row of nelem
+        values per pixel (see lqg_batch_add_reso); returns the per-chunk status."""
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        delta = np.ascontiguousarray(delta, dtype=np.float64)
+        ivar = np.ascontiguousarray(ivar, dtype=np.float64)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        rm = np.ascontiguousarray(resomat, dtype=np.float64)
+        if rm.ndim != 2 or rm.shape[0] != len(lam):
+            raise ValueError("resomat must have one row per pixel")
+        n = len(offsets) - 1
+        status = np.zeros(max(n, 1), dtype=np.int32)
+        rc = self.lib.lqg_batch_add_reso(self.h, n, offsets.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         _dptr(lam), _dptr(delta), _dptr(ivar), int(oversampling),
+                                         rm.shape[1], _dptr(rm), _iptr(status))
+        self._check(rc, "lqg_batch_add_reso")
+        return status[:n]
+
+    def add_chunk_list_reso(self, chunks, oversampling):
+        """chunks: iterable of (lambda_angstrom, delta, ivar, resomat), resomat
+        the chunk's oversampled rows [n][nelem] (oversampling > 0) or its
+        diagonal matrix values[ndiags][n] (oversampling <= 0)."""
+        chunks = list(chunks)
+        offs = np.zeros(len(chunks) + 1, dtype=np.int64)
+        for i, c in enumerate(chunks):
+            offs[i + 1] = offs[i] + len(c[0])
+        cat = lambda j: np.concatenate([np.asarray(c[j], dtype=np.float64) for c in chunks])
+        per_pixel = [np.asarray(c[3]) if oversampling > 0 else np.asarray(c[3]).T for c in chunks]
+        return self.add_chunks_reso(cat(0), cat(1), cat(2), offs, oversampling, np.concatenate(per_pixel))
+
     def clear(self):
         self._check(self.lib.lqg_batch_clear(self.h), "lqg_batch_clear")
 
@@ -212,3 +247,26 @@ class Engine:
 
     def launch_count(self):
         return self.lib.lqg_last_launch_count(self.h)
+
+
+def resomat_deconvolve(values, m):
+    """DiaMatrix::deconvolve through the library (host only): values[ndiags][n]."""
+    lib = load_library()
+    v = np.array(values, dtype=np.float64, order="C")
+    nd, n = v.shape
+    rc = lib.lqg_resomat_deconvolve(n, nd, _dptr(v), float(m))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_resomat_deconvolve failed with {rc}")
+    return v
+
+
+def resomat_oversample(values, osamp, dlambda):
+    """Resolution::oversample through the library (host only): rows[n][nelem]."""
+    lib = load_library()
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    nd, n = v.shape
+    rows = np.zeros((n, 2 * (nd // 2) * osamp + 1))
+    rc = lib.lqg_resomat_oversample(n, nd, _dptr(v), int(osamp), float(dlambda), _dptr(rows))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_resomat_oversample failed with {rc}")
+    return rows

@@ -11,13 +11,16 @@ import golden_cases as G
 
 pytestmark = pytest.mark.gpu
 MIXED_TOL = 1e-5
-CASES = ["tiny_nomarg", "tiny_marg1", "tiny_masked", "small_cfg", "desi_sub"]
+CASES = ["tiny_nomarg", "tiny_marg1", "tiny_masked", "small_cfg", "desi_sub", "tiny_reso", "tiny_reso_dia"]
 
 
 def make_engine(c):
     from lyspeq_gb300 import lqg
     eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg)
-    st = eng.add_chunk_list(c.chunks)
+    if c.reso is None:
+        st = eng.add_chunk_list(c.chunks)
+    else:
+        st = eng.add_chunk_list_reso([ch[:3] + (rm,) for ch, rm in zip(c.chunks, c.rmats)], c.reso[0])
     assert (st == 0).all(), st
     return eng
 

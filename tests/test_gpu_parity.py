@@ -20,7 +20,10 @@ FP64_TOL = {"tiny_marg3": 1e-7}
 def make_engine(c, **kw):
     from lyspeq_gb300 import lqg
     eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg, **kw)
-    st = eng.add_chunk_list(c.chunks)
+    if c.reso is None:
+        st = eng.add_chunk_list(c.chunks)
+    else:
+        st = eng.add_chunk_list_reso([ch[:3] + (rm,) for ch, rm in zip(c.chunks, c.rmats)], c.reso[0])
     return eng, st
 
 
