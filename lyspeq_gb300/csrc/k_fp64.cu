@@ -16,6 +16,7 @@
 // Gram product G = P R^T with rows P = [A_0^T .. A_{ns-1}^T, (C^-1 S)^T, N C^-1]
 // and R = [A_0 .. A_{ns-1}].
 #include "lqg_internal.cuh"
+#include "lqg_ff.cuh"
 
 namespace lqg {
 
@@ -80,14 +81,6 @@ __device__ __forceinline__ void vindex(const TableGrid &g, double v, int &n, dou
 // (Sterbenz), so v_ij, the interpolation fraction and the redshift weights
 // keep ~1e-7 relative accuracy, down to the small weights at a bin's edge.
 
-// a * b for double-float a, b: p + e (the lo * lo term is below 2^-46)
-__device__ __forceinline__ void two_prod_ff(float2 a, float2 b, float &p, float &e) {
-    p = __fmul_rn(a.x, b.x);
-    e = __fmaf_rn(a.x, b.x, -p);
-    e = __fmaf_rn(a.x, b.y, e);
-    e = __fmaf_rn(a.y, b.x, e);
-}
-
 // Table index and fraction at v = c (ln w_hi - ln w_lo): xx = v / dv as p + e,
 // then the reference's clamped linear-interpolation index
 // (mathtools/discrete_interpolation.cpp:61-72, v1 = 0).
@@ -103,24 +96,6 @@ __device__ __forceinline__ void vindex_ff(const TableGrid &g, float2 lwh, float2
     if (nn < 0) { nn = 0; f = __fadd_rn(p, e); }
     n = nn;
     dn = f;
-}
-
-// Redshift weight of bin zm at 1 + z = P + E (zweight's rules): u = z - z_c
-// as u_hi (exact) + u_lo, and dz - |u| formed before any rounding.
-__device__ __forceinline__ float zweight_ff(const DeviceBins &b, int zm, float P, float E) {
-    const float u_hi = __fsub_rn(P, b.zc1_hi[zm]);
-    const float u_lo = __fsub_rn(E, b.zc1_lo[zm]);
-    const float u = __fadd_rn(u_hi, u_lo);
-    const float au_hi = fabsf(u_hi);
-    const float au_lo = u_hi > 0.f ? u_lo : (u_hi < 0.f ? -u_lo : fabsf(u_lo));
-    if (!b.triangular || b.nz == 1) {
-        const float r = __fadd_rn(__fsub_rn(b.dzh_hi, au_hi), __fsub_rn(b.dzh_lo, au_lo));
-        return r >= 0.f ? 1.f : 0.f;
-    }
-    if (zm == 0 && u < 0.f) return 1.f;
-    if (zm == b.nz - 1 && u > 0.f) return 1.f;
-    const float r = __fadd_rn(__fsub_rn(b.dz_hi, au_hi), __fsub_rn(b.dz_lo, au_lo));
-    return r >= 0.f ? r * b.inv_dz : 0.f;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

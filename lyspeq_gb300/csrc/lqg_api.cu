@@ -24,7 +24,7 @@ struct lqg_ctx {
     std::vector<int> r_fwhm;
     std::vector<double> tdv, qmax, smax;
     TableGrid grid{};
-    DevBuf d_deriv, d_deriv_f, d_signal, d_bins;
+    DevBuf d_deriv, d_deriv_f, d_signal, d_signal_ff, d_bins;
     lqg_opts opts{};
     // batch
     struct HostChunk {
@@ -148,6 +148,9 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
         const float2 kv = split_ff(kSpeedOfLight / ctx->grid.dv);
         ctx->grid.kv_hi = kv.x;
         ctx->grid.kv_lo = kv.y;
+        const float2 z1p = split_ff(1.0 + ctx->grid.z1), idz = split_ff(1.0 / ctx->grid.dz);
+        ctx->grid.z1p_hi = z1p.x; ctx->grid.z1p_lo = z1p.y;
+        ctx->grid.idz_hi = idz.x; ctx->grid.idz_lo = idz.y;
     }
     size_t nd = (size_t) tables->n_tables * bins->nk * tables->nv;
     size_t ns = (size_t) tables->n_tables * tables->nv * tables->nzp;
@@ -171,6 +174,12 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     if (tables->signal) {
         if (ctx->d_signal.alloc(ns * 8) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "tables");
         cudaMemcpy(ctx->d_signal.p, tables->signal, ns * 8, cudaMemcpyHostToDevice);
+        {
+            std::vector<float2> sf(ns);
+            for (size_t e = 0; e < ns; ++e) sf[e] = split_ff(tables->signal[e]);
+            if (ctx->d_signal_ff.alloc(ns * 8) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "tables");
+            cudaMemcpy(ctx->d_signal_ff.p, sf.data(), ns * 8, cudaMemcpyHostToDevice);
+        }
         for (int t = 0; t < tables->n_tables; ++t) {
             double m = 0;
             const double *s = tables->signal + (size_t) t * tables->nv * tables->nzp;
@@ -596,7 +605,9 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             const int idx = g.members[k];
             const auto &h = ctx->chunks[idx];
             const int gt = gram_blocks(h.ns), splits = gram_splits_for(h.ld, precision);
-            const int64_t need = chunk_ws_bytes(h.ld, h.ns, precision, splits, gt);
+            int64_t need = chunk_ws_bytes(h.ld, h.ns, precision, splits, gt);
+            if (precision == LQG_PRECISION_MIXED && h.nelem > 0)
+                need += align_up((int64_t) h.kbin_upp * h.nf * 8, 256);   // grid-point phases
             bool fresh = g.waves.empty() || g.waves.back().ld != h.ld || g.waves.back().gt != gt;
             if (!fresh) {
                 const auto &w = g.waves.back();
@@ -623,6 +634,9 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             for (int k : w.members) {
                 ChunkDesc d = desc[g.desc_off + k];
                 d.o_dpart = off; off += align_up(tiles * 16 * d.ns * 8, 256);
+                if (precision == LQG_PRECISION_MIXED && d.nelem > 0) {
+                    d.o_ph = off; off += align_up((int64_t) d.kbin_upp * d.nf * 8, 256);
+                }
                 if (precision == LQG_PRECISION_FP64) {
                     d.o_part = off; off += align_up(gblk * 8, 256);
                     d.o_q = off; off += align_up(m * d.ns, 256);
@@ -757,6 +771,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.deriv = ctx->d_deriv.as<double>();
     base.deriv_f = ctx->d_deriv_f.as<float>();
     base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
+    base.signal_ff = ctx->d_signal_ff.p ? ctx->d_signal_ff.as<float2>() : nullptr;
     base.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
     base.results = ctx->d_results.as<double>();
     base.status = ctx->d_status.as<int>();

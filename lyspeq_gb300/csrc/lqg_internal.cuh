@@ -50,6 +50,7 @@ struct ChunkDesc {
     // a diagonal matrix), whose ln(lambda) and sqrt(lambda) start at fpix.
     int nelem, os, sh, nf;
     int64_t fpix, rw_off;
+    int64_t o_ph;         // wave workspace: cos, sin of k_c u at each grid point (mixed path)
     double rw_sum;        // largest sum of |weights| of a row (bound of R M R^T)
 };
 
@@ -70,6 +71,8 @@ struct TableGrid {
     int nv, nzp, n_tables;
     double v1, dv, z1, dz;
     float kv_hi, kv_lo;   // speed of light / dv as double-float
+    float z1p_hi, z1p_lo; // 1 + z1 as double-float
+    float idz_hi, idz_lo; // 1 / dz as double-float
 };
 
 // Thin RAII for device allocations owned by the context.
@@ -105,6 +108,7 @@ struct WaveArgs {
     const double *flogw, *fsqw, *rw;                 // resolution-matrix grids and weights
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
+    const float2 *signal_ff;                         // signal table as double-float (mixed path)
     const double *theta;                             // device, nkz
     double *results;                                 // per-chunk results
     int *status;                                     // per-chunk status (wave-local)

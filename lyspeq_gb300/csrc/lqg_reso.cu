@@ -18,6 +18,7 @@
 // matrix, and each grid point of M is evaluated once per tile.  Only tiles on
 // or above the diagonal are computed; each writes its mirror tile too.
 #include "lqg_internal.cuh"
+#include "lqg_ff.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -394,12 +395,11 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso(WaveArgs a) {
     }
 }
 
-// Phase B: Q_s = w_m(z_ij) (R Q_k R^T)_ij for the chunk's stored (k, m) and the
-// per-block partial sums of d_s = y^T Q_s y.  FP64 slots (ws o_q) or, MIXED,
-// fp16 hi/lo planes with the slot scale.  d partial rows: each 64 x 64 tile of
-// the plain build owns `parts` rows; this tile's sub-tile writes its sum into
-// the first of its share and zeros into the rest (lower tiles only zeros).
-template <bool MIXED>
+// Phase B, FP64 path: Q_s = w_m(z_ij) (R Q_k R^T)_ij for the chunk's stored
+// (k, m) into the FP64 slots (ws o_q), and the per-block partial sums of
+// d_s = y^T Q_s y.  d partial rows: each 64 x 64 tile of the plain build owns
+// 8 rows; this tile's quarter writes its sum into the first of its two rows and
+// zero into the other (tiles below the diagonal write zeros only).
 __global__ void __launch_bounds__(RTH) k_build_q_reso(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     ResoShared &sm = *reinterpret_cast<ResoShared *>(smraw);
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso(WaveArgs a) {
     const int ld = ch.ld, n = ch.n, nt = ld / RT, t64 = ld / 64;
     if ((int) blockIdx.x >= nt * nt) return;
     const int I = blockIdx.x / nt, J = blockIdx.x % nt;
-    const int parts = MIXED ? 16 : 8, share = parts / 4;
+    const int parts = 8, share = parts / 4;
     double *dpart = ws_d(a, ch.o_dpart) +
                     ((size_t) ((I / 2) * t64 + J / 2) * parts + ((I % 2) * 2 + (J % 2)) * share) * ch.ns;
     if (I > J) {
@@ -450,21 +450,9 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso(WaveArgs a) {
                 const int gi = I * RT + r8 + 8 * u;
                 const double q = valid[u] ? b[u] * zweight_r(bins, ch.zb0 + iz, zz[u]) : 0.0;
                 part += yy[u] * q;
-                const size_t e1 = (size_t) gi * ld + gj, e2 = (size_t) gj * ld + gi;
-                if (MIXED) {
-                    const float qs = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + s];
-                    const float x = (float) q * qs;
-                    const __half h = __float2half_rn(x);
-                    const __half l = __float2half_rn(x - __half2float(h));
-                    __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
-                    __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
-                    qh[e1] = h; ql[e1] = l;
-                    if (I != J) { qh[e2] = h; ql[e2] = l; }
-                } else {
-                    double *Q = ws_d(a, ch.o_q) + (size_t) s * plane;
-                    Q[e1] = q;
-                    if (I != J) Q[e2] = q;
-                }
+                double *Q = ws_d(a, ch.o_q) + (size_t) s * plane;
+                Q[(size_t) gi * ld + gj] = q;
+                if (I != J) Q[(size_t) gj * ld + gi] = q;
             }
             for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
             if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = part;
@@ -480,14 +468,368 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso(WaveArgs a) {
     }
 }
 
+// Mixed path, per grid point p and stored k band: (cos, sin)(k_c u_p) with
+// u_p = c ln(w_p / w_0), in FP64.  cos(k_c v_pq) = C_p C_q + S_p S_q then
+// needs no large-argument reduction on the FP32 pipe.
+__global__ void k_reso_phases(WaveArgs a) {
+    const ChunkDesc &ch = a.chunks[blockIdx.y];
+    if (ch.nelem <= 0 || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    const DeviceBins &bins = *a.bins;
+    float2 *ph = reinterpret_cast<float2 *>(a.ws + ch.o_ph);
+    const double l0 = a.flogw[ch.fpix];
+    const int total = ch.kbin_upp * ch.nf;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int kn = e / ch.nf, p = e % ch.nf;
+        const double kc = (bins.k_edges[kn] + bins.k_edges[kn + 1]) / 2.;
+        double sn, cs;
+        sincos(kc * (kSpeedOfLight * (a.flogw[ch.fpix + p] - l0)), &sn, &cs);
+        ph[e] = make_float2((float) cs, (float) sn);
+    }
+}
+
+constexpr int FSLAB = 16;
+
+struct ResoSharedF {
+    float sinc[RLF][RLF + 1];      // sin(x) / x on the tile's grid block, x = dk v / 2, for one dk
+    float fq[FSLAB * (RLF + 1)];   // a slab of Q_k on the block; later the 32 x 33 output tile
+    float t[RLF][RT + 1];          // T = M_block R_J^T
+    float wi[RT][RME + 1], wj[RT][RME + 1];
+    float2 lwr[RLF], lwc[RLF];     // ln w of the block's grid rows / columns (double-float)
+    float cr[RLF], sr[RLF], cc[RLF], sc[RLF];   // (cos, sin)(k_c u) of the rows / columns
+    float qscale[kMaxGramBlocks * 128];
+};
+
+// Phase B, mixed path: the same Q_s as k_build_q_reso on the FP32 pipe, into
+// fp16 hi/lo planes with the slot scale.  Q_k on the grid is
+// (dk / pi) sinc(dk v / 2) (C_p C_q + S_p S_q): v from double-float ln w
+// (relative error ~1e-7), the cosine from FP64 phases (absolute error ~1e-7);
+// the sinc block is computed once per distinct dk.  Redshift weights in
+// double-float arithmetic (as the plain mixed build).  d partial rows: 16 per
+// 64 x 64 tile, 4 per quarter.
+__global__ void __launch_bounds__(RTH) k_build_q_reso_f32(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    ResoSharedF &sm = *reinterpret_cast<ResoSharedF *>(smraw);
+    __shared__ double red[RTH / 32];
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    if (ch.nelem <= 0 || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    const int ld = ch.ld, n = ch.n, nt = ld / RT, t64 = ld / 64;
+    if ((int) blockIdx.x >= nt * nt) return;
+    const int I = blockIdx.x / nt, J = blockIdx.x % nt;
+    const int parts = 16, share = parts / 4;
+    double *dpart = ws_d(a, ch.o_dpart) +
+                    ((size_t) ((I / 2) * t64 + J / 2) * parts + ((I % 2) * 2 + (J % 2)) * share) * ch.ns;
+    if (I > J) {
+        for (int e = threadIdx.x; e < share * ch.ns; e += blockDim.x) dpart[e] = 0.0;
+        return;
+    }
+    const int os = ch.os, nel = ch.nelem, lf = (RT - 1) * os + nel;
+    const int r0 = I * RT * os - ch.sh, c0 = J * RT * os - ch.sh;
+    for (int e = threadIdx.x; e < RT * nel; e += blockDim.x) {
+        const int r = e / nel, k = e % nel;
+        const int ri = I * RT + r, rj = J * RT + r;
+        sm.wi[r][k] = ri < n ? (float) a.rw[ch.rw_off + (int64_t) ri * nel + k] : 0.f;
+        sm.wj[r][k] = rj < n ? (float) a.rw[ch.rw_off + (int64_t) rj * nel + k] : 0.f;
+    }
+    for (int e = threadIdx.x; e < lf; e += blockDim.x) {
+        const int pr = r0 + e, pc = c0 + e;
+        const double lr = (pr >= 0 && pr < ch.nf) ? a.flogw[ch.fpix + pr] : 0.0;
+        const double lc = (pc >= 0 && pc < ch.nf) ? a.flogw[ch.fpix + pc] : 0.0;
+        sm.lwr[e] = make_float2((float) lr, (float) (lr - (double) (float) lr));
+        sm.lwc[e] = make_float2((float) lc, (float) (lc - (double) (float) lc));
+    }
+    for (int t = threadIdx.x; t < ch.ns; t += blockDim.x)
+        sm.qscale[t] = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + t];
+    __syncthreads();
+    const DeviceBins &bins = *a.bins;
+    const int j = threadIdx.x % 32, r8 = threadIdx.x / 32, gj = J * RT + j;
+    const int nzb = ch.ns / ch.kbin_upp;
+    const double *y = fws_d(a, ch.o_y);
+    const float2 *sw2 = a.sqw2 + ch.pix;
+    // per element: y_i y_j, 1 + z_ij as double-float, weights of the first 4 redshift bins
+    float yy[4], zp[4], ze[4], zw[4][4];
+    bool valid[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int gi = I * RT + r8 + 8 * u;
+        valid[u] = gi < n && gj < n;
+        yy[u] = valid[u] ? (float) (y[gi] * y[gj]) : 0.f;
+        zp[u] = 0.f; ze[u] = 0.f;
+        if (valid[u]) two_prod_ff(sw2[min(gi, gj)], sw2[max(gi, gj)], zp[u], ze[u]);
+#pragma unroll
+        for (int iz = 0; iz < 4; ++iz)
+            zw[u][iz] = (valid[u] && iz < nzb) ? zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]) : 0.f;
+    }
+    const float2 *ph = reinterpret_cast<const float2 *>(a.ws + ch.o_ph);
+    const float mult = (I == J) ? 1.f : 2.f;
+    const size_t plane = (size_t) ld * ld;
+    float dk_cached = -1.f;
+    float (*fs)[RLF + 1] = reinterpret_cast<float (*)[RLF + 1]>(sm.fq);
+    float (*qt)[RT + 1] = reinterpret_cast<float (*)[RT + 1]>(sm.fq);
+    for (int kn = 0; kn < ch.kbin_upp; ++kn) {
+        const double k1 = bins.k_edges[kn], k2 = bins.k_edges[kn + 1];
+        const float dkf = (float) (k2 - k1), coef = (float) ((k2 - k1) / kPi);
+        // phases of the block's grid rows and columns for this band
+        for (int e = threadIdx.x; e < lf; e += blockDim.x) {
+            const int pr = r0 + e, pc = c0 + e;
+            const float2 a1 = (pr >= 0 && pr < ch.nf) ? ph[(size_t) kn * ch.nf + pr] : make_float2(0.f, 0.f);
+            const float2 a2 = (pc >= 0 && pc < ch.nf) ? ph[(size_t) kn * ch.nf + pc] : make_float2(0.f, 0.f);
+            sm.cr[e] = a1.x; sm.sr[e] = a1.y;
+            sm.cc[e] = a2.x; sm.sc[e] = a2.y;
+        }
+        if (dkf != dk_cached) {
+            const float hdk = 0.5f * dkf;
+            for (int e = threadIdx.x; e < lf * lf; e += RTH) {
+                const int fr = e / lf, fc = e % lf;
+                const int p = r0 + fr, q = c0 + fc;
+                float v = 0.f;
+                bool ok = p >= 0 && q >= 0 && p < ch.nf && q < ch.nf;
+                if (ok) {
+                    const float2 hi = p <= q ? sm.lwc[fc] : sm.lwr[fr], lo = p <= q ? sm.lwr[fr] : sm.lwc[fc];
+                    v = __fmul_rn((float) kSpeedOfLight, __fadd_rn(__fsub_rn(hi.x, lo.x), __fsub_rn(hi.y, lo.y)));
+                }
+                const float x = hdk * v;
+                sm.sinc[fr][fc] = !ok ? 0.f : (x == 0.f ? 1.f : __fdiv_rn(sinf(x), x));
+            }
+            dk_cached = dkf;
+        }
+        __syncthreads();
+        for (int s0 = 0; s0 < lf; s0 += FSLAB) {
+            const int rows = min(FSLAB, lf - s0);
+            for (int e = threadIdx.x; e < rows * lf; e += RTH) {
+                const int fr = e / lf, fc = e % lf;
+                const float cs = fmaf(sm.cr[s0 + fr], sm.cc[fc], sm.sr[s0 + fr] * sm.sc[fc]);
+                fs[fr][fc] = coef * sm.sinc[s0 + fr][fc] * cs;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < FSLAB / 8; ++u) {
+                const int fr = r8 + 8 * u;
+                if (fr < rows) {
+                    const float *frow = &fs[fr][j * os];
+                    float acc = 0.f;
+                    for (int bb = 0; bb < nel; ++bb) acc = fmaf(frow[bb], sm.wj[j][bb], acc);
+                    sm.t[s0 + fr][j] = acc;
+                }
+            }
+            __syncthreads();
+        }
+        float b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = r8 + 8 * u;
+            float acc = 0.f;
+            for (int aa = 0; aa < nel; ++aa) acc = fmaf(sm.wi[i][aa], sm.t[i * os + aa][j], acc);
+            b[u] = acc;
+        }
+        for (int iz = 0; iz < nzb; ++iz) {
+            const int s = iz * ch.kbin_upp + kn;
+            const float qs = sm.qscale[s];
+            __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
+            __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
+            float part = 0.f;
+            __syncthreads();   // qt (aliasing the slab) is free
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = r8 + 8 * u, gi = I * RT + i;
+                float w = 0.f;
+                if (valid[u]) w = iz < 4 ? zw[u][iz] : zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]);
+                const float q = b[u] * w;
+                part = fmaf(yy[u], q, part);
+                const float x = q * qs;
+                qt[i][j] = x;
+                const __half h = __float2half_rn(x);
+                qh[(size_t) gi * ld + gj] = h;
+                ql[(size_t) gi * ld + gj] = __float2half_rn(x - __half2float(h));
+            }
+            __syncthreads();
+            if (I != J) {
+                // mirror tile, row J*RT + r8 + 8u, column I*RT + j: element (j, r8 + 8u) of this tile
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int rr = J * RT + r8 + 8 * u, cc2 = I * RT + j;
+                    const float x = qt[j][r8 + 8 * u];
+                    const __half h = __float2half_rn(x);
+                    qh[(size_t) rr * ld + cc2] = h;
+                    ql[(size_t) rr * ld + cc2] = __float2half_rn(x - __half2float(h));
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+            if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = (double) part;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double acc = 0.0;
+                for (int w = 0; w < RTH / 32; ++w) acc += red[w];
+                dpart[s] = mult * acc;
+                for (int r = 1; r < share; ++r) dpart[(size_t) r * ch.ns + s] = 0.0;
+            }
+        }
+        __syncthreads();   // before the next band overwrites the phases and the slab
+    }
+}
+
+// ---- double-float arithmetic on the FP32 pipe (value = hi + lo) ----
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 ff_norm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    const float2 s = ff_two_sum(a.x, b.x);
+    return ff_norm(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 ff_sub(float2 a, float2 b) { return ff_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    float p, e;
+    two_prod_ff(a, b, p, e);
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return ff_add(ff_mul(a, b), c); }
+__device__ __forceinline__ float2 ff_of(double x) {
+    const float h = (float) x;
+    return make_float2(h, (float) (x - (double) h));
+}
+
+// Clamped interpolation index and fraction of x (a double-float >= any
+// negative value), the reference's rule (discrete_interpolation.cpp:61-72,
+// 221-242): n = trunc(x) clamped to [0, nmax], fraction x - n.
+__device__ __forceinline__ void ff_index(float2 x, int nmax, int &n, float2 &frac) {
+    int nn = (int) floorf(x.x);
+    float2 f = ff_norm(__fsub_rn(x.x, (float) nn), x.y);
+    if (f.x < 0.f) { --nn; f = ff_add(f, make_float2(1.f, 0.f)); }
+    else if (f.x >= 1.f) { ++nn; f = ff_sub(f, make_float2(1.f, 0.f)); }
+    // trunc rather than floor below zero (the reference casts to int)
+    if (nn < 0) nn = (x.x < 0.f && x.x > -1.f) ? 0 : nn;
+    if (nn > nmax) nn = nmax;
+    if (nn < 0) nn = 0;
+    f = ff_norm(__fsub_rn(x.x, (float) nn), x.y);
+    n = nn;
+    frac = f;
+}
+
+struct ResoSharedFF {
+    float2 wi[RT][RME + 1], wj[RT][RME + 1];
+    float2 f[RSLAB][RLF + 1];
+    float2 t[RLF][RT + 1];
+    float2 lwr[RLF], swr[RLF], lwc[RLF], swc[RLF];
+};
+
+// Phase A, mixed path without theta: S = R S_grid R^T and C~ = D S D + I in
+// double-float arithmetic (about 48 significant bits) on the FP32 pipe;
+// grid v, z, interpolation fractions and table values in double-float, the
+// sandwich with double-float multiply-adds.  Stored as FP64.
+__global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    ResoSharedFF &sm = *reinterpret_cast<ResoSharedFF *>(smraw);
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    if (ch.nelem <= 0) return;
+    const int ld = ch.ld, n = ch.n, nt = ld / RT;
+    if ((int) blockIdx.x >= nt * nt) return;
+    const int I = blockIdx.x / nt, J = blockIdx.x % nt;
+    if (I > J) return;
+    const int os = ch.os, nel = ch.nelem, lf = (RT - 1) * os + nel;
+    const int r0 = I * RT * os - ch.sh, c0 = J * RT * os - ch.sh;
+    for (int e = threadIdx.x; e < RT * nel; e += blockDim.x) {
+        const int r = e / nel, k = e % nel;
+        const int ri = I * RT + r, rj = J * RT + r;
+        sm.wi[r][k] = ri < n ? ff_of(a.rw[ch.rw_off + (int64_t) ri * nel + k]) : make_float2(0.f, 0.f);
+        sm.wj[r][k] = rj < n ? ff_of(a.rw[ch.rw_off + (int64_t) rj * nel + k]) : make_float2(0.f, 0.f);
+    }
+    for (int e = threadIdx.x; e < lf; e += blockDim.x) {
+        const int pr = r0 + e, pc = c0 + e;
+        const bool okr = pr >= 0 && pr < ch.nf, okc = pc >= 0 && pc < ch.nf;
+        sm.lwr[e] = okr ? ff_of(a.flogw[ch.fpix + pr]) : make_float2(0.f, 0.f);
+        sm.swr[e] = okr ? ff_of(a.fsqw[ch.fpix + pr]) : make_float2(0.f, 0.f);
+        sm.lwc[e] = okc ? ff_of(a.flogw[ch.fpix + pc]) : make_float2(0.f, 0.f);
+        sm.swc[e] = okc ? ff_of(a.fsqw[ch.fpix + pc]) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const TableGrid &gr = a.grid;
+    const float2 *tab = (a.signal_ff && !a.turn_off_sfid) ? a.signal_ff + (size_t) ch.res * gr.nv * gr.nzp : nullptr;
+    const int j = threadIdx.x % 32, r8 = threadIdx.x / 32, gj = J * RT + j;
+    float2 sv[4] = {};
+    if (tab) {
+        const float2 kv = make_float2(gr.kv_hi, gr.kv_lo), z1p = make_float2(gr.z1p_hi, gr.z1p_lo);
+        const float2 idz = make_float2(gr.idz_hi, gr.idz_lo), one = make_float2(1.f, 0.f);
+        for (int s0 = 0; s0 < lf; s0 += RSLAB) {
+            const int rows = min(RSLAB, lf - s0);
+            for (int e = threadIdx.x; e < rows * lf; e += RTH) {
+                const int fr = e / lf, fc = e % lf, p = r0 + s0 + fr, q = c0 + fc;
+                float2 val = make_float2(0.f, 0.f);
+                if (p >= 0 && q >= 0 && p < ch.nf && q < ch.nf) {
+                    const bool up = p <= q;
+                    const float2 lh = up ? sm.lwc[fc] : sm.lwr[s0 + fr], ll = up ? sm.lwr[s0 + fr] : sm.lwc[fc];
+                    const float2 yy = ff_mul(ff_sub(lh, ll), kv);               // v / dv
+                    float zp, ze;
+                    two_prod_ff(sm.swr[s0 + fr], sm.swc[fc], zp, ze);            // 1 + z
+                    const float2 xx = ff_mul(ff_sub(ff_norm(zp, ze), z1p), idz); // (z - z1) / dz
+                    int nx, ny;
+                    float2 fx, fy;
+                    ff_index(xx, gr.nzp - 2, nx, fx);
+                    ff_index(yy, gr.nv - 2, ny, fy);
+                    const size_t ind = (size_t) nx + (size_t) gr.nzp * ny;
+                    const float2 gx = ff_sub(one, fx), gy = ff_sub(one, fy);
+                    val = ff_mul(ff_mul(tab[ind], gx), gy);
+                    val = ff_fma(ff_mul(tab[ind + 1], fx), gy, val);
+                    val = ff_fma(ff_mul(tab[ind + gr.nzp], gx), fy, val);
+                    val = ff_fma(ff_mul(tab[ind + gr.nzp + 1], fx), fy, val);
+                }
+                sm.f[fr][fc] = val;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < RSLAB / 8; ++u) {
+                const int fr = r8 + 8 * u;
+                if (fr < rows) {
+                    float2 acc = make_float2(0.f, 0.f);
+                    for (int b = 0; b < nel; ++b) acc = ff_fma(sm.f[fr][j * os + b], sm.wj[j][b], acc);
+                    sm.t[s0 + fr][j] = acc;
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = r8 + 8 * u;
+            float2 acc = make_float2(0.f, 0.f);
+            for (int aa = 0; aa < nel; ++aa) acc = ff_fma(sm.wi[i][aa], sm.t[i * os + aa][j], acc);
+            sv[u] = acc;
+        }
+    }
+    double *S = fws_d(a, ch.o_s), *C = fws_d(a, ch.o_c);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int gi = I * RT + r8 + 8 * u;
+        double s_d = 0.0, c_d = (gi == gj) ? 1.0 : 0.0;
+        if (gi < n && gj < n) {
+            s_d = (double) sv[u].x + (double) sv[u].y;
+            const float2 cv = ff_mul(ff_mul(ff_of(a.sqiv[ch.pix + gi]), sv[u]), ff_of(a.sqiv[ch.pix + gj]));
+            c_d += (double) cv.x + (double) cv.y;
+        }
+        S[(size_t) gi * ld + gj] = s_d;
+        C[(size_t) gi * ld + gj] = c_d;
+        if (I != J) {
+            S[(size_t) gj * ld + gi] = s_d;
+            C[(size_t) gj * ld + gi] = c_d;
+        }
+    }
+}
+
 bool reso_attr_set = false;
 
 void set_reso_attrs() {
     if (reso_attr_set) return;
     const int bytes = (int) sizeof(ResoShared);
     cudaFuncSetAttribute(k_build_s_c_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_build_q_reso<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_build_q_reso<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_build_q_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_build_q_reso_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) sizeof(ResoSharedF));
+    cudaFuncSetAttribute(k_build_s_c_reso_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) sizeof(ResoSharedFF));
     reso_attr_set = true;
 }
 
@@ -496,18 +838,25 @@ void set_reso_attrs() {
 void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st) {
     set_reso_attrs();
     const int nt = a.max_ld / RT;
-    k_build_s_c_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
+    // mixed path: double-float build unless theta is given (then the FP64 one)
+    if (a.precision == LQG_PRECISION_MIXED && !a.theta)
+        k_build_s_c_reso_ff<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoSharedFF), st>>>(a);
+    else
+        k_build_s_c_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
     a.launches++;
 }
 
 void launch_build_q_reso(WaveArgs &a, cudaStream_t st) {
     set_reso_attrs();
     const int nt = a.max_ld / RT;
-    if (a.precision == LQG_PRECISION_MIXED)
-        k_build_q_reso<true><<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
-    else
-        k_build_q_reso<false><<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
-    a.launches++;
+    if (a.precision == LQG_PRECISION_MIXED) {
+        k_reso_phases<<<dim3(32, a.n_chunks), 256, 0, st>>>(a);
+        k_build_q_reso_f32<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoSharedF), st>>>(a);
+        a.launches += 2;
+    } else {
+        k_build_q_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
+        a.launches++;
+    }
 }
 
 }  // namespace lqg

@@ -277,7 +277,9 @@ def _make_reso_workload(name, rng, seed, nch):
     osamp = -1 if name == "tiny_reso_dia" else 3
     table_dv = round(dv / 3.0, 1)
     longest = max(float(np.log(s.wave[-1] / s.wave[0]) * C_KMS) for s in spectra)
-    mfl = 20000.0 if name == "desi_reso" else 6000.0
+    # MaximumForestLength such that no chunk is too short (150 pixels of 50 km/s
+    # at 0.45 of it), as the other workloads choose it
+    mfl = 15000.0 if name == "desi_reso" else 6000.0
     lenv = float(math.ceil(max(longest + 12 * dv, mfl) * 1.02 / 100.0) * 100.0)
     nv = int(math.ceil(lenv / (table_dv / 2.0))) + 1
     nzp = max(10, bins.nz + 2)
