@@ -9,6 +9,12 @@ marginalisation of amplitude + slope.  Inputs are seeded synthetic data of
 those shapes (lyspeq_gb300.synth); the per-iteration working set (tens of GB
 of operand planes) is far larger than L2, so no L2 flush is needed.
 
+`--workload desi_reso` runs the resolution-matrix configuration instead:
+16384 chunks, N log-uniform in [150, 1000], 11-diagonal resolution matrices
+deconvolved and oversampled x 3 (S and Q_k built as R M R^T), 20 k x 3 z
+bins; the matrices are prepared on the host before timing, as lyspeq does
+while reading its files.
+
 A step is one lqg_nr_iteration over the whole batch (table interpolation ->
 C -> FP64 Cholesky/inverse -> C^-1 Q_k on tensor cores -> traces) plus the
 global Fisher inversion and theta update.  `value` times steps with the
@@ -97,17 +103,48 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def chunk_arrays(w):
-    """Chunks as lqg_batch_add takes them: lambda (A), delta, ivar, R."""
-    return [(s.wave, s.delta, 1.0 / np.asarray(s.sigma) ** 2, s.r_fwhm) for s in w.spectra]
+def chunk_arrays(w, lib=None):
+    """Chunks as lqg_batch_add takes them: lambda (A), delta, ivar, R.  For a
+    resolution-matrix workload the last item is the spectrum's matrix after
+    deconvolution and oversampling: through the library's host routines when
+    lib is given, else None (the CPU legs prepare it with the oracle)."""
+    out = []
+    for s in w.spectra:
+        ivar = 1.0 / np.asarray(s.sigma) ** 2
+        if not w.reso:
+            out.append((s.wave, s.delta, ivar, s.r_fwhm))
+            continue
+        rows = None
+        if lib is not None:
+            v = lib.resomat_deconvolve(s.resomat, w.deconv_m) if w.deconv_m > 0 else s.resomat
+            rows = lib.resomat_oversample(v, w.oversample, float(np.median(np.diff(s.wave)))) \
+                if w.oversample > 0 else np.ascontiguousarray(v.T)
+        out.append((s.wave, s.delta, ivar, rows))
+    return out
 
 
-def pack(chunks):
+def pack(chunks, reso=False):
     offs = np.zeros(len(chunks) + 1, dtype=np.int64)
     for i, c in enumerate(chunks):
         offs[i + 1] = offs[i] + len(c[0])
     cat = lambda j: np.ascontiguousarray(np.concatenate([np.asarray(c[j], np.float64) for c in chunks]))
-    return cat(0), cat(1), cat(2), offs, np.array([c[3] for c in chunks], dtype=np.int32)
+    last = cat(3).reshape(int(offs[-1]), -1) if reso else np.array([c[3] for c in chunks], dtype=np.int32)
+    return cat(0), cat(1), cat(2), offs, last
+
+
+def add_packed(eng, w, packed):
+    lam, delta, ivar, offs, last = packed
+    if w.reso:
+        return eng.add_chunks_reso(lam, delta, ivar, offs, w.oversample, last)
+    return eng.add_chunks(lam, delta, ivar, offs, last)
+
+
+def describe(w, n_ok):
+    if w.reso:
+        return (f"{w.name}: {n_ok} chunks, N log-uniform 150-1000, dv 50 km/s, 11-diagonal resolution "
+                f"matrices deconvolved and oversampled x{w.oversample}, 20 k x 3 z bins, no marginalisation")
+    return (f"{w.name}: {n_ok} chunks, N log-uniform 200-1200, dv 50 km/s, R 2000-5000, 35 k x 13 z bins, "
+            "amplitude+slope marginalisation")
 
 
 def flop_counts(ns_list, n_list):
@@ -120,29 +157,39 @@ def flop_counts(ns_list, n_list):
                 traces=float(np.sum(2 * (ns + 2) * ns * n ** 2)))
 
 
-def cpu_port_rate(w, chunks, budget_s=15.0, max_chunks=None):
+def cpu_port_rate(w, chunks, budget_s=15.0, max_chunks=None, order=None):
     """Chunks/s of the CPU restatement of lyspeq's per-chunk path (numpy +
-    scipy's OpenBLAS, all host threads) on a bounded sample of the workload."""
+    scipy's OpenBLAS, all host threads) on a bounded sample of the workload.
+    Resolution matrices are prepared by the restatement's own reader steps,
+    outside the timed work (the reference does it while reading files)."""
     from oracle import qmle_port as P
     s = P.Settings(max_forest_length=w.max_forest_length, cont_logl_order=w.cont_logl_order,
                    cont_l_order=w.cont_l_order)
     keys = w.table_index()
     tvs = {}
-    t0 = time.perf_counter()
+    work = 0.0
     done = 0
-    for lam, delta, ivar, r in chunks:
+    for i in (order if order is not None else range(len(chunks))):
+        lam, delta, ivar, r = chunks[i]
+        reso = rm = None
+        if w.reso:
+            reso = (w.oversample, w.deconv_m)
+            v = P.dia_deconvolve(np.array(w.spectra[i].resomat), w.deconv_m) if w.deconv_m > 0 \
+                else np.array(w.spectra[i].resomat)
+            rm = P.dia_oversample(v, w.oversample, P._median(np.diff(lam))) if w.oversample > 0 else v
+        t0 = time.perf_counter()
         try:
-            ch = P.make_chunk(lam, delta, ivar, r, w.bins, keys, s)
+            ch = P.make_chunk(lam, delta, ivar, 0 if w.reso else r, w.bins, keys, s, reso, rm)
         except (ValueError, KeyError):
             continue
         if ch.res_index not in tvs:
             tvs[ch.res_index] = P.table_view(w.tables[ch.res_index], w.bins, w.nv, w.lenv, w.nzp)
         P.chunk_iteration(ch, w.bins, tvs[ch.res_index], np.zeros(w.bins.nkz), s)
+        work += time.perf_counter() - t0
         done += 1
-        if time.perf_counter() - t0 > budget_s or (max_chunks and done >= max_chunks):
+        if work > budget_s or (max_chunks and done >= max_chunks):
             break
-    dt = time.perf_counter() - t0
-    return done / dt, done, dt
+    return done / work, done, work
 
 
 def run_reference(args, rank, world):
@@ -155,7 +202,7 @@ def run_reference(args, rank, world):
     rates, times, counts = [], [], []
     for step in range(args.warmup + args.steps):
         order = rng.permutation(len(chunks))
-        rate, done, dt = cpu_port_rate(w, [chunks[i] for i in order], budget_s=args.cpu_budget)
+        rate, done, dt = cpu_port_rate(w, chunks, budget_s=args.cpu_budget, order=order)
         if step >= args.warmup:
             rates.append(rate)
             times.append(dt)
@@ -167,7 +214,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times) * 1e3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded, DESI-like shapes)",
-        "config": {"workload": f"{args.workload}: 4096 chunks, N 200-1200, dv 50, 35 k x 13 z bins",
+        "config": {"workload": describe(w, len(w.spectra)),
                    "sample": f"{int(np.mean(counts))} random chunks per step (~{args.cpu_budget:.0f} s)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{int(np.mean(counts))} chunks/step of the {args.workload} workload"},
@@ -204,12 +251,15 @@ def main():
     build.build()
     seed = None if world == 1 else 20240602 + 7919 * rank
     w = synth.make_workload(args.workload, seed=seed, n_chunks=args.chunks)
-    chunks = chunk_arrays(w)
-    lam, delta, ivar, offs, rr = pack(chunks)
-    lam_p, delta_p, ivar_p = (torch.from_numpy(x).pin_memory().numpy() for x in (lam, delta, ivar))
+    chunks = chunk_arrays(w, lqg)
+    lam, delta, ivar, offs, rr = pack(chunks, w.reso)
+    pinned = tuple(torch.from_numpy(x).pin_memory().numpy() for x in (lam, delta, ivar))
+    if w.reso:
+        rr = torch.from_numpy(rr).pin_memory().numpy()
+    packed = pinned + (offs, rr)
     eng = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
                      cont=(w.cont_logl_order, w.cont_l_order), device=local)
-    st = eng.add_chunks(lam_p, delta_p, ivar_p, offs, rr)
+    st = add_packed(eng, w, packed)
     n_ok = int((st == 0).sum())
     infos = [eng.chunk_info(i) for i in range(eng.size)]
     ns_list = [(i["nq"] // w.bins.nk) * i["kbin_upp"] for i in infos]
@@ -230,7 +280,7 @@ def main():
 
     def step_e2e():
         eng.clear()
-        eng.add_chunks(lam_p, delta_p, ivar_p, offs, rr)
+        add_packed(eng, w, packed)
         return step_resident()
 
     def barrier():
@@ -274,7 +324,7 @@ def main():
     barrier()
     ms_e2e = e2.elapsed_time(e3) / args.steps
     e2e_value = n_ok * world / (ms_e2e / 1e3)
-    h2d = int(lam.nbytes + delta.nbytes + ivar.nbytes + 8 * nkz)
+    h2d = int(lam.nbytes + delta.nbytes + ivar.nbytes + 8 * nkz + (rr.nbytes if w.reso else 0))
     d2h = int(8 * (nkz * nkz + 3 * nkz))
 
     if rank != 0:
@@ -287,7 +337,10 @@ def main():
     sub = chunks[:args.fp64_chunks]
     e64 = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
                      cont=(w.cont_logl_order, w.cont_l_order), device=local)
-    e64.add_chunk_list(sub)
+    if w.reso:
+        e64.add_chunks_reso(*pack(sub, True)[:4], w.oversample, pack(sub, True)[4])
+    else:
+        e64.add_chunk_list(sub)
     e64.iterate(precision="fp64")
     t0 = time.perf_counter()
     e64.iterate(precision="fp64")
@@ -362,8 +415,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f16x3 products / df64 factorisation", "data": "synthetic (seeded)",
-        "config": {"workload": f"{args.workload}: {n_ok} chunks, N log-uniform 200-1200, dv 50 km/s, "
-                               "R 2000-5000, 35 k x 13 z bins, amplitude+slope marginalisation",
+        "config": {"workload": describe(w, n_ok),
                    "l2": "working set of tens of GB per iteration (>> 129 MB L2); no flush"},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -767,6 +767,17 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.sqiv = ctx->d_sqiv.as<double>(); base.niv = ctx->d_niv.as<double>();
     base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
     base.n_fpix = (int64_t) ctx->h_flogw.size();
+    base.reso_nelem = base.reso_os = 0;
+    {
+        int ne = -1, os = -1;
+        bool uniform = true;
+        for (const auto &h : ctx->chunks) {
+            if (h.nelem <= 0) continue;
+            if (ne < 0) { ne = h.nelem; os = h.os; }
+            uniform &= h.nelem == ne && h.os == os;
+        }
+        if (uniform && ne > 0) { base.reso_nelem = ne; base.reso_os = os; }
+    }
     base.n_rw = (int64_t) ctx->h_rw.size();
     base.deriv = ctx->d_deriv.as<double>();
     base.deriv_f = ctx->d_deriv_f.as<float>();

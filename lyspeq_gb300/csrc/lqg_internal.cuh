@@ -106,6 +106,7 @@ struct WaveArgs {
     const float2 *logw2, *sqw2;                      // ln w and sqrt w as double-float (hi, lo)
     const double *sqiv, *niv;                        // sqrt(ivar), and 1 / ivar (0 where ivar = 0)
     const double *flogw, *fsqw, *rw;                 // resolution-matrix grids and weights
+    int reso_nelem, reso_os;                         // shape shared by every resolution chunk, else 0
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
     const float2 *signal_ff;                         // signal table as double-float (mixed path)

@@ -506,7 +506,12 @@ struct ResoSharedF {
 // the sinc block is computed once per distinct dk.  Redshift weights in
 // double-float arithmetic (as the plain mixed build).  d partial rows: 16 per
 // 64 x 64 tile, 4 per quarter.
-__global__ void __launch_bounds__(RTH) k_build_q_reso_f32(WaveArgs a) {
+// NEL, OS > 0 fix the row width and oversampling of every chunk at compile
+// time: each thread then keeps the weights of two adjacent columns in
+// registers and forms both T entries of a row from one pass over the shared
+// slab (NEL + OS loads for 2 NEL multiply-adds instead of 4 NEL loads).
+template <int NEL, int OS>
+__global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     ResoSharedF &sm = *reinterpret_cast<ResoSharedF *>(smraw);
     __shared__ double red[RTH / 32];
@@ -523,7 +528,7 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso_f32(WaveArgs a) {
         for (int e = threadIdx.x; e < share * ch.ns; e += blockDim.x) dpart[e] = 0.0;
         return;
     }
-    const int os = ch.os, nel = ch.nelem, lf = (RT - 1) * os + nel;
+    const int os = NEL > 0 ? OS : ch.os, nel = NEL > 0 ? NEL : ch.nelem, lf = (RT - 1) * os + nel;
     const int r0 = I * RT * os - ch.sh, c0 = J * RT * os - ch.sh;
     for (int e = threadIdx.x; e < RT * nel; e += blockDim.x) {
         const int r = e / nel, k = e % nel;
@@ -531,6 +536,9 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso_f32(WaveArgs a) {
         sm.wi[r][k] = ri < n ? (float) a.rw[ch.rw_off + (int64_t) ri * nel + k] : 0.f;
         sm.wj[r][k] = rj < n ? (float) a.rw[ch.rw_off + (int64_t) rj * nel + k] : 0.f;
     }
+    // stage-1 thread layout of the fixed-width kernel: column pair jp, slab row fr1
+    const int jp = threadIdx.x % 16, fr1 = threadIdx.x / 16;
+    float w0[NEL > 0 ? NEL : 1], w1[NEL > 0 ? NEL : 1];
     for (int e = threadIdx.x; e < lf; e += blockDim.x) {
         const int pr = r0 + e, pc = c0 + e;
         const double lr = (pr >= 0 && pr < ch.nf) ? a.flogw[ch.fpix + pr] : 0.0;
@@ -541,6 +549,13 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso_f32(WaveArgs a) {
     for (int t = threadIdx.x; t < ch.ns; t += blockDim.x)
         sm.qscale[t] = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + t];
     __syncthreads();
+    if constexpr (NEL > 0) {
+#pragma unroll
+        for (int bb = 0; bb < NEL; ++bb) {
+            w0[bb] = sm.wj[2 * jp][bb];
+            w1[bb] = sm.wj[2 * jp + 1][bb];
+        }
+    }
     const DeviceBins &bins = *a.bins;
     const int j = threadIdx.x % 32, r8 = threadIdx.x / 32, gj = J * RT + j;
     const int nzb = ch.ns / ch.kbin_upp;
@@ -602,14 +617,29 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso_f32(WaveArgs a) {
                 fs[fr][fc] = coef * sm.sinc[s0 + fr][fc] * cs;
             }
             __syncthreads();
+            if constexpr (NEL > 0) {
+                if (fr1 < rows) {
+                    const float *frow = &fs[fr1][2 * jp * OS];
+                    float a0 = 0.f, a1 = 0.f;
 #pragma unroll
-            for (int u = 0; u < FSLAB / 8; ++u) {
-                const int fr = r8 + 8 * u;
-                if (fr < rows) {
-                    const float *frow = &fs[fr][j * os];
-                    float acc = 0.f;
-                    for (int bb = 0; bb < nel; ++bb) acc = fmaf(frow[bb], sm.wj[j][bb], acc);
-                    sm.t[s0 + fr][j] = acc;
+                    for (int bb = 0; bb < NEL + OS; ++bb) {
+                        const float fv = frow[bb];
+                        if (bb < NEL) a0 = fmaf(fv, w0[bb], a0);
+                        if (bb >= OS) a1 = fmaf(fv, w1[bb - OS], a1);
+                    }
+                    sm.t[s0 + fr1][2 * jp] = a0;
+                    sm.t[s0 + fr1][2 * jp + 1] = a1;
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < FSLAB / 8; ++u) {
+                    const int fr = r8 + 8 * u;
+                    if (fr < rows) {
+                        const float *frow = &fs[fr][j * os];
+                        float acc = 0.f;
+                        for (int bb = 0; bb < nel; ++bb) acc = fmaf(frow[bb], sm.wj[j][bb], acc);
+                        sm.t[s0 + fr][j] = acc;
+                    }
                 }
             }
             __syncthreads();
@@ -826,7 +856,11 @@ void set_reso_attrs() {
     const int bytes = (int) sizeof(ResoShared);
     cudaFuncSetAttribute(k_build_s_c_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_build_q_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_build_q_reso_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_build_q_reso_f32<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) sizeof(ResoSharedF));
+    cudaFuncSetAttribute(k_build_q_reso_f32<31, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) sizeof(ResoSharedF));
+    cudaFuncSetAttribute(k_build_q_reso_f32<11, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedF));
     cudaFuncSetAttribute(k_build_s_c_reso_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedFF));
@@ -851,7 +885,14 @@ void launch_build_q_reso(WaveArgs &a, cudaStream_t st) {
     const int nt = a.max_ld / RT;
     if (a.precision == LQG_PRECISION_MIXED) {
         k_reso_phases<<<dim3(32, a.n_chunks), 256, 0, st>>>(a);
-        k_build_q_reso_f32<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoSharedF), st>>>(a);
+        // a fixed-width kernel when every resolution chunk of the batch has its shape
+        const dim3 grid(nt * nt, a.n_chunks);
+        if (a.reso_nelem == 31 && a.reso_os == 3)
+            k_build_q_reso_f32<31, 3><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
+        else if (a.reso_nelem == 11 && a.reso_os == 1)
+            k_build_q_reso_f32<11, 1><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
+        else
+            k_build_q_reso_f32<0, 0><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
         a.launches += 2;
     } else {
         k_build_q_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);

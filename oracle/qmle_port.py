@@ -19,6 +19,7 @@ import dataclasses
 import math
 
 import numpy as np
+from scipy import sparse
 from scipy.linalg import lapack
 
 C_KMS = 299792.458
@@ -359,7 +360,8 @@ def make_chunk(wave, delta, ivar, r_fwhm, bins, table_keys, settings, reso=None,
     rmat = fine = None
     if reso is not None:
         osamp = reso[0]
-        rmat = resolution_dense(rm, osamp if osamp > 0 else None, n)
+        # sparse (banded) R: R M R^T costs O(n^2 nelem) as in the reference
+        rmat = sparse.csr_matrix(resolution_dense(rm, osamp if osamp > 0 else None, n))
         w0 = wave[0] / LYA_REST
         if osamp > 0:
             # Chunk::_initMatrices, core/chunk_estimate.cpp:927-938; dlambda is
@@ -516,12 +518,12 @@ def build_matrices(ch: ChunkData, bins, tv: TableView):
             m = np.empty((nf, nf))
             m[iuf] = val
             m = _sym_upper_fill(m)
-            q[kn] = _sym_upper_fill(r @ m @ r.T)
+            q[kn] = _sym_upper_fill(np.asarray((r @ m) @ r.T))
         m = np.empty((nf, nf))
         m[iuf] = interp2d(tv.signal.ravel(), nzp, tv.signal.shape[0], tv.z1, tv.dz, tv.v1, tv.dv,
                           zf, vf)
         m = _sym_upper_fill(m)
-        sm = _sym_upper_fill(r @ m @ r.T)
+        sm = _sym_upper_fill(np.asarray((r @ m) @ r.T))
     for s in range(ch.kbin_upp, ns):
         q[s] = q[stored[s] % bins.nk]
     zu = zmat[iu]
