@@ -507,9 +507,9 @@ struct ResoSharedF {
 // double-float arithmetic (as the plain mixed build).  d partial rows: 16 per
 // 64 x 64 tile, 4 per quarter.
 // NEL, OS > 0 fix the row width and oversampling of every chunk at compile
-// time: each thread then keeps the weights of two adjacent columns in
-// registers and forms both T entries of a row from one pass over the shared
-// slab (NEL + OS loads for 2 NEL multiply-adds instead of 4 NEL loads).
+// time: each thread then keeps its column's weights, scaled by the column
+// phases, in registers and reads the cached sinc block directly (no slab of
+// Q_k is formed, one barrier per band).
 template <int NEL, int OS>
 __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -536,9 +536,7 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
         sm.wi[r][k] = ri < n ? (float) a.rw[ch.rw_off + (int64_t) ri * nel + k] : 0.f;
         sm.wj[r][k] = rj < n ? (float) a.rw[ch.rw_off + (int64_t) rj * nel + k] : 0.f;
     }
-    // stage-1 thread layout of the fixed-width kernel: column pair jp, slab row fr1
-    const int jp = threadIdx.x % 16, fr1 = threadIdx.x / 16;
-    float w0[NEL > 0 ? NEL : 1], w1[NEL > 0 ? NEL : 1];
+
     for (int e = threadIdx.x; e < lf; e += blockDim.x) {
         const int pr = r0 + e, pc = c0 + e;
         const double lr = (pr >= 0 && pr < ch.nf) ? a.flogw[ch.fpix + pr] : 0.0;
@@ -549,13 +547,6 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     for (int t = threadIdx.x; t < ch.ns; t += blockDim.x)
         sm.qscale[t] = (float) a.scales[(size_t) 4 * a.n_chunks + ch.slot_q + t];
     __syncthreads();
-    if constexpr (NEL > 0) {
-#pragma unroll
-        for (int bb = 0; bb < NEL; ++bb) {
-            w0[bb] = sm.wj[2 * jp][bb];
-            w1[bb] = sm.wj[2 * jp + 1][bb];
-        }
-    }
     const DeviceBins &bins = *a.bins;
     const int j = threadIdx.x % 32, r8 = threadIdx.x / 32, gj = J * RT + j;
     const int nzb = ch.ns / ch.kbin_upp;
@@ -609,28 +600,38 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
             dk_cached = dkf;
         }
         __syncthreads();
-        for (int s0 = 0; s0 < lf; s0 += FSLAB) {
-            const int rows = min(FSLAB, lf - s0);
-            for (int e = threadIdx.x; e < rows * lf; e += RTH) {
-                const int fr = e / lf, fc = e % lf;
-                const float cs = fmaf(sm.cr[s0 + fr], sm.cc[fc], sm.sr[s0 + fr] * sm.sc[fc]);
-                fs[fr][fc] = coef * sm.sinc[s0 + fr][fc] * cs;
+        if constexpr (NEL > 0) {
+            // T[fr][j] = coef (C_fr X + S_fr Y) with X = sum_b sinc[fr][c] C_c w_jb and
+            // Y likewise with S_c (c = j OS + b): the row phase factors leave the
+            // sum, so the cached sinc block is read directly, one load per two FMAs
+            float wc[NEL], wsn[NEL];
+#pragma unroll
+            for (int bb = 0; bb < NEL; ++bb) {
+                const float w = sm.wj[j][bb];
+                wc[bb] = sm.cc[j * OS + bb] * w;
+                wsn[bb] = sm.sc[j * OS + bb] * w;
+            }
+            for (int fr = r8; fr < lf; fr += 8) {
+                const float *srow = &sm.sinc[fr][j * OS];
+                float x = 0.f, yv = 0.f;
+#pragma unroll
+                for (int bb = 0; bb < NEL; ++bb) {
+                    const float sv = srow[bb];
+                    x = fmaf(sv, wc[bb], x);
+                    yv = fmaf(sv, wsn[bb], yv);
+                }
+                sm.t[fr][j] = coef * fmaf(sm.cr[fr], x, sm.sr[fr] * yv);
             }
             __syncthreads();
-            if constexpr (NEL > 0) {
-                if (fr1 < rows) {
-                    const float *frow = &fs[fr1][2 * jp * OS];
-                    float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-                    for (int bb = 0; bb < NEL + OS; ++bb) {
-                        const float fv = frow[bb];
-                        if (bb < NEL) a0 = fmaf(fv, w0[bb], a0);
-                        if (bb >= OS) a1 = fmaf(fv, w1[bb - OS], a1);
-                    }
-                    sm.t[s0 + fr1][2 * jp] = a0;
-                    sm.t[s0 + fr1][2 * jp + 1] = a1;
+        } else {
+            for (int s0 = 0; s0 < lf; s0 += FSLAB) {
+                const int rows = min(FSLAB, lf - s0);
+                for (int e = threadIdx.x; e < rows * lf; e += RTH) {
+                    const int fr = e / lf, fc = e % lf;
+                    const float cs = fmaf(sm.cr[s0 + fr], sm.cc[fc], sm.sr[s0 + fr] * sm.sc[fc]);
+                    fs[fr][fc] = coef * sm.sinc[s0 + fr][fc] * cs;
                 }
-            } else {
+                __syncthreads();
 #pragma unroll
                 for (int u = 0; u < FSLAB / 8; ++u) {
                     const int fr = r8 + 8 * u;
@@ -641,8 +642,8 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
                         sm.t[s0 + fr][j] = acc;
                     }
                 }
+                __syncthreads();
             }
-            __syncthreads();
         }
         float b[4];
 #pragma unroll
