@@ -293,6 +293,7 @@ def main():
         step_resident()
     phase = np.zeros(8)
     launches = 0
+    waves = 1
     barrier()
     with ClockSampler(local) as clk:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -301,6 +302,7 @@ def main():
             step_resident()
             phase += eng.timings()
             launches += eng.launch_count()
+            waves = eng.wave_count()
         e1.record()
         barrier()
     ms = e0.elapsed_time(e1) / args.steps
@@ -379,7 +381,23 @@ def main():
     peaks = {}
     if os.path.exists(PEAKS_FILE):
         peaks = json.load(open(PEAKS_FILE))
-    if names[dom] == "factor":
+    if names[dom] == "build_q" and w.reso:
+        # the resolution-matrix Q build, FP32 pipe: algorithmic flops of R M R^T
+        # per stored band, half of the symmetric product (nelem n (nf + n))
+        ne = 2 * (w.spectra[0].resomat.shape[0] // 2) * max(w.oversample, 1) + 1
+        osm = max(w.oversample, 1)
+        n_a = np.asarray(n_list, dtype=np.float64)
+        kup = np.asarray([i["kbin_upp"] for i in infos], dtype=np.float64)
+        flops = float(np.sum(kup * 2.0 * ne * n_a * (n_a * osm + ne - 1 + n_a) / 2.0))
+        achieved = flops / (phase[2] / 1e3) / 1e12
+        props = torch.cuda.get_device_properties(local)
+        mhz = clk.summary().get("sm_max_mhz") or 2070.0
+        pk = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+        roof = {"kernel": "k_build_q_reso_f32", "bound": "fp32", "achieved": achieved, "peak": pk,
+                "unit": "TFLOP/s", "frac": achieved / pk, "traffic": None,
+                "peak_source": "nominal FP32 FMA rate at the sampled maximum SM clock "
+                               "(MEASURED_PEAKS.json has no FP32 figure)"}
+    elif names[dom] == "factor":
         achieved = fl["factor"] / (phase[1] / 1e3) / 1e12
         roof = {"kernel": "k_factor", "bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
                 "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
@@ -393,7 +411,7 @@ def main():
         # fp16 hi/lo) times the measured/algorithmic ratio, 1.14, of an ncu
         # capture of the same kernel on 64 chunks of this workload
         traffic = None
-        n_waves = (launches_per_iter - 3) // 6     # 2 phase-A launches, 6 per wave, 1 accumulation
+        n_waves = waves                            # one launch of the products kernel per wave
         if key == "products" and n_waves > 0:
             ld = np.ceil(np.asarray(n_list) / 64.0) * 64.0
             alg = float(np.sum((3.0 * (np.asarray(ns_list) + 1) - 1) * ld * ld * 4.0))

@@ -208,6 +208,9 @@ int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n);
 
 /* Number of kernel launches the last lqg_nr_iteration enqueued. */
 int lqg_last_launch_count(const lqg_ctx *ctx);
+/* Number of size-bucketed waves of the last iteration: each phase-B kernel
+ * (Q build, products, traces, reduction) is launched once per wave. */
+int lqg_last_wave_count(const lqg_ctx *ctx);
 
 /* Factorisation of one chunk's covariance without allocating: no counterpart
  * in the reference (there it is part of Chunk::setInvertCovarianceMatrix,

@@ -52,6 +52,7 @@ struct lqg_ctx {
     std::vector<int> last_status;
     double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int launches = 0;
+    int waves = 0;
     std::vector<cudaEvent_t> evpool;
 };
 
@@ -715,6 +716,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     ctx->last_status.assign(nb, LQG_CHUNK_OK);
     std::fill(ctx->timings, ctx->timings + 8, 0.0);
     ctx->launches = 0;
+    ctx->waves = 0;
 
     std::vector<GroupPlan> groups;
     std::vector<ChunkDesc> desc;
@@ -882,6 +884,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
             spans.push_back({w0 + 2, 4});
             spans.push_back({w0 + 3, 5});
             ctx->launches += b.launches;
+            ctx->waves++;
         }
     }
     const size_t eacc = nev++;
@@ -951,6 +954,8 @@ extern "C" int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n) {
 }
 
 extern "C" int lqg_last_launch_count(const lqg_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int lqg_last_wave_count(const lqg_ctx *ctx) { return ctx ? ctx->waves : 0; }
 
 extern "C" int lqg_fisher_solve_n(int n, const double *fisher_sum, const double *dbt, double *fisher,
                                   double *solver, double *inverse, double *weighted, double *theta,

@@ -514,7 +514,7 @@ template <int NEL, int OS>
 __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     ResoSharedF &sm = *reinterpret_cast<ResoSharedF *>(smraw);
-    __shared__ double red[RTH / 32];
+    __shared__ double red[4 * (RTH / 32)];
     const int c = blockIdx.y;
     const ChunkDesc &ch = a.chunks[c];
     if (ch.nelem <= 0 || a.status[ch.gidx] != LQG_CHUNK_OK) return;
@@ -571,7 +571,6 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     const size_t plane = (size_t) ld * ld;
     float dk_cached = -1.f;
     float (*fs)[RLF + 1] = reinterpret_cast<float (*)[RLF + 1]>(sm.fq);
-    float (*qt)[RT + 1] = reinterpret_cast<float (*)[RT + 1]>(sm.fq);
     for (int kn = 0; kn < ch.kbin_upp; ++kn) {
         const double k1 = bins.k_edges[kn], k2 = bins.k_edges[kn + 1];
         const float dkf = (float) (k2 - k1), coef = (float) ((k2 - k1) / kPi);
@@ -653,44 +652,60 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
             for (int aa = 0; aa < nel; ++aa) acc = fmaf(sm.wi[i][aa], sm.t[i * os + aa][j], acc);
             b[u] = acc;
         }
-        for (int iz = 0; iz < nzb; ++iz) {
-            const int s = iz * ch.kbin_upp + kn;
-            const float qs = sm.qscale[s];
-            __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
-            __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
-            float part = 0.f;
-            __syncthreads();   // qt (aliasing the slab) is free
+        // Output of the band for up to 4 redshift bins at a time: Q_s tiles through
+        // the T buffer (free once every thread holds its b) for the mirrored
+        // stores, one block reduction of the d partials per group.
+        float (*qts)[RT][RT + 1] = reinterpret_cast<float (*)[RT][RT + 1]>(&sm.t[0][0]);
+        static_assert(4 * RT * (RT + 1) <= RLF * (RT + 1), "T buffer too small for 4 output tiles");
+        for (int z0 = 0; z0 < nzb; z0 += 4) {
+            const int nzg = min(4, nzb - z0);
+            float part[4] = {0.f, 0.f, 0.f, 0.f};
+            __syncthreads();   // T (stage 2) or the previous group's tiles are no longer read
+            for (int g = 0; g < nzg; ++g) {
+                const int iz = z0 + g, s = iz * ch.kbin_upp + kn;
+                const float qs = sm.qscale[s];
+                __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
+                __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int i = r8 + 8 * u, gi = I * RT + i;
-                float w = 0.f;
-                if (valid[u]) w = iz < 4 ? zw[u][iz] : zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]);
-                const float q = b[u] * w;
-                part = fmaf(yy[u], q, part);
-                const float x = q * qs;
-                qt[i][j] = x;
-                const __half h = __float2half_rn(x);
-                qh[(size_t) gi * ld + gj] = h;
-                ql[(size_t) gi * ld + gj] = __float2half_rn(x - __half2float(h));
+                for (int u = 0; u < 4; ++u) {
+                    const int i = r8 + 8 * u, gi = I * RT + i;
+                    float w = 0.f;
+                    if (valid[u]) w = iz < 4 ? zw[u][iz] : zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]);
+                    const float q = b[u] * w;
+                    part[g] = fmaf(yy[u], q, part[g]);
+                    const float x = q * qs;
+                    qts[g][i][j] = x;
+                    const __half h = __float2half_rn(x);
+                    qh[(size_t) gi * ld + gj] = h;
+                    ql[(size_t) gi * ld + gj] = __float2half_rn(x - __half2float(h));
+                }
+            }
+            for (int g = 0; g < nzg; ++g) {
+                float v = part[g];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                if (threadIdx.x % 32 == 0) red[g * (RTH / 32) + threadIdx.x / 32] = (double) v;
             }
             __syncthreads();
             if (I != J) {
                 // mirror tile, row J*RT + r8 + 8u, column I*RT + j: element (j, r8 + 8u) of this tile
+                for (int g = 0; g < nzg; ++g) {
+                    const int s = (z0 + g) * ch.kbin_upp + kn;
+                    __half *qh = a.q_hi + (size_t) (ch.slot_q + s) * plane;
+                    __half *ql = a.q_lo + (size_t) (ch.slot_q + s) * plane;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int rr = J * RT + r8 + 8 * u, cc2 = I * RT + j;
-                    const float x = qt[j][r8 + 8 * u];
-                    const __half h = __float2half_rn(x);
-                    qh[(size_t) rr * ld + cc2] = h;
-                    ql[(size_t) rr * ld + cc2] = __float2half_rn(x - __half2float(h));
+                    for (int u = 0; u < 4; ++u) {
+                        const int rr = J * RT + r8 + 8 * u, cc2 = I * RT + j;
+                        const float x = qts[g][j][r8 + 8 * u];
+                        const __half h = __float2half_rn(x);
+                        qh[(size_t) rr * ld + cc2] = h;
+                        ql[(size_t) rr * ld + cc2] = __float2half_rn(x - __half2float(h));
+                    }
                 }
             }
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
-            if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = (double) part;
-            __syncthreads();
-            if (threadIdx.x == 0) {
+            if (threadIdx.x < nzg) {
+                const int g = threadIdx.x, s = (z0 + g) * ch.kbin_upp + kn;
                 double acc = 0.0;
-                for (int w = 0; w < RTH / 32; ++w) acc += red[w];
+                for (int w = 0; w < RTH / 32; ++w) acc += red[g * (RTH / 32) + w];
                 dpart[s] = mult * acc;
                 for (int r = 1; r < share; ++r) dpart[(size_t) r * ch.ns + s] = 0.0;
             }

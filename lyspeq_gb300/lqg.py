@@ -22,7 +22,7 @@ CHUNK_STATUS = {0: "ok", 1: "short", 2: "no_table", 3: "empty", 4: "out_of_range
 EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_error",
            "lqg_batch_add", "lqg_batch_clear", "lqg_batch_size", "lqg_chunk_info",
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
-           "lqg_last_timings", "lqg_last_launch_count", "lqg_batch_add_reso",
+           "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
            "lqg_resomat_deconvolve", "lqg_resomat_oversample"]
 
 
@@ -78,6 +78,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_fisher_solve.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, dp]
     lib.lqg_last_timings.argtypes = [vp, dp, C.c_int]
     lib.lqg_last_launch_count.argtypes = [vp]
+    lib.lqg_last_wave_count.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -247,6 +248,9 @@ class Engine:
 
     def launch_count(self):
         return self.lib.lqg_last_launch_count(self.h)
+
+    def wave_count(self):
+        return self.lib.lqg_last_wave_count(self.h)
 
 
 def resomat_deconvolve(values, m):
