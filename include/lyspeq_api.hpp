@@ -85,6 +85,9 @@ struct Specifics {
     int cont_l_order = -1;              // ContinuumLambdaMargOrder
     bool turn_off_sfid = false;         // TurnOffBaseline
     bool precomputed_fisher = false;    // PrecomputedFisher given
+    bool use_reso_matrix = false;       // UseResoMatrix
+    int oversampling = -1;              // OversampleRmat
+    double resomat_deconvolution_m = 0; // ResoMatDeconvolutionM
     double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
 };
 
@@ -93,6 +96,10 @@ struct Specifics {
 struct QSOSpectrum {
     std::vector<double> wave, delta, ivar;
     int r_fwhm = 0;
+    // resolution matrix (UseResoMatrix), DiaMatrix layout resomat[ndiags][n]:
+    // diagonal d holds offset ndiags / 2 - d, its entry of column c at [d][c]
+    std::vector<double> resomat;
+    int ndiags = 0;
 };
 
 class OneDQuadraticPowerEstimate;
@@ -223,9 +230,43 @@ public:
         for (int i = 0; i < nch; ++i) offs[i + 1] = offs[i] + (idx[i + 1] - idx[i]);
         std::vector<int> rr(nch, q.r_fwhm), st(nch, 0);
         const int before = lqg_batch_size(ctx_.get());
-        check(lqg_batch_add(ctx_.get(), nch, offs.data(), w.data() + a, d.data() + a, iv.data() + a, rr.data(),
-                            st.data()),
-              "lqg_batch_add");
+        if (sp_.use_reso_matrix) {
+            // Resolution matrix as OneQSOEstimate::_readQsoFile prepares it
+            // (core/one_qso_estimate.cpp:75-89): deconvolution and oversampling on
+            // the whole spectrum, then one row (or column of diagonals) per pixel
+            const int nd = q.ndiags;
+            if (nd < 1 || q.resomat.size() != (size_t) nd * n0)
+                throw std::invalid_argument("QSOSpectrum resomat must hold ndiags x n values");
+            std::vector<double> vals = q.resomat;
+            if (sp_.resomat_deconvolution_m > 0)
+                check(lqg_resomat_deconvolve((int) n0, nd, vals.data(), sp_.resomat_deconvolution_m),
+                      "lqg_resomat_deconvolve");
+            int nelem = nd;
+            std::vector<double> per_pixel;
+            if (sp_.oversampling > 0) {
+                nelem = 2 * (nd / 2) * sp_.oversampling + 1;
+                std::vector<double> dl(n0 - 1);
+                for (size_t i = 0; i + 1 < n0; ++i) dl[i] = q.wave[i + 1] - q.wave[i];
+                std::sort(dl.begin(), dl.end());
+                const size_t m = dl.size();
+                const double dlambda = (m % 2 == 0) ? (dl[m / 2 - 1] + dl[m / 2]) / 2 : dl[m / 2];
+                per_pixel.resize(n0 * nelem);
+                check(lqg_resomat_oversample((int) n0, nd, vals.data(), sp_.oversampling, dlambda,
+                                             per_pixel.data()),
+                      "lqg_resomat_oversample");
+            } else {
+                per_pixel.resize(n0 * nd);
+                for (size_t c = 0; c < n0; ++c)
+                    for (int k = 0; k < nd; ++k) per_pixel[c * nd + k] = vals[(size_t) k * n0 + c];
+            }
+            check(lqg_batch_add_reso(ctx_.get(), nch, offs.data(), w.data() + a, d.data() + a, iv.data() + a,
+                                     sp_.oversampling, nelem, per_pixel.data() + a * nelem, st.data()),
+                  "lqg_batch_add_reso");
+        } else {
+            check(lqg_batch_add(ctx_.get(), nch, offs.data(), w.data() + a, d.data() + a, iv.data() + a,
+                                rr.data(), st.data()),
+                  "lqg_batch_add");
+        }
         int next = before;
         for (int i = 0; i < nch; ++i) {
             if (st[i] != LQG_CHUNK_OK) {
