@@ -140,6 +140,9 @@ def add_packed(eng, w, packed):
 
 
 def describe(w, n_ok):
+    if w.name == "echelle":
+        return (f"echelle: {n_ok} chunks, N uniform-int 1000-4000, dv 2.5-5 km/s, R 30000-50000, "
+                "40 k x 6 z bins, no marginalisation")
     if w.reso:
         return (f"{w.name}: {n_ok} chunks, N log-uniform 150-1000, dv 50 km/s, 11-diagonal resolution "
                 f"matrices deconvolved and oversampled x{w.oversample}, 20 k x 3 z bins, no marginalisation")
