@@ -158,6 +158,25 @@ int lqg_batch_add_reso(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
 int lqg_resomat_deconvolve(int n, int ndiags, double *values, double m);
 int lqg_resomat_oversample(int n, int ndiags, const double *values, int osamp, double dlambda,
                            double *rows);
+/* SQ lookup tables on the GPU: SQLookupTable::computeTables
+ * (core/sq_table.cpp:201-323, CreateSQLookUpTable), for n_tables (R, dv)
+ * pairs on the grids lqg_tables describes (nv points over [0, v_length], nzp
+ * redshift points over [z_c0 - dz, z_c0 - dz + dz (nz + 1)]).
+ *   deriv  [n_tables][nk][nv]: Q_k(v) = (1/pi) int_{k1}^{k2} W^2(k) cos(k v) dk,
+ *          W(k) = sinc(k dv / 2) exp(-k^2 R^2 / 2), R = c / R_fwhm / 2.35482
+ *          (q_matrix_integrand, core/fiducial_cosmology.cpp:305-331), by
+ *          composite 8-point Gauss-Legendre quadrature on panels of width
+ *          <= 3 / v_length (the reference integrates with GSL QAWO);
+ *   signal [n_tables][nv][nzp] (z fastest), if with_signal: the reference's
+ *          own discretisation, the real inverse FFT of W^2 P_fid(k, z) on the
+ *          grid of RealField(2^(ceil(log2(4 nv)) + 1), dv_table / 2) sampled at
+ *          every second point (core/sq_table.cpp:222-228, 286-310).
+ * fid: the six PD13 parameters A, n, alpha, B, beta, lambda
+ * (core/fiducial_cosmology.cpp:268-282).  FP64; synchronous; allocates and
+ * frees its own device memory on `device`; host arrays in and out. */
+int lqg_tables_generate(const lqg_bins *bins, int n_tables, const int *r_fwhm, const double *dv,
+                        int nv, double v_length, int nzp, const double *fid, int with_signal,
+                        double *deriv, double *signal, int device);
 int lqg_batch_clear(lqg_ctx *ctx);
 int lqg_batch_size(const lqg_ctx *ctx);
 

@@ -23,7 +23,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_batch_add", "lqg_batch_clear", "lqg_batch_size", "lqg_chunk_info",
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
-           "lqg_resomat_deconvolve", "lqg_resomat_oversample"]
+           "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate"]
 
 
 class LqgBins(C.Structure):
@@ -69,6 +69,8 @@ def load_library(path: str = LIB_PATH):
                                        dp, ip]
     lib.lqg_resomat_deconvolve.argtypes = [C.c_int, C.c_int, dp, C.c_double]
     lib.lqg_resomat_oversample.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_double, dp]
+    lib.lqg_tables_generate.argtypes = [C.POINTER(LqgBins), C.c_int, ip, dp, C.c_int, C.c_double, C.c_int,
+                                        dp, C.c_int, dp, dp, C.c_int]
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
@@ -274,3 +276,24 @@ def resomat_oversample(values, osamp, dlambda):
     if rc != LQG_OK:
         raise RuntimeError(f"lqg_resomat_oversample failed with {rc}")
     return rows
+
+
+def generate_tables(bins, rd_pairs, nv, v_length, nzp, fid, with_signal=True, device=0):
+    """SQ lookup tables for (R, dv) pairs on the GPU (lqg_tables_generate).
+    Returns (deriv [n][nk][nv], signal [n][nv][nzp] or None)."""
+    lib = load_library()
+    k_edges = np.ascontiguousarray(bins.k_edges, dtype=np.float64)
+    zc = np.ascontiguousarray(bins.z_centers, dtype=np.float64)
+    b = LqgBins(bins.nk, bins.nz, _dptr(k_edges), _dptr(zc), bins.dz, 1 if bins.triangular else 0)
+    r = np.ascontiguousarray([p[0] for p in rd_pairs], dtype=np.int32)
+    dv = np.ascontiguousarray([p[1] for p in rd_pairs], dtype=np.float64)
+    n = len(rd_pairs)
+    deriv = np.zeros((n, bins.nk, nv))
+    signal = np.zeros((n, nv, nzp)) if with_signal else None
+    f = np.ascontiguousarray(fid, dtype=np.float64)
+    rc = lib.lqg_tables_generate(C.byref(b), n, _iptr(r), _dptr(dv), int(nv), float(v_length), int(nzp),
+                                 _dptr(f), int(bool(with_signal)), _dptr(deriv),
+                                 _dptr(signal) if with_signal else None, int(device))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_tables_generate failed with {rc}")
+    return deriv, signal
