@@ -225,6 +225,24 @@ int lqg_fisher_solve(lqg_ctx *ctx, const double *fisher_sum, const double *dbt,
  * [6] global accumulation, [7] whole iteration.  Returns the number written. */
 int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n);
 
+/* Poisson bootstrap over spectra after an iteration, lyspeq's FastBootstrap
+ * (PoissonBootstrapper::_fastBootstrap and _meanBootstrap, core/bootstrapper.hpp,
+ * with OneQSOEstimate::collapseBootstrap, core/one_qso_estimate.cpp:200-238).
+ * The spectra are consecutive ranges of the batch's chunks: spectrum q owns
+ * batch chunks [qso_offsets[q], qso_offsets[q+1]) (ranges may be empty, for a
+ * spectrum all of whose chunks were rejected; it still takes its draws).
+ * theta_q = sum of its chunks' d - b - t from the last lqg_nr_iteration;
+ * realization x_b = sum_q p_qb theta_q with p_qb ~ Poisson(1) drawn on the host
+ * by std::mt19937_64 seeded with `seed` (the reference seeds with the MPI rank)
+ * and std::poisson_distribution, nboots draws per spectrum in order.
+ * Out (any may be NULL): mean [nkz] of the realizations (not normalised, as
+ * the reference writes it), fisher_cov [nkz^2] = covariance / 4, cov [nkz^2] =
+ * F^-1 (covariance / 4) F^-T with F^-1 = solver_invfisher (the solver matrix of
+ * lqg_fisher_solve; required for cov), realizations [nboots][nkz].  FP64 on
+ * the device; synchronous. */
+int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
+                  const double *solver_invfisher, double *mean, double *cov, double *fisher_cov,
+                  double *realizations);
 /* Number of kernel launches the last lqg_nr_iteration enqueued. */
 int lqg_last_launch_count(const lqg_ctx *ctx);
 /* Number of size-bucketed waves of the last iteration: each phase-B kernel

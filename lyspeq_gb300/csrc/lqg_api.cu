@@ -53,6 +53,7 @@ struct lqg_ctx {
     double timings[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int launches = 0;
     int waves = 0;
+    bool have_results = false;   // an iteration has run on the current batch
     std::vector<cudaEvent_t> evpool;
 };
 
@@ -238,6 +239,7 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
     ctx->h_sqiv.clear(); ctx->h_niv.clear();
     ctx->h_flogw.clear(); ctx->h_fsqw.clear(); ctx->h_rw.clear();
     ctx->has_reso = false;
+    ctx->have_results = false;
     ctx->results_size = 0;
     ctx->pix_dirty = true;
     return LQG_OK;
@@ -398,6 +400,7 @@ int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double 
         ctx->chunks.push_back(hc);
     }
     ctx->pix_dirty = true;
+    ctx->have_results = false;
     return LQG_OK;
 }
 
@@ -915,6 +918,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     cudaEventElapsedTime(&tt, ev_start, ev_end);
     ctx->timings[6] = ta;
     ctx->timings[7] = tt;
+    ctx->have_results = true;
     return LQG_OK;
 }
 
@@ -954,6 +958,25 @@ extern "C" int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n) {
 }
 
 extern "C" int lqg_last_launch_count(const lqg_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+namespace lqg {
+int run_fast_bootstrap(cudaStream_t st, const ChunkDesc *d_meta, const double *d_results, int nkz, int n_chunks,
+                       int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
+                       const double *solver, double *mean, double *cov, double *fisher_cov, double *realizations,
+                       std::string &err);
+}
+
+extern "C" int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
+                             const double *solver_invfisher, double *mean, double *cov, double *fisher_cov,
+                             double *realizations) {
+    if (!ctx || n_qso < 0 || !qso_offsets || nboots < 2)
+        return set_err(ctx, LQG_ERR_ARG, "lqg_bootstrap: bad arguments");
+    if (!ctx->have_results) return set_err(ctx, LQG_ERR_STATE, "lqg_bootstrap: no iteration on this batch yet");
+    cudaSetDevice(ctx->device);
+    return lqg::run_fast_bootstrap(ctx->stream, ctx->d_meta.as<ChunkDesc>(), ctx->d_results.as<double>(), ctx->nkz,
+                                   (int) ctx->chunks.size(), n_qso, qso_offsets, nboots, seed, solver_invfisher,
+                                   mean, cov, fisher_cov, realizations, ctx->err);
+}
 
 extern "C" int lqg_last_wave_count(const lqg_ctx *ctx) { return ctx ? ctx->waves : 0; }
 

@@ -23,7 +23,8 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_batch_add", "lqg_batch_clear", "lqg_batch_size", "lqg_chunk_info",
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
-           "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate"]
+           "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate",
+           "lqg_bootstrap"]
 
 
 class LqgBins(C.Structure):
@@ -71,6 +72,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_resomat_oversample.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_double, dp]
     lib.lqg_tables_generate.argtypes = [C.POINTER(LqgBins), C.c_int, ip, dp, C.c_int, C.c_double, C.c_int,
                                         dp, C.c_int, dp, dp, C.c_int]
+    lib.lqg_bootstrap.argtypes = [vp, C.c_int, ip, C.c_int, C.c_ulonglong, dp, dp, dp, dp, dp]
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
@@ -190,6 +192,22 @@ class Engine:
         cat = lambda j: np.concatenate([np.asarray(c[j], dtype=np.float64) for c in chunks])
         per_pixel = [np.asarray(c[3]) if oversampling > 0 else np.asarray(c[3]).T for c in chunks]
         return self.add_chunks_reso(cat(0), cat(1), cat(2), offs, oversampling, np.concatenate(per_pixel))
+
+    def bootstrap(self, qso_offsets, nboots, seed=0, solver=None, realizations=False):
+        """FastBootstrap over spectra (lqg_bootstrap): returns mean, fisher_cov
+        (covariance / 4), cov (sandwiched with solver, if given) and optionally
+        the realizations."""
+        off = np.ascontiguousarray(qso_offsets, dtype=np.int32)
+        nkz = self.nkz
+        mean = np.zeros(nkz)
+        fcov = np.zeros((nkz, nkz))
+        cov = np.zeros((nkz, nkz)) if solver is not None else None
+        real = np.zeros((nboots, nkz)) if realizations else None
+        sv = None if solver is None else np.ascontiguousarray(solver, dtype=np.float64)
+        rc = self.lib.lqg_bootstrap(self.h, len(off) - 1, _iptr(off), int(nboots), int(seed), _dptr(sv),
+                                    _dptr(mean), _dptr(cov), _dptr(fcov), _dptr(real))
+        self._check(rc, "lqg_bootstrap")
+        return dict(mean=mean, fisher_cov=fcov, cov=cov, realizations=real)
 
     def clear(self):
         self._check(self.lib.lqg_batch_clear(self.h), "lqg_batch_clear")

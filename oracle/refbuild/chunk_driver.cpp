@@ -24,9 +24,19 @@
 // OversampleRmat and ResoMatDeconvolutionM keys apply;
 // specifics::USE_RESOLUTION_MATRIX is switched on after the config is read.
 //
-// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso]
+// With --boot N the driver then runs lyspeq's Poisson bootstrap over the
+// spectra (PoissonBootstrapper, core/bootstrapper.hpp, after
+// OneQSOEstimate::collapseBootstrap, as core/quadratic_estimate.cpp:536-545
+// does) and dumps its mean, covariance and realizations at full precision.
+// The bootstrapper keeps them in private members and writes them to text
+// files with 7 digits only, so this one translation unit opens the class's
+// private members when it includes the header (the header itself is used
+// unmodified).
+//
+// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso] [--boot N]
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -43,6 +53,9 @@
 #include "io/logger.hpp"
 #include "mathtools/matrix_helper.hpp"
 #include "mathtools/smoother.hpp"
+#define private public
+#include "core/bootstrapper.hpp"
+#undef private
 
 namespace {
 void putI(FILE *f, int v) { std::fwrite(&v, sizeof v, 1, f); }
@@ -100,9 +113,11 @@ int main(int argc, char *argv[]) {
         return 2;
     }
     bool dump_pixels = true, reso = false;
+    int nboots = 0;
     for (int a = 3; a < argc; ++a) {
         if (std::strcmp(argv[a], "--no-pixels") == 0) dump_pixels = false;
         else if (std::strcmp(argv[a], "--reso") == 0) reso = true;
+        else if (std::strcmp(argv[a], "--boot") == 0 && a + 1 < argc) nboots = std::atoi(argv[++a]);
     }
 
     ConfigFile config;
@@ -246,6 +261,19 @@ int main(int argc, char *argv[]) {
     putD(out, pfid.data(), nkz);
     putD(out, &t_chunks, 1);
     putD(out, &t_global, 1);
+    if (nboots > 0) {
+        // core/quadratic_estimate.cpp:536-545 with FastBootstrap (the default)
+        specifics::FAST_BOOTSTRAP = true;
+        PoissonBootstrapper pbooter(nboots, solver.get());
+        for (auto &q : qsos) q->collapseBootstrap();
+        pbooter.run(qsos);
+        std::fwrite("BOOT0001", 1, 8, out);
+        putI(out, nboots);
+        putI(out, (int) qsos.size());
+        putD(out, pbooter.temppower.get(), nkz);                         // mean of the realizations
+        putD(out, pbooter.tempfisher.get(), (size_t) nkz * nkz);         // F^-1 (cov / 4) F^-T
+        putD(out, pbooter.allpowers.get(), (size_t) nboots * nkz);       // realizations
+    }
     std::fclose(out);
 
     glmemory::dealloc();

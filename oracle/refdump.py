@@ -61,6 +61,10 @@ class RefDump:
     pfid: np.ndarray
     t_chunks: float
     t_global: float
+    boot_mean: np.ndarray | None = None        # FastBootstrap: mean of the realizations
+    boot_cov: np.ndarray | None = None         # F^-1 (cov / 4) F^-T
+    boot_real: np.ndarray | None = None        # realizations [nboots][nkz]
+    n_qso: int = 0
 
 
 class _Reader:
@@ -117,8 +121,16 @@ def read_dump(path: str) -> RefDump:
     damp = float(r.d(1)[0])
     pfid = r.d(nkz)
     t_chunks, t_global = float(r.d(1)[0]), float(r.d(1)[0])
-    return RefDump(nkz, nk, nz, chunks, fisher, dbt, solver, invf, theta, damped, dof, damp,
+    dump = RefDump(nkz, nk, nz, chunks, fisher, dbt, solver, invf, theta, damped, dof, damp,
                    pfid, t_chunks, t_global)
+    if r.pos < len(r.buf):
+        r.magic(b"BOOT0001")
+        nb, nq = r.i(), r.i()
+        dump.n_qso = nq
+        dump.boot_mean = r.d(nkz)
+        dump.boot_cov = r.d(nkz * nkz).reshape(nkz, nkz)
+        dump.boot_real = r.d(nb * nkz).reshape(nb, nkz)
+    return dump
 
 
 def available() -> bool:
@@ -126,14 +138,15 @@ def available() -> bool:
 
 
 def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None,
-               reso: bool = False) -> RefDump:
+               reso: bool = False, boots: int = 0) -> RefDump:
     env = dict(os.environ)
     env.setdefault("OPENBLAS_NUM_THREADS", "1")
     # One OpenMP thread: with more, Chunk::_applyRedshiftInterp races on the
     # shared `low`/`tmp` bounds (core/chunk_estimate.cpp:486, 512-516) and the
     # redshift weights of some rows come out wrong from run to run.
     env["OMP_NUM_THREADS"] = str(threads or 1)
-    args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else [])
+    args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else []) \
+        + (["--boot", str(boots)] if boots else [])
     subprocess.run(args, check=True, env=env, stdout=subprocess.DEVNULL,
                    stderr=subprocess.DEVNULL)
     return read_dump(out)

@@ -40,6 +40,8 @@ CASES = {
     "desi_sub": ("desi", 6, (1, -1), 0.0, None),
     "tiny_reso": ("tiny_reso", None, (-1, -1), 0.0, None),
     "tiny_reso_dia": ("tiny_reso_dia", None, (-1, -1), 0.0, None),
+    # lyspeq's FastBootstrap (200 realizations) after the iteration of tiny_marg1
+    "tiny_boot": ("tiny", None, (1, -1), 0.0, None, 200),
 }
 
 
@@ -55,13 +57,14 @@ def _mask(w, frac, seed):
 
 
 def make_case(name, spec):
-    wl, nch, marg, mask, keep = spec
+    wl, nch, marg, mask, keep = spec[:5]
+    boots = spec[5] if len(spec) > 5 else 0
     w = synth.make_workload(wl, n_chunks=nch)
     w.cont_logl_order, w.cont_l_order = marg
     _mask(w, mask, 99)
     with tempfile.TemporaryDirectory() as tmp:
         cfg = synth.write_reference_inputs(w, tmp)
-        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso)
+        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso, boots=boots)
     chunks = dump.chunks
     if keep is not None:
         chunks = chunks[:keep]
@@ -78,6 +81,12 @@ def make_case(name, spec):
         g_inverse=dump.inverse_fisher, g_damped=np.array(dump.damped),
         g_complete=np.array(keep is None),
     )
+    if boots:
+        out["boot_mean"] = dump.boot_mean
+        out["boot_cov"] = dump.boot_cov
+        out["boot_real"] = dump.boot_real
+        out["boot_qso"] = np.array([c.qso for c in chunks], dtype=np.int32)
+        out["boot_nqso"] = np.array(dump.n_qso)
     if w.reso:
         # resolution-matrix case: the reader's options, every spectrum's raw
         # matrix and wavelengths (for the preprocessing parity) and, per chunk,

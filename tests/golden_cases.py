@@ -33,6 +33,7 @@ class GoldenCase:
     # resolution-matrix cases: (oversampling, deconvolution m), per chunk the
     # matrix as the reference's chunk holds it and (spectrum, first pixel),
     # per spectrum (lambda, raw DiaMatrix values)
+    boot: dict | None = None   # FastBootstrap: mean, cov, realizations, qso of each chunk, n_qso
     reso: tuple | None = None
     rmats: list | None = None
     src: list | None = None
@@ -65,6 +66,9 @@ def load(name: str) -> GoldenCase:
     g = {k[2:]: z[k] for k in z.files if k.startswith("g_")}
     case = GoldenCase(name, bins, tables, nv, float(lenv), nzp, float(mfl), (int(m0), int(m1)),
                       chunks, meta, dbt, fis, g, bool(z["g_complete"]))
+    if "boot_mean" in z.files:
+        case.boot = dict(mean=z["boot_mean"], cov=z["boot_cov"], real=z["boot_real"],
+                         qso=z["boot_qso"], n_qso=int(z["boot_nqso"]))
     if "reso" in z.files:
         case.reso = (int(z["reso"][0]), float(z["reso"][1]))
         case.rmats = [z[f"c{i}_rmat"] for i in range(n)]
