@@ -33,7 +33,13 @@
 // private members when it includes the header (the header itself is used
 // unmodified).
 //
-// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso] [--boot N]
+// With --iterate the driver finally runs lyspeq's whole Newton-Raphson loop,
+// OneDQuadraticPowerEstimate::iterate() (core/quadratic_estimate.cpp:398-546:
+// NumberOfIterations iterations with convergence tests and the smoothing of
+// the estimate by the smbivspline.py script between them; the script must be
+// on PATH), and dumps the estimator's final state.
+//
+// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso] [--boot N] [--iterate]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -53,8 +59,13 @@
 #include "io/logger.hpp"
 #include "mathtools/matrix_helper.hpp"
 #include "mathtools/smoother.hpp"
+#include <algorithm>
+#include <random>
 #define private public
+#define protected public
 #include "core/bootstrapper.hpp"
+#include "core/quadratic_estimate.hpp"
+#undef protected
 #undef private
 
 namespace {
@@ -114,7 +125,9 @@ int main(int argc, char *argv[]) {
     }
     bool dump_pixels = true, reso = false;
     int nboots = 0;
+    bool nr_loop = false;
     for (int a = 3; a < argc; ++a) {
+        if (std::strcmp(argv[a], "--iterate") == 0) { nr_loop = true; continue; }
         if (std::strcmp(argv[a], "--no-pixels") == 0) dump_pixels = false;
         else if (std::strcmp(argv[a], "--reso") == 0) reso = true;
         else if (std::strcmp(argv[a], "--boot") == 0 && a + 1 < argc) nboots = std::atoi(argv[++a]);
@@ -275,8 +288,24 @@ int main(int argc, char *argv[]) {
         putD(out, pbooter.allpowers.get(), (size_t) nboots * nkz);       // realizations
     }
     std::fclose(out);
-
     glmemory::dealloc();
+    if (nr_loop) {
+        // LyaPowerEstimate.cpp:109-125 on the set-up above
+        OneDQuadraticPowerEstimate qps(config);
+        qps.iterate();
+        FILE *o2 = std::fopen((std::string(argv[2]) + ".iter").c_str(), "wb");
+        if (!o2) { std::perror("fopen"); return 1; }
+        std::fwrite("ITER0001", 1, 8, o2);
+        putI(o2, nkz);
+        putD(o2, qps.current_power_estimate_vector.get(), nkz);
+        putD(o2, qps.previous_power_estimate_vector.get(), nkz);
+        putD(o2, qps.powerspectra_fits.get(), nkz);
+        putD(o2, qps.fisher_matrix_sum.get(), (size_t) nkz * nkz);
+        putD(o2, qps.inverse_fisher_matrix_sum.get(), (size_t) nkz * nkz);
+        for (int i = 0; i < 3; ++i) putD(o2, qps.dbt_estimate_sum_before_fisher_vector[i].get(), nkz);
+        std::fclose(o2);
+    }
+
     std::printf("chunks=%d t_chunks=%.6f s t_global=%.6f s damped=%d\n", nchunks_total, t_chunks,
                 t_global, warn);
     return 0;

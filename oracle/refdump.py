@@ -13,6 +13,7 @@ from __future__ import annotations
 import dataclasses
 import os
 import subprocess
+import sys
 
 import numpy as np
 
@@ -20,6 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 DRIVER = os.path.join(REF_DIR, "chunk_driver")
 LYAPOWER = os.path.join(REF_DIR, "LyaPowerEstimate")
+REFERENCE_PY = "/root/reference/py"      # lyspeq's own helper scripts (smoothing)
 
 
 @dataclasses.dataclass
@@ -137,8 +139,31 @@ def available() -> bool:
     return os.path.exists(DRIVER)
 
 
+@dataclasses.dataclass
+class RefIteration:
+    """Final state of lyspeq's OneDQuadraticPowerEstimate after iterate()."""
+    theta: np.ndarray            # current_power_estimate_vector
+    previous: np.ndarray         # previous_power_estimate_vector
+    fits: np.ndarray             # powerspectra_fits (smoothed theta fed to the last iteration)
+    fisher: np.ndarray           # fisher_matrix_sum, halved and symmetric
+    inverse: np.ndarray          # inverse_fisher_matrix_sum
+    dbt: np.ndarray              # 3 x nkz
+
+
+def read_iteration(path: str) -> RefIteration:
+    with open(path, "rb") as f:
+        r = _Reader(f.read())
+    r.magic(b"ITER0001")
+    nkz = r.i()
+    th, prev, fits = r.d(nkz), r.d(nkz), r.d(nkz)
+    fm = r.d(nkz * nkz).reshape(nkz, nkz)
+    inv = r.d(nkz * nkz).reshape(nkz, nkz)
+    dbt = np.stack([r.d(nkz) for _ in range(3)])
+    return RefIteration(th, prev, fits, fm, inv, dbt)
+
+
 def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None,
-               reso: bool = False, boots: int = 0) -> RefDump:
+               reso: bool = False, boots: int = 0, iterate: bool = False) -> RefDump:
     env = dict(os.environ)
     env.setdefault("OPENBLAS_NUM_THREADS", "1")
     # One OpenMP thread: with more, Chunk::_applyRedshiftInterp races on the
@@ -146,7 +171,16 @@ def run_driver(config: str, out: str, pixels: bool = True, threads: int | None =
     # redshift weights of some rows come out wrong from run to run.
     env["OMP_NUM_THREADS"] = str(threads or 1)
     args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else []) \
-        + (["--boot", str(boots)] if boots else [])
+        + (["--boot", str(boots)] if boots else []) + (["--iterate"] if iterate else [])
+    if iterate:
+        # lyspeq's smoothing step runs its script smbivspline.py from PATH
+        wrap = os.path.join(os.path.dirname(os.path.abspath(out)), "bin")
+        os.makedirs(wrap, exist_ok=True)
+        script = os.path.join(wrap, "smbivspline.py")
+        with open(script, "w") as f:
+            f.write(f"#!/bin/sh\nexec {sys.executable} {REFERENCE_PY}/smbivspline.py \"$@\"\n")
+        os.chmod(script, 0o755)
+        env["PATH"] = wrap + os.pathsep + env.get("PATH", "")
     subprocess.run(args, check=True, env=env, stdout=subprocess.DEVNULL,
                    stderr=subprocess.DEVNULL)
     return read_dump(out)

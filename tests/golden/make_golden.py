@@ -42,6 +42,8 @@ CASES = {
     "tiny_reso_dia": ("tiny_reso_dia", None, (-1, -1), 0.0, None),
     # lyspeq's FastBootstrap (200 realizations) after the iteration of tiny_marg1
     "tiny_boot": ("tiny", None, (1, -1), 0.0, None, 200),
+    # lyspeq's full Newton-Raphson loop (NumberOfIterations 4, smoothing between)
+    "tiny_iter": ("tiny", None, (1, -1), 0.0, None, 0, 4),
 }
 
 
@@ -59,12 +61,18 @@ def _mask(w, frac, seed):
 def make_case(name, spec):
     wl, nch, marg, mask, keep = spec[:5]
     boots = spec[5] if len(spec) > 5 else 0
+    iters = spec[6] if len(spec) > 6 else 1
     w = synth.make_workload(wl, n_chunks=nch)
     w.cont_logl_order, w.cont_l_order = marg
     _mask(w, mask, 99)
     with tempfile.TemporaryDirectory() as tmp:
         cfg = synth.write_reference_inputs(w, tmp)
-        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso, boots=boots)
+        if iters > 1:
+            text = open(cfg).read().replace("NumberOfIterations 1", f"NumberOfIterations {iters}")
+            open(cfg, "w").write(text)
+        dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso, boots=boots,
+                                  iterate=iters > 1)
+        it = refdump.read_iteration(os.path.join(tmp, "dump.bin.iter")) if iters > 1 else None
     chunks = dump.chunks
     if keep is not None:
         chunks = chunks[:keep]
@@ -81,6 +89,10 @@ def make_case(name, spec):
         g_inverse=dump.inverse_fisher, g_damped=np.array(dump.damped),
         g_complete=np.array(keep is None),
     )
+    if it is not None:
+        out["it_n"] = np.array(iters)
+        out["it_theta"], out["it_prev"], out["it_fits"] = it.theta, it.previous, it.fits
+        out["it_fisher"], out["it_inverse"], out["it_dbt"] = it.fisher, it.inverse, it.dbt
     if boots:
         out["boot_mean"] = dump.boot_mean
         out["boot_cov"] = dump.boot_cov

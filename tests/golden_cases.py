@@ -34,6 +34,7 @@ class GoldenCase:
     # matrix as the reference's chunk holds it and (spectrum, first pixel),
     # per spectrum (lambda, raw DiaMatrix values)
     boot: dict | None = None   # FastBootstrap: mean, cov, realizations, qso of each chunk, n_qso
+    nr: dict | None = None     # full NR loop: iterations and the estimator's final state
     reso: tuple | None = None
     rmats: list | None = None
     src: list | None = None
@@ -66,6 +67,9 @@ def load(name: str) -> GoldenCase:
     g = {k[2:]: z[k] for k in z.files if k.startswith("g_")}
     case = GoldenCase(name, bins, tables, nv, float(lenv), nzp, float(mfl), (int(m0), int(m1)),
                       chunks, meta, dbt, fis, g, bool(z["g_complete"]))
+    if "it_n" in z.files:
+        case.nr = dict(n=int(z["it_n"]), theta=z["it_theta"], previous=z["it_prev"], fits=z["it_fits"],
+                       fisher=z["it_fisher"], inverse=z["it_inverse"], dbt=z["it_dbt"])
     if "boot_mean" in z.files:
         case.boot = dict(mean=z["boot_mean"], cov=z["boot_cov"], real=z["boot_real"],
                          qso=z["boot_qso"], n_qso=int(z["boot_nqso"]))
