@@ -224,15 +224,16 @@ constexpr int R_SMEM = R_STAGES * R_STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 320;             // producer, MMA, 8 epilogue warps
 constexpr int R_THREADS = TC_THREADS;
 constexpr int kGramK = 32768;               // K elements per Gram split
-constexpr int kGemmDrain = 4;               // K blocks per drained hi*hi partial: products
+constexpr int kGemmDrain = 8;               // K blocks per drained hi*hi partial: products
 constexpr int kGramDrain = 2;               // and traces
 
 // Accumulation: the tensor cores round every fp32 accumulation of an MMA, with a
 // bias that grows with the number of accumulations into one accumulator.  The
 // hi*hi products and the (2^11 times smaller) cross products therefore go to
 // separate TMEM accumulators, and the hi*hi accumulator is drained every DRAIN
-// K blocks (8 MMAs of K = 16) into fp32 sums held in registers: a ping-pong pair
-// of hi*hi accumulators lets the MMAs continue while one is drained.
+// K blocks (4 DRAIN MMAs of K = 16: 32 in the products, 8 in the traces) into
+// fp32 sums held in registers: a ping-pong pair of hi*hi accumulators lets the
+// MMAs continue while one is drained.
 //
 // TMEM columns: hi*hi ping [0, 128), pong [128, 256), cross [256, 384).
 // Epilogue warps 2..9: warp w reads TMEM lanes 32 (w % 4) .. +31 and the 64
