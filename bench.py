@@ -411,14 +411,14 @@ def main():
         pk = peaks.get("bf16_tflops", 1900.0)
         # DRAM traffic per launch of the products kernel (one launch per wave):
         # algorithmic bytes (Q_s read, A_s written to R and transposed to P,
-        # fp16 hi/lo) times the measured/algorithmic ratio, 1.14, of an ncu
+        # fp16 hi/lo) times the measured/algorithmic ratio, 0.99, of an ncu
         # capture of the same kernel on 64 chunks of this workload
         traffic = None
         n_waves = waves                            # one launch of the products kernel per wave
         if key == "products" and n_waves > 0:
             ld = np.ceil(np.asarray(n_list) / 64.0) * 64.0
             alg = float(np.sum((3.0 * (np.asarray(ns_list) + 1) - 1) * ld * ld * 4.0))
-            traffic = 1.14 * alg / n_waves
+            traffic = 0.99 * alg / n_waves
         roof = {"kernel": "k_tc_gemm" if key == "products" else "k_tc_gram", "bound": "tensor",
                 "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
                 "traffic": traffic, "traffic_unit": "bytes per launch",
