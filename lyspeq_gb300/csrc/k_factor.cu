@@ -678,12 +678,15 @@ __global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
     double *scratch = reinterpret_cast<double *>(a.fws + ch.o_fscr);
     const double *iv = a.ivar + ch.pix;
     if (DF) {
-        // C~ to df64 in place (the pair occupies the double's 8 bytes)
-        for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
-            const double v = A[e];
-            reinterpret_cast<float2 *>(A)[e] = to_df(v);
+        // C~ to df64 in place (the pair occupies the double's 8 bytes), unless
+        // the matrix build already wrote it in that form
+        if (!a.c_is_ff) {
+            for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
+                const double v = A[e];
+                reinterpret_cast<float2 *>(A)[e] = to_df(v);
+            }
+            __syncthreads();
         }
-        __syncthreads();
         float2 *A2 = reinterpret_cast<float2 *>(A);
         if (!potrf_df(A2, ld, nb, s)) {
             if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_NOT_SPD;

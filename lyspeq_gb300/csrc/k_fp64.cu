@@ -154,6 +154,56 @@ __global__ void k_build_s_c(WaveArgs a) {
     }
 }
 
+// Phase A, mixed path without theta: S and C~ = D S D + I in double-float
+// arithmetic on the FP32 pipe (48 significant bits; FP64 is 1/60 of the FP32
+// rate here), written as (hi, lo) float pairs in the 8 bytes of each element,
+// the form the mixed factorisation works in.  v_ij / dv, (z_ij - z1) / dz, the
+// interpolation fractions and the table values are all double-float.
+__global__ void k_build_s_c_ff(WaveArgs a) {
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    const int ld = ch.ld, n = ch.n, tpr = ld / T64;
+    if ((int) blockIdx.x >= tpr * tpr || ch.nelem > 0) return;
+    const int ti = blockIdx.x / tpr, tj = blockIdx.x % tpr;
+    float2 *S = reinterpret_cast<float2 *>(a.fws + ch.o_s), *C = reinterpret_cast<float2 *>(a.fws + ch.o_c);
+    const float2 *lw = a.logw2 + ch.pix, *sw = a.sqw2 + ch.pix, *sq = a.sqiv2 + ch.pix;
+    const TableGrid &gr = a.grid;
+    const float2 *tab = (a.signal_ff && !a.turn_off_sfid) ? a.signal_ff + (size_t) ch.res * gr.nv * gr.nzp : nullptr;
+    const float2 kv = make_float2(gr.kv_hi, gr.kv_lo), z1p = make_float2(gr.z1p_hi, gr.z1p_lo);
+    const float2 idz = make_float2(gr.idz_hi, gr.idz_lo), one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < T64 * T64; e += blockDim.x) {
+        const int i = ti * T64 + e / T64, j = tj * T64 + e % T64;
+        const size_t idx = (size_t) i * ld + j;
+        if (i >= n || j >= n) {
+            S[idx] = zero;
+            C[idx] = (i == j) ? one : zero;
+            continue;
+        }
+        float2 val = zero;
+        if (tab) {
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            const float2 yy = ff_mul(ff_sub(lw[hi], lw[lo]), kv);               // v / dv
+            float zp, ze;
+            two_prod_ff(sw[lo], sw[hi], zp, ze);                                // 1 + z
+            const float2 xx = ff_mul(ff_sub(ff_norm(zp, ze), z1p), idz);         // (z - z1) / dz
+            int nx, ny;
+            float2 fx, fy;
+            ff_index(xx, gr.nzp - 2, nx, fx);
+            ff_index(yy, gr.nv - 2, ny, fy);
+            const size_t ind = (size_t) nx + (size_t) gr.nzp * ny;
+            const float2 gx = ff_sub(one, fx), gy = ff_sub(one, fy);
+            val = ff_mul(ff_mul(tab[ind], gx), gy);
+            val = ff_fma(ff_mul(tab[ind + 1], fx), gy, val);
+            val = ff_fma(ff_mul(tab[ind + gr.nzp], gx), fy, val);
+            val = ff_fma(ff_mul(tab[ind + gr.nzp + 1], fx), fy, val);
+        }
+        S[idx] = val;
+        float2 cv = ff_mul(ff_mul(sq[i], val), sq[j]);
+        if (i == j) cv = ff_add(cv, one);
+        C[idx] = cv;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Phase B, K1b: stored derivative matrices Q_s (Chunk::_setQiMatrix and
 // _applyRedshiftInterp, core/chunk_estimate.cpp:429-536) and per-warp partial
@@ -345,7 +395,13 @@ __global__ void k_prep_mixed(WaveArgs a) {
         __half h = __float2half_rn(x);
         a.c_hi[(size_t) c * plane + idx] = h;
         a.c_lo[(size_t) c * plane + idx] = __float2half_rn(x - __half2float(h));
-        float xs = (float) (S[idx] * ss);
+        float xs;
+        if (a.c_is_ff) {
+            const float2 s2 = reinterpret_cast<const float2 *>(S)[idx];
+            xs = __fadd_rn(s2.x, s2.y) * (float) ss;
+        } else {
+            xs = (float) (S[idx] * ss);
+        }
         __half hs = __float2half_rn(xs);
         a.q_hi[(size_t) (ch.slot_q + ch.ns) * plane + idx] = hs;
         a.q_lo[(size_t) (ch.slot_q + ch.ns) * plane + idx] = __float2half_rn(xs - __half2float(hs));
@@ -552,7 +608,10 @@ __global__ void k_finish(WaveArgs a, int mixed) {
 
 void launch_build_s_c(WaveArgs &a, cudaStream_t st) {
     int tiles = (a.max_ld / T64) * (a.max_ld / T64);
-    k_build_s_c<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
+    if (a.c_is_ff)
+        k_build_s_c_ff<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
+    else
+        k_build_s_c<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
     a.launches++;
 }
 

@@ -38,11 +38,12 @@ struct lqg_ctx {
     std::vector<double> h_wave, h_delta, h_ivar, h_logw, h_sqw;
     std::vector<float2> h_logw2, h_sqw2;
     std::vector<double> h_sqiv, h_niv;
+    std::vector<float2> h_sqiv2;
     std::vector<double> h_flogw, h_fsqw, h_rw;   // resolution-matrix grids and weights
     bool has_reso = false;
     bool pix_dirty = true;
     DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw, d_logw2, d_sqw2, d_sqiv, d_niv;
-    DevBuf d_flogw, d_fsqw, d_rw;
+    DevBuf d_flogw, d_fsqw, d_rw, d_sqiv2;
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
@@ -236,7 +237,7 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
     ctx->h_wave.clear(); ctx->h_delta.clear(); ctx->h_ivar.clear();
     ctx->h_logw.clear(); ctx->h_sqw.clear();
     ctx->h_logw2.clear(); ctx->h_sqw2.clear();
-    ctx->h_sqiv.clear(); ctx->h_niv.clear();
+    ctx->h_sqiv.clear(); ctx->h_niv.clear(); ctx->h_sqiv2.clear();
     ctx->h_flogw.clear(); ctx->h_fsqw.clear(); ctx->h_rw.clear();
     ctx->has_reso = false;
     ctx->have_results = false;
@@ -395,6 +396,7 @@ int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double 
             ctx->h_delta.push_back(delta[i]);
             ctx->h_ivar.push_back(ivar[i]);
             ctx->h_sqiv.push_back(std::sqrt(ivar[i]));
+            ctx->h_sqiv2.push_back(split_ff(ctx->h_sqiv.back()));
             ctx->h_niv.push_back(ivar[i] != 0 ? 1.0 / ivar[i] : 0.0);
         }
         ctx->chunks.push_back(hc);
@@ -462,6 +464,8 @@ int upload_pixels(lqg_ctx *ctx) {
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqiv.p, ctx->h_sqiv.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_niv.p, ctx->h_niv.data(), np * 8, cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqw2.p, ctx->h_sqw2.data(), np * 8, cudaMemcpyHostToDevice, s));
+    if (ctx->d_sqiv2.alloc(bytes)) return set_err(ctx, LQG_ERR_NOMEM, "pixel arrays");
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_sqiv2.p, ctx->h_sqiv2.data(), np * 8, cudaMemcpyHostToDevice, s));
     const size_t nfp = ctx->h_flogw.size(), nrw = ctx->h_rw.size();
     if (ctx->d_flogw.alloc(std::max<size_t>(nfp, 1) * 8) || ctx->d_fsqw.alloc(std::max<size_t>(nfp, 1) * 8) ||
         ctx->d_rw.alloc(std::max<size_t>(nrw, 1) * 8))
@@ -770,6 +774,9 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.logw = ctx->d_logw.as<double>(); base.sqw = ctx->d_sqw.as<double>();
     base.logw2 = ctx->d_logw2.as<float2>(); base.sqw2 = ctx->d_sqw2.as<float2>();
     base.sqiv = ctx->d_sqiv.as<double>(); base.niv = ctx->d_niv.as<double>();
+    base.sqiv2 = ctx->d_sqiv2.as<float2>();
+    // mixed path without theta: S and C~ built in double-float, handed over as pairs
+    base.c_is_ff = (precision == LQG_PRECISION_MIXED && !use_theta && ctx->d_signal_ff.p) ? 1 : 0;
     base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
     base.n_fpix = (int64_t) ctx->h_flogw.size();
     base.reso_nelem = base.reso_os = 0;

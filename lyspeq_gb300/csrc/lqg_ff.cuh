@@ -32,4 +32,46 @@ __device__ __forceinline__ float zweight_ff(const DeviceBins &b, int zm, float P
     return r >= 0.f ? r * b.inv_dz : 0.f;
 }
 
+// ---- double-float arithmetic on the FP32 pipe (value = hi + lo) ----
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 ff_norm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    const float2 s = ff_two_sum(a.x, b.x);
+    return ff_norm(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 ff_sub(float2 a, float2 b) { return ff_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    float p, e;
+    two_prod_ff(a, b, p, e);
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return ff_add(ff_mul(a, b), c); }
+__device__ __forceinline__ float2 ff_of(double x) {
+    const float h = (float) x;
+    return make_float2(h, (float) (x - (double) h));
+}
+
+// Clamped interpolation index and fraction of x (a double-float >= any
+// negative value), the reference's rule (discrete_interpolation.cpp:61-72,
+// 221-242): n = trunc(x) clamped to [0, nmax], fraction x - n.
+__device__ __forceinline__ void ff_index(float2 x, int nmax, int &n, float2 &frac) {
+    int nn = (int) floorf(x.x);
+    float2 f = ff_norm(__fsub_rn(x.x, (float) nn), x.y);
+    if (f.x < 0.f) { --nn; f = ff_add(f, make_float2(1.f, 0.f)); }
+    else if (f.x >= 1.f) { ++nn; f = ff_sub(f, make_float2(1.f, 0.f)); }
+    // trunc rather than floor below zero (the reference casts to int)
+    if (nn < 0) nn = (x.x < 0.f && x.x > -1.f) ? 0 : nn;
+    if (nn > nmax) nn = nmax;
+    if (nn < 0) nn = 0;
+    f = ff_norm(__fsub_rn(x.x, (float) nn), x.y);
+    n = nn;
+    frac = f;
+}
+
 }  // namespace lqg

@@ -105,6 +105,8 @@ struct WaveArgs {
     const double *wave, *delta, *ivar, *logw, *sqw;  // pixel arrays
     const float2 *logw2, *sqw2;                      // ln w and sqrt w as double-float (hi, lo)
     const double *sqiv, *niv;                        // sqrt(ivar), and 1 / ivar (0 where ivar = 0)
+    const float2 *sqiv2;                             // sqrt(ivar) as double-float
+    int c_is_ff;                                     // S and C~ written as double-float pairs (mixed, no theta)
     const double *flogw, *fsqw, *rw;                 // resolution-matrix grids and weights
     int reso_nelem, reso_os;                         // shape shared by every resolution chunk, else 0
     const double *deriv, *signal, *qmax;             // tables

@@ -714,48 +714,6 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     }
 }
 
-// ---- double-float arithmetic on the FP32 pipe (value = hi + lo) ----
-__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
-    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
-}
-__device__ __forceinline__ float2 ff_norm(float s, float e) {
-    const float h = __fadd_rn(s, e);
-    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
-}
-__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
-    const float2 s = ff_two_sum(a.x, b.x);
-    return ff_norm(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
-}
-__device__ __forceinline__ float2 ff_sub(float2 a, float2 b) { return ff_add(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
-    float p, e;
-    two_prod_ff(a, b, p, e);
-    return ff_norm(p, e);
-}
-__device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return ff_add(ff_mul(a, b), c); }
-__device__ __forceinline__ float2 ff_of(double x) {
-    const float h = (float) x;
-    return make_float2(h, (float) (x - (double) h));
-}
-
-// Clamped interpolation index and fraction of x (a double-float >= any
-// negative value), the reference's rule (discrete_interpolation.cpp:61-72,
-// 221-242): n = trunc(x) clamped to [0, nmax], fraction x - n.
-__device__ __forceinline__ void ff_index(float2 x, int nmax, int &n, float2 &frac) {
-    int nn = (int) floorf(x.x);
-    float2 f = ff_norm(__fsub_rn(x.x, (float) nn), x.y);
-    if (f.x < 0.f) { --nn; f = ff_add(f, make_float2(1.f, 0.f)); }
-    else if (f.x >= 1.f) { ++nn; f = ff_sub(f, make_float2(1.f, 0.f)); }
-    // trunc rather than floor below zero (the reference casts to int)
-    if (nn < 0) nn = (x.x < 0.f && x.x > -1.f) ? 0 : nn;
-    if (nn > nmax) nn = nmax;
-    if (nn < 0) nn = 0;
-    f = ff_norm(__fsub_rn(x.x, (float) nn), x.y);
-    n = nn;
-    frac = f;
-}
-
 struct ResoSharedFF {
     float2 wi[RT][RME + 1], wj[RT][RME + 1];
     float2 f[RSLAB][RLF + 1];
@@ -846,21 +804,22 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
             sv[u] = acc;
         }
     }
-    double *S = fws_d(a, ch.o_s), *C = fws_d(a, ch.o_c);
+    // S and C~ as double-float pairs (c_is_ff: the form the mixed factorisation uses)
+    float2 *S = reinterpret_cast<float2 *>(a.fws + ch.o_s), *C = reinterpret_cast<float2 *>(a.fws + ch.o_c);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         const int gi = I * RT + r8 + 8 * u;
-        double s_d = 0.0, c_d = (gi == gj) ? 1.0 : 0.0;
+        float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(gi == gj ? 1.f : 0.f, 0.f);
         if (gi < n && gj < n) {
-            s_d = (double) sv[u].x + (double) sv[u].y;
-            const float2 cv = ff_mul(ff_mul(ff_of(a.sqiv[ch.pix + gi]), sv[u]), ff_of(a.sqiv[ch.pix + gj]));
-            c_d += (double) cv.x + (double) cv.y;
+            s2 = sv[u];
+            const float2 cv = ff_mul(ff_mul(a.sqiv2[ch.pix + gi], sv[u]), a.sqiv2[ch.pix + gj]);
+            c2 = (gi == gj) ? ff_add(cv, make_float2(1.f, 0.f)) : cv;
         }
-        S[(size_t) gi * ld + gj] = s_d;
-        C[(size_t) gi * ld + gj] = c_d;
+        S[(size_t) gi * ld + gj] = s2;
+        C[(size_t) gi * ld + gj] = c2;
         if (I != J) {
-            S[(size_t) gj * ld + gi] = s_d;
-            C[(size_t) gj * ld + gi] = c_d;
+            S[(size_t) gj * ld + gi] = s2;
+            C[(size_t) gj * ld + gi] = c2;
         }
     }
 }
@@ -888,8 +847,8 @@ void set_reso_attrs() {
 void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st) {
     set_reso_attrs();
     const int nt = a.max_ld / RT;
-    // mixed path: double-float build unless theta is given (then the FP64 one)
-    if (a.precision == LQG_PRECISION_MIXED && !a.theta)
+    // mixed path without theta: the double-float build (pairs, c_is_ff); else FP64
+    if (a.c_is_ff)
         k_build_s_c_reso_ff<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoSharedFF), st>>>(a);
     else
         k_build_s_c_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
