@@ -31,6 +31,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstdint>
 #include <functional>
 #include <memory>
@@ -85,6 +87,14 @@ struct Specifics {
     int cont_l_order = -1;              // ContinuumLambdaMargOrder
     bool turn_off_sfid = false;         // TurnOffBaseline
     bool precomputed_fisher = false;    // PrecomputedFisher given
+    double chisq_convergence = 0.01;    // ChiSqConvergence (CHISQ_CONVERGENCE_EPS)
+    bool smooth_logk_logp = true;       // SmoothLnkLnP
+    // the six PD13 fiducial parameters (FiducialAmplitude, ...Slope, ...Curvature,
+    // ...RedshiftPower, ...RedshiftCurvature, ...LorentzianLambda)
+    double fiducial[6] = {6.621420e-02, -2.685349e+00, -2.232763e-01, 3.591244e+00, -1.768045e-01, 3.598261e+02};
+    // the smoothing command between iterations (lyspeq runs its smbivspline.py)
+    std::string smoothing_command = "python3 -m lyspeq_gb300.smoothing";
+    std::string tmp_folder = ".";       // TemporaryFolder
     bool use_reso_matrix = false;       // UseResoMatrix
     int oversampling = -1;              // OversampleRmat
     double resomat_deconvolution_m = 0; // ResoMatDeconvolutionM
@@ -156,9 +166,14 @@ public:
     std::vector<std::unique_ptr<double[]>> dbt_estimate_sum_before_fisher_vector,
         dbt_estimate_fisher_weighted_vector;
     // TOTAL_KZ_BINS
-    std::unique_ptr<double[]> current_power_estimate_vector, powerspectra_fits;
-    // TOTAL_KZ_BINS^2
+    std::unique_ptr<double[]> current_power_estimate_vector, previous_power_estimate_vector, powerspectra_fits;
+    // TOTAL_KZ_BINS^2 (fisher_matrix_sum as downloaded: upper triangle, not
+    // halved; fisher_matrix_halved: halved and symmetric, as the reference
+    // holds it after an iteration)
     std::unique_ptr<double[]> fisher_matrix_sum, inverse_fisher_matrix_sum, solver_invfisher_matrix;
+    std::vector<double> fisher_matrix_halved;
+    // bootstrap(): mean of the realizations, covariance / 4, F^-1 (covariance / 4) F^-T
+    std::vector<double> bootstrap_mean, bootstrap_fisher_covariance, bootstrap_covariance;
     std::vector<std::unique_ptr<OneQSOEstimate>> local_queue;
     int damped = 0, dof = 0;
     double damp = 0;
@@ -192,7 +207,9 @@ public:
             dbt_estimate_fisher_weighted_vector.emplace_back(new double[nkz_]());
         }
         current_power_estimate_vector.reset(new double[nkz_]());
+        previous_power_estimate_vector.reset(new double[nkz_]());
         powerspectra_fits.reset(new double[nkz_]());
+        fisher_matrix_halved.assign((size_t) nkz_ * nkz_, 0.0);
         fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
         inverse_fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
         solver_invfisher_matrix.reset(new double[(size_t) nkz_ * nkz_]());
@@ -290,19 +307,110 @@ public:
         return *local_queue.back();
     }
 
-    // iterate(): for each iteration, every chunk's d, b, t and Fisher matrix
-    // (one batched lqg_nr_iteration with powerspectra_fits as the fiducial
-    // offset), the sums, invertTotalFisherMatrix and
-    // computePowerSpectrumEstimates.
-    void iterate(int number_of_iterations = 1, Precision precision = Precision::FP64) {
-        for (int it = 0; it < number_of_iterations; ++it) {
+    // iterate() (core/quadratic_estimate.cpp:398-528): per iteration every
+    // chunk's d, b, t and Fisher matrix (one batched lqg_nr_iteration with
+    // powerspectra_fits as the offset from the fiducial), the sums,
+    // invertTotalFisherMatrix and computePowerSpectrumEstimates; then
+    // hasConverged, and unless done the smoothing of the estimate into the
+    // next powerspectra_fits.  Returns the number of iterations run.
+    int iterate(int number_of_iterations = 1, Precision precision = Precision::FP64) {
+        int it = 0;
+        for (it = 1; it <= number_of_iterations; ++it) {
             check(lqg_nr_iteration(ctx_.get(), powerspectra_fits.get(), (int) precision), "lqg_nr_iteration");
             check(lqg_download(ctx_.get(), dbt_estimate_sum_before_fisher_vector[0].get(),
                                dbt_estimate_sum_before_fisher_vector[1].get(),
                                dbt_estimate_sum_before_fisher_vector[2].get(), fisher_matrix_sum.get(), nullptr),
                   "lqg_download");
+            std::copy(current_power_estimate_vector.get(), current_power_estimate_vector.get() + nkz_,
+                      previous_power_estimate_vector.get());
             invertTotalFisherMatrix();
+            if (hasConverged() || it == number_of_iterations) break;
+            smoothPowerSpectra();
         }
+        return std::min(it, number_of_iterations);
+    }
+
+    // P_fid(k_c, z_c) of bin i_kz (powerSpectrumFiducial; PD13 fit,
+    // core/fiducial_cosmology.cpp:273-282)
+    double powerSpectrumFiducial(int i_kz) const {
+        const int kn = i_kz % bins_.nk(), zm = i_kz / bins_.nk();
+        const double k = (bins_.k_edges[kn] + bins_.k_edges[kn + 1]) / 2, z = bins_.z_centers[zm];
+        const double *p = sp_.fiducial;
+        const double q0 = k / 0.009 + 1e-15, x0 = (1. + z) / (1. + 3.0);
+        return (p[0] * 3.14159265358979323846 / 0.009) * std::pow(q0, 2. + p[1] + p[2] * std::log(q0) + p[4] * std::log(x0)) *
+               std::pow(x0, p[3]) / (1. + p[5] * k * k);
+    }
+
+    // hasConverged (core/quadratic_estimate.cpp:548-614): with
+    // dp = previous - current (left in previous_power_estimate_vector),
+    // sqrt(sum dp^2 / diag(F^-1) / dof) or sqrt(|dp^T F dp| / dof) below
+    // ChiSqConvergence.
+    bool hasConverged() {
+        double *dp = previous_power_estimate_vector.get();
+        for (int i = 0; i < nkz_; ++i) dp[i] -= current_power_estimate_vector[i];
+        double r = 0, rfull = 0;
+        for (int i = 0; i < nkz_; ++i) {
+            const double e = inverse_fisher_matrix_sum[(size_t) (nkz_ + 1) * i];
+            if (e > 0) r += dp[i] * dp[i] / e;
+        }
+        const std::vector<double> &fh = fisher_matrix_halved;
+        for (int i = 0; i < nkz_; ++i) {
+            double s = 0;
+            for (int j = 0; j < nkz_; ++j) s += fh[(size_t) i * nkz_ + j] * dp[j];
+            rfull += dp[i] * s;
+        }
+        r = std::sqrt(r / dof);
+        rfull = std::sqrt(std::fabs(rfull) / dof);
+        return r < sp_.chisq_convergence || rfull < sp_.chisq_convergence;
+    }
+
+    // _smoothPowerSpectra (core/quadratic_estimate.cpp:353-396): the estimate
+    // as writeSpectrumEstimates prints it, the smoothing command, and its
+    // output minus P_fid as the next powerspectra_fits.
+    void smoothPowerSpectra() {
+        const std::string in = sp_.tmp_folder + "/tmp-power-0.txt", out = sp_.tmp_folder + "/tmp-smooth-0.txt";
+        FILE *f = std::fopen(in.c_str(), "w");
+        if (!f) throw std::runtime_error("cannot write " + in);
+        std::fprintf(f, "%d %d\n", bins_.nz(), bins_.nk());
+        for (int zm = 0; zm < bins_.nz(); ++zm) std::fprintf(f, "%d ", 0);
+        std::fprintf(f, "\n");
+        for (int i = 0; i < nkz_; ++i) {
+            const int kn = i % bins_.nk(), zm = i / bins_.nk();
+            std::fprintf(f, "%.3lf %e %e %e\n", bins_.z_centers[zm], (bins_.k_edges[kn] + bins_.k_edges[kn + 1]) / 2,
+                         current_power_estimate_vector[i] + powerSpectrumFiducial(i),
+                         std::sqrt(inverse_fisher_matrix_sum[(size_t) (nkz_ + 1) * i]));
+        }
+        std::fclose(f);
+        const std::string cmd = sp_.smoothing_command + " " + in + " " + out + (sp_.smooth_logk_logp ? " --interp_log" : "");
+        if (std::system(cmd.c_str()) != 0) throw std::runtime_error("smoothing error: " + cmd);
+        FILE *g = std::fopen(out.c_str(), "r");
+        if (!g) throw std::runtime_error("cannot read " + out);
+        for (int i = 0; i < nkz_; ++i) {
+            if (std::fscanf(g, "%le\n", &powerspectra_fits[i]) != 1) {
+                std::fclose(g);
+                throw std::runtime_error("Reading fit power values from " + out);
+            }
+            powerspectra_fits[i] -= powerSpectrumFiducial(i);
+        }
+        std::fclose(g);
+        std::remove(in.c_str());
+        std::remove(out.c_str());
+    }
+
+    // PoissonBootstrapper with FastBootstrap after the last iteration
+    // (core/quadratic_estimate.cpp:536-545) over this estimator's spectra:
+    // bootstrap_mean, bootstrap_fisher_covariance (covariance / 4) and
+    // bootstrap_covariance (F^-1 (covariance / 4) F^-T).
+    void bootstrap(int number_of_boots, unsigned long long seed = 0) {
+        std::vector<int> off(1, 0);
+        for (const auto &q : local_queue) off.push_back(off.back() + (int) q->chunks.size());
+        bootstrap_mean.assign(nkz_, 0.0);
+        bootstrap_covariance.assign((size_t) nkz_ * nkz_, 0.0);
+        bootstrap_fisher_covariance.assign((size_t) nkz_ * nkz_, 0.0);
+        check(lqg_bootstrap(ctx_.get(), (int) local_queue.size(), off.data(), number_of_boots, seed,
+                            solver_invfisher_matrix.get(), bootstrap_mean.data(), bootstrap_covariance.data(),
+                            bootstrap_fisher_covariance.data(), nullptr),
+              "lqg_bootstrap");
     }
 
     // invertTotalFisherMatrix + computePowerSpectrumEstimates
@@ -316,6 +424,7 @@ public:
                                   solver_invfisher_matrix.get(), inverse_fisher_matrix_sum.get(), w.data(),
                                   current_power_estimate_vector.get(), &damped, &dof, &damp);
         if (rc != LQG_OK) throw std::runtime_error(std::string("Fisher matrix inversion: ") + lqg_last_error(ctx_.get()));
+        fisher_matrix_halved = fh;
         for (int i = 0; i < 3; ++i)
             std::copy(w.begin() + (size_t) i * nkz_, w.begin() + (size_t) (i + 1) * nkz_,
                       dbt_estimate_fisher_weighted_vector[i].get());

@@ -4,7 +4,8 @@
 // run one Newton-Raphson iteration, compare with expected arrays, return
 // non-zero on a mismatch.  Input: one binary file written by
 // tests/test_cpp_facade.py (spectra, tables, binning, expected results of the
-// CPU restatement of lyspeq's path).
+// CPU restatement of lyspeq's path) and optionally a second one with lyspeq's
+// own bootstrap and multi-iteration results on the same spectra.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -54,7 +55,7 @@ double fisher_err(const double *f, const double *ref, int n) {
 
 int main(int argc, char **argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: test_facade <case.bin> <tolerance>\n");
+        std::fprintf(stderr, "usage: test_facade <case.bin> <tolerance> [<loop.bin>]\n");
         return 2;
     }
     const double tol = std::stod(argv[2]);
@@ -125,5 +126,41 @@ int main(int argc, char **argv) {
         }
     std::printf("max rel err: global fisher %.2e, dbt %.2e, theta %.2e, per chunk %.2e (tolerance %.1e)\n", ef,
                 edbt, eth, ech, tol);
-    return (ef < tol && edbt < tol && eth < tol && ech < tol) ? 0 : 1;
+    bool ok = ef < tol && edbt < tol && eth < tol && ech < tol;
+    if (argc > 3) {
+        // lyspeq's own NR loop and FastBootstrap on these spectra (expected values
+        // from the reference): iterate(N) with smoothing, bootstrap(nboots) after
+        // the single iteration above
+        Reader r2(argv[3]);
+        auto str = [&r2]() {
+            std::string t(r2.i64(), ' ');
+            r2.f.read(&t[0], t.size());
+            return t;
+        };
+        const std::string cmd = str(), tmp = str();
+        const int niter = (int) r2.i64();
+        const std::vector<double> theta_it = r2.vec(), fits_it = r2.vec();
+        const int nboots = (int) r2.i64();
+        const std::vector<double> boot_mean = r2.vec(), boot_cov = r2.vec();
+        if (!r2.ok()) {
+            std::fprintf(stderr, "could not read %s\n", argv[3]);
+            return 2;
+        }
+        qe.bootstrap(nboots, 0);
+        const double ebm = rel_err(qe.bootstrap_mean.data(), boot_mean.data(), nkz);
+        const double ebc = rel_err(qe.bootstrap_covariance.data(), boot_cov.data(), (size_t) nkz * nkz);
+        Specifics sp2 = sp;
+        sp2.smooth_logk_logp = false;
+        sp2.smoothing_command = cmd;
+        sp2.tmp_folder = tmp;
+        OneDQuadraticPowerEstimate qe2(bins, grid, tables, sp2);
+        for (const auto &q : spectra) qe2.addQSO(q);
+        const int its = qe2.iterate(niter, Precision::FP64);
+        const double eit = rel_err(qe2.current_power_estimate_vector.get(), theta_it.data(), nkz);
+        const double efit = rel_err(qe2.powerspectra_fits.get(), fits_it.data(), nkz);
+        std::printf("bootstrap: mean %.2e, covariance %.2e; NR loop (%d iterations): theta %.2e, fits %.2e\n", ebm,
+                    ebc, its, eit, efit);
+        ok = ok && ebm < 1e-10 && ebc < 1e-9 && eit < 1e-8 && efit < 1e-8;
+    }
+    return ok ? 0 : 1;
 }

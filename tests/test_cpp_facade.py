@@ -2,7 +2,9 @@
 (tests/cpp/test_facade.cpp) the way lyspeq's own tests drive its classes: the
 tiny workload's spectra go through OneQSOEstimate chunking and one FP64
 Newton-Raphson iteration, compared with the CPU restatement of lyspeq's path
-(global Fisher matrix, d/b/t sums, theta and every chunk's own results)."""
+(global Fisher matrix, d/b/t sums, theta and every chunk's own results); then
+the FastBootstrap after that iteration and a 4-iteration loop with smoothing,
+compared with lyspeq's own results (golden fixtures tiny_boot, tiny_iter)."""
 import os
 import shutil
 import struct
@@ -81,6 +83,26 @@ def test_cpp_facade_one_iteration_matches_the_oracle(tmp_path):
     nr = P.newton_raphson_step(fsum, dbt)
     path = str(tmp_path / "case.bin")
     _write(path, w, s, chunks, results, dict(fsum=fsum, dbt=dbt, theta=nr["theta"]))
-    r = subprocess.run([exe, path, "1e-9"], capture_output=True, text=True)
+    # lyspeq's own NR loop (4 iterations) and FastBootstrap (200) on these spectra
+    import sys
+    import golden_cases as G
+    it, bt = G.load("tiny_iter").nr, G.load("tiny_boot").boot
+    loop = str(tmp_path / "loop.bin")
+    with open(loop, "wb") as f:
+        def blob(b):
+            f.write(struct.pack("<q", len(b)))
+            f.write(b)
+
+        def vec(a):
+            a = np.ascontiguousarray(a, dtype="<f8").ravel()
+            f.write(struct.pack("<q", a.size))
+            f.write(a.tobytes())
+        blob(f"cd {ROOT} && {sys.executable} -m lyspeq_gb300.smoothing".encode())
+        blob(str(tmp_path).encode())
+        f.write(struct.pack("<q", it["n"]))
+        vec(it["theta"]); vec(it["fits"])
+        f.write(struct.pack("<q", bt["real"].shape[0]))
+        vec(bt["mean"]); vec(bt["cov"])
+    r = subprocess.run([exe, path, "1e-9", loop], capture_output=True, text=True)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stdout + r.stderr
