@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define LQG_ABI_VERSION 1
+#define LQG_ABI_VERSION 2
 
 /* status codes */
 #define LQG_OK 0
@@ -99,6 +99,15 @@ typedef struct {
     int turn_off_sfid;          /* TurnOffBaseline > 0 */
     int skip_fisher;            /* PrecomputedFisher given: Fisher not computed */
     size_t workspace_bytes;     /* device workspace cap; 0 = 60% of free memory */
+    int smooth_noise_weights;   /* SmoothNoiseWeights: < 0 off; 0 the mean noise;
+                                   > 0 Gaussian sigma in pixels.  C is built with the
+                                   smoothed ivar (Chunk::setInvertCovarianceMatrix,
+                                   core/chunk_estimate.cpp:685-691), N of the bias
+                                   traces keeps the raw ivar (:767-786) */
+    int redshift_growth_on;     /* RedshiftGrowthOn > 0: Q_k scaled by
+                                   ((1 + z_ij) / (1 + z_m))^B
+                                   (_scaleDerivativesWithRedshiftGrowth, :539-573) */
+    double fid_redshift_power;  /* B of the fiducial PD13 (FiducialRedshiftPower) */
 } lqg_opts;
 
 /* Create a context on CUDA device `device`; bins and tables are copied.
@@ -158,6 +167,14 @@ int lqg_batch_add_reso(lqg_ctx *ctx, int n_chunks, const int64_t *offsets,
 int lqg_resomat_deconvolve(int n, int ndiags, double *values, double m);
 int lqg_resomat_oversample(int n, int ndiags, const double *values, int osamp, double dlambda,
                            double *rows);
+/* Smoother::smoothIvar (mathtools/smoother.cpp:170-218) for one chunk's ivar
+ * of n pixels: sigmapix = SmoothNoiseWeights (0: the mean ivar, > 0: Gaussian
+ * filter of 51 taps with that sigma on the noise variance), masked and
+ * high-noise pixels keep their ivar.  The reference's padding is kept as it
+ * is: its right-hand pad lands on the last 25 pixels and leaves the 25 pad
+ * cells beyond them at 0, so unless the last pixel is masked the last 25
+ * pixels come out with ivar 0.  Host only; out may not alias ivar. */
+int lqg_smooth_ivar(int n, const double *ivar, int sigmapix, double *out);
 /* SQ lookup tables on the GPU: SQLookupTable::computeTables
  * (core/sq_table.cpp:201-323, CreateSQLookUpTable), for n_tables (R, dv)
  * pairs on the grids lqg_tables describes (nv points over [0, v_length], nzp

@@ -98,6 +98,8 @@ struct Specifics {
     bool use_reso_matrix = false;       // UseResoMatrix
     int oversampling = -1;              // OversampleRmat
     double resomat_deconvolution_m = 0; // ResoMatDeconvolutionM
+    int smooth_noise_weights = -1;      // SmoothNoiseWeights
+    bool redshift_growth_on = false;    // RedshiftGrowthOn > 0 (exponent: fiducial[3])
     double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
 };
 
@@ -197,7 +199,8 @@ public:
         lqg_tables tb{(int) tables.size(), r.data(), dv.data(), grid.nv, grid.v_length, grid.nzp,
                       deriv.data(), sp.turn_off_sfid ? nullptr : signal.data()};
         lqg_opts o{sp.max_forest_length_v(), sp.max_mean_pixel_size, sp.cont_logl_order, sp.cont_l_order,
-                   sp.turn_off_sfid ? 1 : 0, sp.precomputed_fisher ? 1 : 0, 0};
+                   sp.turn_off_sfid ? 1 : 0, sp.precomputed_fisher ? 1 : 0, 0, sp.smooth_noise_weights,
+                   sp.redshift_growth_on ? 1 : 0, sp.fiducial[3]};
         lqg_ctx *c = nullptr;
         if (lqg_ctx_create(&c, &b, &tb, &o, device) != LQG_OK)
             throw std::runtime_error("lqg_ctx_create failed (tables, binning or CUDA device)");

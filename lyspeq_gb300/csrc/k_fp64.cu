@@ -54,19 +54,6 @@ __device__ __forceinline__ double signal_at(const double *tab, const TableGrid &
          + tab[ind + g.nzp] * (1 - dnx) * dny + tab[ind + g.nzp + 1] * dnx * dny;
 }
 
-// Redshift weight of bin zm at z, element-wise form of bins::zBinTriangular1/2,
-// zBinTriangular and zBinTopHat (core/global_numbers.cpp:393-471); on the
-// sorted rows the reference walks these conditions select the same elements.
-__device__ __forceinline__ double zweight(const DeviceBins &b, int zm, double z) {
-    double zc = b.z_centers[zm], dz = b.dz;
-    if (!b.triangular || b.nz == 1)
-        return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.0 : 0.0;
-    if (zm == 0 && z < zc) return 1.0;
-    if (zm == b.nz - 1 && z > zc) return 1.0;
-    if (z >= zc - dz && z <= zc + dz) return 1.0 - fabs(z - zc) / dz;
-    return 0.0;
-}
-
 // Linear interpolation index of a derivative-table row (discrete_interpolation.cpp:61-72);
 // shared by all k bands at one v.
 __device__ __forceinline__ void vindex(const TableGrid &g, double v, int &n, double &dn) {
@@ -145,7 +132,7 @@ __global__ void k_build_s_c(WaveArgs a) {
                 if (th == 0.0) continue;
                 const double *row = a.deriv + ((size_t) ch.res * bins.nk + kn) * a.grid.nv;
                 double q = row[nidx] * (1 - dn) + row[nidx + 1] * dn;
-                q *= zweight(bins, ch.zb0 + iz, z);
+                q *= zfactor(bins, ch.zb0 + iz, z);
                 cv += th * q;
             }
         }
@@ -262,7 +249,7 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
             double part = 0.0;
 #pragma unroll
             for (int u = 0; u < QEPT; ++u) {
-                const double q = valid[u] ? base[u] * zweight(bins, zm, zz[u]) : 0.0;
+                const double q = valid[u] ? base[u] * zfactor(bins, zm, zz[u]) : 0.0;
                 part += yy[u] * q;
                 Q[off[u]] = q;
             }
@@ -336,7 +323,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
         for (int g = 0; g < kZGroup; ++g)
 #pragma unroll
             for (int k = 0; k < E; ++k)
-                w[g][k] = (z0 + g < nzb && zp[k] > 0.f) ? zweight_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k]) : 0.f;
+                w[g][k] = (z0 + g < nzb && zp[k] > 0.f) ? zfactor_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k]) : 0.f;
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
             const float *row = rows + (size_t) kn * a.grid.nv;
             float base[E];

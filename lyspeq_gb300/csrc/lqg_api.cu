@@ -118,6 +118,7 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
         if (nvec > kMaxContVecs) return LQG_ERR_UNSUPPORTED;
     }
     if (!(opts->max_mean_pixel_size > 0) || !(opts->max_forest_length >= 0)) return LQG_ERR_ARG;
+    if (opts->redshift_growth_on > 0 && !std::isfinite(opts->fid_redshift_power)) return LQG_ERR_ARG;
     auto ctx = std::make_unique<lqg_ctx>();
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess) return LQG_ERR_CUDA;
@@ -208,6 +209,8 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
         db.dz_hi = d.x; db.dz_lo = d.y; db.dzh_hi = dh.x; db.dzh_lo = dh.y;
         db.inv_dz = (float) (1.0 / ctx->dz);
     }
+    db.growth = opts->redshift_growth_on > 0;
+    db.growth_b = opts->fid_redshift_power;
     if (ctx->d_bins.alloc(sizeof(DeviceBins)) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "bins");
     cudaMemcpy(ctx->d_bins.p, &db, sizeof db, cudaMemcpyHostToDevice);
     if (ctx->d_fisher.alloc((size_t) ctx->nkz * ctx->nkz * 8) != cudaSuccess ||
@@ -382,6 +385,10 @@ int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double 
             }
             ctx->h_rw.insert(ctx->h_rw.end(), rw.begin(), rw.end());
         }
+        // SmoothNoiseWeights: C takes the smoothed ivar, N the raw one
+        std::vector<double> ivc(ivar + a, ivar + b);
+        if (ctx->opts.smooth_noise_weights >= 0)
+            smooth_ivar(n, ivar + a, ctx->opts.smooth_noise_weights, ivc.data());
         hc.input_index = c;
         hc.pix = (int64_t) ctx->h_wave.size();
         hc.res_off = ctx->results_size;
@@ -394,8 +401,8 @@ int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double 
             ctx->h_logw2.push_back(split_ff(ctx->h_logw.back()));
             ctx->h_sqw2.push_back(split_ff(ctx->h_sqw.back()));
             ctx->h_delta.push_back(delta[i]);
-            ctx->h_ivar.push_back(ivar[i]);
-            ctx->h_sqiv.push_back(std::sqrt(ivar[i]));
+            ctx->h_ivar.push_back(ivc[i - a]);
+            ctx->h_sqiv.push_back(std::sqrt(ivc[i - a]));
             ctx->h_sqiv2.push_back(split_ff(ctx->h_sqiv.back()));
             ctx->h_niv.push_back(ivar[i] != 0 ? 1.0 / ivar[i] : 0.0);
         }

@@ -32,6 +32,15 @@ __device__ __forceinline__ float zweight_ff(const DeviceBins &b, int zm, float P
     return r >= 0.f ? r * b.inv_dz : 0.f;
 }
 
+// zweight_ff times, with the growth option on, ((1 + z) / (1 + z_m))^B in
+// FP32 (the ratio is within 1e-7 relative, as the 22-bit operands need).
+__device__ __forceinline__ float zfactor_ff(const DeviceBins &b, int zm, float P, float E) {
+    float w = zweight_ff(b, zm, P, E);
+    if (b.growth && w != 0.f)
+        w *= powf(__fdiv_rn(__fadd_rn(P, E), __fadd_rn(b.zc1_hi[zm], b.zc1_lo[zm])), (float) b.growth_b);
+    return w;
+}
+
 // ---- double-float arithmetic on the FP32 pipe (value = hi + lo) ----
 __device__ __forceinline__ float2 ff_two_sum(float a, float b) {
     const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);

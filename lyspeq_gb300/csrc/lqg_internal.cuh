@@ -65,7 +65,28 @@ struct DeviceBins {
     // mixed path: 1 + z_c per bin, dz, dz / 2, and 1 / dz
     float zc1_hi[64], zc1_lo[64];
     float dz_hi, dz_lo, dzh_hi, dzh_lo, inv_dz;
+    // RedshiftGrowthOn: Q_k of bin m scaled by ((1 + z_ij) / (1 + z_m))^B
+    int growth;
+    double growth_b;
 };
+
+// Redshift weight of bin zm at z, element-wise form of bins::zBinTriangular1/2,
+// zBinTriangular and zBinTopHat (core/global_numbers.cpp:393-471); on the
+// sorted rows the reference walks these conditions select the same elements.
+// With the growth option on, times ((1 + z) / (1 + z_m))^B
+// (Chunk::_scaleDerivativesWithRedshiftGrowth, core/chunk_estimate.cpp:539-573,
+// which takes 1 + z_ij as z_ij + 1 and 1 + z_m as ZBIN_CENTERS[m] + 1).
+__device__ __forceinline__ double zfactor(const DeviceBins &b, int zm, double z) {
+    const double zc = b.z_centers[zm], dz = b.dz;
+    double w;
+    if (!b.triangular || b.nz == 1) w = (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.0 : 0.0;
+    else if (zm == 0 && z < zc) w = 1.0;
+    else if (zm == b.nz - 1 && z > zc) w = 1.0;
+    else if (z >= zc - dz && z <= zc + dz) w = 1.0 - fabs(z - zc) / dz;
+    else w = 0.0;
+    if (b.growth && w != 0.0) w *= pow((z + 1.0) / (zc + 1), b.growth_b);
+    return w;
+}
 
 struct TableGrid {
     int nv, nzp, n_tables;
@@ -170,6 +191,8 @@ void launch_finish(WaveArgs &a, cudaStream_t st);
 
 bool tc_available();
 int gram_splits_mixed(int ld);
+// Smoother::smoothIvar on the host (lqg_smooth.cu)
+int smooth_ivar(int n, const double *ivar, int sigmapix, double *out);
 
 }  // namespace lqg
 

@@ -287,17 +287,6 @@ __device__ void reso_sandwich(ResoShared &sm, const ResoGeom &g, Eval ev, double
     __syncthreads();
 }
 
-// Redshift weight of bin zm at z (bins::zBin*, core/global_numbers.cpp:393-471),
-// the element-wise form used by the plain Q build.
-__device__ __forceinline__ double zweight_r(const DeviceBins &b, int zm, double z) {
-    const double zc = b.z_centers[zm], dz = b.dz;
-    if (!b.triangular || b.nz == 1) return (z >= zc - dz / 2 && z <= zc + dz / 2) ? 1.0 : 0.0;
-    if (zm == 0 && z < zc) return 1.0;
-    if (zm == b.nz - 1 && z > zc) return 1.0;
-    if (z >= zc - dz && z <= zc + dz) return 1.0 - fabs(z - zc) / dz;
-    return 0.0;
-}
-
 // DiscreteInterpolation2D::evaluate (mathtools/discrete_interpolation.cpp:221-242).
 __device__ __forceinline__ double signal_at_r(const double *tab, const TableGrid &gr, double z, double v) {
     const double xx = (z - gr.z1) / gr.dz, yy = (v - gr.v1) / gr.dv;
@@ -372,7 +361,7 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso(WaveArgs a) {
                 if (gi < n && gj < n) {
                     const int lo = min(gi, gj), hi = max(gi, gj);
                     const double z = a.sqw[ch.pix + lo] * a.sqw[ch.pix + hi] - 1.0;
-                    c_out[u] += gm[u] * zweight_r(bins, ch.zb0 + iz, z);
+                    c_out[u] += gm[u] * zfactor(bins, ch.zb0 + iz, z);
                 }
             }
         }
@@ -448,7 +437,7 @@ __global__ void __launch_bounds__(RTH) k_build_q_reso(WaveArgs a) {
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int gi = I * RT + r8 + 8 * u;
-                const double q = valid[u] ? b[u] * zweight_r(bins, ch.zb0 + iz, zz[u]) : 0.0;
+                const double q = valid[u] ? b[u] * zfactor(bins, ch.zb0 + iz, zz[u]) : 0.0;
                 part += yy[u] * q;
                 double *Q = ws_d(a, ch.o_q) + (size_t) s * plane;
                 Q[(size_t) gi * ld + gj] = q;
@@ -564,7 +553,7 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
         if (valid[u]) two_prod_ff(sw2[min(gi, gj)], sw2[max(gi, gj)], zp[u], ze[u]);
 #pragma unroll
         for (int iz = 0; iz < 4; ++iz)
-            zw[u][iz] = (valid[u] && iz < nzb) ? zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]) : 0.f;
+            zw[u][iz] = (valid[u] && iz < nzb) ? zfactor_ff(bins, ch.zb0 + iz, zp[u], ze[u]) : 0.f;
     }
     const float2 *ph = reinterpret_cast<const float2 *>(a.ws + ch.o_ph);
     const float mult = (I == J) ? 1.f : 2.f;
@@ -670,7 +659,7 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
                 for (int u = 0; u < 4; ++u) {
                     const int i = r8 + 8 * u, gi = I * RT + i;
                     float w = 0.f;
-                    if (valid[u]) w = iz < 4 ? zw[u][iz] : zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]);
+                    if (valid[u]) w = iz < 4 ? zw[u][iz] : zfactor_ff(bins, ch.zb0 + iz, zp[u], ze[u]);
                     const float q = b[u] * w;
                     part[g] = fmaf(yy[u], q, part[g]);
                     const float x = q * qs;

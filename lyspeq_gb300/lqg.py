@@ -24,7 +24,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
            "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate",
-           "lqg_bootstrap"]
+           "lqg_bootstrap", "lqg_smooth_ivar"]
 
 
 class LqgBins(C.Structure):
@@ -44,7 +44,8 @@ class LqgOpts(C.Structure):
     _fields_ = [("max_forest_length", C.c_double), ("max_mean_pixel_size", C.c_double),
                 ("cont_logl_order", C.c_int), ("cont_l_order", C.c_int),
                 ("turn_off_sfid", C.c_int), ("skip_fisher", C.c_int),
-                ("workspace_bytes", C.c_size_t)]
+                ("workspace_bytes", C.c_size_t), ("smooth_noise_weights", C.c_int),
+                ("redshift_growth_on", C.c_int), ("fid_redshift_power", C.c_double)]
 
 
 _lib = None
@@ -73,6 +74,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_tables_generate.argtypes = [C.POINTER(LqgBins), C.c_int, ip, dp, C.c_int, C.c_double, C.c_int,
                                         dp, C.c_int, dp, dp, C.c_int]
     lib.lqg_bootstrap.argtypes = [vp, C.c_int, ip, C.c_int, C.c_ulonglong, dp, dp, dp, dp, dp]
+    lib.lqg_smooth_ivar.argtypes = [C.c_int, dp, C.c_int, dp]
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
@@ -101,7 +103,7 @@ class Engine:
 
     def __init__(self, bins, tables, nv, lenv, nzp, max_forest_length, max_mean_pixel_size=150.0,
                  cont=(-1, -1), turn_off_sfid=False, skip_fisher=False, device=0,
-                 workspace_bytes=0):
+                 workspace_bytes=0, smooth_noise_weights=-1, redshift_growth=False, fid_b=0.0):
         self.lib = load_library()
         self.bins = bins
         self.nkz = bins.nk * bins.nz
@@ -116,7 +118,8 @@ class Engine:
         t = LqgTables(len(tables), _iptr(self._r), _dptr(self._dv), nv, lenv, nzp,
                       _dptr(self._deriv), None if turn_off_sfid else _dptr(self._signal))
         o = LqgOpts(max_forest_length, max_mean_pixel_size, cont[0], cont[1], int(turn_off_sfid),
-                    int(skip_fisher), workspace_bytes)
+                    int(skip_fisher), workspace_bytes, int(smooth_noise_weights), int(bool(redshift_growth)),
+                    float(fid_b))
         h = C.c_void_p()
         rc = self.lib.lqg_ctx_create(C.byref(h), C.byref(b), C.byref(t), C.byref(o), device)
         if rc != LQG_OK:
@@ -271,6 +274,17 @@ class Engine:
 
     def wave_count(self):
         return self.lib.lqg_last_wave_count(self.h)
+
+
+def smooth_ivar(ivar, sigmapix):
+    """Smoother::smoothIvar through the library (host only)."""
+    lib = load_library()
+    iv = np.ascontiguousarray(ivar, dtype=np.float64)
+    out = np.empty_like(iv)
+    rc = lib.lqg_smooth_ivar(len(iv), _dptr(iv), int(sigmapix), _dptr(out))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_smooth_ivar failed with {rc}")
+    return out
 
 
 def resomat_deconvolve(values, m):

@@ -37,6 +37,9 @@ class Settings:
     cont_logl_order: int = 1
     cont_l_order: int = -1
     turn_off_sfid: bool = False
+    smooth_noise_weights: int = -1   # SmoothNoiseWeights (mathtools/smoother.hpp:8-9)
+    redshift_growth: bool = False    # RedshiftGrowthOn > 0 (core/global_numbers.cpp:127)
+    growth_b: float = 0.0            # FIDUCIAL_PD13_PARAMS.B
 
     @property
     def max_forest_length_v(self):
@@ -444,6 +447,64 @@ def zbin_weight(bins, zm, z):
     return out
 
 
+SMOOTH_HWSIZE = 25                # Smoother::HWSIZE (mathtools/smoother.hpp:12)
+
+
+def _median_statistics(arr, thres=1e3):
+    """_findMedianStatistics (mathtools/smoother.cpp:66-81): median, mean and
+    scaled MAD of the sorted values <= thres (the mean a sequential sum)."""
+    a = np.sort(arr)
+    m = len(a)
+    while m and a[m - 1] > thres:
+        m -= 1
+    if m == 0:
+        return a[0], math.nan, math.nan
+    median = _median_sorted(a[:m])
+    mean = float(np.cumsum(a[:m])[-1]) / m
+    mad = 1.4826 * _median_sorted(np.sort(np.abs(a[:m] - median)))
+    return median, mean, mad
+
+
+def smooth_ivar(ivar, sigmapix):
+    """Smoother::smoothIvar (mathtools/smoother.cpp:171-217) with its filter
+    (_constructFilter :102-113), padding (padArray :18-26: the right-hand pad
+    is written over the last SMOOTH_HWSIZE pixels, the cells past them stay 0)
+    and masked-region fill (_fillMaskedRegion :84-99)."""
+    ivar = np.asarray(ivar, dtype=np.float64)
+    n, hw = len(ivar), SMOOTH_HWSIZE
+    with np.errstate(divide="ignore"):
+        var = np.where(ivar == 0, 1e15, 1.0 / ivar)
+    median, mean, mad = _median_statistics(var)
+    if math.isnan(mean):
+        return ivar.copy()
+    mean = 1.0 / mean
+    cut = 1.0 / (median + 3.5 * mad)
+    masked = np.flatnonzero(ivar < cut)
+    if sigmapix == 0:
+        out = np.full(n, mean)
+    else:
+        pad = np.zeros(n + 2 * hw)
+        pad[hw:hw + n] = ivar
+        pad[:hw] = ivar[0]
+        pad[n:n + hw] = ivar[-1]
+        if masked.size:
+            if masked[0] == 0:
+                pad[:hw] = mean
+            pad[masked + hw] = mean
+            if masked[-1] == n - 1:
+                pad[-hw:] = mean
+        with np.errstate(divide="ignore"):
+            pad = 1.0 / pad
+        x = np.arange(-hw, hw + 1) * 1.0 / sigmapix
+        g = np.exp(-(x * x) / 2)
+        g = g / float(np.cumsum(g)[-1])
+        win = np.lib.stride_tricks.sliding_window_view(pad, 2 * hw + 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            out = 1.0 / (win @ g)
+    out[masked] = ivar[masked]
+    return out
+
+
 def _sym_upper(a):
     return np.triu(a) + np.triu(a, 1).T
 
@@ -476,10 +537,14 @@ def table_view(table, bins, nv, lenv, nzp):
                      bins.z_centers[0] - bins.dz, lenz / (nzp - 1.0))
 
 
-def build_matrices(ch: ChunkData, bins, tv: TableView):
+def build_matrices(ch: ChunkData, bins, tv: TableView, growth_b=None):
     """v/z matrices, stored Q_k with redshift weights, and S_fid
     (core/chunk_estimate.cpp:384-536, :861-882).  Returns (stored i_kz list,
-    Q stack [ns, n, n], S)."""
+    Q stack [ns, n, n], S).  growth_b: RedshiftGrowthOn with exponent B
+    (_scaleDerivativesWithRedshiftGrowth, :539-573), Q_k of bin m times
+    ((1 + z_ij) / (1 + z_m))^B, on the full symmetric z_ij (the reference's
+    z matrix is only complete with an oversampled resolution matrix; without
+    one its lower triangle is scratch that the growth step reads as it is)."""
     n = ch.n
     li, lj = ch.wave[:, None], ch.wave[None, :]
     vmat = C_KMS * np.log(lj / li)
@@ -534,6 +599,12 @@ def build_matrices(ch: ChunkData, bins, tv: TableView):
         w[iu] = zbin_weight(bins, zm, zu)
         w = _sym_upper_fill(w)
         q[iz * ch.kbin_upp:(iz + 1) * ch.kbin_upp] *= w[None]
+    if growth_b is not None:
+        z1 = zmat + 1.0
+        for iz in range(nzb):
+            zm = ch.fisher_index_start // bins.nk + iz
+            g = (z1 / (bins.z_centers[zm] + 1)) ** growth_b
+            q[iz * ch.kbin_upp:(iz + 1) * ch.kbin_upp] *= g[None]
     return stored, q, sm
 
 
@@ -551,10 +622,13 @@ def inverse_covariance(ch: ChunkData, stored, q, sm, theta, settings):
     cov = np.zeros((n, n)) if settings.turn_off_sfid else sm.copy()
     for s, ikz in enumerate(stored):
         cov += theta[ch.fisher_index_start + ikz] * q[s]
-    cov *= ch.ivar[:, None]
+    ivec = ch.ivar
+    if settings.smooth_noise_weights >= 0:
+        ivec = smooth_ivar(ch.ivar, settings.smooth_noise_weights)
+    cov *= ivec[:, None]
     cov[np.diag_indices(n)] += 1.0
     cinv = lu_inverse(cov)
-    cinv *= ch.ivar[None, :]
+    cinv *= ivec[None, :]
     nvec = settings.cont_nvecs
     if nvec > 0:
         vecs = [np.full(n, 1.0 / math.sqrt(n))]
@@ -582,7 +656,7 @@ def inverse_covariance(ch: ChunkData, stored, q, sm, theta, settings):
 def chunk_iteration(ch: ChunkData, bins, tv: TableView, theta, settings, compute_fisher=True):
     """Chunk::oneQSOiteration for one chunk: returns (d, b, t, F) with
     F (nq x nq) upper triangle filled and not halved (core/chunk_estimate.cpp:738-914)."""
-    stored, q, sm = build_matrices(ch, bins, tv)
+    stored, q, sm = build_matrices(ch, bins, tv, settings.growth_b if settings.redshift_growth else None)
     cinv = inverse_covariance(ch, stored, q, sm, theta, settings)
     n, nq, ns = ch.n, ch.nq, len(stored)
     d, b, t = np.zeros(nq), np.zeros(nq), np.zeros(nq)

@@ -44,6 +44,18 @@ CASES = {
     "tiny_boot": ("tiny", None, (1, -1), 0.0, None, 200),
     # lyspeq's full Newton-Raphson loop (NumberOfIterations 4, smoothing between)
     "tiny_iter": ("tiny", None, (1, -1), 0.0, None, 0, 4),
+    # noise-weight smoothing (Gaussian, and the mean) and redshift growth
+    "tiny_smooth": ("tiny", None, (1, -1), 0.04, None),
+    "tiny_smooth_mean": ("tiny", None, (-1, -1), 0.0, None),
+    "tiny_reso_growth": ("tiny_reso", None, (-1, -1), 0.0, None),
+}
+
+# config keys set for a case: SmoothNoiseWeights and RedshiftGrowthOn
+# (the growth exponent is the fiducial FiducialRedshiftPower)
+OPTIONS = {
+    "tiny_smooth": {"SmoothNoiseWeights": 3},
+    "tiny_smooth_mean": {"SmoothNoiseWeights": 0},
+    "tiny_reso_growth": {"RedshiftGrowthOn": 1},
 }
 
 
@@ -70,6 +82,15 @@ def make_case(name, spec):
         if iters > 1:
             text = open(cfg).read().replace("NumberOfIterations 1", f"NumberOfIterations {iters}")
             open(cfg, "w").write(text)
+        opts = OPTIONS.get(name, {})
+        if opts:
+            text = open(cfg).read()
+            for key, val in opts.items():
+                if f"\n{key} " in text:
+                    text = "\n".join(f"{key} {val}" if ln.startswith(f"{key} ") else ln for ln in text.split("\n"))
+                else:
+                    text += f"{key} {val}\n"
+            open(cfg, "w").write(text)
         dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso, boots=boots,
                                   iterate=iters > 1)
         it = refdump.read_iteration(os.path.join(tmp, "dump.bin.iter")) if iters > 1 else None
@@ -88,6 +109,9 @@ def make_case(name, spec):
         g_fisher=dump.fisher, g_dbt=dump.dbt, g_theta=dump.theta, g_solver=dump.solver_invfisher,
         g_inverse=dump.inverse_fisher, g_damped=np.array(dump.damped),
         g_complete=np.array(keep is None),
+        # SmoothNoiseWeights, RedshiftGrowthOn, FiducialRedshiftPower
+        opts=np.array([OPTIONS.get(name, {}).get("SmoothNoiseWeights", -1),
+                       OPTIONS.get(name, {}).get("RedshiftGrowthOn", -1), w.fid[3]], dtype=float),
     )
     if it is not None:
         out["it_n"] = np.array(iters)

@@ -10,8 +10,8 @@ from lyspeq_gb300 import synth
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub",
-         "tiny_reso", "tiny_reso_dia"]
-RESO_CASES = ["tiny_reso", "tiny_reso_dia"]
+         "tiny_reso", "tiny_reso_dia", "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth"]
+RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth"]
 
 
 @dataclasses.dataclass
@@ -39,6 +39,15 @@ class GoldenCase:
     rmats: list | None = None
     src: list | None = None
     spectra: list | None = None
+    # SmoothNoiseWeights, RedshiftGrowthOn and its exponent, as Engine keywords
+    opts: dict = dataclasses.field(default_factory=lambda: dict(smooth_noise_weights=-1, redshift_growth=False,
+                                                                  fid_b=0.0))
+
+    def port_settings(self, P):
+        """The oracle's Settings for this case."""
+        return P.Settings(max_forest_length=self.max_forest_length, cont_logl_order=self.marg[0],
+                          cont_l_order=self.marg[1], smooth_noise_weights=self.opts["smooth_noise_weights"],
+                          redshift_growth=self.opts["redshift_growth"], growth_b=self.opts["fid_b"])
 
 
 _cache = {}
@@ -67,6 +76,9 @@ def load(name: str) -> GoldenCase:
     g = {k[2:]: z[k] for k in z.files if k.startswith("g_")}
     case = GoldenCase(name, bins, tables, nv, float(lenv), nzp, float(mfl), (int(m0), int(m1)),
                       chunks, meta, dbt, fis, g, bool(z["g_complete"]))
+    if "opts" in z.files:
+        o = z["opts"]
+        case.opts = dict(smooth_noise_weights=int(o[0]), redshift_growth=bool(o[1] > 0), fid_b=float(o[2]))
     if "it_n" in z.files:
         case.nr = dict(n=int(z["it_n"]), theta=z["it_theta"], previous=z["it_prev"], fits=z["it_fits"],
                        fisher=z["it_fisher"], inverse=z["it_inverse"], dbt=z["it_dbt"])

@@ -28,4 +28,4 @@ def test_library_exports_header(engine_lib):
 def test_null_arguments_rejected_without_gpu(engine_lib):
     h = C.c_void_p()
     assert engine_lib.lqg_ctx_create(C.byref(h), None, None, None, 0) == -1
-    assert engine_lib.lqg_abi_version() == 1
+    assert engine_lib.lqg_abi_version() == 2

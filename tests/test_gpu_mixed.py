@@ -11,12 +11,13 @@ import golden_cases as G
 
 pytestmark = pytest.mark.gpu
 MIXED_TOL = 1e-5
-CASES = ["tiny_nomarg", "tiny_marg1", "tiny_masked", "small_cfg", "desi_sub", "tiny_reso", "tiny_reso_dia"]
+CASES = ["tiny_nomarg", "tiny_marg1", "tiny_masked", "small_cfg", "desi_sub", "tiny_reso", "tiny_reso_dia",
+         "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth"]
 
 
 def make_engine(c):
     from lyspeq_gb300 import lqg
-    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg)
+    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg, **c.opts)
     if c.reso is None:
         st = eng.add_chunk_list(c.chunks)
     else:

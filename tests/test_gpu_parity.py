@@ -19,7 +19,8 @@ FP64_TOL = {"tiny_marg3": 1e-7}
 
 def make_engine(c, **kw):
     from lyspeq_gb300 import lqg
-    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg, **kw)
+    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg,
+                     **{**c.opts, **kw})
     if c.reso is None:
         st = eng.add_chunk_list(c.chunks)
     else:

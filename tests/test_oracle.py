@@ -84,8 +84,7 @@ TOL = {"tiny_marg3": 1e-7}
 def test_port_matches_reference(name):
     c = G.load(name)
     tol = TOL.get(name, 1e-12)
-    s = P.Settings(max_forest_length=c.max_forest_length, cont_logl_order=c.marg[0],
-                   cont_l_order=c.marg[1])
+    s = c.port_settings(P)
     keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
     tvs = [P.table_view(t, c.bins, c.nv, c.lenv, c.nzp) for t in c.tables]
     results = []

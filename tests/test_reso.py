@@ -42,8 +42,7 @@ def test_preprocessing_rejects_bad_arguments(engine_lib):
 
 
 def _port_results(c, theta):
-    s = P.Settings(max_forest_length=c.max_forest_length, cont_logl_order=c.marg[0],
-                   cont_l_order=c.marg[1])
+    s = c.port_settings(P)
     keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
     tv = P.table_view(c.tables[0], c.bins, c.nv, c.lenv, c.nzp)
     out = []
