@@ -260,6 +260,29 @@ int lqg_last_timings(const lqg_ctx *ctx, double *ms, int n);
 int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
                   const double *solver_invfisher, double *mean, double *cov, double *fisher_cov,
                   double *realizations);
+/* The complete bootstrap (FastBootstrap 0, PoissonBootstrapper::_oneBoot and
+ * _meanBootstrap, core/bootstrapper.hpp:126-135, 217-257, 291-345): realization
+ * b draws one coefficient per spectrum (spectra in order, realizations in
+ * order) and solves F_b x_b = r_b with F_b = sum_q p_bq F_q and r_b = sum_q
+ * p_bq theta_q, F_q the upper sum of the spectrum's chunk Fisher matrices
+ * (collapseBootstrap, core/one_qso_estimate.cpp:225-235), by Cholesky with
+ * zero-diagonal bins held out (LAPACKE_safeSolveCho,
+ * mathtools/matrix_helper.cpp:385-396).  Realizations whose F_b is not
+ * positive definite are dropped; the valid ones fill the slots of
+ * realizations [nboots][nkz] in order (a failed last realization leaves its
+ * unsolved sum in the next slot, zeros after it, as the reference's buffer
+ * holds them), *n_valid receives their number, mean [nkz] = sum of all slots /
+ * n_valid and cov [nkz^2] = sum over all slots of (x - mean)(x - mean)^T /
+ * (n_valid - 1).  nkz <= 1023.  FP64 on the device; synchronous;
+ * LQG_ERR_STATE when fewer than two realizations are valid. */
+int lqg_bootstrap_complete(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots,
+                           unsigned long long seed, double *mean, double *cov, double *realizations,
+                           int *n_valid);
+/* The Poisson coefficients either bootstrap draws, p[q * nboots + b]: host
+ * only (per_realization = 0: FastBootstrap's order, 1: the complete
+ * bootstrap's). */
+int lqg_bootstrap_coefficients(int n_qso, int nboots, unsigned long long seed, int per_realization,
+                               unsigned char *p);
 /* Number of kernel launches the last lqg_nr_iteration enqueued. */
 int lqg_last_launch_count(const lqg_ctx *ctx);
 /* Number of size-bucketed waves of the last iteration: each phase-B kernel

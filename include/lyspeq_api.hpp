@@ -176,6 +176,7 @@ public:
     std::vector<double> fisher_matrix_halved;
     // bootstrap(): mean of the realizations, covariance / 4, F^-1 (covariance / 4) F^-T
     std::vector<double> bootstrap_mean, bootstrap_fisher_covariance, bootstrap_covariance;
+    int bootstrap_valid = 0;
     std::vector<std::unique_ptr<OneQSOEstimate>> local_queue;
     int damped = 0, dof = 0;
     double damp = 0;
@@ -400,20 +401,30 @@ public:
         std::remove(out.c_str());
     }
 
-    // PoissonBootstrapper with FastBootstrap after the last iteration
-    // (core/quadratic_estimate.cpp:536-545) over this estimator's spectra:
-    // bootstrap_mean, bootstrap_fisher_covariance (covariance / 4) and
-    // bootstrap_covariance (F^-1 (covariance / 4) F^-T).
-    void bootstrap(int number_of_boots, unsigned long long seed = 0) {
+    // PoissonBootstrapper after the last iteration (core/quadratic_estimate.cpp:536-545)
+    // over this estimator's spectra.  FastBootstrap (the default): bootstrap_mean,
+    // bootstrap_fisher_covariance (covariance / 4) and bootstrap_covariance
+    // (F^-1 (covariance / 4) F^-T).  FastBootstrap 0 (fast = false): a Fisher
+    // solve per realization; bootstrap_mean and bootstrap_covariance of the
+    // solved realizations, bootstrap_valid of them valid.
+    void bootstrap(int number_of_boots, unsigned long long seed = 0, bool fast = true) {
         std::vector<int> off(1, 0);
         for (const auto &q : local_queue) off.push_back(off.back() + (int) q->chunks.size());
         bootstrap_mean.assign(nkz_, 0.0);
         bootstrap_covariance.assign((size_t) nkz_ * nkz_, 0.0);
         bootstrap_fisher_covariance.assign((size_t) nkz_ * nkz_, 0.0);
+        if (!fast) {
+            check(lqg_bootstrap_complete(ctx_.get(), (int) local_queue.size(), off.data(), number_of_boots, seed,
+                                         bootstrap_mean.data(), bootstrap_covariance.data(), nullptr,
+                                         &bootstrap_valid),
+                  "lqg_bootstrap_complete");
+            return;
+        }
         check(lqg_bootstrap(ctx_.get(), (int) local_queue.size(), off.data(), number_of_boots, seed,
                             solver_invfisher_matrix.get(), bootstrap_mean.data(), bootstrap_covariance.data(),
                             bootstrap_fisher_covariance.data(), nullptr),
               "lqg_bootstrap");
+        bootstrap_valid = number_of_boots;
     }
 
     // invertTotalFisherMatrix + computePowerSpectrumEstimates

@@ -978,6 +978,12 @@ int run_fast_bootstrap(cudaStream_t st, const ChunkDesc *d_meta, const double *d
                        int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
                        const double *solver, double *mean, double *cov, double *fisher_cov, double *realizations,
                        std::string &err);
+int run_complete_bootstrap(cudaStream_t st, const ChunkDesc *d_meta, const double *d_results, int nkz,
+                           int n_chunks, const int *chunk_fis, const int *chunk_nq, int n_qso,
+                           const int *qso_offsets, int nboots, unsigned long long seed, double *mean, double *cov,
+                           double *realizations, int *n_valid, std::string &err);
+int draw_coefficients(unsigned long long seed, int n_qso, int nboots, bool per_realization, unsigned char *p,
+                      std::string &err);
 }
 
 extern "C" int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
@@ -990,6 +996,31 @@ extern "C" int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, in
     return lqg::run_fast_bootstrap(ctx->stream, ctx->d_meta.as<ChunkDesc>(), ctx->d_results.as<double>(), ctx->nkz,
                                    (int) ctx->chunks.size(), n_qso, qso_offsets, nboots, seed, solver_invfisher,
                                    mean, cov, fisher_cov, realizations, ctx->err);
+}
+
+extern "C" int lqg_bootstrap_complete(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots,
+                                      unsigned long long seed, double *mean, double *cov, double *realizations,
+                                      int *n_valid) {
+    if (!ctx || n_qso < 0 || !qso_offsets || nboots < 2)
+        return set_err(ctx, LQG_ERR_ARG, "lqg_bootstrap_complete: bad arguments");
+    if (!ctx->have_results)
+        return set_err(ctx, LQG_ERR_STATE, "lqg_bootstrap_complete: no iteration on this batch yet");
+    cudaSetDevice(ctx->device);
+    std::vector<int> fis(ctx->chunks.size()), nq(ctx->chunks.size());
+    for (size_t c = 0; c < ctx->chunks.size(); ++c) {
+        fis[c] = ctx->chunks[c].fis;
+        nq[c] = ctx->chunks[c].nq;
+    }
+    return lqg::run_complete_bootstrap(ctx->stream, ctx->d_meta.as<ChunkDesc>(), ctx->d_results.as<double>(),
+                                       ctx->nkz, (int) ctx->chunks.size(), fis.data(), nq.data(), n_qso,
+                                       qso_offsets, nboots, seed, mean, cov, realizations, n_valid, ctx->err);
+}
+
+extern "C" int lqg_bootstrap_coefficients(int n_qso, int nboots, unsigned long long seed, int per_realization,
+                                          unsigned char *p) {
+    if (n_qso < 0 || nboots < 0 || !p) return LQG_ERR_ARG;
+    std::string err;
+    return lqg::draw_coefficients(seed, n_qso, nboots, per_realization != 0, p, err);
 }
 
 extern "C" int lqg_last_wave_count(const lqg_ctx *ctx) { return ctx ? ctx->waves : 0; }

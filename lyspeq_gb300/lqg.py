@@ -24,7 +24,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
            "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate",
-           "lqg_bootstrap", "lqg_smooth_ivar"]
+           "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients"]
 
 
 class LqgBins(C.Structure):
@@ -75,6 +75,9 @@ def load_library(path: str = LIB_PATH):
                                         dp, C.c_int, dp, dp, C.c_int]
     lib.lqg_bootstrap.argtypes = [vp, C.c_int, ip, C.c_int, C.c_ulonglong, dp, dp, dp, dp, dp]
     lib.lqg_smooth_ivar.argtypes = [C.c_int, dp, C.c_int, dp]
+    lib.lqg_bootstrap_complete.argtypes = [vp, C.c_int, ip, C.c_int, C.c_ulonglong, dp, dp, dp, ip]
+    lib.lqg_bootstrap_coefficients.argtypes = [C.c_int, C.c_int, C.c_ulonglong, C.c_int,
+                                               C.POINTER(C.c_ubyte)]
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
@@ -212,6 +215,18 @@ class Engine:
         self._check(rc, "lqg_bootstrap")
         return dict(mean=mean, fisher_cov=fcov, cov=cov, realizations=real)
 
+    def bootstrap_complete(self, qso_offsets, nboots, seed=0):
+        """The complete bootstrap (lqg_bootstrap_complete): mean, cov, the
+        realization slots and the number of valid realizations."""
+        off = np.ascontiguousarray(qso_offsets, dtype=np.int32)
+        nkz = self.nkz
+        mean, cov, real = np.zeros(nkz), np.zeros((nkz, nkz)), np.zeros((nboots, nkz))
+        nv = C.c_int(0)
+        rc = self.lib.lqg_bootstrap_complete(self.h, len(off) - 1, _iptr(off), int(nboots), int(seed), _dptr(mean),
+                                             _dptr(cov), _dptr(real), C.byref(nv))
+        self._check(rc, "lqg_bootstrap_complete")
+        return dict(mean=mean, cov=cov, realizations=real, n_valid=nv.value)
+
     def clear(self):
         self._check(self.lib.lqg_batch_clear(self.h), "lqg_batch_clear")
 
@@ -274,6 +289,17 @@ class Engine:
 
     def wave_count(self):
         return self.lib.lqg_last_wave_count(self.h)
+
+
+def bootstrap_coefficients(n_qso, nboots, seed=0, per_realization=False):
+    """The Poisson coefficients of the bootstraps, p[q, b] (host only)."""
+    lib = load_library()
+    p = np.zeros((n_qso, nboots), dtype=np.uint8)
+    rc = lib.lqg_bootstrap_coefficients(int(n_qso), int(nboots), int(seed), int(bool(per_realization)),
+                                        p.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_bootstrap_coefficients failed with {rc}")
+    return p
 
 
 def smooth_ivar(ivar, sigmapix):

@@ -739,3 +739,55 @@ def newton_raphson_step(fsum, dbt):
     theta = w[0] - w[1] - w[2]
     return dict(fisher=f, solver=solver, inverse=sinv, theta=theta, warn=warn, dof=dof, damp=damp,
                 weighted=w)
+
+
+# ---------------------------------------------------------------------------
+# Complete bootstrap (FastBootstrap 0): core/bootstrapper.hpp:126-135,
+# 217-257, 291-345, core/one_qso_estimate.cpp:200-238, one_qso_estimate.hpp:43-53
+
+def complete_bootstrap(nkz, chunks, qso_offsets, p):
+    """chunks: per batch chunk (fisher_index_start, nq, d, b, t, F upper);
+    qso_offsets: spectrum q owns chunks [off[q], off[q+1]); p[q, b]: the
+    coefficient of spectrum q in realization b.  Returns (slots, n_valid,
+    mean, cov) as PoissonBootstrapper leaves them."""
+    from scipy.linalg import cho_factor, cho_solve
+    nq_, nb = p.shape
+    blocks = []
+    for q in range(nq_):
+        cs = chunks[qso_offsets[q]:qso_offsets[q + 1]]
+        if not cs:
+            blocks.append((0, np.zeros(0), np.zeros((0, 0))))
+            continue
+        lo = min(c[0] for c in cs)
+        hi = max(c[0] + c[1] for c in cs)
+        th, fq = np.zeros(hi - lo), np.zeros((hi - lo, hi - lo))
+        for fis, nq, d, b, t, f in cs:
+            o = fis - lo
+            th[o:o + nq] += (d - b) - t
+            fq[o:o + nq, o:o + nq] += np.triu(f)
+        blocks.append((lo, th, fq))
+    slots = np.zeros((nb, nkz))
+    nvalid = 0
+    for jj in range(nb):
+        power, fisher = np.zeros(nkz), np.zeros((nkz, nkz))
+        for q, (lo, th, fq) in enumerate(blocks):
+            if p[q, jj] == 0:
+                continue
+            m = len(th)
+            fisher[lo:lo + m, lo:lo + m] += p[q, jj] * fq
+            power[lo:lo + m] += p[q, jj] * th
+        slots[nvalid] = power
+        empty = np.flatnonzero(np.diag(fisher) == 0)
+        fisher[empty, empty] = 1.0
+        full = np.triu(fisher) + np.triu(fisher, 1).T
+        try:
+            x = cho_solve(cho_factor(full, lower=False), power)
+        except np.linalg.LinAlgError:
+            continue
+        x[empty] = 0.0
+        slots[nvalid] = x
+        nvalid += 1
+    mean = np.cumsum(slots, axis=0)[-1] * (1.0 / nvalid)
+    v = slots - mean
+    cov = (v.T @ v) * (1.0 / (nvalid - 1))
+    return slots, nvalid, mean, cov

@@ -39,7 +39,7 @@
 // the estimate by the smbivspline.py script between them; the script must be
 // on PATH), and dumps the estimator's final state.
 //
-// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso] [--boot N] [--iterate]
+// Usage: chunk_driver <config> <out.bin> [--no-pixels] [--reso] [--boot N [--boot-complete]] [--iterate]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -125,12 +125,13 @@ int main(int argc, char *argv[]) {
     }
     bool dump_pixels = true, reso = false;
     int nboots = 0;
-    bool nr_loop = false;
+    bool nr_loop = false, boot_complete = false;
     for (int a = 3; a < argc; ++a) {
         if (std::strcmp(argv[a], "--iterate") == 0) { nr_loop = true; continue; }
         if (std::strcmp(argv[a], "--no-pixels") == 0) dump_pixels = false;
         else if (std::strcmp(argv[a], "--reso") == 0) reso = true;
         else if (std::strcmp(argv[a], "--boot") == 0 && a + 1 < argc) nboots = std::atoi(argv[++a]);
+        else if (std::strcmp(argv[a], "--boot-complete") == 0) boot_complete = true;
     }
 
     ConfigFile config;
@@ -274,7 +275,21 @@ int main(int argc, char *argv[]) {
     putD(out, pfid.data(), nkz);
     putD(out, &t_chunks, 1);
     putD(out, &t_global, 1);
-    if (nboots > 0) {
+    if (nboots > 0 && boot_complete) {
+        // core/quadratic_estimate.cpp:536-545 with FastBootstrap 0: a Cholesky
+        // solve of the bootstrapped Fisher matrix per realization
+        specifics::FAST_BOOTSTRAP = false;
+        PoissonBootstrapper pbooter(nboots, solver.get());
+        for (auto &q : qsos) q->collapseBootstrap();
+        pbooter.run(qsos);
+        std::fwrite("BOOT0002", 1, 8, out);
+        putI(out, nboots);
+        putI(out, (int) qsos.size());
+        putI(out, (int) pbooter.remaining_boots);
+        putD(out, pbooter.temppower.get(), nkz);                         // mean of the realizations
+        putD(out, pbooter.tempfisher.get(), (size_t) nkz * nkz);         // covariance
+        putD(out, pbooter.allpowers.get(), (size_t) nboots * nkz);       // realizations (solved)
+    } else if (nboots > 0) {
         // core/quadratic_estimate.cpp:536-545 with FastBootstrap (the default)
         specifics::FAST_BOOTSTRAP = true;
         PoissonBootstrapper pbooter(nboots, solver.get());

@@ -67,6 +67,8 @@ class RefDump:
     boot_cov: np.ndarray | None = None         # F^-1 (cov / 4) F^-T
     boot_real: np.ndarray | None = None        # realizations [nboots][nkz]
     n_qso: int = 0
+    boot_complete: bool = False                # FastBootstrap 0: boot_cov is the covariance itself
+    boot_valid: int = 0                        # realizations whose Fisher solve succeeded
 
 
 class _Reader:
@@ -126,9 +128,12 @@ def read_dump(path: str) -> RefDump:
     dump = RefDump(nkz, nk, nz, chunks, fisher, dbt, solver, invf, theta, damped, dof, damp,
                    pfid, t_chunks, t_global)
     if r.pos < len(r.buf):
-        r.magic(b"BOOT0001")
+        complete = r.buf[r.pos:r.pos + 8] == b"BOOT0002"
+        r.magic(b"BOOT0002" if complete else b"BOOT0001")
         nb, nq = r.i(), r.i()
         dump.n_qso = nq
+        dump.boot_complete = complete
+        dump.boot_valid = r.i() if complete else nb
         dump.boot_mean = r.d(nkz)
         dump.boot_cov = r.d(nkz * nkz).reshape(nkz, nkz)
         dump.boot_real = r.d(nb * nkz).reshape(nb, nkz)
@@ -163,7 +168,8 @@ def read_iteration(path: str) -> RefIteration:
 
 
 def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None,
-               reso: bool = False, boots: int = 0, iterate: bool = False) -> RefDump:
+               reso: bool = False, boots: int = 0, iterate: bool = False,
+               boot_complete: bool = False) -> RefDump:
     env = dict(os.environ)
     env.setdefault("OPENBLAS_NUM_THREADS", "1")
     # One OpenMP thread: with more, Chunk::_applyRedshiftInterp races on the
@@ -171,7 +177,8 @@ def run_driver(config: str, out: str, pixels: bool = True, threads: int | None =
     # redshift weights of some rows come out wrong from run to run.
     env["OMP_NUM_THREADS"] = str(threads or 1)
     args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else []) \
-        + (["--boot", str(boots)] if boots else []) + (["--iterate"] if iterate else [])
+        + (["--boot", str(boots)] if boots else []) + (["--boot-complete"] if boot_complete else []) \
+        + (["--iterate"] if iterate else [])
     if iterate:
         # lyspeq's smoothing step runs its script smbivspline.py from PATH
         wrap = os.path.join(os.path.dirname(os.path.abspath(out)), "bin")

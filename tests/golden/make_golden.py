@@ -42,6 +42,8 @@ CASES = {
     "tiny_reso_dia": ("tiny_reso_dia", None, (-1, -1), 0.0, None),
     # lyspeq's FastBootstrap (200 realizations) after the iteration of tiny_marg1
     "tiny_boot": ("tiny", None, (1, -1), 0.0, None, 200),
+    # the complete bootstrap (FastBootstrap 0: a Fisher solve per realization)
+    "tiny_boot_complete": ("tiny", None, (1, -1), 0.0, None, 100),
     # lyspeq's full Newton-Raphson loop (NumberOfIterations 4, smoothing between)
     "tiny_iter": ("tiny", None, (1, -1), 0.0, None, 0, 4),
     # noise-weight smoothing (Gaussian, and the mean) and redshift growth
@@ -92,7 +94,7 @@ def make_case(name, spec):
                     text += f"{key} {val}\n"
             open(cfg, "w").write(text)
         dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso, boots=boots,
-                                  iterate=iters > 1)
+                                  iterate=iters > 1, boot_complete=name.endswith("_complete"))
         it = refdump.read_iteration(os.path.join(tmp, "dump.bin.iter")) if iters > 1 else None
     chunks = dump.chunks
     if keep is not None:
@@ -123,6 +125,7 @@ def make_case(name, spec):
         out["boot_real"] = dump.boot_real
         out["boot_qso"] = np.array([c.qso for c in chunks], dtype=np.int32)
         out["boot_nqso"] = np.array(dump.n_qso)
+        out["boot_complete"] = np.array([int(dump.boot_complete), dump.boot_valid])
     if w.reso:
         # resolution-matrix case: the reader's options, every spectrum's raw
         # matrix and wavelengths (for the preprocessing parity) and, per chunk,

@@ -84,7 +84,9 @@ def load(name: str) -> GoldenCase:
                        fisher=z["it_fisher"], inverse=z["it_inverse"], dbt=z["it_dbt"])
     if "boot_mean" in z.files:
         case.boot = dict(mean=z["boot_mean"], cov=z["boot_cov"], real=z["boot_real"],
-                         qso=z["boot_qso"], n_qso=int(z["boot_nqso"]))
+                         qso=z["boot_qso"], n_qso=int(z["boot_nqso"]),
+                         complete=bool(z["boot_complete"][0]) if "boot_complete" in z.files else False,
+                         valid=int(z["boot_complete"][1]) if "boot_complete" in z.files else len(z["boot_real"]))
     if "reso" in z.files:
         case.reso = (int(z["reso"][0]), float(z["reso"][1]))
         case.rmats = [z[f"c{i}_rmat"] for i in range(n)]
