@@ -175,6 +175,13 @@ int lqg_resomat_oversample(int n, int ndiags, const double *values, int osamp, d
  * cells beyond them at 0, so unless the last pixel is masked the last 25
  * pixels come out with ivar 0.  Host only; out may not alias ivar. */
 int lqg_smooth_ivar(int n, const double *ivar, int sigmapix, double *out);
+/* Smoother::smooth1D (mathtools/smoother.cpp:144-168) on each of the ndiags
+ * diagonals of a DiaMatrix values[ndiags][n], in place: what
+ * OneQSOEstimate::_readQsoFile does before deconvolution when
+ * SmoothResolutionMatrix > 0 and SmoothNoiseWeights >= 0
+ * (core/one_qso_estimate.cpp:79-81).  sigmapix = SmoothNoiseWeights; the
+ * padding is the one lqg_smooth_ivar describes.  Host only. */
+int lqg_resomat_smooth(int n, int ndiags, double *values, int sigmapix);
 /* SQ lookup tables on the GPU: SQLookupTable::computeTables
  * (core/sq_table.cpp:201-323, CreateSQLookUpTable), for n_tables (R, dv)
  * pairs on the grids lqg_tables describes (nv points over [0, v_length], nzp

@@ -99,6 +99,7 @@ struct Specifics {
     int oversampling = -1;              // OversampleRmat
     double resomat_deconvolution_m = 0; // ResoMatDeconvolutionM
     int smooth_noise_weights = -1;      // SmoothNoiseWeights
+    bool smooth_resolution_matrix = false;  // SmoothResolutionMatrix > 0 (needs SmoothNoiseWeights >= 0)
     bool redshift_growth_on = false;    // RedshiftGrowthOn > 0 (exponent: fiducial[3])
     double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
 };
@@ -253,12 +254,15 @@ public:
         const int before = lqg_batch_size(ctx_.get());
         if (sp_.use_reso_matrix) {
             // Resolution matrix as OneQSOEstimate::_readQsoFile prepares it
-            // (core/one_qso_estimate.cpp:75-89): deconvolution and oversampling on
-            // the whole spectrum, then one row (or column of diagonals) per pixel
+            // (core/one_qso_estimate.cpp:75-89): smoothing, deconvolution and
+            // oversampling on the whole spectrum, then one row (or column of
+            // diagonals) per pixel
             const int nd = q.ndiags;
             if (nd < 1 || q.resomat.size() != (size_t) nd * n0)
                 throw std::invalid_argument("QSOSpectrum resomat must hold ndiags x n values");
             std::vector<double> vals = q.resomat;
+            if (sp_.smooth_resolution_matrix && sp_.smooth_noise_weights >= 0)
+                check(lqg_resomat_smooth((int) n0, nd, vals.data(), sp_.smooth_noise_weights), "lqg_resomat_smooth");
             if (sp_.resomat_deconvolution_m > 0)
                 check(lqg_resomat_deconvolve((int) n0, nd, vals.data(), sp_.resomat_deconvolution_m),
                       "lqg_resomat_deconvolve");

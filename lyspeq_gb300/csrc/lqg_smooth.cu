@@ -1,4 +1,5 @@
-// Noise-weight smoothing of a chunk's ivar (SmoothNoiseWeights), host side.
+// Noise-weight smoothing of a chunk's ivar (SmoothNoiseWeights) and of a
+// resolution matrix's diagonals (SmoothResolutionMatrix), host side.
 //
 // lyspeq builds the covariance with a smoothed ivar when SmoothNoiseWeights >= 0
 // (Chunk::setInvertCovarianceMatrix, core/chunk_estimate.cpp:685-691, calling
@@ -98,7 +99,52 @@ int smooth_ivar(int n, const double *ivar, int sigmapix, double *out) {
     return LQG_OK;
 }
 
+// Smoother::smooth1D (mathtools/smoother.cpp:144-168) over `rows` rows of n
+// values each (a resolution matrix's diagonals, SmoothResolutionMatrix):
+// sigmapix = 0 replaces a row by the mean of its values <= 1e3; sigmapix > 0
+// convolves it with the 51-tap Gaussian after the same padding as above
+// (left pad the first value, right pad over the last 25 values, zeros past them).
+int smooth_rows(int n, int rows, double *values, int sigmapix) {
+    if (n <= 0 || rows <= 0 || !values || sigmapix < 0) return LQG_ERR_ARG;
+    double g[kTaps], gs = 0;
+    for (int k = 0; k < kTaps; ++k) {
+        const double x = (k - kHw) * 1. / sigmapix;
+        g[k] = sigmapix > 0 ? std::exp(-(x * x) / 2) : 0.0;
+        gs += g[k];
+    }
+    if (sigmapix > 0)
+        for (double &v : g) v /= gs;
+    std::vector<double> pad(n + 2 * kHw);
+    for (int r = 0; r < rows; ++r) {
+        double *row = values + (size_t) r * n;
+        if (sigmapix == 0) {
+            std::vector<double> v(row, row + n);
+            std::sort(v.begin(), v.end());
+            int m = n;
+            while (m > 0 && v[m - 1] > 1e3) --m;
+            double sum = 0;
+            for (int i = 0; i < m; ++i) sum += v[i];
+            std::fill(row, row + n, sum / m);
+            continue;
+        }
+        std::fill(pad.begin(), pad.end(), 0.0);
+        std::copy(row, row + n, pad.begin() + kHw);
+        std::fill(pad.begin(), pad.begin() + kHw, row[0]);
+        std::fill(pad.begin() + n, pad.begin() + n + kHw, row[n - 1]);
+        for (int i = 0; i < n; ++i) {
+            double acc = 0;
+            for (int k = 0; k < kTaps; ++k) acc += g[k] * pad[i + k];
+            row[i] = acc;
+        }
+    }
+    return LQG_OK;
+}
+
 }  // namespace lqg
+
+extern "C" int lqg_resomat_smooth(int n, int ndiags, double *values, int sigmapix) {
+    return lqg::smooth_rows(n, ndiags, values, sigmapix);
+}
 
 extern "C" int lqg_smooth_ivar(int n, const double *ivar, int sigmapix, double *out) {
     if (out == ivar) return LQG_ERR_ARG;

@@ -24,7 +24,8 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_nr_iteration", "lqg_download", "lqg_chunk_result", "lqg_fisher_solve",
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
            "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate",
-           "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients"]
+           "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients",
+           "lqg_resomat_smooth"]
 
 
 class LqgBins(C.Structure):
@@ -75,6 +76,7 @@ def load_library(path: str = LIB_PATH):
                                         dp, C.c_int, dp, dp, C.c_int]
     lib.lqg_bootstrap.argtypes = [vp, C.c_int, ip, C.c_int, C.c_ulonglong, dp, dp, dp, dp, dp]
     lib.lqg_smooth_ivar.argtypes = [C.c_int, dp, C.c_int, dp]
+    lib.lqg_resomat_smooth.argtypes = [C.c_int, C.c_int, dp, C.c_int]
     lib.lqg_bootstrap_complete.argtypes = [vp, C.c_int, ip, C.c_int, C.c_ulonglong, dp, dp, dp, ip]
     lib.lqg_bootstrap_coefficients.argtypes = [C.c_int, C.c_int, C.c_ulonglong, C.c_int,
                                                C.POINTER(C.c_ubyte)]
@@ -311,6 +313,17 @@ def smooth_ivar(ivar, sigmapix):
     if rc != LQG_OK:
         raise RuntimeError(f"lqg_smooth_ivar failed with {rc}")
     return out
+
+
+def resomat_smooth(values, sigmapix):
+    """Smoother::smooth1D on each diagonal through the library (host only): values[ndiags][n]."""
+    lib = load_library()
+    v = np.array(values, dtype=np.float64, order="C")
+    nd, n = v.shape
+    rc = lib.lqg_resomat_smooth(n, nd, _dptr(v), int(sigmapix))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_resomat_smooth failed with {rc}")
+    return v
 
 
 def resomat_deconvolve(values, m):

@@ -121,11 +121,12 @@ def preprocess_spectrum(spec, bins, reso=None):
     (sigma -> ivar), :189-230 (maskOutliers), :159-187 (cutBoundary) and
     core/one_qso_estimate.cpp:52-100.  Returns (wave, delta, ivar) in
     Angstrom, or raises ValueError when the reference would drop the file.
-    With reso = (oversampling, deconvolution m) the spectrum's resolution
-    matrix is deconvolved and oversampled before the cut
-    (core/one_qso_estimate.cpp:75-89) and a fourth item, the matrix cut with
-    the pixels (rows [n][nelem] when oversampled, else values[ndiags][n]),
-    is returned."""
+    With reso = (oversampling, deconvolution m[, smoothing sigma]) the
+    spectrum's resolution matrix is smoothed (sigma >= 0:
+    SmoothResolutionMatrix with SmoothNoiseWeights sigma), deconvolved and
+    oversampled before the cut (core/one_qso_estimate.cpp:75-89) and a fourth
+    item, the matrix cut with the pixels (rows [n][nelem] when oversampled,
+    else values[ndiags][n]), is returned."""
     wave = np.array(spec.wave, dtype=np.float64)
     delta = np.array(spec.delta, dtype=np.float64)
     ivar = 1.0 / (np.asarray(spec.sigma, dtype=np.float64) ** 2)
@@ -145,8 +146,10 @@ def preprocess_spectrum(spec, bins, reso=None):
             ivar[i] = 0.0
     rm = None
     if reso is not None:
-        osamp, m = reso
+        osamp, m = reso[:2]
         vals = np.array(spec.resomat, dtype=np.float64)
+        if len(reso) > 2 and reso[2] >= 0:
+            vals = smooth_rows(vals, reso[2])
         if m > 0:
             vals = dia_deconvolve(vals, m)
         if osamp > 0:
@@ -502,6 +505,33 @@ def smooth_ivar(ivar, sigmapix):
         with np.errstate(divide="ignore", invalid="ignore"):
             out = 1.0 / (win @ g)
     out[masked] = ivar[masked]
+    return out
+
+
+def smooth_rows(values, sigmapix):
+    """Smoother::smooth1D (mathtools/smoother.cpp:144-168) on every row of
+    values (a DiaMatrix's diagonals): sigmapix = 0 the mean of the row's values
+    <= 1e3, else the 51-tap Gaussian convolution after padArray's padding."""
+    out = np.array(values, dtype=np.float64)
+    hw = SMOOTH_HWSIZE
+    x = np.arange(-hw, hw + 1) * 1.0 / max(sigmapix, 1)
+    g = np.exp(-(x * x) / 2)
+    g = g / float(np.cumsum(g)[-1])
+    for r in range(out.shape[0]):
+        row = out[r]
+        n = len(row)
+        if sigmapix == 0:
+            a = np.sort(row)
+            m = len(a)
+            while m and a[m - 1] > 1e3:
+                m -= 1
+            out[r] = float(np.cumsum(a[:m])[-1]) / m
+            continue
+        pad = np.zeros(n + 2 * hw)
+        pad[hw:hw + n] = row
+        pad[:hw] = row[0]
+        pad[n:n + hw] = row[-1]
+        out[r] = np.lib.stride_tricks.sliding_window_view(pad, 2 * hw + 1) @ g
     return out
 
 

@@ -96,6 +96,9 @@ std::unique_ptr<OneQSOEstimate> read_with_resomat(const std::string &path) {
         size_t got = std::fread(qFile->Rmat->matrix(), sizeof(double), nval, rf);
         std::fclose(rf);
         if (got != nval) throw std::runtime_error("short resolution matrix file");
+        if (process::smoother->isSmoothingOnRmat())
+            process::smoother->smooth1D(qFile->Rmat->matrix(), qFile->Rmat->getNCols(),
+                                        qFile->Rmat->getNElemPerRow());
         if (specifics::RESOMAT_DECONVOLUTION_M > 0)
             qFile->Rmat->deconvolve(specifics::RESOMAT_DECONVOLUTION_M);
         if (specifics::OVERSAMPLING_FACTOR > 0)

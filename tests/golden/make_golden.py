@@ -50,6 +50,9 @@ CASES = {
     "tiny_smooth": ("tiny", None, (1, -1), 0.04, None),
     "tiny_smooth_mean": ("tiny", None, (-1, -1), 0.0, None),
     "tiny_reso_growth": ("tiny_reso", None, (-1, -1), 0.0, None),
+    # SmoothResolutionMatrix (the matrices' diagonals smoothed before
+    # deconvolution) with SmoothNoiseWeights 2
+    "tiny_reso_smooth": ("tiny_reso", None, (-1, -1), 0.0, None),
 }
 
 # config keys set for a case: SmoothNoiseWeights and RedshiftGrowthOn
@@ -58,6 +61,7 @@ OPTIONS = {
     "tiny_smooth": {"SmoothNoiseWeights": 3},
     "tiny_smooth_mean": {"SmoothNoiseWeights": 0},
     "tiny_reso_growth": {"RedshiftGrowthOn": 1},
+    "tiny_reso_smooth": {"SmoothNoiseWeights": 2, "SmoothResolutionMatrix": 1},
 }
 
 
@@ -113,7 +117,8 @@ def make_case(name, spec):
         g_complete=np.array(keep is None),
         # SmoothNoiseWeights, RedshiftGrowthOn, FiducialRedshiftPower
         opts=np.array([OPTIONS.get(name, {}).get("SmoothNoiseWeights", -1),
-                       OPTIONS.get(name, {}).get("RedshiftGrowthOn", -1), w.fid[3]], dtype=float),
+                       OPTIONS.get(name, {}).get("RedshiftGrowthOn", -1), w.fid[3],
+                       OPTIONS.get(name, {}).get("SmoothResolutionMatrix", -1)], dtype=float),
     )
     if it is not None:
         out["it_n"] = np.array(iters)

@@ -10,8 +10,9 @@ from lyspeq_gb300 import synth
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub",
-         "tiny_reso", "tiny_reso_dia", "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth"]
-RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth"]
+         "tiny_reso", "tiny_reso_dia", "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth",
+         "tiny_reso_smooth"]
+RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth", "tiny_reso_smooth"]
 
 
 @dataclasses.dataclass
@@ -42,6 +43,7 @@ class GoldenCase:
     # SmoothNoiseWeights, RedshiftGrowthOn and its exponent, as Engine keywords
     opts: dict = dataclasses.field(default_factory=lambda: dict(smooth_noise_weights=-1, redshift_growth=False,
                                                                   fid_b=0.0))
+    smooth_rmat: bool = False
 
     def port_settings(self, P):
         """The oracle's Settings for this case."""
@@ -79,6 +81,8 @@ def load(name: str) -> GoldenCase:
     if "opts" in z.files:
         o = z["opts"]
         case.opts = dict(smooth_noise_weights=int(o[0]), redshift_growth=bool(o[1] > 0), fid_b=float(o[2]))
+        # SmoothResolutionMatrix: applied while the matrices are prepared
+        case.smooth_rmat = len(o) > 3 and o[3] > 0 and o[0] >= 0
     if "it_n" in z.files:
         case.nr = dict(n=int(z["it_n"]), theta=z["it_theta"], previous=z["it_prev"], fits=z["it_fits"],
                        fisher=z["it_fisher"], inverse=z["it_inverse"], dbt=z["it_dbt"])

@@ -119,6 +119,8 @@ def test_port_resolution_preprocessing_matches_reference(name):
     for i, (qso, start) in enumerate(c.src):
         if qso not in prepared:
             lam, vals = c.spectra[qso]
+            if c.smooth_rmat:
+                vals = P.smooth_rows(vals, c.opts["smooth_noise_weights"])
             v = P.dia_deconvolve(np.array(vals), m) if m > 0 else np.array(vals)
             prepared[qso] = P.dia_oversample(v, osamp, P._median(np.diff(lam))) if osamp > 0 else v
         n = c.meta[i][0]

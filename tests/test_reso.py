@@ -26,11 +26,22 @@ def test_library_preprocessing_matches_reference(engine_lib, name):
     for i, (qso, start) in enumerate(c.src):
         if qso not in prepared:
             lam, vals = c.spectra[qso]
+            if c.smooth_rmat:
+                vals = lqg.resomat_smooth(vals, c.opts["smooth_noise_weights"])
             v = lqg.resomat_deconvolve(vals, m) if m > 0 else np.array(vals)
             prepared[qso] = lqg.resomat_oversample(v, osamp, P._median(np.diff(lam))) if osamp > 0 else v
         n = c.meta[i][0]
         mine = prepared[qso][start:start + n] if osamp > 0 else prepared[qso][:, start:start + n]
         assert np.max(np.abs(mine - c.rmats[i])) < 1e-12
+
+
+@pytest.mark.parametrize("sigmapix", [0, 1, 4])
+def test_library_resomat_smoothing_matches_oracle(engine_lib, sigmapix):
+    from lyspeq_gb300 import lqg
+    rng = np.random.Generator(np.random.PCG64(8))
+    vals = rng.uniform(0, 0.3, size=(11, 140))
+    mine, ref = lqg.resomat_smooth(vals, sigmapix), P.smooth_rows(vals, sigmapix)
+    assert np.max(np.abs(mine - ref)) <= 1e-15
 
 
 def test_preprocessing_rejects_bad_arguments(engine_lib):
