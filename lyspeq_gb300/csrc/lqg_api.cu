@@ -787,6 +787,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
     base.n_fpix = (int64_t) ctx->h_flogw.size();
     base.reso_nelem = base.reso_os = 0;
+    base.growth = ctx->opts.redshift_growth_on > 0;
     {
         int ne = -1, os = -1;
         bool uniform = true;

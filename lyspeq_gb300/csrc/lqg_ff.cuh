@@ -32,12 +32,16 @@ __device__ __forceinline__ float zweight_ff(const DeviceBins &b, int zm, float P
     return r >= 0.f ? r * b.inv_dz : 0.f;
 }
 
-// zweight_ff times, with the growth option on, ((1 + z) / (1 + z_m))^B in
-// FP32 (the ratio is within 1e-7 relative, as the 22-bit operands need).
+// ((1 + z) / (1 + z_m))^B in FP32 (the ratio is within 1e-7 relative, as the
+// 22-bit operands need).
+__device__ __forceinline__ float growth_ff(const DeviceBins &b, int zm, float P, float E) {
+    return powf(__fdiv_rn(__fadd_rn(P, E), __fadd_rn(b.zc1_hi[zm], b.zc1_lo[zm])), (float) b.growth_b);
+}
+
+// zweight_ff times, with the growth option on, the growth factor.
 __device__ __forceinline__ float zfactor_ff(const DeviceBins &b, int zm, float P, float E) {
     float w = zweight_ff(b, zm, P, E);
-    if (b.growth && w != 0.f)
-        w *= powf(__fdiv_rn(__fadd_rn(P, E), __fadd_rn(b.zc1_hi[zm], b.zc1_lo[zm])), (float) b.growth_b);
+    if (b.growth && w != 0.f) w *= growth_ff(b, zm, P, E);
     return w;
 }
 

@@ -130,6 +130,7 @@ struct WaveArgs {
     int c_is_ff;                                     // S and C~ written as double-float pairs (mixed, no theta)
     const double *flogw, *fsqw, *rw;                 // resolution-matrix grids and weights
     int reso_nelem, reso_os;                         // shape shared by every resolution chunk, else 0
+    int growth;                                      // RedshiftGrowthOn (as DeviceBins::growth)
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
     const float2 *signal_ff;                         // signal table as double-float (mixed path)

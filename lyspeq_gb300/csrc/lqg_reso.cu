@@ -499,7 +499,10 @@ struct ResoSharedF {
 // time: each thread then keeps its column's weights, scaled by the column
 // phases, in registers and reads the cached sinc block directly (no slab of
 // Q_k is formed, one barrier per band).
-template <int NEL, int OS>
+//
+// GR: the redshift-growth factor is applied (a separate instantiation: its
+// code, even untaken, slows the register-bound loop of the others by a quarter).
+template <int NEL, int OS, bool GR>
 __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     ResoSharedF &sm = *reinterpret_cast<ResoSharedF *>(smraw);
@@ -553,7 +556,9 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
         if (valid[u]) two_prod_ff(sw2[min(gi, gj)], sw2[max(gi, gj)], zp[u], ze[u]);
 #pragma unroll
         for (int iz = 0; iz < 4; ++iz)
-            zw[u][iz] = (valid[u] && iz < nzb) ? zfactor_ff(bins, ch.zb0 + iz, zp[u], ze[u]) : 0.f;
+            zw[u][iz] = (valid[u] && iz < nzb) ? (GR ? zfactor_ff(bins, ch.zb0 + iz, zp[u], ze[u])
+                                                     : zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]))
+                                               : 0.f;
     }
     const float2 *ph = reinterpret_cast<const float2 *>(a.ws + ch.o_ph);
     const float mult = (I == J) ? 1.f : 2.f;
@@ -659,7 +664,10 @@ __global__ void __launch_bounds__(RTH, 2) k_build_q_reso_f32(WaveArgs a) {
                 for (int u = 0; u < 4; ++u) {
                     const int i = r8 + 8 * u, gi = I * RT + i;
                     float w = 0.f;
-                    if (valid[u]) w = iz < 4 ? zw[u][iz] : zfactor_ff(bins, ch.zb0 + iz, zp[u], ze[u]);
+                    if (valid[u])
+                        w = iz < 4 ? zw[u][iz]
+                                   : (GR ? zfactor_ff(bins, ch.zb0 + iz, zp[u], ze[u])
+                                         : zweight_ff(bins, ch.zb0 + iz, zp[u], ze[u]));
                     const float q = b[u] * w;
                     part[g] = fmaf(yy[u], q, part[g]);
                     const float x = q * qs;
@@ -820,11 +828,13 @@ void set_reso_attrs() {
     const int bytes = (int) sizeof(ResoShared);
     cudaFuncSetAttribute(k_build_s_c_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_build_q_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_build_q_reso_f32<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_build_q_reso_f32<0, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedF));
-    cudaFuncSetAttribute(k_build_q_reso_f32<31, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_build_q_reso_f32<0, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedF));
-    cudaFuncSetAttribute(k_build_q_reso_f32<11, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_build_q_reso_f32<31, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) sizeof(ResoSharedF));
+    cudaFuncSetAttribute(k_build_q_reso_f32<11, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedF));
     cudaFuncSetAttribute(k_build_s_c_reso_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedFF));
@@ -851,12 +861,14 @@ void launch_build_q_reso(WaveArgs &a, cudaStream_t st) {
         k_reso_phases<<<dim3(32, a.n_chunks), 256, 0, st>>>(a);
         // a fixed-width kernel when every resolution chunk of the batch has its shape
         const dim3 grid(nt * nt, a.n_chunks);
-        if (a.reso_nelem == 31 && a.reso_os == 3)
-            k_build_q_reso_f32<31, 3><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
+        if (a.growth)
+            k_build_q_reso_f32<0, 0, true><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
+        else if (a.reso_nelem == 31 && a.reso_os == 3)
+            k_build_q_reso_f32<31, 3, false><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
         else if (a.reso_nelem == 11 && a.reso_os == 1)
-            k_build_q_reso_f32<11, 1><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
+            k_build_q_reso_f32<11, 1, false><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
         else
-            k_build_q_reso_f32<0, 0><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
+            k_build_q_reso_f32<0, 0, false><<<grid, RTH, sizeof(ResoSharedF), st>>>(a);
         a.launches += 2;
     } else {
         k_build_q_reso<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoShared), st>>>(a);
