@@ -271,6 +271,9 @@ __global__ void __launch_bounds__(256) k_build_q(WaveArgs a) {
 constexpr int QM_PAIRS = 4;
 constexpr int kZGroup = 4;
 
+// GR: with the redshift-growth factor (its own instantiation, so that the
+// common case carries none of its code).
+template <bool GR>
 __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     const int c = blockIdx.y;
     const ChunkDesc &ch = a.chunks[c];
@@ -323,7 +326,9 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
         for (int g = 0; g < kZGroup; ++g)
 #pragma unroll
             for (int k = 0; k < E; ++k)
-                w[g][k] = (z0 + g < nzb && zp[k] > 0.f) ? zfactor_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k]) : 0.f;
+                w[g][k] = (z0 + g < nzb && zp[k] > 0.f) ? (GR ? zfactor_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k])
+                                                              : zweight_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k]))
+                                                         : 0.f;
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
             const float *row = rows + (size_t) kn * a.grid.nv;
             float base[E];
@@ -606,7 +611,10 @@ void launch_build_q(WaveArgs &a, cudaStream_t st) {
     int tiles = (a.max_ld / T64) * (a.max_ld / T64);
     if (a.precision == LQG_PRECISION_MIXED) {
         k_prep_mixed<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
-        k_build_q_mixed<<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
+        if (a.growth)
+            k_build_q_mixed<true><<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
+        else
+            k_build_q_mixed<false><<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
     } else {
         k_build_q<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
         k_wn_fp64<<<dim3(64, a.n_chunks), 256, 0, st>>>(a);
