@@ -59,9 +59,16 @@ extern "C" {
 
 /* arithmetic of the per-chunk products */
 #define LQG_PRECISION_FP64 0    /* everything in IEEE binary64 */
-#define LQG_PRECISION_MIXED 1   /* FP64 factorisation; C^-1 Q_k, Fisher and bias traces
-                                   on tensor cores as fp16 hi/lo split products (3 terms),
-                                   fp32 accumulation, fp64 reduction of partial sums */
+#define LQG_PRECISION_MIXED 1   /* df64 factorisation to W = P L^-1 D (C^-1 = W^T W, P the
+                                   continuum projector); B_k = W Q_k W^T on tensor cores as
+                                   fp16 hi/lo split products (3 terms, fp32 accumulation),
+                                   traces F_ij = <B_i, B_j> over B's upper triangle, fp64
+                                   reduction of partial sums */
+#define LQG_PRECISION_MIXED_DIRECT 2 /* as MIXED but with the direct products A_k = C^-1 Q_k
+                                   and F_ij = <A_i^T, A_j>: cheaper with continuum
+                                   marginalisation, less accurate at high signal to noise
+                                   (its errors grow with the ratio of signal to noise
+                                   power at low k) */
 
 typedef struct lqg_ctx lqg_ctx;
 

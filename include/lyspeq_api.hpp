@@ -49,7 +49,7 @@ constexpr double SPEED_OF_LIGHT = 299792.458;   // core/global_numbers.hpp
 constexpr double LYA_REST = 1215.67;
 constexpr int MIN_PIXELS_IN_FILE = 100;         // core/one_qso_estimate.cpp:14
 
-enum class Precision { FP64 = LQG_PRECISION_FP64, Mixed = LQG_PRECISION_MIXED };
+enum class Precision { FP64 = LQG_PRECISION_FP64, Mixed = LQG_PRECISION_MIXED, MixedDirect = LQG_PRECISION_MIXED_DIRECT };
 
 // bins:: (core/global_numbers.cpp:209-251)
 struct Binning {

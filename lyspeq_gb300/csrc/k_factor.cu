@@ -550,13 +550,12 @@ __device__ __forceinline__ double ipow(double x, int m) {
     return r;
 }
 
-// Continuum marginalisation: templates [1/sqrt(n), (ln w)^m, w^m] (each of unit
-// norm), their left singular vectors by one-sided Jacobi on the n x nv matrix,
-// vectors with s_i / s_0 <= 1e-15 dropped, then sequential rank-1 removal
-// C^-1 <- C^-1 - (C^-1 v)(C^-1 v)^T / (v^T C^-1 v).
-__device__ void marginalize_all(double *A, int ld, int n, const double *wave, int logl, int lord,
-                                double *V /* (2 kMaxContVecs + 1) * ld */, FactorSmem &s) {
-    double *y = V + kMaxContVecs * ld, *U = y + ld;
+// Continuum templates [1/sqrt(n), (ln w)^m, w^m] (each of unit norm) and their
+// left singular vectors by one-sided Jacobi on the n x nv matrix; vectors with
+// s_i / s_0 <= 1e-15 are dropped (Chunk::_addMarginalizations,
+// core/chunk_estimate.cpp:605-665).  The nuse vectors are left at U[u * ld].
+__device__ int cont_basis(int ld, int n, const double *wave, int logl, int lord, double *V, double *U,
+                          FactorSmem &s) {
     __shared__ double sv[kMaxContVecs], rot[2];
     __shared__ int order[kMaxContVecs], nuse_s, changed;
     int nv = 0;
@@ -640,6 +639,15 @@ __device__ void marginalize_all(double *A, int ld, int n, const double *wave, in
         for (int i = threadIdx.x; i < n; i += FTH) U[u * ld + i] = V[p * ld + i] * inv;
     }
     __syncthreads();
+    return nuse;
+}
+
+// Continuum marginalisation of C^-1: sequential rank-1 removal
+// C^-1 <- C^-1 - (C^-1 v)(C^-1 v)^T / (v^T C^-1 v) over the basis above.
+__device__ void marginalize_all(double *A, int ld, int n, const double *wave, int logl, int lord,
+                                double *V /* (2 kMaxContVecs + 1) * ld */, FactorSmem &s) {
+    double *y = V + kMaxContVecs * ld, *U = y + ld;
+    const int nuse = cont_basis(ld, n, wave, logl, lord, V, U, s);
     for (int u = 0; u < nuse; ++u) {
         const double *vv = U + u * ld;
         for (int i = threadIdx.x; i < n; i += FTH) {
@@ -657,6 +665,140 @@ __device__ void marginalize_all(double *A, int ld, int n, const double *wave, in
             if (j < n) A[e] += cnorm * y[i] * y[j];
         }
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Whitened factor of the mixed path.  With C~ = L L^T and D = diag(sqrt(ivar)),
+// C^-1 = T^T T for T = L^-1 D (lower triangular), and the marginalised inverse
+// is T^T P T with P = I - U U^T, U the orthonormal basis of {T v} for the
+// continuum templates v taken in the reference's order (the sequential
+// rank-1 removals of _addMarginalizations are Gram-Schmidt in this space).
+// The mixed products then work with W = P T, C^-1 = W^T W: F_ij =
+// tr(C^-1 Q_i C^-1 Q_j) = <W Q_i W^T, W Q_j W^T>_F.  Without marginalisation
+// W = T is lower triangular and the products skip its zero tiles.
+//
+// T from the df64 inverse factor, as FP64: A[i][j] = L^-1_ij sqrt(ivar_j) on
+// and below the diagonal, 0 elsewhere (padding included).
+__device__ void form_t_df(float2 *A2, int ld, int n, const double *ivar, double *sq) {
+    for (int i = threadIdx.x; i < n; i += FTH) sq[i] = sqrt(ivar[i]);
+    __syncthreads();
+    double *A = reinterpret_cast<double *>(A2);
+    for (size_t e = threadIdx.x; e < (size_t) ld * ld; e += FTH) {
+        const int i = (int) (e / ld), j = (int) (e % ld);
+        double v = 0.0;
+        if (j <= i && i < n) v = df_to_d(A2[e]) * sq[j];
+        A[e] = v;
+    }
+    __syncthreads();
+}
+
+// W = P T in place for the nuse plain-space template vectors U[u * ld]:
+// w_u = T U_u, orthonormalised in order (modified Gram-Schmidt) into Wh,
+// then W = T - Wh (Wh^T T).  Scratch: Wh and Z, nuse * ld each.  (Applying P
+// afterwards as rank-r corrections of the traces instead cancels most of the
+// low-k Fisher elements and loses their precision; W itself carries none.)
+__device__ void project_w(double *A, int ld, int n, const double *U, int nuse, double *Wh, double *Z,
+                          FactorSmem &s) {
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    for (int u = 0; u < nuse; ++u) {
+        // w = T U_u, one warp per row (T is lower triangular)
+        for (int i = warp; i < n; i += FTH / 32) {
+            double acc = 0;
+            const double *Ai = A + (size_t) i * ld;
+            for (int j = lane; j <= i; j += 32) acc += Ai[j] * U[u * ld + j];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0) Wh[u * ld + i] = acc;
+        }
+        __syncthreads();
+        for (int v = 0; v < u; ++v) {
+            double part = 0;
+            for (int i = threadIdx.x; i < n; i += FTH) part += Wh[v * ld + i] * Wh[u * ld + i];
+            const double c = block_sum_all(part, s.red);
+            for (int i = threadIdx.x; i < n; i += FTH) Wh[u * ld + i] -= c * Wh[v * ld + i];
+            __syncthreads();
+        }
+        double part = 0;
+        for (int i = threadIdx.x; i < n; i += FTH) part += Wh[u * ld + i] * Wh[u * ld + i];
+        const double nrm = sqrt(block_sum_all(part, s.red));
+        const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+        for (int i = threadIdx.x; i < n; i += FTH) Wh[u * ld + i] *= inv;
+        __syncthreads();
+    }
+    // Z = Wh^T T: thread per column, rows j .. n - 1 (coalesced along the row)
+    for (int j = threadIdx.x; j < n; j += FTH) {
+        double z[kMaxContVecs] = {0, 0, 0, 0};
+        for (int i = j; i < n; ++i) {
+            const double t = A[(size_t) i * ld + j];
+            for (int u = 0; u < nuse; ++u) z[u] += Wh[u * ld + i] * t;
+        }
+        for (int u = 0; u < nuse; ++u) Z[u * ld + j] = z[u];
+    }
+    __syncthreads();
+    for (size_t e = threadIdx.x; e < (size_t) n * ld; e += FTH) {
+        const int i = (int) (e / ld), j = (int) (e % ld);
+        if (j >= n) continue;
+        double v = A[e];
+        for (int u = 0; u < nuse; ++u) v -= Wh[u * ld + i] * Z[u * ld + j];
+        A[e] = v;
+    }
+    __syncthreads();
+}
+
+// The rest of the whitened factor: W (T, or P T with marginalisation) in A,
+// y = W^T W delta, and the bounds max |W| and largest row sum of |W|
+// (fbounds[4 gidx], [4 gidx + 1]).
+__device__ void whitened_factor(const WaveArgs &a, const ChunkDesc &ch, float2 *A2, double *scratch,
+                                FactorSmem &s) {
+    const int ld = ch.ld, n = ch.n;
+    double *A = reinterpret_cast<double *>(A2);
+    form_t_df(A2, ld, n, a.ivar + ch.pix, scratch);
+    int nuse = 0;
+    if (a.cont_logl >= 0 || a.cont_l >= 0) {
+        double *V = scratch, *U = V + kMaxContVecs * ld, *Wh = U + kMaxContVecs * ld, *Z = Wh + kMaxContVecs * ld;
+        nuse = cont_basis(ld, n, a.wave + ch.pix, a.cont_logl, a.cont_l, V, U, s);
+        project_w(A, ld, n, U, nuse, Wh, Z, s);
+    }
+    // t = W delta (warp per row), y = W^T t (thread per column)
+    double *t = scratch;
+    double *y = reinterpret_cast<double *>(a.fws + ch.o_y);
+    const double *dl = a.delta + ch.pix;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    double mx = 0, rs = 0;
+    for (int i = warp; i < ld; i += FTH / 32) {
+        double acc = 0, r = 0;
+        if (i < n) {
+            const double *Ai = A + (size_t) i * ld;
+            for (int j = lane; j < n; j += 32) {
+                const double v = Ai[j];
+                acc += v * dl[j];
+                r += fabs(v);
+                mx = fmax(mx, fabs(v));
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_down_sync(0xffffffffu, acc, o);
+            r += __shfl_down_sync(0xffffffffu, r, o);
+        }
+        if (lane == 0) {
+            t[i] = acc;
+            rs = fmax(rs, r);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < ld; j += FTH) {
+        double acc = 0;
+        if (j < n)
+            for (int i = 0; i < n; ++i) acc += A[(size_t) i * ld + j] * t[i];
+        y[j] = acc;
+    }
+    mx = block_max_all(mx, s.red);
+    rs = block_max_all(rs, s.red);
+    if (threadIdx.x == 0) {
+        a.fbounds[4 * ch.gidx] = mx;
+        a.fbounds[4 * ch.gidx + 1] = rs;
+        a.fbounds[4 * ch.gidx + 2] = nuse;
+        a.fbounds[4 * ch.gidx + 3] = 0.0;
     }
 }
 
@@ -695,6 +837,10 @@ __global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
         __syncthreads();
         trtri_df(A2, ld, nb, reinterpret_cast<float2 *>(scratch), s);
         __syncthreads();
+        if (a.sym) {
+            whitened_factor(a, ch, A2, scratch, s);
+            return;
+        }
         lauum_df(A2, ld, nb, n, iv, scratch, s);
     } else {
         if (!potrf_blocked(A, ld, nb, s)) {
@@ -737,8 +883,8 @@ __global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
     mx = block_max_all(mx, s.red);
     rs = block_max_all(rs, s.red);
     if (threadIdx.x == 0) {
-        a.fbounds[2 * ch.gidx] = mx;
-        a.fbounds[2 * ch.gidx + 1] = rs;
+        a.fbounds[4 * ch.gidx] = mx;
+        a.fbounds[4 * ch.gidx + 1] = rs;
     }
 }
 

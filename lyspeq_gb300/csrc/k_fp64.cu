@@ -552,8 +552,10 @@ __global__ void k_finish(WaveArgs a, int mixed) {
     if (mixed) {
         // G = P R^T: P rows = A_i^T (i < ns), R rows = A_j (j < ns), C^-1 S, C^-1 N;
         // blocks bi <= bj only.  F_ij = G_ij (i <= j), t_i = G_{i,ns}, b_i = G_{i,ns+1}.
+        // Whitened form: rows B_i of P on both sides (B_ns = W S W^T, B_{ns+1} = W N W^T).
         const double *psc = a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + ch.slot_p;
-        const double *rsc = a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + a.total_slots_p + ch.slot_r;
+        const double *rsc = a.sym ? psc
+                                  : a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + a.total_slots_p + ch.slot_r;
         auto gram = [&](int i, int j) {
             const int blk = (i / GR) * a.gt + j / GR, li = i % GR, lj = j % GR;
             const float *gp = a.gram_part + ((size_t) c * a.gt * a.gt + blk) * blkstride;

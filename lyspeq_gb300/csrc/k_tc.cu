@@ -347,16 +347,40 @@ __device__ __forceinline__ bool drain_tile(uint32_t tmem, uint32_t lane_addr, in
 // alternates between two TMEM buffers, so that the epilogue of tile t
 // (conversion and stores) overlaps the MMAs of tile t + 1.
 // TMEM: hi*hi ping [0, 128), pong [128, 256), cross [256, 384) and [384, 512).
+//
+// STAGE selects the product (all three share the pipeline):
+//   0  A_s = C^-1 Q_s: every 128 x 128 tile, written row-major to R and
+//      transposed to P;
+//   1  X_s = W Q_s (whitened path, W in the C planes): written row-major to R;
+//   2  B_s = X_s W^T (X_s from R, W as the second operand): tiles on and above
+//      the diagonal only, weighted for the trace Gram (off-diagonal elements
+//      times sqrt 2, the lower half of a diagonal tile zero) and stored as
+//      compact 128 x 128 tiles in P.
+// Stages 1 and 2 stop the K loop where W's lower triangle ends (a.w_tri).
 struct GemmTile {
-    int c, s, m0, n0;
+    int c, s, m0, n0, tu;   // tu: compact index of an upper tile (stage 2)
 };
 
+template <int STAGE>
 __device__ __forceinline__ GemmTile gemm_tile(const int *jobs, long long t, int mt) {
-    const long long tpj = (long long) mt * mt;
+    const long long tpj = STAGE == 2 ? (long long) mt * (mt + 1) / 2 : (long long) mt * mt;
     const int job = (int) (t / tpj), tix = (int) (t % tpj);
-    return GemmTile{jobs[2 * job], jobs[2 * job + 1], (tix % mt) * G_BM, (tix / mt) * G_BN};
+    if (STAGE != 2) return GemmTile{jobs[2 * job], jobs[2 * job + 1], (tix % mt) * G_BM, (tix / mt) * G_BN, 0};
+    // upper tiles row by row: row I holds tiles J = I .. mt - 1
+    int I = 0, r = tix;
+    while (r >= mt - I) { r -= mt - I; ++I; }
+    return GemmTile{jobs[2 * job], jobs[2 * job + 1], I * G_BM, (I + r) * G_BN, tix};
 }
 
+// K blocks of a tile: the whole row, or up to the end of W's lower triangle
+template <int STAGE>
+__device__ __forceinline__ int tile_kblocks(const WaveArgs &a, const GemmTile &tl, int kblocks) {
+    if (STAGE == 0 || !a.w_tri) return kblocks;
+    const int end = ((STAGE == 1 ? tl.m0 : tl.n0) + G_BM) / BK;
+    return min(kblocks, end);
+}
+
+template <int STAGE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
           const __grid_constant__ CUtensorMap mc_lo, const __grid_constant__ CUtensorMap mq_hi,
@@ -376,7 +400,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
 
     const int ld = a.max_ld;
     const int mt = (ld + G_BM - 1) / G_BM;
-    const long long total = (long long) njobs * mt * mt;
+    const long long total = (long long) njobs * (STAGE == 2 ? mt * (mt + 1) / 2 : mt * mt);
     const int kblocks = ld / BK;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
 
@@ -402,23 +426,28 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         // TMA producer
         int kb_all = 0;
         for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
-            const GemmTile tl = gemm_tile(jobs, t, mt);
-            const int qslot = a.chunks[tl.c].slot_q + tl.s;
-            if (!LQG_IN_BOUNDS(a, tl.c >= 0 && tl.c < a.n_chunks && qslot >= 0 && qslot < a.total_slots_q &&
-                                      tl.m0 < ld && tl.n0 < ld && a.chunks[tl.c].ld == ld,
-                               1, tl.c, qslot)) {
+            const GemmTile tl = gemm_tile<STAGE>(jobs, t, mt);
+            // stages 0, 1: A = C planes of the chunk, B = Q slot; stage 2: A = R slot, B = C planes
+            const int aidx = STAGE == 2 ? a.chunks[tl.c].slot_r + tl.s : tl.c;
+            const int bidx = STAGE == 2 ? tl.c : a.chunks[tl.c].slot_q + tl.s;
+            const bool idx_ok = STAGE == 2 ? (aidx >= 0 && aidx < a.total_slots_r)
+                                           : (bidx >= 0 && bidx < a.total_slots_q);
+            if (!LQG_IN_BOUNDS(a, tl.c >= 0 && tl.c < a.n_chunks && idx_ok && tl.m0 < ld && tl.n0 < ld &&
+                                      a.chunks[tl.c].ld == ld,
+                               1, tl.c, STAGE == 2 ? aidx : bidx)) {
                 *abort_flag = 1;
                 break;
             }
-            for (int kb = 0; kb < kblocks; ++kb) {
+            const int kbt = tile_kblocks<STAGE>(a, tl, kblocks);
+            for (int kb = 0; kb < kbt; ++kb) {
                 const int st = kb_all % G_STAGES;
                 if (!mbar_wait(&empty[st], ((kb_all / G_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
                 unsigned char *sb = smem + st * G_STAGE_BYTES;
                 mbar_expect_tx(&full[st], G_STAGE_BYTES);
-                tma_load_3d(sb, &mc_hi, &full[st], kb * BK, tl.m0, tl.c);
-                tma_load_3d(sb + G_TILE_A, &mc_lo, &full[st], kb * BK, tl.m0, tl.c);
-                tma_load_3d(sb + 2 * G_TILE_A, &mq_hi, &full[st], kb * BK, tl.n0, qslot);
-                tma_load_3d(sb + 2 * G_TILE_A + G_TILE_B, &mq_lo, &full[st], kb * BK, tl.n0, qslot);
+                tma_load_3d(sb, &mc_hi, &full[st], kb * BK, tl.m0, aidx);
+                tma_load_3d(sb + G_TILE_A, &mc_lo, &full[st], kb * BK, tl.m0, aidx);
+                tma_load_3d(sb + 2 * G_TILE_A, &mq_hi, &full[st], kb * BK, tl.n0, bidx);
+                tma_load_3d(sb + 2 * G_TILE_A + G_TILE_B, &mq_lo, &full[st], kb * BK, tl.n0, bidx);
                 ++kb_all;
             }
         }
@@ -432,8 +461,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const int x = lt & 1;
             if (lt >= 2 && !mbar_wait(&xempty[x], ((lt >> 1) - 1) & 1)) { *abort_flag = 1; break; }
             fence_after();
+            const int kbt = tile_kblocks<STAGE>(a, gemm_tile<STAGE>(jobs, t, mt), kblocks);
             if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN, kGemmDrain>(
-                    tmem, tmem + 2 * G_BN + x * G_BN, smem, full, empty, dfull, dempty, &xfull[x], kblocks,
+                    tmem, tmem + 2 * G_BN + x * G_BN, smem, full, empty, dfull, dempty, &xfull[x], kbt,
                     idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag))
                 break;
         }
@@ -449,17 +479,66 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         const int nq4 = 4 * a.n_chunks;
         int g_all = 0, lt = 0;
         for (long long t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
-            const GemmTile tl = gemm_tile(jobs, t, mt);
+            const GemmTile tl = gemm_tile<STAGE>(jobs, t, mt);
             const ChunkDesc &ch = a.chunks[tl.c];
             float sum[64];
 #pragma unroll
             for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-            bool got = drain_tile<false, kGemmDrain>(tmem, lane_addr, col0, dfull, dempty, kblocks, sum, g_all,
-                                                     abort_flag);
+            bool got = drain_tile<false, kGemmDrain>(tmem, lane_addr, col0, dfull, dempty,
+                                                     tile_kblocks<STAGE>(a, tl, kblocks), sum, g_all, abort_flag);
             const int x = lt & 1;
             got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1)) && !*abort_flag;
             if (!got) break;
             fence_after();
+            if (STAGE == 2) {
+                // B_s = (R scale X_s)(C scale W)^T: to the P scale, weighted, compact upper tile
+                const int s = tl.s;
+                const double rs = a.scales[nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r + s];
+                const double bs = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
+                const float mult = (float) (bs / (rs * a.scales[4 * tl.c + 2]));
+                const int rt = quad * 32 + lane;   // row within the tile
+                const size_t tbase = (size_t) (ch.slot_p + s) * a.p_plane + (size_t) tl.tu * (G_BM * G_BN) +
+                                     (size_t) rt * G_BN;
+                const bool ok = LQG_IN_BOUNDS(a, ch.slot_p + s < a.total_slots_p &&
+                                                     (size_t) tl.tu * (G_BM * G_BN) + G_BM * G_BN <= a.p_plane,
+                                              2, tl.c, s);
+                const float sqrt2 = 1.41421356237309515f;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int cb = col0 + h * 32;   // column within the tile
+                    float xv[32];
+                    tmem_ld32(tmem + lane_addr + 2 * G_BN + x * G_BN + cb, xv);
+                    if (!ok) continue;
+                    uint32_t hp[16], lp[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        float v[2];
+#pragma unroll
+                        for (int e2 = 0; e2 < 2; ++e2) {
+                            const int cc = cb + 2 * j + e2;
+                            float wgt = sqrt2;
+                            if (tl.m0 == tl.n0) wgt = cc > rt ? sqrt2 : (cc == rt ? 1.f : 0.f);
+                            v[e2] = (sum[h * 32 + 2 * j + e2] + xv[2 * j + e2]) * mult * wgt;
+                        }
+                        const __half2 hv = __floats2half2_rn(v[0], v[1]);
+                        const float2 hf = __half22float2(hv);
+                        const __half2 lv = __floats2half2_rn(v[0] - hf.x, v[1] - hf.y);
+                        hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
+                        lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
+                    }
+                    uint4 *dh = reinterpret_cast<uint4 *>(a.p_hi + tbase + cb);
+                    uint4 *dl = reinterpret_cast<uint4 *>(a.p_lo + tbase + cb);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+                        dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
+                    }
+                }
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&xempty[x]);
+                continue;
+            }
             const int row = tl.m0 + quad * 32 + lane;
             const int s = tl.s;
             const double sc = a.scales[4 * tl.c + 2];
@@ -470,7 +549,8 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
             __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
             // A_s (s < ns) goes to R and, transposed, to P; C^-1 S (s = ns) to R only
-            const bool write_p = s < ch.ns;
+            // (stage 1: every X_s to R only)
+            const bool write_p = STAGE == 0 && s < ch.ns;
             const bool slots_ok = LQG_IN_BOUNDS(a, ch.slot_r + s < a.total_slots_r &&
                                                      (!write_p || ch.slot_p + s < a.total_slots_p), 2, tl.c, s);
 #pragma unroll
@@ -527,7 +607,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     }
     if (threadIdx.x == 0 && *abort_flag)
         for (long long t = blockIdx.x; t < total; t += gridDim.x)
-            atomicExch(&a.status[a.chunks[gemm_tile(jobs, t, mt).c].gidx], LQG_CHUNK_TIMEOUT);
+            atomicExch(&a.status[a.chunks[gemm_tile<STAGE>(jobs, t, mt).c].gidx], LQG_CHUNK_TIMEOUT);
 }
 
 // ---------------------------------------------------------------------------
@@ -555,12 +635,13 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     // t, b columns ns and ns + 1).
     const int bi = blk / a.gt, bj = blk % a.gt;
     if (bi > bj || bi * R_BM >= ch.ns || bj * R_BN >= ch.ns + 2) return;
-    const int64_t K = (int64_t) ch.ld * ch.ld;
+    const int64_t K = a.sym ? a.p_plane : (int64_t) ch.ld * ch.ld;
     const int64_t kper = ((K + a.gram_splits - 1) / a.gram_splits + BK - 1) / BK * BK;
     const int64_t k_lo = sp * kper, k_hi = min(K, k_lo + kper);
     const int kblocks = k_hi > k_lo ? (int) ((k_hi - k_lo) / BK) : 0;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int prow = ch.slot_p + bi * R_BM, rrow = ch.slot_r + bj * R_BN;
+    // whitened form: both operands are the B_s rows of P (B_0 .. B_{ns+1})
+    const int prow = ch.slot_p + bi * R_BM, rrow = (a.sym ? ch.slot_p : ch.slot_r) + bj * R_BN;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < R_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
@@ -578,8 +659,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 
     if (warp == 0 && lane == 0) {
         int issued = 0;
-        if (!LQG_IN_BOUNDS(a, prow >= 0 && prow < a.total_slots_p && rrow >= 0 && rrow < a.total_slots_r &&
-                                  k_hi <= K, 3, c, prow))
+        if (!LQG_IN_BOUNDS(a, prow >= 0 && prow < a.total_slots_p && rrow >= 0 &&
+                                  rrow < (a.sym ? a.total_slots_p : a.total_slots_r) && k_hi <= K, 3, c, prow))
             *abort_flag = 1;
         for (int kb = 0; kb < kblocks && !*abort_flag; ++kb) {
             const int st = kb % R_STAGES;
@@ -655,7 +736,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 }
 
 // Operand scales of the mixed path (powers of two), from the FP64 bounds the
-// factorisation left per chunk: max |C^-1| and the largest row sum of |C^-1|.
+// factorisation left per chunk: max |C^-1| and the largest row sum of |C^-1|
+// (of W in the whitened form).
 __global__ void k_scales(WaveArgs a) {
     const int c = blockIdx.x;
     const ChunkDesc &ch = a.chunks[c];
@@ -671,7 +753,7 @@ __global__ void k_scales(WaveArgs a) {
     if (threadIdx.x != 0) return;
     for (int i = 1; i < (int) blockDim.x / 32; ++i) mx = fmax(mx, red[i]);
     double *sc = a.scales + 4 * c;
-    const double maxc = a.fbounds[2 * ch.gidx], rowsum = a.fbounds[2 * ch.gidx + 1];
+    const double maxc = a.fbounds[4 * ch.gidx], rowsum = a.fbounds[4 * ch.gidx + 1];
     const double target = 16384.0;
     sc[0] = maxc;
     sc[1] = rowsum;
@@ -682,12 +764,16 @@ __global__ void k_scales(WaveArgs a) {
     double *psc = a.scales + nq4 + a.total_slots_q + ch.slot_p;
     double *rsc = a.scales + nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r;
     for (int s = 0; s <= ch.ns; ++s) {
-        // |C^-1 B| <= rowsum * max|B| and max|B| <= target / (B scale)
+        // |C^-1 B| <= rowsum * max|B| and max|B| <= target / (B scale); the
+        // same bound for X_s = W Q_s in the whitened form
         double r = pow2_floor(qsc[s] / rowsum);
         rsc[s] = r;
-        if (s < ch.ns) psc[s] = r;
+        if (s < ch.ns && !a.sym) psc[s] = r;
     }
-    rsc[ch.ns + 1] = sc[3];   // C^-1 N
+    rsc[ch.ns + 1] = sc[3];   // C^-1 N, or X_N = W N
+    if (a.sym)
+        // |B_s| = |X_s W^T| <= max|X_s| rowsum, and sqrt 2 for the off-diagonal weight
+        for (int s = 0; s <= ch.ns + 1; ++s) psc[s] = pow2_floor(rsc[s] / (2.0 * rowsum));
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point, so that the
@@ -727,10 +813,13 @@ void launch_scales_mixed(WaveArgs &a, cudaStream_t st) {
     a.launches++;
 }
 
-void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs) {
+void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs, const int *d_jobs2,
+                           int njobs2) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        cudaFuncSetAttribute(k_tc_gemm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
         cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, R_SMEM);
         attr = true;
     }
@@ -745,14 +834,25 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     CUtensorMap mcl = make_map(a.c_lo, 3, d3c, s3, boxa, &ok);
     CUtensorMap mqh = make_map(a.q_hi, 3, d3q, s3, boxb, &ok);
     CUtensorMap mql = make_map(a.q_lo, 3, d3q, s3, boxb, &ok);
-    cuuint64_t d2p[2] = {plane, (cuuint64_t) a.total_slots_p};
+    const cuuint64_t pplane = (cuuint64_t) a.p_plane;
+    cuuint64_t d2p[2] = {pplane, (cuuint64_t) a.total_slots_p};
     cuuint64_t d2r[2] = {plane, (cuuint64_t) a.total_slots_r};
-    cuuint64_t s2[1] = {plane * 2};
+    cuuint64_t s2p[1] = {pplane * 2}, s2[1] = {plane * 2};
     cuuint32_t box2[2] = {BK, R_BM};
-    CUtensorMap mph = make_map(a.p_hi, 2, d2p, s2, box2, &ok);
-    CUtensorMap mpl = make_map(a.p_lo, 2, d2p, s2, box2, &ok);
-    CUtensorMap mrh = make_map(a.r_hi, 2, d2r, s2, box2, &ok);
-    CUtensorMap mrl = make_map(a.r_lo, 2, d2r, s2, box2, &ok);
+    CUtensorMap mph = make_map(a.p_hi, 2, d2p, s2p, box2, &ok);
+    CUtensorMap mpl = make_map(a.p_lo, 2, d2p, s2p, box2, &ok);
+    // whitened form: the Gram's second operand is P as well
+    CUtensorMap mrh = a.sym ? mph : make_map(a.r_hi, 2, d2r, s2, box2, &ok);
+    CUtensorMap mrl = a.sym ? mpl : make_map(a.r_lo, 2, d2r, s2, box2, &ok);
+    // whitened form, second product: A = X_s (R planes), B = W (C planes)
+    cuuint64_t d3r[3] = {(cuuint64_t) ld, (cuuint64_t) ld, (cuuint64_t) a.total_slots_r};
+    CUtensorMap mxh{}, mxl{}, mwh{}, mwl{};
+    if (a.sym) {
+        mxh = make_map(a.r_hi, 3, d3r, s3, boxa, &ok);
+        mxl = make_map(a.r_lo, 3, d3r, s3, boxa, &ok);
+        mwh = make_map(a.c_hi, 3, d3c, s3, boxb, &ok);
+        mwl = make_map(a.c_lo, 3, d3c, s3, boxb, &ok);
+    }
     if (!ok) {
         fprintf(stderr, "lqg: cuTensorMapEncodeTiled failed\n");
         return;
@@ -765,17 +865,23 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         if (n_sm <= 0) n_sm = 1;
     }
     // persistent: one CTA per SM (one fits: 197 KB of shared memory)
-    const long long tiles = (long long) ((ld + G_BM - 1) / G_BM) * ((ld + G_BN - 1) / G_BN) * njobs;
+    const long long mt = (ld + G_BM - 1) / G_BM;
+    const long long tiles = mt * mt * njobs;
     const int grid = (int) std::min<long long>(tiles, n_sm);
-    k_tc_gemm<<<grid, TC_THREADS, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
+    if (!a.sym) {
+        k_tc_gemm<0><<<grid, TC_THREADS, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
+    } else {
+        k_tc_gemm<1><<<grid, TC_THREADS, G_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh, mql);
+        const long long tiles2 = mt * (mt + 1) / 2 * njobs2;
+        const int grid2 = (int) std::min<long long>(tiles2, n_sm);
+        k_tc_gemm<2><<<grid2, TC_THREADS, G_SMEM, st>>>(a, d_jobs2, njobs2, mxh, mxl, mwh, mwl);
+        a.launches++;
+    }
     if (a.mid_event) cudaEventRecord(a.mid_event, st);
     k_tc_gram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), R_THREADS, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
     a.launches += 2;
 }
 
-int gram_splits_mixed(int ld) {
-    int64_t K = (int64_t) ld * ld;
-    return (int) ((K + kGramK - 1) / kGramK);
-}
+int gram_splits_mixed(int64_t K) { return (int) ((K + kGramK - 1) / kGramK); }
 
 }  // namespace lqg

@@ -502,8 +502,8 @@ int upload_pixels(lqg_ctx *ctx) {
     return LQG_OK;
 }
 
-int gram_splits_for(int ld, int precision) {
-    if (precision == LQG_PRECISION_MIXED) return gram_splits_mixed(ld);
+int gram_splits_for(int ld, int precision, bool sym) {
+    if (precision == LQG_PRECISION_MIXED) return gram_splits_mixed(sym ? sym_plane(ld) : (int64_t) ld * ld);
     int64_t K = (int64_t) ld * ld;
     int64_t s = (K + 32767) / 32768;
     return (int) std::max<int64_t>(1, std::min<int64_t>(s, 256));
@@ -517,15 +517,19 @@ int64_t chunk_fws_bytes(int64_t ld) {
 }
 
 // Wave workspace of one chunk in a wave with the given Gram blocking.
-int64_t chunk_ws_bytes(int64_t ld, int ns, int precision, int splits, int gt) {
+int64_t chunk_ws_bytes(int64_t ld, int ns, int precision, bool sym, int splits, int gt) {
     const int64_t m = ld * ld * 8, tiles = (ld / 64) * (ld / 64);
     int64_t b = align_up(tiles * 16 * ns * 8, 256);
     const int64_t gblk = (int64_t) gt * gt * splits * 128 * 128;
     if (precision == LQG_PRECISION_FP64)
         b += align_up(gblk * 8, 256) + align_up(m * ns, 256) * 2 + align_up(m * (ns + 2), 256);
-    else
-        // fp16 hi/lo planes of C^-1, Q (ns + 1 slots), R (ns) and P (ns + 2), and fp32 Gram partials
+    else if (!sym)
+        // fp16 hi/lo planes of C^-1, Q (ns + 1 slots), R (ns + 2) and P (ns), and fp32 Gram partials
         b += ld * ld * 2 * 2 * (int64_t) (1 + (ns + 1) + ns + (ns + 2)) + gblk * 4;
+    else
+        // W, Q (ns + 1), X (ns + 2) planes of ld^2 and the compact B slots (ns + 2)
+        b += ld * ld * 2 * 2 * (int64_t) (1 + (ns + 1) + (ns + 2)) + sym_plane((int) ld) * 2 * 2 * (ns + 2) +
+             gblk * 4;
     return b;
 }
 
@@ -534,8 +538,8 @@ struct WavePlan {
     int ld = 0, gt = 1, splits = 1;
     int slot_q = 0, slot_r = 0, slot_p = 0;
     int64_t ws_bytes = 0, half_bytes = 0;
-    size_t desc_off = 0, jobs_off = 0, scales_off = 0;
-    int njobs = 0, nscales = 0;
+    size_t desc_off = 0, jobs_off = 0, scales_off = 0, jobs2_off = 0;
+    int njobs = 0, nscales = 0, njobs2 = 0;
 };
 
 struct GroupPlan {
@@ -560,7 +564,7 @@ cudaEvent_t pool_event(lqg_ctx *ctx, size_t i) {
 // split into waves of equal padded size (phase B: Q_s, products, traces).
 // Descriptors, jobs and host-known scales of every launch are packed into
 // single arrays, uploaded once.
-int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, std::vector<ChunkDesc> &desc,
+int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan> &groups, std::vector<ChunkDesc> &desc,
                    std::vector<int> &jobs, std::vector<double> &scales, int64_t &max_fws, int64_t &max_ws,
                    int64_t &max_half, int64_t &max_gram) {
     const int nb = (int) ctx->chunks.size();
@@ -619,8 +623,8 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
         for (size_t k = 0; k < g.members.size(); ++k) {
             const int idx = g.members[k];
             const auto &h = ctx->chunks[idx];
-            const int gt = gram_blocks(h.ns), splits = gram_splits_for(h.ld, precision);
-            int64_t need = chunk_ws_bytes(h.ld, h.ns, precision, splits, gt);
+            const int gt = gram_blocks(h.ns), splits = gram_splits_for(h.ld, precision, sym);
+            int64_t need = chunk_ws_bytes(h.ld, h.ns, precision, sym, splits, gt);
             if (precision == LQG_PRECISION_MIXED && h.nelem > 0)
                 need += align_up((int64_t) h.kbin_upp * h.nf * 8, 256);   // grid-point phases
             bool fresh = g.waves.empty() || g.waves.back().ld != h.ld || g.waves.back().gt != gt;
@@ -660,10 +664,11 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
                 }
                 d.slot_q = w.slot_q; w.slot_q += d.ns + 1;
                 // trace-Gram operand stacks.  FP64: P = [A_s^T, (C^-1 S)^T, N C^-1],
-                // R = [A_s].  Mixed: P = [A_s^T], R = [A_s, C^-1 S, C^-1 N].
+                // R = [A_s].  Mixed: P = [A_s^T], R = [A_s, C^-1 S, C^-1 N].  Whitened
+                // form: R = [X_s, W S, W N], P = [B_s, W S W^T, W N W^T] (compact).
                 const bool mixed = precision == LQG_PRECISION_MIXED;
                 d.slot_r = w.slot_r; w.slot_r += mixed ? d.ns + 2 : d.ns;
-                d.slot_p = w.slot_p; w.slot_p += mixed ? d.ns : d.ns + 2;
+                d.slot_p = w.slot_p; w.slot_p += mixed ? (sym ? d.ns + 2 : d.ns) : d.ns + 2;
                 desc.push_back(d);
             }
             const int nch = (int) w.members.size();
@@ -671,7 +676,8 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             w.half_bytes = 0;
             int64_t gram = 0;
             if (precision == LQG_PRECISION_MIXED) {
-                w.half_bytes = (int64_t) ld * ld * 2 * 2 * ((int64_t) nch + w.slot_q + w.slot_r + w.slot_p);
+                const int64_t pp = sym ? sym_plane(ld) : (int64_t) ld * ld;
+                w.half_bytes = (int64_t) ld * ld * 2 * 2 * ((int64_t) nch + w.slot_q + w.slot_r) + pp * 2 * 2 * w.slot_p;
                 gram = (int64_t) nch * gblk;
             }
             max_ws = std::max(max_ws, w.ws_bytes);
@@ -681,6 +687,12 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
             for (int i = 0; i < nch; ++i)
                 for (int s = 0; s <= desc[w.desc_off + i].ns; ++s) { jobs.push_back(i); jobs.push_back(s); }
             w.njobs = (int) (jobs.size() - w.jobs_off) / 2;
+            // whitened form, second product: B_s for s <= ns + 1
+            w.jobs2_off = jobs.size();
+            if (sym)
+                for (int i = 0; i < nch; ++i)
+                    for (int s = 0; s <= desc[w.desc_off + i].ns + 1; ++s) { jobs.push_back(i); jobs.push_back(s); }
+            w.njobs2 = (int) (jobs.size() - w.jobs2_off) / 2;
             w.scales_off = scales.size();
             w.nscales = 4 * nch + w.slot_q + w.slot_p + w.slot_r;
             scales.resize(scales.size() + w.nscales, 1.0);
@@ -713,8 +725,13 @@ int plan_iteration(lqg_ctx *ctx, int precision, std::vector<GroupPlan> &groups, 
 
 extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision) {
     if (!ctx) return LQG_ERR_ARG;
-    if (precision != LQG_PRECISION_FP64 && precision != LQG_PRECISION_MIXED)
+    if (precision != LQG_PRECISION_FP64 && precision != LQG_PRECISION_MIXED &&
+        precision != LQG_PRECISION_MIXED_DIRECT)
         return set_err(ctx, LQG_ERR_ARG, "unknown precision");
+    // both mixed forms share the kernels up to the products; sym selects the
+    // whitened symmetric one
+    const bool sym = precision == LQG_PRECISION_MIXED;
+    if (precision == LQG_PRECISION_MIXED_DIRECT) precision = LQG_PRECISION_MIXED;
     if (precision == LQG_PRECISION_MIXED && !tc_available())
         return set_err(ctx, LQG_ERR_UNSUPPORTED, "mixed precision needs the sm_103a tensor-core kernels");
     cudaSetDevice(ctx->device);
@@ -731,16 +748,25 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     std::fill(ctx->timings, ctx->timings + 8, 0.0);
     ctx->launches = 0;
     ctx->waves = 0;
+    if (nb == 0) {
+        // an empty batch contributes nothing: zero sums, as the reference's
+        // accumulators stay when no chunk is processed
+        LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_fisher.p, 0, (size_t) ctx->nkz * ctx->nkz * 8, st));
+        LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_dbt.p, 0, (size_t) 3 * ctx->nkz * 8, st));
+        LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
+        ctx->have_results = true;
+        return LQG_OK;
+    }
 
     std::vector<GroupPlan> groups;
     std::vector<ChunkDesc> desc;
     std::vector<int> jobs;
     std::vector<double> scales;
     int64_t max_fws = 0, max_ws = 0, max_half = 0, max_gram = 0;
-    if ((rc = plan_iteration(ctx, precision, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram)))
+    if ((rc = plan_iteration(ctx, precision, sym, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram)))
         return rc;
     if (ctx->d_fws.alloc(std::max<int64_t>(max_fws, 256)) || ctx->d_ws.alloc(std::max<int64_t>(max_ws, 256)) ||
-        ctx->d_fbounds.alloc(std::max(2 * nb, 1) * 8))
+        ctx->d_fbounds.alloc(std::max(4 * nb, 1) * 8))
         return set_err(ctx, LQG_ERR_NOMEM, "workspace");
     if (precision == LQG_PRECISION_MIXED &&
         (ctx->d_halves.alloc(max_half + 1024) || ctx->d_gram.alloc(std::max<int64_t>(max_gram, 1) * 4)))
@@ -788,6 +814,9 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.n_fpix = (int64_t) ctx->h_flogw.size();
     base.reso_nelem = base.reso_os = 0;
     base.growth = ctx->opts.redshift_growth_on > 0;
+    base.sym = sym;
+    // W = T is lower triangular unless the continuum projector makes it full
+    base.w_tri = sym && ctx->opts.cont_logl_order < 0 && ctx->opts.cont_l_order < 0;
     {
         int ne = -1, os = -1;
         bool uniform = true;
@@ -873,8 +902,9 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
                 b.q_lo = hb; hb += pl * w.slot_q;
                 b.r_hi = hb; hb += pl * w.slot_r;
                 b.r_lo = hb; hb += pl * w.slot_r;
-                b.p_hi = hb; hb += pl * w.slot_p;
-                b.p_lo = hb; hb += pl * w.slot_p;
+                b.p_plane = sym ? sym_plane(w.ld) : pl;
+                b.p_hi = hb; hb += b.p_plane * w.slot_p;
+                b.p_lo = hb; hb += b.p_plane * w.slot_p;
                 b.gram_part = ctx->d_gram.as<float>();
                 b.gram_elems = (int64_t) nch * w.gt * w.gt * w.splits * 128 * 128;
             }
@@ -889,7 +919,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
             if ((rc = step("build_q", w.ld, nch))) return rc;
             cudaEventRecord(pool_event(ctx, w0 + 1), st);
             if (precision == LQG_PRECISION_MIXED)
-                launch_products_mixed(b, st, d_jobs, w.njobs);
+                launch_products_mixed(b, st, d_jobs, w.njobs, ctx->d_jobs.as<int>() + w.jobs2_off, w.njobs2);
             else
                 launch_products_fp64(b, st, d_jobs, w.njobs);
             if ((rc = step("products", w.ld, nch))) return rc;

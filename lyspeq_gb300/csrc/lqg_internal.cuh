@@ -131,6 +131,9 @@ struct WaveArgs {
     const double *flogw, *fsqw, *rw;                 // resolution-matrix grids and weights
     int reso_nelem, reso_os;                         // shape shared by every resolution chunk, else 0
     int growth;                                      // RedshiftGrowthOn (as DeviceBins::growth)
+    int sym;                                         // mixed path in the whitened symmetric form
+    int w_tri;                                       // W lower triangular (no marginalisation)
+    int64_t p_plane;                                 // elements of one P slot
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
     const float2 *signal_ff;                         // signal table as double-float (mixed path)
@@ -186,12 +189,19 @@ size_t factor_smem_bytes();
 // Phase B (per wave): Q_k, products, traces, per-chunk results.
 void launch_build_q(WaveArgs &a, cudaStream_t st);
 void launch_products_fp64(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs);
-void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs);
+void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs, const int *d_jobs2,
+                           int njobs2);
 void launch_scales_mixed(WaveArgs &a, cudaStream_t st);
 void launch_finish(WaveArgs &a, cudaStream_t st);
 
 bool tc_available();
-int gram_splits_mixed(int ld);
+int gram_splits_mixed(int64_t K);
+// Elements of one compact upper-triangle slot of the whitened form: the
+// ceil(ld / 128) (ceil(ld / 128) + 1) / 2 tiles of 128 x 128 on and above the diagonal
+inline int64_t sym_plane(int ld) {
+    const int64_t mt = (ld + 127) / 128;
+    return mt * (mt + 1) / 2 * 128 * 128;
+}
 // Smoother::smoothIvar on the host (lqg_smooth.cu)
 int smooth_ivar(int n, const double *ivar, int sigmapix, double *out);
 

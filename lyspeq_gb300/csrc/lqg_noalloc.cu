@@ -25,7 +25,7 @@ namespace {
 
 constexpr int kNoallocMaxLd = 4096;                     // largest padded chunk size
 constexpr size_t kNoallocDescBytes = 256;               // ChunkDesc
-constexpr size_t kNoallocBoundsOff = 256;               // 2 doubles: max |C^-1|, max row sum
+constexpr size_t kNoallocBoundsOff = 256;               // 4 doubles: max |C^-1|, max row sum, 2 unused
 constexpr size_t kNoallocScratchOff = 1024;             // 64 ld doubles of factorisation scratch
 constexpr size_t kNoallocBytes = kNoallocScratchOff + (size_t) 64 * kNoallocMaxLd * sizeof(double);
 static_assert(sizeof(ChunkDesc) <= kNoallocDescBytes, "descriptor slot too small");

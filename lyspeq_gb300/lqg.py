@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("LQG_LIB", os.path.join(HERE, "liblqg.so"))
 
 LQG_OK = 0
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed_direct": 2}
 CHUNK_STATUS = {0: "ok", 1: "short", 2: "no_table", 3: "empty", 4: "out_of_range",
                 5: "not_spd", 6: "bad_input", 7: "too_large"}
 

@@ -1,8 +1,12 @@
-"""Mixed-precision path (fp16 hi/lo split products on tcgen05 tensor cores).
+"""Mixed-precision paths (fp16 hi/lo split products on tcgen05 tensor cores):
+"mixed", the whitened symmetric form B_k = W Q_k W^T, and "mixed_direct",
+the direct products C^-1 Q_k.
 
 Bar: d, b, t and the Fisher matrix within 1e-5 relative of lyspeq's own FP64
 results (Fisher elements normalised by sqrt(F_ii F_jj); d, b, t by the largest
-magnitude of the vector), and the same for the global sums and theta.
+magnitude of the vector), and the same for the global sums and theta.  On
+high signal-to-noise, high-resolution chunks (the echelle-like set) only the
+whitened form meets it.
 """
 import numpy as np
 import pytest
@@ -26,11 +30,12 @@ def make_engine(c):
     return eng
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_direct"])
 @pytest.mark.parametrize("name", CASES)
-def test_mixed_matches_reference(engine_lib, name):
+def test_mixed_matches_reference(engine_lib, name, precision):
     c = G.load(name)
     eng = make_engine(c)
-    eng.iterate(precision="mixed")
+    eng.iterate(precision=precision)
     out = eng.download()
     assert (out["status"] == 0).all(), out["status"]
     worst = 0.0
@@ -47,7 +52,8 @@ def test_mixed_matches_reference(engine_lib, name):
     eng.close()
 
 
-def test_mixed_matches_fp64_on_desi_like_chunks(engine_lib):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_direct"])
+def test_mixed_matches_fp64_on_desi_like_chunks(engine_lib, precision):
     from lyspeq_gb300 import lqg, synth
     w = synth.make_workload("desi", n_chunks=24)
     eng = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length, cont=(1, -1))
@@ -56,7 +62,7 @@ def test_mixed_matches_fp64_on_desi_like_chunks(engine_lib):
     eng.iterate(precision="fp64")
     ref = eng.download()
     per = [eng.chunk_result(i) for i in range(eng.size)]
-    eng.iterate(precision="mixed")
+    eng.iterate(precision=precision)
     mix = eng.download()
     assert (mix["status"] == ref["status"]).all()
     for i in range(eng.size):
@@ -65,4 +71,27 @@ def test_mixed_matches_fp64_on_desi_like_chunks(engine_lib):
         assert G.rel_err(b, per[i][1]) < MIXED_TOL and G.rel_err(t, per[i][2]) < MIXED_TOL
         assert G.rel_err(d, per[i][0]) < MIXED_TOL
     assert G.fisher_err(mix["fisher"], ref["fisher"]) < MIXED_TOL
+    eng.close()
+
+
+def test_whitened_form_meets_the_bar_on_echelle_chunks(engine_lib):
+    """High resolution at sigma ~ 0.05: the low-k modes are signal dominated
+    ~10^3 times, which the direct products turn into Fisher errors of a few
+    1e-5 (tensor-core accumulation of cancelling terms); the whitened form
+    stays below 1e-5."""
+    from lyspeq_gb300 import lqg, synth
+    w = synth.make_workload("echelle", n_chunks=4)
+    eng = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
+                     cont=(w.cont_logl_order, w.cont_l_order))
+    st = eng.add_chunk_list([(s.wave, s.delta, 1.0 / s.sigma ** 2, s.r_fwhm) for s in w.spectra])
+    assert (st == 0).all()
+    eng.iterate(precision="fp64")
+    ref = [eng.chunk_result(i) for i in range(eng.size)]
+    eng.iterate(precision="mixed")
+    worst = 0.0
+    for i in range(eng.size):
+        d, b, t, f = eng.chunk_result(i)
+        worst = max(worst, G.fisher_err(f, ref[i][3]), G.rel_err(d, ref[i][0]), G.rel_err(b, ref[i][1]),
+                    G.rel_err(t, ref[i][2]))
+    assert worst < MIXED_TOL, worst
     eng.close()

@@ -63,3 +63,19 @@ def test_fp64_deterministic(engine_lib):
     b = eng.download()
     assert np.array_equal(a["fisher"], b["fisher"]) and np.array_equal(a["d"], b["d"])
     eng.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_direct"])
+def test_empty_batch_iterates_to_zero(engine_lib, precision):
+    """A batch whose chunks were all rejected (no table for their resolution)
+    iterates to zero sums, as the reference's accumulators stay."""
+    from lyspeq_gb300 import lqg
+    c = G.load("tiny_marg1")
+    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg)
+    lam, delta, ivar, _ = c.chunks[0]
+    st = eng.add_chunk_list([(lam, delta, ivar, 123456)])
+    assert (st == 2).all() and eng.size == 0
+    eng.iterate(precision=precision)
+    out = eng.download()
+    assert not out["fisher"].any() and not out["d"].any() and not out["b"].any() and not out["t"].any()
+    eng.close()
