@@ -409,17 +409,19 @@ def main():
         key = "products" if names[dom] == "products_tc" else "traces"
         achieved = fl[key] / (phase[dom] / 1e3) / 1e12
         pk = peaks.get("bf16_tflops", 1900.0)
-        # DRAM traffic per launch of the products kernel (one launch per wave):
-        # algorithmic bytes (Q_s read, A_s written to R and transposed to P,
-        # fp16 hi/lo) times the measured/algorithmic ratio, 0.99, of an ncu
-        # capture of the same kernel on 64 chunks of this workload
+        # DRAM traffic per launch of the first product kernel, X_s = W Q_s (one
+        # launch per wave; the larger of the two product stages): algorithmic
+        # bytes (Q_s read and X_s written, fp16 hi/lo, ns + 1 slots) times the
+        # measured/algorithmic ratio, 0.99, of an ncu capture of the same kernel
+        # on 64 chunks of this workload (profiles/k_tc_gemm_whitened_desi64.md)
         traffic = None
-        n_waves = waves                            # one launch of the products kernel per wave
+        n_waves = waves                            # one launch of each product kernel per wave
         if key == "products" and n_waves > 0:
             ld = np.ceil(np.asarray(n_list) / 64.0) * 64.0
-            alg = float(np.sum((3.0 * (np.asarray(ns_list) + 1) - 1) * ld * ld * 4.0))
+            alg = float(np.sum(2.0 * (np.asarray(ns_list) + 1) * ld * ld * 4.0))
             traffic = 0.99 * alg / n_waves
-        roof = {"kernel": "k_tc_gemm" if key == "products" else "k_tc_gram", "bound": "tensor",
+        roof = {"kernel": "k_tc_gemm<1> + k_tc_gemm<2> (phase); traffic of k_tc_gemm<1>" if key == "products"
+                else "k_tc_gram", "bound": "tensor",
                 "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
                 "traffic": traffic, "traffic_unit": "bytes per launch",
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}

@@ -765,6 +765,10 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     int64_t max_fws = 0, max_ws = 0, max_half = 0, max_gram = 0;
     if ((rc = plan_iteration(ctx, precision, sym, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram)))
         return rc;
+    ctx->d_fws.trim(std::max<int64_t>(max_fws, 256));
+    ctx->d_ws.trim(std::max<int64_t>(max_ws, 256));
+    ctx->d_halves.trim(precision == LQG_PRECISION_MIXED ? max_half + 1024 : 0);
+    ctx->d_gram.trim(precision == LQG_PRECISION_MIXED ? std::max<int64_t>(max_gram, 1) * 4 : 0);
     if (ctx->d_fws.alloc(std::max<int64_t>(max_fws, 256)) || ctx->d_ws.alloc(std::max<int64_t>(max_ws, 256)) ||
         ctx->d_fbounds.alloc(std::max(4 * nb, 1) * 8))
         return set_err(ctx, LQG_ERR_NOMEM, "workspace");

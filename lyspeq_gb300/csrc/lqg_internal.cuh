@@ -109,6 +109,13 @@ struct DevBuf {
         if (e == cudaSuccess) bytes = n;
         return e;
     }
+    // Release the buffer when it is much larger than n: the iteration planner
+    // counts held buffers as free memory, so an oversized one (from a larger
+    // plan, e.g. the FP64 path before the mixed one) must go before the
+    // other buffers of the new plan are allocated.
+    void trim(size_t n) {
+        if (p && bytes > n + n / 4) { cudaFree(p); p = nullptr; bytes = 0; }
+    }
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
