@@ -627,7 +627,7 @@ void launch_build_q(WaveArgs &a, cudaStream_t st) {
 void launch_products_fp64(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs) {
     int tiles = (a.max_ld / GT) * (a.max_ld / GT);
     k_dgemm<<<dim3(tiles, njobs), 256, 0, st>>>(a, d_jobs, njobs);
-    if (a.mid_event) cudaEventRecord(a.mid_event, st);
+    if (a.mid_event) record_event(a.mid_event, st);
     k_dgram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), 256, 0, st>>>(a);
     a.launches += 2;
 }

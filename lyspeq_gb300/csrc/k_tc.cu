@@ -877,7 +877,7 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         k_tc_gemm<2><<<grid2, TC_THREADS, G_SMEM, st>>>(a, d_jobs2, njobs2, mxh, mxl, mwh, mwl);
         a.launches++;
     }
-    if (a.mid_event) cudaEventRecord(a.mid_event, st);
+    if (a.mid_event) record_event(a.mid_event, st);
     k_tc_gram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), R_THREADS, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
     a.launches += 2;
 }

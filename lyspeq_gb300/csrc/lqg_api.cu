@@ -56,6 +56,16 @@ struct lqg_ctx {
     int waves = 0;
     bool have_results = false;   // an iteration has run on the current batch
     std::vector<cudaEvent_t> evpool;
+    // CUDA graph of one iteration's launches: captured on the second iteration
+    // with the same key (batch, precision, theta use, device buffers) and
+    // replayed while the key holds
+    uint64_t batch_version = 0;
+    std::vector<uintptr_t> graph_key, last_key;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+    int graph_launches = 0, graph_waves = 0;
+    std::vector<std::pair<size_t, int>> graph_spans;
+    size_t graph_eacc = 0;
 };
 
 namespace {
@@ -227,6 +237,7 @@ extern "C" int lqg_ctx_destroy(lqg_ctx *ctx) {
     if (!ctx) return LQG_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     for (auto &e : ctx->evpool) cudaEventDestroy(e);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -246,6 +257,7 @@ extern "C" int lqg_batch_clear(lqg_ctx *ctx) {
     ctx->have_results = false;
     ctx->results_size = 0;
     ctx->pix_dirty = true;
+    ctx->batch_version++;
     return LQG_OK;
 }
 
@@ -410,6 +422,7 @@ int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double 
     }
     ctx->pix_dirty = true;
     ctx->have_results = false;
+    ctx->batch_version++;
     return LQG_OK;
 }
 
@@ -863,88 +876,144 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     };
     // events: [0] start, then 3 per group and 5 per wave, [1] end
     std::vector<std::pair<size_t, int>> spans;   // (first event, timing slot) of each measured span
-    size_t nev = 2;
+    size_t eacc = 0;
     cudaEvent_t ev_start = pool_event(ctx, 0), ev_end = pool_event(ctx, 1);
-    cudaEventRecord(ev_start, st);
-    for (auto &g : groups) {
-        WaveArgs a = base;
-        a.chunks = ctx->d_desc.as<ChunkDesc>() + g.desc_off;
-        a.n_chunks = (int) g.members.size();
-        a.max_ld = g.max_ld;
-        a.fws_bytes = g.fws_bytes;
-        const size_t e0 = nev;
-        nev += 3;
-        cudaEventRecord(pool_event(ctx, e0), st);
-        launch_build_s_c(a, st);
-        if (ctx->has_reso) launch_build_s_c_reso(a, st);
-        if ((rc = step("build_s_c", g.max_ld, a.n_chunks))) return rc;
-        cudaEventRecord(pool_event(ctx, e0 + 1), st);
-        launch_factor_all(a, st);
-        if ((rc = step("factor", g.max_ld, a.n_chunks))) return rc;
-        cudaEventRecord(pool_event(ctx, e0 + 2), st);
-        spans.push_back({e0, 0});
-        spans.push_back({e0 + 1, 1});
-        ctx->launches += a.launches;
-        for (auto &w : g.waves) {
-            WaveArgs b = base;
-            const int nch = (int) w.members.size();
-            b.chunks = ctx->d_desc.as<ChunkDesc>() + w.desc_off;
-            b.n_chunks = nch;
-            b.max_ld = w.ld;
-            b.gt = w.gt;
-            b.fws_bytes = g.fws_bytes;
-            b.ws_bytes = w.ws_bytes;
-            b.total_slots_q = w.slot_q; b.total_slots_r = w.slot_r; b.total_slots_p = w.slot_p;
-            b.gram_splits = w.splits;
-            b.scales = ctx->d_scales.as<double>() + w.scales_off;
-            if (precision == LQG_PRECISION_MIXED) {
-                __half *hb = ctx->d_halves.as<__half>();
-                const int64_t pl = (int64_t) w.ld * w.ld;
-                b.c_hi = hb; hb += pl * nch;
-                b.c_lo = hb; hb += pl * nch;
-                b.q_hi = hb; hb += pl * w.slot_q;
-                b.q_lo = hb; hb += pl * w.slot_q;
-                b.r_hi = hb; hb += pl * w.slot_r;
-                b.r_lo = hb; hb += pl * w.slot_r;
-                b.p_plane = sym ? sym_plane(w.ld) : pl;
-                b.p_hi = hb; hb += b.p_plane * w.slot_p;
-                b.p_lo = hb; hb += b.p_plane * w.slot_p;
-                b.gram_part = ctx->d_gram.as<float>();
-                b.gram_elems = (int64_t) nch * w.gt * w.gt * w.splits * 128 * 128;
+    auto launch_all = [&]() -> int {
+        int rc = LQG_OK;
+        size_t nev = 2;
+        record_event(ev_start, st);
+        for (auto &g : groups) {
+            WaveArgs a = base;
+            a.chunks = ctx->d_desc.as<ChunkDesc>() + g.desc_off;
+            a.n_chunks = (int) g.members.size();
+            a.max_ld = g.max_ld;
+            a.fws_bytes = g.fws_bytes;
+            const size_t e0 = nev;
+            nev += 3;
+            record_event(pool_event(ctx, e0), st);
+            launch_build_s_c(a, st);
+            if (ctx->has_reso) launch_build_s_c_reso(a, st);
+            if ((rc = step("build_s_c", g.max_ld, a.n_chunks))) return rc;
+            record_event(pool_event(ctx, e0 + 1), st);
+            launch_factor_all(a, st);
+            if ((rc = step("factor", g.max_ld, a.n_chunks))) return rc;
+            record_event(pool_event(ctx, e0 + 2), st);
+            spans.push_back({e0, 0});
+            spans.push_back({e0 + 1, 1});
+            ctx->launches += a.launches;
+            for (auto &w : g.waves) {
+                WaveArgs b = base;
+                const int nch = (int) w.members.size();
+                b.chunks = ctx->d_desc.as<ChunkDesc>() + w.desc_off;
+                b.n_chunks = nch;
+                b.max_ld = w.ld;
+                b.gt = w.gt;
+                b.fws_bytes = g.fws_bytes;
+                b.ws_bytes = w.ws_bytes;
+                b.total_slots_q = w.slot_q; b.total_slots_r = w.slot_r; b.total_slots_p = w.slot_p;
+                b.gram_splits = w.splits;
+                b.scales = ctx->d_scales.as<double>() + w.scales_off;
+                if (precision == LQG_PRECISION_MIXED) {
+                    __half *hb = ctx->d_halves.as<__half>();
+                    const int64_t pl = (int64_t) w.ld * w.ld;
+                    b.c_hi = hb; hb += pl * nch;
+                    b.c_lo = hb; hb += pl * nch;
+                    b.q_hi = hb; hb += pl * w.slot_q;
+                    b.q_lo = hb; hb += pl * w.slot_q;
+                    b.r_hi = hb; hb += pl * w.slot_r;
+                    b.r_lo = hb; hb += pl * w.slot_r;
+                    b.p_plane = sym ? sym_plane(w.ld) : pl;
+                    b.p_hi = hb; hb += b.p_plane * w.slot_p;
+                    b.p_lo = hb; hb += b.p_plane * w.slot_p;
+                    b.gram_part = ctx->d_gram.as<float>();
+                    b.gram_elems = (int64_t) nch * w.gt * w.gt * w.splits * 128 * 128;
+                }
+                const size_t w0 = nev;
+                nev += 5;
+                b.mid_event = pool_event(ctx, w0 + 2);
+                const int *d_jobs = ctx->d_jobs.as<int>() + w.jobs_off;
+                record_event(pool_event(ctx, w0), st);
+                if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(b, st);
+                launch_build_q(b, st);
+                if (ctx->has_reso) launch_build_q_reso(b, st);
+                if ((rc = step("build_q", w.ld, nch))) return rc;
+                record_event(pool_event(ctx, w0 + 1), st);
+                if (precision == LQG_PRECISION_MIXED)
+                    launch_products_mixed(b, st, d_jobs, w.njobs, ctx->d_jobs.as<int>() + w.jobs2_off, w.njobs2);
+                else
+                    launch_products_fp64(b, st, d_jobs, w.njobs);
+                if ((rc = step("products", w.ld, nch))) return rc;
+                record_event(pool_event(ctx, w0 + 3), st);
+                launch_finish(b, st);
+                if ((rc = step("finish", w.ld, nch))) return rc;
+                record_event(pool_event(ctx, w0 + 4), st);
+                spans.push_back({w0, 2});
+                spans.push_back({w0 + 1, 3});
+                spans.push_back({w0 + 2, 4});
+                spans.push_back({w0 + 3, 5});
+                ctx->launches += b.launches;
+                ctx->waves++;
             }
-            const size_t w0 = nev;
-            nev += 5;
-            b.mid_event = pool_event(ctx, w0 + 2);
-            const int *d_jobs = ctx->d_jobs.as<int>() + w.jobs_off;
-            cudaEventRecord(pool_event(ctx, w0), st);
-            if (precision == LQG_PRECISION_MIXED) launch_scales_mixed(b, st);
-            launch_build_q(b, st);
-            if (ctx->has_reso) launch_build_q_reso(b, st);
-            if ((rc = step("build_q", w.ld, nch))) return rc;
-            cudaEventRecord(pool_event(ctx, w0 + 1), st);
-            if (precision == LQG_PRECISION_MIXED)
-                launch_products_mixed(b, st, d_jobs, w.njobs, ctx->d_jobs.as<int>() + w.jobs2_off, w.njobs2);
-            else
-                launch_products_fp64(b, st, d_jobs, w.njobs);
-            if ((rc = step("products", w.ld, nch))) return rc;
-            cudaEventRecord(pool_event(ctx, w0 + 3), st);
-            launch_finish(b, st);
-            if ((rc = step("finish", w.ld, nch))) return rc;
-            cudaEventRecord(pool_event(ctx, w0 + 4), st);
-            spans.push_back({w0, 2});
-            spans.push_back({w0 + 1, 3});
-            spans.push_back({w0 + 2, 4});
-            spans.push_back({w0 + 3, 5});
-            ctx->launches += b.launches;
-            ctx->waves++;
+        }
+        eacc = nev++;
+        record_event(pool_event(ctx, eacc), st);
+        launch_accumulate(ctx->d_meta.as<ChunkDesc>(), nb, ctx->d_results.as<double>(), ctx->d_status.as<int>(),
+                          ctx->nkz, ctx->d_fisher.as<double>(), ctx->d_dbt.as<double>(), st);
+        ctx->launches++;
+        record_event(ev_end, st);
+        return LQG_OK;
+    };
+    // the key of everything a captured iteration would bake in
+    std::vector<uintptr_t> key = {
+        (uintptr_t) ctx->batch_version, (uintptr_t) precision, (uintptr_t) sym, (uintptr_t) use_theta,
+        (uintptr_t) base.c_is_ff, (uintptr_t) ctx->d_fws.p, (uintptr_t) ctx->d_ws.p, (uintptr_t) ctx->d_halves.p,
+        (uintptr_t) ctx->d_gram.p, (uintptr_t) ctx->d_desc.p, (uintptr_t) ctx->d_jobs.p, (uintptr_t) ctx->d_scales.p,
+        (uintptr_t) ctx->d_fbounds.p, (uintptr_t) ctx->d_check.p, (uintptr_t) ctx->d_results.p,
+        (uintptr_t) ctx->d_status.p, (uintptr_t) ctx->d_meta.p, (uintptr_t) ctx->d_wave.p, (uintptr_t) ctx->d_flogw.p,
+        (uintptr_t) ctx->d_rw.p, (uintptr_t) ctx->d_sqiv2.p, (uintptr_t) ctx->d_niv.p};
+    if (ctx->graph && key == ctx->graph_key) {
+        LQG_CUDA_CHECK_RET(cudaGraphLaunch(ctx->graph, st));
+        ctx->launches = ctx->graph_launches;
+        ctx->waves = ctx->graph_waves;
+        spans = ctx->graph_spans;
+        eacc = ctx->graph_eacc;
+    } else {
+        if (ctx->graph) {
+            cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+        }
+        const bool capture = !sync_each && !ctx->graph_failed && key == ctx->last_key;
+        bool captured = false;
+        if (capture && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            rc = launch_all();
+            cudaGraph_t g = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(st, &g);
+            cudaGraphExec_t ge = nullptr;
+            if (rc == LQG_OK && ec == cudaSuccess && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+                captured = true;
+                ctx->graph = ge;
+                ctx->graph_key = key;
+                ctx->graph_launches = ctx->launches;
+                ctx->graph_waves = ctx->waves;
+                ctx->graph_spans = spans;
+                ctx->graph_eacc = eacc;
+            } else {
+                ctx->graph_failed = true;
+            }
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (captured) {
+                LQG_CUDA_CHECK_RET(cudaGraphLaunch(ctx->graph, st));
+            }
+        }
+        if (!captured) {
+            spans.clear();
+            ctx->launches = 0;
+            ctx->waves = 0;
+            if ((rc = launch_all())) return rc;
         }
     }
-    const size_t eacc = nev++;
-    cudaEventRecord(pool_event(ctx, eacc), st);
-    launch_accumulate(ctx->d_meta.as<ChunkDesc>(), nb, ctx->d_results.as<double>(), ctx->d_status.as<int>(),
-                      ctx->nkz, ctx->d_fisher.as<double>(), ctx->d_dbt.as<double>(), st);
-    ctx->launches++;
-    cudaEventRecord(ev_end, st);
+    ctx->last_key = key;
     unsigned long long *chk = reinterpret_cast<unsigned long long *>(hs);
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(chk, ctx->d_check.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->last_status.data(), ctx->d_status.p, nb * 4, cudaMemcpyDeviceToHost, st));
@@ -959,12 +1028,13 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     // [6] accumulation, [7] whole iteration
     for (auto &sp : spans) {
         float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->evpool[sp.first], ctx->evpool[sp.first + 1]);
-        ctx->timings[sp.second] += ms;
+        if (cudaEventElapsedTime(&ms, ctx->evpool[sp.first], ctx->evpool[sp.first + 1]) == cudaSuccess)
+            ctx->timings[sp.second] += ms;
     }
     float ta = 0, tt = 0;
-    cudaEventElapsedTime(&ta, ctx->evpool[eacc], ev_end);
-    cudaEventElapsedTime(&tt, ev_start, ev_end);
+    if (cudaEventElapsedTime(&ta, ctx->evpool[eacc], ev_end) != cudaSuccess) ta = 0;
+    if (cudaEventElapsedTime(&tt, ev_start, ev_end) != cudaSuccess) tt = 0;
+    cudaGetLastError();   // a timing query that failed leaves no error behind
     ctx->timings[6] = ta;
     ctx->timings[7] = tt;
     ctx->have_results = true;

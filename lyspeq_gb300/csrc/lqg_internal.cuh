@@ -201,6 +201,17 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
 void launch_scales_mixed(WaveArgs &a, cudaStream_t st);
 void launch_finish(WaveArgs &a, cudaStream_t st);
 
+// Timing event on the stream; inside a stream capture it becomes an external
+// event record node, which (unlike the default internal one) can be timed
+// (the external flag is refused outside a capture)
+inline void record_event(cudaEvent_t e, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    else
+        cudaEventRecord(e, st);
+}
+
 bool tc_available();
 int gram_splits_mixed(int64_t K);
 // Elements of one compact upper-triangle slot of the whitened form: the

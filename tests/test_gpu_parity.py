@@ -79,3 +79,28 @@ def test_empty_batch_iterates_to_zero(engine_lib, precision):
     out = eng.download()
     assert not out["fisher"].any() and not out["d"].any() and not out["b"].any() and not out["t"].any()
     eng.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_replayed_iterations_are_identical(engine_lib, precision):
+    """From the second iteration on an unchanged batch the launches are
+    captured in a CUDA graph and replayed: results stay bit-identical, and a
+    changed theta (read from device memory by the graph) still takes effect."""
+    c = G.load("tiny_marg1")
+    eng, _ = make_engine(c)
+    outs = []
+    for _ in range(4):
+        eng.iterate(precision=precision)
+        outs.append(eng.download())
+    for o in outs[1:]:
+        assert np.array_equal(o["fisher"], outs[0]["fisher"]) and np.array_equal(o["d"], outs[0]["d"])
+        assert np.array_equal(o["b"], outs[0]["b"]) and np.array_equal(o["t"], outs[0]["t"])
+    theta = 0.1 * c.g["theta"]
+    eng.iterate(theta=theta, precision=precision)
+    a = eng.download()
+    eng.iterate(theta=theta, precision=precision)
+    eng.iterate(theta=theta, precision=precision)
+    b = eng.download()
+    assert np.array_equal(a["fisher"], b["fisher"]) and np.array_equal(a["d"], b["d"])
+    assert not np.array_equal(a["fisher"], outs[0]["fisher"])
+    eng.close()
