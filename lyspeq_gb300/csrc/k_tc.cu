@@ -225,6 +225,7 @@ constexpr int TC_THREADS = 320;             // producer, MMA, 8 epilogue warps
 constexpr int R_THREADS = TC_THREADS;
 constexpr int kGramK = 32768;               // K elements per Gram split
 constexpr int kGemmDrain = 8;               // K blocks per drained hi*hi partial: products
+constexpr int kGemmDrainST = 2;             // the whitened form's S and N slots
 constexpr int kGramDrain = 2;               // and traces
 
 // Accumulation: the tensor cores round every fp32 accumulation of an MMA, with a
@@ -250,10 +251,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // the tiles of a persistent CTA.  Commits `done` after the tile's last MMA.
 // Returns false after a timed-out wait (abort flag set).
 // Stage layout: A hi, A lo, B hi, B lo.
-template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN, int DRAIN>
+template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN>
 __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned char *smem, uint64_t *full,
                                          uint64_t *empty, uint64_t *dfull, uint64_t *dempty, uint64_t *done,
-                                         int kblocks, uint32_t idesc, int &kb_all, int &g_all, int *abort_flag) {
+                                         int kblocks, int DRAIN, uint32_t idesc, int &kb_all, int &g_all,
+                                         int *abort_flag) {
     const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
     for (int g = 0; g < ngroups; ++g) {
         const int b = g_all & 1;
@@ -291,9 +293,9 @@ __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned cha
 // (registers are the limit: ten warps leave 168 per thread).  g_all runs on
 // across tiles like the issuer's.  Returns false (warp-uniform) if a wait
 // timed out or the CTA aborted.
-template <bool KAHAN, int DRAIN>
+template <bool KAHAN>
 __device__ __forceinline__ bool drain_tile(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
-                                           uint64_t *dempty, int kblocks, float (&sum)[64], int &g_all,
+                                           uint64_t *dempty, int kblocks, int DRAIN, float (&sum)[64], int &g_all,
                                            int *abort_flag) {
     const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
     bool alive = true;
@@ -380,6 +382,16 @@ __device__ __forceinline__ int tile_kblocks(const WaveArgs &a, const GemmTile &t
     return min(kblocks, end);
 }
 
+// hi*hi drain interval of a tile: the whitened signal and noise slots (B_ns =
+// W S W^T, B_{ns+1} = W N W^T, two of ns + 2 slots, which enter every t_k and
+// b_k) drain every 2 K blocks: their accumulation, not the operands, sets the
+// error of t and b (2 blocks for every slot cut b, t from 6e-6, 9e-6 to 1e-6,
+// 2e-6 on DESI-like chunks, at 28 % more product time)
+template <int STAGE>
+__device__ __forceinline__ int tile_drain(const WaveArgs &a, const GemmTile &tl) {
+    return (STAGE != 0 && tl.s >= a.chunks[tl.c].ns) ? kGemmDrainST : kGemmDrain;
+}
+
 template <int STAGE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
@@ -461,10 +473,11 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const int x = lt & 1;
             if (lt >= 2 && !mbar_wait(&xempty[x], ((lt >> 1) - 1) & 1)) { *abort_flag = 1; break; }
             fence_after();
-            const int kbt = tile_kblocks<STAGE>(a, gemm_tile<STAGE>(jobs, t, mt), kblocks);
-            if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN, kGemmDrain>(
+            const GemmTile tl = gemm_tile<STAGE>(jobs, t, mt);
+            const int kbt = tile_kblocks<STAGE>(a, tl, kblocks);
+            if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN>(
                     tmem, tmem + 2 * G_BN + x * G_BN, smem, full, empty, dfull, dempty, &xfull[x], kbt,
-                    idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag))
+                    tile_drain<STAGE>(a, tl), idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag))
                 break;
         }
         // every MMA of this CTA completes before its tensor memory is freed
@@ -484,8 +497,8 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             float sum[64];
 #pragma unroll
             for (int j = 0; j < 64; ++j) sum[j] = 0.f;
-            bool got = drain_tile<false, kGemmDrain>(tmem, lane_addr, col0, dfull, dempty,
-                                                     tile_kblocks<STAGE>(a, tl, kblocks), sum, g_all, abort_flag);
+            bool got = drain_tile<false>(tmem, lane_addr, col0, dfull, dempty, tile_kblocks<STAGE>(a, tl, kblocks),
+                                         tile_drain<STAGE>(a, tl), sum, g_all, abort_flag);
             const int x = lt & 1;
             got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1)) && !*abort_flag;
             if (!got) break;
@@ -678,9 +691,9 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             mbar_wait(&full[kb % R_STAGES], (kb / R_STAGES) & 1);
     } else if (warp == 1 && lane == 0) {
         int kb_all = 0, g_all = 0;
-        mma_tile<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN, kGramDrain>(tmem, tmem + 2 * R_BN, smem, full, empty, dfull,
-                                                               dempty, accum, kblocks, idesc_f16(R_BM, R_BN),
-                                                               kb_all, g_all, abort_flag);
+        mma_tile<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN>(tmem, tmem + 2 * R_BN, smem, full, empty, dfull,
+                                                               dempty, accum, kblocks, kGramDrain,
+                                                               idesc_f16(R_BM, R_BN), kb_all, g_all, abort_flag);
         // every MMA completes before the tensor memory is freed
         umma_commit(mdone);
         mbar_wait(mdone, 0);
@@ -692,8 +705,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
 #pragma unroll
         for (int j = 0; j < 64; ++j) sum[j] = 0.f;
         int g_all = 0;
-        const bool alive = drain_tile<true, kGramDrain>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, sum, g_all,
-                                                        abort_flag);
+        const bool alive = drain_tile<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, kGramDrain, sum,
+                                            g_all, abort_flag);
         const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
         fence_after();
         if (got) {
