@@ -138,3 +138,61 @@ def test_natural_cspline_matches_scipy():
     t = np.linspace(x[0], x[-1], 97)
     mine = np.array([P.cspline_eval(x, y, mm, u) for u in t])
     assert np.max(np.abs(mine - ref(t))) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["tiny_marg1", "tiny_marg3", "tiny_masked", "tiny_smooth"])
+def test_whitened_form_identities(name):
+    """The algebra of the mixed path's whitened form, in FP64 on the CPU: with
+    C~ = L L^T (C~ = D C D + I, D = diag(sqrt(ivar))), T = L^-1 D and P = I - U U^T
+    for U the Gram-Schmidt basis of the whitened continuum templates {T v}
+    (taken in the reference's order), W = P T gives W^T W = the reference's
+    marginalised C^-1, and F_ij = <W Q_i W^T, W Q_j W^T>, t_i = <W Q_i W^T, W S W^T>,
+    b_i = <W Q_i W^T, W N W^T> (N of the raw ivar) reproduce its traces."""
+    c = G.load(name)
+    s = c.port_settings(P)
+    keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
+    tvs = [P.table_view(t, c.bins, c.nv, c.lenv, c.nzp) for t in c.tables]
+    lam, delta, ivar, r = c.chunks[0]
+    ch = P.make_chunk(lam, delta, ivar, r, c.bins, keys, s)
+    stored, q, sm = P.build_matrices(ch, c.bins, tvs[ch.res_index])
+    theta = np.zeros(c.bins.nkz)
+    cinv = P._sym_upper(P.inverse_covariance(ch, stored, q, sm, theta, s))
+    ivc = P.smooth_ivar(ch.ivar, s.smooth_noise_weights) if s.smooth_noise_weights >= 0 else ch.ivar
+    dd = np.sqrt(ivc)
+    n = ch.n
+    L = np.linalg.cholesky(dd[:, None] * sm * dd[None, :] + np.eye(n))
+    T = np.linalg.solve(L, np.diag(dd))
+    W = T.copy()
+    if s.cont_nvecs > 0:
+        vecs = [np.full(n, 1.0 / np.sqrt(n))]
+        for m in range(1, s.cont_logl_order + 1):
+            v = np.log(ch.wave) ** m
+            vecs.append(v / np.linalg.norm(v))
+        for m in range(1, s.cont_l_order + 1):
+            v = ch.wave ** m
+            vecs.append(v / np.linalg.norm(v))
+        u, sv, _ = np.linalg.svd(np.stack(vecs, axis=1), full_matrices=False)
+        basis = []
+        for k in range(len(sv)):
+            if not sv[k] / sv[0] > P.DOUBLE_EPSILON:
+                break
+            w = T @ u[:, k]
+            for b in basis:
+                w = w - (b @ w) * b
+            basis.append(w / np.linalg.norm(w))
+        U = np.stack(basis, axis=1)
+        W = T - U @ (U.T @ T)
+    assert np.max(np.abs(W.T @ W - cinv)) <= TOL.get(name, 1e-11) * np.max(np.abs(cinv))
+    d, b, t, f = P.chunk_iteration(ch, c.bins, tvs[ch.res_index], theta, s)
+    nvec = np.where(ch.ivar != 0, 1.0 / np.where(ch.ivar != 0, ch.ivar, 1.0), 0.0)
+    B = [W @ q[k] @ W.T for k in range(len(stored))]
+    MS, MN = W @ sm @ W.T, (W * nvec[None, :]) @ W.T
+    idx = np.array(stored)
+    fw = np.array([[np.sum(B[i] * B[j]) for j in range(len(B))] for i in range(len(B))])
+    tw = np.array([np.sum(Bk * MS) for Bk in B])
+    bw = np.array([np.sum(Bk * MN) for Bk in B])
+    # 1e-7: the (2, 1)-template case fixes the projected inverse only to ~1e-8
+    # (singular values of the templates span 3e-9); the others agree to ~1e-13
+    tol = TOL.get(name, 1e-11)
+    assert G.rel_err(np.triu(fw), f[np.ix_(idx, idx)]) < tol
+    assert G.rel_err(tw, t[idx]) < tol and G.rel_err(bw, b[idx]) < tol
