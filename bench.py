@@ -2,7 +2,7 @@
 """Benchmark: chunks/s of one Newton-Raphson iteration of lyspeq's per-chunk
 QMLE on one GB300, mixed precision vs FP64, with the CPU baseline beside it.
 
-Workload (BASELINE "DESI-like" configuration): 4096 synthetic chunks, N_pix
+Workload (the DESI-like configuration): 4096 synthetic chunks, N_pix
 log-uniform in [200, 1200], dv = 50 km/s, R uniform in [2000, 5000], 35 k bins,
 13 triangular z bins, S/N per pixel lognormal(ln 1, 0.8), continuum
 marginalisation of amplitude + slope.  Inputs are seeded synthetic data of
