@@ -53,7 +53,12 @@ CASES = {
     # SmoothResolutionMatrix (the matrices' diagonals smoothed before
     # deconvolution) with SmoothNoiseWeights 2
     "tiny_reso_smooth": ("tiny_reso", None, (-1, -1), 0.0, None),
+    # top-hat redshift bins (RedshiftBinningMethod 0, bins::zBinTopHat)
+    "tiny_tophat": ("tiny", None, (1, -1), 0.0, None),
 }
+
+# cases whose redshift bins are top hats instead of triangles
+TOPHAT = {"tiny_tophat"}
 
 # config keys set for a case: SmoothNoiseWeights and RedshiftGrowthOn
 # (the growth exponent is the fiducial FiducialRedshiftPower)
@@ -82,6 +87,8 @@ def make_case(name, spec):
     iters = spec[6] if len(spec) > 6 else 1
     w = synth.make_workload(wl, n_chunks=nch)
     w.cont_logl_order, w.cont_l_order = marg
+    if name in TOPHAT:
+        w.bins.triangular = False
     _mask(w, mask, 99)
     with tempfile.TemporaryDirectory() as tmp:
         cfg = synth.write_reference_inputs(w, tmp)

@@ -11,7 +11,7 @@ from lyspeq_gb300 import synth
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub",
          "tiny_reso", "tiny_reso_dia", "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth",
-         "tiny_reso_smooth"]
+         "tiny_reso_smooth", "tiny_tophat"]
 RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth", "tiny_reso_smooth"]
 
 

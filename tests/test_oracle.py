@@ -140,7 +140,7 @@ def test_natural_cspline_matches_scipy():
     assert np.max(np.abs(mine - ref(t))) < 1e-12
 
 
-@pytest.mark.parametrize("name", ["tiny_marg1", "tiny_marg3", "tiny_masked", "tiny_smooth"])
+@pytest.mark.parametrize("name", ["tiny_marg1", "tiny_marg3", "tiny_masked", "tiny_smooth", "tiny_tophat"])
 def test_whitened_form_identities(name):
     """The algebra of the mixed path's whitened form, in FP64 on the CPU: with
     C~ = L L^T (C~ = D C D + I, D = diag(sqrt(ivar))), T = L^-1 D and P = I - U U^T
