@@ -55,6 +55,8 @@ CASES = {
     "tiny_reso_smooth": ("tiny_reso", None, (-1, -1), 0.0, None),
     # top-hat redshift bins (RedshiftBinningMethod 0, bins::zBinTopHat)
     "tiny_tophat": ("tiny", None, (1, -1), 0.0, None),
+    # TurnOffBaseline: C without the fiducial signal, no t trace
+    "tiny_nosfid": ("tiny", None, (1, -1), 0.0, None),
 }
 
 # cases whose redshift bins are top hats instead of triangles
@@ -67,6 +69,7 @@ OPTIONS = {
     "tiny_smooth_mean": {"SmoothNoiseWeights": 0},
     "tiny_reso_growth": {"RedshiftGrowthOn": 1},
     "tiny_reso_smooth": {"SmoothNoiseWeights": 2, "SmoothResolutionMatrix": 1},
+    "tiny_nosfid": {"TurnOffBaseline": 1},
 }
 
 
@@ -122,10 +125,12 @@ def make_case(name, spec):
         g_fisher=dump.fisher, g_dbt=dump.dbt, g_theta=dump.theta, g_solver=dump.solver_invfisher,
         g_inverse=dump.inverse_fisher, g_damped=np.array(dump.damped),
         g_complete=np.array(keep is None),
-        # SmoothNoiseWeights, RedshiftGrowthOn, FiducialRedshiftPower
+        # SmoothNoiseWeights, RedshiftGrowthOn, FiducialRedshiftPower,
+        # SmoothResolutionMatrix, TurnOffBaseline
         opts=np.array([OPTIONS.get(name, {}).get("SmoothNoiseWeights", -1),
                        OPTIONS.get(name, {}).get("RedshiftGrowthOn", -1), w.fid[3],
-                       OPTIONS.get(name, {}).get("SmoothResolutionMatrix", -1)], dtype=float),
+                       OPTIONS.get(name, {}).get("SmoothResolutionMatrix", -1),
+                       OPTIONS.get(name, {}).get("TurnOffBaseline", -1)], dtype=float),
     )
     if it is not None:
         out["it_n"] = np.array(iters)

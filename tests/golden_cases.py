@@ -11,7 +11,7 @@ from lyspeq_gb300 import synth
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", "desi_sub",
          "tiny_reso", "tiny_reso_dia", "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth",
-         "tiny_reso_smooth", "tiny_tophat"]
+         "tiny_reso_smooth", "tiny_tophat", "tiny_nosfid"]
 RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth", "tiny_reso_smooth"]
 
 
@@ -40,16 +40,17 @@ class GoldenCase:
     rmats: list | None = None
     src: list | None = None
     spectra: list | None = None
-    # SmoothNoiseWeights, RedshiftGrowthOn and its exponent, as Engine keywords
+    # SmoothNoiseWeights, RedshiftGrowthOn and its exponent, TurnOffBaseline, as Engine keywords
     opts: dict = dataclasses.field(default_factory=lambda: dict(smooth_noise_weights=-1, redshift_growth=False,
-                                                                  fid_b=0.0))
+                                                                  fid_b=0.0, turn_off_sfid=False))
     smooth_rmat: bool = False
 
     def port_settings(self, P):
         """The oracle's Settings for this case."""
         return P.Settings(max_forest_length=self.max_forest_length, cont_logl_order=self.marg[0],
                           cont_l_order=self.marg[1], smooth_noise_weights=self.opts["smooth_noise_weights"],
-                          redshift_growth=self.opts["redshift_growth"], growth_b=self.opts["fid_b"])
+                          redshift_growth=self.opts["redshift_growth"], growth_b=self.opts["fid_b"],
+                          turn_off_sfid=self.opts["turn_off_sfid"])
 
 
 _cache = {}
@@ -80,7 +81,8 @@ def load(name: str) -> GoldenCase:
                       chunks, meta, dbt, fis, g, bool(z["g_complete"]))
     if "opts" in z.files:
         o = z["opts"]
-        case.opts = dict(smooth_noise_weights=int(o[0]), redshift_growth=bool(o[1] > 0), fid_b=float(o[2]))
+        case.opts = dict(smooth_noise_weights=int(o[0]), redshift_growth=bool(o[1] > 0), fid_b=float(o[2]),
+                         turn_off_sfid=bool(len(o) > 4 and o[4] > 0))
         # SmoothResolutionMatrix: applied while the matrices are prepared
         case.smooth_rmat = len(o) > 3 and o[3] > 0 and o[0] >= 0
     if "it_n" in z.files:

@@ -16,7 +16,8 @@ import golden_cases as G
 pytestmark = pytest.mark.gpu
 MIXED_TOL = 1e-5
 CASES = ["tiny_nomarg", "tiny_marg1", "tiny_masked", "small_cfg", "desi_sub", "tiny_reso", "tiny_reso_dia",
-         "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth", "tiny_reso_smooth", "tiny_tophat"]
+         "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth", "tiny_reso_smooth", "tiny_tophat",
+         "tiny_nosfid"]
 
 
 def make_engine(c):

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import golden_cases as G
+from oracle import qmle_port as P
 
 pytestmark = pytest.mark.gpu
 
@@ -103,4 +104,65 @@ def test_replayed_iterations_are_identical(engine_lib, precision):
     b = eng.download()
     assert np.array_equal(a["fisher"], b["fisher"]) and np.array_equal(a["d"], b["d"])
     assert not np.array_equal(a["fisher"], outs[0]["fisher"])
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_direct"])
+def test_precomputed_fisher_skips_only_the_fisher_matrix(engine_lib, precision):
+    """PrecomputedFisher (Chunk::computePSbeforeFvector returns before the
+    Fisher loop, core/chunk_estimate.cpp:805-807): d, b and t are the
+    reference's, the chunk Fisher matrices and their sum stay zero."""
+    c = G.load("tiny_marg1")
+    tol = 1e-10 if precision == "fp64" else 1e-5
+    eng, st = make_engine(c, skip_fisher=True)
+    assert (st == 0).all()
+    eng.iterate(precision=precision)
+    out = eng.download()
+    assert not out["fisher"].any()
+    for i, dbt in enumerate(c.dbt):
+        d, b, t, f = eng.chunk_result(i)
+        assert not f.any()
+        errs = (G.rel_err(d, dbt[0]), G.rel_err(b, dbt[1]), G.rel_err(t, dbt[2]))
+        assert max(errs) < tol, (i, errs)
+    assert G.rel_err(np.stack([out["d"], out["b"], out["t"]]), c.g["dbt"]) < tol
+    eng.close()
+
+
+def test_rejected_chunks_get_their_status_and_leave_the_rest(engine_lib):
+    """Chunks the reference would drop (Chunk::Chunk throws, the caller logs
+    and skips it, core/chunk_estimate.cpp:905-913) come back with an
+    LQG_CHUNK_* status, stay out of the batch and leave the other chunks'
+    results and the sums as the reference's."""
+    from lyspeq_gb300 import lqg
+    c = G.load("tiny_marg1")
+    lam, delta, ivar, r = c.chunks[0]
+    masked = np.zeros_like(ivar)
+    nan_delta = delta.copy()
+    nan_delta[5] = np.nan
+    bad = [((lam[:10], delta[:10], ivar[:10], r), 1),          # LQG_CHUNK_SHORT
+           ((lam, delta, masked, r), 3),                        # LQG_CHUNK_EMPTY
+           ((lam, nan_delta, ivar, r), 6),                      # LQG_CHUNK_BAD_INPUT
+           ((lam, delta, ivar, 123456), 2),                     # LQG_CHUNK_NO_TABLE
+           ((lam * 1.5, delta, ivar, r), 4)]                    # LQG_CHUNK_OUT_OF_RANGE
+    s = c.port_settings(P)
+    keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
+    for (bl, bd, bi, br), _ in [bad[0], bad[3]]:
+        with pytest.raises((ValueError, KeyError)):   # the oracle's Chunk::Chunk throws too
+            P.make_chunk(bl, bd, bi, br, c.bins, keys, s)
+    batch, want = [], []
+    for i, ch in enumerate(c.chunks):
+        batch += [bad[i][0]] if i < len(bad) else []
+        want += [bad[i][1]] if i < len(bad) else []
+        batch.append(ch)
+        want.append(0)
+    eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg, **c.opts)
+    st = eng.add_chunk_list(batch)
+    assert list(st) == want
+    assert eng.size == len(c.chunks)
+    eng.iterate(precision="fp64")
+    out = eng.download()
+    for i, (dbt, fis) in enumerate(zip(c.dbt, c.fisher)):
+        d, b, t, f = eng.chunk_result(i)
+        assert max(G.rel_err(d, dbt[0]), G.rel_err(b, dbt[1]), G.rel_err(t, dbt[2]), G.fisher_err(f, fis)) < 1e-10
+    assert G.rel_err(np.stack([out["d"], out["b"], out["t"]]), c.g["dbt"]) < 1e-10
     eng.close()
