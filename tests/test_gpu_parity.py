@@ -166,3 +166,35 @@ def test_rejected_chunks_get_their_status_and_leave_the_rest(engine_lib):
         assert max(G.rel_err(d, dbt[0]), G.rel_err(b, dbt[1]), G.rel_err(t, dbt[2]), G.fisher_err(f, fis)) < 1e-10
     assert G.rel_err(np.stack([out["d"], out["b"], out["t"]]), c.g["dbt"]) < 1e-10
     eng.close()
+
+
+def test_last_k_edge_band_matches_oracle(engine_lib):
+    """LastKEdge above the last regular edge adds one k band (bins::setUpBins,
+    core/global_numbers.cpp:209-251).  The compiled reference cannot read
+    tables with that band, so the engine is checked against the oracle's
+    restatement on tables rebuilt for the extended bands."""
+    import dataclasses
+    from lyspeq_gb300 import lqg, synth
+    c = G.load("tiny_marg1")
+    bins = dataclasses.replace(c.bins, klast=0.08)
+    assert bins.nk == c.bins.nk + 1
+    tables = [synth.build_table(bins, t.r_fwhm, t.dv, c.nv, c.lenv, c.nzp) for t in c.tables]
+    s = c.port_settings(P)
+    keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(tables)}
+    tvs = [P.table_view(t, bins, c.nv, c.lenv, c.nzp) for t in tables]
+    theta = 0.02 * synth.pd13_power(np.tile(bins.k_centers, bins.nz), np.repeat(bins.z_centers, bins.nk),
+                                    synth.PD13_DEFAULT)
+    ref = []
+    for lam, delta, ivar, r in c.chunks:
+        ch = P.make_chunk(lam, delta, ivar, r, bins, keys, s)
+        assert ch.kbin_upp == bins.nk
+        ref.append(P.chunk_iteration(ch, bins, tvs[ch.res_index], theta, s))
+    eng = lqg.Engine(bins, tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg, **c.opts)
+    assert (eng.add_chunk_list(c.chunks) == 0).all()
+    for precision, tol in (("fp64", 1e-10), ("mixed", 1e-5)):
+        eng.iterate(theta=theta, precision=precision)
+        for i, (d0, b0, t0, f0) in enumerate(ref):
+            d, b, t, f = eng.chunk_result(i)
+            errs = (G.rel_err(d, d0), G.rel_err(b, b0), G.rel_err(t, t0), G.fisher_err(f, f0))
+            assert max(errs) < tol, (precision, i, errs)
+    eng.close()
