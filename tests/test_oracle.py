@@ -196,3 +196,35 @@ def test_whitened_form_identities(name):
     tol = TOL.get(name, 1e-11)
     assert G.rel_err(np.triu(fw), f[np.ix_(idx, idx)]) < tol
     assert G.rel_err(tw, t[idx]) < tol and G.rel_err(bw, b[idx]) < tol
+
+
+@pytest.mark.skipif(not refdump.available(), reason="compiled reference not built")
+@pytest.mark.parametrize("workload,nchunks", [("tiny", 1), ("tiny", 2), ("small", 1), ("small", 3)])
+def test_reading_and_chunking_match_reference(tmp_path, workload, nchunks):
+    """The restatement's reading and chunking (preprocess_spectrum: the reader's
+    cuts and masks; decide_indices: OneQSOEstimate::decideIndices,
+    core/one_qso_estimate.cpp:17-50; make_chunk: Chunk::Chunk's rejections)
+    builds the chunks the compiled reference builds from the same files, with
+    DynamicChunkNumber 1 and above (MaximumForestLength divided by it,
+    core/global_numbers.cpp:102-107)."""
+    w = synth.make_workload(workload)
+    cfg = synth.write_reference_inputs(w, str(tmp_path))
+    text = open(cfg).read()
+    assert "DynamicChunkNumber 1\n" in text
+    open(cfg, "w").write(text.replace("DynamicChunkNumber 1\n", f"DynamicChunkNumber {nchunks}\n"))
+    dump = refdump.run_driver(cfg, str(tmp_path / "dump.bin"))
+    s = P.Settings(max_forest_length=w.max_forest_length, number_of_chunks=nchunks,
+                   cont_logl_order=w.cont_logl_order, cont_l_order=w.cont_l_order)
+    mine = P.chunks_from_spectra(w.spectra, w.bins, w.table_index(), s)
+    key = lambda wave: (float(wave[0]), len(wave))
+    ref = {key(c.wave): c for c in dump.chunks}
+    assert len(ref) == len(dump.chunks) and len(mine) == len(dump.chunks)
+    for ch in mine:
+        c = ref[key(ch.wave)]
+        assert np.array_equal(ch.wave, c.wave)
+        assert np.array_equal(ch.delta, c.delta) and np.array_equal(ch.ivar, c.ivar)
+        assert (ch.fisher_index_start, ch.nq, ch.kbin_upp) == (c.fisher_index_start, c.nq, c.kbin_upp)
+    if nchunks > 1:
+        # the option did split spectra
+        assert len(mine) > len(P.chunks_from_spectra(w.spectra, w.bins, w.table_index(),
+                                                     P.Settings(max_forest_length=w.max_forest_length)))
