@@ -106,3 +106,44 @@ def test_cpp_facade_one_iteration_matches_the_oracle(tmp_path):
     r = subprocess.run([exe, path, "1e-9", loop], capture_output=True, text=True)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("workload", ["tiny", "small"])
+def test_cpp_chunking_matches_the_oracle(tmp_path, workload):
+    """Host-only: the facade's OneQSOEstimate::decideIndices cuts every cleaned
+    spectrum of the workload where the restatement's decide_indices does
+    (itself pinned to the compiled reference's chunks in tests/test_oracle.py),
+    for DynamicChunkNumber 1 to 3."""
+    from lyspeq_gb300 import build, synth
+    from oracle import qmle_port as P
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    lib = build.build()
+    exe = str(tmp_path / "decide_indices")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(HERE, "cpp", "decide_indices.cpp"), "-L", os.path.dirname(lib), "-llqg",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", exe], check=True)
+    w = synth.make_workload(workload)
+    waves = []
+    for s in w.spectra:
+        try:
+            waves.append(P.preprocess_spectrum(s, w.bins)[0])
+        except ValueError:
+            continue
+    cases, want = [], []
+    for nch in (1, 2, 3):
+        st = P.Settings(max_forest_length=w.max_forest_length, number_of_chunks=nch)
+        for wave in waves:
+            cases.append((w.max_forest_length, nch, wave))
+            want.append(P.decide_indices(wave, st))
+    path = tmp_path / "waves.bin"
+    with open(path, "wb") as out:
+        out.write(struct.pack("<q", len(cases)))
+        for mfl, nch, wave in cases:
+            out.write(struct.pack("<dqq", mfl, nch, len(wave)))
+            out.write(np.ascontiguousarray(wave, dtype="<f8").tobytes())
+    r = subprocess.run([exe, str(path)], capture_output=True, text=True, check=True)
+    got = [[int(x) for x in ln.split()] for ln in r.stdout.strip().split("\n")]
+    assert got == want
+    assert any(len(idx) > 2 for idx in want)      # some spectra were split
