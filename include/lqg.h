@@ -249,6 +249,13 @@ int lqg_fisher_solve(lqg_ctx *ctx, const double *fisher_sum, const double *dbt,
                      double *fisher, double *solver, double *inverse, double *weighted,
                      double *theta, int *damped, int *dof, double *damp);
 
+/* lqg_fisher_solve without a context, for nkz (k, z) bins: the same update
+ * for a caller that holds only the sums (the rank that reduced the other
+ * processes' sums).  Host only: needs no GPU. */
+int lqg_fisher_solve_n(int nkz, const double *fisher_sum, const double *dbt, double *fisher,
+                       double *solver, double *inverse, double *weighted, double *theta,
+                       int *damped, int *dof, double *damp);
+
 /* Device time (ms) of the phases of the last iteration, CUDA events on the
  * context stream, summed over the size-bucketed waves: [0] S and C build,
  * [1] FP64 factorisation, inverse and marginalisation, [2] Q_k build,

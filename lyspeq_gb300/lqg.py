@@ -25,7 +25,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
            "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate",
            "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients",
-           "lqg_resomat_smooth"]
+           "lqg_resomat_smooth", "lqg_fisher_solve_n"]
 
 
 class LqgBins(C.Structure):
@@ -87,6 +87,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_download.argtypes = [vp, dp, dp, dp, dp, ip]
     lib.lqg_chunk_result.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     lib.lqg_fisher_solve.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ip, ip, dp]
+    lib.lqg_fisher_solve_n.argtypes = [C.c_int, dp, dp, dp, dp, dp, dp, dp, ip, ip, dp]
     lib.lqg_last_timings.argtypes = [vp, dp, C.c_int]
     lib.lqg_last_launch_count.argtypes = [vp]
     lib.lqg_last_wave_count.argtypes = [vp]
@@ -291,6 +292,29 @@ class Engine:
 
     def wave_count(self):
         return self.lib.lqg_last_wave_count(self.h)
+
+
+def fisher_solve(fisher_sum, dbt):
+    """The Newton-Raphson update from the global sums alone (lqg_fisher_solve_n,
+    host only): fisher_sum nkz x nkz (upper triangle, unhalved), dbt 3 x nkz.
+    Returns the same dictionary as Engine.fisher_solve."""
+    lib = load_library()
+    fs = np.ascontiguousarray(fisher_sum, dtype=np.float64)
+    db = np.ascontiguousarray(dbt, dtype=np.float64)
+    n = fs.shape[0]
+    if fs.shape != (n, n) or db.shape != (3, n):
+        raise ValueError("fisher_sum must be nkz x nkz and dbt 3 x nkz")
+    out = {k: np.zeros((n, n)) for k in ("fisher", "solver", "inverse")}
+    w = np.zeros((3, n))
+    th = np.zeros(n)
+    damped, dof, damp = C.c_int(), C.c_int(), C.c_double()
+    rc = lib.lqg_fisher_solve_n(n, _dptr(fs), _dptr(db), _dptr(out["fisher"]), _dptr(out["solver"]),
+                                _dptr(out["inverse"]), _dptr(w), _dptr(th), C.byref(damped), C.byref(dof),
+                                C.byref(damp))
+    if rc != 0:
+        raise RuntimeError(f"lqg_fisher_solve_n failed with {rc}")
+    out.update(weighted=w, theta=th, damped=damped.value, dof=dof.value, damp=damp.value)
+    return out
 
 
 def bootstrap_coefficients(n_qso, nboots, seed=0, per_realization=False):

@@ -1,0 +1,72 @@
+"""The library's Newton-Raphson update (lqg_fisher_solve_n, host FP64) against
+lyspeq's own global results.
+
+Every complete golden fixture holds the reference's halved, symmetric Fisher
+matrix, the d, b, t sums, the solver and inverse matrices, theta and whether
+the damped solver was taken (OneDQuadraticPowerEstimate::iterate tail,
+core/quadratic_estimate.cpp:456-498; stableInvertSym,
+mathtools/matrix_helper.cpp:330-358).  The unhalved upper sum the engine
+accumulates is twice the halved matrix's upper triangle, which is exact.
+"""
+import numpy as np
+import pytest
+
+import golden_cases as G
+from oracle import qmle_port as P
+
+
+def _complete_cases():
+    return [n for n in G.CASES if G.load(n).complete]
+
+
+@pytest.mark.parametrize("name", _complete_cases())
+def test_library_update_matches_reference(engine_lib, name):
+    from lyspeq_gb300 import lqg
+    c = G.load(name)
+    # the condition number of the global Fisher matrix bounds the agreement
+    # of two FP64 inversions (LU here, LAPACK dgetrf/dgetri in the reference)
+    tol = max(1e-10, 1e-15 * np.linalg.cond(c.g["fisher"]))
+    fsum = 2.0 * np.triu(c.g["fisher"])
+    g = lqg.fisher_solve(fsum, c.g["dbt"])
+    assert np.array_equal(g["fisher"], c.g["fisher"])
+    assert g["damped"] == int(c.g["damped"])
+    assert G.rel_err(g["solver"], c.g["solver"]) < tol
+    assert G.rel_err(g["inverse"], c.g["inverse"]) < tol
+    assert G.rel_err(g["theta"], c.g["theta"]) < tol
+    # the oracle's restatement of the same step
+    o = P.newton_raphson_step(fsum, c.g["dbt"])
+    assert G.rel_err(g["theta"], o["theta"]) < tol
+
+
+def test_damped_solver_branch(engine_lib):
+    """A Fisher matrix whose spectrum has a jump above 8 takes the damped
+    solver (F^2 + s I)^-1 F, as the restatement does; a zero-diagonal bin
+    is held out and comes back as zero."""
+    from lyspeq_gb300 import lqg
+    rng = np.random.Generator(np.random.PCG64(5))
+    n = 12
+    # spectrum of the bins in use: ..., 10, 1, 0.05; the empty bin 4 enters
+    # the inversion as 1, so the smallest ratio is 1 / 0.05 = 20 > 8
+    q, _ = np.linalg.qr(rng.standard_normal((n - 1, n - 1)))
+    ev = np.concatenate([np.geomspace(1e4, 1e3, n - 4), [10.0, 1.0, 0.05]])
+    used = [i for i in range(n) if i != 4]
+    f = np.zeros((n, n))
+    f[np.ix_(used, used)] = (q * ev) @ q.T
+    fsum = 2.0 * np.triu(f)
+    dbt = rng.standard_normal((3, n))
+    g = lqg.fisher_solve(fsum, dbt)
+    o = P.newton_raphson_step(fsum, dbt)
+    assert g["damped"] == 1 == int(o["warn"])
+    assert g["solver"][4, 4] == 0 and g["inverse"][4, 4] == 0
+    # two FP64 solves of F^2 + s I agree to its condition number
+    sq = f.copy()               # F as the solve holds it: fsum halved, symmetric
+    sq[4, 4] = 1.0
+    tol = 1e-15 * np.linalg.cond(sq @ sq + o["damp"] * np.eye(n))
+    assert G.rel_err(g["solver"], o["solver"]) < tol
+    assert G.rel_err(g["theta"], o["theta"]) < tol
+
+
+def test_rejects_bad_shapes(engine_lib):
+    from lyspeq_gb300 import lqg
+    with pytest.raises(ValueError):
+        lqg.fisher_solve(np.zeros((3, 4)), np.zeros((3, 3)))
