@@ -867,7 +867,8 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         mwl = make_map(a.c_lo, 3, d3c, s3, boxb, &ok);
     }
     if (!ok) {
-        fprintf(stderr, "lqg: cuTensorMapEncodeTiled failed\n");
+        // nothing launched: the caller turns this into an error return
+        a.host_failed = 1;
         return;
     }
     static int n_sm = 0;

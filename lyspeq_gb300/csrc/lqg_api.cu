@@ -942,6 +942,8 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
                     launch_products_mixed(b, st, d_jobs, w.njobs, ctx->d_jobs.as<int>() + w.jobs2_off, w.njobs2);
                 else
                     launch_products_fp64(b, st, d_jobs, w.njobs);
+                if (b.host_failed)
+                    return set_err(ctx, LQG_ERR_CUDA, "products: TMA descriptor encoding (cuTensorMapEncodeTiled) failed");
                 if ((rc = step("products", w.ld, nch))) return rc;
                 record_event(pool_event(ctx, w0 + 3), st);
                 launch_finish(b, st);

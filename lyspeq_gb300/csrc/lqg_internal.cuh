@@ -157,6 +157,7 @@ struct WaveArgs {
     int gram_splits;
     double *scales;              // per-slot scales (mixed): q [slots], r, p and c
     int launches;
+    int host_failed;             // set by a launcher that could not launch (host side)
     cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
     // extents of the buffers above, used by the LQG_CHECKED build to validate indices
     int64_t ws_bytes, fws_bytes, results_elems, gram_elems, n_pix, n_fpix, n_rw;
