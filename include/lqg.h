@@ -56,6 +56,8 @@ extern "C" {
 #define LQG_CHUNK_BAD_INPUT 6   /* non-finite pixel values */
 #define LQG_CHUNK_TOO_LARGE 7   /* more pixels than the engine's maximum */
 #define LQG_CHUNK_TIMEOUT 8     /* a bounded device wait gave up; results dropped */
+#define LQG_CHUNK_INDEX_CHECK 9 /* self-checking build only: an index would have left
+                                   its buffer; the chunk was skipped */
 
 /* arithmetic of the per-chunk products */
 #define LQG_PRECISION_FP64 0    /* everything in IEEE binary64 */
@@ -64,6 +66,10 @@ extern "C" {
                                    fp16 hi/lo split products (3 terms, fp32 accumulation),
                                    traces F_ij = <B_i, B_j> over B's upper triangle, fp64
                                    reduction of partial sums */
+#define LQG_PRECISION_MIXED_AUTO 3 /* mixed, with the form (whitened or direct), the products'
+                                   drain interval and the Gram's K split chosen per padded
+                                   chunk size by the context's table (lqg_autotune,
+                                   lqg_tuning_set); MIXED's choices where it has none */
 #define LQG_PRECISION_MIXED_DIRECT 2 /* as MIXED but with the direct products A_k = C^-1 Q_k
                                    and F_ij = <A_i^T, A_j>: cheaper with continuum
                                    marginalisation, less accurate at high signal to noise
@@ -222,8 +228,46 @@ int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info);
  * into the global accumulators exactly as Chunk::oneQSOiteration does
  * (core/chunk_estimate.cpp:837-914): F upper triangle, NOT halved.
  * theta: TOTAL_KZ_BINS values (powerspectra_fits) or NULL for zeros.
- * Enqueued on the context stream; results stay on the device. */
+ * Runs on the context stream and returns when the iteration has finished;
+ * results stay on the device. */
 int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision);
+
+/* The same iteration, asynchronous: ordered after the work already enqueued
+ * on `stream` (a cudaStream_t; NULL: no ordering), and work enqueued on
+ * `stream` afterwards waits for it; returns once the launches are enqueued
+ * (planning, workspace allocation and the batch upload happen on the host
+ * before that, and the first iteration of a batch may wait for them).  theta
+ * is copied before the call returns.  lqg_sync, lqg_download,
+ * lqg_chunk_result, the bootstraps and the next iteration complete it (the
+ * chunk statuses, the index checks of the self-checking build and the phase
+ * timings are read then).  Replaces the per-chunk loop of
+ * OneDQuadraticPowerEstimate::iterate (core/quadratic_estimate.cpp:438-475),
+ * with a stream argument the reference does not have. */
+int lqg_nr_iteration_async(lqg_ctx *ctx, const double *theta, int precision, void *stream);
+/* Waits for the iteration lqg_nr_iteration_async enqueued; returns its status. */
+int lqg_sync(lqg_ctx *ctx);
+
+/* Autotuner of the mixed path's launch plan (no counterpart in the reference,
+ * whose only scheduling input is its cost model, core/chunk_estimate.cpp:
+ * 297-382).  For every padded chunk size (ld, a multiple of 64) in the
+ * current batch it runs the FP64 path on up to 4 chunks of that size and the
+ * mixed path on the same chunks with each candidate plan: whitened or direct
+ * form (flags & 1), hi*hi drain interval of the products 4, 8 or 16 K blocks
+ * (flags & 2); a candidate is kept when every per-chunk d, b, t (normwise)
+ * and Fisher element (normalised by sqrt(F_ii F_jj)) of the sample is within
+ * half of max_rel_err of the FP64 results (room for the chunks not sampled).
+ * The kept candidates are timed on up to max_chunks chunks of that size
+ * (device time of an iteration over them) and the fastest is stored; then the
+ * Gram's K elements per split, 16384, 32768 or 65536 (flags & 4), by time.
+ * LQG_PRECISION_MIXED_AUTO iterations use the table; the results of the
+ * batch's last iteration are invalidated.  flags = 0 means all (7);
+ * max_rel_err <= 0 means 1e-5; max_chunks <= 0 means 48. */
+int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, int flags);
+/* The table, one entry of 4 ints per padded size: ld, form (1 whitened, 0
+ * direct), drain interval, Gram K per split.  lqg_tuning_get returns the
+ * number of entries (writing at most n); lqg_tuning_set replaces the table. */
+int lqg_tuning_get(const lqg_ctx *ctx, int *entries, int n);
+int lqg_tuning_set(lqg_ctx *ctx, const int *entries, int n);
 
 /* Copy the accumulated results of the last iteration to host memory (any
  * pointer may be NULL): d, b, t [nkz] and fisher [nkz * nkz] (upper, not
@@ -310,6 +354,19 @@ int lqg_last_launch_count(const lqg_ctx *ctx);
  * (Q build, products, traces, reduction) is launched once per wave. */
 int lqg_last_wave_count(const lqg_ctx *ctx);
 
+/* Limit of every wait inside the tensor-core kernels of later iterations
+ * (seconds, at most 60; 0 restores the default of 2 s).  A wait that runs out
+ * makes its CTA stop, drain its own copies and MMAs, free its tensor memory
+ * and mark its chunks LQG_CHUNK_TIMEOUT; the iteration returns and the context
+ * stays usable.  No counterpart in the reference (its loops have no device
+ * waits); tests use a tiny limit to exercise that path without a fault. */
+int lqg_set_wait_limit(lqg_ctx *ctx, double seconds);
+
+/* Measured FP64 (DFMA) throughput of device `device` in TFLOP/s: independent
+ * FMA chains on every SM, best of five timed launches.  The denominator of the
+ * FP64 kernels' rooflines; no counterpart in the reference. */
+int lqg_probe_fp64_rate(int device, double *tflops);
+
 /* Factorisation of one chunk's covariance without allocating: no counterpart
  * in the reference (there it is part of Chunk::setInvertCovarianceMatrix,
  * _addMarginalizations and computePSbeforeFvector, core/chunk_estimate.cpp:
@@ -329,13 +386,16 @@ int lqg_last_wave_count(const lqg_ctx *ctx);
  *   cont_*      ContinuumLogLambdaMargOrder / ContinuumLambdaMargOrder
  *               (at most 4 template vectors, else LQG_ERR_UNSUPPORTED)
  *   y           out: C^-1 delta, ld values
- *   status      device int, out: LQG_CHUNK_OK or LQG_CHUNK_NOT_SPD.  The call
- *               sets it to LQG_CHUNK_OK first: nothing needs to start at zero.
+ *   status      device int, out: LQG_CHUNK_OK or LQG_CHUNK_NOT_SPD (and, in the
+ *               self-checking build, LQG_CHUNK_INDEX_CHECK).  The call sets it to
+ *               LQG_CHUNK_OK first: nothing needs to start at zero.
  * The static scratch is shared by every call on a device: two calls in flight
  * at the same time (other streams, other host threads) race on it and give
  * wrong results; order them (one stream, or events).  The first call on each
  * device looks up the scratch address and sets a kernel attribute; make it
- * before any stream capture. */
+ * before any stream capture.  The address is kept for the life of the
+ * process: resetting a device (cudaDeviceReset) while this library is loaded
+ * is not supported. */
 int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave, const double *delta,
                        const double *ivar, int cont_logl_order, int cont_l_order, double *y,
                        int *status, void *stream);

@@ -23,7 +23,7 @@ CHECKED_LIB = os.path.join(HERE, "liblqg_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["lqg_api.cu", "lqg_fisher.cu", "k_fp64.cu", "k_factor.cu", "k_accum.cu", "k_tc.cu",
            "lqg_noalloc.cu", "lqg_reso.cu", "lqg_tables.cu",
-           "lqg_boot.cu", "lqg_smooth.cu"]
+           "lqg_boot.cu", "lqg_smooth.cu", "lqg_probe.cu"]
 
 
 def nvcc_path() -> str:

@@ -802,6 +802,22 @@ __device__ void whitened_factor(const WaveArgs &a, const ChunkDesc &ch, float2 *
     }
 }
 
+// The marginalised C^-1 of the whitened form in FP64 at o_m, from the df64
+// inverse factor X = L^-1 (left in place for W): a copy of X, C^-1 = D X^T X D
+// (lauum_df) and the reference's rank-1 removals.  k_dx_mixed contracts it
+// with every Q_s for x_s = tr(Q_s C^-1), from which k_finish forms
+// d_s - b_s - t_s without the 22-bit trace products.
+__device__ void marginal_inverse_df(const WaveArgs &a, const ChunkDesc &ch, const float2 *X2, int nb,
+                                    double *scratch, FactorSmem &s) {
+    const int ld = ch.ld, n = ch.n;
+    float2 *M2 = reinterpret_cast<float2 *>(a.fws + ch.o_m);
+    for (size_t e = threadIdx.x; e < (size_t) nb * FB * ld; e += FTH) M2[e] = X2[e];
+    __syncthreads();
+    lauum_df(M2, ld, nb, n, a.ivar + ch.pix, scratch, s);
+    if (a.cont_logl >= 0 || a.cont_l >= 0)
+        marginalize_all(reinterpret_cast<double *>(M2), ld, n, a.wave + ch.pix, a.cont_logl, a.cont_l, scratch, s);
+}
+
 template <bool DF>
 __global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -810,12 +826,16 @@ __global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
     const ChunkDesc &ch = a.chunks[c];
     if (a.status[ch.gidx] != LQG_CHUNK_OK) return;
     const int ld = ch.ld, n = ch.n, nb = (n + FB - 1) / FB;
-    if (!LQG_IN_BOUNDS(a, ch.o_c + (int64_t) ld * ld * 8 <= a.fws_bytes &&
-                              ch.o_fscr + (int64_t) FB * ld * 8 <= a.fws_bytes &&
-                              ch.o_y + (int64_t) ld * 8 <= a.fws_bytes && nb * FB <= ld && ch.o_c >= 0 &&
-                              ch.o_fscr >= 0 && ch.o_y >= 0 && ch.pix >= 0 && ch.pix + n <= a.n_pix,
-                       10, c, ch.o_fscr))
+    if (!LQG_IN_BOUNDS(a, (a.ext_cy || (ch.o_c >= 0 && ch.o_c + (int64_t) ld * ld * 8 <= a.fws_bytes &&
+                                         ch.o_y >= 0 && ch.o_y + (int64_t) ld * 8 <= a.fws_bytes)) &&
+                              ch.o_fscr >= 0 && ch.o_fscr + (int64_t) FB * ld * 8 <= a.fws_bytes &&
+                              nb * FB <= ld && ch.pix >= 0 && ch.pix + n <= a.n_pix &&
+                              (!ch.cinv_m || (ch.o_m >= 0 && ch.o_m + (int64_t) ld * ld * 8 <= a.fws_bytes)),
+                       10, c, ch.o_fscr)) {
+        // only the self-checking build gets here: skip the chunk, visibly
+        if (threadIdx.x == 0) a.status[ch.gidx] = LQG_CHUNK_INDEX_CHECK;
         return;
+    }
     double *A = reinterpret_cast<double *>(a.fws + ch.o_c);
     double *scratch = reinterpret_cast<double *>(a.fws + ch.o_fscr);
     const double *iv = a.ivar + ch.pix;
@@ -837,7 +857,11 @@ __global__ void __launch_bounds__(FTH, 3) k_factor_tiled(WaveArgs a) {
         __syncthreads();
         trtri_df(A2, ld, nb, reinterpret_cast<float2 *>(scratch), s);
         __syncthreads();
-        if (a.sym) {
+        if (ch.sym) {
+            if (ch.cinv_m) {
+                marginal_inverse_df(a, ch, A2, nb, scratch, s);
+                __syncthreads();
+            }
             whitened_factor(a, ch, A2, scratch, s);
             return;
         }
@@ -896,13 +920,19 @@ size_t factor_smem_bytes() { return sizeof(FactorSmem); }
 // products in df64 on the FP32 pipe (the diagonal-block Cholesky and inverse,
 // the scaling and the marginalisation stay FP64).
 void launch_factor_all(WaveArgs &a, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_factor_tiled<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int) sizeof(FactorSmem));
-        cudaFuncSetAttribute(k_factor_tiled<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int) sizeof(FactorSmem));
-        attr = true;
+    // FactorSmem is above the 48 KB default: the attribute, once per device
+    static std::atomic<unsigned long long> attr{0};
+    const bool ready = once_per_device(attr, [](int) {
+        cudaError_t e = cudaFuncSetAttribute(k_factor_tiled<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int) sizeof(FactorSmem));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_factor_tiled<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int) sizeof(FactorSmem));
+        return e;
+    });
+    if (!ready) {
+        a.host_failed = 1;
+        return;
     }
     if (a.precision == LQG_PRECISION_MIXED)
         k_factor_tiled<true><<<a.n_chunks, FTH, sizeof(FactorSmem), st>>>(a);

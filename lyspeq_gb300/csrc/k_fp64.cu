@@ -91,6 +91,28 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // ---------------------------------------------------------------------------
+// theta-weighted derivative tables, one row per ((table, KBIN_UPP), z bin):
+// ttab[(cb nz + zm) nv + v] = sum_{kn < KBIN_UPP} theta[zm nk + kn] deriv[table][kn][v];
+// the mixed path also gets the rows as double-float pairs (ttab_ff non-null).
+__global__ void k_theta_tables(const double *deriv, const double *theta, const int *combos, int nk, int nz,
+                               int nv, double *ttab, float2 *ttab_ff) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x, zm = blockIdx.y, cb = blockIdx.z;
+    if (v >= nv) return;
+    const int res = combos[2 * cb], kup = combos[2 * cb + 1];
+    double acc = 0.0;
+    for (int kn = 0; kn < kup; ++kn) {
+        const double th = theta[zm * nk + kn];
+        if (th != 0.0) acc += th * deriv[((size_t) res * nk + kn) * nv + v];
+    }
+    const size_t o = ((size_t) cb * nz + zm) * nv + v;
+    ttab[o] = acc;
+    if (ttab_ff) {
+        const float h = (float) acc;
+        ttab_ff[o] = make_float2(h, (float) (acc - (double) h));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Phase A, K1a: S_fid and C~ = D (S + sum_s theta_s Q_s) D + I.
 __global__ void k_build_s_c(WaveArgs a) {
     const int c = blockIdx.y;
@@ -123,17 +145,17 @@ __global__ void k_build_s_c(WaveArgs a) {
         S[idx] = s;
         double cv = a.turn_off_sfid ? 0.0 : s;
         if (a.theta) {
+            // sum_s theta_s Q_s (core/chunk_estimate.cpp:674-683): interpolation is
+            // linear, so the k bands of one redshift bin come from one
+            // theta-weighted table row, r_T(v) = sum_kn theta_kn r_kn(v)
             int nidx;
             double dn;
             vindex(a.grid, v, nidx, dn);
-            for (int sl = 0; sl < ch.ns; ++sl) {
-                int iz = sl / ch.kbin_upp, kn = sl % ch.kbin_upp;
-                double th = a.theta[ch.fis + iz * bins.nk + kn];
-                if (th == 0.0) continue;
-                const double *row = a.deriv + ((size_t) ch.res * bins.nk + kn) * a.grid.nv;
-                double q = row[nidx] * (1 - dn) + row[nidx + 1] * dn;
-                q *= zfactor(bins, ch.zb0 + iz, z);
-                cv += th * q;
+            const int nzb = ch.ns / ch.kbin_upp;
+            for (int iz = 0; iz < nzb; ++iz) {
+                const double *row = a.ttab + ((size_t) ch.tcombo * bins.nz + ch.zb0 + iz) * a.grid.nv;
+                const double w = zfactor(bins, ch.zb0 + iz, z);
+                if (w != 0.0) cv += (row[nidx] * (1 - dn) + row[nidx + 1] * dn) * w;
             }
         }
         const double di = sq[i], dj = sq[j];
@@ -185,7 +207,32 @@ __global__ void k_build_s_c_ff(WaveArgs a) {
             val = ff_fma(ff_mul(tab[ind + gr.nzp + 1], fx), fy, val);
         }
         S[idx] = val;
-        float2 cv = ff_mul(ff_mul(sq[i], val), sq[j]);
+        float2 sv = a.turn_off_sfid ? zero : val;
+        if (a.ttab_ff) {
+            // sum_s theta_s Q_s from the theta-weighted rows (see k_build_s_c), in
+            // double-float: the row interpolated at v (the signal table's v grid),
+            // times the redshift weight (and growth factor)
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            float2 fv;
+            int nvx;
+            ff_index(ff_mul(ff_sub(lw[hi], lw[lo]), kv), gr.nv - 2, nvx, fv);
+            float zp, ze;
+            two_prod_ff(sw[lo], sw[hi], zp, ze);
+            const DeviceBins &bins = *a.bins;
+            const int nzb = ch.ns / ch.kbin_upp;
+            for (int iz = 0; iz < nzb; ++iz) {
+                float2 w = zweight_dd(bins, ch.zb0 + iz, zp, ze);
+                if (w.x == 0.f) continue;
+                if (bins.growth) {
+                    const double z1 = (double) zp + (double) ze;
+                    w = ff_mul(w, ff_of(pow(z1 / (bins.z_centers[ch.zb0 + iz] + 1.0), bins.growth_b)));
+                }
+                const float2 *row = a.ttab_ff + ((size_t) ch.tcombo * bins.nz + ch.zb0 + iz) * gr.nv;
+                const float2 r0 = row[nvx], r1 = row[nvx + 1];
+                sv = ff_add(sv, ff_mul(ff_add(r0, ff_mul(ff_sub(r1, r0), fv)), w));
+            }
+        }
+        float2 cv = ff_mul(ff_mul(sq[i], sv), sq[j]);
         if (i == j) cv = ff_add(cv, one);
         C[idx] = cv;
     }
@@ -283,36 +330,28 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
     const int ti = tile / tpr, tj = tile % tpr;
     const DeviceBins &bins = *a.bins;
     const float2 *lw2 = a.logw2 + ch.pix, *sw2 = a.sqw2 + ch.pix;
-    const double *y = fws_d(a, ch.o_y);
     const int nzb = ch.ns / ch.kbin_upp;
     constexpr int E = 2 * QM_PAIRS;
     int nidx[E];
-    float dnf[E], yyf[E];
+    float dnf[E];
     float zp[E], ze[E];      // 1 + z_ij as double-float; zp = 0 marks padding
     size_t off[QM_PAIRS];    // element offset of each pair's first element
-    // y of this thread's two columns (the same for its four rows)
-    const int jc = tj * T64 + 2 * (threadIdx.x % 32);
-    const float yc0 = jc < n ? (float) y[jc] : 0.f, yc1 = jc + 1 < n ? (float) y[jc + 1] : 0.f;
 #pragma unroll
     for (int u = 0; u < QM_PAIRS; ++u) {
         const int p = threadIdx.x + 256 * u;
         const int i = ti * T64 + hrow + p / 32, j0 = tj * T64 + 2 * (p % 32);
         off[u] = (size_t) i * ld + j0;
-        const float yr = i < n ? (float) y[i] : 0.f;
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
             const int k = 2 * u + e, j = j0 + e;
-            nidx[k] = 0; dnf[k] = 0.f; yyf[k] = 0.f; zp[k] = 0.f; ze[k] = 0.f;
+            nidx[k] = 0; dnf[k] = 0.f; zp[k] = 0.f; ze[k] = 0.f;
             if (i < n && j < n) {
                 const int lo = i < j ? i : j, hi = i < j ? j : i;
                 vindex_ff(a.grid, lw2[hi], lw2[lo], nidx[k], dnf[k]);
                 two_prod_ff(sw2[i], sw2[j], zp[k], ze[k]);
-                yyf[k] = yr * (e == 0 ? yc0 : yc1);
             }
         }
     }
-    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
     const size_t plane = (size_t) ld * ld;
     const float *rows = a.deriv_f + (size_t) ch.res * bins.nk * a.grid.nv;
     // slot scales as floats, converted once per block
@@ -341,11 +380,9 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
                 const float qs = qscale[s];
                 uint32_t *qh = reinterpret_cast<uint32_t *>(a.q_hi + (size_t) (ch.slot_q + s) * plane);
                 uint32_t *ql = reinterpret_cast<uint32_t *>(a.q_lo + (size_t) (ch.slot_q + s) * plane);
-                float fpart = 0.f;
 #pragma unroll
                 for (int u = 0; u < QM_PAIRS; ++u) {
                     const float q0 = base[2 * u] * w[g][2 * u], q1 = base[2 * u + 1] * w[g][2 * u + 1];
-                    fpart = fmaf(yyf[2 * u], q0, fmaf(yyf[2 * u + 1], q1, fpart));
                     if (!LQG_IN_BOUNDS(a, (size_t) (ch.slot_q + s) * plane + off[u] + 1 <
                                               (size_t) a.total_slots_q * plane, 5, c, off[u]))
                         continue;
@@ -355,8 +392,111 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
                     qh[off[u] / 2] = *reinterpret_cast<const uint32_t *>(&hv);
                     ql[off[u] / 2] = *reinterpret_cast<const uint32_t *>(&lv);
                 }
-                for (int o = 16; o > 0; o >>= 1) fpart += __shfl_down_sync(0xffffffffu, fpart, o);
-                if (lane == 0) dpart[s] = (double) fpart;
+            }
+        }
+    }
+}
+
+// Mixed path, the d and x partials in double-float arithmetic on the FP32 pipe:
+//   d_s = y^T Q_s y       (computePSbeforeFvector, core/chunk_estimate.cpp:754-759)
+//   x_s = tr(Q_s C^-1) = sum_ij Q_s,ij C^-1_ij   (C^-1 marginalised, when cinv_m)
+// over the upper triangle, off-diagonal elements counted twice.  k_finish
+// forms d - b - t = d - x + (F theta) from them (b_s + t_s = tr(C^-1 Q_s C^-1 (S +
+// N)) with C^-1 C C^-1 = C^-1), a difference much smaller than its terms on
+// high signal-to-noise chunks: a float Q_s (2^-24) or float y y^T - C^-1 already
+// moves it by ~2e-7 of max |b| (CPU emulation on echelle-size chunks), so Q_s
+// (table value, interpolation fraction and redshift weight), y_i y_j, C^-1_ij
+// and the accumulation are all double-float (~48 bits).  No FP64 work in the
+// slot loop (the FP64 pipe is 1/64 of the FP32 one): warp sums in
+// double-float, and each warp's (hi, lo) pair is stored in its 8-byte partial
+// slot.  Blocks and warps map to the d-partial slots of k_build_q_mixed's
+// layout (half tiles of 32 x 64, 8 warps); blocks of lower tiles write zeros.
+constexpr int DX_E = 8;   // elements per thread: rows warp + 8u (u < 4), columns 2 lane, 2 lane + 1
+
+template <bool GR>
+__global__ void __launch_bounds__(256, 2) k_dx_mixed(WaveArgs a) {
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    const int ld = ch.ld, n = ch.n, tpr = ld / T64;
+    const int tile = blockIdx.x >> 1, hrow = (blockIdx.x & 1) * 32;
+    if (tile >= tpr * tpr || a.status[ch.gidx] != LQG_CHUNK_OK || ch.nelem > 0) return;
+    const int ti = tile / tpr, tj = tile % tpr;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const bool want_x = a.dbt_id && ch.cinv_m;
+    double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
+    double *xpart = want_x ? ws_d(a, ch.o_xpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns : nullptr;
+    if (ti > tj) {
+        // counted through the mirrored upper tile
+        for (int s = lane; s < ch.ns; s += 32) {
+            dpart[s] = 0.0;
+            if (want_x) xpart[s] = 0.0;
+        }
+        return;
+    }
+    const DeviceBins &bins = *a.bins;
+    const float2 *lw2 = a.logw2 + ch.pix, *sw2 = a.sqw2 + ch.pix;
+    const double *y = fws_d(a, ch.o_y);
+    const double *cm = want_x ? fws_d(a, ch.o_m) : nullptr;
+    const int nzb = ch.ns / ch.kbin_upp;
+    int nidx[DX_E];
+    float2 dn[DX_E], yy[DX_E], cmv[DX_E];
+    float zp[DX_E], ze[DX_E];   // 1 + z_ij as double-float; zp = 0: no element
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int i = ti * T64 + hrow + warp + 8 * u;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int k = 2 * u + e, j = tj * T64 + 2 * lane + e;
+            nidx[k] = 0;
+            dn[k] = yy[k] = cmv[k] = make_float2(0.f, 0.f);
+            zp[k] = ze[k] = 0.f;
+            // weight of the element in the full sum: 2 above the diagonal, 1 on it
+            const double wt = (i < n && j < n) ? (i < j ? 2.0 : (i == j ? 1.0 : 0.0)) : 0.0;
+            if (wt == 0.0) continue;
+            vindex_dd(a.grid, lw2[j], lw2[i], nidx[k], dn[k]);
+            two_prod_ff(sw2[i], sw2[j], zp[k], ze[k]);
+            yy[k] = ff_of(wt * y[i] * y[j]);
+            if (want_x) cmv[k] = ff_of(wt * cm[(size_t) i * ld + j]);
+        }
+    }
+    const float4 *rows = a.deriv_ff + (size_t) ch.res * bins.nk * a.grid.nv;
+    for (int iz = 0; iz < nzb; ++iz) {
+        float2 w[DX_E];
+#pragma unroll
+        for (int k = 0; k < DX_E; ++k) {
+            w[k] = make_float2(0.f, 0.f);
+            if (zp[k] > 0.f) {
+                w[k] = zweight_dd(bins, ch.zb0 + iz, zp[k], ze[k]);
+                if (GR && w[k].x != 0.f) {
+                    const double z1 = (double) zp[k] + (double) ze[k];
+                    w[k] = ff_mul(w[k], ff_of(pow(z1 / (bins.z_centers[ch.zb0 + iz] + 1.0), bins.growth_b)));
+                }
+            }
+        }
+        for (int kn = 0; kn < ch.kbin_upp; ++kn) {
+            const float4 *row = rows + (size_t) kn * a.grid.nv;
+            float sd = 0.f, cd = 0.f, sx = 0.f, cx = 0.f;
+#pragma unroll
+            for (int k = 0; k < DX_E; ++k) {
+                if (w[k].x == 0.f) continue;
+                // the reference's r0 (1 - dn) + r1 dn, as r0 + (r1 - r0) dn with
+                // the node's difference stored: product (p, e), then two-sum
+                const float4 r = row[nidx[k]];
+                float p, e;
+                two_prod_ff(make_float2(r.z, r.w), dn[k], p, e);
+                const float2 s0 = ff_two_sum(r.x, p);
+                const float2 base = make_float2(s0.x, __fadd_rn(s0.y, __fadd_rn(r.y, e)));
+                float qp, qe;
+                two_prod_ff(base, w[k], qp, qe);
+                dd_mac(sd, cd, qp, qe, yy[k]);
+                if (want_x) dd_mac(sx, cx, qp, qe, cmv[k]);
+            }
+            const int s = iz * ch.kbin_upp + kn;
+            const float2 dsum = warp_sum_ff(make_float2(sd, cd));
+            if (lane == 0) reinterpret_cast<float2 *>(dpart)[s] = dsum;
+            if (want_x) {
+                const float2 xsum = warp_sum_ff(make_float2(sx, cx));
+                if (lane == 0) reinterpret_cast<float2 *>(xpart)[s] = xsum;
             }
         }
     }
@@ -543,9 +683,16 @@ __global__ void k_finish(WaveArgs a, int mixed) {
     // d partials: 8 warps per 64 x 64 tile (FP64 build) or per 32 x 64 half tile (mixed)
     const int ns = ch.ns, parts = (ch.ld / T64) * (ch.ld / T64) * 8 * (mixed ? 2 : 1);
     const double *dpart = ws_d(a, ch.o_dpart);
+    // the mixed path's table chunks leave (hi, lo) float pairs (k_dx_mixed)
+    const bool pairs = mixed && ch.nelem == 0;
+    auto part = [&](const double *base, int p, int s) {
+        if (!pairs) return base[(size_t) p * ns + s];
+        const float2 v = reinterpret_cast<const float2 *>(base)[(size_t) p * ns + s];
+        return (double) v.x + (double) v.y;
+    };
     for (int s = threadIdx.x; s < ns; s += blockDim.x) {
         double acc = 0;
-        for (int p = 0; p < parts; ++p) acc += dpart[(size_t) p * ns + s];
+        for (int p = 0; p < parts; ++p) acc += part(dpart, p, s);
         d[(s / ch.kbin_upp) * bins.nk + s % ch.kbin_upp] = acc;
     }
     const size_t blkstride = (size_t) a.gram_splits * GR * GR;
@@ -577,6 +724,31 @@ __global__ void k_finish(WaveArgs a, int mixed) {
                 b[ikz] = g;
             }
         }
+        if (!(a.dbt_id && ch.cinv_m)) return;
+        // d - b - t without the 22-bit traces.  With C = S + N + sum_s theta_s Q_s
+        // (the stored slots) and the marginalised C^-1 (C^-1 C C^-1 = C^-1),
+        //   b_s + t_s = tr(C^-1 Q_s C^-1 (S + N)) = tr(Q_s C^-1) - sum_s' F_ss' theta_s',
+        // so e_s = d_s - b_s - t_s = d_s - x_s + (F theta)_s with x_s = tr(Q_s C^-1)
+        // from k_dx_mixed.  The larger of b_s and t_s (b_s alone without S_fid)
+        // takes the difference, so that d - b - t = e exactly and each keeps its
+        // own relative accuracy.
+        __syncthreads();
+        const double *xp = ws_d(a, ch.o_xpart);
+        for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+            double x = 0;
+            for (int p = 0; p < parts; ++p) x += part(xp, p, s);
+            const int ikz = (s / ch.kbin_upp) * bins.nk + s % ch.kbin_upp;
+            double e = d[ikz] - x;
+            if (a.theta)
+                for (int s2 = 0; s2 < ns; ++s2) {
+                    const double th = a.theta[ch.fis + (s2 / ch.kbin_upp) * bins.nk + s2 % ch.kbin_upp];
+                    if (th != 0.0) e += th * gram(min(s, s2), max(s, s2));
+                }
+            const double bt = d[ikz] - e;
+            if (a.turn_off_sfid) b[ikz] = bt;
+            else if (fabs(b[ikz]) >= fabs(t[ikz])) b[ikz] = bt - t[ikz];
+            else t[ikz] = bt - b[ikz];
+        }
         return;
     }
     const int rows = ns + 2;
@@ -600,6 +772,12 @@ __global__ void k_finish(WaveArgs a, int mixed) {
 
 }  // namespace
 
+void launch_theta_tables(const double *deriv, const double *theta, const int *combos, int n_combos, int nk, int nz,
+                         int nv, double *ttab, float2 *ttab_ff, cudaStream_t st) {
+    k_theta_tables<<<dim3((nv + 255) / 256, nz, n_combos), 256, 0, st>>>(deriv, theta, combos, nk, nz, nv, ttab,
+                                                                        ttab_ff);
+}
+
 void launch_build_s_c(WaveArgs &a, cudaStream_t st) {
     int tiles = (a.max_ld / T64) * (a.max_ld / T64);
     if (a.c_is_ff)
@@ -613,10 +791,14 @@ void launch_build_q(WaveArgs &a, cudaStream_t st) {
     int tiles = (a.max_ld / T64) * (a.max_ld / T64);
     if (a.precision == LQG_PRECISION_MIXED) {
         k_prep_mixed<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
-        if (a.growth)
+        if (a.growth) {
             k_build_q_mixed<true><<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
-        else
+            k_dx_mixed<true><<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
+        } else {
             k_build_q_mixed<false><<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
+            k_dx_mixed<false><<<dim3(2 * tiles, a.n_chunks), 256, 0, st>>>(a);
+        }
+        a.launches++;
     } else {
         k_build_q<<<dim3(tiles, a.n_chunks), 256, 0, st>>>(a);
         k_wn_fp64<<<dim3(64, a.n_chunks), 256, 0, st>>>(a);

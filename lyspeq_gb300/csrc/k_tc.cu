@@ -52,8 +52,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-// Bounded wait for the phase of the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait for the phase of the given parity to complete.  The pipeline
+// waits take the iteration's limit (lqg_set_wait_limit; 2 s unless set); the
+// waits of a CTA's exit for its own copies and MMAs always take 2 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
     uint64_t t0 = 0;
     while (true) {
         uint32_t ok;
@@ -67,7 +69,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
         if (ok) return true;
         uint64_t t = now_ns();
         if (t0 == 0) t0 = t;
-        else if (t - t0 > kWaitLimitNs) return false;
+        else if (t - t0 > limit_ns) return false;
     }
 }
 
@@ -255,17 +257,17 @@ template <int STAGES, int STAGE_BYTES, int TILE_A, int TILE_B, int BN>
 __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned char *smem, uint64_t *full,
                                          uint64_t *empty, uint64_t *dfull, uint64_t *dempty, uint64_t *done,
                                          int kblocks, int DRAIN, uint32_t idesc, int &kb_all, int &g_all,
-                                         int *abort_flag) {
+                                         int *abort_flag, uint64_t lim) {
     const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
     for (int g = 0; g < ngroups; ++g) {
         const int b = g_all & 1;
-        if (g_all >= 2 && !mbar_wait(&dempty[b], ((g_all >> 1) - 1) & 1)) { *abort_flag = 1; return false; }
+        if (g_all >= 2 && !mbar_wait(&dempty[b], ((g_all >> 1) - 1) & 1, lim)) { *abort_flag = 1; return false; }
         fence_after();
         const uint32_t th = thh + b * BN;
         const int kb_end = min(kblocks, (g + 1) * DRAIN);
         for (int kb = g * DRAIN; kb < kb_end; ++kb) {
             const int st = kb_all % STAGES;
-            if (!mbar_wait(&full[st], (kb_all / STAGES) & 1)) { *abort_flag = 1; return false; }
+            if (!mbar_wait(&full[st], (kb_all / STAGES) & 1, lim)) { *abort_flag = 1; return false; }
             fence_after();
             unsigned char *sb = smem + st * STAGE_BYTES;
             const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + TILE_A);
@@ -296,12 +298,12 @@ __device__ __forceinline__ bool mma_tile(uint32_t thh, uint32_t tx, unsigned cha
 template <bool KAHAN>
 __device__ __forceinline__ bool drain_tile(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
                                            uint64_t *dempty, int kblocks, int DRAIN, float (&sum)[64], int &g_all,
-                                           int *abort_flag) {
+                                           int *abort_flag, uint64_t lim) {
     const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
     bool alive = true;
     for (int g = 0; g < ngroups; ++g) {
         const int b = g_all & 1;
-        alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g_all >> 1) & 1)) && !*abort_flag;
+        alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g_all >> 1) & 1, lim)) && !*abort_flag;
         if (!alive) break;
         fence_after();
         if (!KAHAN) {
@@ -389,7 +391,7 @@ __device__ __forceinline__ int tile_kblocks(const WaveArgs &a, const GemmTile &t
 // 2e-6 on DESI-like chunks, at 28 % more product time)
 template <int STAGE>
 __device__ __forceinline__ int tile_drain(const WaveArgs &a, const GemmTile &tl) {
-    return (STAGE != 0 && tl.s >= a.chunks[tl.c].ns) ? kGemmDrainST : kGemmDrain;
+    return (STAGE != 0 && tl.s >= a.chunks[tl.c].ns) ? kGemmDrainST : (a.gemm_drain > 0 ? a.gemm_drain : kGemmDrain);
 }
 
 template <int STAGE>
@@ -415,6 +417,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     const long long total = (long long) njobs * (STAGE == 2 ? mt * (mt + 1) / 2 : mt * mt);
     const int kblocks = ld / BK;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint64_t lim = a.wait_ns ? a.wait_ns : kWaitLimitNs;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < G_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
@@ -453,7 +456,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             const int kbt = tile_kblocks<STAGE>(a, tl, kblocks);
             for (int kb = 0; kb < kbt; ++kb) {
                 const int st = kb_all % G_STAGES;
-                if (!mbar_wait(&empty[st], ((kb_all / G_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
+                if (!mbar_wait(&empty[st], ((kb_all / G_STAGES) & 1) ^ 1, lim)) { *abort_flag = 1; break; }
                 unsigned char *sb = smem + st * G_STAGE_BYTES;
                 mbar_expect_tx(&full[st], G_STAGE_BYTES);
                 tma_load_3d(sb, &mc_hi, &full[st], kb * BK, tl.m0, aidx);
@@ -471,13 +474,13 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         int kb_all = 0, g_all = 0, lt = 0;
         for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x, ++lt) {
             const int x = lt & 1;
-            if (lt >= 2 && !mbar_wait(&xempty[x], ((lt >> 1) - 1) & 1)) { *abort_flag = 1; break; }
+            if (lt >= 2 && !mbar_wait(&xempty[x], ((lt >> 1) - 1) & 1, lim)) { *abort_flag = 1; break; }
             fence_after();
             const GemmTile tl = gemm_tile<STAGE>(jobs, t, mt);
             const int kbt = tile_kblocks<STAGE>(a, tl, kblocks);
             if (!mma_tile<G_STAGES, G_STAGE_BYTES, G_TILE_A, G_TILE_B, G_BN>(
                     tmem, tmem + 2 * G_BN + x * G_BN, smem, full, empty, dfull, dempty, &xfull[x], kbt,
-                    tile_drain<STAGE>(a, tl), idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag))
+                    tile_drain<STAGE>(a, tl), idesc_f16(G_BM, G_BN), kb_all, g_all, abort_flag, lim))
                 break;
         }
         // every MMA of this CTA completes before its tensor memory is freed
@@ -498,9 +501,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
 #pragma unroll
             for (int j = 0; j < 64; ++j) sum[j] = 0.f;
             bool got = drain_tile<false>(tmem, lane_addr, col0, dfull, dempty, tile_kblocks<STAGE>(a, tl, kblocks),
-                                         tile_drain<STAGE>(a, tl), sum, g_all, abort_flag);
+                                         tile_drain<STAGE>(a, tl), sum, g_all, abort_flag, lim);
             const int x = lt & 1;
-            got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1)) && !*abort_flag;
+            got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1, lim)) && !*abort_flag;
             if (!got) break;
             fence_after();
             if (STAGE == 2) {
@@ -653,6 +656,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     const int64_t k_lo = sp * kper, k_hi = min(K, k_lo + kper);
     const int kblocks = k_hi > k_lo ? (int) ((k_hi - k_lo) / BK) : 0;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint64_t lim = a.wait_ns ? a.wait_ns : kWaitLimitNs;
     // whitened form: both operands are the B_s rows of P (B_0 .. B_{ns+1})
     const int prow = ch.slot_p + bi * R_BM, rrow = (a.sym ? ch.slot_p : ch.slot_r) + bj * R_BN;
 
@@ -677,7 +681,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             *abort_flag = 1;
         for (int kb = 0; kb < kblocks && !*abort_flag; ++kb) {
             const int st = kb % R_STAGES;
-            if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1)) { *abort_flag = 1; break; }
+            if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1, lim)) { *abort_flag = 1; break; }
             unsigned char *sb = smem + st * R_STAGE_BYTES;
             const int x = (int) (k_lo + (int64_t) kb * BK);
             mbar_expect_tx(&full[st], R_STAGE_BYTES);
@@ -693,7 +697,7 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         int kb_all = 0, g_all = 0;
         mma_tile<R_STAGES, R_STAGE_BYTES, R_TILE, R_TILE, R_BN>(tmem, tmem + 2 * R_BN, smem, full, empty, dfull,
                                                                dempty, accum, kblocks, kGramDrain,
-                                                               idesc_f16(R_BM, R_BN), kb_all, g_all, abort_flag);
+                                                               idesc_f16(R_BM, R_BN), kb_all, g_all, abort_flag, lim);
         // every MMA completes before the tensor memory is freed
         umma_commit(mdone);
         mbar_wait(mdone, 0);
@@ -706,8 +710,8 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
         for (int j = 0; j < 64; ++j) sum[j] = 0.f;
         int g_all = 0;
         const bool alive = drain_tile<true>(tmem, lane_addr, half * 64, dfull, dempty, kblocks, kGramDrain, sum,
-                                            g_all, abort_flag);
-        const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0)) && !*abort_flag;
+                                            g_all, abort_flag, lim);
+        const bool got = __all_sync(0xffffffffu, alive && mbar_wait(accum, 0, lim)) && !*abort_flag;
         fence_after();
         if (got) {
             const int row = quad * 32 + lane;
@@ -828,14 +832,28 @@ void launch_scales_mixed(WaveArgs &a, cudaStream_t st) {
 
 void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int njobs, const int *d_jobs2,
                            int njobs2) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_tc_gemm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
-        cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
-        cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
-        cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, R_SMEM);
-        attr = true;
+    // shared memory above the 48 KB default, and the SM count: once per device
+    static std::atomic<unsigned long long> attr{0};
+    static int n_sm_dev[64];
+    const bool ready = once_per_device(attr, [](int dev) {
+        cudaError_t e = cudaFuncSetAttribute(k_tc_gemm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, R_SMEM);
+        int sms = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess && dev >= 0 && dev < 64) n_sm_dev[dev] = sms > 0 ? sms : 1;
+        return e;
+    });
+    if (!ready) {
+        a.host_failed = 1;
+        return;
     }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int n_sm = (dev >= 0 && dev < 64) ? n_sm_dev[dev] : 0;
+    if (n_sm <= 0 && (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n_sm <= 0))
+        n_sm = 1;
     const int ld = a.max_ld;
     const cuuint64_t plane = (cuuint64_t) ld * ld;
     bool ok = true;
@@ -871,13 +889,6 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         a.host_failed = 1;
         return;
     }
-    static int n_sm = 0;
-    if (!n_sm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-        if (n_sm <= 0) n_sm = 1;
-    }
     // persistent: one CTA per SM (one fits: 197 KB of shared memory)
     const long long mt = (ld + G_BM - 1) / G_BM;
     const long long tiles = mt * mt * njobs;
@@ -896,6 +907,9 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     a.launches += 2;
 }
 
-int gram_splits_mixed(int64_t K) { return (int) ((K + kGramK - 1) / kGramK); }
+int gram_splits_mixed(int64_t K, int gram_k) {
+    const int64_t k = gram_k > 0 ? gram_k : kGramK;
+    return (int) ((K + k - 1) / k);
+}
 
 }  // namespace lqg

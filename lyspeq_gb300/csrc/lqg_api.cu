@@ -2,6 +2,7 @@
 #include "lqg_internal.cuh"
 
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -24,8 +25,15 @@ struct lqg_ctx {
     std::vector<int> r_fwhm;
     std::vector<double> tdv, qmax, smax;
     TableGrid grid{};
-    DevBuf d_deriv, d_deriv_f, d_signal, d_signal_ff, d_bins;
+    DevBuf d_deriv, d_deriv_f, d_deriv_ff, d_signal, d_signal_ff, d_bins;
     lqg_opts opts{};
+    uint64_t wait_ns = 0;   // lqg_set_wait_limit; 0: the kernels' 2 s
+    // LQG_PRECISION_MIXED_AUTO: per padded size ld, the mixed form, the drain
+    // interval of the products and the Gram's K split (lqg_autotune)
+    struct Tune {
+        int sym = 1, drain = 8, gram_k = 32768;
+    };
+    std::map<int, Tune> tuning;
     // batch
     struct HostChunk {
         int n, ld, nq, ns, kbin_upp, fis, res, zlow, zupp, input_index;
@@ -47,7 +55,7 @@ struct lqg_ctx {
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
-    DevBuf d_fws, d_ws, d_fbounds, d_desc, d_jobs, d_scales, d_halves, d_gram, d_check;
+    DevBuf d_fws, d_ws, d_fbounds, d_desc, d_jobs, d_scales, d_halves, d_gram, d_check, d_ttab, d_ttab_ff;
     void *h_stage = nullptr;   // pinned staging of the per-iteration descriptors
     size_t h_stage_bytes = 0;
     std::vector<int> last_status;
@@ -56,16 +64,30 @@ struct lqg_ctx {
     int waves = 0;
     bool have_results = false;   // an iteration has run on the current batch
     std::vector<cudaEvent_t> evpool;
-    // CUDA graph of one iteration's launches: captured on the second iteration
-    // with the same key (batch, precision, theta use, device buffers) and
-    // replayed while the key holds
+    // CUDA graphs of iterations' launches: an iteration whose key (batch,
+    // precision, theta use, device buffers, launch plan) was seen by one of the
+    // last kKeyHistory iterations is captured, and replayed while the key holds.
+    // A few graphs are kept, so that an NR loop alternating between keys (the
+    // first iteration at theta = 0, the later ones with theta) replays each.
+    struct GraphEntry {
+        std::vector<uintptr_t> key;
+        cudaGraphExec_t exec = nullptr;
+        int launches = 0, waves = 0;
+        std::vector<std::pair<size_t, int>> spans;
+        size_t eacc = 0;
+    };
+    static constexpr size_t kMaxGraphs = 4, kKeyHistory = 8;
     uint64_t batch_version = 0;
-    std::vector<uintptr_t> graph_key, last_key;
-    cudaGraphExec_t graph = nullptr;
+    std::vector<std::vector<uintptr_t>> key_history;
+    std::vector<GraphEntry> graphs;
     bool graph_failed = false;
-    int graph_launches = 0, graph_waves = 0;
-    std::vector<std::pair<size_t, int>> graph_spans;
-    size_t graph_eacc = 0;
+    // an iteration enqueued by lqg_nr_iteration_async and not yet finished
+    // (its statuses, index-check counters and timings are read by finish_pending)
+    bool pending = false;
+    cudaEvent_t ev_after = nullptr;   // orders the iteration after the caller's stream
+    int pending_nb = 0;
+    std::vector<std::pair<size_t, int>> pending_spans;
+    size_t pending_eacc = 0;
 };
 
 namespace {
@@ -175,6 +197,17 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
         std::vector<float> df(tables->deriv, tables->deriv + nd);
         if (ctx->d_deriv_f.alloc(nd * 4) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "tables");
         cudaMemcpy(ctx->d_deriv_f.p, df.data(), nd * 4, cudaMemcpyHostToDevice);
+        // double-float (value, difference to the next node) per node, for the
+        // mixed path's interpolation r0 + (r1 - r0) dn in double-float
+        std::vector<float4> dff(nd);
+        for (size_t e = 0; e < nd; ++e) {
+            const size_t v = e % (size_t) tables->nv;
+            const double r = tables->deriv[e], dr = v + 1 < (size_t) tables->nv ? tables->deriv[e + 1] - r : 0.0;
+            const float2 a = split_ff(r), b = split_ff(dr);
+            dff[e] = make_float4(a.x, a.y, b.x, b.y);
+        }
+        if (ctx->d_deriv_ff.alloc(nd * 16) != cudaSuccess) return set_err(c, LQG_ERR_NOMEM, "tables");
+        cudaMemcpy(ctx->d_deriv_ff.p, dff.data(), nd * 16, cudaMemcpyHostToDevice);
     }
     ctx->qmax.assign((size_t) tables->n_tables * bins->nk, 0.0);
     for (int t = 0; t < tables->n_tables; ++t)
@@ -218,6 +251,8 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
         const float2 d = split_ff(ctx->dz), dh = split_ff(ctx->dz / 2);
         db.dz_hi = d.x; db.dz_lo = d.y; db.dzh_hi = dh.x; db.dzh_lo = dh.y;
         db.inv_dz = (float) (1.0 / ctx->dz);
+        const float2 idz = split_ff(1.0 / ctx->dz);
+        db.idz_hi = idz.x; db.idz_lo = idz.y;
     }
     db.growth = opts->redshift_growth_on > 0;
     db.growth_b = opts->fid_redshift_power;
@@ -237,8 +272,9 @@ extern "C" int lqg_ctx_destroy(lqg_ctx *ctx) {
     if (!ctx) return LQG_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.exec);
     for (auto &e : ctx->evpool) cudaEventDestroy(e);
+    if (ctx->ev_after) cudaEventDestroy(ctx->ev_after);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -515,8 +551,21 @@ int upload_pixels(lqg_ctx *ctx) {
     return LQG_OK;
 }
 
-int gram_splits_for(int ld, int precision, bool sym) {
-    if (precision == LQG_PRECISION_MIXED) return gram_splits_mixed(sym ? sym_plane(ld) : (int64_t) ld * ld);
+// The plan's choices for chunks of padded size ld under a requested precision
+// mode: the kernels' defaults for the fixed modes, the context's table for
+// LQG_PRECISION_MIXED_AUTO (defaults where it has no entry).
+lqg_ctx::Tune form_for(const lqg_ctx *ctx, int mode, int ld) {
+    lqg_ctx::Tune t;
+    if (mode == LQG_PRECISION_FP64 || mode == LQG_PRECISION_MIXED_DIRECT) t.sym = 0;
+    if (mode == LQG_PRECISION_MIXED_AUTO) {
+        auto it = ctx->tuning.find(ld);
+        if (it != ctx->tuning.end()) t = it->second;
+    }
+    return t;
+}
+
+int gram_splits_for(int ld, int precision, bool sym, int gram_k) {
+    if (precision == LQG_PRECISION_MIXED) return gram_splits_mixed(sym ? sym_plane(ld) : (int64_t) ld * ld, gram_k);
     int64_t K = (int64_t) ld * ld;
     int64_t s = (K + 32767) / 32768;
     return (int) std::max<int64_t>(1, std::min<int64_t>(s, 256));
@@ -524,15 +573,23 @@ int gram_splits_for(int ld, int precision, bool sym) {
 
 int gram_blocks(int ns) { return (ns + 2 + 127) / 128; }
 
-// Factor workspace of one chunk: S_fid, C~ (becomes C^-1), y and 64 ld of scratch.
-int64_t chunk_fws_bytes(int64_t ld) {
-    return align_up(ld * ld * 8, 256) * 2 + align_up(ld * 8, 256) + align_up(64 * ld * 8, 256);
+// Factor workspace of one chunk: S_fid, C~ (becomes C^-1), y and 64 ld of scratch;
+// the whitened mixed form adds the marginalised C^-1 next to W.
+int64_t chunk_fws_bytes(int64_t ld, bool cinv_m) {
+    return align_up(ld * ld * 8, 256) * (cinv_m ? 3 : 2) + align_up(ld * 8, 256) + align_up(64 * ld * 8, 256);
+}
+
+// Mixed path: d - b - t from the x partials (k_finish).  It rests on C = S + N +
+// sum theta Q with the N of b, which smoothed noise weights break (C takes the
+// smoothed ivar, N the raw one); the Gram's b and t stand alone then.
+bool dbt_identity(const lqg_ctx *ctx, int precision) {
+    return precision == LQG_PRECISION_MIXED && ctx->opts.smooth_noise_weights < 0;
 }
 
 // Wave workspace of one chunk in a wave with the given Gram blocking.
 int64_t chunk_ws_bytes(int64_t ld, int ns, int precision, bool sym, int splits, int gt) {
     const int64_t m = ld * ld * 8, tiles = (ld / 64) * (ld / 64);
-    int64_t b = align_up(tiles * 16 * ns * 8, 256);
+    int64_t b = align_up(tiles * 16 * ns * 8, 256) * (precision == LQG_PRECISION_MIXED ? 2 : 1);
     const int64_t gblk = (int64_t) gt * gt * splits * 128 * 128;
     if (precision == LQG_PRECISION_FP64)
         b += align_up(gblk * 8, 256) + align_up(m * ns, 256) * 2 + align_up(m * (ns + 2), 256);
@@ -549,6 +606,7 @@ int64_t chunk_ws_bytes(int64_t ld, int ns, int precision, bool sym, int splits, 
 struct WavePlan {
     std::vector<int> members;   // batch chunk indices
     int ld = 0, gt = 1, splits = 1;
+    int sym = 0, drain = 8;     // mixed form and products drain interval (one per ld)
     int slot_q = 0, slot_r = 0, slot_p = 0;
     int64_t ws_bytes = 0, half_bytes = 0;
     size_t desc_off = 0, jobs_off = 0, scales_off = 0, jobs2_off = 0;
@@ -577,9 +635,9 @@ cudaEvent_t pool_event(lqg_ctx *ctx, size_t i) {
 // split into waves of equal padded size (phase B: Q_s, products, traces).
 // Descriptors, jobs and host-known scales of every launch are packed into
 // single arrays, uploaded once.
-int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan> &groups, std::vector<ChunkDesc> &desc,
+int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan> &groups, std::vector<ChunkDesc> &desc,
                    std::vector<int> &jobs, std::vector<double> &scales, int64_t &max_fws, int64_t &max_ws,
-                   int64_t &max_half, int64_t &max_gram) {
+                   int64_t &max_half, int64_t &max_gram, int &n_combos) {
     const int nb = (int) ctx->chunks.size();
     size_t budget = ctx->opts.workspace_bytes;
     if (budget == 0) {
@@ -597,9 +655,13 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
         return gram_blocks(a.ns) > gram_blocks(b.ns);
     });
     const int64_t fws_limit = (int64_t) (0.35 * (double) budget);
+    const bool ident = dbt_identity(ctx, precision);
+    auto own_m = [&](const lqg_ctx::HostChunk &h) {
+        return ident && form_for(ctx, mode, h.ld).sym && h.nelem == 0;
+    };
     int64_t fsum = 0;
     for (int idx : order) {
-        const int64_t need = chunk_fws_bytes(ctx->chunks[idx].ld);
+        const int64_t need = chunk_fws_bytes(ctx->chunks[idx].ld, own_m(ctx->chunks[idx]));
         // gridDim.y carries the chunk index of a launch: at most 65535 per launch
         if (groups.empty() || fsum + need > fws_limit || groups.back().members.size() >= 65535) {
             groups.emplace_back();
@@ -610,6 +672,15 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
         groups.back().fws_bytes = fsum;
     }
     max_fws = max_ws = max_half = max_gram = 0;
+    // (table, KBIN_UPP) pairs of the batch: one theta-weighted table row block
+    // each, as (res, kbin_upp) ints at the front of jobs
+    std::vector<std::pair<int, int>> combos;
+    for (const auto &h : ctx->chunks)
+        if (h.res >= 0 && h.nelem == 0) combos.push_back({h.res, h.kbin_upp});
+    std::sort(combos.begin(), combos.end());
+    combos.erase(std::unique(combos.begin(), combos.end()), combos.end());
+    n_combos = (int) combos.size();
+    for (const auto &cb : combos) { jobs.push_back(cb.first); jobs.push_back(cb.second); }
     for (auto &g : groups) {
         max_fws = std::max(max_fws, g.fws_bytes);
         g.desc_off = desc.size();
@@ -617,15 +688,25 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
         for (int idx : g.members) {
             const auto &h = ctx->chunks[idx];
             ChunkDesc d{};
+            d.tcombo = -1;
+            if (h.res >= 0 && h.nelem == 0)
+                d.tcombo = (int) (std::lower_bound(combos.begin(), combos.end(), std::make_pair(h.res, h.kbin_upp)) -
+                                  combos.begin());
             d.n = h.n; d.ld = h.ld; d.nq = h.nq; d.ns = h.ns; d.kbin_upp = h.kbin_upp; d.fis = h.fis;
             d.res = h.res; d.zb0 = h.fis / ctx->nk; d.pix = h.pix; d.res_off = h.res_off; d.gidx = idx;
             d.nelem = h.nelem; d.os = h.os; d.sh = h.sh; d.nf = h.nf; d.fpix = h.fpix; d.rw_off = h.rw_off;
             d.rw_sum = h.rw_sum;
+            d.sym = precision == LQG_PRECISION_MIXED ? form_for(ctx, mode, h.ld).sym : 0;
             const int64_t m = (int64_t) h.ld * h.ld * 8;
             d.o_s = off; off += align_up(m, 256);
             d.o_c = off; off += align_up(m, 256);
             d.o_y = off; off += align_up((int64_t) h.ld * 8, 256);
             d.o_fscr = off; off += align_up(64 * (int64_t) h.ld * 8, 256);
+            // the marginalised C^-1: its own buffer next to W (whitened form), or
+            // C^-1 itself (direct form); not formed for resolution-matrix chunks
+            d.cinv_m = ident && h.nelem == 0 ? 1 : 0;
+            d.o_m = d.o_c;
+            if (own_m(h)) { d.o_m = off; off += align_up(m, 256); }
             g.max_ld = std::max(g.max_ld, h.ld);
             desc.push_back(d);
         }
@@ -636,7 +717,9 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
         for (size_t k = 0; k < g.members.size(); ++k) {
             const int idx = g.members[k];
             const auto &h = ctx->chunks[idx];
-            const int gt = gram_blocks(h.ns), splits = gram_splits_for(h.ld, precision, sym);
+            const lqg_ctx::Tune tn = form_for(ctx, mode, h.ld);
+            const bool sym = precision == LQG_PRECISION_MIXED && tn.sym;
+            const int gt = gram_blocks(h.ns), splits = gram_splits_for(h.ld, precision, sym, tn.gram_k);
             int64_t need = chunk_ws_bytes(h.ld, h.ns, precision, sym, splits, gt);
             if (precision == LQG_PRECISION_MIXED && h.nelem > 0)
                 need += align_up((int64_t) h.kbin_upp * h.nf * 8, 256);   // grid-point phases
@@ -650,6 +733,8 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
                 g.waves.back().ld = h.ld;
                 g.waves.back().gt = gt;
                 g.waves.back().splits = splits;
+                g.waves.back().sym = sym ? 1 : 0;
+                g.waves.back().drain = tn.drain;
             }
             WavePlan &w = g.waves.back();
             w.members.push_back((int) k);   // index within the group
@@ -658,6 +743,7 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
         }
         for (auto &w : g.waves) {
             const int ld = w.ld;
+            const bool sym = w.sym != 0;
             w.slot_q = 0;
             const int64_t m = (int64_t) ld * ld * 8, tiles = (ld / 64) * (ld / 64);
             const int64_t gblk = (int64_t) w.gt * w.gt * w.splits * 128 * 128;
@@ -666,6 +752,9 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
             for (int k : w.members) {
                 ChunkDesc d = desc[g.desc_off + k];
                 d.o_dpart = off; off += align_up(tiles * 16 * d.ns * 8, 256);
+                if (precision == LQG_PRECISION_MIXED) {
+                    d.o_xpart = off; off += align_up(tiles * 16 * d.ns * 8, 256);
+                }
                 if (precision == LQG_PRECISION_MIXED && d.nelem > 0) {
                     d.o_ph = off; off += align_up((int64_t) d.kbin_upp * d.nf * 8, 256);
                 }
@@ -736,21 +825,65 @@ int plan_iteration(lqg_ctx *ctx, int precision, bool sym, std::vector<GroupPlan>
 
 }  // namespace
 
-extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision) {
-    if (!ctx) return LQG_ERR_ARG;
+namespace {
+
+// Waits for the last enqueued iteration and reads what it left on the host
+// side: per-chunk statuses, the index-check counters and the phase timings.
+int finish_pending(lqg_ctx *ctx) {
+    if (!ctx->pending) return LQG_OK;
+    ctx->pending = false;
+    LQG_CUDA_CHECK_RET(cudaStreamSynchronize(ctx->stream));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, std::string("iteration kernels: ") + cudaGetErrorString(e));
+    const char *hs = static_cast<const char *>(ctx->h_stage);
+    const unsigned long long *chk = reinterpret_cast<const unsigned long long *>(hs);
+    const int *st = reinterpret_cast<const int *>(hs + 4 * sizeof(unsigned long long));
+    ctx->last_status.assign(st, st + ctx->pending_nb);
+    if (chk[0] != 0)
+        return set_err(ctx, LQG_ERR_STATE, "index check failed " + std::to_string(chk[0]) + " times: code " +
+                                               std::to_string(chk[1]) + " chunk " + std::to_string(chk[2]) +
+                                               " index " + std::to_string(chk[3]));
+    // [0] S/C build, [1] factorisation, [2] Q build, [3] products, [4] Gram, [5] finish,
+    // [6] accumulation, [7] whole iteration
+    for (auto &sp : ctx->pending_spans) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, ctx->evpool[sp.first], ctx->evpool[sp.first + 1]) == cudaSuccess)
+            ctx->timings[sp.second] += ms;
+    }
+    float ta = 0, tt = 0;
+    if (cudaEventElapsedTime(&ta, ctx->evpool[ctx->pending_eacc], ctx->evpool[1]) != cudaSuccess) ta = 0;
+    if (cudaEventElapsedTime(&tt, ctx->evpool[0], ctx->evpool[1]) != cudaSuccess) tt = 0;
+    cudaGetLastError();   // a timing query that failed leaves no error behind
+    ctx->timings[6] = ta;
+    ctx->timings[7] = tt;
+    ctx->have_results = true;
+    return LQG_OK;
+}
+
+// Plans and enqueues one iteration on the context's stream, ordered after
+// `after` (a caller's stream) when given; finish_pending completes it.
+int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStream_t after) {
     if (precision != LQG_PRECISION_FP64 && precision != LQG_PRECISION_MIXED &&
-        precision != LQG_PRECISION_MIXED_DIRECT)
+        precision != LQG_PRECISION_MIXED_DIRECT && precision != LQG_PRECISION_MIXED_AUTO)
         return set_err(ctx, LQG_ERR_ARG, "unknown precision");
-    // both mixed forms share the kernels up to the products; sym selects the
-    // whitened symmetric one
-    const bool sym = precision == LQG_PRECISION_MIXED;
-    if (precision == LQG_PRECISION_MIXED_DIRECT) precision = LQG_PRECISION_MIXED;
+    // the mixed forms share the kernels up to the products; the plan picks the
+    // form per padded size (whitened or direct) from the requested mode
+    const int mode = precision;
+    if (precision != LQG_PRECISION_FP64) precision = LQG_PRECISION_MIXED;
     if (precision == LQG_PRECISION_MIXED && !tc_available())
         return set_err(ctx, LQG_ERR_UNSUPPORTED, "mixed precision needs the sm_103a tensor-core kernels");
     cudaSetDevice(ctx->device);
-    int rc = upload_pixels(ctx);
+    int rc = finish_pending(ctx);
     if (rc) return rc;
+    if ((rc = upload_pixels(ctx))) return rc;
     cudaStream_t st = ctx->stream;
+    if (after && after != st) {
+        // inputs the caller produced on its stream come first
+        if (!ctx->ev_after && cudaEventCreateWithFlags(&ctx->ev_after, cudaEventDisableTiming) != cudaSuccess)
+            return set_err(ctx, LQG_ERR_CUDA, "event");
+        LQG_CUDA_CHECK_RET(cudaEventRecord(ctx->ev_after, after));
+        LQG_CUDA_CHECK_RET(cudaStreamWaitEvent(st, ctx->ev_after, 0));
+    }
     bool use_theta = false;
     if (theta) {
         for (int i = 0; i < ctx->nkz; ++i) use_theta |= theta[i] != 0.0;
@@ -776,8 +909,14 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     std::vector<int> jobs;
     std::vector<double> scales;
     int64_t max_fws = 0, max_ws = 0, max_half = 0, max_gram = 0;
-    if ((rc = plan_iteration(ctx, precision, sym, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram)))
+    int n_combos = 0;
+    if ((rc = plan_iteration(ctx, precision, mode, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram,
+                             n_combos)))
         return rc;
+    const size_t ttab_bytes = (size_t) n_combos * ctx->nz * ctx->grid.nv * 8;
+    if (use_theta && n_combos > 0 &&
+        (ctx->d_ttab.alloc(ttab_bytes) || (precision == LQG_PRECISION_MIXED && ctx->d_ttab_ff.alloc(ttab_bytes))))
+        return set_err(ctx, LQG_ERR_NOMEM, "theta tables");
     ctx->d_fws.trim(std::max<int64_t>(max_fws, 256));
     ctx->d_ws.trim(std::max<int64_t>(max_ws, 256));
     ctx->d_halves.trim(precision == LQG_PRECISION_MIXED ? max_half + 1024 : 0);
@@ -794,7 +933,8 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
         ctx->d_check.alloc(4 * sizeof(unsigned long long)))
         return set_err(ctx, LQG_ERR_NOMEM, "descriptors");
     // pinned staging, so that the uploads below are asynchronous
-    const size_t stage = desc.size() * sizeof(ChunkDesc) + jobs.size() * 4 + scales.size() * 8;
+    const size_t stage = std::max(desc.size() * sizeof(ChunkDesc) + jobs.size() * 4 + scales.size() * 8,
+                                  4 * sizeof(unsigned long long) + (size_t) nb * 4);
     if (ctx->h_stage_bytes < stage) {
         if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
         ctx->h_stage = nullptr;
@@ -825,15 +965,18 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.logw2 = ctx->d_logw2.as<float2>(); base.sqw2 = ctx->d_sqw2.as<float2>();
     base.sqiv = ctx->d_sqiv.as<double>(); base.niv = ctx->d_niv.as<double>();
     base.sqiv2 = ctx->d_sqiv2.as<float2>();
-    // mixed path without theta: S and C~ built in double-float, handed over as pairs
-    base.c_is_ff = (precision == LQG_PRECISION_MIXED && !use_theta && ctx->d_signal_ff.p) ? 1 : 0;
+    // mixed path: S and C~ built in double-float, handed over as pairs (with
+    // theta too, unless resolution-matrix chunks need their FP64 theta sandwiches)
+    base.c_is_ff = (precision == LQG_PRECISION_MIXED && ctx->d_signal_ff.p && (!use_theta || !ctx->has_reso)) ? 1 : 0;
     base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
     base.n_fpix = (int64_t) ctx->h_flogw.size();
     base.reso_nelem = base.reso_os = 0;
     base.growth = ctx->opts.redshift_growth_on > 0;
-    base.sym = sym;
+    base.sym = 0;   // per wave (and per chunk in the factorisation)
+    base.dbt_id = dbt_identity(ctx, precision) ? 1 : 0;
     // W = T is lower triangular unless the continuum projector makes it full
-    base.w_tri = sym && ctx->opts.cont_logl_order < 0 && ctx->opts.cont_l_order < 0;
+    const bool no_marg = ctx->opts.cont_logl_order < 0 && ctx->opts.cont_l_order < 0;
+    base.w_tri = 0;
     {
         int ne = -1, os = -1;
         bool uniform = true;
@@ -847,9 +990,12 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.n_rw = (int64_t) ctx->h_rw.size();
     base.deriv = ctx->d_deriv.as<double>();
     base.deriv_f = ctx->d_deriv_f.as<float>();
+    base.deriv_ff = ctx->d_deriv_ff.as<float4>();
     base.signal = ctx->d_signal.p ? ctx->d_signal.as<double>() : nullptr;
     base.signal_ff = ctx->d_signal_ff.p ? ctx->d_signal_ff.as<float2>() : nullptr;
     base.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
+    base.ttab = use_theta && n_combos > 0 ? ctx->d_ttab.as<double>() : nullptr;
+    base.ttab_ff = base.ttab && base.c_is_ff ? ctx->d_ttab_ff.as<float2>() : nullptr;
     base.results = ctx->d_results.as<double>();
     base.status = ctx->d_status.as<int>();
     base.grid = ctx->grid;
@@ -862,6 +1008,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     base.results_elems = ctx->results_size;
     base.n_pix = (int64_t) ctx->h_wave.size();
     base.check = ctx->d_check.as<unsigned long long>();
+    base.wait_ns = ctx->wait_ns;
 
     // LQG_SYNC_EACH=1: synchronise after every kernel and name the one that failed
     static const bool sync_each = getenv("LQG_SYNC_EACH") && getenv("LQG_SYNC_EACH")[0] == '1';
@@ -882,6 +1029,11 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
         int rc = LQG_OK;
         size_t nev = 2;
         record_event(ev_start, st);
+        if (base.ttab) {
+            launch_theta_tables(base.deriv, base.theta, ctx->d_jobs.as<int>(), n_combos, ctx->nk, ctx->nz,
+                                ctx->grid.nv, ctx->d_ttab.as<double>(), const_cast<float2 *>(base.ttab_ff), st);
+            ctx->launches++;
+        }
         for (auto &g : groups) {
             WaveArgs a = base;
             a.chunks = ctx->d_desc.as<ChunkDesc>() + g.desc_off;
@@ -896,6 +1048,8 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
             if ((rc = step("build_s_c", g.max_ld, a.n_chunks))) return rc;
             record_event(pool_event(ctx, e0 + 1), st);
             launch_factor_all(a, st);
+            if (a.host_failed)
+                return set_err(ctx, LQG_ERR_CUDA, "factorisation: kernel attribute setup failed");
             if ((rc = step("factor", g.max_ld, a.n_chunks))) return rc;
             record_event(pool_event(ctx, e0 + 2), st);
             spans.push_back({e0, 0});
@@ -912,6 +1066,9 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
                 b.ws_bytes = w.ws_bytes;
                 b.total_slots_q = w.slot_q; b.total_slots_r = w.slot_r; b.total_slots_p = w.slot_p;
                 b.gram_splits = w.splits;
+                b.sym = w.sym;
+                b.w_tri = w.sym && no_marg;
+                b.gemm_drain = w.drain;
                 b.scales = ctx->d_scales.as<double>() + w.scales_off;
                 if (precision == LQG_PRECISION_MIXED) {
                     __half *hb = ctx->d_halves.as<__half>();
@@ -922,7 +1079,7 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
                     b.q_lo = hb; hb += pl * w.slot_q;
                     b.r_hi = hb; hb += pl * w.slot_r;
                     b.r_lo = hb; hb += pl * w.slot_r;
-                    b.p_plane = sym ? sym_plane(w.ld) : pl;
+                    b.p_plane = w.sym ? sym_plane(w.ld) : pl;
                     b.p_hi = hb; hb += b.p_plane * w.slot_p;
                     b.p_lo = hb; hb += b.p_plane * w.slot_p;
                     b.gram_part = ctx->d_gram.as<float>();
@@ -943,7 +1100,9 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
                 else
                     launch_products_fp64(b, st, d_jobs, w.njobs);
                 if (b.host_failed)
-                    return set_err(ctx, LQG_ERR_CUDA, "products: TMA descriptor encoding (cuTensorMapEncodeTiled) failed");
+                    return set_err(ctx, LQG_ERR_CUDA,
+                                   "products: kernel attribute setup or TMA descriptor encoding "
+                                   "(cuTensorMapEncodeTiled) failed");
                 if ((rc = step("products", w.ld, nch))) return rc;
                 record_event(pool_event(ctx, w0 + 3), st);
                 launch_finish(b, st);
@@ -967,45 +1126,72 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
     };
     // the key of everything a captured iteration would bake in
     std::vector<uintptr_t> key = {
-        (uintptr_t) ctx->batch_version, (uintptr_t) precision, (uintptr_t) sym, (uintptr_t) use_theta,
+        (uintptr_t) ctx->batch_version, (uintptr_t) precision, (uintptr_t) mode, (uintptr_t) use_theta,
         (uintptr_t) base.c_is_ff, (uintptr_t) ctx->d_fws.p, (uintptr_t) ctx->d_ws.p, (uintptr_t) ctx->d_halves.p,
         (uintptr_t) ctx->d_gram.p, (uintptr_t) ctx->d_desc.p, (uintptr_t) ctx->d_jobs.p, (uintptr_t) ctx->d_scales.p,
         (uintptr_t) ctx->d_fbounds.p, (uintptr_t) ctx->d_check.p, (uintptr_t) ctx->d_results.p,
         (uintptr_t) ctx->d_status.p, (uintptr_t) ctx->d_meta.p, (uintptr_t) ctx->d_wave.p, (uintptr_t) ctx->d_flogw.p,
-        (uintptr_t) ctx->d_rw.p, (uintptr_t) ctx->d_sqiv2.p, (uintptr_t) ctx->d_niv.p};
-    if (ctx->graph && key == ctx->graph_key) {
-        LQG_CUDA_CHECK_RET(cudaGraphLaunch(ctx->graph, st));
-        ctx->launches = ctx->graph_launches;
-        ctx->waves = ctx->graph_waves;
-        spans = ctx->graph_spans;
-        eacc = ctx->graph_eacc;
+        (uintptr_t) ctx->d_rw.p, (uintptr_t) ctx->d_sqiv2.p, (uintptr_t) ctx->d_niv.p, (uintptr_t) ctx->d_ttab.p,
+        (uintptr_t) ctx->d_ttab_ff.p, (uintptr_t) ctx->wait_ns, (uintptr_t) n_combos};
+    // the launch plan: grid sizes and the by-value kernel arguments follow from these
+    for (const auto &g : groups) {
+        key.insert(key.end(), {(uintptr_t) g.members.size(), (uintptr_t) g.max_ld, (uintptr_t) g.fws_bytes,
+                               (uintptr_t) g.desc_off, (uintptr_t) g.waves.size()});
+        for (const auto &w : g.waves)
+            key.insert(key.end(), {(uintptr_t) w.members.size(), (uintptr_t) w.ld, (uintptr_t) w.gt,
+                                   (uintptr_t) w.splits, (uintptr_t) w.slot_q, (uintptr_t) w.slot_r,
+                                   (uintptr_t) w.slot_p, (uintptr_t) w.ws_bytes, (uintptr_t) w.desc_off,
+                                   (uintptr_t) w.jobs_off, (uintptr_t) w.scales_off, (uintptr_t) w.jobs2_off,
+                                   (uintptr_t) w.njobs, (uintptr_t) w.njobs2, (uintptr_t) w.sym,
+                                   (uintptr_t) w.drain});
+    }
+    auto cached = std::find_if(ctx->graphs.begin(), ctx->graphs.end(),
+                               [&](const lqg_ctx::GraphEntry &g) { return g.key == key; });
+    if (cached != ctx->graphs.end()) {
+        LQG_CUDA_CHECK_RET(cudaGraphLaunch(cached->exec, st));
+        ctx->launches = cached->launches;
+        ctx->waves = cached->waves;
+        spans = cached->spans;
+        eacc = cached->eacc;
     } else {
-        if (ctx->graph) {
-            cudaGraphExecDestroy(ctx->graph);
-            ctx->graph = nullptr;
-        }
-        const bool capture = !sync_each && !ctx->graph_failed && key == ctx->last_key;
+        const bool seen = std::find(ctx->key_history.begin(), ctx->key_history.end(), key) != ctx->key_history.end();
+        const bool capture = !sync_each && !ctx->graph_failed && seen;
         bool captured = false;
         if (capture && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
             rc = launch_all();
             cudaGraph_t g = nullptr;
             const cudaError_t ec = cudaStreamEndCapture(st, &g);
             cudaGraphExec_t ge = nullptr;
-            if (rc == LQG_OK && ec == cudaSuccess && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+            if (rc != LQG_OK) {
+                // a launcher refused on the host (no kernel ran): report it and
+                // keep capturing later iterations; the graph itself did not fail
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                return rc;
+            }
+            if (ec == cudaSuccess && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
                 captured = true;
-                ctx->graph = ge;
-                ctx->graph_key = key;
-                ctx->graph_launches = ctx->launches;
-                ctx->graph_waves = ctx->waves;
-                ctx->graph_spans = spans;
-                ctx->graph_eacc = eacc;
+                if (ctx->graphs.size() >= lqg_ctx::kMaxGraphs) {
+                    // the oldest entry goes; nothing of it can be in flight (the
+                    // previous iteration synchronised)
+                    cudaGraphExecDestroy(ctx->graphs.front().exec);
+                    ctx->graphs.erase(ctx->graphs.begin());
+                }
+                lqg_ctx::GraphEntry ent;
+                ent.key = key;
+                ent.exec = ge;
+                ent.launches = ctx->launches;
+                ent.waves = ctx->waves;
+                ent.spans = spans;
+                ent.eacc = eacc;
+                ctx->graphs.push_back(std::move(ent));
             } else {
                 ctx->graph_failed = true;
             }
             if (g) cudaGraphDestroy(g);
             cudaGetLastError();
             if (captured) {
-                LQG_CUDA_CHECK_RET(cudaGraphLaunch(ctx->graph, st));
+                LQG_CUDA_CHECK_RET(cudaGraphLaunch(ge, st));
             }
         }
         if (!captured) {
@@ -1015,36 +1201,45 @@ extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision
             if ((rc = launch_all())) return rc;
         }
     }
-    ctx->last_key = key;
-    unsigned long long *chk = reinterpret_cast<unsigned long long *>(hs);
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(chk, ctx->d_check.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->last_status.data(), ctx->d_status.p, nb * 4, cudaMemcpyDeviceToHost, st));
-    LQG_CUDA_CHECK_RET(cudaStreamSynchronize(st));
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return set_err(ctx, LQG_ERR_CUDA, std::string("iteration kernels: ") + cudaGetErrorString(e));
-    if (chk[0] != 0)
-        return set_err(ctx, LQG_ERR_STATE, "index check failed " + std::to_string(chk[0]) + " times: code " +
-                                               std::to_string(chk[1]) + " chunk " + std::to_string(chk[2]) +
-                                               " index " + std::to_string(chk[3]));
-    // [0] S/C build, [1] factorisation, [2] Q build, [3] products, [4] Gram, [5] finish,
-    // [6] accumulation, [7] whole iteration
-    for (auto &sp : spans) {
-        float ms = 0;
-        if (cudaEventElapsedTime(&ms, ctx->evpool[sp.first], ctx->evpool[sp.first + 1]) == cudaSuccess)
-            ctx->timings[sp.second] += ms;
+    if (std::find(ctx->key_history.begin(), ctx->key_history.end(), key) == ctx->key_history.end()) {
+        ctx->key_history.push_back(key);
+        if (ctx->key_history.size() > lqg_ctx::kKeyHistory) ctx->key_history.erase(ctx->key_history.begin());
     }
-    float ta = 0, tt = 0;
-    if (cudaEventElapsedTime(&ta, ctx->evpool[eacc], ev_end) != cudaSuccess) ta = 0;
-    if (cudaEventElapsedTime(&tt, ev_start, ev_end) != cudaSuccess) tt = 0;
-    cudaGetLastError();   // a timing query that failed leaves no error behind
-    ctx->timings[6] = ta;
-    ctx->timings[7] = tt;
-    ctx->have_results = true;
+    // index-check counters and statuses into the pinned staging buffer (the
+    // uploads from it were enqueued before), read by finish_pending
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(hs, ctx->d_check.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    LQG_CUDA_CHECK_RET(cudaMemcpyAsync(hs + 4 * sizeof(unsigned long long), ctx->d_status.p, nb * 4,
+                                       cudaMemcpyDeviceToHost, st));
+    if (after && after != st) {
+        // the caller's later work waits for the iteration's results
+        cudaEvent_t ev = pool_event(ctx, eacc + 1);
+        LQG_CUDA_CHECK_RET(cudaEventRecord(ev, st));
+        LQG_CUDA_CHECK_RET(cudaStreamWaitEvent(after, ev, 0));
+    }
+    ctx->pending = true;
+    ctx->pending_nb = nb;
+    ctx->pending_spans = spans;
+    ctx->pending_eacc = eacc;
     return LQG_OK;
+}
+
+}  // namespace
+
+extern "C" int lqg_nr_iteration(lqg_ctx *ctx, const double *theta, int precision) {
+    if (!ctx) return LQG_ERR_ARG;
+    const int rc = enqueue_iteration(ctx, theta, precision, nullptr);
+    if (rc) return rc;
+    return finish_pending(ctx);
+}
+
+extern "C" int lqg_nr_iteration_async(lqg_ctx *ctx, const double *theta, int precision, void *stream) {
+    if (!ctx) return LQG_ERR_ARG;
+    return enqueue_iteration(ctx, theta, precision, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int lqg_download(lqg_ctx *ctx, double *d, double *b, double *t, double *fisher, int *chunk_status) {
     if (!ctx) return LQG_ERR_ARG;
+    if (int rc = finish_pending(ctx)) return rc;
     cudaStream_t s = ctx->stream;
     const int nkz = ctx->nkz;
     if (d) LQG_CUDA_CHECK_RET(cudaMemcpyAsync(d, ctx->d_dbt.as<double>(), nkz * 8, cudaMemcpyDeviceToHost, s));
@@ -1059,6 +1254,7 @@ extern "C" int lqg_download(lqg_ctx *ctx, double *d, double *b, double *t, doubl
 
 extern "C" int lqg_chunk_result(lqg_ctx *ctx, int i, double *d, double *b, double *t, double *fisher) {
     if (!ctx || i < 0 || i >= (int) ctx->chunks.size()) return LQG_ERR_ARG;
+    if (int rc = finish_pending(ctx)) return rc;
     const auto &h = ctx->chunks[i];
     std::vector<double> buf(3 * h.nq + (size_t) h.nq * h.nq);
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(buf.data(), ctx->d_results.as<double>() + h.res_off, buf.size() * 8,
@@ -1096,6 +1292,9 @@ int draw_coefficients(unsigned long long seed, int n_qso, int nboots, bool per_r
 extern "C" int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots, unsigned long long seed,
                              const double *solver_invfisher, double *mean, double *cov, double *fisher_cov,
                              double *realizations) {
+    if (ctx) {
+        if (int rc = finish_pending(ctx)) return rc;
+    }
     if (!ctx || n_qso < 0 || !qso_offsets || nboots < 2)
         return set_err(ctx, LQG_ERR_ARG, "lqg_bootstrap: bad arguments");
     if (!ctx->have_results) return set_err(ctx, LQG_ERR_STATE, "lqg_bootstrap: no iteration on this batch yet");
@@ -1108,6 +1307,9 @@ extern "C" int lqg_bootstrap(lqg_ctx *ctx, int n_qso, const int *qso_offsets, in
 extern "C" int lqg_bootstrap_complete(lqg_ctx *ctx, int n_qso, const int *qso_offsets, int nboots,
                                       unsigned long long seed, double *mean, double *cov, double *realizations,
                                       int *n_valid) {
+    if (ctx) {
+        if (int rc = finish_pending(ctx)) return rc;
+    }
     if (!ctx || n_qso < 0 || !qso_offsets || nboots < 2)
         return set_err(ctx, LQG_ERR_ARG, "lqg_bootstrap_complete: bad arguments");
     if (!ctx->have_results)
@@ -1131,6 +1333,181 @@ extern "C" int lqg_bootstrap_coefficients(int n_qso, int nboots, unsigned long l
 }
 
 extern "C" int lqg_last_wave_count(const lqg_ctx *ctx) { return ctx ? ctx->waves : 0; }
+
+extern "C" int lqg_set_wait_limit(lqg_ctx *ctx, double seconds) {
+    if (!ctx || !(seconds >= 0.0) || seconds > 60.0) return LQG_ERR_ARG;
+    ctx->wait_ns = (uint64_t) (seconds * 1e9);
+    return LQG_OK;
+}
+
+extern "C" int lqg_sync(lqg_ctx *ctx) {
+    if (!ctx) return LQG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return finish_pending(ctx);
+}
+
+namespace {
+
+// One iteration over a subset of the batch (the tuner's samples): the chunk
+// list is swapped for the subset and restored; per-chunk results land at the
+// chunks' own result offsets, the global sums are not meaningful.
+int iterate_subset(lqg_ctx *ctx, const std::vector<int> &subset, int mode, double *ms) {
+    std::vector<lqg_ctx::HostChunk> full;
+    full.swap(ctx->chunks);
+    for (int i : subset) ctx->chunks.push_back(full[i]);
+    const uint64_t ver = ctx->batch_version;
+    ctx->batch_version = ((uint64_t) 1 << 62) ^ (uint64_t) subset.front() ^ ((uint64_t) subset.size() << 32);
+    int rc = enqueue_iteration(ctx, nullptr, mode, nullptr);
+    if (rc == LQG_OK) rc = finish_pending(ctx);
+    if (ms) *ms = ctx->timings[7];
+    for (int s : ctx->last_status)
+        if (rc == LQG_OK && s != LQG_CHUNK_OK) rc = set_err(ctx, LQG_ERR_STATE, "autotune: a sample chunk failed");
+    ctx->chunks.swap(full);
+    ctx->batch_version = ver;
+    ctx->have_results = false;
+    ctx->last_status.assign(ctx->chunks.size(), LQG_CHUNK_OK);
+    return rc;
+}
+
+// Per-chunk results (3 nq + nq^2 doubles each) of the chunks at their offsets.
+int read_results(lqg_ctx *ctx, const std::vector<int> &subset, std::vector<std::vector<double>> &out) {
+    out.clear();
+    for (int i : subset) {
+        const auto &h = ctx->chunks[i];
+        std::vector<double> buf(3 * h.nq + (size_t) h.nq * h.nq);
+        LQG_CUDA_CHECK_RET(cudaMemcpy(buf.data(), ctx->d_results.as<double>() + h.res_off, buf.size() * 8,
+                                      cudaMemcpyDeviceToHost));
+        out.push_back(std::move(buf));
+    }
+    return LQG_OK;
+}
+
+// Largest error of mixed against FP64 over the chunks: d, b, t normwise, F
+// per element normalised by sqrt(F_ii F_jj).
+double max_error(const lqg_ctx *ctx, const std::vector<int> &subset, const std::vector<std::vector<double>> &mix,
+                 const std::vector<std::vector<double>> &ref) {
+    double worst = 0;
+    for (size_t c = 0; c < subset.size(); ++c) {
+        const int nq = ctx->chunks[subset[c]].nq;
+        const double *x = mix[c].data(), *r = ref[c].data();
+        for (int v = 0; v < 3; ++v) {
+            double scale = 0, err = 0;
+            for (int i = 0; i < nq; ++i) {
+                scale = std::max(scale, std::fabs(r[v * nq + i]));
+                err = std::max(err, std::fabs(x[v * nq + i] - r[v * nq + i]));
+            }
+            if (scale > 0) worst = std::max(worst, err / scale);
+        }
+        const double *f = x + 3 * nq, *fr = r + 3 * nq;
+        for (int i = 0; i < nq; ++i)
+            for (int j = i; j < nq; ++j) {
+                double den = std::sqrt(std::fabs(fr[i * nq + i] * fr[j * nq + j]));
+                if (den == 0) den = 1;
+                worst = std::max(worst, std::fabs(f[i * nq + j] - fr[i * nq + j]) / den);
+            }
+    }
+    return worst;
+}
+
+}  // namespace
+
+extern "C" int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, int flags) {
+    if (!ctx) return LQG_ERR_ARG;
+    if (!tc_available()) return set_err(ctx, LQG_ERR_UNSUPPORTED, "autotune: mixed path unavailable");
+    cudaSetDevice(ctx->device);
+    if (int rc = finish_pending(ctx)) return rc;
+    if (max_rel_err <= 0) max_rel_err = 1e-5;
+    if (max_chunks <= 0) max_chunks = 48;
+    if (flags == 0) flags = 7;
+    std::map<int, std::vector<int>> buckets;   // padded size -> batch indices (table chunks only)
+    for (int i = 0; i < (int) ctx->chunks.size(); ++i)
+        if (ctx->chunks[i].nelem == 0) buckets[ctx->chunks[i].ld].push_back(i);
+    if (buckets.empty()) return set_err(ctx, LQG_ERR_STATE, "autotune: no chunk in the batch");
+    const std::map<int, lqg_ctx::Tune> saved = ctx->tuning;
+    for (auto &bk : buckets) {
+        const int ld = bk.first;
+        std::vector<int> timing(bk.second.begin(), bk.second.begin() + std::min<size_t>(bk.second.size(), max_chunks));
+        std::vector<int> acc(timing.begin(), timing.begin() + std::min<size_t>(timing.size(), 4));
+        std::vector<std::vector<double>> ref, mix;
+        int rc = iterate_subset(ctx, acc, LQG_PRECISION_FP64, nullptr);
+        if (!rc) rc = read_results(ctx, acc, ref);
+        if (rc) { ctx->tuning = saved; return rc; }
+        lqg_ctx::Tune best;
+        double best_ms = -1, best_err = 1e300;
+        lqg_ctx::Tune best_any;   // the most accurate, if no candidate meets the bound
+        for (int sym = 1; sym >= ((flags & 1) ? 0 : 1); --sym)
+            for (int drain : {8, 4, 16}) {
+                if (!(flags & 2) && drain != 8) continue;
+                lqg_ctx::Tune t;
+                t.sym = sym;
+                t.drain = drain;
+                ctx->tuning[ld] = t;
+                rc = iterate_subset(ctx, acc, LQG_PRECISION_MIXED_AUTO, nullptr);
+                if (!rc) rc = read_results(ctx, acc, mix);
+                if (rc) { ctx->tuning = saved; return rc; }
+                const double err = max_error(ctx, acc, mix, ref);
+                if (err < best_err) { best_err = err; best_any = t; }
+                // half the bound on the sample leaves room for the chunks not sampled
+                if (!(err <= 0.5 * max_rel_err)) continue;
+                double ms = 0;
+                // twice: the second replays the captured graph
+                rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
+                if (!rc) rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
+                if (rc) { ctx->tuning = saved; return rc; }
+                if (best_ms < 0 || ms < best_ms) { best_ms = ms; best = t; }
+            }
+        if (best_ms < 0) best = best_any;
+        if (flags & 4) {
+            double bms = -1;
+            int bk_k = best.gram_k;
+            for (int gk : {32768, 16384, 65536}) {
+                lqg_ctx::Tune t = best;
+                t.gram_k = gk;
+                ctx->tuning[ld] = t;
+                double ms = 0;
+                rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
+                if (!rc) rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
+                if (rc) { ctx->tuning = saved; return rc; }
+                if (bms < 0 || ms < bms) { bms = ms; bk_k = gk; }
+            }
+            best.gram_k = bk_k;
+        }
+        ctx->tuning[ld] = best;
+    }
+    return LQG_OK;
+}
+
+extern "C" int lqg_tuning_get(const lqg_ctx *ctx, int *entries, int n) {
+    if (!ctx) return LQG_ERR_ARG;
+    int k = 0;
+    for (const auto &e : ctx->tuning) {
+        if (entries && k < n) {
+            entries[4 * k] = e.first;
+            entries[4 * k + 1] = e.second.sym;
+            entries[4 * k + 2] = e.second.drain;
+            entries[4 * k + 3] = e.second.gram_k;
+        }
+        ++k;
+    }
+    return k;
+}
+
+extern "C" int lqg_tuning_set(lqg_ctx *ctx, const int *entries, int n) {
+    if (!ctx || n < 0 || (n > 0 && !entries)) return LQG_ERR_ARG;
+    std::map<int, lqg_ctx::Tune> t;
+    for (int k = 0; k < n; ++k) {
+        const int ld = entries[4 * k], sym = entries[4 * k + 1], drain = entries[4 * k + 2], gk = entries[4 * k + 3];
+        if (ld <= 0 || ld % kPad || (sym != 0 && sym != 1) || drain < 1 || drain > 64 || gk < 4096 || gk % 64)
+            return set_err(ctx, LQG_ERR_ARG, "lqg_tuning_set: bad entry " + std::to_string(k));
+        lqg_ctx::Tune e;
+        e.sym = sym;
+        e.drain = drain;
+        e.gram_k = gk;
+        t[ld] = e;
+    }
+    ctx->tuning = t;
+    return LQG_OK;
+}
 
 extern "C" int lqg_fisher_solve_n(int n, const double *fisher_sum, const double *dbt, double *fisher,
                                   double *solver, double *inverse, double *weighted, double *theta,

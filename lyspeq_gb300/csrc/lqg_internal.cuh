@@ -1,6 +1,7 @@
 // Internal declarations shared by the engine's translation units.
 #pragma once
 
+#include <atomic>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cstdint>
@@ -38,9 +39,14 @@ struct ChunkDesc {
     // Factor workspace (bytes, relative to WaveArgs::fws): S_fid, C~ -> C^-1, y and
     // the factorisation scratch (64 ld doubles), kept for the whole iteration.
     int64_t o_s, o_c, o_y, o_fscr;
+    // Mixed path: the marginalised C^-1 in FP64 at o_m when cinv_m is set (its
+    // own buffer in the whitened form, o_c in the direct form), read by
+    // k_dx_mixed for the partials of x_s = tr(Q_s C^-1).
+    int64_t o_m;
+    int cinv_m;
     // Wave workspace (bytes, relative to WaveArgs::ws): FP64 product stacks, per-tile
-    // d partials and FP64 Gram partials.
-    int64_t o_q, o_r, o_p, o_part, o_dpart;
+    // d partials (and x partials, mixed path) and FP64 Gram partials.
+    int64_t o_q, o_r, o_p, o_part, o_dpart, o_xpart;
     int slot_q, slot_r, slot_p;  // first matrix slot of this chunk in the stacked operand buffers
     int gidx;             // index of the chunk in the batch (factor bounds, status)
     int status;
@@ -51,6 +57,8 @@ struct ChunkDesc {
     int nelem, os, sh, nf;
     int64_t fpix, rw_off;
     int64_t o_ph;         // wave workspace: cos, sin of k_c u at each grid point (mixed path)
+    int tcombo;           // row block of this chunk's (table, KBIN_UPP) in WaveArgs::ttab
+    int sym;              // mixed path: whitened symmetric form (else direct)
     double rw_sum;        // largest sum of |weights| of a row (bound of R M R^T)
 };
 
@@ -65,6 +73,7 @@ struct DeviceBins {
     // mixed path: 1 + z_c per bin, dz, dz / 2, and 1 / dz
     float zc1_hi[64], zc1_lo[64];
     float dz_hi, dz_lo, dzh_hi, dzh_lo, inv_dz;
+    float idz_hi, idz_lo;   // 1 / dz as double-float
     // RedshiftGrowthOn: Q_k of bin m scaled by ((1 + z_ij) / (1 + z_m))^B
     int growth;
     double growth_b;
@@ -139,12 +148,19 @@ struct WaveArgs {
     int reso_nelem, reso_os;                         // shape shared by every resolution chunk, else 0
     int growth;                                      // RedshiftGrowthOn (as DeviceBins::growth)
     int sym;                                         // mixed path in the whitened symmetric form
+    int dbt_id;                                      // mixed path: d - b - t from the x partials (see k_finish)
     int w_tri;                                       // W lower triangular (no marginalisation)
+    int gemm_drain;                                  // K blocks per drained hi*hi partial of the products; 0: 8
     int64_t p_plane;                                 // elements of one P slot
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)
+    const float4 *deriv_ff;                          // per node: deriv and (next - this) as double-floats
     const float2 *signal_ff;                         // signal table as double-float (mixed path)
     const double *theta;                             // device, nkz
+    // theta-weighted derivative tables: ttab[(tcombo nz + zm) nv + v] =
+    // sum_{kn < KBIN_UPP} theta[zm nk + kn] deriv[table][kn][v] (nullptr without theta)
+    const double *ttab;
+    const float2 *ttab_ff;                           // the same rows as double-float (mixed path)
     double *results;                                 // per-chunk results
     int *status;                                     // per-chunk status (wave-local)
     TableGrid grid;
@@ -161,6 +177,8 @@ struct WaveArgs {
     cudaEvent_t mid_event;       // recorded between the product and the Gram kernels
     // extents of the buffers above, used by the LQG_CHECKED build to validate indices
     int64_t ws_bytes, fws_bytes, results_elems, gram_elems, n_pix, n_fpix, n_rw;
+    int ext_cy;                  // C and y are caller buffers (o_c, o_y may fall outside fws)
+    uint64_t wait_ns;            // limit of the tensor-core pipeline waits; 0: 2 s
     unsigned long long *check;   // [0] violations, [1] first code, [2] first chunk, [3] first index
 };
 
@@ -185,6 +203,9 @@ __device__ __forceinline__ bool lqg_in_bounds(const WaveArgs &a, bool ok, int co
 
 // Phase A (all chunks of a group): S_fid and C~, then the FP64 factorisation.
 void launch_build_s_c(WaveArgs &a, cudaStream_t st);
+// The theta-weighted tables of an iteration (before the groups' S/C builds).
+void launch_theta_tables(const double *deriv, const double *theta, const int *combos, int n_combos, int nk, int nz,
+                         int nv, double *ttab, float2 *ttab_ff, cudaStream_t st);
 // The same two matrix builds for chunks with a resolution matrix (lqg_reso.cu);
 // each kind of kernel skips the chunks of the other kind.
 void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st);
@@ -213,8 +234,24 @@ inline void record_event(cudaEvent_t e, cudaStream_t st) {
         cudaEventRecord(e, st);
 }
 
+// Per-device one-time setup for a launcher: true once fn() has returned
+// cudaSuccess on the current device.  Kernel attributes (dynamic shared memory
+// above 48 KB) are per device; two host threads that race here both run fn,
+// which only sets attributes, so the race is harmless.  A device index beyond
+// the mask runs fn on every call.
+template <class Fn>
+inline bool once_per_device(std::atomic<unsigned long long> &done, Fn fn) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return true;
+    if (fn(dev) != cudaSuccess) return false;
+    if (bit) done.fetch_or(bit, std::memory_order_release);
+    return true;
+}
+
 bool tc_available();
-int gram_splits_mixed(int64_t K);
+int gram_splits_mixed(int64_t K, int gram_k);
 // Elements of one compact upper-triangle slot of the whitened form: the
 // ceil(ld / 128) (ceil(ld / 128) + 1) / 2 tiles of 128 x 128 on and above the diagonal
 inline int64_t sym_plane(int ld) {

@@ -16,7 +16,6 @@
 #include "lqg_internal.cuh"
 
 #include <algorithm>
-#include <climits>
 #include <mutex>
 
 namespace lqg {
@@ -110,7 +109,8 @@ extern "C" int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave
     a.n_chunks = 1;
     a.max_ld = ld;
     a.fws = reinterpret_cast<char *>(scratch);
-    a.fws_bytes = INT64_MAX;
+    a.fws_bytes = (int64_t) kNoallocBytes;
+    a.ext_cy = 1;   // C^-1 and y live in the caller's buffers, outside the scratch
     a.fbounds = reinterpret_cast<double *>(scratch + kNoallocBoundsOff);
     a.status = status;
     a.wave = wave;
@@ -122,5 +122,6 @@ extern "C" int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave
     a.n_pix = n;
     a.check = nullptr;
     launch_factor_all(a, st);
+    if (a.host_failed) return LQG_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? LQG_OK : LQG_ERR_CUDA;
 }

@@ -15,9 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("LQG_LIB", os.path.join(HERE, "liblqg.so"))
 
 LQG_OK = 0
-PRECISION = {"fp64": 0, "mixed": 1, "mixed_direct": 2}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed_direct": 2, "mixed_auto": 3}
 CHUNK_STATUS = {0: "ok", 1: "short", 2: "no_table", 3: "empty", 4: "out_of_range",
-                5: "not_spd", 6: "bad_input", 7: "too_large"}
+                5: "not_spd", 6: "bad_input", 7: "too_large", 8: "timeout", 9: "index_check"}
 
 EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_error",
            "lqg_batch_add", "lqg_batch_clear", "lqg_batch_size", "lqg_chunk_info",
@@ -25,7 +25,9 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_last_timings", "lqg_last_launch_count", "lqg_last_wave_count", "lqg_batch_add_reso",
            "lqg_resomat_deconvolve", "lqg_resomat_oversample", "lqg_tables_generate",
            "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients",
-           "lqg_resomat_smooth", "lqg_fisher_solve_n"]
+           "lqg_resomat_smooth", "lqg_fisher_solve_n", "lqg_set_wait_limit", "lqg_factor_noalloc",
+           "lqg_probe_fp64_rate", "lqg_nr_iteration_async", "lqg_sync", "lqg_autotune", "lqg_tuning_get",
+           "lqg_tuning_set"]
 
 
 class LqgBins(C.Structure):
@@ -91,6 +93,14 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_last_timings.argtypes = [vp, dp, C.c_int]
     lib.lqg_last_launch_count.argtypes = [vp]
     lib.lqg_last_wave_count.argtypes = [vp]
+    lib.lqg_set_wait_limit.argtypes = [vp, C.c_double]
+    lib.lqg_factor_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, vp]
+    lib.lqg_probe_fp64_rate.argtypes = [C.c_int, dp]
+    lib.lqg_nr_iteration_async.argtypes = [vp, dp, C.c_int, vp]
+    lib.lqg_sync.argtypes = [vp]
+    lib.lqg_autotune.argtypes = [vp, C.c_double, C.c_int, C.c_int]
+    lib.lqg_tuning_get.argtypes = [vp, ip, C.c_int]
+    lib.lqg_tuning_set.argtypes = [vp, ip, C.c_int]
     _lib = lib
     return lib
 
@@ -249,6 +259,33 @@ class Engine:
         rc = self.lib.lqg_nr_iteration(self.h, _dptr(th), PRECISION[precision])
         self._check(rc, "lqg_nr_iteration")
 
+    def iterate_async(self, theta=None, precision="fp64", stream=None):
+        """lqg_nr_iteration_async on a cudaStream_t handle (an int, e.g.
+        torch.cuda.Stream.cuda_stream) or None; complete with sync()."""
+        th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+        rc = self.lib.lqg_nr_iteration_async(self.h, _dptr(th), PRECISION[precision],
+                                             None if stream is None else C.c_void_p(stream))
+        self._check(rc, "lqg_nr_iteration_async")
+
+    def sync(self):
+        self._check(self.lib.lqg_sync(self.h), "lqg_sync")
+
+    def autotune(self, max_rel_err=1e-5, max_chunks=48, flags=0):
+        """lqg_autotune on the current batch; returns the table (see tuning())."""
+        self._check(self.lib.lqg_autotune(self.h, float(max_rel_err), int(max_chunks), int(flags)), "lqg_autotune")
+        return self.tuning()
+
+    def tuning(self):
+        """The autotuner's table: rows (ld, whitened form, drain interval, Gram K per split)."""
+        n = self.lib.lqg_tuning_get(self.h, None, 0)
+        buf = np.zeros(4 * max(n, 1), dtype=np.int32)
+        self.lib.lqg_tuning_get(self.h, _iptr(buf), n)
+        return buf[:4 * n].reshape(n, 4)
+
+    def set_tuning(self, table):
+        t = np.ascontiguousarray(np.asarray(table, dtype=np.int32).reshape(-1, 4))
+        self._check(self.lib.lqg_tuning_set(self.h, _iptr(t), len(t)), "lqg_tuning_set")
+
     def download(self):
         d, b, t = (np.zeros(self.nkz) for _ in range(3))
         f = np.zeros((self.nkz, self.nkz))
@@ -292,6 +329,20 @@ class Engine:
 
     def wave_count(self):
         return self.lib.lqg_last_wave_count(self.h)
+
+    def set_wait_limit(self, seconds):
+        """Limit of the tensor-core kernels' waits (0: the default 2 s)."""
+        self._check(self.lib.lqg_set_wait_limit(self.h, float(seconds)), "lqg_set_wait_limit")
+
+
+def probe_fp64_rate(device=0):
+    """Measured DFMA throughput of the device, TFLOP/s."""
+    lib = load_library()
+    out = C.c_double(0.0)
+    rc = lib.lqg_probe_fp64_rate(int(device), C.byref(out))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_probe_fp64_rate failed ({rc})")
+    return out.value
 
 
 def fisher_solve(fisher_sum, dbt):
