@@ -291,7 +291,8 @@ def _make_reso_workload(name, rng, seed, nch):
 def make_workload(name: str, seed: int | None = None, n_chunks: int | None = None) -> Workload:
     """Build one of the named synthetic workloads."""
     seeds = {"small": 20240601, "desi": 20240602, "echelle": 20240604, "tiny": 20240605,
-             "desi_reso": 20240606, "tiny_reso": 20240607, "tiny_reso_dia": 20240607}
+             "desi_reso": 20240606, "tiny_reso": 20240607, "tiny_reso_dia": 20240607,
+             "echelle_small": 20240608}
     seed = seeds[name] if seed is None else seed
     rng = np.random.Generator(np.random.PCG64(seed))
     if name in ("desi_reso", "tiny_reso", "tiny_reso_dia"):
@@ -325,11 +326,13 @@ def make_workload(name: str, seed: int | None = None, n_chunks: int | None = Non
         dvs = np.full(nch, dv)
         mfl = 20000.0
         cont = (1, -1)
-    elif name == "echelle":
+    elif name in ("echelle", "echelle_small"):
+        # echelle_small: the echelle-like set's binning, resolution and noise
+        # with N uniform-int in [1000, 1500] (the reference runs it in seconds)
         dklog = math.log10(0.2 / 0.005) / 30.0
         bins = Bins(0.0, 10, 5e-4, 30, dklog, 2.0, 0.2, 6)
-        nch = 512 if n_chunks is None else n_chunks
-        npix = rng.integers(1000, 4001, size=nch)
+        nch = (512 if name == "echelle" else 3) if n_chunks is None else n_chunks
+        npix = rng.integers(1000, 4001, size=nch) if name == "echelle" else rng.integers(1000, 1501, size=nch)
         dvs = np.round(rng.uniform(2.5, 5.0, size=nch), 1)
         span = np.exp(npix * dvs / C_KMS)
         lmin, lmax = LYA_REST * (1 + bins.z_lower) * 1.0005, LYA_REST * (1 + bins.z_upper) * 0.9995

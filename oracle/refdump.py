@@ -17,11 +17,13 @@ import sys
 
 import numpy as np
 
+from oracle.refsrc import reference_root
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 DRIVER = os.path.join(REF_DIR, "chunk_driver")
 LYAPOWER = os.path.join(REF_DIR, "LyaPowerEstimate")
-REFERENCE_PY = "/root/reference/py"      # lyspeq's own helper scripts (smoothing)
+REFERENCE_PY = os.path.join(reference_root(), "py")   # lyspeq's own helper scripts (smoothing)
 
 
 @dataclasses.dataclass

@@ -9,8 +9,11 @@ the reference compiled from its own sources (oracle/refbuild, run through
 oracle/_ref/chunk_driver with one OpenMP thread), so the fixtures travel to
 machines where the reference sources are absent.
 
+Fixture lyspeq_test_it1 holds lyspeq's own end-to-end test input and truth
+(read from the lyspeq tree, see make_lyspeq_test).
+
 Run (needs the oracle built: make -C oracle/refbuild):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -38,6 +41,8 @@ CASES = {
     "tiny_masked": ("tiny", None, (1, -1), 0.04, None),
     "small_cfg": ("small", None, (-1, -1), 0.0, 12),
     "desi_sub": ("desi", 6, (1, -1), 0.0, None),
+    # echelle-size chunks: N 1000-1500, R 30000-50000, 40 k x 6 z bins
+    "echelle_sub": ("echelle_small", 12, (-1, -1), 0.0, None),
     "tiny_reso": ("tiny_reso", None, (-1, -1), 0.0, None),
     "tiny_reso_dia": ("tiny_reso_dia", None, (-1, -1), 0.0, None),
     # lyspeq's FastBootstrap (200 realizations) after the iteration of tiny_marg1
@@ -175,12 +180,52 @@ def make_case(name, spec):
     print(f"{name}: {len(chunks)} chunks -> {os.path.getsize(path) / 1024:.0f} KiB")
 
 
+def make_lyspeq_test():
+    """lyspeq's own end-to-end test, as fixture lyspeq_test_it1: the binary
+    spectrum file of tests/input (bytes), the numbers of tests/input/test.config
+    and slist.txt the path needs, and the truth files of its first iteration
+    (tests/truth/test_it1_fisher_matrix.dat, halved Fisher matrix, and the
+    columns Pfid, ThetaP, Pest, ErrorP, the Fisher-weighted d, b, t and the
+    d, b, t sums of test_it1_quadratic_power_estimate_detailed.dat)."""
+    from oracle.refsrc import reference_root
+    ref = reference_root()
+    cfg = {}
+    for line in open(os.path.join(ref, "tests", "input", "test.config")):
+        parts = line.split()
+        if len(parts) >= 2 and not parts[0].startswith("#"):
+            cfg[parts[0]] = parts[1]
+    fl = [ln.strip() for ln in open(os.path.join(ref, "tests", "input", "flist.txt")) if ln.strip()]
+    sl = [ln.split() for ln in open(os.path.join(ref, "tests", "input", "slist.txt")) if ln.strip()]
+    dat = np.frombuffer(open(os.path.join(ref, "tests", "input", fl[1]), "rb").read(), dtype=np.uint8)
+    f = lambda k: float(cfg[k])
+    bins = np.array([f("K0"), f("NumberOfLinearBins"), f("LinearKBinWidth"), f("NumberOfLog10Bins"),
+                     f("Log10KBinWidth"), f("FirstRedshiftBinCenter"), f("RedshiftBinWidth"),
+                     f("NumberOfRedshiftBins")])
+    grid = np.array([f("NumberVPoints"), f("VelocityLength"), f("NumberZPoints"), f("MaximumForestLength"),
+                     f("ContinuumLogLambdaMargOrder"), f("ContinuumLambdaMargOrder")])
+    fid = np.array([f("FiducialAmplitude"), f("FiducialSlope"), f("FiducialCurvature"), f("FiducialRedshiftPower"),
+                    f("FiducialRedshiftCurvature"), f("FiducialLorentzianLambda")])
+    tables = np.array([[float(a), float(b)] for a, b in sl[1:]])
+    truth = os.path.join(ref, "tests", "truth")
+    with open(os.path.join(truth, "test_it1_quadratic_power_estimate_detailed.dat")) as fh:
+        rows = [ln for ln in fh if not ln.startswith("#")]
+    detailed = np.loadtxt(rows, skiprows=1)
+    fisher = np.loadtxt(os.path.join(truth, "test_it1_fisher_matrix.dat"), skiprows=1)
+    path = os.path.join(HERE, "lyspeq_test_it1.npz")
+    np.savez_compressed(path, dat=dat, bins=bins, grid=grid, fid=fid, tables=tables,
+                        detailed=detailed[:, 4:], fisher_halved=fisher)
+    print(f"lyspeq_test_it1: {dat.size} bytes of spectrum -> {os.path.getsize(path) / 1024:.0f} KiB")
+
+
 def main():
     if not refdump.available():
         raise SystemExit("oracle not built: make -C oracle/refbuild")
-    names = sys.argv[1:] or list(CASES)
+    names = sys.argv[1:] or list(CASES) + ["lyspeq_test_it1"]
     for name in names:
-        make_case(name, CASES[name])
+        if name == "lyspeq_test_it1":
+            make_lyspeq_test()
+        else:
+            make_case(name, CASES[name])
 
 
 if __name__ == "__main__":

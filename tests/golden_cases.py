@@ -117,3 +117,40 @@ def fisher_err(f, ref):
     den = np.outer(d, d)
     den[den == 0] = 1.0
     return float(np.max(np.abs(np.asarray(f) - ref) / den))
+
+
+def elem_err(x, ref, floor=1e-3):
+    """Largest per-element relative error |x_k - ref_k| / |ref_k| over the
+    elements with |ref_k| above floor * max |ref| (the others are zero or at a
+    zero crossing, where a relative error says nothing)."""
+    x, ref = np.asarray(x), np.asarray(ref)
+    m = np.abs(ref) > floor * np.max(np.abs(ref))
+    if not m.any():
+        return 0.0
+    return float(np.max(np.abs(x - ref)[m] / np.abs(ref)[m]))
+
+
+def p1d_err(bins, g_ref, g_mix, fsum, nsig=5.0):
+    """Per-bin relative error of P1D = P_fid(k_c, z_c) + theta against the
+    reference solution, over the bins measured at nsig sigma or more
+    (sigma = sqrt(diag F^-1)); (error, number of such bins).  On the other
+    bins the estimate is noise and its relative error says nothing."""
+    pfid = synth.pd13_power(np.tile(bins.k_centers, bins.nz), np.repeat(bins.z_centers, bins.nk))
+    p_ref, p_mix = pfid + np.asarray(g_ref["theta"]), pfid + np.asarray(g_mix["theta"])
+    sig = np.sqrt(np.abs(np.diag(g_ref["inverse"])))
+    good = (np.diag(fsum) > 0) & (sig > 0) & (np.abs(p_ref) > nsig * sig)
+    if not good.any():
+        return 0.0, 0
+    return float(np.max(np.abs(p_mix - p_ref)[good] / np.abs(p_ref)[good])), int(good.sum())
+
+
+def global_sums(case):
+    """Global Fisher sum (upper, unhalved) and d, b, t of a fixture's chunks,
+    accumulated as Chunk::oneQSOiteration does (core/chunk_estimate.cpp:893-903)."""
+    nkz = case.bins.nkz
+    fsum, dbt = np.zeros((nkz, nkz)), np.zeros((3, nkz))
+    for m, x, f in zip(case.meta, case.dbt, case.fisher):
+        fis, nq = m[1], m[2]
+        fsum[fis:fis + nq, fis:fis + nq] += f
+        dbt[:, fis:fis + nq] += x
+    return fsum, dbt

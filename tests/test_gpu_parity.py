@@ -198,3 +198,39 @@ def test_last_k_edge_band_matches_oracle(engine_lib):
             errs = (G.rel_err(d, d0), G.rel_err(b, b0), G.rel_err(t, t0), G.fisher_err(f, f0))
             assert max(errs) < tol, (precision, i, errs)
     eng.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_async_iteration_on_a_caller_stream_matches_the_synchronous_one(engine_lib, precision):
+    """lqg_nr_iteration_async ordered on a torch stream: work the caller enqueues
+    on that stream afterwards sees the finished sums, and the results (sums,
+    per-chunk results, statuses) equal those of lqg_nr_iteration bit for bit,
+    at theta = 0 and with theta (the later ones replay captured graphs)."""
+    import torch
+    c = G.load("desi_sub")
+    eng, st = make_engine(c)
+    assert (st == 0).all()
+    nkz = c.bins.nkz
+    theta = np.linspace(-0.01, 0.02, nkz)
+    ref = []
+    for th in (None, theta, theta):
+        eng.iterate(theta=th, precision=precision)
+        ref.append((eng.download(), [eng.chunk_result(i) for i in range(eng.size)]))
+    s = torch.cuda.Stream()
+    for k, th in enumerate((None, theta, theta)):
+        marker = torch.zeros(1, device="cuda")
+        with torch.cuda.stream(s):
+            marker.fill_(1.0)
+        eng.iterate_async(theta=th, precision=precision, stream=s.cuda_stream)
+        with torch.cuda.stream(s):
+            marker.add_(1.0)
+        s.synchronize()
+        assert float(marker.item()) == 2.0
+        eng.sync()
+        out = eng.download()
+        for key in ("d", "b", "t", "fisher", "status"):
+            assert np.array_equal(out[key], ref[k][0][key]), key
+        for i in range(eng.size):
+            for x, y in zip(eng.chunk_result(i), ref[k][1][i]):
+                assert np.array_equal(x, y)
+    eng.close()

@@ -18,8 +18,9 @@ import golden_cases as G
 from lyspeq_gb300 import synth
 from oracle import qmle_port as P
 from oracle import refdump
+from oracle.refsrc import reference_root
 
-REFERENCE = "/root/reference"
+REFERENCE = reference_root()
 have_ref = pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference sources absent")
 
 
