@@ -5,11 +5,16 @@
 // same with the engine underneath:
 //
 //   lyspeq                                            here
-//   qio::QSOFile (after reading)                      QSOSpectrum
-//   OneQSOEstimate(const std::string &fname)          OneQSOEstimate(estimator, spectrum)
+//   qio::QSOFile (binary .dat files)                  qio::QSOFile (same reading steps);
+//     (io/qso_file.cpp:37-230, 334-369)                 QSOSpectrum for arrays in memory
+//   OneQSOEstimate(const std::string &fname)          same signature, and addQSO(spectrum)
 //     (core/one_qso_estimate.cpp:52-121)
-//   Chunk(const qio::QSOFile&, int i1, int i2)        Chunk (made by OneQSOEstimate)
+//   Chunk(const qio::QSOFile&, int i1, int i2)        same signature
 //     (core/chunk_estimate.cpp:141-257)
+//   Chunk::oneQSOiteration(ps, dbt_sum, fisher_sum)   same signature: the first call for a theta
+//   OneQSOEstimate::oneQSOiteration(same)               runs one batched iteration of every chunk
+//     (core/chunk_estimate.cpp:837-914,                 on the GPU; each call then adds its own
+//      core/one_qso_estimate.cpp:176-197)               chunk's results to the caller's sums
 //   Chunk::dbt_estimate_before_fisher_vector,         same members, filled after iterate()
 //     Chunk::fisher_matrix                              (fetchResults())
 //   OneDQuadraticPowerEstimate::iterate()             same name; one batched NR iteration per
@@ -23,7 +28,10 @@
 //
 // Errors follow the reference: a spectrum or chunk the reference rejects
 // with an exception is skipped (logged through the optional log callback),
-// and a failure of the engine throws std::runtime_error.
+// and a failure of the engine throws std::runtime_error.  Like the
+// reference's process-wide tables and settings, the constructors with the
+// reference's signatures use the process's current estimator: the last
+// OneDQuadraticPowerEstimate constructed (not thread safe, as the reference).
 //
 // Header-only; link with -llqg (lyspeq_gb300/liblqg.so).
 #ifndef LYSPEQ_API_HPP
@@ -33,6 +41,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <cstdint>
 #include <functional>
 #include <memory>
@@ -49,7 +58,12 @@ constexpr double SPEED_OF_LIGHT = 299792.458;   // core/global_numbers.hpp
 constexpr double LYA_REST = 1215.67;
 constexpr int MIN_PIXELS_IN_FILE = 100;         // core/one_qso_estimate.cpp:14
 
-enum class Precision { FP64 = LQG_PRECISION_FP64, Mixed = LQG_PRECISION_MIXED, MixedDirect = LQG_PRECISION_MIXED_DIRECT };
+enum class Precision {
+    FP64 = LQG_PRECISION_FP64,
+    Mixed = LQG_PRECISION_MIXED,
+    MixedDirect = LQG_PRECISION_MIXED_DIRECT,
+    MixedAuto = LQG_PRECISION_MIXED_AUTO   // the autotuned plan (autotune(), loadTuning())
+};
 
 // bins:: (core/global_numbers.cpp:209-251)
 struct Binning {
@@ -101,6 +115,7 @@ struct Specifics {
     int smooth_noise_weights = -1;      // SmoothNoiseWeights
     bool smooth_resolution_matrix = false;  // SmoothResolutionMatrix > 0 (needs SmoothNoiseWeights >= 0)
     bool redshift_growth_on = false;    // RedshiftGrowthOn > 0 (exponent: fiducial[3])
+    double min_snr_cut = 0;             // MinimumSnrCut
     double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
 };
 
@@ -115,6 +130,165 @@ struct QSOSpectrum {
     int ndiags = 0;
 };
 
+namespace qio {
+
+enum ifileformat { Binary, Picca };
+
+// A spectrum file as lyspeq's qio::QSOFile reads it.  Binary files only
+// (qio::BQFile, io/qso_file.cpp:334-369): an 88-byte header (int size, double
+// z, dec, ra, int R_fwhm, double S/N, pixel width in km/s, lower and upper
+// observed and rest wavelengths; C struct layout) and then size doubles each
+// of lambda (Angstrom), delta and sigma; ivar = 1 / sigma^2, 0 below 1e-15.
+// picca FITS files are not read by this build.
+class QSOFile {
+public:
+    std::string fname;
+    double z_qso = 0, snr = 0, dv_kms = -1, dlambda = -1, ra = 0, dec = 0, R_kms = 0;
+    int R_fwhm = 0;
+    long id = 0;
+
+    QSOFile(const std::string &fname_qso, ifileformat p_or_b = Binary) : fname(fname_qso) {
+        if (p_or_b != Binary) throw std::runtime_error("QSOFile: picca FITS input is not supported");
+    }
+    // A slice [i1, i2) of a read file with its masked ends removed
+    // (QSOFile::QSOFile(qmaster, i1, i2), io/qso_file.cpp:61-89)
+    QSOFile(const QSOFile &q, int i1, int i2)
+        : fname(q.fname), z_qso(q.z_qso), snr(q.snr), ra(q.ra), dec(q.dec), R_kms(q.R_kms), R_fwhm(q.R_fwhm),
+          id(q.id) {
+        if (i1 < 0 || i2 > q.size() || i2 <= i1) throw std::out_of_range("QSOFile: slice out of range");
+        w_.assign(q.wave() + i1, q.wave() + i2);
+        d_.assign(q.delta() + i1, q.delta() + i2);
+        iv_.assign(q.ivar() + i1, q.ivar() + i2);
+        first_ = 0;
+        n_ = i2 - i1;
+        cutMaskedBoundary();
+        recalc();
+    }
+
+    // QSOFile::readParameters + BQFile::readParameters (io/qso_file.cpp:91-105, 334-351)
+    void readParameters() {
+        std::FILE *f = std::fopen(fname.c_str(), "rb");
+        if (!f) throw std::runtime_error("QSOFile: cannot open " + fname);
+        unsigned char h[88];
+        const bool ok = std::fread(h, 1, 88, f) == 88;
+        std::fclose(f);
+        if (!ok) throw std::runtime_error("fread error in header BQFile!");
+        auto i32 = [&](int off) { int v; std::memcpy(&v, h + off, 4); return v; };
+        auto f64 = [&](int off) { double v; std::memcpy(&v, h + off, 8); return v; };
+        n_file_ = i32(0);
+        z_qso = f64(8); dec = f64(16); ra = f64(24);
+        R_fwhm = i32(32);
+        snr = f64(40); dv_kms = f64(48);
+        R_kms = SPEED_OF_LIGHT / R_fwhm / ONE_SIGMA_2_FWHM;
+    }
+
+    // QSOFile::readData + BQFile::readData (io/qso_file.cpp:107-129, 353-369)
+    void readData() {
+        if (n_file_ <= 0) throw std::runtime_error("File is non-positive!");
+        std::FILE *f = std::fopen(fname.c_str(), "rb");
+        if (!f) throw std::runtime_error("QSOFile: cannot open " + fname);
+        w_.resize(n_file_); d_.resize(n_file_); iv_.resize(n_file_);
+        bool ok = std::fseek(f, 88, SEEK_SET) == 0;
+        ok = ok && std::fread(w_.data(), 8, n_file_, f) == (size_t) n_file_;
+        ok = ok && std::fread(d_.data(), 8, n_file_, f) == (size_t) n_file_;
+        ok = ok && std::fread(iv_.data(), 8, n_file_, f) == (size_t) n_file_;
+        std::fclose(f);
+        if (!ok) throw std::runtime_error("fread error in data BQFile!");
+        for (auto &x : iv_) {
+            x = 1.0 / (x * x);
+            if (x < 1e-15) x = 0;
+        }
+        first_ = 0;
+        n_ = n_file_;
+        if (dlambda < 0 || dv_kms < 0) recalc();
+    }
+
+    void closeFile() {}
+
+    int size() const { return n_; }
+    int realSize() const {
+        return (int) std::count_if(iv_.begin() + first_, iv_.begin() + first_ + n_, [](double x) { return x != 0; });
+    }
+    const double *wave() const { return w_.data() + first_; }
+    const double *delta() const { return d_.data() + first_; }
+    const double *ivar() const { return iv_.data() + first_; }
+    double *wave() { return w_.data() + first_; }
+    double *delta() { return d_.data() + first_; }
+    double *ivar() { return iv_.data() + first_; }
+
+    // QSOFile::maskOutliers (io/qso_file.cpp:189-230); returns the number masked
+    int maskOutliers(double factor = 5.0) {
+        std::vector<double> tmp;
+        for (int i = 0; i < n_; ++i)
+            if (ivar()[i] != 0) tmp.push_back(delta()[i]);
+        if (tmp.empty()) return 0;
+        const double med = median(tmp);
+        for (auto &x : tmp) x = std::fabs(x - med);
+        double mad = 1.4826 * (1.0 + 1.0 / std::sqrt((double) tmp.size())) * median(tmp);
+        mad = std::max(1.0, mad);
+        int j = 0;
+        for (int i = 0; i < n_; ++i) {
+            double &iv = ivar()[i], &f = delta()[i];
+            if (iv == 0) continue;
+            const double s = factor * std::max(1.0 / std::sqrt(iv), mad);
+            const double fup = std::exp(1.663e-03 * std::pow(wave()[i] / LYA_REST, 4.107));
+            if (f < (-1.0 - s) || f > (fup + s)) {
+                f = 0;
+                iv = 0;
+                ++j;
+            }
+        }
+        return j;
+    }
+
+    // QSOFile::cutBoundary (io/qso_file.cpp:159-187)
+    void cutBoundary(double z_lower_edge, double z_upper_edge) {
+        const double l1 = LYA_REST * (1 + z_lower_edge), l2 = LYA_REST * (1 + z_upper_edge);
+        const int wi1 = (int) (std::lower_bound(wave(), wave() + n_, l1) - wave());
+        const int wi2 = (int) (std::upper_bound(wave(), wave() + n_, l2) - wave());
+        if (wi1 == n_ || wi2 == 0) throw std::runtime_error("Empty spectrum when redshift boundary is applied!");
+        first_ += wi1;
+        n_ = wi2 - wi1;
+        cutMaskedBoundary();
+    }
+
+    static double median(std::vector<double> v) {
+        std::sort(v.begin(), v.end());
+        const size_t n = v.size();
+        return n % 2 == 0 ? (v[n / 2 - 1] + v[n / 2]) / 2 : v[n / 2];
+    }
+
+    static constexpr double ONE_SIGMA_2_FWHM = 2.35482004503;
+
+private:
+    std::vector<double> w_, d_, iv_;
+    int first_ = 0, n_ = 0, n_file_ = 0;
+
+    // QSOFile::_cutMaskedBoundary (io/qso_file.cpp:139-157)
+    void cutMaskedBoundary() {
+        int a = 0, b = n_;
+        while (a < n_ && ivar()[a] == 0) ++a;
+        while (b > 0 && ivar()[b - 1] == 0) --b;
+        if (b - a <= 0) throw std::runtime_error("Empty spectrum when masked pixels at boundary are removed!");
+        first_ += a;
+        n_ = b - a;
+    }
+
+    // QSOFile::recalcDvDLam (io/qso_file.cpp:325-329): median pixel widths
+    void recalc() {
+        if (n_ < 2) return;
+        std::vector<double> dl(n_ - 1), dv(n_ - 1);
+        for (int i = 0; i + 1 < n_; ++i) {
+            dl[i] = wave()[i + 1] - wave()[i];
+            dv[i] = SPEED_OF_LIGHT * std::log(wave()[i + 1] / wave()[i]);
+        }
+        dlambda = median(dl);
+        dv_kms = median(dv);
+    }
+};
+
+}  // namespace qio
+
 class OneDQuadraticPowerEstimate;
 
 // One chunk of a spectrum in the estimator's batch (Chunk).
@@ -122,22 +296,51 @@ class Chunk {
 public:
     int fisher_index_start = 0, N_Q_MATRICES = 0;
     int ZBIN_LOW = 0, ZBIN_UPP = 0, KBIN_UPP = 0, RES_INDEX = 0;
-    // filled by OneDQuadraticPowerEstimate::fetchResults after an iteration
+    // filled by oneQSOiteration, or by OneDQuadraticPowerEstimate::fetchResults
     std::vector<std::unique_ptr<double[]>> dbt_estimate_before_fisher_vector;
     std::unique_ptr<double[]> fisher_matrix;   // N_Q x N_Q, upper triangle, not halved
     int status = LQG_CHUNK_OK;
+
+    Chunk() = default;
+    // Chunk::Chunk (core/chunk_estimate.cpp:141-257): pixels [i1, i2) of a read
+    // file join the current estimator's batch; a chunk the reference rejects
+    // throws std::runtime_error (short, no table, out of the redshift range)
+    Chunk(const qio::QSOFile &qmaster, int i1, int i2);
+
+    // Chunk::oneQSOiteration (core/chunk_estimate.cpp:837-914): this chunk's
+    // d, b, t and Fisher matrix at theta = ps_estimate (TOTAL_KZ_BINS), added
+    // to dbt_sum_vector (3 x TOTAL_KZ_BINS) at fisher_index_start and to
+    // fisher_sum (TOTAL_KZ_BINS^2, upper triangle, not halved) at diagonal
+    // offset fisher_index_start.  The first call for a theta computes every
+    // chunk of the batch in one GPU iteration; a failed chunk throws.
+    void oneQSOiteration(const double *ps_estimate, std::vector<std::unique_ptr<double[]>> &dbt_sum_vector,
+                         double *fisher_sum);
 
     int size() const { return n_pix; }
 
 private:
     friend class OneDQuadraticPowerEstimate;
     int n_pix = 0, batch_index = -1;
+    OneDQuadraticPowerEstimate *owner = nullptr;
 };
 
 // One spectrum cut into chunks (OneQSOEstimate).
 class OneQSOEstimate {
 public:
+    std::string fname_qso;
     std::vector<std::unique_ptr<Chunk>> chunks;
+
+    OneQSOEstimate() = default;
+    // OneQSOEstimate::OneQSOEstimate (core/one_qso_estimate.cpp:52-121): reads
+    // the binary file, masks outliers, cuts to the redshift range, drops a
+    // short file, decides the chunk boundaries and makes one Chunk per range;
+    // a rejected file or chunk is logged and skipped, as the reference does.
+    explicit OneQSOEstimate(const std::string &f_qso);
+
+    // OneQSOEstimate::oneQSOiteration (core/one_qso_estimate.cpp:176-197):
+    // every chunk's oneQSOiteration; a chunk that fails is dropped.
+    void oneQSOiteration(const double *ps_estimate, std::vector<std::unique_ptr<double[]>> &dbt_sum_vector,
+                         double *fisher_sum);
 
     // OneQSOEstimate::decideIndices, core/one_qso_estimate.cpp:17-50
     static std::vector<int> decideIndices(int size, const double *wave, const Specifics &sp) {
@@ -218,7 +421,24 @@ public:
         fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
         inverse_fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
         solver_invfisher_matrix.reset(new double[(size_t) nkz_ * nkz_]());
+        current_slot() = this;
     }
+    ~OneDQuadraticPowerEstimate() {
+        if (current_slot() == this) current_slot() = nullptr;
+    }
+    OneDQuadraticPowerEstimate(const OneDQuadraticPowerEstimate &) = delete;
+    OneDQuadraticPowerEstimate &operator=(const OneDQuadraticPowerEstimate &) = delete;
+
+    // The process's current estimator (the last one constructed): what the
+    // reference-signature constructors of OneQSOEstimate and Chunk use.
+    static OneDQuadraticPowerEstimate *current() { return current_slot(); }
+
+    // Precision of the batched iterations that Chunk::oneQSOiteration runs.
+    Precision chunk_precision = Precision::FP64;
+
+    const Binning &binning() const { return bins_; }
+    const Specifics &specifics() const { return sp_; }
+    int totalKZBins() const { return nkz_; }
 
     int numberOfChunks() const { return lqg_batch_size(ctx_.get()); }
 
@@ -309,6 +529,7 @@ public:
             ch->ZBIN_LOW = info[5];
             ch->ZBIN_UPP = info[6];
             ch->batch_index = next++;
+            ch->owner = this;
             est->chunks.push_back(std::move(ch));
         }
         local_queue.push_back(std::move(est));
@@ -470,6 +691,30 @@ public:
         }
     }
 
+    // lqg_autotune on the current batch (the per-size plan of Precision::MixedAuto)
+    void autotune(double max_rel_err = 1e-5, int max_chunks = 48, int flags = 0) {
+        check(lqg_autotune(ctx_.get(), max_rel_err, max_chunks, flags), "lqg_autotune");
+    }
+    // The table as text, one line "ld form drain gram_k" per padded size
+    void saveTuning(const std::string &path) const {
+        const int n = lqg_tuning_get(ctx_.get(), nullptr, 0);
+        std::vector<int> e(4 * (size_t) std::max(n, 1));
+        lqg_tuning_get(ctx_.get(), e.data(), n);
+        std::FILE *f = std::fopen(path.c_str(), "w");
+        if (!f) throw std::runtime_error("cannot write " + path);
+        for (int k = 0; k < n; ++k) std::fprintf(f, "%d %d %d %d\n", e[4 * k], e[4 * k + 1], e[4 * k + 2], e[4 * k + 3]);
+        std::fclose(f);
+    }
+    void loadTuning(const std::string &path) {
+        std::FILE *f = std::fopen(path.c_str(), "r");
+        if (!f) throw std::runtime_error("cannot read " + path);
+        std::vector<int> e;
+        int v[4];
+        while (std::fscanf(f, "%d %d %d %d", &v[0], &v[1], &v[2], &v[3]) == 4) e.insert(e.end(), v, v + 4);
+        std::fclose(f);
+        check(lqg_tuning_set(ctx_.get(), e.data(), (int) e.size() / 4), "lqg_tuning_set");
+    }
+
     // Device time of the last iteration's phases (ms), lqg_last_timings.
     std::vector<double> timings() const {
         std::vector<double> t(8);
@@ -478,6 +723,7 @@ public:
     }
 
 private:
+    friend class Chunk;
     struct CtxDel {
         void operator()(lqg_ctx *c) const { lqg_ctx_destroy(c); }
     };
@@ -485,6 +731,43 @@ private:
     Binning bins_;
     Specifics sp_;
     int nkz_ = 0;
+    // the batched iteration behind Chunk::oneQSOiteration: its theta, the
+    // batch size it covered and the chunks' statuses
+    std::vector<double> batch_theta_;
+    int batch_size_done_ = -1;
+    std::vector<int> batch_status_;
+
+    static OneDQuadraticPowerEstimate *&current_slot() {
+        static OneDQuadraticPowerEstimate *slot = nullptr;
+        return slot;
+    }
+
+    // One chunk (pixels already cut to the chunk) into the batch; returns its
+    // LQG_CHUNK_* status and, when accepted, its lqg_chunk_info.
+    int addChunkPixels(const qio::QSOFile &q, int *info, int &index) {
+        const int n = q.size();
+        int64_t offs[2] = {0, n};
+        int r = q.R_fwhm, st = LQG_CHUNK_OK;
+        index = lqg_batch_size(ctx_.get());
+        check(lqg_batch_add(ctx_.get(), 1, offs, q.wave(), q.delta(), q.ivar(), &r, &st), "lqg_batch_add");
+        if (st == LQG_CHUNK_OK) check(lqg_chunk_info(ctx_.get(), index, info), "lqg_chunk_info");
+        return st;
+    }
+
+    // Runs one iteration of the whole batch at theta unless the last one was
+    // at the same theta over the same batch.
+    void runBatch(const double *theta) {
+        const int nb = lqg_batch_size(ctx_.get());
+        bool same = nb == batch_size_done_ && (int) batch_theta_.size() == nkz_;
+        for (int i = 0; same && i < nkz_; ++i) same = batch_theta_[i] == (theta ? theta[i] : 0.0);
+        if (same) return;
+        check(lqg_nr_iteration(ctx_.get(), theta, (int) chunk_precision), "lqg_nr_iteration");
+        batch_status_.assign(std::max(nb, 1), 0);
+        check(lqg_download(ctx_.get(), nullptr, nullptr, nullptr, nullptr, batch_status_.data()), "lqg_download");
+        batch_theta_.assign(nkz_, 0.0);
+        if (theta) std::copy(theta, theta + nkz_, batch_theta_.begin());
+        batch_size_done_ = nb;
+    }
 
     void check(int rc, const char *what) {
         if (rc != LQG_OK) throw std::runtime_error(std::string(what) + ": " + lqg_last_error(ctx_.get()));
@@ -518,6 +801,100 @@ private:
         }
     }
 };
+
+inline Chunk::Chunk(const qio::QSOFile &qmaster, int i1, int i2) {
+    OneDQuadraticPowerEstimate *est = OneDQuadraticPowerEstimate::current();
+    if (!est) throw std::runtime_error("Chunk: no OneDQuadraticPowerEstimate in this process");
+    qio::QSOFile q(qmaster, i1, i2);
+    int info[8], index = -1;
+    const int st = est->addChunkPixels(q, info, index);
+    switch (st) {
+    case LQG_CHUNK_OK: break;
+    case LQG_CHUNK_SHORT: throw std::runtime_error("Chunk::_copyQSOFile: Short chunk");
+    case LQG_CHUNK_NO_TABLE: throw std::out_of_range("SQLookupTable::findSpecResIndex: no table for (R, dv)");
+    case LQG_CHUNK_OUT_OF_RANGE: throw std::runtime_error("Chunk::_findRedshiftBin: out of the redshift range");
+    default: throw std::runtime_error("Chunk: rejected, status " + std::to_string(st));
+    }
+    owner = est;
+    n_pix = info[0];
+    fisher_index_start = info[1];
+    N_Q_MATRICES = info[2];
+    KBIN_UPP = info[3];
+    RES_INDEX = info[4];
+    ZBIN_LOW = info[5];
+    ZBIN_UPP = info[6];
+    batch_index = index;
+}
+
+inline void Chunk::oneQSOiteration(const double *ps_estimate, std::vector<std::unique_ptr<double[]>> &dbt_sum_vector,
+                                   double *fisher_sum) {
+    if (!owner) throw std::runtime_error("Chunk::oneQSOiteration: chunk is not in a batch");
+    owner->runBatch(ps_estimate);
+    status = owner->batch_status_[batch_index];
+    if (status != LQG_CHUNK_OK)
+        throw std::runtime_error("Chunk::oneQSOiteration: chunk failed, status " + std::to_string(status));
+    const int nq = N_Q_MATRICES, nkz = owner->nkz_;
+    dbt_estimate_before_fisher_vector.clear();
+    for (int i = 0; i < 3; ++i) dbt_estimate_before_fisher_vector.emplace_back(new double[nq]());
+    fisher_matrix.reset(new double[(size_t) nq * nq]());
+    owner->check(lqg_chunk_result(owner->ctx_.get(), batch_index, dbt_estimate_before_fisher_vector[0].get(),
+                                  dbt_estimate_before_fisher_vector[1].get(),
+                                  dbt_estimate_before_fisher_vector[2].get(), fisher_matrix.get()),
+                 "lqg_chunk_result");
+    // core/chunk_estimate.cpp:893-903: F at diagonal offset (nkz + 1) fis with
+    // stride nkz, d, b, t at fis
+    const int fis = fisher_index_start;
+    for (int i = 0; i < nq; ++i)
+        for (int j = 0; j < nq; ++j) fisher_sum[(size_t) (fis + i) * nkz + fis + j] += fisher_matrix[(size_t) i * nq + j];
+    for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < nq; ++i) dbt_sum_vector[k][fis + i] += dbt_estimate_before_fisher_vector[k][i];
+}
+
+inline OneQSOEstimate::OneQSOEstimate(const std::string &f_qso) : fname_qso(f_qso) {
+    OneDQuadraticPowerEstimate *est = OneDQuadraticPowerEstimate::current();
+    if (!est) throw std::runtime_error("OneQSOEstimate: no OneDQuadraticPowerEstimate in this process");
+    const Specifics &sp = est->specifics();
+    const Binning &bins = est->binning();
+    try {
+        // OneQSOEstimate::_readQsoFile (core/one_qso_estimate.cpp:52-98); the
+        // input is delta (InputIsDeltaFlux), as in every configuration here
+        qio::QSOFile q(f_qso, qio::Binary);
+        q.readParameters();
+        if (q.snr < sp.min_snr_cut) throw std::runtime_error("OneQSOEstimate::_readQsoFile::Low SNR");
+        q.readData();
+        const int nout = q.maskOutliers();
+        if (nout > 0) est->log("found " + std::to_string(nout) + " outlier pixels in " + f_qso);
+        q.cutBoundary(bins.z_lower(), bins.z_upper());
+        if (q.realSize() < MIN_PIXELS_IN_FILE) throw std::runtime_error("OneQSOEstimate::_readQsoFile::Short file");
+        const std::vector<int> idx = decideIndices(q.size(), q.wave(), sp);
+        const int nchunks = (int) idx.size() - 1;
+        for (int nc = 0; nc < nchunks; ++nc) {
+            try {
+                chunks.push_back(std::make_unique<Chunk>(q, idx[nc], idx[nc + 1]));
+            } catch (std::exception &e) {
+                est->log(std::string(e.what()) + " Skipping chunk " + std::to_string(nc + 1) + "/" +
+                         std::to_string(nchunks) + " of " + f_qso);
+            }
+        }
+    } catch (std::exception &e) {
+        est->log(std::string(e.what()) + " in " + f_qso);
+    }
+}
+
+inline void OneQSOEstimate::oneQSOiteration(const double *ps_estimate,
+                                            std::vector<std::unique_ptr<double[]>> &dbt_sum_vector,
+                                            double *fisher_sum) {
+    OneDQuadraticPowerEstimate *est = OneDQuadraticPowerEstimate::current();
+    for (auto &ch : chunks) {
+        try {
+            ch->oneQSOiteration(ps_estimate, dbt_sum_vector, fisher_sum);
+        } catch (std::exception &e) {
+            if (est) est->log(std::string(e.what()) + " Skipping " + fname_qso);
+            ch.reset();
+        }
+    }
+    chunks.erase(std::remove_if(chunks.begin(), chunks.end(), [](const auto &x) { return !x; }), chunks.end());
+}
 
 }  // namespace lyspeq_gb300
 

@@ -147,3 +147,63 @@ def test_cpp_chunking_matches_the_oracle(tmp_path, workload):
     got = [[int(x) for x in ln.split()] for ln in r.stdout.strip().split("\n")]
     assert got == want
     assert any(len(idx) > 2 for idx in want)      # some spectra were split
+
+
+def _compile(name):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    from lyspeq_gb300 import build
+    lib = build.build()
+    exe = os.path.join(HERE, "cpp", name)
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(HERE, "cpp", name + ".cpp"), "-L", os.path.dirname(lib), "-llqg",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", exe], check=True)
+    return exe
+
+
+def test_dropin_program_compiles_against_the_header():
+    """Host-only: the reference-signature drop-in program compiles and links."""
+    assert os.path.exists(_compile("test_dropin"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-5), (1, 1e-5)])
+def test_reference_signatures_reproduce_lyspeqs_own_test(engine_lib, tmp_path, precision, tol):
+    """lyspeq's end-to-end test (its spectrum file and test.config, truth
+    test_it1_*: fixture lyspeq_test_it1) through OneQSOEstimate(fname),
+    Chunk(QSOFile, i1, i2) and their oneQSOiteration with the reference's
+    signatures, at the reference's own comparison tolerance
+    (tests/compareTestResults.py: 1e-8 absolute + 1e-5 relative)."""
+    from lyspeq_gb300 import synth
+    exe = _compile("test_dropin")
+    z = np.load(os.path.join(HERE, "golden", "lyspeq_test_it1.npz"))
+    b = z["bins"]
+    bins = synth.Bins(b[0], int(b[1]), b[2], int(b[3]), b[4], b[5], b[6], int(b[7]))
+    nv, lenv, nzp, mfl, c0, c1 = z["grid"]
+    fid = tuple(float(x) for x in z["fid"])
+    r, dv = z["tables"][0]
+    table = synth.build_table(bins, int(r), float(dv), int(nv), float(lenv), int(nzp), fid=fid)
+    dat = tmp_path / "spectrum.dat"
+    dat.write_bytes(z["dat"].tobytes())
+    path = tmp_path / "case.bin"
+    with open(path, "wb") as out:
+        i64 = lambda v: out.write(struct.pack("<q", int(v)))
+        f64 = lambda v: out.write(struct.pack("<d", float(v)))
+
+        def vec(a):
+            a = np.ascontiguousarray(a, dtype="<f8").ravel()
+            i64(a.size)
+            out.write(a.tobytes())
+
+        vec(bins.k_edges); vec(bins.z_centers); f64(bins.dz); i64(1)
+        i64(nv); f64(lenv); i64(nzp)
+        i64(int(r)); f64(dv); vec(table.deriv); vec(table.signal)
+        f64(mfl); i64(c0); i64(c1)
+        for x in fid:
+            f64(x)
+        s = str(dat).encode()
+        i64(len(s)); out.write(s)
+        vec(z["detailed"]); vec(z["fisher_halved"])
+    res = subprocess.run([exe, str(path), str(precision), str(tol)], capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout[-4000:] + res.stderr[-2000:]
