@@ -15,11 +15,21 @@ deconvolved and oversampled x 3 (S and Q_k built as R M R^T), 20 k x 3 z
 bins; the matrices are prepared on the host before timing, as lyspeq does
 while reading its files.
 
-A step is one lqg_nr_iteration over the whole batch (table interpolation ->
-C -> FP64 Cholesky/inverse -> C^-1 Q_k on tensor cores -> traces) plus the
-global Fisher inversion and theta update.  `value` times steps with the
-chunks resident on the device; `e2e` times the same through the C ABI from
-host buffers (chunk upload, iteration, result download, solve).
+A step is one Newton-Raphson iteration: lqg_nr_iteration over the whole
+batch (table interpolation -> C -> df64 Cholesky and inverse factor -> the
+Q_k products on tensor cores -> traces) plus the global Fisher inversion and
+theta update.  Steps alternate between the two kinds an NR run is made of:
+the first iteration (theta = 0) and a later one (theta from the previous
+solve, which adds sum theta_k Q_k to C).  `value` times steps with the chunks
+resident on the device; `e2e` times the same through the C ABI from host
+buffers (chunk upload, iteration, result download, solve).
+
+Beside it: the FP64 GPU path on a subset stratified by chunk size (both kinds
+of iteration) with the mixed path's errors against it, a DFMA probe for the
+FP64 roofline, and the CPU restatement of the reference on a fixed sample of
+64 chunks stratified by size (16 quantile groups x 4), the same sample the
+`--impl reference` arm times, with its relative standard error.
+`--precision mixed_auto` runs the autotuner first (its time is reported).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -41,7 +51,6 @@ sys.path.insert(0, HERE)
 METRIC = "chunks/s per NR iteration (mixed precision, one GB300)"
 UNIT = "chunks/s"
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
-FP64_PEAK_TFLOPS = 1.191   # DFMA throughput measured on this machine's GB300 (see profiles/)
 
 
 def dist_env():
@@ -160,9 +169,23 @@ def flop_counts(ns_list, n_list):
                 traces=float(np.sum(2 * (ns + 2) * ns * n ** 2)))
 
 
-def cpu_port_rate(w, chunks, budget_s=15.0, max_chunks=None, order=None):
-    """Chunks/s of the CPU restatement of lyspeq's per-chunk path (numpy +
-    scipy's OpenBLAS, all host threads) on a bounded sample of the workload.
+def stratified_sample(n_list, strata=16, per=4, seed=12345):
+    """A fixed sample of the workload's chunks for the CPU legs: the chunks
+    sorted by size N, cut into `strata` equal quantile groups, `per` chunks
+    drawn from each (seeded); ordered round by round, so that every run of
+    `strata` consecutive entries holds one chunk of each group.  The cost of a
+    chunk grows like N^3, so a sample that follows the N distribution keeps the
+    rate estimate unbiased and its error small."""
+    order = np.argsort(np.asarray(n_list), kind="stable")
+    groups = np.array_split(order, strata)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    picks = [rng.choice(g, size=min(per, len(g)), replace=False) for g in groups]
+    return [int(picks[h][r]) for r in range(per) for h in range(strata) if r < len(picks[h])]
+
+
+def cpu_port_times(w, chunks, indices):
+    """Seconds per chunk of the CPU restatement of lyspeq's per-chunk path
+    (numpy + scipy's OpenBLAS, all host threads) for the given chunks.
     Resolution matrices are prepared by the restatement's own reader steps,
     outside the timed work (the reference does it while reading files)."""
     from oracle import qmle_port as P
@@ -170,9 +193,8 @@ def cpu_port_rate(w, chunks, budget_s=15.0, max_chunks=None, order=None):
                    cont_l_order=w.cont_l_order)
     keys = w.table_index()
     tvs = {}
-    work = 0.0
-    done = 0
-    for i in (order if order is not None else range(len(chunks))):
+    times = []
+    for i in indices:
         lam, delta, ivar, r = chunks[i]
         reso = rm = None
         if w.reso:
@@ -188,55 +210,117 @@ def cpu_port_rate(w, chunks, budget_s=15.0, max_chunks=None, order=None):
         if ch.res_index not in tvs:
             tvs[ch.res_index] = P.table_view(w.tables[ch.res_index], w.bins, w.nv, w.lenv, w.nzp)
         P.chunk_iteration(ch, w.bins, tvs[ch.res_index], np.zeros(w.bins.nkz), s)
-        work += time.perf_counter() - t0
-        done += 1
-        if work > budget_s or (max_chunks and done >= max_chunks):
-            break
-    return done / work, done, work
+        times.append(time.perf_counter() - t0)
+    return np.asarray(times)
+
+
+def stratified_rate(times, strata):
+    """chunks/s of a round-ordered stratified sample and the relative standard
+    error of that rate (within-group variance of the per-chunk times)."""
+    t = np.asarray(times)
+    groups = [t[h::strata] for h in range(strata) if len(t[h::strata])]
+    mean = float(np.mean([g.mean() for g in groups]))
+    var = sum((g.var(ddof=1) / len(g) if len(g) > 1 else 0.0) for g in groups) / len(groups) ** 2
+    return 1.0 / mean, float(np.sqrt(var) / mean)
+
+
+def cpu_sample_desc(w, strata, per):
+    return (f"{strata * per} chunks of the {w.name} workload stratified by N ({strata} quantile groups "
+            f"x {per}, seed 12345), numpy + scipy OpenBLAS on all host threads")
 
 
 def run_reference(args, rank, world):
+    """The reference arm: lyspeq's per-chunk path on the host cores (the numpy
+    restatement; the compiled reference does not exist on the GPU machine).  Each
+    timed step is one round of the stratified sample (one chunk of every size
+    group); warm-up steps run two chunks."""
     if rank != 0:
         return 0
     from lyspeq_gb300 import synth
     w = synth.make_workload(args.workload)
     chunks = chunk_arrays(w)
-    rng = np.random.default_rng(1)
-    rates, times, counts = [], [], []
-    for step in range(args.warmup + args.steps):
-        order = rng.permutation(len(chunks))
-        rate, done, dt = cpu_port_rate(w, chunks, budget_s=args.cpu_budget, order=order)
-        if step >= args.warmup:
-            rates.append(rate)
-            times.append(dt)
-            counts.append(done)
-    value = float(np.mean(rates))
+    strata, per = args.cpu_strata, args.cpu_per
+    sample = stratified_sample([len(c[0]) for c in chunks], strata, per)
+    for step in range(args.warmup):
+        cpu_port_times(w, chunks, sample[:2])
+    times, steps = [], []
+    for step in range(args.steps):
+        r = step % per
+        t = cpu_port_times(w, chunks, sample[r * strata:(r + 1) * strata])
+        times.extend(t.tolist())
+        steps.append(float(t.sum()))
+    value = len(times) / float(np.sum(times))
+    # step-to-step spread of the round means, as a relative standard error
+    rates = np.asarray([strata / x for x in steps])
+    rel_se = float(np.std(rates, ddof=1) / np.sqrt(len(rates)) / value) if len(rates) > 1 else None
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times) * 1e3),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(steps) * 1e3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded, DESI-like shapes)",
         "config": {"workload": describe(w, len(w.spectra)),
-                   "sample": f"{int(np.mean(counts))} random chunks per step (~{args.cpu_budget:.0f} s)"},
+                   "sample": f"step k: round k mod {per} of the stratified sample ({strata} chunks, one per N group)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{int(np.mean(counts))} chunks/step of the {args.workload} workload"},
+                         "sample": cpu_sample_desc(w, strata, per), "rel_stderr": rel_se},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
 
 
+def p1d_errors(w, g_ref, g_mix, fsum):
+    """Mixed against FP64: P1D relative error on the bins measured at 5 sigma
+    or more (the others are noise), and the largest |dP| in sigma."""
+    from lyspeq_gb300 import synth
+    pfid = synth.pd13_power(np.tile(w.bins.k_centers, w.bins.nz), np.repeat(w.bins.z_centers, w.bins.nk))
+    p_ref, p_mix = pfid + g_ref["theta"], pfid + g_mix["theta"]
+    sig = np.sqrt(np.abs(np.diag(g_ref["inverse"])))
+    used = (np.diag(fsum) > 0) & (sig > 0)
+    good = used & (np.abs(p_ref) > 5 * sig)
+    rel = float(np.max(np.abs(p_mix - p_ref)[good] / np.abs(p_ref)[good])) if good.any() else None
+    insig = float(np.max(np.abs(p_mix - p_ref)[used] / sig[used])) if used.any() else None
+    return rel, int(good.sum()), insig
+
+
+def mixed_vs_fp64(w, e64, theta):
+    """One FP64 and one mixed iteration of the engine at theta: the FP64 device
+    time and the mixed errors (global F per element normalised by
+    sqrt(F_ii F_jj), d, b, t normwise, d - b - t normwise on max |b|, P1D)."""
+    e64.iterate(theta=theta, precision="fp64")
+    fp64_ms = e64.timings()[7]
+    ref = e64.download()
+    g_ref = e64.fisher_solve(ref["fisher"], np.stack([ref["d"], ref["b"], ref["t"]]))
+    e64.iterate(theta=theta, precision="mixed")
+    mix = e64.download()
+    g_mix = e64.fisher_solve(mix["fisher"], np.stack([mix["d"], mix["b"], mix["t"]]))
+    dg = np.sqrt(np.abs(np.diag(g_ref["fisher"])))
+    den = np.outer(dg, dg)
+    den[den == 0] = 1
+    err_f = float(np.max(np.abs(g_mix["fisher"] - g_ref["fisher"]) / den))
+    dbt_ref = np.stack([ref["d"], ref["b"], ref["t"]])
+    dbt_mix = np.stack([mix["d"], mix["b"], mix["t"]])
+    err_dbt = float(np.max(np.abs(dbt_mix - dbt_ref) / np.max(np.abs(dbt_ref), axis=1, keepdims=True)))
+    e_ref, e_mix = dbt_ref[0] - dbt_ref[1] - dbt_ref[2], dbt_mix[0] - dbt_mix[1] - dbt_mix[2]
+    err_e = float(np.max(np.abs(e_mix - e_ref)) / np.max(np.abs(dbt_ref[1])))
+    p1d, nbins, insig = p1d_errors(w, g_ref, g_mix, ref["fisher"])
+    return fp64_ms, {"fisher": err_f, "dbt": err_dbt, "d_minus_b_minus_t": err_e, "p1d": p1d,
+                     "p1d_bins": nbins, "p1d_in_sigma": insig}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="desi")
     ap.add_argument("--chunks", type=int, default=None)
-    ap.add_argument("--fp64-chunks", type=int, default=96)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_direct", "mixed_auto"])
+    ap.add_argument("--fp64-chunks", type=int, default=128,
+                    help="chunks of the FP64 GPU comparison (a stratified subset); 0: all")
+    ap.add_argument("--cpu-strata", type=int, default=16)
+    ap.add_argument("--cpu-per", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -268,6 +352,11 @@ def main():
     ns_list = [(i["nq"] // w.bins.nk) * i["kbin_upp"] for i in infos]
     n_list = [i["n"] for i in infos]
     nkz = w.bins.nkz
+    tune_s = None
+    if args.precision == "mixed_auto":
+        t0 = time.perf_counter()
+        eng.autotune()
+        tune_s = time.perf_counter() - t0
 
     def allreduce(out):
         if world == 1:
@@ -276,15 +365,18 @@ def main():
         f, d, b, t = allreduce_sums(out["fisher"], out["d"], out["b"], out["t"], device=f"cuda:{local}")
         return dict(fisher=f, d=d, b=b, t=t, status=out["status"])
 
-    def step_resident():
-        eng.iterate(precision="mixed")
+    def nr_step(theta):
+        eng.iterate(theta=theta, precision=args.precision)
         out = allreduce(eng.download())
         return eng.fisher_solve(out["fisher"], np.stack([out["d"], out["b"], out["t"]]))
 
-    def step_e2e():
-        eng.clear()
-        add_packed(eng, w, packed)
-        return step_resident()
+    # A step is one Newton-Raphson iteration.  An NR run is one iteration at
+    # theta = 0 and then iterations at the theta of the previous solve; the
+    # steps alternate between the two (theta_1 from a first iteration before
+    # the warm-up), so that both kinds are timed.  Each kind replays its own
+    # captured graph after its second occurrence.
+    theta1 = nr_step(None)["theta"]
+    thetas = [theta1, None]
 
     def barrier():
         if world > 1:
@@ -292,18 +384,22 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        step_resident()
+    for k in range(args.warmup):
+        nr_step(thetas[k % 2])
     phase = np.zeros(8)
+    kind_ms = {0: [], 1: []}
     launches = 0
     waves = 1
     barrier()
     with ClockSampler(local) as clk:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        for _ in range(args.steps):
-            step_resident()
-            phase += eng.timings()
+        for k in range(args.steps):
+            th = thetas[(args.warmup + k) % 2]
+            nr_step(th)
+            tm = eng.timings()
+            phase += tm
+            kind_ms[0 if th is None else 1].append(float(tm[7]))
             launches += eng.launch_count()
             waves = eng.wave_count()
         e1.record()
@@ -316,15 +412,17 @@ def main():
         ms = float(t.item())
     value = n_ok * world / (ms / 1e3)
     phase /= args.steps
-    launches_per_iter = launches // max(args.steps, 1)
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the C ABI from pinned host buffers: upload, iteration,
+    # download of the sums, Fisher solve
     barrier()
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
     e2.record()
-    for _ in range(args.steps):
-        step_e2e()
+    for k in range(args.steps):
+        eng.clear()
+        add_packed(eng, w, packed)
+        nr_step(thetas[(args.warmup + k) % 2])
     e3.record()
     barrier()
     ms_e2e = e2.elapsed_time(e3) / args.steps
@@ -338,45 +436,29 @@ def main():
             dist.destroy_process_group()
         return 0
 
-    # FP64 GPU path on a subset of the same chunks, and accuracy of mixed vs FP64 there
-    sub = chunks[:args.fp64_chunks]
+    # FP64 GPU path on a stratified subset (or all chunks), and the accuracy of
+    # the mixed path against it at theta = 0 and at theta_1
+    if args.fp64_chunks and args.fp64_chunks < len(chunks):
+        per = max(1, args.fp64_chunks // 16)
+        sub_idx = stratified_sample([len(c[0]) for c in chunks], 16, per, seed=777)
+    else:
+        sub_idx = list(range(len(chunks)))
+    sub = [chunks[i] for i in sub_idx]
     e64 = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
                      cont=(w.cont_logl_order, w.cont_l_order), device=local)
     if w.reso:
         e64.add_chunks_reso(*pack(sub, True)[:4], w.oversample, pack(sub, True)[4])
     else:
         e64.add_chunk_list(sub)
-    e64.iterate(precision="fp64")
-    t0 = time.perf_counter()
-    e64.iterate(precision="fp64")
-    fp64_ms = e64.timings()[7]
-    ref = e64.download()
-    g_ref = e64.fisher_solve(ref["fisher"], np.stack([ref["d"], ref["b"], ref["t"]]))
-    fp64_rate = int((ref["status"] == 0).sum()) / (fp64_ms / 1e3)
-    e64.iterate(precision="mixed")
-    mix = e64.download()
-    g_mix = e64.fisher_solve(mix["fisher"], np.stack([mix["d"], mix["b"], mix["t"]]))
-    dg = np.sqrt(np.abs(np.diag(g_ref["fisher"])))
-    den = np.outer(dg, dg)
-    den[den == 0] = 1
-    err_f = float(np.max(np.abs(g_mix["fisher"] - g_ref["fisher"]) / den))
-    dbt_ref = np.stack([ref["d"], ref["b"], ref["t"]])
-    dbt_mix = np.stack([mix["d"], mix["b"], mix["t"]])
-    err_dbt = float(np.max(np.abs(dbt_mix - dbt_ref) / np.max(np.abs(dbt_ref), axis=1, keepdims=True)))
-    pfid = synth.pd13_power(np.tile(w.bins.k_centers, w.bins.nz),
-                            np.repeat(w.bins.z_centers, w.bins.nk))
-    p_ref, p_mix = pfid + g_ref["theta"], pfid + g_mix["theta"]
-    # P1D error on the bins the subset measures: P_ref at least 5 sigma from 0
-    # (sigma = sqrt(diag F^-1)); on the others the estimate is noise and a
-    # relative error says nothing.  Also the largest |dP| in units of sigma.
-    sig = np.sqrt(np.abs(np.diag(g_ref["inverse"])))
-    used = (np.diag(g_ref["fisher"]) > 0) & (sig > 0)
-    good = used & (np.abs(p_ref) > 5 * sig)
-    err_p1d = float(np.max(np.abs(p_mix - p_ref)[good] / np.abs(p_ref)[good])) if good.any() else None
-    err_p1d_sigma = float(np.max(np.abs(p_mix - p_ref)[used] / sig[used])) if used.any() else None
+    e64.iterate(precision="fp64")   # warm-up
+    fp64_ms, err0 = mixed_vs_fp64(w, e64, None)
+    fp64_ms1, err1 = mixed_vs_fp64(w, e64, theta1)
+    # the same alternation as the timed steps: the mean of the two kinds
+    fp64_rate = len(sub) / ((fp64_ms + fp64_ms1) / 2e3)
     e64.close()
+    fp64_peak = lqg.probe_fp64_rate(local)
 
-    # roofline of the dominant kernel
+    # roofline of the dominant phase
     fl = flop_counts(ns_list, n_list)
     names = ["build_s_c", "factor", "build_q", "products_tc", "traces_tc", "finish", "accumulate"]
     shares = {nm: float(phase[i] / phase[7]) for i, nm in enumerate(names)}
@@ -402,43 +484,47 @@ def main():
                                "(MEASURED_PEAKS.json has no FP32 figure)"}
     elif names[dom] == "factor":
         achieved = fl["factor"] / (phase[1] / 1e3) / 1e12
-        roof = {"kernel": "k_factor", "bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
-                "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
-                "peak_source": "DFMA throughput probe on GB300 (MEASURED_PEAKS.json has no FP64 figure)"}
+        roof = {"kernel": "k_factor_tiled", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                "peak_source": "DFMA probe (lqg_probe_fp64_rate) run by this bench"}
     else:
         key = "products" if names[dom] == "products_tc" else "traces"
         achieved = fl[key] / (phase[dom] / 1e3) / 1e12
-        pk = peaks.get("bf16_tflops", 1900.0)
+        pk = peaks.get("bf16_tflops_sustained", 1700.0)
         # DRAM traffic per launch of the first product kernel, X_s = W Q_s (one
-        # launch per wave; the larger of the two product stages): algorithmic
-        # bytes (Q_s read and X_s written, fp16 hi/lo, ns + 1 slots) times the
-        # measured/algorithmic ratio, 0.99, of an ncu capture of the same kernel
-        # on 64 chunks of this workload (profiles/k_tc_gemm_whitened_desi64.md)
+        # launch per wave, the larger of the two product stages): its
+        # algorithmic bytes (Q_s read and X_s written as fp16 hi/lo, ns + 1
+        # slots) times 0.99, the measured/algorithmic ratio of an ncu capture
+        # of the same kernel on 64 chunks of this workload
         traffic = None
-        n_waves = waves                            # one launch of each product kernel per wave
-        if key == "products" and n_waves > 0:
+        if key == "products" and waves > 0:
             ld = np.ceil(np.asarray(n_list) / 64.0) * 64.0
             alg = float(np.sum(2.0 * (np.asarray(ns_list) + 1) * ld * ld * 4.0))
-            traffic = 0.99 * alg / n_waves
+            traffic = 0.99 * alg / waves
         roof = {"kernel": "k_tc_gemm<1> + k_tc_gemm<2> (phase); traffic of k_tc_gemm<1>" if key == "products"
                 else "k_tc_gram", "bound": "tensor",
                 "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
                 "traffic": traffic, "traffic_unit": "bytes per launch",
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (the kernel runs inside a "
+                               "seconds-long step), of measured"}
     tensor_tf = fl["products"] / (phase[3] / 1e3) / 1e12 if phase[3] > 0 else None
-    fp64_tf = fl["factor"] / (phase[1] / 1e3) / 1e12 if phase[1] > 0 else None
+    df64_tf = fl["factor"] / (phase[1] / 1e3) / 1e12 if phase[1] > 0 else None
 
     cpu = None
     if not args.no_cpu:
-        rate, done, dt = cpu_port_rate(w, chunks, budget_s=args.cpu_budget)
+        sample = stratified_sample([len(c[0]) for c in chunks], args.cpu_strata, args.cpu_per)
+        times = cpu_port_times(w, chunks, sample)
+        rate, rel_se = stratified_rate(times, args.cpu_strata)
         cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"first {done} chunks of the workload, {dt:.1f} s, numpy + scipy OpenBLAS"}
+               "sample": cpu_sample_desc(w, args.cpu_strata, args.cpu_per) + f", {float(np.sum(times)):.1f} s",
+               "rel_stderr": rel_se}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f16x3 products / df64 factorisation", "data": "synthetic (seeded)",
-        "config": {"workload": describe(w, n_ok),
+        "config": {"workload": describe(w, n_ok), "precision": args.precision,
+                   "step": "one NR iteration; steps alternate theta = 0 and theta from the previous solve",
                    "l2": "working set of tens of GB per iteration (>> 129 MB L2); no flush"},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -446,14 +532,19 @@ def main():
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "fp64_gpu": {"value": fp64_rate, "unit": UNIT, "chunks": len(sub), "ms": fp64_ms},
+        "iteration_ms": {"theta_0": float(np.mean(kind_ms[0])) if kind_ms[0] else None,
+                         "theta_1": float(np.mean(kind_ms[1])) if kind_ms[1] else None},
+        "fp64_gpu": {"value": fp64_rate, "unit": UNIT, "chunks": len(sub), "ms_theta_0": fp64_ms,
+                     "ms_theta_1": fp64_ms1, "sample": "stratified by N" if len(sub) < len(chunks) else "all"},
+        "fp64_peak_tflops": fp64_peak,
         "mixed_over_fp64": value / fp64_rate if fp64_rate else None,
-        "mixed_rel_err": {"fisher": err_f, "dbt": err_dbt, "p1d": err_p1d, "p1d_bins": int(good.sum()),
-                          "p1d_in_sigma": err_p1d_sigma},
+        "mixed_rel_err": {"theta_0": err0, "theta_1": err1},
         "phase_ms": {nm: float(phase[i]) for i, nm in enumerate(names)},
         "phase_share": shares,
-        "achieved_tflops": {"factor_df64": fp64_tf, "tensor_products": tensor_tf},
+        "achieved_tflops": {"factor_df64": df64_tf, "tensor_products": tensor_tf},
     }
+    if tune_s is not None:
+        line["autotune_s"] = tune_s
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
