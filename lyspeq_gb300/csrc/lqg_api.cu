@@ -133,6 +133,7 @@ extern "C" const char *lqg_last_error(const lqg_ctx *ctx) {
 
 extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tables *tables,
                               const lqg_opts *opts, int device) {
+    cudaGetLastError();   // an error left by earlier work of the process is not this call's
     if (!out || !bins || !tables || !opts) return LQG_ERR_ARG;
     *out = nullptr;
     if (bins->nk <= 0 || bins->nk > kMaxKBands || bins->nz <= 0 || bins->nz > 64 || !bins->k_edges || !bins->z_centers ||
@@ -1419,6 +1420,9 @@ extern "C" int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, in
     if (max_rel_err <= 0) max_rel_err = 1e-5;
     if (max_chunks <= 0) max_chunks = 48;
     if (flags == 0) flags = 7;
+    // the batch-wide buffers (statuses, metadata, results) are sized by the
+    // whole batch before the sample iterations swap in their subsets
+    if (int rc = upload_pixels(ctx)) return rc;
     std::map<int, std::vector<int>> buckets;   // padded size -> batch indices (table chunks only)
     for (int i = 0; i < (int) ctx->chunks.size(); ++i)
         if (ctx->chunks[i].nelem == 0) buckets[ctx->chunks[i].ld].push_back(i);
