@@ -283,7 +283,7 @@ def p1d_errors(w, g_ref, g_mix, fsum):
     return rel, int(good.sum()), insig
 
 
-def mixed_vs_fp64(w, e64, theta):
+def mixed_vs_fp64(w, e64, theta, precision="mixed"):
     """One FP64 and one mixed iteration of the engine at theta: the FP64 device
     time and the mixed errors (global F per element normalised by
     sqrt(F_ii F_jj), d, b, t normwise, d - b - t normwise on max |b|, P1D)."""
@@ -291,7 +291,7 @@ def mixed_vs_fp64(w, e64, theta):
     fp64_ms = e64.timings()[7]
     ref = e64.download()
     g_ref = e64.fisher_solve(ref["fisher"], np.stack([ref["d"], ref["b"], ref["t"]]))
-    e64.iterate(theta=theta, precision="mixed")
+    e64.iterate(theta=theta, precision=precision)
     mix = e64.download()
     g_mix = e64.fisher_solve(mix["fisher"], np.stack([mix["d"], mix["b"], mix["t"]]))
     dg = np.sqrt(np.abs(np.diag(g_ref["fisher"])))
@@ -450,9 +450,11 @@ def main():
         e64.add_chunks_reso(*pack(sub, True)[:4], w.oversample, pack(sub, True)[4])
     else:
         e64.add_chunk_list(sub)
+    if args.precision == "mixed_auto":
+        e64.set_tuning(eng.tuning())
     e64.iterate(precision="fp64")   # warm-up
-    fp64_ms, err0 = mixed_vs_fp64(w, e64, None)
-    fp64_ms1, err1 = mixed_vs_fp64(w, e64, theta1)
+    fp64_ms, err0 = mixed_vs_fp64(w, e64, None, args.precision)
+    fp64_ms1, err1 = mixed_vs_fp64(w, e64, theta1, args.precision)
     # the same alternation as the timed steps: the mean of the two kinds
     fp64_rate = len(sub) / ((fp64_ms + fp64_ms1) / 2e3)
     e64.close()

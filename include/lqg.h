@@ -255,7 +255,7 @@ int lqg_sync(lqg_ctx *ctx);
  * form (flags & 1), hi*hi drain interval of the products 4, 8 or 16 K blocks
  * (flags & 2); a candidate is kept when every per-chunk d, b, t (normwise)
  * and Fisher element (normalised by sqrt(F_ii F_jj)) of the sample is within
- * half of max_rel_err of the FP64 results (room for the chunks not sampled).
+ * 0.8 max_rel_err of the FP64 results (room for the chunks not sampled).
  * The kept candidates are timed on up to max_chunks chunks of that size
  * (device time of an iteration over them) and the fastest is stored; then the
  * Gram's K elements per split, 16384, 32768 or 65536 (flags & 4), by time.

@@ -741,8 +741,12 @@ __global__ void k_finish(WaveArgs a, int mixed) {
             double e = d[ikz] - x;
             if (a.theta)
                 for (int s2 = 0; s2 < ns; ++s2) {
-                    const double th = a.theta[ch.fis + (s2 / ch.kbin_upp) * bins.nk + s2 % ch.kbin_upp];
-                    if (th != 0.0) e += th * gram(min(s, s2), max(s, s2));
+                    const int jkz = (s2 / ch.kbin_upp) * bins.nk + s2 % ch.kbin_upp;
+                    const double th = a.theta[ch.fis + jkz];
+                    if (th == 0.0) continue;
+                    // F as written above (upper triangle), else from the Gram partials
+                    const int lo = min(ikz, jkz), hi = max(ikz, jkz);
+                    e += th * (a.skip_fisher ? gram(min(s, s2), max(s, s2)) : F[(size_t) lo * nq + hi]);
                 }
             const double bt = d[ikz] - e;
             if (a.turn_off_sfid) b[ikz] = bt;

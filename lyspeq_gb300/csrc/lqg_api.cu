@@ -1451,8 +1451,8 @@ extern "C" int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, in
                 if (rc) { ctx->tuning = saved; return rc; }
                 const double err = max_error(ctx, acc, mix, ref);
                 if (err < best_err) { best_err = err; best_any = t; }
-                // half the bound on the sample leaves room for the chunks not sampled
-                if (!(err <= 0.5 * max_rel_err)) continue;
+                // a margin on the sample leaves room for the chunks not sampled
+                if (!(err <= 0.8 * max_rel_err)) continue;
                 double ms = 0;
                 // twice: the second replays the captured graph
                 rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
