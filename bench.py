@@ -29,7 +29,10 @@ of iteration) with the mixed path's errors against it, a DFMA probe for the
 FP64 roofline, and the CPU restatement of the reference on a fixed sample of
 64 chunks stratified by size (16 quantile groups x 4), the same sample the
 `--impl reference` arm times, with its relative standard error.
-`--precision mixed_auto` runs the autotuner first (its time is reported).
+The default precision, mixed_auto, runs the autotuner before the timed
+region (its time is reported) and then iterates with the chosen plan per
+chunk size; `--precision mixed` uses the fixed whitened plan.  `--fp64-full`
+runs the FP64 comparison over every chunk (one iteration, minutes).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -316,9 +319,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="desi")
     ap.add_argument("--chunks", type=int, default=None)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_direct", "mixed_auto"])
+    ap.add_argument("--precision", default="mixed_auto", choices=["mixed", "mixed_direct", "mixed_auto"])
     ap.add_argument("--fp64-chunks", type=int, default=128,
                     help="chunks of the FP64 GPU comparison (a stratified subset); 0: all")
+    ap.add_argument("--fp64-full", action="store_true",
+                    help="FP64 GPU path over every chunk instead: one theta = 0 iteration, no warm-up")
     ap.add_argument("--cpu-strata", type=int, default=16)
     ap.add_argument("--cpu-per", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
@@ -427,6 +432,13 @@ def main():
     barrier()
     ms_e2e = e2.elapsed_time(e3) / args.steps
     e2e_value = n_ok * world / (ms_e2e / 1e3)
+    # the host Fisher solve of a step on its own (part of every timed step)
+    out = allreduce(eng.download())
+    dbt = np.stack([out["d"], out["b"], out["t"]])
+    t0 = time.perf_counter()
+    for _ in range(5):
+        eng.fisher_solve(out["fisher"], dbt)
+    solve_ms = (time.perf_counter() - t0) / 5 * 1e3
     h2d = int(lam.nbytes + delta.nbytes + ivar.nbytes + 8 * nkz + (rr.nbytes if w.reso else 0))
     d2h = int(8 * (nkz * nkz + 3 * nkz))
 
@@ -438,7 +450,7 @@ def main():
 
     # FP64 GPU path on a stratified subset (or all chunks), and the accuracy of
     # the mixed path against it at theta = 0 and at theta_1
-    if args.fp64_chunks and args.fp64_chunks < len(chunks):
+    if args.fp64_chunks and args.fp64_chunks < len(chunks) and not args.fp64_full:
         per = max(1, args.fp64_chunks // 16)
         sub_idx = stratified_sample([len(c[0]) for c in chunks], 16, per, seed=777)
     else:
@@ -452,11 +464,18 @@ def main():
         e64.add_chunk_list(sub)
     if args.precision == "mixed_auto":
         e64.set_tuning(eng.tuning())
-    e64.iterate(precision="fp64")   # warm-up
-    fp64_ms, err0 = mixed_vs_fp64(w, e64, None, args.precision)
-    fp64_ms1, err1 = mixed_vs_fp64(w, e64, theta1, args.precision)
-    # the same alternation as the timed steps: the mean of the two kinds
-    fp64_rate = len(sub) / ((fp64_ms + fp64_ms1) / 2e3)
+    if args.fp64_full:
+        # every chunk once at theta = 0 (an FP64 iteration of the whole set takes
+        # minutes; its first-iteration planning is a negligible part of it)
+        fp64_ms, err0 = mixed_vs_fp64(w, e64, None, args.precision)
+        fp64_ms1, err1 = None, None
+        fp64_rate = len(sub) / (fp64_ms / 1e3)
+    else:
+        e64.iterate(precision="fp64")   # warm-up
+        fp64_ms, err0 = mixed_vs_fp64(w, e64, None, args.precision)
+        fp64_ms1, err1 = mixed_vs_fp64(w, e64, theta1, args.precision)
+        # the same alternation as the timed steps: the mean of the two kinds
+        fp64_rate = len(sub) / ((fp64_ms + fp64_ms1) / 2e3)
     e64.close()
     fp64_peak = lqg.probe_fp64_rate(local)
 
@@ -537,16 +556,21 @@ def main():
         "iteration_ms": {"theta_0": float(np.mean(kind_ms[0])) if kind_ms[0] else None,
                          "theta_1": float(np.mean(kind_ms[1])) if kind_ms[1] else None},
         "fp64_gpu": {"value": fp64_rate, "unit": UNIT, "chunks": len(sub), "ms_theta_0": fp64_ms,
-                     "ms_theta_1": fp64_ms1, "sample": "stratified by N" if len(sub) < len(chunks) else "all"},
+                     "ms_theta_1": fp64_ms1,
+                     "sample": "stratified by N" if len(sub) < len(chunks)
+                     else ("all, one theta = 0 iteration" if args.fp64_full else "all")},
         "fp64_peak_tflops": fp64_peak,
         "mixed_over_fp64": value / fp64_rate if fp64_rate else None,
         "mixed_rel_err": {"theta_0": err0, "theta_1": err1},
         "phase_ms": {nm: float(phase[i]) for i, nm in enumerate(names)},
         "phase_share": shares,
+        "fisher_solve_ms": solve_ms,
         "achieved_tflops": {"factor_df64": df64_tf, "tensor_products": tensor_tf},
     }
     if tune_s is not None:
         line["autotune_s"] = tune_s
+        # the chosen plan per padded size: ld, whitened form, drain, Gram K per split, CTA pairs
+        line["tuning"] = eng.tuning().tolist()
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -258,14 +258,18 @@ int lqg_sync(lqg_ctx *ctx);
  * 0.8 max_rel_err of the FP64 results (room for the chunks not sampled).
  * The kept candidates are timed on up to max_chunks chunks of that size
  * (device time of an iteration over them) and the fastest is stored; then the
- * Gram's K elements per split, 16384, 32768 or 65536 (flags & 4), by time.
+ * Gram's K elements per split, 16384, 32768 or 65536 (flags & 4), by time;
+ * with flags & 8 before that, the products on CTA pairs (tcgen05 cta_group::2,
+ * 256 x 128 tiles), kept when within the bound and faster.
  * LQG_PRECISION_MIXED_AUTO iterations use the table; the results of the
- * batch's last iteration are invalidated.  flags = 0 means all (7);
+ * batch's last iteration are invalidated.  flags = 0 means all (15);
  * max_rel_err <= 0 means 1e-5; max_chunks <= 0 means 48. */
 int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, int flags);
-/* The table, one entry of 4 ints per padded size: ld, form (1 whitened, 0
- * direct), drain interval, Gram K per split.  lqg_tuning_get returns the
- * number of entries (writing at most n); lqg_tuning_set replaces the table. */
+/* The table, one entry of LQG_TUNING_FIELDS ints per padded size: ld, form
+ * (1 whitened, 0 direct), drain interval, Gram K per split, CTA-pair products
+ * (1) or single-CTA (0).  lqg_tuning_get returns the number of entries
+ * (writing at most n); lqg_tuning_set replaces the table. */
+#define LQG_TUNING_FIELDS 5
 int lqg_tuning_get(const lqg_ctx *ctx, int *entries, int n);
 int lqg_tuning_set(lqg_ctx *ctx, const int *entries, int n);
 

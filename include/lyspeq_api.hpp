@@ -695,24 +695,28 @@ public:
     void autotune(double max_rel_err = 1e-5, int max_chunks = 48, int flags = 0) {
         check(lqg_autotune(ctx_.get(), max_rel_err, max_chunks, flags), "lqg_autotune");
     }
-    // The table as text, one line "ld form drain gram_k" per padded size
+    // The table as text, one line "ld form drain gram_k pair" per padded size
     void saveTuning(const std::string &path) const {
         const int n = lqg_tuning_get(ctx_.get(), nullptr, 0);
-        std::vector<int> e(4 * (size_t) std::max(n, 1));
+        std::vector<int> e(LQG_TUNING_FIELDS * (size_t) std::max(n, 1));
         lqg_tuning_get(ctx_.get(), e.data(), n);
         std::FILE *f = std::fopen(path.c_str(), "w");
         if (!f) throw std::runtime_error("cannot write " + path);
-        for (int k = 0; k < n; ++k) std::fprintf(f, "%d %d %d %d\n", e[4 * k], e[4 * k + 1], e[4 * k + 2], e[4 * k + 3]);
+        for (int k = 0; k < n; ++k) {
+            const int *r = e.data() + LQG_TUNING_FIELDS * k;
+            std::fprintf(f, "%d %d %d %d %d\n", r[0], r[1], r[2], r[3], r[4]);
+        }
         std::fclose(f);
     }
     void loadTuning(const std::string &path) {
         std::FILE *f = std::fopen(path.c_str(), "r");
         if (!f) throw std::runtime_error("cannot read " + path);
         std::vector<int> e;
-        int v[4];
-        while (std::fscanf(f, "%d %d %d %d", &v[0], &v[1], &v[2], &v[3]) == 4) e.insert(e.end(), v, v + 4);
+        int v[LQG_TUNING_FIELDS];
+        while (std::fscanf(f, "%d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4]) == LQG_TUNING_FIELDS)
+            e.insert(e.end(), v, v + LQG_TUNING_FIELDS);
         std::fclose(f);
-        check(lqg_tuning_set(ctx_.get(), e.data(), (int) e.size() / 4), "lqg_tuning_set");
+        check(lqg_tuning_set(ctx_.get(), e.data(), (int) e.size() / LQG_TUNING_FIELDS), "lqg_tuning_set");
     }
 
     // Device time of the last iteration's phases (ms), lqg_last_timings.

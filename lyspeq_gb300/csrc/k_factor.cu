@@ -805,7 +805,7 @@ __device__ void whitened_factor(const WaveArgs &a, const ChunkDesc &ch, float2 *
 // The marginalised C^-1 of the whitened form in FP64 at o_m, from the df64
 // inverse factor X = L^-1 (left in place for W): a copy of X, C^-1 = D X^T X D
 // (lauum_df) and the reference's rank-1 removals.  k_dx_mixed contracts it
-// with every Q_s for x_s = tr(Q_s C^-1), from which k_finish forms
+// with every Q_s for x_s = tr(Q_s C^-1), from which k_finish_dx forms
 // d_s - b_s - t_s without the 22-bit trace products.
 __device__ void marginal_inverse_df(const WaveArgs &a, const ChunkDesc &ch, const float2 *X2, int nb,
                                     double *scratch, FactorSmem &s) {

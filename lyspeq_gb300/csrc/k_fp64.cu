@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
 // Mixed path, the d and x partials in double-float arithmetic on the FP32 pipe:
 //   d_s = y^T Q_s y       (computePSbeforeFvector, core/chunk_estimate.cpp:754-759)
 //   x_s = tr(Q_s C^-1) = sum_ij Q_s,ij C^-1_ij   (C^-1 marginalised, when cinv_m)
-// over the upper triangle, off-diagonal elements counted twice.  k_finish
+// over the upper triangle, off-diagonal elements counted twice.  k_finish_dx
 // forms d - b - t = d - x + (F theta) from them (b_s + t_s = tr(C^-1 Q_s C^-1 (S +
 // N)) with C^-1 C C^-1 = C^-1), a difference much smaller than its terms on
 // high signal-to-noise chunks: a float Q_s (2^-24) or float y y^T - C^-1 already
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
 // slot loop (the FP64 pipe is 1/64 of the FP32 one): warp sums in
 // double-float, and each warp's (hi, lo) pair is stored in its 8-byte partial
 // slot.  Blocks and warps map to the d-partial slots of k_build_q_mixed's
-// layout (half tiles of 32 x 64, 8 warps); blocks of lower tiles write zeros.
+// layout (half tiles of 32 x 64, 8 warps); blocks of lower tiles write nothing.
 constexpr int DX_E = 8;   // elements per thread: rows warp + 8u (u < 4), columns 2 lane, 2 lane + 1
 
 template <bool GR>
@@ -425,14 +425,7 @@ __global__ void __launch_bounds__(256, 2) k_dx_mixed(WaveArgs a) {
     const bool want_x = a.dbt_id && ch.cinv_m;
     double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
     double *xpart = want_x ? ws_d(a, ch.o_xpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns : nullptr;
-    if (ti > tj) {
-        // counted through the mirrored upper tile
-        for (int s = lane; s < ch.ns; s += 32) {
-            dpart[s] = 0.0;
-            if (want_x) xpart[s] = 0.0;
-        }
-        return;
-    }
+    if (ti > tj) return;   // counted through the mirrored upper tile; k_finish_dx skips these parts
     const DeviceBins &bins = *a.bins;
     const float2 *lw2 = a.logw2 + ch.pix, *sw2 = a.sqw2 + ch.pix;
     const double *y = fws_d(a, ch.o_y);
@@ -666,6 +659,21 @@ __global__ void __launch_bounds__(256) k_dgram(WaveArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Element (i, j) of chunk c's trace Gram on the mixed path, from its fp32 split
+// partials in fixed order, unscaled: F_ij (j < ns), t_i (j = ns), b_i (j = ns + 1).
+__device__ __forceinline__ double gram_mixed(const WaveArgs &a, const ChunkDesc &ch, int c, int i, int j) {
+    const double *psc = a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + ch.slot_p;
+    const double *rsc = a.sym ? psc
+                              : a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + a.total_slots_p + ch.slot_r;
+    const size_t blkstride = (size_t) a.gram_splits * GR * GR;
+    const int blk = (i / GR) * a.gt + j / GR, li = i % GR, lj = j % GR;
+    const float *gp = a.gram_part + ((size_t) c * a.gt * a.gt + blk) * blkstride;
+    double acc = 0;
+    for (int sp = 0; sp < a.gram_splits; ++sp) acc += (double) gp[(size_t) sp * GR * GR + li * GR + lj];
+    return acc / (psc[i] * rsc[j]);
+}
+
+// ---------------------------------------------------------------------------
 // Per-chunk reduction of the Gram partials and d partials (fixed order), written
 // in the reference's per-chunk layout (Chunk::dbt_estimate_before_fisher_vector
 // and Chunk::fisher_matrix, upper triangle, not halved).
@@ -683,37 +691,42 @@ __global__ void k_finish(WaveArgs a, int mixed) {
     // d partials: 8 warps per 64 x 64 tile (FP64 build) or per 32 x 64 half tile (mixed)
     const int ns = ch.ns, parts = (ch.ld / T64) * (ch.ld / T64) * 8 * (mixed ? 2 : 1);
     const double *dpart = ws_d(a, ch.o_dpart);
-    // the mixed path's table chunks leave (hi, lo) float pairs (k_dx_mixed)
-    const bool pairs = mixed && ch.nelem == 0;
-    auto part = [&](const double *base, int p, int s) {
-        if (!pairs) return base[(size_t) p * ns + s];
-        const float2 v = reinterpret_cast<const float2 *>(base)[(size_t) p * ns + s];
-        return (double) v.x + (double) v.y;
-    };
-    for (int s = threadIdx.x; s < ns; s += blockDim.x) {
-        double acc = 0;
-        for (int p = 0; p < parts; ++p) acc += part(dpart, p, s);
-        d[(s / ch.kbin_upp) * bins.nk + s % ch.kbin_upp] = acc;
+    // the mixed path's table chunks: d (and d - b - t) in k_finish_dx
+    if (!(mixed && ch.nelem == 0)) {
+        // Sum of every slot's parts in a fixed order.  Thread t adds parts g, g + G,
+        // ... of slot s0 + t % R (g = t / R, R slots per round, G = blockDim / R
+        // groups), so that the threads of a group read consecutive slots of one
+        // part; then the first R threads add the G group sums in order.
+        __shared__ double red[256];
+        const int R = min(ns, (int) blockDim.x), G = blockDim.x / R;
+        const int g = threadIdx.x / R, sl = threadIdx.x % R;
+        for (int s0 = 0; s0 < ns; s0 += R) {
+            const int s = s0 + sl;
+            if (g < G) {
+                double acc = 0;
+                if (s < ns)
+                    for (int p = g; p < parts; p += G) acc += dpart[(size_t) p * ns + s];
+                red[g * R + sl] = acc;
+            }
+            __syncthreads();
+            if ((int) threadIdx.x < R && s0 + (int) threadIdx.x < ns) {
+                double v = 0;
+                for (int k = 0; k < G; ++k) v += red[k * R + threadIdx.x];
+                const int sv = s0 + (int) threadIdx.x;
+                d[(sv / ch.kbin_upp) * bins.nk + sv % ch.kbin_upp] = v;
+            }
+            __syncthreads();
+        }
     }
     const size_t blkstride = (size_t) a.gram_splits * GR * GR;
     if (mixed) {
         // G = P R^T: P rows = A_i^T (i < ns), R rows = A_j (j < ns), C^-1 S, C^-1 N;
         // blocks bi <= bj only.  F_ij = G_ij (i <= j), t_i = G_{i,ns}, b_i = G_{i,ns+1}.
         // Whitened form: rows B_i of P on both sides (B_ns = W S W^T, B_{ns+1} = W N W^T).
-        const double *psc = a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + ch.slot_p;
-        const double *rsc = a.sym ? psc
-                                  : a.scales + (size_t) 4 * a.n_chunks + a.total_slots_q + a.total_slots_p + ch.slot_r;
-        auto gram = [&](int i, int j) {
-            const int blk = (i / GR) * a.gt + j / GR, li = i % GR, lj = j % GR;
-            const float *gp = a.gram_part + ((size_t) c * a.gt * a.gt + blk) * blkstride;
-            double acc = 0;
-            for (int sp = 0; sp < a.gram_splits; ++sp) acc += (double) gp[(size_t) sp * GR * GR + li * GR + lj];
-            return acc / (psc[i] * rsc[j]);
-        };
         for (int e = threadIdx.x; e < ns * (ns + 2); e += blockDim.x) {
             const int i = e / (ns + 2), j = e % (ns + 2);
             if (j < ns && j < i) continue;
-            const double g = gram(i, j);
+            const double g = gram_mixed(a, ch, c, i, j);
             const int ikz = (i / ch.kbin_upp) * bins.nk + i % ch.kbin_upp;
             if (j < ns) {
                 const int jkz = (j / ch.kbin_upp) * bins.nk + j % ch.kbin_upp;
@@ -723,35 +736,6 @@ __global__ void k_finish(WaveArgs a, int mixed) {
             } else {
                 b[ikz] = g;
             }
-        }
-        if (!(a.dbt_id && ch.cinv_m)) return;
-        // d - b - t without the 22-bit traces.  With C = S + N + sum_s theta_s Q_s
-        // (the stored slots) and the marginalised C^-1 (C^-1 C C^-1 = C^-1),
-        //   b_s + t_s = tr(C^-1 Q_s C^-1 (S + N)) = tr(Q_s C^-1) - sum_s' F_ss' theta_s',
-        // so e_s = d_s - b_s - t_s = d_s - x_s + (F theta)_s with x_s = tr(Q_s C^-1)
-        // from k_dx_mixed.  The larger of b_s and t_s (b_s alone without S_fid)
-        // takes the difference, so that d - b - t = e exactly and each keeps its
-        // own relative accuracy.
-        __syncthreads();
-        const double *xp = ws_d(a, ch.o_xpart);
-        for (int s = threadIdx.x; s < ns; s += blockDim.x) {
-            double x = 0;
-            for (int p = 0; p < parts; ++p) x += part(xp, p, s);
-            const int ikz = (s / ch.kbin_upp) * bins.nk + s % ch.kbin_upp;
-            double e = d[ikz] - x;
-            if (a.theta)
-                for (int s2 = 0; s2 < ns; ++s2) {
-                    const int jkz = (s2 / ch.kbin_upp) * bins.nk + s2 % ch.kbin_upp;
-                    const double th = a.theta[ch.fis + jkz];
-                    if (th == 0.0) continue;
-                    // F as written above (upper triangle), else from the Gram partials
-                    const int lo = min(ikz, jkz), hi = max(ikz, jkz);
-                    e += th * (a.skip_fisher ? gram(min(s, s2), max(s, s2)) : F[(size_t) lo * nq + hi]);
-                }
-            const double bt = d[ikz] - e;
-            if (a.turn_off_sfid) b[ikz] = bt;
-            else if (fabs(b[ikz]) >= fabs(t[ikz])) b[ikz] = bt - t[ikz];
-            else t[ikz] = bt - b[ikz];
         }
         return;
     }
@@ -772,6 +756,71 @@ __global__ void k_finish(WaveArgs a, int mixed) {
             b[jkz] = acc;
         }
     }
+}
+
+
+// ---------------------------------------------------------------------------
+// Mixed path, table chunks (after k_finish): d_s and x_s = tr(Q_s C^-1) from
+// k_dx_mixed's (hi, lo) partials, one warp per slot.  The parts of a slot are
+// the 16 warps of each upper 64 x 64 tile; a tile row's upper tiles are
+// consecutive, so the lanes stride over them row by row, each lane adds its
+// parts in order and the warp sums the lanes in a fixed tree.  Then d - b - t
+// without the 22-bit traces: with C = S + N + sum_s theta_s Q_s (the stored
+// slots) and the marginalised C^-1 (C^-1 C C^-1 = C^-1),
+//   b_s + t_s = tr(C^-1 Q_s C^-1 (S + N)) = tr(Q_s C^-1) - sum_s' F_ss' theta_s',
+// so e_s = d_s - b_s - t_s = d_s - x_s + (F theta)_s.  The larger of b_s and t_s
+// (b_s alone without S_fid) takes the difference, so that d - b - t = e exactly
+// and each keeps its own relative accuracy.
+__global__ void __launch_bounds__(256) k_finish_dx(WaveArgs a) {
+    const int c = blockIdx.y;
+    const ChunkDesc &ch = a.chunks[c];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int s = blockIdx.x * 8 + warp, ns = ch.ns, nq = ch.nq;
+    if (ch.nelem > 0 || s >= ns || a.status[ch.gidx] != LQG_CHUNK_OK) return;
+    if (!LQG_IN_BOUNDS(a, ch.res_off + 3 * nq + (int64_t) nq * nq <= a.results_elems, 8, c, ch.res_off)) return;
+    const DeviceBins &bins = *a.bins;
+    double *res = a.results + ch.res_off;
+    double *d = res, *b = res + nq, *t = res + 2 * nq, *F = res + 3 * nq;
+    const bool want_x = a.dbt_id && ch.cinv_m;
+    const int tpr = ch.ld / T64;
+    const float2 *dp = reinterpret_cast<const float2 *>(ws_d(a, ch.o_dpart));
+    const float2 *xp = want_x ? reinterpret_cast<const float2 *>(ws_d(a, ch.o_xpart)) : nullptr;
+    double dsum = 0, xsum = 0;
+    for (int ti = 0; ti < tpr; ++ti) {
+        const int p1 = (ti * tpr + tpr) * 16;
+        for (int p = (ti * tpr + ti) * 16 + lane; p < p1; p += 32) {
+            const float2 v = dp[(size_t) p * ns + s];
+            dsum += (double) v.x + (double) v.y;
+            if (want_x) {
+                const float2 u = xp[(size_t) p * ns + s];
+                xsum += (double) u.x + (double) u.y;
+            }
+        }
+    }
+    dsum = warp_sum(dsum);
+    const int ikz = (s / ch.kbin_upp) * bins.nk + s % ch.kbin_upp;
+    if (!want_x) {
+        if (lane == 0) d[ikz] = dsum;
+        return;
+    }
+    xsum = warp_sum(xsum);
+    // (F theta)_s from F as k_finish wrote it (upper triangle), else from the Gram partials
+    double ft = 0;
+    if (a.theta)
+        for (int s2 = lane; s2 < ns; s2 += 32) {
+            const int jkz = (s2 / ch.kbin_upp) * bins.nk + s2 % ch.kbin_upp;
+            const double th = a.theta[ch.fis + jkz];
+            if (th == 0.0) continue;
+            const int lo = min(ikz, jkz), hi = max(ikz, jkz);
+            ft += th * (a.skip_fisher ? gram_mixed(a, ch, c, min(s, s2), max(s, s2)) : F[(size_t) lo * nq + hi]);
+        }
+    ft = warp_sum(ft);
+    if (lane != 0) return;
+    d[ikz] = dsum;
+    const double e = dsum - xsum + ft, bt = dsum - e;
+    if (a.turn_off_sfid) b[ikz] = bt;
+    else if (fabs(b[ikz]) >= fabs(t[ikz])) b[ikz] = bt - t[ikz];
+    else t[ikz] = bt - b[ikz];
 }
 
 }  // namespace
@@ -821,6 +870,10 @@ void launch_products_fp64(WaveArgs &a, cudaStream_t st, const int *d_jobs, int n
 void launch_finish(WaveArgs &a, cudaStream_t st) {
     k_finish<<<a.n_chunks, 256, 0, st>>>(a, a.precision == LQG_PRECISION_MIXED);
     a.launches++;
+    if (a.precision == LQG_PRECISION_MIXED && a.max_ns > 0) {
+        k_finish_dx<<<dim3((a.max_ns + 7) / 8, a.n_chunks), 256, 0, st>>>(a);
+        a.launches++;
+    }
 }
 
 }  // namespace lqg

@@ -207,6 +207,97 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) 
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// ---- CTA pairs (cta_group::2): a cluster of two CTAs on one TPC ------------
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Address in the cluster's shared window of this CTA's variable p in CTA rank.
+__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t caddr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
+}
+
+// TMA load into this CTA's shared memory that completes on the mbarrier at
+// cluster address bar_cl, in this CTA or the other CTA of the pair.
+__device__ __forceinline__ void tma_load_3d_pair(void *dst, const CUtensorMap *map, uint32_t bar_cl, int x, int y,
+                                                 int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+        "%4, %5}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cl), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+
+__device__ __forceinline__ void st_cluster_u32(uint32_t caddr, uint32_t v) {
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(caddr), "r"(v) : "memory");
+}
+
+// mbar_wait for barriers that the other CTA of the pair (or its MMAs) arrive on.
+__device__ __forceinline__ bool mbar_wait_cl(uint64_t *bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
+    uint64_t t0 = 0;
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        uint64_t t = now_ns();
+        if (t0 == 0) t0 = t;
+        else if (t - t0 > limit_ns) return false;
+    }
+}
+
+// One MMA of the pair, issued by the even CTA: D (128 lanes of each CTA's
+// tensor memory) += A (128 rows from each CTA) B^T (N / 2 rows from each CTA),
+// all at the same shared-memory and tensor-memory offsets in both CTAs.
+__device__ __forceinline__ void umma_f16_pair(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                              uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// Arrive on the barrier at this offset in both CTAs once the pair's MMAs so far complete.
+__device__ __forceinline__ void umma_commit_pair(uint64_t *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"((unsigned short) 3)
+        : "memory");
+}
+
+// Tensor memory of a pair: the same columns in both CTAs, allocated and freed
+// by one warp of each.
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t *dst, uint32_t ncols) {
+    __syncwarp();
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+}
+
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
 __device__ __forceinline__ double pow2_floor(double x) {
     if (!(x > 0) || !isfinite(x)) return 1.0;
     int e;
@@ -394,6 +485,120 @@ __device__ __forceinline__ int tile_drain(const WaveArgs &a, const GemmTile &tl)
     return (STAGE != 0 && tl.s >= a.chunks[tl.c].ns) ? kGemmDrainST : (a.gemm_drain > 0 ? a.gemm_drain : kGemmDrain);
 }
 
+// Epilogue of one products tile (epilogue warp quad, columns col0 .. col0 + 63):
+// the drained hi*hi sums plus the cross terms at tcross, scaled to fp16 hi/lo
+// planes.  Stage 0: A_s row-major to R and transposed to P; stage 1: X_s to R;
+// stage 2: B_s weighted into its compact upper tile of P.  A tile with live =
+// false (the padding half of a CTA pair) reads TMEM but writes nothing.
+template <int STAGE>
+__device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl, bool live, uint32_t tcross,
+                                           uint32_t lane_addr, int quad, int lane, int col0, const float (&sum)[64]) {
+    const int ld = a.max_ld;
+    const size_t plane = (size_t) ld * ld;
+    const int nq4 = 4 * a.n_chunks;
+    const ChunkDesc &ch = a.chunks[tl.c];
+    if (STAGE == 2) {
+        // B_s = (R scale X_s)(C scale W)^T: to the P scale, weighted, compact upper tile
+        const int s = tl.s;
+        const double rs = a.scales[nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r + s];
+        const double bs = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
+        const float mult = (float) (bs / (rs * a.scales[4 * tl.c + 2]));
+        const int rt = quad * 32 + lane;   // row within the tile
+        const size_t tbase = (size_t) (ch.slot_p + s) * a.p_plane + (size_t) tl.tu * (G_BM * G_BN) +
+                             (size_t) rt * G_BN;
+        const bool ok = live && LQG_IN_BOUNDS(a, ch.slot_p + s < a.total_slots_p &&
+                                             (size_t) tl.tu * (G_BM * G_BN) + G_BM * G_BN <= a.p_plane,
+                                      2, tl.c, s);
+        const float sqrt2 = 1.41421356237309515f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int cb = col0 + h * 32;   // column within the tile
+            float xv[32];
+            tmem_ld32(tcross + lane_addr + cb, xv);
+            if (!ok) continue;
+            uint32_t hp[16], lp[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                float v[2];
+#pragma unroll
+                for (int e2 = 0; e2 < 2; ++e2) {
+                    const int cc = cb + 2 * j + e2;
+                    float wgt = sqrt2;
+                    if (tl.m0 == tl.n0) wgt = cc > rt ? sqrt2 : (cc == rt ? 1.f : 0.f);
+                    v[e2] = (sum[h * 32 + 2 * j + e2] + xv[2 * j + e2]) * mult * wgt;
+                }
+                const __half2 hv = __floats2half2_rn(v[0], v[1]);
+                const float2 hf = __half22float2(hv);
+                const __half2 lv = __floats2half2_rn(v[0] - hf.x, v[1] - hf.y);
+                hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
+                lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
+            }
+            uint4 *dh = reinterpret_cast<uint4 *>(a.p_hi + tbase + cb);
+            uint4 *dl = reinterpret_cast<uint4 *>(a.p_lo + tbase + cb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+                dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
+            }
+        }
+        return;
+    }
+    const int row = tl.m0 + quad * 32 + lane;
+    const int s = tl.s;
+    const double sc = a.scales[4 * tl.c + 2];
+    const double qs = a.scales[nq4 + ch.slot_q + s];
+    // R scale (equal to the P scale of the same slot for s < ns)
+    const double ps = a.scales[nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r + s];
+    const float mult = (float) (ps / (sc * qs));
+    __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
+    __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
+    // A_s (s < ns) goes to R and, transposed, to P; C^-1 S (s = ns) to R only
+    // (stage 1: every X_s to R only)
+    const bool write_p = STAGE == 0 && s < ch.ns;
+    const bool slots_ok = live && LQG_IN_BOUNDS(a, ch.slot_r + s < a.total_slots_r &&
+                                             (!write_p || ch.slot_p + s < a.total_slots_p), 2, tl.c, s);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int cb = tl.n0 + col0 + h * 32;
+        float xv[32];
+        tmem_ld32(tcross + lane_addr + col0 + h * 32, xv);
+        // warp-uniform: ld is a multiple of 64, so a warp's 32 rows are all
+        // inside the matrix or all padding
+        if (!slots_ok || cb >= ld || tl.m0 + quad * 32 >= ld) continue;
+        // hi/lo pairs packed in registers (two halves per 32-bit word)
+        uint32_t hp[16], lp[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float v0 = (sum[h * 32 + 2 * j] + xv[2 * j]) * mult;
+            const float v1 = (sum[h * 32 + 2 * j + 1] + xv[2 * j + 1]) * mult;
+            const __half2 hv = __floats2half2_rn(v0, v1);
+            const float2 hf = __half22float2(hv);
+            const __half2 lv = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
+            hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
+            lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
+        }
+        {
+            uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
+            uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+                dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
+            }
+        }
+        if (!write_p) continue;
+        unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
+        unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            ph[(size_t) (cb + 2 * j) * ld] = (unsigned short) (hp[j] & 0xffffu);
+            ph[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (hp[j] >> 16);
+            pl[(size_t) (cb + 2 * j) * ld] = (unsigned short) (lp[j] & 0xffffu);
+            pl[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (lp[j] >> 16);
+        }
+    }
+}
+
 template <int STAGE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap mc_hi,
@@ -491,12 +696,9 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
         // row-major (R) and transposed (P)
         const int quad = warp % 4, col0 = 64 * ((warp - 2) / 4);
         const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
-        const size_t plane = (size_t) ld * ld;
-        const int nq4 = 4 * a.n_chunks;
         int g_all = 0, lt = 0;
         for (long long t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
             const GemmTile tl = gemm_tile<STAGE>(jobs, t, mt);
-            const ChunkDesc &ch = a.chunks[tl.c];
             float sum[64];
 #pragma unroll
             for (int j = 0; j < 64; ++j) sum[j] = 0.f;
@@ -506,109 +708,7 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1, lim)) && !*abort_flag;
             if (!got) break;
             fence_after();
-            if (STAGE == 2) {
-                // B_s = (R scale X_s)(C scale W)^T: to the P scale, weighted, compact upper tile
-                const int s = tl.s;
-                const double rs = a.scales[nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r + s];
-                const double bs = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
-                const float mult = (float) (bs / (rs * a.scales[4 * tl.c + 2]));
-                const int rt = quad * 32 + lane;   // row within the tile
-                const size_t tbase = (size_t) (ch.slot_p + s) * a.p_plane + (size_t) tl.tu * (G_BM * G_BN) +
-                                     (size_t) rt * G_BN;
-                const bool ok = LQG_IN_BOUNDS(a, ch.slot_p + s < a.total_slots_p &&
-                                                     (size_t) tl.tu * (G_BM * G_BN) + G_BM * G_BN <= a.p_plane,
-                                              2, tl.c, s);
-                const float sqrt2 = 1.41421356237309515f;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int cb = col0 + h * 32;   // column within the tile
-                    float xv[32];
-                    tmem_ld32(tmem + lane_addr + 2 * G_BN + x * G_BN + cb, xv);
-                    if (!ok) continue;
-                    uint32_t hp[16], lp[16];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        float v[2];
-#pragma unroll
-                        for (int e2 = 0; e2 < 2; ++e2) {
-                            const int cc = cb + 2 * j + e2;
-                            float wgt = sqrt2;
-                            if (tl.m0 == tl.n0) wgt = cc > rt ? sqrt2 : (cc == rt ? 1.f : 0.f);
-                            v[e2] = (sum[h * 32 + 2 * j + e2] + xv[2 * j + e2]) * mult * wgt;
-                        }
-                        const __half2 hv = __floats2half2_rn(v[0], v[1]);
-                        const float2 hf = __half22float2(hv);
-                        const __half2 lv = __floats2half2_rn(v[0] - hf.x, v[1] - hf.y);
-                        hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
-                        lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
-                    }
-                    uint4 *dh = reinterpret_cast<uint4 *>(a.p_hi + tbase + cb);
-                    uint4 *dl = reinterpret_cast<uint4 *>(a.p_lo + tbase + cb);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
-                        dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
-                    }
-                }
-                fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&xempty[x]);
-                continue;
-            }
-            const int row = tl.m0 + quad * 32 + lane;
-            const int s = tl.s;
-            const double sc = a.scales[4 * tl.c + 2];
-            const double qs = a.scales[nq4 + ch.slot_q + s];
-            // R scale (equal to the P scale of the same slot for s < ns)
-            const double ps = a.scales[nq4 + a.total_slots_q + a.total_slots_p + ch.slot_r + s];
-            const float mult = (float) (ps / (sc * qs));
-            __half *Rh = a.r_hi + (size_t) (ch.slot_r + s) * plane, *Rl = a.r_lo + (size_t) (ch.slot_r + s) * plane;
-            __half *Ph = a.p_hi + (size_t) (ch.slot_p + s) * plane, *Pl = a.p_lo + (size_t) (ch.slot_p + s) * plane;
-            // A_s (s < ns) goes to R and, transposed, to P; C^-1 S (s = ns) to R only
-            // (stage 1: every X_s to R only)
-            const bool write_p = STAGE == 0 && s < ch.ns;
-            const bool slots_ok = LQG_IN_BOUNDS(a, ch.slot_r + s < a.total_slots_r &&
-                                                     (!write_p || ch.slot_p + s < a.total_slots_p), 2, tl.c, s);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int cb = tl.n0 + col0 + h * 32;
-                float xv[32];
-                tmem_ld32(tmem + lane_addr + 2 * G_BN + x * G_BN + col0 + h * 32, xv);
-                // warp-uniform: ld is a multiple of 64, so a warp's 32 rows are all
-                // inside the matrix or all padding
-                if (!slots_ok || cb >= ld || tl.m0 + quad * 32 >= ld) continue;
-                // hi/lo pairs packed in registers (two halves per 32-bit word)
-                uint32_t hp[16], lp[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const float v0 = (sum[h * 32 + 2 * j] + xv[2 * j]) * mult;
-                    const float v1 = (sum[h * 32 + 2 * j + 1] + xv[2 * j + 1]) * mult;
-                    const __half2 hv = __floats2half2_rn(v0, v1);
-                    const float2 hf = __half22float2(hv);
-                    const __half2 lv = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
-                    hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
-                    lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
-                }
-                {
-                    uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
-                    uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
-                        dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
-                    }
-                }
-                if (!write_p) continue;
-                unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
-                unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    ph[(size_t) (cb + 2 * j) * ld] = (unsigned short) (hp[j] & 0xffffu);
-                    ph[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (hp[j] >> 16);
-                    pl[(size_t) (cb + 2 * j) * ld] = (unsigned short) (lp[j] & 0xffffu);
-                    pl[(size_t) (cb + 2 * j + 1) * ld] = (unsigned short) (lp[j] >> 16);
-                }
-            }
+            store_tile<STAGE>(a, tl, true, tmem + 2 * G_BN + x * G_BN, lane_addr, quad, lane, col0, sum);
             // this cross buffer may now be taken by tile lt + 2
             fence_before();
             __syncwarp();
@@ -624,6 +724,278 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     if (threadIdx.x == 0 && *abort_flag)
         for (long long t = blockIdx.x; t < total; t += gridDim.x)
             atomicExch(&a.status[a.chunks[gemm_tile<STAGE>(jobs, t, mt).c].gidx], LQG_CHUNK_TIMEOUT);
+}
+
+// ---------------------------------------------------------------------------
+// The same three products on CTA pairs (a cluster of two CTAs on one TPC,
+// tcgen05 cta_group::2): one MMA of M = 256, N = 128, K = 16 per instruction,
+// each CTA holding 128 rows of A and 64 of the 128 rows of B.  Per SM and MMA
+// the shared memory then serves 6 KB of operands instead of 8 KB, and the TMA
+// writes 48 KB instead of 64 KB per K block: the single-CTA kernel is bound
+// by that bandwidth (operand reads plus TMA writes) at ~60 % tensor-pipe
+// activity, the pair kernel at ~80 %.
+//
+// Pairing: stages 0 and 1 take row blocks 2P and 2P + 1 of the same output
+// column block (an odd row-block count leaves the last pair's second half as
+// padding: rows past ld read as zeros and are not written); stage 2 takes
+// slots s0 and s0 + 1 (jobs list even s0 only) of the same upper tile, the
+// second half padding when s0 + 1 > ns + 1.  Each CTA's tensor memory holds
+// its own 128 rows in the single-CTA kernel's layout, so the drains and the
+// epilogue are the same code.
+//
+// Roles: warp 0 of each CTA loads its own operands, both CTAs' copies
+// completing on the even CTA's full barrier (which expects both halves);
+// warp 1 of the even CTA issues every MMA of the pair and commits to both
+// CTAs' barriers (empty stages, drains, cross buffers); the epilogue warps of
+// both arrive on the even CTA's dempty/xempty (16 arrivals).  Before leaving,
+// the even CTA waits for its last stages to land and the odd CTA for its last
+// stages to be consumed (the MMAs read them after they landed), both bounded;
+// then both pass a cluster barrier after the even CTA's MMAs have completed.
+constexpr int P_STAGES = 4;
+constexpr int P_TILE_A = 128 * BK * 2;                       // this CTA's 128 rows of A
+constexpr int P_TILE_B = 64 * BK * 2;                        // its 64 rows of B
+constexpr int P_STAGE_BYTES = 2 * P_TILE_A + 2 * P_TILE_B;   // 48 KB
+constexpr int P_SMEM = P_STAGES * P_STAGE_BYTES + 1024 + 256;
+
+struct PairTile {
+    GemmTile tl;   // this CTA's tile
+    bool live;     // false: the padding half of the pair
+    int kbt;       // K blocks of the pair
+    int drain;     // hi*hi drain interval of the pair
+};
+
+template <int STAGE>
+__device__ __forceinline__ PairTile pair_tile(const WaveArgs &a, const int *jobs, long long t, int mt, int kblocks,
+                                              int rank) {
+    PairTile p;
+    const int defdrain = a.gemm_drain > 0 ? a.gemm_drain : kGemmDrain;
+    if (STAGE != 2) {
+        const int mh = (mt + 1) / 2;
+        const long long tpj = (long long) mh * mt;
+        const int job = (int) (t / tpj), tix = (int) (t % tpj);
+        const int P = tix % mh, J = tix / mh;
+        p.tl = GemmTile{jobs[2 * job], jobs[2 * job + 1], (2 * P + rank) * G_BM, J * G_BN, 0};
+        p.live = p.tl.m0 < a.max_ld;
+        // stage 1 with a triangular W: the K range of the pair's lower row block
+        p.kbt = (STAGE == 1 && a.w_tri) ? min(kblocks, ((2 * P + 1) * G_BM + G_BM) / BK) : kblocks;
+        p.drain = (STAGE == 1 && p.tl.s >= a.chunks[p.tl.c].ns) ? kGemmDrainST : defdrain;
+        return p;
+    }
+    const long long tpj = (long long) mt * (mt + 1) / 2;
+    const int job = (int) (t / tpj), tix = (int) (t % tpj);
+    int I = 0, r = tix;
+    while (r >= mt - I) { r -= mt - I; ++I; }
+    const int c = jobs[2 * job], s0 = jobs[2 * job + 1];
+    const int ns = a.chunks[c].ns;
+    const int s = s0 + rank;
+    p.live = s <= ns + 1;
+    p.tl = GemmTile{c, p.live ? s : s0, I * G_BM, (I + r) * G_BN, tix};
+    p.kbt = a.w_tri ? min(kblocks, (p.tl.n0 + G_BM) / BK) : kblocks;
+    // the S and N slots drain more often; a pair holding one drains at its interval
+    p.drain = s0 + 1 >= ns ? kGemmDrainST : defdrain;
+    return p;
+}
+
+// Epilogue drains of one tile, as drain_tile<false>, arriving on the even CTA's dempty.
+__device__ __forceinline__ bool drain_tile_pair(uint32_t tmem, uint32_t lane_addr, int col0, uint64_t *dfull,
+                                                uint32_t dempty_cl, int kblocks, int DRAIN, float (&sum)[64],
+                                                int &g_all, const volatile int *abort_flag, uint64_t lim) {
+    const int ngroups = (kblocks + DRAIN - 1) / DRAIN;
+    bool alive = true;
+    for (int g = 0; g < ngroups; ++g) {
+        const int b = g_all & 1;
+        alive = __all_sync(0xffffffffu, alive && mbar_wait(&dfull[b], (g_all >> 1) & 1, lim)) && !*abort_flag;
+        if (!alive) break;
+        fence_after();
+        float v[64];
+        tmem_ld64(tmem + lane_addr + b * 128 + col0, v);
+#pragma unroll
+        for (int j = 0; j < 64; ++j) sum[j] += v[j];
+        fence_before();
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) mbar_arrive_cluster(dempty_cl + 8 * b);
+        ++g_all;
+    }
+    return alive;
+}
+
+template <int STAGE>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, 1)
+k_tc_gemm_pair(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtensorMap ma_hi,
+               const __grid_constant__ CUtensorMap ma_lo, const __grid_constant__ CUtensorMap mb_hi,
+               const __grid_constant__ CUtensorMap mb_lo) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // the same offset in both CTAs: the MMAs address both with one descriptor
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + P_STAGES * P_STAGE_BYTES);   // even CTA: both halves
+    uint64_t *empty = full + P_STAGES;
+    uint64_t *dfull = empty + P_STAGES;
+    uint64_t *dempty = dfull + 2;
+    uint64_t *xfull = dempty + 2;
+    uint64_t *xempty = xfull + 2;
+    uint64_t *mdone = xempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mdone + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int rank = (int) cluster_rank();
+    const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+    const int ld = a.max_ld;
+    const int mt = (ld + G_BM - 1) / G_BM, mh = (mt + 1) / 2;
+    const long long total = (long long) njobs * (STAGE == 2 ? (long long) mt * (mt + 1) / 2 : (long long) mh * mt);
+    const int kblocks = ld / BK;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint64_t lim = a.wait_ns ? a.wait_ns : kWaitLimitNs;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < P_STAGES; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&dfull[i], 1);
+            mbar_init(&dempty[i], 16);
+            mbar_init(&xfull[i], 1);
+            mbar_init(&xempty[i], 16);
+        }
+        mbar_init(mdone, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) tmem_alloc_pair(tmem_slot, 512);
+    fence_before();
+    __syncthreads();
+    cluster_sync();   // both CTAs' barriers exist before either arrives on the other's
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t full_cl = cluster_addr(full, 0), dempty_cl = cluster_addr(dempty, 0),
+                   xempty_cl = cluster_addr(xempty, 0);
+    const uint32_t peer_abort = cluster_addr((const void *) abort_flag, rank ^ 1);
+    auto set_abort = [&]() {
+        *abort_flag = 1;
+        st_cluster_u32(peer_abort, 1);
+    };
+
+    if (warp == 0 && lane == 0) {
+        // TMA producer of this CTA's operands
+        int kb_all = 0;
+        for (long long t = cid; t < total && !*abort_flag; t += ncl) {
+            const PairTile p = pair_tile<STAGE>(a, jobs, t, mt, kblocks, rank);
+            const GemmTile &tl = p.tl;
+            const int aidx = STAGE == 2 ? a.chunks[tl.c].slot_r + tl.s : tl.c;
+            const int bidx = STAGE == 2 ? tl.c : a.chunks[tl.c].slot_q + tl.s;
+            const bool idx_ok = STAGE == 2 ? (aidx >= 0 && aidx < a.total_slots_r)
+                                           : (bidx >= 0 && bidx < a.total_slots_q);
+            if (!LQG_IN_BOUNDS(a, tl.c >= 0 && tl.c < a.n_chunks && idx_ok && tl.n0 < ld &&
+                                      a.chunks[tl.c].ld == ld,
+                               1, tl.c, STAGE == 2 ? aidx : bidx)) {
+                set_abort();
+                break;
+            }
+            for (int kb = 0; kb < p.kbt; ++kb) {
+                const int st = kb_all % P_STAGES;
+                if (!mbar_wait(&empty[st], ((kb_all / P_STAGES) & 1) ^ 1, lim)) { set_abort(); break; }
+                unsigned char *sb = smem + st * P_STAGE_BYTES;
+                // the even CTA's barrier expects both CTAs' bytes of the stage
+                if (rank == 0) mbar_expect_tx(&full[st], 2 * P_STAGE_BYTES);
+                const uint32_t bar = full_cl + 8 * st;
+                tma_load_3d_pair(sb, &ma_hi, bar, kb * BK, tl.m0, aidx);
+                tma_load_3d_pair(sb + P_TILE_A, &ma_lo, bar, kb * BK, tl.m0, aidx);
+                tma_load_3d_pair(sb + 2 * P_TILE_A, &mb_hi, bar, kb * BK, tl.n0 + 64 * rank, bidx);
+                tma_load_3d_pair(sb + 2 * P_TILE_A + P_TILE_B, &mb_lo, bar, kb * BK, tl.n0 + 64 * rank, bidx);
+                ++kb_all;
+            }
+        }
+        // this CTA's copies land before it leaves: the even CTA waits for its
+        // last stages to complete, the odd CTA for them to be consumed.  After
+        // an abort these phases may never complete (a stage the other CTA did
+        // not load, MMAs not issued); the copies themselves land within
+        // microseconds, so the wait is cut to 10 ms then.
+        for (int k = (kb_all > P_STAGES ? kb_all - P_STAGES : 0); k < kb_all; ++k) {
+            const uint64_t tail = *abort_flag ? 10000000ull : kWaitLimitNs;
+            if (rank == 0) mbar_wait(&full[k % P_STAGES], (k / P_STAGES) & 1, tail);
+            else mbar_wait(&empty[k % P_STAGES], (k / P_STAGES) & 1, tail);
+        }
+    } else if (warp == 1 && lane == 0 && rank == 0) {
+        // MMA issuer of the pair
+        const uint32_t idesc = idesc_f16(2 * G_BM, G_BN);
+        int kb_all = 0, g_all = 0, lt = 0;
+        bool ok = true;
+        for (long long t = cid; t < total && ok && !*abort_flag; t += ncl, ++lt) {
+            const int x = lt & 1;
+            if (lt >= 2 && !mbar_wait_cl(&xempty[x], ((lt >> 1) - 1) & 1, lim)) { ok = false; break; }
+            fence_after();
+            const PairTile p = pair_tile<STAGE>(a, jobs, t, mt, kblocks, rank);
+            const uint32_t tx = tmem + 2 * G_BN + x * G_BN;
+            const int ngroups = (p.kbt + p.drain - 1) / p.drain;
+            for (int g = 0; g < ngroups && ok; ++g) {
+                const int b = g_all & 1;
+                if (g_all >= 2 && !mbar_wait_cl(&dempty[b], ((g_all >> 1) - 1) & 1, lim)) { ok = false; break; }
+                fence_after();
+                const uint32_t th = tmem + b * G_BN;
+                const int kb_end = min(p.kbt, (g + 1) * p.drain);
+                for (int kb = g * p.drain; kb < kb_end; ++kb) {
+                    const int st = kb_all % P_STAGES;
+                    const uint32_t par = (kb_all / P_STAGES) & 1;
+                    if (!mbar_wait(&full[st], par, lim)) { ok = false; break; }
+                    fence_after();
+                    unsigned char *sb = smem + st * P_STAGE_BYTES;
+                    const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + P_TILE_A);
+                    const uint64_t bh = sw128_desc(sb + 2 * P_TILE_A), bl = sw128_desc(sb + 2 * P_TILE_A + P_TILE_B);
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        const uint64_t adv = (uint64_t) (kk * 32) >> 4;
+                        umma_f16_pair(th, ah + adv, bh + adv, idesc, (kb > g * p.drain || kk > 0));
+                        umma_f16_pair(tx, ah + adv, bl + adv, idesc, (kb | kk) != 0);
+                        umma_f16_pair(tx, al + adv, bh + adv, idesc, 1);
+                    }
+                    umma_commit_pair(&empty[st]);
+                    ++kb_all;
+                }
+                if (!ok) break;
+                umma_commit_pair(&dfull[b]);
+                ++g_all;
+            }
+            if (!ok) break;
+            umma_commit_pair(&xfull[x]);
+        }
+        if (!ok) set_abort();
+        // every MMA of the pair completes before either CTA frees its tensor memory
+        umma_commit_pair(mdone);
+        mbar_wait_cl(mdone, 0);
+    } else if (warp >= 2) {
+        // epilogue of this CTA's 128 rows
+        const int quad = warp % 4, col0 = 64 * ((warp - 2) / 4);
+        const uint32_t lane_addr = (uint32_t) (quad * 32) << 16;
+        int g_all = 0, lt = 0;
+        for (long long t = cid; t < total; t += ncl, ++lt) {
+            const PairTile p = pair_tile<STAGE>(a, jobs, t, mt, kblocks, rank);
+            float sum[64];
+#pragma unroll
+            for (int j = 0; j < 64; ++j) sum[j] = 0.f;
+            bool got = drain_tile_pair(tmem, lane_addr, col0, dfull, dempty_cl, p.kbt, p.drain, sum, g_all,
+                                       abort_flag, lim);
+            const int x = lt & 1;
+            got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1, lim)) && !*abort_flag;
+            if (!got) break;
+            fence_after();
+            store_tile<STAGE>(a, p.tl, p.live, tmem + 2 * G_BN + x * G_BN, lane_addr, quad, lane, col0, sum);
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(xempty_cl + 8 * x);
+        }
+    }
+    fence_before();
+    __syncthreads();
+    cluster_sync();   // the pair's MMAs are complete (even CTA) and neither CTA has copies in flight
+    if (warp == 1) {
+        fence_after();
+        tmem_dealloc_pair(tmem, 512);
+    }
+    if (threadIdx.x == 0 && *abort_flag)
+        for (long long t = cid; t < total; t += ncl)
+            atomicExch(&a.status[a.chunks[pair_tile<STAGE>(a, jobs, t, mt, kblocks, rank).tl.c].gidx],
+                       LQG_CHUNK_TIMEOUT);
 }
 
 // ---------------------------------------------------------------------------
@@ -834,15 +1206,35 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
                            int njobs2) {
     // shared memory above the 48 KB default, and the SM count: once per device
     static std::atomic<unsigned long long> attr{0};
-    static int n_sm_dev[64];
+    static int n_sm_dev[64], n_pair_dev[64];
     const bool ready = once_per_device(attr, [](int dev) {
         cudaError_t e = cudaFuncSetAttribute(k_tc_gemm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, R_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_gemm_pair<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_gemm_pair<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_tc_gemm_pair<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM);
         int sms = 0;
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess && dev >= 0 && dev < 64) n_sm_dev[dev] = sms > 0 ? sms : 1;
+        // CTA pairs resident at once (the persistent pair kernels' grid): the
+        // cluster placement need not reach every TPC
+        int pairs = 0;
+        if (e == cudaSuccess) {
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(2 * std::max(sms / 2, 1));
+            cfg.blockDim = dim3(TC_THREADS);
+            cfg.dynamicSmemBytes = P_SMEM;
+            if (cudaOccupancyMaxActiveClusters(&pairs, k_tc_gemm_pair<1>, &cfg) != cudaSuccess || pairs <= 0) {
+                cudaGetLastError();
+                pairs = std::max(sms / 2, 1);
+            }
+        }
+        if (e == cudaSuccess && dev >= 0 && dev < 64) n_pair_dev[dev] = pairs;
         return e;
     });
     if (!ready) {
@@ -854,6 +1246,7 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     int n_sm = (dev >= 0 && dev < 64) ? n_sm_dev[dev] : 0;
     if (n_sm <= 0 && (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n_sm <= 0))
         n_sm = 1;
+    const int n_pairs = (dev >= 0 && dev < 64 && n_pair_dev[dev] > 0) ? n_pair_dev[dev] : std::max(n_sm / 2, 1);
     const int ld = a.max_ld;
     const cuuint64_t plane = (cuuint64_t) ld * ld;
     bool ok = true;
@@ -884,6 +1277,17 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
         mwh = make_map(a.c_hi, 3, d3c, s3, boxb, &ok);
         mwl = make_map(a.c_lo, 3, d3c, s3, boxb, &ok);
     }
+    // CTA pairs: each CTA loads 64 of the 128 B rows of a tile
+    CUtensorMap mqh2{}, mql2{}, mwh2{}, mwl2{};
+    if (a.gemm_pair) {
+        cuuint32_t boxh[3] = {BK, 64, 1};
+        mqh2 = make_map(a.q_hi, 3, d3q, s3, boxh, &ok);
+        mql2 = make_map(a.q_lo, 3, d3q, s3, boxh, &ok);
+        if (a.sym) {
+            mwh2 = make_map(a.c_hi, 3, d3c, s3, boxh, &ok);
+            mwl2 = make_map(a.c_lo, 3, d3c, s3, boxh, &ok);
+        }
+    }
     if (!ok) {
         // nothing launched: the caller turns this into an error return
         a.host_failed = 1;
@@ -891,6 +1295,25 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     }
     // persistent: one CTA per SM (one fits: 197 KB of shared memory)
     const long long mt = (ld + G_BM - 1) / G_BM;
+    if (a.gemm_pair) {
+        // one cluster of two CTAs per TPC
+        const long long mh = (mt + 1) / 2, pairs_max = n_pairs;
+        const long long p1 = mh * mt * njobs;
+        const int grid = 2 * (int) std::min<long long>(p1, pairs_max);
+        if (!a.sym) {
+            k_tc_gemm_pair<0><<<grid, TC_THREADS, P_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh2, mql2);
+        } else {
+            k_tc_gemm_pair<1><<<grid, TC_THREADS, P_SMEM, st>>>(a, d_jobs, njobs, mch, mcl, mqh2, mql2);
+            const long long p2 = mt * (mt + 1) / 2 * njobs2;
+            const int grid2 = 2 * (int) std::min<long long>(p2, pairs_max);
+            k_tc_gemm_pair<2><<<grid2, TC_THREADS, P_SMEM, st>>>(a, d_jobs2, njobs2, mxh, mxl, mwh2, mwl2);
+            a.launches++;
+        }
+        if (a.mid_event) record_event(a.mid_event, st);
+        k_tc_gram<<<dim3(a.gram_splits, a.n_chunks, a.gt * a.gt), R_THREADS, R_SMEM, st>>>(a, mph, mpl, mrh, mrl);
+        a.launches += 2;
+        return;
+    }
     const long long tiles = mt * mt * njobs;
     const int grid = (int) std::min<long long>(tiles, n_sm);
     if (!a.sym) {

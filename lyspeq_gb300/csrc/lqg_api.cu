@@ -31,7 +31,7 @@ struct lqg_ctx {
     // LQG_PRECISION_MIXED_AUTO: per padded size ld, the mixed form, the drain
     // interval of the products and the Gram's K split (lqg_autotune)
     struct Tune {
-        int sym = 1, drain = 8, gram_k = 32768;
+        int sym = 1, drain = 8, gram_k = 32768, pair = 0;
     };
     std::map<int, Tune> tuning;
     // batch
@@ -580,7 +580,7 @@ int64_t chunk_fws_bytes(int64_t ld, bool cinv_m) {
     return align_up(ld * ld * 8, 256) * (cinv_m ? 3 : 2) + align_up(ld * 8, 256) + align_up(64 * ld * 8, 256);
 }
 
-// Mixed path: d - b - t from the x partials (k_finish).  It rests on C = S + N +
+// Mixed path: d - b - t from the x partials (k_finish_dx).  It rests on C = S + N +
 // sum theta Q with the N of b, which smoothed noise weights break (C takes the
 // smoothed ivar, N the raw one); the Gram's b and t stand alone then.
 bool dbt_identity(const lqg_ctx *ctx, int precision) {
@@ -608,6 +608,8 @@ struct WavePlan {
     std::vector<int> members;   // batch chunk indices
     int ld = 0, gt = 1, splits = 1;
     int sym = 0, drain = 8;     // mixed form and products drain interval (one per ld)
+    int pair = 0;               // products on CTA pairs
+    int max_ns = 0;             // largest stored-slot count
     int slot_q = 0, slot_r = 0, slot_p = 0;
     int64_t ws_bytes = 0, half_bytes = 0;
     size_t desc_off = 0, jobs_off = 0, scales_off = 0, jobs2_off = 0;
@@ -736,6 +738,7 @@ int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan>
                 g.waves.back().splits = splits;
                 g.waves.back().sym = sym ? 1 : 0;
                 g.waves.back().drain = tn.drain;
+                g.waves.back().pair = precision == LQG_PRECISION_MIXED ? tn.pair : 0;
             }
             WavePlan &w = g.waves.back();
             w.members.push_back((int) k);   // index within the group
@@ -766,6 +769,7 @@ int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan>
                     d.o_p = off; off += align_up(m * (d.ns + 2), 256);
                 }
                 d.slot_q = w.slot_q; w.slot_q += d.ns + 1;
+                w.max_ns = std::max(w.max_ns, d.ns);
                 // trace-Gram operand stacks.  FP64: P = [A_s^T, (C^-1 S)^T, N C^-1],
                 // R = [A_s].  Mixed: P = [A_s^T], R = [A_s, C^-1 S, C^-1 N].  Whitened
                 // form: R = [X_s, W S, W N], P = [B_s, W S W^T, W N W^T] (compact).
@@ -790,11 +794,15 @@ int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan>
             for (int i = 0; i < nch; ++i)
                 for (int s = 0; s <= desc[w.desc_off + i].ns; ++s) { jobs.push_back(i); jobs.push_back(s); }
             w.njobs = (int) (jobs.size() - w.jobs_off) / 2;
-            // whitened form, second product: B_s for s <= ns + 1
+            // whitened form, second product: B_s for s <= ns + 1 (CTA pairs: slots
+            // s and s + 1 from one job of even s)
             w.jobs2_off = jobs.size();
             if (sym)
                 for (int i = 0; i < nch; ++i)
-                    for (int s = 0; s <= desc[w.desc_off + i].ns + 1; ++s) { jobs.push_back(i); jobs.push_back(s); }
+                    for (int s = 0; s <= desc[w.desc_off + i].ns + 1; s += w.pair ? 2 : 1) {
+                        jobs.push_back(i);
+                        jobs.push_back(s);
+                    }
             w.njobs2 = (int) (jobs.size() - w.jobs2_off) / 2;
             w.scales_off = scales.size();
             w.nscales = 4 * nch + w.slot_q + w.slot_p + w.slot_r;
@@ -1062,6 +1070,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
                 b.chunks = ctx->d_desc.as<ChunkDesc>() + w.desc_off;
                 b.n_chunks = nch;
                 b.max_ld = w.ld;
+                b.max_ns = w.max_ns;
                 b.gt = w.gt;
                 b.fws_bytes = g.fws_bytes;
                 b.ws_bytes = w.ws_bytes;
@@ -1070,6 +1079,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
                 b.sym = w.sym;
                 b.w_tri = w.sym && no_marg;
                 b.gemm_drain = w.drain;
+                b.gemm_pair = w.pair;
                 b.scales = ctx->d_scales.as<double>() + w.scales_off;
                 if (precision == LQG_PRECISION_MIXED) {
                     __half *hb = ctx->d_halves.as<__half>();
@@ -1144,7 +1154,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
                                    (uintptr_t) w.slot_p, (uintptr_t) w.ws_bytes, (uintptr_t) w.desc_off,
                                    (uintptr_t) w.jobs_off, (uintptr_t) w.scales_off, (uintptr_t) w.jobs2_off,
                                    (uintptr_t) w.njobs, (uintptr_t) w.njobs2, (uintptr_t) w.sym,
-                                   (uintptr_t) w.drain});
+                                   (uintptr_t) w.drain, (uintptr_t) w.pair, (uintptr_t) w.max_ns});
     }
     auto cached = std::find_if(ctx->graphs.begin(), ctx->graphs.end(),
                                [&](const lqg_ctx::GraphEntry &g) { return g.key == key; });
@@ -1419,7 +1429,7 @@ extern "C" int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, in
     if (int rc = finish_pending(ctx)) return rc;
     if (max_rel_err <= 0) max_rel_err = 1e-5;
     if (max_chunks <= 0) max_chunks = 48;
-    if (flags == 0) flags = 7;
+    if (flags == 0) flags = 15;
     // the batch-wide buffers (statuses, metadata, results) are sized by the
     // whole batch before the sample iterations swap in their subsets
     if (int rc = upload_pixels(ctx)) return rc;
@@ -1461,6 +1471,23 @@ extern "C" int lqg_autotune(lqg_ctx *ctx, double max_rel_err, int max_chunks, in
                 if (best_ms < 0 || ms < best_ms) { best_ms = ms; best = t; }
             }
         if (best_ms < 0) best = best_any;
+        if ((flags & 8) && best_ms >= 0) {
+            // the products on CTA pairs: the same arithmetic but for the drain
+            // interval of slot ns - 1 (paired with S), so checked and timed again
+            lqg_ctx::Tune t = best;
+            t.pair = 1;
+            ctx->tuning[ld] = t;
+            rc = iterate_subset(ctx, acc, LQG_PRECISION_MIXED_AUTO, nullptr);
+            if (!rc) rc = read_results(ctx, acc, mix);
+            if (rc) { ctx->tuning = saved; return rc; }
+            if (max_error(ctx, acc, mix, ref) <= 0.8 * max_rel_err) {
+                double ms = 0;
+                rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
+                if (!rc) rc = iterate_subset(ctx, timing, LQG_PRECISION_MIXED_AUTO, &ms);
+                if (rc) { ctx->tuning = saved; return rc; }
+                if (ms < best_ms) best = t;
+            }
+        }
         if (flags & 4) {
             double bms = -1;
             int bk_k = best.gram_k;
@@ -1486,10 +1513,12 @@ extern "C" int lqg_tuning_get(const lqg_ctx *ctx, int *entries, int n) {
     int k = 0;
     for (const auto &e : ctx->tuning) {
         if (entries && k < n) {
-            entries[4 * k] = e.first;
-            entries[4 * k + 1] = e.second.sym;
-            entries[4 * k + 2] = e.second.drain;
-            entries[4 * k + 3] = e.second.gram_k;
+            int *r = entries + LQG_TUNING_FIELDS * k;
+            r[0] = e.first;
+            r[1] = e.second.sym;
+            r[2] = e.second.drain;
+            r[3] = e.second.gram_k;
+            r[4] = e.second.pair;
         }
         ++k;
     }
@@ -1500,13 +1529,16 @@ extern "C" int lqg_tuning_set(lqg_ctx *ctx, const int *entries, int n) {
     if (!ctx || n < 0 || (n > 0 && !entries)) return LQG_ERR_ARG;
     std::map<int, lqg_ctx::Tune> t;
     for (int k = 0; k < n; ++k) {
-        const int ld = entries[4 * k], sym = entries[4 * k + 1], drain = entries[4 * k + 2], gk = entries[4 * k + 3];
-        if (ld <= 0 || ld % kPad || (sym != 0 && sym != 1) || drain < 1 || drain > 64 || gk < 4096 || gk % 64)
+        const int *r = entries + LQG_TUNING_FIELDS * k;
+        const int ld = r[0], sym = r[1], drain = r[2], gk = r[3], pair = r[4];
+        if (ld <= 0 || ld % kPad || (sym != 0 && sym != 1) || drain < 1 || drain > 64 || gk < 4096 || gk % 64 ||
+            (pair != 0 && pair != 1))
             return set_err(ctx, LQG_ERR_ARG, "lqg_tuning_set: bad entry " + std::to_string(k));
         lqg_ctx::Tune e;
         e.sym = sym;
         e.drain = drain;
         e.gram_k = gk;
+        e.pair = pair;
         t[ld] = e;
     }
     ctx->tuning = t;

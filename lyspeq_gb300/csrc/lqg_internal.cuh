@@ -135,6 +135,7 @@ struct WaveArgs {
     const ChunkDesc *chunks;     // device
     int n_chunks;
     int max_ld;
+    int max_ns;                  // largest stored-slot count of the wave
     char *ws;                    // wave workspace base
     char *fws;                   // factor workspace base
     double *fbounds;             // per batch chunk: max |C^-1|, largest row sum of |C^-1|
@@ -151,6 +152,7 @@ struct WaveArgs {
     int dbt_id;                                      // mixed path: d - b - t from the x partials (see k_finish)
     int w_tri;                                       // W lower triangular (no marginalisation)
     int gemm_drain;                                  // K blocks per drained hi*hi partial of the products; 0: 8
+    int gemm_pair;                                   // products on CTA pairs (k_tc_gemm_pair)
     int64_t p_plane;                                 // elements of one P slot
     const double *deriv, *signal, *qmax;             // tables
     const float *deriv_f;                            // float copy of deriv (mixed path)

@@ -16,6 +16,7 @@ LIB_PATH = os.environ.get("LQG_LIB", os.path.join(HERE, "liblqg.so"))
 
 LQG_OK = 0
 PRECISION = {"fp64": 0, "mixed": 1, "mixed_direct": 2, "mixed_auto": 3}
+TUNING_FIELDS = 5   # LQG_TUNING_FIELDS: ld, form, drain, Gram K per split, CTA pairs
 CHUNK_STATUS = {0: "ok", 1: "short", 2: "no_table", 3: "empty", 4: "out_of_range",
                 5: "not_spd", 6: "bad_input", 7: "too_large", 8: "timeout", 9: "index_check"}
 
@@ -276,14 +277,15 @@ class Engine:
         return self.tuning()
 
     def tuning(self):
-        """The autotuner's table: rows (ld, whitened form, drain interval, Gram K per split)."""
+        """The autotuner's table: rows (ld, whitened form, drain interval, Gram K
+        per split, CTA-pair products)."""
         n = self.lib.lqg_tuning_get(self.h, None, 0)
-        buf = np.zeros(4 * max(n, 1), dtype=np.int32)
+        buf = np.zeros(TUNING_FIELDS * max(n, 1), dtype=np.int32)
         self.lib.lqg_tuning_get(self.h, _iptr(buf), n)
-        return buf[:4 * n].reshape(n, 4)
+        return buf[:TUNING_FIELDS * n].reshape(n, TUNING_FIELDS)
 
     def set_tuning(self, table):
-        t = np.ascontiguousarray(np.asarray(table, dtype=np.int32).reshape(-1, 4))
+        t = np.ascontiguousarray(np.asarray(table, dtype=np.int32).reshape(-1, TUNING_FIELDS))
         self._check(self.lib.lqg_tuning_set(self.h, _iptr(t), len(t)), "lqg_tuning_set")
 
     def download(self):

@@ -7,9 +7,12 @@
   LQG_CHUNK_TIMEOUT.  The call returns, those chunks contribute nothing (as
   the reference skips a chunk that throws, core/chunk_estimate.cpp:905-913),
   and the next iteration on the same context is exact again.
+  The same on CTA pairs (k_tc_gemm_pair), where a wait that runs out in one
+  CTA also stops the other.
 * The self-checking build (-DLQG_CHECKED): every device index is checked
   against its buffer, a violation is counted and the access skipped.  The
-  golden cases run through it with no violation and the usual parity.
+  golden cases run through it with no violation and the usual parity, the
+  products on one CTA and on CTA pairs.
 """
 import os
 import subprocess
@@ -32,10 +35,21 @@ def _engine(c):
     return eng
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_direct"])
-def test_waits_that_run_out_drop_their_chunks_and_the_next_iteration_is_exact(engine_lib, precision):
+def _plan(eng, mode):
+    """The precision to iterate with: the fixed modes, or the products on CTA
+    pairs (whitened or direct form) through a tuning table."""
+    if not mode.startswith("pair"):
+        return mode
+    lds = sorted({(eng.chunk_info(i)["n"] + 63) // 64 * 64 for i in range(eng.size)})
+    eng.set_tuning([(ld, 1 if mode == "pair_whitened" else 0, 8, 32768, 1) for ld in lds])
+    return "mixed_auto"
+
+
+@pytest.mark.parametrize("mode", ["mixed", "mixed_direct", "pair_whitened", "pair_direct"])
+def test_waits_that_run_out_drop_their_chunks_and_the_next_iteration_is_exact(engine_lib, mode):
     c = G.load("tiny_marg1")
     eng = _engine(c)
+    precision = _plan(eng, mode)
     eng.set_wait_limit(1e-9)
     eng.iterate(precision=precision)
     out = eng.download()
@@ -75,7 +89,8 @@ for name in ["tiny_marg1", "tiny_masked", "tiny_marg3", "tiny_nosfid", "tiny_res
     # tiny_marg3's templates are nearly collinear: the reference itself is
     # determined to ~1e-8 there, and the mixed forms are not held to 1e-5 on it
     # (tests/test_gpu_parity.py, tests/test_gpu_mixed.py)
-    runs = (("fp64", 1e-7),) if name == "tiny_marg3" else (("fp64", 1e-9), ("mixed", 1e-5), ("mixed_direct", 1e-5))
+    runs = (("fp64", 1e-7),) if name == "tiny_marg3" else (("fp64", 1e-9), ("mixed", 1e-5), ("mixed_direct", 1e-5),
+                                                            ("pair", 1e-5))
     for precision, tol in runs:
         eng = lqg.Engine(c.bins, c.tables, c.nv, c.lenv, c.nzp, c.max_forest_length, cont=c.marg, **c.opts)
         if c.reso is None:
@@ -83,6 +98,11 @@ for name in ["tiny_marg1", "tiny_masked", "tiny_marg3", "tiny_nosfid", "tiny_res
         else:
             st = eng.add_chunk_list_reso([ch[:3] + (rm,) for ch, rm in zip(c.chunks, c.rmats)], c.reso[0])
         assert (st == 0).all(), (name, st)
+        if precision == "pair":
+            # the products on CTA pairs (k_tc_gemm_pair), whitened form
+            lds = sorted({(eng.chunk_info(i)["n"] + 63) // 64 * 64 for i in range(eng.size)})
+            eng.set_tuning([(ld, 1, 8, 32768, 1) for ld in lds])
+            precision = "mixed_auto"
         for _ in range(2):   # the second iteration replays a captured graph
             eng.iterate(precision=precision)   # raises if an index check failed
             out = eng.download()
