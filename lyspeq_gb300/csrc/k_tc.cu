@@ -309,10 +309,14 @@ constexpr int BK = 64;                      // fp16 elements per K step (128 byt
 constexpr int G_BM = 128, G_BN = 128, G_STAGES = 3;
 constexpr int G_TILE_A = G_BM * BK * 2, G_TILE_B = G_BN * BK * 2;
 constexpr int G_STAGE_BYTES = 2 * G_TILE_A + 2 * G_TILE_B;
-constexpr int G_SMEM = G_STAGES * G_STAGE_BYTES + 1024 + 256;
+constexpr int kStoreStage = 2048;                        // per epilogue warp: 32 rows x 64 bytes
+constexpr int kStoreStages = 8 * kStoreStage;
+constexpr int G_SMEM = G_STAGES * G_STAGE_BYTES + kStoreStages + 1024 + 256;
 constexpr int R_BM = 128, R_BN = 128, R_STAGES = 3;
 constexpr int R_TILE = R_BM * BK * 2;
 constexpr int R_STAGE_BYTES = 4 * R_TILE;
+constexpr int kGramBox = 32;                      // rows per TMA box of the Gram operands
+constexpr int kGramBoxBytes = kGramBox * BK * 2;  // 4 KB: whole 1024-byte swizzle groups
 constexpr int R_SMEM = R_STAGES * R_STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 320;             // producer, MMA, 8 epilogue warps
 constexpr int R_THREADS = TC_THREADS;
@@ -485,14 +489,39 @@ __device__ __forceinline__ int tile_drain(const WaveArgs &a, const GemmTile &tl)
     return (STAGE != 0 && tl.s >= a.chunks[tl.c].ns) ? kGemmDrainST : (a.gemm_drain > 0 ? a.gemm_drain : kGemmDrain);
 }
 
+// Row-major stores of a warp's 32 rows x 32 fp16 columns of one plane (w:
+// this lane's row, 16 words), coalesced through the warp's 2 KB shared-memory
+// stage: each lane writes its row's four 16-byte chunks (chunk c at position
+// c ^ ((row >> 1) & 3): no bank conflicts), then stores row 8q + lane / 4,
+// chunk lane % 4 for q = 0..3, four lanes covering one row's 64 contiguous
+// bytes (a lane per row would make every 16-byte store its own request).
+__device__ __forceinline__ void store_rows(uint4 *stg, const uint32_t (&w)[16], __half *row0, size_t pitch,
+                                           int lane) {
+    __syncwarp();   // the previous plane's reads of the stage are done
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        stg[lane * 4 + (c ^ ((lane >> 1) & 3))] = make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int r = 8 * q + lane / 4, c = lane % 4;
+        *reinterpret_cast<uint4 *>(row0 + (size_t) r * pitch + 8 * c) = stg[r * 4 + (c ^ ((r >> 1) & 3))];
+    }
+}
+
 // Epilogue of one products tile (epilogue warp quad, columns col0 .. col0 + 63):
 // the drained hi*hi sums plus the cross terms at tcross, scaled to fp16 hi/lo
 // planes.  Stage 0: A_s row-major to R and transposed to P; stage 1: X_s to R;
 // stage 2: B_s weighted into its compact upper tile of P.  A tile with live =
 // false (the padding half of a CTA pair) reads TMEM but writes nothing.
-template <int STAGE>
+// release() runs once the warp's last read of the cross buffer has completed,
+// before its second half of the global stores: the MMAs of the tile after next
+// may take the buffer while the stores drain (the stores hold the epilogue
+// longer than the MMAs of a tile take).
+template <int STAGE, class Release>
 __device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl, bool live, uint32_t tcross,
-                                           uint32_t lane_addr, int quad, int lane, int col0, const float (&sum)[64]) {
+                                           uint32_t lane_addr, int quad, int lane, int col0, const float (&sum)[64],
+                                           uint4 *stg, Release &&release) {
     const int ld = a.max_ld;
     const size_t plane = (size_t) ld * ld;
     const int nq4 = 4 * a.n_chunks;
@@ -504,8 +533,9 @@ __device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl
         const double bs = a.scales[nq4 + a.total_slots_q + ch.slot_p + s];
         const float mult = (float) (bs / (rs * a.scales[4 * tl.c + 2]));
         const int rt = quad * 32 + lane;   // row within the tile
+        // this warp's first row of the compact tile
         const size_t tbase = (size_t) (ch.slot_p + s) * a.p_plane + (size_t) tl.tu * (G_BM * G_BN) +
-                             (size_t) rt * G_BN;
+                             (size_t) (quad * 32) * G_BN;
         const bool ok = live && LQG_IN_BOUNDS(a, ch.slot_p + s < a.total_slots_p &&
                                              (size_t) tl.tu * (G_BM * G_BN) + G_BM * G_BN <= a.p_plane,
                                       2, tl.c, s);
@@ -515,6 +545,7 @@ __device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl
             const int cb = col0 + h * 32;   // column within the tile
             float xv[32];
             tmem_ld32(tcross + lane_addr + cb, xv);
+            if (h == 1) release();
             if (!ok) continue;
             uint32_t hp[16], lp[16];
 #pragma unroll
@@ -533,13 +564,8 @@ __device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl
                 hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
                 lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
             }
-            uint4 *dh = reinterpret_cast<uint4 *>(a.p_hi + tbase + cb);
-            uint4 *dl = reinterpret_cast<uint4 *>(a.p_lo + tbase + cb);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
-                dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
-            }
+            store_rows(stg, hp, a.p_hi + tbase + cb, G_BN, lane);
+            store_rows(stg, lp, a.p_lo + tbase + cb, G_BN, lane);
         }
         return;
     }
@@ -562,6 +588,7 @@ __device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl
         const int cb = tl.n0 + col0 + h * 32;
         float xv[32];
         tmem_ld32(tcross + lane_addr + col0 + h * 32, xv);
+        if (h == 1) release();
         // warp-uniform: ld is a multiple of 64, so a warp's 32 rows are all
         // inside the matrix or all padding
         if (!slots_ok || cb >= ld || tl.m0 + quad * 32 >= ld) continue;
@@ -577,15 +604,8 @@ __device__ __forceinline__ void store_tile(const WaveArgs &a, const GemmTile &tl
             hp[j] = *reinterpret_cast<const uint32_t *>(&hv);
             lp[j] = *reinterpret_cast<const uint32_t *>(&lv);
         }
-        {
-            uint4 *dh = reinterpret_cast<uint4 *>(Rh + (size_t) row * ld + cb);
-            uint4 *dl = reinterpret_cast<uint4 *>(Rl + (size_t) row * ld + cb);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                dh[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
-                dl[q] = make_uint4(lp[4 * q], lp[4 * q + 1], lp[4 * q + 2], lp[4 * q + 3]);
-            }
-        }
+        store_rows(stg, hp, Rh + (size_t) (row - lane) * ld + cb, ld, lane);
+        store_rows(stg, lp, Rl + (size_t) (row - lane) * ld + cb, ld, lane);
         if (!write_p) continue;
         unsigned short *ph = reinterpret_cast<unsigned short *>(Ph) + row;
         unsigned short *pl = reinterpret_cast<unsigned short *>(Pl) + row;
@@ -607,7 +627,8 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + G_STAGES * G_STAGE_BYTES);
+    uint4 *stg_all = reinterpret_cast<uint4 *>(smem + G_STAGES * G_STAGE_BYTES);   // epilogue store stages
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + G_STAGES * G_STAGE_BYTES + kStoreStages);
     uint64_t *empty = full + G_STAGES;
     uint64_t *dfull = empty + G_STAGES;
     uint64_t *dempty = dfull + 2;
@@ -708,11 +729,13 @@ k_tc_gemm(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ CUtens
             got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1, lim)) && !*abort_flag;
             if (!got) break;
             fence_after();
-            store_tile<STAGE>(a, tl, true, tmem + 2 * G_BN + x * G_BN, lane_addr, quad, lane, col0, sum);
-            // this cross buffer may now be taken by tile lt + 2
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&xempty[x]);
+            // the cross buffer may be taken by tile lt + 2 once read
+            store_tile<STAGE>(a, tl, true, tmem + 2 * G_BN + x * G_BN, lane_addr, quad, lane, col0, sum,
+                              stg_all + (warp - 2) * (kStoreStage / 16), [&] {
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&xempty[x]);
+            });
         }
     }
     fence_before();
@@ -755,7 +778,7 @@ constexpr int P_STAGES = 4;
 constexpr int P_TILE_A = 128 * BK * 2;                       // this CTA's 128 rows of A
 constexpr int P_TILE_B = 64 * BK * 2;                        // its 64 rows of B
 constexpr int P_STAGE_BYTES = 2 * P_TILE_A + 2 * P_TILE_B;   // 48 KB
-constexpr int P_SMEM = P_STAGES * P_STAGE_BYTES + 1024 + 256;
+constexpr int P_SMEM = P_STAGES * P_STAGE_BYTES + kStoreStages + 1024 + 256;
 
 struct PairTile {
     GemmTile tl;   // this CTA's tile
@@ -828,7 +851,8 @@ k_tc_gemm_pair(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ C
     // the same offset in both CTAs: the MMAs address both with one descriptor
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t) 1023);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + P_STAGES * P_STAGE_BYTES);   // even CTA: both halves
+    uint4 *stg_all = reinterpret_cast<uint4 *>(smem + P_STAGES * P_STAGE_BYTES);   // epilogue store stages
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + P_STAGES * P_STAGE_BYTES + kStoreStages);   // even CTA: both halves
     uint64_t *empty = full + P_STAGES;
     uint64_t *dfull = empty + P_STAGES;
     uint64_t *dempty = dfull + 2;
@@ -979,10 +1003,12 @@ k_tc_gemm_pair(WaveArgs a, const int *jobs, int njobs, const __grid_constant__ C
             got = __all_sync(0xffffffffu, got && mbar_wait(&xfull[x], (lt >> 1) & 1, lim)) && !*abort_flag;
             if (!got) break;
             fence_after();
-            store_tile<STAGE>(a, p.tl, p.live, tmem + 2 * G_BN + x * G_BN, lane_addr, quad, lane, col0, sum);
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive_cluster(xempty_cl + 8 * x);
+            store_tile<STAGE>(a, p.tl, p.live, tmem + 2 * G_BN + x * G_BN, lane_addr, quad, lane, col0, sum,
+                              stg_all + (warp - 2) * (kStoreStage / 16), [&] {
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive_cluster(xempty_cl + 8 * x);
+            });
         }
     }
     fence_before();
@@ -1031,6 +1057,14 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
     const uint64_t lim = a.wait_ns ? a.wait_ns : kWaitLimitNs;
     // whitened form: both operands are the B_s rows of P (B_0 .. B_{ns+1})
     const int prow = ch.slot_p + bi * R_BM, rrow = (a.sym ? ch.slot_p : ch.slot_r) + bj * R_BN;
+    // Rows of this block that belong to the chunk (P: ns, or ns + 2 in the
+    // whitened form; R: ns + 2), loaded as 32-row boxes: the rows past them
+    // are the next chunk's and are not fetched (16-row boxes fetch less but
+    // cost more TMA issue than they save).  The shared-memory rows left
+    // unloaded hold stale data that only reaches G's rows >= ns and columns
+    // >= ns + 2, which nothing reads.
+    const int prows = min(R_BM, (a.sym ? ch.ns + 2 : ch.ns) - bi * R_BM), rrows = min(R_BN, ch.ns + 2 - bj * R_BN);
+    const int pboxes = (prows + kGramBox - 1) / kGramBox, rboxes = (rrows + kGramBox - 1) / kGramBox;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < R_STAGES; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
@@ -1056,11 +1090,15 @@ k_tc_gram(WaveArgs a, const __grid_constant__ CUtensorMap mp_hi, const __grid_co
             if (!mbar_wait(&empty[st], ((kb / R_STAGES) & 1) ^ 1, lim)) { *abort_flag = 1; break; }
             unsigned char *sb = smem + st * R_STAGE_BYTES;
             const int x = (int) (k_lo + (int64_t) kb * BK);
-            mbar_expect_tx(&full[st], R_STAGE_BYTES);
-            tma_load_2d(sb, &mp_hi, &full[st], x, prow);
-            tma_load_2d(sb + R_TILE, &mp_lo, &full[st], x, prow);
-            tma_load_2d(sb + 2 * R_TILE, &mr_hi, &full[st], x, rrow);
-            tma_load_2d(sb + 3 * R_TILE, &mr_lo, &full[st], x, rrow);
+            mbar_expect_tx(&full[st], 2 * (pboxes + rboxes) * kGramBoxBytes);
+            for (int q = 0; q < pboxes; ++q) {
+                tma_load_2d(sb + q * kGramBoxBytes, &mp_hi, &full[st], x, prow + q * kGramBox);
+                tma_load_2d(sb + R_TILE + q * kGramBoxBytes, &mp_lo, &full[st], x, prow + q * kGramBox);
+            }
+            for (int q = 0; q < rboxes; ++q) {
+                tma_load_2d(sb + 2 * R_TILE + q * kGramBoxBytes, &mr_hi, &full[st], x, rrow + q * kGramBox);
+                tma_load_2d(sb + 3 * R_TILE + q * kGramBoxBytes, &mr_lo, &full[st], x, rrow + q * kGramBox);
+            }
             ++issued;
         }
         for (int kb = (issued > R_STAGES ? issued - R_STAGES : 0); kb < issued; ++kb)
@@ -1262,7 +1300,7 @@ void launch_products_mixed(WaveArgs &a, cudaStream_t st, const int *d_jobs, int 
     cuuint64_t d2p[2] = {pplane, (cuuint64_t) a.total_slots_p};
     cuuint64_t d2r[2] = {plane, (cuuint64_t) a.total_slots_r};
     cuuint64_t s2p[1] = {pplane * 2}, s2[1] = {plane * 2};
-    cuuint32_t box2[2] = {BK, R_BM};
+    cuuint32_t box2[2] = {BK, kGramBox};
     CUtensorMap mph = make_map(a.p_hi, 2, d2p, s2p, box2, &ok);
     CUtensorMap mpl = make_map(a.p_lo, 2, d2p, s2p, box2, &ok);
     // whitened form: the Gram's second operand is P as well
