@@ -407,11 +407,15 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
 // moves it by ~2e-7 of max |b| (CPU emulation on echelle-size chunks), so Q_s
 // (table value, interpolation fraction and redshift weight), y_i y_j, C^-1_ij
 // and the accumulation are all double-float (~48 bits).  No FP64 work in the
-// slot loop (the FP64 pipe is 1/64 of the FP32 one): warp sums in
-// double-float, and each warp's (hi, lo) pair is stored in its 8-byte partial
-// slot.  Blocks and warps map to the d-partial slots of k_build_q_mixed's
-// layout (half tiles of 32 x 64, 8 warps); blocks of lower tiles write nothing.
+// slot loop (the FP64 pipe is 1/64 of the FP32 one).  The block's sums go
+// through shared memory kDxBatch slots at a time: every thread stores its
+// (d, x) double-float pair of each slot of the batch, then warp w adds slot w
+// of the batch (each lane 8 of the 256 values in a fixed order, then a
+// double-float warp sum), so one warp sum serves 256 values instead of 32.
+// Each block (half tile) stores one (hi, lo) pair per slot in an 8-byte
+// partial slot: part 2 tile + half.  Blocks of lower tiles write nothing.
 constexpr int DX_E = 8;   // elements per thread: rows warp + 8u (u < 4), columns 2 lane, 2 lane + 1
+constexpr int kDxBatch = 8;   // slots per shared-memory reduction (one per warp)
 
 template <bool GR>
 __global__ void __launch_bounds__(256, 2) k_dx_mixed(WaveArgs a) {
@@ -423,8 +427,8 @@ __global__ void __launch_bounds__(256, 2) k_dx_mixed(WaveArgs a) {
     const int ti = tile / tpr, tj = tile % tpr;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const bool want_x = a.dbt_id && ch.cinv_m;
-    double *dpart = ws_d(a, ch.o_dpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns;
-    double *xpart = want_x ? ws_d(a, ch.o_xpart) + ((size_t) blockIdx.x * 8 + warp) * ch.ns : nullptr;
+    double *dpart = ws_d(a, ch.o_dpart) + (size_t) blockIdx.x * ch.ns;
+    double *xpart = want_x ? ws_d(a, ch.o_xpart) + (size_t) blockIdx.x * ch.ns : nullptr;
     if (ti > tj) return;   // counted through the mirrored upper tile; k_finish_dx skips these parts
     const DeviceBins &bins = *a.bins;
     const float2 *lw2 = a.logw2 + ch.pix, *sw2 = a.sqw2 + ch.pix;
@@ -453,6 +457,8 @@ __global__ void __launch_bounds__(256, 2) k_dx_mixed(WaveArgs a) {
         }
     }
     const float4 *rows = a.deriv_ff + (size_t) ch.res * bins.nk * a.grid.nv;
+    // (d hi, d lo, x hi, x lo) of every thread for the slots of one batch
+    __shared__ float4 red[kDxBatch][256];
     for (int iz = 0; iz < nzb; ++iz) {
         float2 w[DX_E];
 #pragma unroll
@@ -484,13 +490,29 @@ __global__ void __launch_bounds__(256, 2) k_dx_mixed(WaveArgs a) {
                 dd_mac(sd, cd, qp, qe, yy[k]);
                 if (want_x) dd_mac(sx, cx, qp, qe, cmv[k]);
             }
-            const int s = iz * ch.kbin_upp + kn;
-            const float2 dsum = warp_sum_ff(make_float2(sd, cd));
-            if (lane == 0) reinterpret_cast<float2 *>(dpart)[s] = dsum;
-            if (want_x) {
-                const float2 xsum = warp_sum_ff(make_float2(sx, cx));
-                if (lane == 0) reinterpret_cast<float2 *>(xpart)[s] = xsum;
+            const int b = kn % kDxBatch;
+            red[b][threadIdx.x] = make_float4(sd, cd, sx, cx);
+            if (b != kDxBatch - 1 && kn != ch.kbin_upp - 1) continue;
+            // the batch is complete: warp w adds the 256 values of its slot
+            __syncthreads();
+            if (warp <= b) {
+                float2 dv = make_float2(0.f, 0.f), xv = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 v = red[warp][lane + 32 * q];
+                    const float2 ds = ff_two_sum(dv.x, v.x), xs = ff_two_sum(xv.x, v.z);
+                    dv = ff_norm(ds.x, __fadd_rn(ds.y, __fadd_rn(dv.y, v.y)));
+                    xv = ff_norm(xs.x, __fadd_rn(xs.y, __fadd_rn(xv.y, v.w)));
+                }
+                const int s = iz * ch.kbin_upp + kn - b + warp;
+                dv = warp_sum_ff(dv);
+                if (lane == 0) reinterpret_cast<float2 *>(dpart)[s] = dv;
+                if (want_x) {
+                    xv = warp_sum_ff(xv);
+                    if (lane == 0) reinterpret_cast<float2 *>(xpart)[s] = xv;
+                }
             }
+            __syncthreads();
         }
     }
 }
@@ -762,7 +784,7 @@ __global__ void k_finish(WaveArgs a, int mixed) {
 // ---------------------------------------------------------------------------
 // Mixed path, table chunks (after k_finish): d_s and x_s = tr(Q_s C^-1) from
 // k_dx_mixed's (hi, lo) partials, one warp per slot.  The parts of a slot are
-// the 16 warps of each upper 64 x 64 tile; a tile row's upper tiles are
+// the two half tiles of each upper 64 x 64 tile; a tile row's upper tiles are
 // consecutive, so the lanes stride over them row by row, each lane adds its
 // parts in order and the warp sums the lanes in a fixed tree.  Then d - b - t
 // without the 22-bit traces: with C = S + N + sum_s theta_s Q_s (the stored
@@ -787,8 +809,8 @@ __global__ void __launch_bounds__(256) k_finish_dx(WaveArgs a) {
     const float2 *xp = want_x ? reinterpret_cast<const float2 *>(ws_d(a, ch.o_xpart)) : nullptr;
     double dsum = 0, xsum = 0;
     for (int ti = 0; ti < tpr; ++ti) {
-        const int p1 = (ti * tpr + tpr) * 16;
-        for (int p = (ti * tpr + ti) * 16 + lane; p < p1; p += 32) {
+        const int p1 = (ti * tpr + tpr) * 2;
+        for (int p = (ti * tpr + ti) * 2 + lane; p < p1; p += 32) {
             const float2 v = dp[(size_t) p * ns + s];
             dsum += (double) v.x + (double) v.y;
             if (want_x) {
