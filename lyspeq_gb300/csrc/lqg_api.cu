@@ -55,7 +55,7 @@ struct lqg_ctx {
     int64_t results_size = 0;
     DevBuf d_results, d_status, d_theta, d_fisher, d_dbt, d_meta;
     // workspace
-    DevBuf d_fws, d_ws, d_fbounds, d_desc, d_jobs, d_scales, d_halves, d_gram, d_check, d_ttab, d_ttab_ff;
+    DevBuf d_fws, d_ws, d_fbounds, d_desc, d_jobs, d_scales, d_halves, d_gram, d_check, d_ttab, d_ttab_ff, d_rtab;
     void *h_stage = nullptr;   // pinned staging of the per-iteration descriptors
     size_t h_stage_bytes = 0;
     std::vector<int> last_status;
@@ -640,7 +640,7 @@ cudaEvent_t pool_event(lqg_ctx *ctx, size_t i) {
 // single arrays, uploaded once.
 int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan> &groups, std::vector<ChunkDesc> &desc,
                    std::vector<int> &jobs, std::vector<double> &scales, int64_t &max_fws, int64_t &max_ws,
-                   int64_t &max_half, int64_t &max_gram, int &n_combos) {
+                   int64_t &max_half, int64_t &max_gram, int &n_combos, int &n_rks) {
     const int nb = (int) ctx->chunks.size();
     size_t budget = ctx->opts.workspace_bytes;
     if (budget == 0) {
@@ -684,6 +684,15 @@ int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan>
     combos.erase(std::unique(combos.begin(), combos.end()), combos.end());
     n_combos = (int) combos.size();
     for (const auto &cb : combos) { jobs.push_back(cb.first); jobs.push_back(cb.second); }
+    // KBIN_UPP values of the resolution-matrix chunks: one theta node table row
+    // block each (the mixed path with theta), after the pairs in jobs
+    std::vector<int> rks;
+    for (const auto &h : ctx->chunks)
+        if (h.nelem > 0) rks.push_back(h.kbin_upp);
+    std::sort(rks.begin(), rks.end());
+    rks.erase(std::unique(rks.begin(), rks.end()), rks.end());
+    n_rks = (int) rks.size();
+    for (int k : rks) jobs.push_back(k);
     for (auto &g : groups) {
         max_fws = std::max(max_fws, g.fws_bytes);
         g.desc_off = desc.size();
@@ -695,6 +704,8 @@ int plan_iteration(lqg_ctx *ctx, int precision, int mode, std::vector<GroupPlan>
             if (h.res >= 0 && h.nelem == 0)
                 d.tcombo = (int) (std::lower_bound(combos.begin(), combos.end(), std::make_pair(h.res, h.kbin_upp)) -
                                   combos.begin());
+            if (h.nelem > 0)
+                d.tcombo = (int) (std::lower_bound(rks.begin(), rks.end(), h.kbin_upp) - rks.begin());
             d.n = h.n; d.ld = h.ld; d.nq = h.nq; d.ns = h.ns; d.kbin_upp = h.kbin_upp; d.fis = h.fis;
             d.res = h.res; d.zb0 = h.fis / ctx->nk; d.pix = h.pix; d.res_off = h.res_off; d.gidx = idx;
             d.nelem = h.nelem; d.os = h.os; d.sh = h.sh; d.nf = h.nf; d.fpix = h.fpix; d.rw_off = h.rw_off;
@@ -918,14 +929,34 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     std::vector<int> jobs;
     std::vector<double> scales;
     int64_t max_fws = 0, max_ws = 0, max_half = 0, max_gram = 0;
-    int n_combos = 0;
+    int n_combos = 0, n_rks = 0;
     if ((rc = plan_iteration(ctx, precision, mode, groups, desc, jobs, scales, max_fws, max_ws, max_half, max_gram,
-                             n_combos)))
+                             n_combos, n_rks)))
         return rc;
     const size_t ttab_bytes = (size_t) n_combos * ctx->nz * ctx->grid.nv * 8;
     if (use_theta && n_combos > 0 &&
         (ctx->d_ttab.alloc(ttab_bytes) || (precision == LQG_PRECISION_MIXED && ctx->d_ttab_ff.alloc(ttab_bytes))))
         return set_err(ctx, LQG_ERR_NOMEM, "theta tables");
+    // Mixed path with theta and resolution-matrix chunks: node tables of
+    // G(v) = sum_k theta_k Q_k(v) on [0, v_max] (the widest fine grid's v) at
+    // h = 1 / (20 k_max), so that the cubic Hermite interpolation's (h k)^4 / 384
+    // stays below 2e-8 of G
+    const bool reso_theta = use_theta && precision == LQG_PRECISION_MIXED && n_rks > 0;
+    int64_t rtab_n = 0;
+    double rtab_h = 0.0;
+    if (reso_theta) {
+        double span = 0.0;
+        int kmax = 0;
+        for (const auto &h : ctx->chunks) {
+            if (h.nelem <= 0 || h.nf < 2) continue;
+            span = std::max(span, ctx->h_flogw[h.fpix + h.nf - 1] - ctx->h_flogw[h.fpix]);
+            kmax = std::max(kmax, h.kbin_upp);
+        }
+        rtab_h = 0.05 / ctx->k_edges[std::max(kmax, 1)];
+        rtab_n = (int64_t) std::ceil(kSpeedOfLight * span / rtab_h) + 4;
+        if (ctx->d_rtab.alloc((size_t) n_rks * ctx->nz * rtab_n * sizeof(float4)))
+            return set_err(ctx, LQG_ERR_NOMEM, "theta node tables");
+    }
     ctx->d_fws.trim(std::max<int64_t>(max_fws, 256));
     ctx->d_ws.trim(std::max<int64_t>(max_ws, 256));
     ctx->d_halves.trim(precision == LQG_PRECISION_MIXED ? max_half + 1024 : 0);
@@ -976,7 +1007,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     base.sqiv2 = ctx->d_sqiv2.as<float2>();
     // mixed path: S and C~ built in double-float, handed over as pairs (with
     // theta too, unless resolution-matrix chunks need their FP64 theta sandwiches)
-    base.c_is_ff = (precision == LQG_PRECISION_MIXED && ctx->d_signal_ff.p && (!use_theta || !ctx->has_reso)) ? 1 : 0;
+    base.c_is_ff = (precision == LQG_PRECISION_MIXED && ctx->d_signal_ff.p) ? 1 : 0;
     base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
     base.n_fpix = (int64_t) ctx->h_flogw.size();
     base.reso_nelem = base.reso_os = 0;
@@ -1005,6 +1036,12 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     base.theta = use_theta ? ctx->d_theta.as<double>() : nullptr;
     base.ttab = use_theta && n_combos > 0 ? ctx->d_ttab.as<double>() : nullptr;
     base.ttab_ff = base.ttab && base.c_is_ff ? ctx->d_ttab_ff.as<float2>() : nullptr;
+    base.rtab = reso_theta ? ctx->d_rtab.as<float4>() : nullptr;
+    base.rtab_n = rtab_n;
+    if (reso_theta) {
+        const double x = kSpeedOfLight / rtab_h;
+        base.rtab_x = make_float2((float) x, (float) (x - (double) (float) x));
+    }
     base.results = ctx->d_results.as<double>();
     base.status = ctx->d_status.as<int>();
     base.grid = ctx->grid;
@@ -1041,6 +1078,11 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
         if (base.ttab) {
             launch_theta_tables(base.deriv, base.theta, ctx->d_jobs.as<int>(), n_combos, ctx->nk, ctx->nz,
                                 ctx->grid.nv, ctx->d_ttab.as<double>(), const_cast<float2 *>(base.ttab_ff), st);
+            ctx->launches++;
+        }
+        if (base.rtab) {
+            launch_theta_reso_tables(base.theta, base.bins, ctx->d_jobs.as<int>() + 2 * n_combos, n_rks, ctx->nk,
+                                     ctx->nz, rtab_n, rtab_h, ctx->d_rtab.as<float4>(), st);
             ctx->launches++;
         }
         for (auto &g : groups) {
@@ -1143,7 +1185,8 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
         (uintptr_t) ctx->d_fbounds.p, (uintptr_t) ctx->d_check.p, (uintptr_t) ctx->d_results.p,
         (uintptr_t) ctx->d_status.p, (uintptr_t) ctx->d_meta.p, (uintptr_t) ctx->d_wave.p, (uintptr_t) ctx->d_flogw.p,
         (uintptr_t) ctx->d_rw.p, (uintptr_t) ctx->d_sqiv2.p, (uintptr_t) ctx->d_niv.p, (uintptr_t) ctx->d_ttab.p,
-        (uintptr_t) ctx->d_ttab_ff.p, (uintptr_t) ctx->wait_ns, (uintptr_t) n_combos};
+        (uintptr_t) ctx->d_ttab_ff.p, (uintptr_t) ctx->wait_ns, (uintptr_t) n_combos, (uintptr_t) ctx->d_rtab.p,
+        (uintptr_t) rtab_n, (uintptr_t) n_rks};
     // the launch plan: grid sizes and the by-value kernel arguments follow from these
     for (const auto &g : groups) {
         key.insert(key.end(), {(uintptr_t) g.members.size(), (uintptr_t) g.max_ld, (uintptr_t) g.fws_bytes,

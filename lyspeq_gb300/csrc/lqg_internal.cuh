@@ -57,7 +57,8 @@ struct ChunkDesc {
     int nelem, os, sh, nf;
     int64_t fpix, rw_off;
     int64_t o_ph;         // wave workspace: cos, sin of k_c u at each grid point (mixed path)
-    int tcombo;           // row block of this chunk's (table, KBIN_UPP) in WaveArgs::ttab
+    int tcombo;           // row block of this chunk's (table, KBIN_UPP) in WaveArgs::ttab, or of a
+                          // resolution-matrix chunk's KBIN_UPP in WaveArgs::rtab
     int sym;              // mixed path: whitened symmetric form (else direct)
     double rw_sum;        // largest sum of |weights| of a row (bound of R M R^T)
 };
@@ -163,6 +164,12 @@ struct WaveArgs {
     // sum_{kn < KBIN_UPP} theta[zm nk + kn] deriv[table][kn][v] (nullptr without theta)
     const double *ttab;
     const float2 *ttab_ff;                           // the same rows as double-float (mixed path)
+    // resolution-matrix chunks, mixed path with theta: G(v) = sum_{kn < KBIN_UPP}
+    // theta[zm nk + kn] Q_kn(v) (the analytic band derivative) at v = i h, row
+    // (tcombo nz + zm) of rtab_n nodes (G hi, G lo, h G', 0) (nullptr otherwise)
+    const float4 *rtab;
+    int64_t rtab_n;
+    float2 rtab_x;                                   // c / h as double-float
     double *results;                                 // per-chunk results
     int *status;                                     // per-chunk status (wave-local)
     TableGrid grid;
@@ -208,6 +215,8 @@ void launch_build_s_c(WaveArgs &a, cudaStream_t st);
 // The theta-weighted tables of an iteration (before the groups' S/C builds).
 void launch_theta_tables(const double *deriv, const double *theta, const int *combos, int n_combos, int nk, int nz,
                          int nv, double *ttab, float2 *ttab_ff, cudaStream_t st);
+void launch_theta_reso_tables(const double *theta, const DeviceBins *bins, const int *ks, int n_ks, int nk, int nz,
+                              int64_t nn, double h, float4 *rtab, cudaStream_t st);
 // The same two matrix builds for chunks with a resolution matrix (lqg_reso.cu);
 // each kind of kernel skips the chunks of the other kind.
 void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st);

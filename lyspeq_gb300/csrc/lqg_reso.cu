@@ -718,10 +718,94 @@ struct ResoSharedFF {
     float2 lwr[RLF], swr[RLF], lwc[RLF], swc[RLF];
 };
 
-// Phase A, mixed path without theta: S = R S_grid R^T and C~ = D S D + I in
-// double-float arithmetic (about 48 significant bits) on the FP32 pipe;
+// Tile of R M R^T in double-float: out[u] = (R M R^T)[I RT + r8 + 8u][J RT + j]
+// for the calling thread, M given at grid rows fr in [0, lf) and columns fc of
+// the tile's block by ev(fr, fc) (the same two stages as reso_sandwich).
+template <class Eval>
+__device__ void reso_sandwich_ff(ResoSharedFF &sm, int lf, int nel, int os, Eval ev, float2 out[4]) {
+    const int j = threadIdx.x % 32, r8 = threadIdx.x / 32;
+    for (int s0 = 0; s0 < lf; s0 += RSLAB) {
+        const int rows = min(RSLAB, lf - s0);
+        for (int e = threadIdx.x; e < rows * lf; e += RTH) {
+            const int fr = e / lf, fc = e % lf;
+            sm.f[fr][fc] = ev(s0 + fr, fc);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < RSLAB / 8; ++u) {
+            const int fr = r8 + 8 * u;
+            if (fr < rows) {
+                float2 acc = make_float2(0.f, 0.f);
+                for (int b = 0; b < nel; ++b) acc = ff_fma(sm.f[fr][j * os + b], sm.wj[j][b], acc);
+                sm.t[s0 + fr][j] = acc;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int i = r8 + 8 * u;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int aa = 0; aa < nel; ++aa) acc = ff_fma(sm.wi[i][aa], sm.t[i * os + aa][j], acc);
+        out[u] = acc;
+    }
+    __syncthreads();
+}
+
+// G(v) = sum_{kn < K} theta[zm nk + kn] Q_kn(v), Q_kn the analytic band
+// derivative with a resolution matrix (core/chunk_estimate.cpp:444-454),
+// on nodes v = i h: G as a double-float pair and h G' as a float, for cubic
+// Hermite interpolation between nodes.  One thread per (node, z bin, K).
+__global__ void k_theta_reso_tables(const double *theta, const DeviceBins *bins, const int *ks, int nk, int nz,
+                                    int64_t nn, double h, float4 *rtab) {
+    const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int zm = blockIdx.y, kr = blockIdx.z;
+    if (i >= nn) return;
+    const int K = ks[kr];
+    const double v = (double) i * h;
+    double g = 0.0, dg = 0.0;
+    for (int kn = 0; kn < K; ++kn) {
+        const double th = theta[zm * nk + kn];
+        if (th == 0.0) continue;
+        const double k1 = bins->k_edges[kn], k2 = bins->k_edges[kn + 1], kc = (k1 + k2) / 2., dk = k2 - k1;
+        double sn, cs, sx, cx;
+        sincos(kc * v, &sn, &cs);
+        const double x = dk * v / 2.;
+        sincos(x, &sx, &cx);
+        // sinc(x) and its derivative; the series below 1e-4 (error < 1e-17)
+        const double sinc = fabs(x) < 1e-4 ? 1. - x * x / 6. : sx / x;
+        const double dsinc = fabs(x) < 1e-4 ? -x / 3. : (x * cx - sx) / (x * x);
+        g += th * (dk / kPi) * cs * sinc;
+        dg += th * (dk / kPi) * (-kc * sn * sinc + cs * dsinc * (dk / 2.));
+    }
+    const float gh = (float) g;
+    rtab[((int64_t) kr * nz + zm) * nn + i] = make_float4(gh, (float) (g - (double) gh), (float) (h * dg), 0.f);
+}
+
+// G at x = v / h (double-float) from a row of k_theta_reso_tables: the node
+// value in double-float plus the cubic Hermite correction t (D0 + t (c2 +
+// t c3)) in float, which is about h k_max = 1/20 of G: the interpolation
+// error (h k)^4 / 384 and the float correction both stay near 1e-8 of G.
+__device__ __forceinline__ float2 rtab_eval(const float4 *row, int64_t nn, float2 x) {
+    int n;
+    float2 t2;
+    ff_index(x, (int) nn - 2, n, t2);
+    const float4 a = row[n], b = row[n + 1];
+    const float t = t2.x;
+    const float dG = __fadd_rn(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y));
+    const float c2 = 3.f * dG - 2.f * a.z - b.z, c3 = -2.f * dG + a.z + b.z;
+    const float corr = t * (a.z + t * (c2 + t * c3));
+    return ff_add(make_float2(a.x, a.y), make_float2(corr, 0.f));
+}
+
+// Phase A, mixed path: S = R S_grid R^T and C~ = D (S + sum_s theta_s Q_s) D + I
+// in double-float arithmetic (about 48 significant bits) on the FP32 pipe;
 // grid v, z, interpolation fractions and table values in double-float, the
-// sandwich with double-float multiply-adds.  Stored as FP64.
+// sandwich with double-float multiply-adds.  The theta term is formed per
+// redshift bin m as w_m(z_ij) (R G_m R^T)_ij, G_m = sum_k theta_{k,m} Q_k on the
+// grid from the node table of k_theta_reso_tables (G_m depends on v only; its
+// nodes are shared by every chunk) instead of the band sum per grid element.
+// Stored as double-float pairs.
 __global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     ResoSharedFF &sm = *reinterpret_cast<ResoSharedFF *>(smraw);
@@ -756,49 +840,62 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
     if (tab) {
         const float2 kv = make_float2(gr.kv_hi, gr.kv_lo), z1p = make_float2(gr.z1p_hi, gr.z1p_lo);
         const float2 idz = make_float2(gr.idz_hi, gr.idz_lo), one = make_float2(1.f, 0.f);
-        for (int s0 = 0; s0 < lf; s0 += RSLAB) {
-            const int rows = min(RSLAB, lf - s0);
-            for (int e = threadIdx.x; e < rows * lf; e += RTH) {
-                const int fr = e / lf, fc = e % lf, p = r0 + s0 + fr, q = c0 + fc;
-                float2 val = make_float2(0.f, 0.f);
-                if (p >= 0 && q >= 0 && p < ch.nf && q < ch.nf) {
-                    const bool up = p <= q;
-                    const float2 lh = up ? sm.lwc[fc] : sm.lwr[s0 + fr], ll = up ? sm.lwr[s0 + fr] : sm.lwc[fc];
-                    const float2 yy = ff_mul(ff_sub(lh, ll), kv);               // v / dv
-                    float zp, ze;
-                    two_prod_ff(sm.swr[s0 + fr], sm.swc[fc], zp, ze);            // 1 + z
-                    const float2 xx = ff_mul(ff_sub(ff_norm(zp, ze), z1p), idz); // (z - z1) / dz
-                    int nx, ny;
-                    float2 fx, fy;
-                    ff_index(xx, gr.nzp - 2, nx, fx);
-                    ff_index(yy, gr.nv - 2, ny, fy);
-                    const size_t ind = (size_t) nx + (size_t) gr.nzp * ny;
-                    const float2 gx = ff_sub(one, fx), gy = ff_sub(one, fy);
-                    val = ff_mul(ff_mul(tab[ind], gx), gy);
-                    val = ff_fma(ff_mul(tab[ind + 1], fx), gy, val);
-                    val = ff_fma(ff_mul(tab[ind + gr.nzp], gx), fy, val);
-                    val = ff_fma(ff_mul(tab[ind + gr.nzp + 1], fx), fy, val);
-                }
-                sm.f[fr][fc] = val;
+        reso_sandwich_ff(sm, lf, nel, os, [&](int fr, int fc) {
+            const int p = r0 + fr, q = c0 + fc;
+            float2 val = make_float2(0.f, 0.f);
+            if (p >= 0 && q >= 0 && p < ch.nf && q < ch.nf) {
+                const bool up = p <= q;
+                const float2 lh = up ? sm.lwc[fc] : sm.lwr[fr], ll = up ? sm.lwr[fr] : sm.lwc[fc];
+                const float2 yy = ff_mul(ff_sub(lh, ll), kv);               // v / dv
+                float zp, ze;
+                two_prod_ff(sm.swr[fr], sm.swc[fc], zp, ze);                 // 1 + z
+                const float2 xx = ff_mul(ff_sub(ff_norm(zp, ze), z1p), idz); // (z - z1) / dz
+                int nx, ny;
+                float2 fx, fy;
+                ff_index(xx, gr.nzp - 2, nx, fx);
+                ff_index(yy, gr.nv - 2, ny, fy);
+                const size_t ind = (size_t) nx + (size_t) gr.nzp * ny;
+                const float2 gx = ff_sub(one, fx), gy = ff_sub(one, fy);
+                val = ff_mul(ff_mul(tab[ind], gx), gy);
+                val = ff_fma(ff_mul(tab[ind + 1], fx), gy, val);
+                val = ff_fma(ff_mul(tab[ind + gr.nzp], gx), fy, val);
+                val = ff_fma(ff_mul(tab[ind + gr.nzp + 1], fx), fy, val);
             }
-            __syncthreads();
+            return val;
+        }, sv);
+    }
+    // sum_s theta_s Q_s on the pixel grid
+    float2 tv[4] = {};
+    if (a.theta && a.rtab && ch.tcombo >= 0) {
+        const DeviceBins &bins = *a.bins;
+        const int nzb = ch.ns / ch.kbin_upp;
+        for (int iz = 0; iz < nzb; ++iz) {
+            const double *th = a.theta + ch.fis + iz * bins.nk;
+            bool any = false;
+            for (int kn = 0; kn < ch.kbin_upp; ++kn) any |= th[kn] != 0.0;
+            if (!any) continue;   // uniform over the block
+            const float4 *row = a.rtab + ((int64_t) ch.tcombo * bins.nz + ch.zb0 + iz) * a.rtab_n;
+            float2 gm[4];
+            reso_sandwich_ff(sm, lf, nel, os, [&](int fr, int fc) {
+                const int p = r0 + fr, q = c0 + fc;
+                if (p < 0 || q < 0 || p >= ch.nf || q >= ch.nf) return make_float2(0.f, 0.f);
+                const bool up = p <= q;
+                const float2 lh = up ? sm.lwc[fc] : sm.lwr[fr], ll = up ? sm.lwr[fr] : sm.lwc[fc];
+                return rtab_eval(row, a.rtab_n, ff_mul(ff_sub(lh, ll), a.rtab_x));   // v / h
+            }, gm);
 #pragma unroll
-            for (int u = 0; u < RSLAB / 8; ++u) {
-                const int fr = r8 + 8 * u;
-                if (fr < rows) {
-                    float2 acc = make_float2(0.f, 0.f);
-                    for (int b = 0; b < nel; ++b) acc = ff_fma(sm.f[fr][j * os + b], sm.wj[j][b], acc);
-                    sm.t[s0 + fr][j] = acc;
+            for (int u = 0; u < 4; ++u) {
+                const int gi = I * RT + r8 + 8 * u;
+                if (gi >= n || gj >= n) continue;
+                float zp, ze;
+                two_prod_ff(a.sqw2[ch.pix + gi], a.sqw2[ch.pix + gj], zp, ze);   // 1 + z_ij
+                float2 w = zweight_dd(bins, ch.zb0 + iz, zp, ze);
+                if (a.growth && w.x != 0.f) {
+                    const double z1 = (double) zp + (double) ze;
+                    w = ff_mul(w, ff_of(pow(z1 / (bins.z_centers[ch.zb0 + iz] + 1.0), bins.growth_b)));
                 }
+                tv[u] = ff_fma(gm[u], w, tv[u]);
             }
-            __syncthreads();
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int i = r8 + 8 * u;
-            float2 acc = make_float2(0.f, 0.f);
-            for (int aa = 0; aa < nel; ++aa) acc = ff_fma(sm.wi[i][aa], sm.t[i * os + aa][j], acc);
-            sv[u] = acc;
         }
     }
     // S and C~ as double-float pairs (c_is_ff: the form the mixed factorisation uses)
@@ -809,7 +906,7 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
         float2 s2 = make_float2(0.f, 0.f), c2 = make_float2(gi == gj ? 1.f : 0.f, 0.f);
         if (gi < n && gj < n) {
             s2 = sv[u];
-            const float2 cv = ff_mul(ff_mul(a.sqiv2[ch.pix + gi], sv[u]), a.sqiv2[ch.pix + gj]);
+            const float2 cv = ff_mul(ff_mul(a.sqiv2[ch.pix + gi], ff_add(sv[u], tv[u])), a.sqiv2[ch.pix + gj]);
             c2 = (gi == gj) ? ff_add(cv, make_float2(1.f, 0.f)) : cv;
         }
         S[(size_t) gi * ld + gj] = s2;
@@ -821,10 +918,10 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
     }
 }
 
-bool reso_attr_set = false;
+// Shared memory above the 48 KB default: once per device (the attribute is per device)
+std::atomic<unsigned long long> reso_attr{0};
 
-void set_reso_attrs() {
-    if (reso_attr_set) return;
+cudaError_t set_reso_attrs_now() {
     const int bytes = (int) sizeof(ResoShared);
     cudaFuncSetAttribute(k_build_s_c_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_build_q_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -836,17 +933,29 @@ void set_reso_attrs() {
                          (int) sizeof(ResoSharedF));
     cudaFuncSetAttribute(k_build_q_reso_f32<11, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) sizeof(ResoSharedF));
-    cudaFuncSetAttribute(k_build_s_c_reso_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) sizeof(ResoSharedFF));
-    reso_attr_set = true;
+    return cudaFuncSetAttribute(k_build_s_c_reso_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int) sizeof(ResoSharedFF));
+}
+
+bool set_reso_attrs() {
+    return once_per_device(reso_attr, [](int) { return set_reso_attrs_now(); });
 }
 
 }  // namespace
 
+void launch_theta_reso_tables(const double *theta, const DeviceBins *bins, const int *ks, int n_ks, int nk, int nz,
+                              int64_t nn, double h, float4 *rtab, cudaStream_t st) {
+    k_theta_reso_tables<<<dim3((unsigned) ((nn + 255) / 256), nz, n_ks), 256, 0, st>>>(theta, bins, ks, nk, nz, nn, h,
+                                                                                      rtab);
+}
+
 void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st) {
-    set_reso_attrs();
+    if (!set_reso_attrs()) {
+        a.host_failed = 1;
+        return;
+    }
     const int nt = a.max_ld / RT;
-    // mixed path without theta: the double-float build (pairs, c_is_ff); else FP64
+    // mixed path: the double-float build (pairs, c_is_ff); FP64 path: FP64
     if (a.c_is_ff)
         k_build_s_c_reso_ff<<<dim3(nt * nt, a.n_chunks), RTH, sizeof(ResoSharedFF), st>>>(a);
     else
@@ -855,7 +964,10 @@ void launch_build_s_c_reso(WaveArgs &a, cudaStream_t st) {
 }
 
 void launch_build_q_reso(WaveArgs &a, cudaStream_t st) {
-    set_reso_attrs();
+    if (!set_reso_attrs()) {
+        a.host_failed = 1;
+        return;
+    }
     const int nt = a.max_ld / RT;
     if (a.precision == LQG_PRECISION_MIXED) {
         k_reso_phases<<<dim3(32, a.n_chunks), 256, 0, st>>>(a);

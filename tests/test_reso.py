@@ -103,3 +103,46 @@ def test_batch_mixing_resolution_and_table_chunks(engine_lib):
         d, b, t, f = eng.chunk_result(i)
         assert np.array_equal(d, d0) and np.array_equal(f, f0)
     eng.close()
+
+
+@pytest.mark.gpu
+def test_nonzero_theta_mixed_matches_fp64_on_desi_resolution_chunks(engine_lib):
+    """The mixed path's theta term for resolution-matrix chunks comes from node
+    tables of G(v) = sum_k theta_k Q_k(v) with cubic Hermite interpolation
+    (error ~2e-8 of G) inside the double-float C build; the FP64 path sums the
+    analytic band derivatives per grid element.  24 DESI-like resolution
+    chunks at theta from a first NR step: every chunk's d, b, t and F within
+    1e-5 of FP64, and the NR step itself (theta) within 1e-5 on the bins
+    measured at 5 sigma or more."""
+    from lyspeq_gb300 import lqg, synth
+    w = synth.make_workload("desi_reso", n_chunks=24)
+    eng = lqg.Engine(w.bins, w.tables, w.nv, w.lenv, w.nzp, w.max_forest_length,
+                     cont=(w.cont_logl_order, w.cont_l_order))
+    # each spectrum's matrix deconvolved and oversampled as lyspeq's reader does
+    rr = []
+    for s in w.spectra:
+        v = lqg.resomat_deconvolve(s.resomat, w.deconv_m) if w.deconv_m > 0 else s.resomat
+        rr.append(lqg.resomat_oversample(v, w.oversample, float(np.median(np.diff(s.wave))))
+                  if w.oversample > 0 else v)
+    st = eng.add_chunk_list_reso([(s.wave, s.delta, 1.0 / s.sigma ** 2, r) for s, r in zip(w.spectra, rr)],
+                                 w.oversample)
+    assert (st == 0).all()
+    eng.iterate(precision="fp64")
+    out = eng.download()
+    theta = eng.fisher_solve(out["fisher"], np.stack([out["d"], out["b"], out["t"]]))["theta"]
+    assert np.any(theta != 0)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        eng.iterate(theta=theta, precision=prec)
+        o = eng.download()
+        assert (o["status"] == 0).all()
+        res[prec] = ([eng.chunk_result(i) for i in range(eng.size)],
+                     eng.fisher_solve(o["fisher"], np.stack([o["d"], o["b"], o["t"]])))
+    for (d, b, t, f), (d0, b0, t0, f0) in zip(res["mixed"][0], res["fp64"][0]):
+        assert max(G.rel_err(d, d0), G.rel_err(b, b0), G.rel_err(t, t0), G.fisher_err(f, f0)) < 1e-5
+    g0, g1 = res["fp64"][1], res["mixed"][1]
+    sig = np.sqrt(np.abs(np.diag(g0["inverse"])))
+    good = (sig > 0) & (np.abs(g0["theta"]) > 5 * sig)
+    if good.any():
+        assert np.max(np.abs(g1["theta"] - g0["theta"])[good] / np.abs(g0["theta"])[good]) < 1e-5
+    eng.close()
