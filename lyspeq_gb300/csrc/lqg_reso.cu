@@ -922,19 +922,16 @@ __global__ void __launch_bounds__(RTH) k_build_s_c_reso_ff(WaveArgs a) {
 std::atomic<unsigned long long> reso_attr{0};
 
 cudaError_t set_reso_attrs_now() {
-    const int bytes = (int) sizeof(ResoShared);
-    cudaFuncSetAttribute(k_build_s_c_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_build_q_reso, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_build_q_reso_f32<0, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) sizeof(ResoSharedF));
-    cudaFuncSetAttribute(k_build_q_reso_f32<0, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) sizeof(ResoSharedF));
-    cudaFuncSetAttribute(k_build_q_reso_f32<31, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) sizeof(ResoSharedF));
-    cudaFuncSetAttribute(k_build_q_reso_f32<11, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) sizeof(ResoSharedF));
-    return cudaFuncSetAttribute(k_build_s_c_reso_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int) sizeof(ResoSharedFF));
+    const int bytes = (int) sizeof(ResoShared), bytes_f = (int) sizeof(ResoSharedF), bytes_ff = (int) sizeof(ResoSharedFF);
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(k_build_s_c_reso, at, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_build_q_reso, at, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_build_q_reso_f32<0, 0, false>, at, bytes_f);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_build_q_reso_f32<0, 0, true>, at, bytes_f);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_build_q_reso_f32<31, 3, false>, at, bytes_f);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_build_q_reso_f32<11, 1, false>, at, bytes_f);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_build_s_c_reso_ff, at, bytes_ff);
+    return e;
 }
 
 bool set_reso_attrs() {
