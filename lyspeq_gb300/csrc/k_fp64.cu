@@ -368,11 +368,19 @@ __global__ void __launch_bounds__(256, 2) k_build_q_mixed(WaveArgs a) {
                 w[g][k] = (z0 + g < nzb && zp[k] > 0.f) ? (GR ? zfactor_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k])
                                                               : zweight_ff(bins, ch.zb0 + z0 + g, zp[k], ze[k]))
                                                          : 0.f;
+        // the node pairs of band kn are loaded while band kn - 1 is stored
+        float r0[E], r1[E];
+#pragma unroll
+        for (int k = 0; k < E; ++k) { r0[k] = rows[nidx[k]]; r1[k] = rows[nidx[k] + 1]; }
         for (int kn = 0; kn < ch.kbin_upp; ++kn) {
-            const float *row = rows + (size_t) kn * a.grid.nv;
             float base[E];
 #pragma unroll
-            for (int k = 0; k < E; ++k) base[k] = fmaf(row[nidx[k] + 1] - row[nidx[k]], dnf[k], row[nidx[k]]);
+            for (int k = 0; k < E; ++k) base[k] = fmaf(r1[k] - r0[k], dnf[k], r0[k]);
+            if (kn + 1 < ch.kbin_upp) {
+                const float *next = rows + (size_t) (kn + 1) * a.grid.nv;
+#pragma unroll
+                for (int k = 0; k < E; ++k) { r0[k] = next[nidx[k]]; r1[k] = next[nidx[k] + 1]; }
+            }
 #pragma unroll
             for (int g = 0; g < kZGroup; ++g) {
                 if (z0 + g >= nzb) break;
