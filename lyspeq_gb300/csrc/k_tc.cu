@@ -10,11 +10,16 @@
 // k_tc_gemm:  A_s = C^-1 Q_s for every stored derivative matrix and A_S = C^-1 S
 //             (Chunk::_getWeightedMatrix, core/chunk_estimate.cpp:721-736, and
 //             the S_fid C^-1 product at :796-799).  The epilogue writes A_s as
-//             hi/lo planes twice: row-major into R and transposed into P.
-// k_tc_gram:  G = P R^T over K = ld^2, split over K; per-split fp32 partial
-//             tiles are reduced in FP64 by k_finish.  Rows of P are A_s^T,
-//             A_S^T = S C^-1 and N C^-1, so G holds F_ij = <A_i^T, A_j>,
-//             t_j and b_j (core/chunk_estimate.cpp:783-832).
+//             hi/lo planes twice: row-major into R and transposed into P.  The
+//             whitened form's two stages (X_s = W Q_s, B_s = X_s W^T) are
+//             stages 1 and 2 of the same persistent kernel.
+// k_tc_gemm_pair: the same products on CTA pairs (cta_group::2, 256 x 128
+//             tiles), an autotuned alternative per padded size.
+// k_tc_gram:  G = P R^T over K = ld^2 (or the whitened form's compact upper
+//             tiles), split over K; per-split fp32 partial tiles are reduced in
+//             FP64 by k_finish.  Rows of P are A_s^T, A_S^T = S C^-1 and
+//             N C^-1, so G holds F_ij = <A_i^T, A_j>, t_j and b_j
+//             (core/chunk_estimate.cpp:783-832).
 //
 // Warp roles (320 threads): warp 0 issues TMA loads, warp 1 owns tensor memory
 // and issues the MMAs, warps 2-9 drain the accumulators.  Every wait on an
