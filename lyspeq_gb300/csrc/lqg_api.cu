@@ -941,7 +941,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     // G(v) = sum_k theta_k Q_k(v) on [0, v_max] (the widest fine grid's v) at
     // h = 1 / (20 k_max), so that the cubic Hermite interpolation's (h k)^4 / 384
     // stays below 2e-8 of G
-    const bool reso_theta = use_theta && precision == LQG_PRECISION_MIXED && n_rks > 0;
+    bool reso_theta = use_theta && precision == LQG_PRECISION_MIXED && n_rks > 0;
     int64_t rtab_n = 0;
     double rtab_h = 0.0;
     if (reso_theta) {
@@ -954,8 +954,15 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
         }
         rtab_h = 0.05 / ctx->k_edges[std::max(kmax, 1)];
         rtab_n = (int64_t) std::ceil(kSpeedOfLight * span / rtab_h) + 4;
-        if (ctx->d_rtab.alloc((size_t) n_rks * ctx->nz * rtab_n * sizeof(float4)))
+        // a binning whose tables would pass 1 GiB (very high k over very long
+        // chunks) keeps the FP64 build of C for its resolution chunks instead
+        const double bytes = (double) n_rks * ctx->nz * (double) rtab_n * sizeof(float4);
+        if (!(bytes <= 1073741824.0) || rtab_n > INT32_MAX) {
+            reso_theta = false;
+            rtab_n = 0;
+        } else if (ctx->d_rtab.alloc((size_t) bytes)) {
             return set_err(ctx, LQG_ERR_NOMEM, "theta node tables");
+        }
     }
     ctx->d_fws.trim(std::max<int64_t>(max_fws, 256));
     ctx->d_ws.trim(std::max<int64_t>(max_ws, 256));
@@ -1007,7 +1014,9 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     base.sqiv2 = ctx->d_sqiv2.as<float2>();
     // mixed path: S and C~ built in double-float, handed over as pairs (with
     // theta too, unless resolution-matrix chunks need their FP64 theta sandwiches)
-    base.c_is_ff = (precision == LQG_PRECISION_MIXED && ctx->d_signal_ff.p) ? 1 : 0;
+    // the double-float S/C build; with theta, resolution chunks need their node tables
+    base.c_is_ff = (precision == LQG_PRECISION_MIXED && ctx->d_signal_ff.p &&
+                    (!use_theta || !ctx->has_reso || reso_theta)) ? 1 : 0;
     base.flogw = ctx->d_flogw.as<double>(); base.fsqw = ctx->d_fsqw.as<double>(); base.rw = ctx->d_rw.as<double>();
     base.n_fpix = (int64_t) ctx->h_flogw.size();
     base.reso_nelem = base.reso_os = 0;
