@@ -33,7 +33,9 @@
 extern "C" {
 #endif
 
-#define LQG_ABI_VERSION 2
+/* 3: the tuning table entries of lqg_tuning_get / lqg_tuning_set carry
+ * LQG_TUNING_FIELDS (5) ints */
+#define LQG_ABI_VERSION 3
 
 /* status codes */
 #define LQG_OK 0

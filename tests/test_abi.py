@@ -28,4 +28,10 @@ def test_library_exports_header(engine_lib):
 def test_null_arguments_rejected_without_gpu(engine_lib):
     h = C.c_void_p()
     assert engine_lib.lqg_ctx_create(C.byref(h), None, None, None, 0) == -1
-    assert engine_lib.lqg_abi_version() == 2
+    assert engine_lib.lqg_abi_version() == 3
+
+
+def test_tuning_field_count_matches_the_header():
+    text = open(HEADER).read()
+    m = re.search(r"#define LQG_TUNING_FIELDS (\d+)", text)
+    assert m and int(m.group(1)) == lqg.TUNING_FIELDS
