@@ -3,12 +3,18 @@
 // :261-288, :290-318 and mathtools/matrix_helper.cpp:220-358 (stableInvertSym).
 // The reference decides damping from the singular values of F (dgesvd); F is
 // symmetric, so they are the absolute eigenvalues, found here by Householder
-// tridiagonalisation and implicit QL.  Inverses use Gauss-Jordan elimination
-// with partial pivoting (the reference: LU, dgetrf + dgetri).  O(nkz^3) FP64.
+// tridiagonalisation and implicit QL, unless F is positive definite and a
+// Lanczos estimate on its Cholesky factor shows its two smallest eigenvalues
+// well within the damping threshold.  The undamped inverse of the positive
+// definite F is taken from that factor, the columns solved on the host's
+// cores; Gauss-Jordan elimination with partial pivoting where the factor
+// fails and in the damped branch (the reference: LU, dgetrf + dgetri).
+// O(nkz^3) FP64.
 #include "lqg_internal.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 struct lqg_ctx;
@@ -126,6 +132,140 @@ bool invert(Mat a, int n, Mat &inv) {
     return true;
 }
 
+// Dot product of two contiguous rows with four independent partial sums, so
+// that the inner loops of the factor and the substitutions are not one chain
+// of dependent additions.
+inline double dot(const double *a, const double *b, int len) {
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int k = 0;
+    for (; k + 4 <= len; k += 4) {
+        s0 += a[k] * b[k];
+        s1 += a[k + 1] * b[k + 1];
+        s2 += a[k + 2] * b[k + 2];
+        s3 += a[k + 3] * b[k + 3];
+    }
+    for (; k < len; ++k) s0 += a[k] * b[k];
+    return (s0 + s1) + (s2 + s3);
+}
+
+// Cholesky factor of a symmetric positive definite matrix: a = L L^T by rows
+// (left-looking, every inner product over contiguous rows); U = L^T row-major
+// for the back substitutions.  False if a pivot is not positive.
+bool spd_factor(const Mat &a, int n, Mat &L, Mat &U) {
+    L.assign((size_t) n * n, 0.0);
+    for (int j = 0; j < n; ++j) {
+        const double *lj = &L[(size_t) j * n];
+        double d = a[(size_t) j * n + j] - dot(lj, lj, j);
+        if (!(d > 0) || !std::isfinite(d)) return false;
+        d = std::sqrt(d);
+        L[(size_t) j * n + j] = d;
+        for (int i = j + 1; i < n; ++i)
+            L[(size_t) i * n + j] = (a[(size_t) i * n + j] - dot(&L[(size_t) i * n], lj, j)) / d;
+    }
+    U.assign((size_t) n * n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k <= i; ++k) U[(size_t) k * n + i] = L[(size_t) i * n + k];
+    return true;
+}
+
+// x = (L L^T)^-1 b by forward and back substitution.
+void spd_solve(const Mat &L, const Mat &U, int n, const double *b, double *y, double *x) {
+    for (int i = 0; i < n; ++i) {
+        const double *li = &L[(size_t) i * n];
+        y[i] = (b[i] - dot(li, y, i)) / li[i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        const double *ui = &U[(size_t) i * n];
+        x[i] = (y[i] - dot(ui + i + 1, x + i + 1, n - 1 - i)) / ui[i];
+    }
+}
+
+// The inverse from the factor: column c from L y = e_c and L^T x = y, the
+// columns split over up to 16 threads, created and joined here.
+void spd_inverse(const Mat &L, const Mat &U, int n, Mat &inv) {
+    inv.assign((size_t) n * n, 0.0);
+    auto columns = [&](int first, int step) {
+        std::vector<double> y(n), x(n);
+        for (int c = first; c < n; c += step) {
+            std::fill(y.begin(), y.begin() + c, 0.0);
+            for (int i = c; i < n; ++i) {
+                const double *li = &L[(size_t) i * n];
+                y[i] = ((i == c ? 1.0 : 0.0) - dot(li + c, &y[c], i - c)) / li[i];
+            }
+            for (int i = n - 1; i >= 0; --i) {
+                const double *ui = &U[(size_t) i * n];
+                x[i] = (y[i] - dot(ui + i + 1, &x[i + 1], n - 1 - i)) / ui[i];
+            }
+            for (int i = 0; i < n; ++i) inv[(size_t) i * n + c] = x[i];
+        }
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nt = (int) std::max(1u, std::min(16u, hw ? hw : 1u));
+    if (nt == 1 || n < 64) {
+        columns(0, 1);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) pool.emplace_back(columns, t, nt);
+        columns(0, nt);
+        for (auto &th : pool) th.join();
+    }
+}
+
+// Whether the damping test of stableInvertSym could fire: it needs the two
+// smallest eigenvalues of the positive definite F (its singular values) more
+// than 8 apart.  They are the two largest of F^-1, estimated by 40 Lanczos
+// steps with full reorthogonalisation (two triangular solves per step) from a
+// fixed start vector: a component along the smallest eigenvector as small as
+// rounding grows by the ratio (> 8) every step, so a separated smallest
+// eigenvalue is not missed.  Returns false (no damping) only when the ratio of
+// the estimates is below 4 and stable over the last 10 steps; true sends the
+// caller to the full eigenvalue test.
+bool damping_possible(const Mat &L, const Mat &U, int n) {
+    const int K = 40;
+    if (n < 64) return true;   // the full test costs little there
+    std::vector<std::vector<double>> V(K + 1, std::vector<double>(n));
+    for (int i = 0; i < n; ++i) V[0][i] = 1.0 + 0.25 * std::sin(1.0 + 0.7 * i);
+    double nrm = 0;
+    for (double v : V[0]) nrm += v * v;
+    nrm = std::sqrt(nrm);
+    for (double &v : V[0]) v /= nrm;
+    std::vector<double> alpha(K), beta(K), w(n), y(n);
+    double prev_ratio = -1, ratio = -1;
+    for (int k = 0; k < K; ++k) {
+        spd_solve(L, U, n, V[k].data(), y.data(), w.data());
+        const double a = dot(w.data(), V[k].data(), n);
+        alpha[k] = a;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int j = 0; j <= k; ++j) {
+                const double h = dot(w.data(), V[j].data(), n);
+                for (int i = 0; i < n; ++i) w[i] -= h * V[j][i];
+            }
+        const double b = std::sqrt(dot(w.data(), w.data(), n));
+        beta[k] = b;
+        // the two largest Ritz values of the (k + 1) x (k + 1) tridiagonal
+        const int m = k + 1;
+        if (m >= 2) {
+            Mat T((size_t) m * m, 0.0);
+            for (int i = 0; i < m; ++i) {
+                T[(size_t) i * m + i] = alpha[i];
+                if (i + 1 < m) T[(size_t) i * m + i + 1] = T[(size_t) (i + 1) * m + i] = beta[i];
+            }
+            std::vector<double> ev;
+            if (!sym_eigenvalues(T, m, ev)) return true;
+            std::sort(ev.begin(), ev.end(), std::greater<double>());
+            if (!(ev[1] > 0)) return true;
+            if (k == K - 10) prev_ratio = ev[0] / ev[1];
+            ratio = ev[0] / ev[1];   // lambda_2 / lambda_1 of F
+        }
+        // a Krylov space that closes early may have missed an eigenvector
+        if (!(b > 1e-12 * std::fabs(a)) || !std::isfinite(b)) return true;
+        for (int i = 0; i < n; ++i) V[k + 1][i] = w[i] / b;
+    }
+    if (!(ratio > 0) || !std::isfinite(ratio) || !(prev_ratio > 0)) return true;
+    if (std::fabs(ratio - prev_ratio) > 1e-6 * ratio) return true;
+    return !(ratio < 4.0);
+}
+
 Mat matmul(const Mat &a, const Mat &b, int n) {
     Mat c((size_t) n * n, 0.0);
     for (int i = 0; i < n; ++i)
@@ -152,14 +292,28 @@ extern "C" int lqg_fisher_solve_n(int n, const double *fisher_sum, const double 
     std::vector<int> empty;
     for (int i = 0; i < n; ++i)
         if (S[(size_t) i * n + i] == 0) { empty.push_back(i); S[(size_t) i * n + i] = 1.0; }
-    std::vector<double> ev;
-    if (!sym_eigenvalues(S, n, ev)) return LQG_ERR_SINGULAR;
-    for (auto &v : ev) v = std::fabs(v);
-    std::sort(ev.begin(), ev.end(), std::greater<double>());
+    // F positive definite with its two smallest eigenvalues clearly within a
+    // factor 8: no damping, and the inverse from the Cholesky factor, taken
+    // while one more thread runs the Lanczos test (the damped branch, rare,
+    // discards it)
+    Mat L, U, spd_inv;
+    const bool spd = spd_factor(S, n, L, U);
+    bool possible = true;
+    if (spd) {
+        std::thread test([&] { possible = damping_possible(L, U, n); });
+        spd_inverse(L, U, n, spd_inv);
+        test.join();
+    }
     double damp = 0;
-    for (int i = n - 1; i > 0; --i) {
-        if (ev[i - 1] / ev[i] > 8.) damp = ev[i];
-        else break;
+    if (possible) {
+        std::vector<double> ev;
+        if (!sym_eigenvalues(S, n, ev)) return LQG_ERR_SINGULAR;
+        for (auto &v : ev) v = std::fabs(v);
+        std::sort(ev.begin(), ev.end(), std::greater<double>());
+        for (int i = n - 1; i > 0; --i) {
+            if (ev[i - 1] / ev[i] > 8.) damp = ev[i];
+            else break;
+        }
     }
     Mat sol, inv;
     int warn = 0;
@@ -172,7 +326,8 @@ extern "C" int lqg_fisher_solve_n(int n, const double *fisher_sum, const double 
         if (!invert(A, n, Ai)) return LQG_ERR_SINGULAR;
         sol = matmul(Ai, S, n);
     } else {
-        if (!invert(S, n, sol)) return LQG_ERR_SINGULAR;
+        if (spd) sol.swap(spd_inv);
+        else if (!invert(S, n, sol)) return LQG_ERR_SINGULAR;
         inv = sol;
     }
     for (int i : empty) { sol[(size_t) i * n + i] = 0; inv[(size_t) i * n + i] = 0; }

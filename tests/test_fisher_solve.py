@@ -66,6 +66,38 @@ def test_damped_solver_branch(engine_lib):
     assert G.rel_err(g["theta"], o["theta"]) < tol
 
 
+@pytest.mark.parametrize("ratio,spread", [(8.6, "linear"), (7.4, "linear"), (1.02, "cluster"),
+                                          (30.0, "geometric"), (2.0, "geometric")])
+def test_damping_decision_of_large_matrices(engine_lib, ratio, spread):
+    """From n = 64 up a positive definite F goes through the Lanczos test on
+    its Cholesky factor before the full eigenvalue test: the decision must be
+    the reference's (damp when the smallest |eigenvalue| is more than 8 below
+    the next) on both sides of the threshold, for a flat, a clustered and a
+    widely spread spectrum, and the results those of the restatement."""
+    from lyspeq_gb300 import lqg
+    rng = np.random.Generator(np.random.PCG64(11))
+    n = 200
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    if spread == "linear":
+        ev = np.linspace(1.0, 100.0, n)
+    elif spread == "cluster":
+        ev = 1.0 + 1e-3 * rng.random(n)
+        ev[-1] = 50.0
+    else:
+        ev = np.geomspace(1.0, 1e7, n)
+    ev = np.sort(ev)
+    ev[0] = ev[1] / ratio
+    f = (q * ev) @ q.T
+    f = 0.5 * (f + f.T)
+    fsum = 2.0 * np.triu(f)
+    dbt = rng.standard_normal((3, n))
+    g = lqg.fisher_solve(fsum, dbt)
+    o = P.newton_raphson_step(fsum, dbt)
+    assert g["damped"] == int(o["warn"]) == int(ratio > 8)
+    tol = 1e-14 * np.linalg.cond(f) ** (2 if ratio > 8 else 1)
+    assert G.rel_err(g["theta"], o["theta"]) < max(tol, 1e-10)
+
+
 def test_rejects_bad_shapes(engine_lib):
     from lyspeq_gb300 import lqg
     with pytest.raises(ValueError):
