@@ -397,11 +397,11 @@ int lqg_probe_fp64_rate(int device, double *tflops);
  *               LQG_CHUNK_OK first: nothing needs to start at zero.
  * The static scratch is shared by every call on a device: two calls in flight
  * at the same time (other streams, other host threads) race on it and give
- * wrong results; order them (one stream, or events).  The first call on each
- * device looks up the scratch address and sets a kernel attribute; make it
- * before any stream capture.  The address is kept for the life of the
- * process: resetting a device (cudaDeviceReset) while this library is loaded
- * is not supported. */
+ * wrong results; order them (one stream, or events).  Every call looks up
+ * the scratch address on the current device (no allocation); the first call
+ * on each device also sets a kernel attribute, so make it before any stream
+ * capture.  That attribute is kept for the life of the process: resetting a
+ * device (cudaDeviceReset) while this library is loaded is not supported. */
 int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave, const double *delta,
                        const double *ivar, int cont_logl_order, int cont_l_order, double *y,
                        int *status, void *stream);

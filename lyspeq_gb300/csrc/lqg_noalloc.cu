@@ -16,7 +16,6 @@
 #include "lqg_internal.cuh"
 
 #include <algorithm>
-#include <mutex>
 
 namespace lqg {
 
@@ -54,9 +53,6 @@ __global__ void k_noalloc_whiten(double *cov, int n, int ld, const double *ivar)
     }
 }
 
-std::mutex g_mu;
-void *g_scratch_ptr[64];   // per device, looked up once
-
 }  // namespace
 
 }  // namespace lqg
@@ -73,18 +69,12 @@ extern "C" int lqg_factor_noalloc(int n, int ld, double *cov, const double *wave
     if (cont_logl_order >= 0 || cont_l_order >= 0)
         nvec = 1 + (cont_logl_order > 0 ? cont_logl_order : 0) + (cont_l_order > 0 ? cont_l_order : 0);
     if (nvec > kMaxContVecs) return LQG_ERR_UNSUPPORTED;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return LQG_ERR_CUDA;
-    unsigned char *scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch_ptr[dev]) {
-            void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LQG_ERR_CUDA;
-            g_scratch_ptr[dev] = p;
-        }
-        scratch = static_cast<unsigned char *>(g_scratch_ptr[dev]);
-    }
+    // the scratch's address on the current device, looked up on every call
+    // (it allocates nothing, and a reset context reloads the module at
+    // another address)
+    void *sym = nullptr;
+    if (cudaGetSymbolAddress(&sym, g_noalloc_scratch) != cudaSuccess || !sym) return LQG_ERR_CUDA;
+    unsigned char *scratch = static_cast<unsigned char *>(sym);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // Offsets of the caller's buffers relative to the scratch base, which the
