@@ -7,9 +7,27 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <utility>
 #include <numeric>
 
 using namespace lqg;
+
+namespace {
+
+// Allocator whose value-initialisation leaves trivial elements unset: resize()
+// of the batch's host arrays then costs no fill, each element being written
+// once by the chunk it belongs to.
+template <class T>
+struct HostAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = HostAlloc<U>; };
+    HostAlloc() = default;
+    template <class U> HostAlloc(const HostAlloc<U> &) noexcept {}
+    template <class U> void construct(U *p) noexcept { ::new ((void *) p) U; }
+    template <class U, class... A> void construct(U *p, A &&...a) { ::new ((void *) p) U(std::forward<A>(a)...); }
+};
+template <class T> using HostVec = std::vector<T, HostAlloc<T>>;
+
+}  // namespace
 
 struct lqg_ctx {
     int device = 0;
@@ -43,11 +61,11 @@ struct lqg_ctx {
         double rw_sum;
     };
     std::vector<HostChunk> chunks;
-    std::vector<double> h_wave, h_delta, h_ivar, h_logw, h_sqw;
-    std::vector<float2> h_logw2, h_sqw2;
-    std::vector<double> h_sqiv, h_niv;
-    std::vector<float2> h_sqiv2;
-    std::vector<double> h_flogw, h_fsqw, h_rw;   // resolution-matrix grids and weights
+    HostVec<double> h_wave, h_delta, h_ivar, h_logw, h_sqw;
+    HostVec<float2> h_logw2, h_sqw2;
+    HostVec<double> h_sqiv, h_niv;
+    HostVec<float2> h_sqiv2;
+    HostVec<double> h_flogw, h_fsqw, h_rw;   // resolution-matrix grids and weights
     bool has_reso = false;
     bool pix_dirty = true;
     DevBuf d_wave, d_delta, d_ivar, d_logw, d_sqw, d_logw2, d_sqw2, d_sqiv, d_niv;
@@ -97,11 +115,18 @@ int set_err(lqg_ctx *ctx, int code, const std::string &msg) {
     return code;
 }
 
+// The median of the sorted values (stats::medianOfSortedArray,
+// mathtools/stats.cpp:8-16) from the order statistics n/2 and n/2 - 1, which
+// nth_element places without sorting the rest: the same values, so the same
+// result.
 double median_of(std::vector<double> v) {
-    std::sort(v.begin(), v.end());
-    size_t n = v.size();
+    const size_t n = v.size();
     if (n == 0) return -1;
-    return (n % 2 == 0) ? (v[n / 2 - 1] + v[n / 2]) / 2 : v[n / 2];
+    std::nth_element(v.begin(), v.begin() + n / 2, v.end());
+    const double upper = v[n / 2];
+    if (n % 2) return upper;
+    const double lower = *std::max_element(v.begin(), v.begin() + n / 2);
+    return (lower + upper) / 2;
 }
 
 // bins::findRedshiftBin, core/global_numbers.cpp:344-355
@@ -302,161 +327,218 @@ extern "C" int lqg_batch_size(const lqg_ctx *ctx) { return ctx ? (int) ctx->chun
 
 namespace {
 
+// One chunk of an lqg_batch_add / lqg_batch_add_reso call after Chunk::Chunk:
+// its status, its description and (resolution matrix) its weights and grid.
+struct ChunkSetup {
+    int st = LQG_CHUNK_OK;
+    int64_t a = 0, b = 0;        // pixel range after the masked edges are cut
+    lqg_ctx::HostChunk hc{};
+    std::vector<double> rw, fgrid;   // the diagonal form's weights, built here; the grid
+    const double *rw_src = nullptr;  // the weights: the caller's rows (oversampled) or rw
+    size_t rw_len = 0;
+};
+
+// Chunk::Chunk for chunk c.  resomat == NULL: table lookup by (R, dv).
+// Otherwise the chunk's resolution matrix, per pixel: nelem weights of its
+// oversampled row (reso_os > 0) or its column's entries on the ndiags = nelem
+// diagonals (reso_os <= 0).  Reads the context, writes only `out`.
+void setup_chunk(const lqg_ctx *ctx, int c, const int64_t *offsets, const double *lambda,
+                 const double *delta, const double *ivar, const int *r_fwhm, int reso_os, int reso_nelem,
+                 const double *resomat, ChunkSetup &out) {
+    const double max_v = ctx->opts.max_forest_length, min_v = 0.90 / 2 * max_v;
+    const bool reso = resomat != nullptr;
+    lqg_ctx::HostChunk &hc = out.hc;
+    std::vector<double> &fgrid = out.fgrid;
+    int64_t a = offsets[c], b = offsets[c + 1];
+    int st = LQG_CHUNK_OK;
+    // QSOFile::_cutMaskedBoundary (io/qso_file.cpp:139-157)
+    while (a < b && ivar[a] == 0) ++a;
+    while (b > a && ivar[b - 1] == 0) --b;
+    int n = (int) (b - a);
+    if (n <= 0) st = LQG_CHUNK_EMPTY;
+    for (int64_t i = a; st == LQG_CHUNK_OK && i < b; ++i)
+        if (!std::isfinite(lambda[i]) || !std::isfinite(delta[i]) || !std::isfinite(ivar[i]) ||
+            ivar[i] < 0 || !(lambda[i] > 0))
+            st = LQG_CHUNK_BAD_INPUT;
+    if (st == LQG_CHUNK_OK && n > kMaxPixels) st = LQG_CHUNK_TOO_LARGE;
+    if (st == LQG_CHUNK_OK && n < 2) st = LQG_CHUNK_SHORT;
+    if (st == LQG_CHUNK_OK) {
+        int realsize = 0;
+        for (int64_t i = a; i < b; ++i) realsize += ivar[i] != 0;
+        // QSOFile::recalcDvDLam (io/qso_file.cpp:325-329)
+        std::vector<double> dvs(n - 1);
+        for (int i = 0; i < n - 1; ++i) dvs[i] = std::log(lambda[a + i + 1] / lambda[a + i]) * kSpeedOfLight;
+        double dv = median_of(dvs);
+        // Chunk::_copyQSOFile short-chunk rule (core/chunk_estimate.cpp:173-187)
+        double lenv = kSpeedOfLight * std::log(lambda[b - 1] / lambda[a]);
+        int minnopix = (int) (lenv / ctx->opts.max_mean_pixel_size);
+        if (realsize < minnopix || lenv < min_v) st = LQG_CHUNK_SHORT;
+        // SQLookupTable::findSpecResIndex (core/sq_table.cpp:388-397); with a
+        // resolution matrix RES_INDEX = 0 (core/chunk_estimate.cpp:189-193)
+        int res = reso ? 0 : -1;
+        if (st == LQG_CHUNK_OK && !reso) {
+            double rounded = std::round(dv * 10) / 10;
+            for (int t = 0; t < ctx->n_tables; ++t)
+                if (ctx->r_fwhm[t] == r_fwhm[c] && std::fabs(rounded - ctx->tdv[t]) < 0.01) { res = t; break; }
+            if (res < 0) st = LQG_CHUNK_NO_TABLE;
+        }
+        if (st == LQG_CHUNK_OK) {
+            double zmin = lambda[a] / kLyaRest - 1, zmax = lambda[b - 1] / kLyaRest - 1;
+            // _getMaxKindex (core/chunk_estimate.cpp:32-39)
+            int kup = (int) (std::lower_bound(ctx->k_centers.begin(), ctx->k_centers.end(),
+                                              0.85 * (kPi / dv)) - ctx->k_centers.begin());
+            int zl = find_redshift_bin(ctx, zmin), zu = find_redshift_bin(ctx, zmax);
+            // Chunk::_setNQandFisherIndex (core/chunk_estimate.cpp:240-257)
+            int nq = zu - zl + 1, fis = ctx->nk * zl;
+            if (ctx->triangular) {
+                if (zl >= 0 && zl < ctx->nz && zmin < ctx->z_centers[zl] && zl != 0) { ++nq; fis -= ctx->nk; }
+                if (zu >= 0 && zu < ctx->nz && ctx->z_centers[zu] < zmax && zu < ctx->nz - 1) ++nq;
+            }
+            nq *= ctx->nk;
+            if (zl < 0 || zu >= ctx->nz || fis < 0 || fis + nq > ctx->nkz || kup <= 0)
+                st = LQG_CHUNK_OUT_OF_RANGE;
+            hc.n = n;
+            hc.ld = (int) align_up(n, kPad);
+            hc.nq = nq;
+            hc.kbin_upp = kup;
+            hc.ns = (nq / ctx->nk) * kup;
+            hc.fis = fis;
+            hc.res = res;
+            hc.zlow = zl;
+            hc.zupp = zu;
+            if (st == LQG_CHUNK_OK && hc.ns + 2 > 128 * kMaxGramBlocks)
+                st = LQG_CHUNK_TOO_LARGE;
+        }
+    }
+    // resolution matrix of the chunk: weights per coarse row and its grid
+    if (st == LQG_CHUNK_OK && reso) {
+        const int nel = reso_nelem;
+        hc.nelem = nel;
+        if (reso_os > 0) {
+            // OversampledMatrix rows; grid of Chunk::_initMatrices
+            // (core/chunk_estimate.cpp:927-938): w_0 + (p - nelem/2) dlambda / LYA / os,
+            // dlambda the chunk's median pixel width (io/qso_file.cpp:86-88, 325-329)
+            hc.os = reso_os;
+            hc.sh = 0;
+            hc.nf = n * reso_os + nel - 1;
+            out.rw_src = resomat + a * nel;
+            out.rw_len = (size_t) n * nel;
+            std::vector<double> dl(n - 1);
+            for (int i = 0; i < n - 1; ++i) dl[i] = lambda[a + i + 1] - lambda[a + i];
+            const double fine = median_of(dl) / kLyaRest / reso_os, w0 = lambda[a] / kLyaRest;
+            const int disp = nel / 2;
+            fgrid.resize(hc.nf);
+            for (int p = 0; p < hc.nf; ++p) fgrid[p] = w0 + (p - disp) * fine;
+        } else {
+            // DiaMatrix: row r has entries at columns r + off, off = a - nel/2,
+            // held on diagonal d = nel - 1 - a (mathtools/matrix_helper.cpp:503-520,
+            // 684-813); columns outside the chunk drop out
+            hc.os = 1;
+            hc.sh = nel / 2;
+            hc.nf = n;
+            std::vector<double> &rw = out.rw;
+            rw.assign((size_t) n * nel, 0.0);
+            for (int r = 0; r < n; ++r)
+                for (int k = 0; k < nel; ++k) {
+                    const int col = r - hc.sh + k;
+                    if (col >= 0 && col < n) rw[(size_t) r * nel + k] = resomat[(a + col) * nel + (nel - 1 - k)];
+                }
+            out.rw_src = rw.data();
+            out.rw_len = rw.size();
+            for (int64_t i = a; i < b; ++i) fgrid.push_back(lambda[i] / kLyaRest);
+        }
+        hc.rw_sum = 0;
+        for (int r = 0; r < n; ++r) {
+            double sum = 0;
+            for (int k = 0; k < nel; ++k) {
+                const double w = out.rw_src[(size_t) r * nel + k];
+                if (!std::isfinite(w)) st = LQG_CHUNK_BAD_INPUT;
+                sum += std::fabs(w);
+            }
+            hc.rw_sum = std::max(hc.rw_sum, sum);
+        }
+        for (double w : fgrid)
+            if (!(w > 0) || !std::isfinite(w)) st = LQG_CHUNK_BAD_INPUT;
+    }
+    out.st = st;
+    out.a = a;
+    out.b = b;
+}
+
 // Chunk::Chunk for every chunk of an lqg_batch_add / lqg_batch_add_reso call.
-// resomat == NULL: table lookup by (R, dv).  Otherwise the chunk's resolution
-// matrix, per pixel: nelem weights of its oversampled row (reso_os > 0) or
-// its column's entries on the ndiags = nelem diagonals (reso_os <= 0).
+// The chunks are set up and their pixel arrays filled on the host's cores;
+// the accepted ones join the batch in input order, each at the offsets a
+// serial walk over the call's chunks gives them.  Offsets that decrease
+// reject the whole call before anything is added.
 int add_chunks(lqg_ctx *ctx, int n_chunks, const int64_t *offsets, const double *lambda,
                const double *delta, const double *ivar, const int *r_fwhm, int reso_os, int reso_nelem,
                const double *resomat, int *status_out) {
-    const double max_v = ctx->opts.max_forest_length, min_v = 0.90 / 2 * max_v;
+    for (int c = 0; c < n_chunks; ++c)
+        if (offsets[c + 1] < offsets[c]) return set_err(ctx, LQG_ERR_ARG, "lqg_batch_add: offsets not increasing");
     const bool reso = resomat != nullptr;
+    std::vector<ChunkSetup> set(n_chunks);
+    host_parallel_for(n_chunks, 16, [&](int c) {
+        setup_chunk(ctx, c, offsets, lambda, delta, ivar, r_fwhm, reso_os, reso_nelem, resomat, set[c]);
+    });
+    std::vector<int> accepted;
+    size_t np = ctx->h_wave.size(), nfp = ctx->h_flogw.size(), nrw = ctx->h_rw.size();
     for (int c = 0; c < n_chunks; ++c) {
-        int64_t a = offsets[c], b = offsets[c + 1];
-        int st = LQG_CHUNK_OK;
-        if (b < a) return set_err(ctx, LQG_ERR_ARG, "lqg_batch_add: offsets not increasing");
-        // QSOFile::_cutMaskedBoundary (io/qso_file.cpp:139-157)
-        while (a < b && ivar[a] == 0) ++a;
-        while (b > a && ivar[b - 1] == 0) --b;
-        int n = (int) (b - a);
-        if (n <= 0) st = LQG_CHUNK_EMPTY;
-        for (int64_t i = a; st == LQG_CHUNK_OK && i < b; ++i)
-            if (!std::isfinite(lambda[i]) || !std::isfinite(delta[i]) || !std::isfinite(ivar[i]) ||
-                ivar[i] < 0 || !(lambda[i] > 0))
-                st = LQG_CHUNK_BAD_INPUT;
-        if (st == LQG_CHUNK_OK && n > kMaxPixels) st = LQG_CHUNK_TOO_LARGE;
-        if (st == LQG_CHUNK_OK && n < 2) st = LQG_CHUNK_SHORT;
-        lqg_ctx::HostChunk hc{};
-        if (st == LQG_CHUNK_OK) {
-            int realsize = 0;
-            for (int64_t i = a; i < b; ++i) realsize += ivar[i] != 0;
-            // QSOFile::recalcDvDLam (io/qso_file.cpp:325-329)
-            std::vector<double> dvs(n - 1);
-            for (int i = 0; i < n - 1; ++i) dvs[i] = std::log(lambda[a + i + 1] / lambda[a + i]) * kSpeedOfLight;
-            double dv = median_of(dvs);
-            // Chunk::_copyQSOFile short-chunk rule (core/chunk_estimate.cpp:173-187)
-            double lenv = kSpeedOfLight * std::log(lambda[b - 1] / lambda[a]);
-            int minnopix = (int) (lenv / ctx->opts.max_mean_pixel_size);
-            if (realsize < minnopix || lenv < min_v) st = LQG_CHUNK_SHORT;
-            // SQLookupTable::findSpecResIndex (core/sq_table.cpp:388-397); with a
-            // resolution matrix RES_INDEX = 0 (core/chunk_estimate.cpp:189-193)
-            int res = reso ? 0 : -1;
-            if (st == LQG_CHUNK_OK && !reso) {
-                double rounded = std::round(dv * 10) / 10;
-                for (int t = 0; t < ctx->n_tables; ++t)
-                    if (ctx->r_fwhm[t] == r_fwhm[c] && std::fabs(rounded - ctx->tdv[t]) < 0.01) { res = t; break; }
-                if (res < 0) st = LQG_CHUNK_NO_TABLE;
-            }
-            if (st == LQG_CHUNK_OK) {
-                double zmin = lambda[a] / kLyaRest - 1, zmax = lambda[b - 1] / kLyaRest - 1;
-                // _getMaxKindex (core/chunk_estimate.cpp:32-39)
-                int kup = (int) (std::lower_bound(ctx->k_centers.begin(), ctx->k_centers.end(),
-                                                  0.85 * (kPi / dv)) - ctx->k_centers.begin());
-                int zl = find_redshift_bin(ctx, zmin), zu = find_redshift_bin(ctx, zmax);
-                // Chunk::_setNQandFisherIndex (core/chunk_estimate.cpp:240-257)
-                int nq = zu - zl + 1, fis = ctx->nk * zl;
-                if (ctx->triangular) {
-                    if (zl >= 0 && zl < ctx->nz && zmin < ctx->z_centers[zl] && zl != 0) { ++nq; fis -= ctx->nk; }
-                    if (zu >= 0 && zu < ctx->nz && ctx->z_centers[zu] < zmax && zu < ctx->nz - 1) ++nq;
-                }
-                nq *= ctx->nk;
-                if (zl < 0 || zu >= ctx->nz || fis < 0 || fis + nq > ctx->nkz || kup <= 0)
-                    st = LQG_CHUNK_OUT_OF_RANGE;
-                hc.n = n;
-                hc.ld = (int) align_up(n, kPad);
-                hc.nq = nq;
-                hc.kbin_upp = kup;
-                hc.ns = (nq / ctx->nk) * kup;
-                hc.fis = fis;
-                hc.res = res;
-                hc.zlow = zl;
-                hc.zupp = zu;
-                if (st == LQG_CHUNK_OK && hc.ns + 2 > 128 * kMaxGramBlocks)
-                    st = LQG_CHUNK_TOO_LARGE;
-            }
-        }
-        // resolution matrix of the chunk: weights per coarse row and its grid
-        std::vector<double> rw, fgrid;
-        if (st == LQG_CHUNK_OK && reso) {
-            const int nel = reso_nelem;
-            hc.nelem = nel;
-            if (reso_os > 0) {
-                // OversampledMatrix rows; grid of Chunk::_initMatrices
-                // (core/chunk_estimate.cpp:927-938): w_0 + (p - nelem/2) dlambda / LYA / os,
-                // dlambda the chunk's median pixel width (io/qso_file.cpp:86-88, 325-329)
-                hc.os = reso_os;
-                hc.sh = 0;
-                hc.nf = n * reso_os + nel - 1;
-                rw.assign(resomat + a * nel, resomat + b * nel);
-                std::vector<double> dl(n - 1);
-                for (int i = 0; i < n - 1; ++i) dl[i] = lambda[a + i + 1] - lambda[a + i];
-                const double fine = median_of(dl) / kLyaRest / reso_os, w0 = lambda[a] / kLyaRest;
-                const int disp = nel / 2;
-                fgrid.resize(hc.nf);
-                for (int p = 0; p < hc.nf; ++p) fgrid[p] = w0 + (p - disp) * fine;
-            } else {
-                // DiaMatrix: row r has entries at columns r + off, off = a - nel/2,
-                // held on diagonal d = nel - 1 - a (mathtools/matrix_helper.cpp:503-520,
-                // 684-813); columns outside the chunk drop out
-                hc.os = 1;
-                hc.sh = nel / 2;
-                hc.nf = n;
-                rw.assign((size_t) n * nel, 0.0);
-                for (int r = 0; r < n; ++r)
-                    for (int k = 0; k < nel; ++k) {
-                        const int col = r - hc.sh + k;
-                        if (col >= 0 && col < n) rw[(size_t) r * nel + k] = resomat[(a + col) * nel + (nel - 1 - k)];
-                    }
-                for (int64_t i = a; i < b; ++i) fgrid.push_back(lambda[i] / kLyaRest);
-            }
-            hc.rw_sum = 0;
-            for (int r = 0; r < n; ++r) {
-                double sum = 0;
-                for (int k = 0; k < nel; ++k) {
-                    const double w = rw[(size_t) r * nel + k];
-                    if (!std::isfinite(w)) st = LQG_CHUNK_BAD_INPUT;
-                    sum += std::fabs(w);
-                }
-                hc.rw_sum = std::max(hc.rw_sum, sum);
-            }
-            for (double w : fgrid)
-                if (!(w > 0) || !std::isfinite(w)) st = LQG_CHUNK_BAD_INPUT;
-        }
-        if (status_out) status_out[c] = st;
-        if (st != LQG_CHUNK_OK) continue;
+        ChunkSetup &u = set[c];
+        if (status_out) status_out[c] = u.st;
+        if (u.st != LQG_CHUNK_OK) continue;
+        lqg_ctx::HostChunk &hc = u.hc;
         if (reso) {
             ctx->has_reso = true;
-            hc.fpix = (int64_t) ctx->h_flogw.size();
-            hc.rw_off = (int64_t) ctx->h_rw.size();
-            for (double w : fgrid) {
-                ctx->h_flogw.push_back(std::log(w));
-                ctx->h_fsqw.push_back(std::sqrt(w));
-            }
-            ctx->h_rw.insert(ctx->h_rw.end(), rw.begin(), rw.end());
+            hc.fpix = (int64_t) nfp;
+            hc.rw_off = (int64_t) nrw;
+            nfp += u.fgrid.size();
+            nrw += u.rw_len;
         }
-        // SmoothNoiseWeights: C takes the smoothed ivar, N the raw one
-        std::vector<double> ivc(ivar + a, ivar + b);
-        if (ctx->opts.smooth_noise_weights >= 0)
-            smooth_ivar(n, ivar + a, ctx->opts.smooth_noise_weights, ivc.data());
         hc.input_index = c;
-        hc.pix = (int64_t) ctx->h_wave.size();
+        hc.pix = (int64_t) np;
+        np += (size_t) (u.b - u.a);
         hc.res_off = ctx->results_size;
         ctx->results_size += 3 * hc.nq + (int64_t) hc.nq * hc.nq;
-        for (int64_t i = a; i < b; ++i) {
-            double w = lambda[i] / kLyaRest;   // Chunk::_copyQSOFile divides by LYA_REST
-            ctx->h_wave.push_back(w);
-            ctx->h_logw.push_back(std::log(w));
-            ctx->h_sqw.push_back(std::sqrt(w));
-            ctx->h_logw2.push_back(split_ff(ctx->h_logw.back()));
-            ctx->h_sqw2.push_back(split_ff(ctx->h_sqw.back()));
-            ctx->h_delta.push_back(delta[i]);
-            ctx->h_ivar.push_back(ivc[i - a]);
-            ctx->h_sqiv.push_back(std::sqrt(ivc[i - a]));
-            ctx->h_sqiv2.push_back(split_ff(ctx->h_sqiv.back()));
-            ctx->h_niv.push_back(ivar[i] != 0 ? 1.0 / ivar[i] : 0.0);
-        }
-        ctx->chunks.push_back(hc);
+        accepted.push_back(c);
     }
+    for (auto *v : {&ctx->h_wave, &ctx->h_logw, &ctx->h_sqw, &ctx->h_delta, &ctx->h_ivar, &ctx->h_sqiv,
+                    &ctx->h_niv})
+        v->resize(np);
+    for (auto *v : {&ctx->h_logw2, &ctx->h_sqw2, &ctx->h_sqiv2}) v->resize(np);
+    ctx->h_flogw.resize(nfp);
+    ctx->h_fsqw.resize(nfp);
+    ctx->h_rw.resize(nrw);
+    host_parallel_for((int) accepted.size(), 8, [&](int j) {
+        const ChunkSetup &u = set[accepted[j]];
+        const lqg_ctx::HostChunk &hc = u.hc;
+        if (reso) {
+            for (size_t p = 0; p < u.fgrid.size(); ++p) {
+                ctx->h_flogw[hc.fpix + p] = std::log(u.fgrid[p]);
+                ctx->h_fsqw[hc.fpix + p] = std::sqrt(u.fgrid[p]);
+            }
+            std::copy(u.rw_src, u.rw_src + u.rw_len, ctx->h_rw.begin() + hc.rw_off);
+        }
+        // SmoothNoiseWeights: C takes the smoothed ivar, N the raw one
+        const int64_t a = u.a, n = u.b - u.a;
+        std::vector<double> ivc(ivar + a, ivar + u.b);
+        if (ctx->opts.smooth_noise_weights >= 0)
+            smooth_ivar((int) n, ivar + a, ctx->opts.smooth_noise_weights, ivc.data());
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t q = hc.pix + i;
+            const double w = lambda[a + i] / kLyaRest;   // Chunk::_copyQSOFile divides by LYA_REST
+            ctx->h_wave[q] = w;
+            ctx->h_logw[q] = std::log(w);
+            ctx->h_sqw[q] = std::sqrt(w);
+            ctx->h_logw2[q] = split_ff(ctx->h_logw[q]);
+            ctx->h_sqw2[q] = split_ff(ctx->h_sqw[q]);
+            ctx->h_delta[q] = delta[a + i];
+            ctx->h_ivar[q] = ivc[i];
+            ctx->h_sqiv[q] = std::sqrt(ivc[i]);
+            ctx->h_sqiv2[q] = split_ff(ctx->h_sqiv[q]);
+            ctx->h_niv[q] = ivar[a + i] != 0 ? 1.0 / ivar[a + i] : 0.0;
+        }
+    });
+    for (int c : accepted) ctx->chunks.push_back(set[c].hc);
     ctx->pix_dirty = true;
     ctx->have_results = false;
     ctx->batch_version++;

@@ -1,12 +1,14 @@
 // Internal declarations shared by the engine's translation units.
 #pragma once
 
+#include <algorithm>
 #include <atomic>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/lqg.h"
@@ -259,6 +261,30 @@ inline bool once_per_device(std::atomic<unsigned long long> &done, Fn fn) {
     if (fn(dev) != cudaSuccess) return false;
     if (bit) done.fetch_or(bit, std::memory_order_release);
     return true;
+}
+
+// fn(i) for i in [0, n) on up to 16 host threads (the calling one included),
+// handed out `grain` at a time; serial when n <= grain.  fn must not throw
+// and must write no state that another i writes.
+template <class Fn>
+inline void host_parallel_for(int n, int grain, Fn fn) {
+    if (n <= 0) return;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nt = (int) std::min<long long>({16ll, hw ? (long long) hw : 1ll, (n + (long long) grain - 1) / grain});
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    auto worker = [&] {
+        for (int i0; (i0 = next.fetch_add(grain, std::memory_order_relaxed)) < n;)
+            for (int i = i0; i < std::min(n, i0 + grain); ++i) fn(i);
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &th : pool) th.join();
 }
 
 bool tc_available();
