@@ -1501,7 +1501,18 @@ int iterate_subset(lqg_ctx *ctx, const std::vector<int> &subset, int mode, doubl
     full.swap(ctx->chunks);
     for (int i : subset) ctx->chunks.push_back(full[i]);
     const uint64_t ver = ctx->batch_version;
-    ctx->batch_version = ((uint64_t) 1 << 62) ^ (uint64_t) subset.front() ^ ((uint64_t) subset.size() << 32);
+    // the sample's own batch version, for the graph cache: a hash (FNV-1a) of
+    // the batch's version and the sample's indices, so that repeats of one
+    // sample replay its graph and no other sample or batch matches it; bit 62
+    // keeps it apart from the counter of real batches
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](uint64_t v) {
+        for (int k = 0; k < 8; ++k) { h ^= (v >> (8 * k)) & 0xff; h *= 1099511628211ull; }
+    };
+    mix(ver);
+    mix(subset.size());
+    for (int i : subset) mix((uint64_t) i);
+    ctx->batch_version = ((uint64_t) 1 << 62) | (h & (((uint64_t) 1 << 62) - 1));
     int rc = enqueue_iteration(ctx, nullptr, mode, nullptr);
     if (rc == LQG_OK) rc = finish_pending(ctx);
     if (ms) *ms = ctx->timings[7];
