@@ -368,6 +368,15 @@ int lqg_last_wave_count(const lqg_ctx *ctx);
  * waits); tests use a tiny limit to exercise that path without a fault. */
 int lqg_set_wait_limit(lqg_ctx *ctx, double seconds);
 
+/* on = 1: the results of later iterations are those of lyspeq built with
+ * FISHER_OPTIMIZATION (./configure --enable-fisher-optimization): of each
+ * chunk's Fisher matrix only the pairs of local kz indices i <= j with
+ * j - i <= 5 or |j - i - NUMBER_OF_K_BANDS| <= 2 are kept, the others are 0
+ * (Chunk::oneQSOiteration, core/chunk_estimate.cpp:823-827), in the per-chunk
+ * results, the global sum and the bootstraps alike.  on = 0 (the default):
+ * full matrices.  LQG_ERR_ARG for any other value. */
+int lqg_set_fisher_optimization(lqg_ctx *ctx, int on);
+
 /* Measured FP64 (DFMA) throughput of device `device` in TFLOP/s: independent
  * FMA chains on every SM, best of five timed launches.  The denominator of the
  * FP64 kernels' rooflines; no counterpart in the reference. */

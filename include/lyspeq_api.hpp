@@ -410,6 +410,10 @@ public:
         if (lqg_ctx_create(&c, &b, &tb, &o, device) != LQG_OK)
             throw std::runtime_error("lqg_ctx_create failed (tables, binning or CUDA device)");
         ctx_.reset(c);
+#ifdef FISHER_OPTIMIZATION
+        // the caller's build option (./configure --enable-fisher-optimization)
+        lqg_set_fisher_optimization(c, 1);
+#endif
         for (int i = 0; i < 3; ++i) {
             dbt_estimate_sum_before_fisher_vector.emplace_back(new double[nkz_]());
             dbt_estimate_fisher_weighted_vector.emplace_back(new double[nkz_]());

@@ -45,7 +45,32 @@ __global__ void k_accumulate(const ChunkDesc *chunks, int n_chunks, const double
     else if (e < total) dbt[which * nkz + r] = acc;
 }
 
+// lyspeq built with FISHER_OPTIMIZATION (./configure --enable-fisher-optimization)
+// computes of a chunk's Fisher matrix only the pairs i <= j of local kz indices
+// with j - i <= 5 or |j - i - Nk| <= 2 (core/chunk_estimate.cpp:823-827); the
+// others stay 0.  One block per chunk zeroes them in the chunk's results
+// (upper triangle; the lower one is 0 already), before the accumulation.
+__global__ void k_fisher_band(const ChunkDesc *chunks, int n_chunks, double *results, int64_t results_elems,
+                              int nk) {
+    const int c = blockIdx.x;
+    if (c >= n_chunks) return;
+    const int nq = chunks[c].nq;
+    const int64_t off = chunks[c].res_off + 3 * (int64_t) nq;
+    if (nq <= 0 || chunks[c].res_off < 0 || off + (int64_t) nq * nq > results_elems) return;
+    double *f = results + off;
+    for (int64_t e = threadIdx.x; e < (int64_t) nq * nq; e += blockDim.x) {
+        const int diff = (int) (e % nq) - (int) (e / nq);
+        if (diff > 5 && abs(diff - nk) > 2) f[e] = 0.0;
+    }
+}
+
 }  // namespace
+
+void launch_fisher_band(const ChunkDesc *chunks, int n_chunks, double *results, int64_t results_elems, int nk,
+                        cudaStream_t st) {
+    if (n_chunks <= 0) return;
+    k_fisher_band<<<n_chunks, 256, 0, st>>>(chunks, n_chunks, results, results_elems, nk);
+}
 
 void launch_accumulate(const ChunkDesc *chunks, int n_chunks, const double *results,
                        const int *status, int nkz, double *fisher, double *dbt, cudaStream_t st) {

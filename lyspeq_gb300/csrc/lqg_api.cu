@@ -46,6 +46,7 @@ struct lqg_ctx {
     DevBuf d_deriv, d_deriv_f, d_deriv_ff, d_signal, d_signal_ff, d_bins;
     lqg_opts opts{};
     uint64_t wait_ns = 0;   // lqg_set_wait_limit; 0: the kernels' 2 s
+    int fisher_band = 0;    // lqg_set_fisher_optimization: banded chunk Fisher matrices
     // LQG_PRECISION_MIXED_AUTO: per padded size ld, the mixed form, the drain
     // interval of the products and the Gram's K split (lqg_autotune)
     struct Tune {
@@ -581,6 +582,8 @@ extern "C" int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info) {
 namespace lqg {
 void launch_accumulate(const ChunkDesc *chunks, int n_chunks, const double *results,
                        const int *status, int nkz, double *fisher, double *dbt, cudaStream_t st);
+void launch_fisher_band(const ChunkDesc *chunks, int n_chunks, double *results, int64_t results_elems, int nk,
+                        cudaStream_t st);
 }
 
 namespace {
@@ -1262,6 +1265,11 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
         }
         eacc = nev++;
         record_event(pool_event(ctx, eacc), st);
+        if (ctx->fisher_band) {
+            launch_fisher_band(ctx->d_meta.as<ChunkDesc>(), nb, ctx->d_results.as<double>(), ctx->results_size,
+                               ctx->nk, st);
+            ctx->launches++;
+        }
         launch_accumulate(ctx->d_meta.as<ChunkDesc>(), nb, ctx->d_results.as<double>(), ctx->d_status.as<int>(),
                           ctx->nkz, ctx->d_fisher.as<double>(), ctx->d_dbt.as<double>(), st);
         ctx->launches++;
@@ -1277,7 +1285,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
         (uintptr_t) ctx->d_status.p, (uintptr_t) ctx->d_meta.p, (uintptr_t) ctx->d_wave.p, (uintptr_t) ctx->d_flogw.p,
         (uintptr_t) ctx->d_rw.p, (uintptr_t) ctx->d_sqiv2.p, (uintptr_t) ctx->d_niv.p, (uintptr_t) ctx->d_ttab.p,
         (uintptr_t) ctx->d_ttab_ff.p, (uintptr_t) ctx->wait_ns, (uintptr_t) n_combos, (uintptr_t) ctx->d_rtab.p,
-        (uintptr_t) rtab_n, (uintptr_t) n_rks};
+        (uintptr_t) rtab_n, (uintptr_t) n_rks, (uintptr_t) ctx->fisher_band};
     // the launch plan: grid sizes and the by-value kernel arguments follow from these
     for (const auto &g : groups) {
         key.insert(key.end(), {(uintptr_t) g.members.size(), (uintptr_t) g.max_ld, (uintptr_t) g.fws_bytes,
@@ -1482,6 +1490,12 @@ extern "C" int lqg_last_wave_count(const lqg_ctx *ctx) { return ctx ? ctx->waves
 extern "C" int lqg_set_wait_limit(lqg_ctx *ctx, double seconds) {
     if (!ctx || !(seconds >= 0.0) || seconds > 60.0) return LQG_ERR_ARG;
     ctx->wait_ns = (uint64_t) (seconds * 1e9);
+    return LQG_OK;
+}
+
+extern "C" int lqg_set_fisher_optimization(lqg_ctx *ctx, int on) {
+    if (!ctx || (on != 0 && on != 1)) return LQG_ERR_ARG;
+    ctx->fisher_band = on;
     return LQG_OK;
 }
 

@@ -28,7 +28,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients",
            "lqg_resomat_smooth", "lqg_fisher_solve_n", "lqg_set_wait_limit", "lqg_factor_noalloc",
            "lqg_probe_fp64_rate", "lqg_nr_iteration_async", "lqg_sync", "lqg_autotune", "lqg_tuning_get",
-           "lqg_tuning_set"]
+           "lqg_tuning_set", "lqg_set_fisher_optimization"]
 
 
 class LqgBins(C.Structure):
@@ -95,6 +95,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_last_launch_count.argtypes = [vp]
     lib.lqg_last_wave_count.argtypes = [vp]
     lib.lqg_set_wait_limit.argtypes = [vp, C.c_double]
+    lib.lqg_set_fisher_optimization.argtypes = [vp, C.c_int]
     lib.lqg_factor_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, vp]
     lib.lqg_probe_fp64_rate.argtypes = [C.c_int, dp]
     lib.lqg_nr_iteration_async.argtypes = [vp, dp, C.c_int, vp]
@@ -335,6 +336,10 @@ class Engine:
     def set_wait_limit(self, seconds):
         """Limit of the tensor-core kernels' waits (0: the default 2 s)."""
         self._check(self.lib.lqg_set_wait_limit(self.h, float(seconds)), "lqg_set_wait_limit")
+
+    def set_fisher_optimization(self, on=True):
+        """Banded chunk Fisher matrices, as lyspeq built with FISHER_OPTIMIZATION."""
+        self._check(self.lib.lqg_set_fisher_optimization(self.h, 1 if on else 0), "lqg_set_fisher_optimization")
 
 
 def probe_fp64_rate(device=0):

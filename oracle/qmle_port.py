@@ -40,6 +40,7 @@ class Settings:
     smooth_noise_weights: int = -1   # SmoothNoiseWeights (mathtools/smoother.hpp:8-9)
     redshift_growth: bool = False    # RedshiftGrowthOn > 0 (core/global_numbers.cpp:127)
     growth_b: float = 0.0            # FIDUCIAL_PD13_PARAMS.B
+    fisher_optimization: bool = False   # built with -DFISHER_OPTIMIZATION (configure --enable-fisher-optimization)
 
     @property
     def max_forest_length_v(self):
@@ -708,6 +709,11 @@ def chunk_iteration(ch: ChunkData, bins, tv: TableView, theta, settings, compute
         f = at @ a2.T                              # F_ij = <A_i^T, A_j>
         idx = np.array(stored)
         fu = np.triu(f)
+        if settings.fisher_optimization:
+            # only the bands |j - i| <= 5 and |j - i - Nk| <= 2 of the local kz
+            # indices are computed, the rest stays 0 (core/chunk_estimate.cpp:823-827)
+            diff = idx[None, :] - idx[:, None]
+            fu = np.where((diff > 5) & (np.abs(diff - bins.nk) > 2), 0.0, fu)
         fisher[np.ix_(idx, idx)] = fu
     return d, b, t, fisher
 

@@ -22,6 +22,7 @@ from oracle.refsrc import reference_root
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 DRIVER = os.path.join(REF_DIR, "chunk_driver")
+DRIVER_FOPT = os.path.join(REF_DIR, "chunk_driver_fopt")   # built with -DFISHER_OPTIMIZATION
 LYAPOWER = os.path.join(REF_DIR, "LyaPowerEstimate")
 REFERENCE_PY = os.path.join(reference_root(), "py")   # lyspeq's own helper scripts (smoothing)
 
@@ -171,14 +172,14 @@ def read_iteration(path: str) -> RefIteration:
 
 def run_driver(config: str, out: str, pixels: bool = True, threads: int | None = None,
                reso: bool = False, boots: int = 0, iterate: bool = False,
-               boot_complete: bool = False) -> RefDump:
+               boot_complete: bool = False, fisher_optimization: bool = False) -> RefDump:
     env = dict(os.environ)
     env.setdefault("OPENBLAS_NUM_THREADS", "1")
     # One OpenMP thread: with more, Chunk::_applyRedshiftInterp races on the
     # shared `low`/`tmp` bounds (core/chunk_estimate.cpp:486, 512-516) and the
     # redshift weights of some rows come out wrong from run to run.
     env["OMP_NUM_THREADS"] = str(threads or 1)
-    args = [DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else []) \
+    args = [DRIVER_FOPT if fisher_optimization else DRIVER, config, out] + ([] if pixels else ["--no-pixels"]) + (["--reso"] if reso else []) \
         + (["--boot", str(boots)] if boots else []) + (["--boot-complete"] if boot_complete else []) \
         + (["--iterate"] if iterate else [])
     if iterate:

@@ -62,10 +62,16 @@ CASES = {
     "tiny_tophat": ("tiny", None, (1, -1), 0.0, None),
     # TurnOffBaseline: C without the fiducial signal, no t trace
     "tiny_nosfid": ("tiny", None, (1, -1), 0.0, None),
+    # the reference built with --enable-fisher-optimization (-DFISHER_OPTIMIZATION):
+    # only the Fisher bands |dj| <= 5 and |dj - Nk| <= 2 are computed
+    "desi_fopt": ("desi", 6, (1, -1), 0.0, None),
 }
 
 # cases whose redshift bins are top hats instead of triangles
 TOPHAT = {"tiny_tophat"}
+
+# cases run by the reference built with FISHER_OPTIMIZATION
+FOPT = {"desi_fopt"}
 
 # config keys set for a case: SmoothNoiseWeights and RedshiftGrowthOn
 # (the growth exponent is the fiducial FiducialRedshiftPower)
@@ -113,7 +119,8 @@ def make_case(name, spec):
                     text += f"{key} {val}\n"
             open(cfg, "w").write(text)
         dump = refdump.run_driver(cfg, os.path.join(tmp, "dump.bin"), reso=w.reso, boots=boots,
-                                  iterate=iters > 1, boot_complete=name.endswith("_complete"))
+                                  iterate=iters > 1, boot_complete=name.endswith("_complete"),
+                                  fisher_optimization=name in FOPT)
         it = refdump.read_iteration(os.path.join(tmp, "dump.bin.iter")) if iters > 1 else None
     chunks = dump.chunks
     if keep is not None:
@@ -137,6 +144,8 @@ def make_case(name, spec):
                        OPTIONS.get(name, {}).get("SmoothResolutionMatrix", -1),
                        OPTIONS.get(name, {}).get("TurnOffBaseline", -1)], dtype=float),
     )
+    if name in FOPT:
+        out["fisher_opt"] = np.array(1)
     if it is not None:
         out["it_n"] = np.array(iters)
         out["it_theta"], out["it_prev"], out["it_fits"] = it.theta, it.previous, it.fits

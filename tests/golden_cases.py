@@ -13,6 +13,9 @@ CASES = ["tiny_nomarg", "tiny_marg1", "tiny_marg3", "tiny_masked", "small_cfg", 
          "tiny_reso", "tiny_reso_dia", "tiny_smooth", "tiny_smooth_mean", "tiny_reso_growth",
          "tiny_reso_smooth", "tiny_tophat", "tiny_nosfid"]
 RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth", "tiny_reso_smooth"]
+# from the reference built with FISHER_OPTIMIZATION (banded chunk Fisher
+# matrices); kept out of CASES, whose tests run the full matrices
+FOPT_CASES = ["desi_fopt"]
 
 
 @dataclasses.dataclass
@@ -44,13 +47,15 @@ class GoldenCase:
     opts: dict = dataclasses.field(default_factory=lambda: dict(smooth_noise_weights=-1, redshift_growth=False,
                                                                   fid_b=0.0, turn_off_sfid=False))
     smooth_rmat: bool = False
+    fisher_optimization: bool = False   # the reference was built with FISHER_OPTIMIZATION
 
     def port_settings(self, P):
         """The oracle's Settings for this case."""
         return P.Settings(max_forest_length=self.max_forest_length, cont_logl_order=self.marg[0],
                           cont_l_order=self.marg[1], smooth_noise_weights=self.opts["smooth_noise_weights"],
                           redshift_growth=self.opts["redshift_growth"], growth_b=self.opts["fid_b"],
-                          turn_off_sfid=self.opts["turn_off_sfid"])
+                          turn_off_sfid=self.opts["turn_off_sfid"],
+                          fisher_optimization=self.fisher_optimization)
 
 
 _cache = {}
@@ -85,6 +90,7 @@ def load(name: str) -> GoldenCase:
                          turn_off_sfid=bool(len(o) > 4 and o[4] > 0))
         # SmoothResolutionMatrix: applied while the matrices are prepared
         case.smooth_rmat = len(o) > 3 and o[3] > 0 and o[0] >= 0
+    case.fisher_optimization = "fisher_opt" in z.files and bool(z["fisher_opt"])
     if "it_n" in z.files:
         case.nr = dict(n=int(z["it_n"]), theta=z["it_theta"], previous=z["it_prev"], fits=z["it_fits"],
                        fisher=z["it_fisher"], inverse=z["it_inverse"], dbt=z["it_dbt"])

@@ -81,7 +81,7 @@ def test_table_builder_reproduces_truth_table():
 TOL = {"tiny_marg3": 1e-7}
 
 
-@pytest.mark.parametrize("name", G.CASES)
+@pytest.mark.parametrize("name", G.CASES + G.FOPT_CASES)
 def test_port_matches_reference(name):
     c = G.load(name)
     tol = TOL.get(name, 1e-12)
@@ -100,6 +100,9 @@ def test_port_matches_reference(name):
         assert G.rel_err(b, dbt[1]) < tol
         assert G.rel_err(t, dbt[2]) < tol
         assert G.fisher_err(f, fis) < tol
+        if c.fisher_optimization:
+            # the elements outside the bands are exact zeros in both
+            assert np.array_equal(f == 0, fis == 0)
         results.append((ch.fisher_index_start, d, b, t, f))
     if c.complete:
         fsum, dbtsum = P.accumulate(c.bins.nkz, results)
