@@ -116,6 +116,10 @@ struct Specifics {
     bool smooth_resolution_matrix = false;  // SmoothResolutionMatrix > 0 (needs SmoothNoiseWeights >= 0)
     bool redshift_growth_on = false;    // RedshiftGrowthOn > 0 (exponent: fiducial[3])
     double min_snr_cut = 0;             // MinimumSnrCut
+    // flux -> delta_F of the input (conv::readConversion, core/fiducial_cosmology.cpp:33-83)
+    bool input_is_delta_flux = true;    // InputIsDeltaFlux > 0
+    bool use_chunks_mean_flux = false;  // UseChunksMeanFlux > 0
+    std::string mean_flux_file;         // MeanFluxFile (binary: int32 n, n doubles z, n doubles F-bar)
     double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
 };
 
@@ -289,6 +293,125 @@ private:
 
 }  // namespace qio
 
+// Flux to flux contrast, lyspeq's conv:: (core/fiducial_cosmology.cpp:18-169),
+// applied to a whole spectrum after reading and before its outliers are
+// masked (core/one_qso_estimate.cpp:62-65).
+namespace conv {
+
+enum class Conversion { None, ChunkMean, MeanFluxFile };
+
+// conv::readConversion's resolution of the three keys: delta input wins over
+// both conversions, the spectrum's own mean over a mean-flux file; with none
+// of them set the input is taken as delta.
+inline Conversion conversion(const Specifics &sp) {
+    if (sp.input_is_delta_flux) return Conversion::None;
+    if (sp.use_chunks_mean_flux) return Conversion::ChunkMean;
+    if (!sp.mean_flux_file.empty()) return Conversion::MeanFluxFile;
+    return Conversion::None;
+}
+
+// Mean flux F-bar(z) of a MeanFluxFile (conv::setMeanFlux, :131-165): the
+// natural cubic spline through its points (GSL_CUBIC_INTERPOLATION), continued
+// past either end along its end slope (Interpolation::evaluate,
+// mathtools/interpolation.cpp:42-62).
+class MeanFlux {
+public:
+    MeanFlux(std::vector<double> z, std::vector<double> f) : x_(std::move(z)), y_(std::move(f)) { init(); }
+    explicit MeanFlux(const std::string &fname) {
+        std::FILE *fp = std::fopen(fname.c_str(), "rb");
+        if (!fp) throw std::runtime_error("MeanFluxFile: cannot open " + fname);
+        int32_t n = 0;
+        bool ok = std::fread(&n, 4, 1, fp) == 1 && n > 0;
+        if (ok) {
+            x_.resize(n);
+            y_.resize(n);
+            ok = std::fread(x_.data(), 8, n, fp) == (size_t) n && std::fread(y_.data(), 8, n, fp) == (size_t) n;
+        }
+        std::fclose(fp);
+        if (!ok) throw std::runtime_error("MeanFluxFile: cannot read " + fname);
+        init();
+    }
+
+    double operator()(double z) const {
+        const size_t n = x_.size();
+        if (z < x_[0]) return eval(0, x_[0]) + (z - x_[0]) * slope(0, x_[0]);
+        if (z > x_[n - 1]) return eval(n - 2, x_[n - 1]) + (z - x_[n - 1]) * slope(n - 2, x_[n - 1]);
+        return eval(interval(z), z);
+    }
+
+private:
+    std::vector<double> x_, y_, m_;   // knots, values, second derivatives
+
+    // second derivatives with M_0 = M_{n-1} = 0 from the tridiagonal system
+    //   h_{i-1} M_{i-1} + 2 (h_{i-1} + h_i) M_i + h_i M_{i+1}
+    //     = 6 ((y_{i+1} - y_i) / h_i - (y_i - y_{i-1}) / h_{i-1})
+    void init() {
+        const size_t n = x_.size();
+        if (n < 3 || y_.size() != n) throw std::runtime_error("MeanFlux: needs 3 or more points");
+        for (size_t i = 1; i < n; ++i)
+            if (!(x_[i] > x_[i - 1])) throw std::runtime_error("MeanFlux: z not increasing");
+        m_.assign(n, 0.0);
+        const size_t k = n - 2;
+        std::vector<double> diag(k), upper(k), rhs(k);
+        for (size_t j = 0; j < k; ++j) {
+            const size_t i = j + 1;
+            const double h0 = x_[i] - x_[i - 1], h1 = x_[i + 1] - x_[i];
+            diag[j] = 2.0 * (h0 + h1);
+            upper[j] = h1;
+            rhs[j] = 6.0 * ((y_[i + 1] - y_[i]) / h1 - (y_[i] - y_[i - 1]) / h0);
+        }
+        for (size_t j = 1; j < k; ++j) {
+            const double f = (x_[j + 1] - x_[j]) / diag[j - 1];
+            diag[j] -= f * upper[j - 1];
+            rhs[j] -= f * rhs[j - 1];
+        }
+        m_[k] = rhs[k - 1] / diag[k - 1];
+        for (size_t j = k - 1; j-- > 0;) m_[j + 1] = (rhs[j] - upper[j] * m_[j + 2]) / diag[j];
+    }
+    // i with x_i <= z < x_{i+1} (the last interval at the last knot)
+    size_t interval(double z) const {
+        size_t lo = 0, hi = x_.size() - 1;
+        while (hi - lo > 1) {
+            const size_t mid = (lo + hi) / 2;
+            if (x_[mid] > z) hi = mid; else lo = mid;
+        }
+        return lo;
+    }
+    double eval(size_t i, double z) const {
+        const double h = x_[i + 1] - x_[i], t1 = x_[i + 1] - z, t0 = z - x_[i];
+        return (m_[i] * t1 * t1 * t1 + m_[i + 1] * t0 * t0 * t0) / (6.0 * h)
+             + (y_[i] / h - m_[i] * h / 6.0) * t1 + (y_[i + 1] / h - m_[i + 1] * h / 6.0) * t0;
+    }
+    double slope(size_t i, double z) const {
+        const double h = x_[i + 1] - x_[i], t1 = x_[i + 1] - z, t0 = z - x_[i];
+        return (3.0 * m_[i + 1] * t0 * t0 - 3.0 * m_[i] * t1 * t1) / (6.0 * h)
+             - (y_[i] / h - m_[i] * h / 6.0) + (y_[i + 1] / h - m_[i + 1] * h / 6.0);
+    }
+};
+
+// conv::chunkMeanConversion and conv::fullConversion (:94-111): delta =
+// F / F-bar - 1 and ivar F-bar^2, F-bar the spectrum's mean flux (over all
+// its pixels, masked ones included) or F-bar(z) at each pixel.
+inline void convertFluxToDeltaF(Conversion c, const MeanFlux *mean_flux, const double *lambda, double *flux,
+                                double *ivar, int size) {
+    if (c == Conversion::ChunkMean) {
+        double mean = 0;
+        for (int i = 0; i < size; ++i) mean += flux[i];
+        mean /= size;
+        for (int i = 0; i < size; ++i) flux[i] = flux[i] / mean - 1;
+        for (int i = 0; i < size; ++i) ivar[i] *= mean * mean;
+    } else if (c == Conversion::MeanFluxFile) {
+        if (!mean_flux) throw std::runtime_error("convertFluxToDeltaF: no mean flux");
+        for (int i = 0; i < size; ++i) {
+            const double fbar = (*mean_flux)(lambda[i] / LYA_REST - 1);
+            flux[i] = flux[i] / fbar - 1;
+            ivar[i] *= fbar * fbar;
+        }
+    }
+}
+
+}  // namespace conv
+
 class OneDQuadraticPowerEstimate;
 
 // One chunk of a spectrum in the estimator's batch (Chunk).
@@ -342,6 +465,23 @@ public:
     void oneQSOiteration(const double *ps_estimate, std::vector<std::unique_ptr<double[]>> &dbt_sum_vector,
                          double *fisher_sum);
 
+    // OneQSOEstimate::_readQsoFile (core/one_qso_estimate.cpp:52-100) on an
+    // opened binary file: header, S/N cut, data, flux -> delta (mean_flux:
+    // the estimator's F-bar(z) when Specifics names a MeanFluxFile), outlier
+    // mask, redshift cut, short-file check.  Throws std::runtime_error where
+    // the reference drops the file; returns the number of outliers masked.
+    static int readQsoFile(qio::QSOFile &q, const Specifics &sp, double z_lower, double z_upper,
+                           const conv::MeanFlux *mean_flux) {
+        q.readParameters();
+        if (q.snr < sp.min_snr_cut) throw std::runtime_error("OneQSOEstimate::_readQsoFile::Low SNR");
+        q.readData();
+        conv::convertFluxToDeltaF(conv::conversion(sp), mean_flux, q.wave(), q.delta(), q.ivar(), q.size());
+        const int nout = q.maskOutliers();
+        q.cutBoundary(z_lower, z_upper);
+        if (q.realSize() < MIN_PIXELS_IN_FILE) throw std::runtime_error("OneQSOEstimate::_readQsoFile::Short file");
+        return nout;
+    }
+
     // OneQSOEstimate::decideIndices, core/one_qso_estimate.cpp:17-50
     static std::vector<int> decideIndices(int size, const double *wave, const Specifics &sp) {
         std::vector<double> vel(size);
@@ -390,6 +530,9 @@ public:
     OneDQuadraticPowerEstimate(const Binning &bins, const SQGrid &grid, const std::vector<SQTable> &tables,
                                const Specifics &sp, int device = 0)
         : bins_(bins), sp_(sp) {
+        // conv::readConversion: the mean-flux file is read once, up front
+        if (conv::conversion(sp) == conv::Conversion::MeanFluxFile)
+            mean_flux_ = std::make_unique<conv::MeanFlux>(sp.mean_flux_file);
         nkz_ = bins.nkz();
         std::vector<int> r;
         std::vector<double> dv, deriv, signal;
@@ -442,6 +585,8 @@ public:
 
     const Binning &binning() const { return bins_; }
     const Specifics &specifics() const { return sp_; }
+    // F-bar(z) of the MeanFluxFile the specifics name (else null)
+    const conv::MeanFlux *meanFlux() const { return mean_flux_.get(); }
     int totalKZBins() const { return nkz_; }
 
     int numberOfChunks() const { return lqg_batch_size(ctx_.get()); }
@@ -738,6 +883,7 @@ private:
     std::unique_ptr<lqg_ctx, CtxDel> ctx_;
     Binning bins_;
     Specifics sp_;
+    std::unique_ptr<conv::MeanFlux> mean_flux_;
     int nkz_ = 0;
     // the batched iteration behind Chunk::oneQSOiteration: its theta, the
     // batch size it covered and the chunks' statuses
@@ -864,16 +1010,9 @@ inline OneQSOEstimate::OneQSOEstimate(const std::string &f_qso) : fname_qso(f_qs
     const Specifics &sp = est->specifics();
     const Binning &bins = est->binning();
     try {
-        // OneQSOEstimate::_readQsoFile (core/one_qso_estimate.cpp:52-98); the
-        // input is delta (InputIsDeltaFlux), as in every configuration here
         qio::QSOFile q(f_qso, qio::Binary);
-        q.readParameters();
-        if (q.snr < sp.min_snr_cut) throw std::runtime_error("OneQSOEstimate::_readQsoFile::Low SNR");
-        q.readData();
-        const int nout = q.maskOutliers();
+        const int nout = readQsoFile(q, sp, bins.z_lower(), bins.z_upper(), est->meanFlux());
         if (nout > 0) est->log("found " + std::to_string(nout) + " outlier pixels in " + f_qso);
-        q.cutBoundary(bins.z_lower(), bins.z_upper());
-        if (q.realSize() < MIN_PIXELS_IN_FILE) throw std::runtime_error("OneQSOEstimate::_readQsoFile::Short file");
         const std::vector<int> idx = decideIndices(q.size(), q.wave(), sp);
         const int nchunks = (int) idx.size() - 1;
         for (int nc = 0; nc < nchunks; ++nc) {

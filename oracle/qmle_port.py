@@ -41,6 +41,10 @@ class Settings:
     redshift_growth: bool = False    # RedshiftGrowthOn > 0 (core/global_numbers.cpp:127)
     growth_b: float = 0.0            # FIDUCIAL_PD13_PARAMS.B
     fisher_optimization: bool = False   # built with -DFISHER_OPTIMIZATION (configure --enable-fisher-optimization)
+    # flux -> delta_F of the input (conv::readConversion, core/fiducial_cosmology.cpp:33-83)
+    input_is_delta_flux: bool = True    # InputIsDeltaFlux > 0
+    use_chunks_mean_flux: bool = False  # UseChunksMeanFlux > 0
+    mean_flux: tuple | None = None      # (z, F-bar) of a MeanFluxFile
 
     @property
     def max_forest_length_v(self):
@@ -117,7 +121,7 @@ def cut_masked_boundary(ivar):
     return int(nz[0]), int(nz[-1]) + 1
 
 
-def preprocess_spectrum(spec, bins, reso=None):
+def preprocess_spectrum(spec, bins, reso=None, settings=None):
     """Reading and cleaning of one binary spectrum: io/qso_file.cpp:352-369
     (sigma -> ivar), :189-230 (maskOutliers), :159-187 (cutBoundary) and
     core/one_qso_estimate.cpp:52-100.  Returns (wave, delta, ivar) in
@@ -132,6 +136,8 @@ def preprocess_spectrum(spec, bins, reso=None):
     delta = np.array(spec.delta, dtype=np.float64)
     ivar = 1.0 / (np.asarray(spec.sigma, dtype=np.float64) ** 2)
     ivar[ivar < DOUBLE_EPSILON] = 0.0
+    # flux -> delta_F (core/one_qso_estimate.cpp:62-65)
+    convert_flux_to_delta(settings, wave, delta, ivar)
     # maskOutliers (factor 5)
     good = ivar != 0
     realsize = int(good.sum())
@@ -244,6 +250,57 @@ def cspline_eval(x, y, mm, t):
     t1, t0 = x[i + 1] - t, t - x[i]
     return ((mm[i] * t1 ** 3 + mm[i + 1] * t0 ** 3) / (6.0 * h)
             + (y[i] / h - mm[i] * h / 6.0) * t1 + (y[i + 1] / h - mm[i + 1] * h / 6.0) * t0)
+
+
+def cspline_slope(x, y, mm, i, t):
+    """First derivative at t of the natural cubic spline's piece on [x_i, x_{i+1}]."""
+    h = x[i + 1] - x[i]
+    t1, t0 = x[i + 1] - t, t - x[i]
+    return ((3.0 * mm[i + 1] * t0 * t0 - 3.0 * mm[i] * t1 * t1) / (6.0 * h)
+            - (y[i] / h - mm[i] * h / 6.0) + (y[i + 1] / h - mm[i + 1] * h / 6.0))
+
+
+def flux_conversion(settings):
+    """conv::readConversion's resolution of InputIsDeltaFlux, UseChunksMeanFlux
+    and MeanFluxFile (core/fiducial_cosmology.cpp:33-83): delta input wins, then
+    the spectrum's own mean, then the file; 'none', 'mean' or 'file'."""
+    if settings is None or settings.input_is_delta_flux:
+        return "none"
+    if settings.use_chunks_mean_flux:
+        return "mean"
+    if settings.mean_flux is not None:
+        return "file"
+    return "none"
+
+
+def mean_flux_at(mean_flux, z):
+    """F-bar(z): Interpolation::evaluate with GSL_CUBIC_INTERPOLATION
+    (mathtools/interpolation.cpp:42-62), the natural cubic spline and, past
+    either end, the line along its end slope."""
+    x, y = (np.asarray(a, dtype=np.float64) for a in mean_flux)
+    mm = natural_cspline(x, y)
+    if z < x[0]:
+        return cspline_eval(x, y, mm, x[0]) + (z - x[0]) * cspline_slope(x, y, mm, 0, x[0])
+    if z > x[-1]:
+        n = len(x)
+        return cspline_eval(x, y, mm, x[-1]) + (z - x[-1]) * cspline_slope(x, y, mm, n - 2, x[-1])
+    return cspline_eval(x, y, mm, z)
+
+
+def convert_flux_to_delta(settings, wave, flux, ivar):
+    """conv::chunkMeanConversion / fullConversion (core/fiducial_cosmology.cpp:94-111)
+    on a whole spectrum, in place: delta = F / F-bar - 1, ivar F-bar^2, F-bar
+    the mean over every pixel (masked ones too, summed in order) or F-bar(z)."""
+    kind = flux_conversion(settings)
+    if kind == "mean":
+        mean = float(np.add.accumulate(flux)[-1]) / len(flux)
+        flux[:] = flux / mean - 1
+        ivar *= mean * mean
+    elif kind == "file":
+        for i in range(len(flux)):
+            fbar = mean_flux_at(settings.mean_flux, wave[i] / LYA_REST - 1)
+            flux[i] = flux[i] / fbar - 1
+            ivar[i] *= fbar * fbar
 
 
 def _nonzero_min_element(row):
@@ -391,7 +448,7 @@ def chunks_from_spectra(spectra, bins, table_keys, settings, reso=None):
     out = []
     for s in spectra:
         try:
-            pre = preprocess_spectrum(s, bins, reso)
+            pre = preprocess_spectrum(s, bins, reso, settings)
         except ValueError:
             continue
         wave, delta, ivar = pre[:3]

@@ -7,7 +7,9 @@
 //    derivative zero at both ends), used by Resolution::oversample
 //    (mathtools/matrix_helper.cpp:1008-1073); gsl_interp_linear as well.
 //    Outside [x_0, x_{n-1}] the evaluation returns NaN, as GSL does with its
-//    error handler off.
+//    error handler off.  gsl_spline (value and first derivative) on top of
+//    it, for the mean flux F-bar(z) of a MeanFluxFile (conv::setMeanFlux,
+//    core/fiducial_cosmology.cpp:131-165).
 //  * fftw_plan_dft_r2c_1d / fftw_plan_dft_c2r_1d with fftw_execute: the
 //    unnormalised discrete Fourier transform of FFTW's definition, evaluated
 //    as a direct O(n^2) sum (RealField::deconvolveSinc transforms 21 points
@@ -17,6 +19,7 @@
 #include "gsl/gsl_shim_common.h"
 #include "fftw3.h"
 
+#include <algorithm>
 #include <cmath>
 #include <limits>
 #include <stdexcept>
@@ -137,11 +140,44 @@ void gsl_interp_free(gsl_interp *g) {
     if (g->type == gsl_interp_cspline) delete static_cast<CsplineState *>(g->state);
     delete g;
 }
-gsl_spline *gsl_spline_alloc(const gsl_interp_type *, size_t) { unavailable("gsl_spline"); }
-int gsl_spline_init(gsl_spline *, const double[], const double[], size_t) { unavailable("gsl_spline"); }
-double gsl_spline_eval(const gsl_spline *, double, gsl_interp_accel *) { unavailable("gsl_spline"); }
-double gsl_spline_eval_deriv(const gsl_spline *, double, gsl_interp_accel *) { unavailable("gsl_spline"); }
-void gsl_spline_free(gsl_spline *) {}
+// gsl_spline: a gsl_interp that keeps its own copy of the knots, as GSL's
+// does; lyspeq's Interpolation (mathtools/interpolation.cpp) reads the mean
+// flux F-bar(z) of a MeanFluxFile through it, and its first derivative to
+// continue the curve past the ends.
+gsl_spline *gsl_spline_alloc(const gsl_interp_type *T, size_t n) {
+    return new gsl_spline{gsl_interp_alloc(T, n), new double[n], new double[n], n};
+}
+int gsl_spline_init(gsl_spline *s, const double xa[], const double ya[], size_t n) {
+    if (!s || n != s->size) throw std::invalid_argument("gsl_spline_init: size mismatch");
+    std::copy(xa, xa + n, s->x);
+    std::copy(ya, ya + n, s->y);
+    return gsl_interp_init(s->interp, s->x, s->y, n);
+}
+double gsl_spline_eval(const gsl_spline *s, double x, gsl_interp_accel *a) {
+    return gsl_interp_eval(s->interp, s->x, s->y, x, a);
+}
+// d/dx of the cubic above: the derivatives of t1^3 and t0^3 are -3 t1^2 and
+// 3 t0^2, of t1 and t0 -1 and 1.
+double gsl_spline_eval_deriv(const gsl_spline *s, double x, gsl_interp_accel *a) {
+    const gsl_interp *g = s->interp;
+    const double *xa = s->x, *ya = s->y;
+    if (!(x >= g->xmin && x <= g->xmax)) return std::numeric_limits<double>::quiet_NaN();
+    const size_t i = find_interval(xa, g->size, x);
+    if (a) a->cache = i;
+    const double h = xa[i + 1] - xa[i];
+    if (g->type == gsl_interp_linear) return (ya[i + 1] - ya[i]) / h;
+    const std::vector<double> &m = static_cast<const CsplineState *>(g->state)->m;
+    const double t1 = xa[i + 1] - x, t0 = x - xa[i];
+    return (3.0 * m[i + 1] * t0 * t0 - 3.0 * m[i] * t1 * t1) / (6.0 * h)
+         - (ya[i] / h - m[i] * h / 6.0) + (ya[i + 1] / h - m[i + 1] * h / 6.0);
+}
+void gsl_spline_free(gsl_spline *s) {
+    if (!s) return;
+    gsl_interp_free(s->interp);
+    delete[] s->x;
+    delete[] s->y;
+    delete s;
+}
 
 gsl_spline2d *gsl_spline2d_alloc(const gsl_interp2d_type *, size_t, size_t) { unavailable("gsl_spline2d"); }
 int gsl_spline2d_init(gsl_spline2d *, const double[], const double[], const double[], size_t, size_t)
