@@ -8,11 +8,14 @@ core/quadratic_estimate.cpp:456-498; stableInvertSym,
 mathtools/matrix_helper.cpp:330-358).  The unhalved upper sum the engine
 accumulates is twice the halved matrix's upper triangle, which is exact.
 """
+import os
+
 import numpy as np
 import pytest
 
 import golden_cases as G
 from oracle import qmle_port as P
+from oracle.refsrc import reference_root
 
 
 def _complete_cases():
@@ -96,6 +99,25 @@ def test_damping_decision_of_large_matrices(engine_lib, ratio, spread):
     assert g["damped"] == int(o["warn"]) == int(ratio > 8)
     tol = 1e-14 * np.linalg.cond(f) ** (2 if ratio > 8 else 1)
     assert G.rel_err(g["theta"], o["theta"]) < max(tol, 1e-10)
+
+
+@pytest.mark.skipif(not os.path.isdir(reference_root()), reason="reference sources absent")
+def test_inverse_matches_the_reference_lu_truth(engine_lib):
+    """lyspeq's test_LAPACKE_InvertMatrixLU_2 (tests/cblas_tests.cpp:257-283): the
+    496 x 496 symmetric matrix of tests/input/test_symmatrix.txt (indefinite, so
+    the solve takes its elimination branch) inverted by the library's solve,
+    against tests/truth/truth_inverse_matrix.txt: the reference's allClose
+    (1e-5 relative, 1e-8 absolute) and the file's printing (6 significant
+    digits, 5e-6 relative) on every nonzero element."""
+    from lyspeq_gb300 import lqg
+    ref = reference_root()
+    a = np.loadtxt(os.path.join(ref, "tests", "input", "test_symmatrix.txt"), skiprows=1)
+    t = np.loadtxt(os.path.join(ref, "tests", "truth", "truth_inverse_matrix.txt"), skiprows=1)
+    assert a.shape == t.shape == (496, 496)
+    inv = lqg.fisher_solve(2.0 * np.triu(a), np.zeros((3, 496)))["inverse"]
+    assert np.all(np.abs(inv - t) < 1e-8 + 1e-5 * np.maximum(np.abs(inv), np.abs(t)))
+    nz = t != 0
+    assert np.max(np.abs(inv - t)[nz] / np.abs(t)[nz]) <= 5e-6 * (1 + 1e-6)
 
 
 def test_rejects_bad_shapes(engine_lib):

@@ -65,6 +65,37 @@ def test_reference_build_reproduces_truth(tmp_path):
 
 
 @have_ref
+def test_port_reproduces_the_reference_signal_and_q0_matrices(tmp_path):
+    """lyspeq's testSQCMatrices (tests/testSQCMatrices.cpp:38-95): S_fid and the
+    first stored Q (k band 0, z bin 0, after the redshift weights) of its test
+    spectrum under tests/input/test.config, against tests/truth/signal_matrix.txt
+    and q0_matrix.txt.  Every element (the reference's test compares the first
+    row at 1e-5), to the files' printing: 7 significant digits, 5e-7 relative,
+    with the same exact zeros."""
+    z = np.load(os.path.join(G.GOLDEN, "lyspeq_test_it1.npz"))
+    b = z["bins"]
+    bins = synth.Bins(b[0], int(b[1]), b[2], int(b[3]), b[4], b[5], b[6], int(b[7]))
+    nv, lenv, nzp, mfl, c0, c1 = z["grid"]
+    r, dv = z["tables"][0]
+    table = synth.build_table(bins, int(r), float(dv), int(nv), float(lenv), int(nzp),
+                              fid=tuple(float(x) for x in z["fid"]))
+    path = tmp_path / "spectrum.dat"
+    path.write_bytes(z["dat"].tobytes())
+    s = P.Settings(max_forest_length=float(mfl), cont_logl_order=int(c0), cont_l_order=int(c1))
+    chunks = P.chunks_from_spectra([synth.read_dat(str(path))], bins, {(int(r), round(float(dv), 1)): 0}, s)
+    assert len(chunks) == 1 and chunks[0].n == 488
+    tv = P.table_view(table, bins, int(nv), float(lenv), int(nzp))
+    stored, q, sm = P.build_matrices(chunks[0], bins, tv)
+    assert stored[0] == 0 and chunks[0].fisher_index_start == 0
+    for got, name in ((sm, "signal_matrix.txt"), (q[0], "q0_matrix.txt")):
+        ref = np.loadtxt(f"{REFERENCE}/tests/truth/{name}", skiprows=1)
+        assert ref.shape == got.shape == (488, 488)
+        assert np.array_equal(got == 0, ref == 0), name
+        nz = ref != 0
+        assert np.max(np.abs(got - ref)[nz] / np.abs(ref)[nz]) <= 5e-7 * (1 + 1e-6), name
+
+
+@have_ref
 def test_table_builder_reproduces_truth_table():
     bins = synth.Bins(0.0, 3, 7e-4, 2, 0.5, 1.8, 0.2, 2)
     t = synth.build_table(bins, 70000, 20.0, 1401, 14000.0, 10, fid=(0.06, -2.6, -0.1, 1.0, 0.0, 0.0))
