@@ -76,6 +76,12 @@ struct Binning {
     int nkz() const { return nk() * nz(); }
     double z_lower() const { return z_centers.front() - z_bin_width / 2; }
     double z_upper() const { return z_centers.back() + z_bin_width / 2; }
+    // bins::findRedshiftBin (core/global_numbers.cpp:344-355): -1 below the
+    // first bin, NUMBER_OF_Z_BINS above the last
+    int findRedshiftBin(double z) const {
+        if (z < z_lower()) return -1;
+        return std::min((int) ((z - z_lower()) / z_bin_width), nz());
+    }
 };
 
 // One (R, dv) pair of SQ lookup tables (SQLookupTable, core/sq_table.cpp):
@@ -120,8 +126,23 @@ struct Specifics {
     bool input_is_delta_flux = true;    // InputIsDeltaFlux > 0
     bool use_chunks_mean_flux = false;  // UseChunksMeanFlux > 0
     std::string mean_flux_file;         // MeanFluxFile (binary: int32 n, n doubles z, n doubles F-bar)
+    // OutputDir / OutputFileBase: with a base name set, every iteration writes
+    // <dir>/<base>_it<N>_{quadratic_power_estimate_detailed, fisher_matrix,
+    // inversefisher_matrix, solver_invfishermatrix}.txt as the reference does
+    std::string output_dir = ".";
+    std::string output_file_base;
     double max_forest_length_v() const { return max_forest_length / std::max(1, number_of_chunks); }
 };
+
+// The PD13 fit with a Lorentzian factor (Palanque_Delabrouille_etal_2013_fit,
+// core/fiducial_cosmology.cpp:273-282); p = A, n, alpha, B, beta, lambda,
+// k0 = 0.009 s/km, z0 = 3.
+inline double fiducialPowerPD13(double k, double z, const double p[6]) {
+    const double q0 = k / 0.009 + 1e-15, x0 = (1. + z) / (1. + 3.0);
+    return (p[0] * 3.14159265358979323846 / 0.009) *
+           std::pow(q0, 2. + p[1] + p[2] * std::log(q0) + p[4] * std::log(x0)) * std::pow(x0, p[3]) /
+           (1. + p[5] * k * k);
+}
 
 // A spectrum as qio::QSOFile holds it after reading: observed wavelength in
 // Angstrom, flux contrast and inverse variance (0 = masked), resolution R.
@@ -412,6 +433,127 @@ inline void convertFluxToDeltaF(Conversion c, const MeanFlux *mean_flux, const d
 
 }  // namespace conv
 
+// The result files of lyspeq's estimator (core/quadratic_estimate.cpp:616-751,
+// 797-830; mathtools/matrix_helper.cpp:459-475).  Every number and every line
+// a reader parses has the reference's format; the explanatory comments are
+// this build's own.
+namespace output {
+
+// mxhelp::fprintfMatrix: "nrows ncols", then each row as %14le values
+inline void fprintfMatrix(const std::string &fname, const double *a, int nrows, int ncols) {
+    std::FILE *f = std::fopen(fname.c_str(), "w");
+    if (!f) throw std::runtime_error("cannot write " + fname);
+    std::fprintf(f, "%d %d\n", nrows, ncols);
+    for (int i = 0; i < nrows; ++i) {
+        for (int j = 0; j < ncols; ++j) std::fprintf(f, "%14le ", a[(size_t) i * ncols + j]);
+        std::fprintf(f, "\n");
+    }
+    std::fclose(f);
+}
+
+// The redshift bin a spectrum counts in, from its median wavelength after the
+// redshift cut (OneQSOEstimate::getComputeTimeEst, core/one_qso_estimate.cpp:
+// 132-174, and QSOFile::readMinMaxMedRedshift, io/qso_file.cpp:293-313); -1
+// for a spectrum the reader drops (S/N cut, empty or short after the cut).
+// Index zbin + 1 of the estimator's Z_BIN_COUNTS.
+inline int redshiftBinOfFile(const std::string &fname, const Specifics &sp, const Binning &bins) {
+    try {
+        qio::QSOFile q(fname, qio::Binary);
+        q.readParameters();
+        if (q.snr < sp.min_snr_cut) return -1;
+        q.readData();
+        q.cutBoundary(bins.z_lower(), bins.z_upper());
+        if (q.realSize() < MIN_PIXELS_IN_FILE) return -1;
+        const int n = q.size();
+        const double *w = q.wave();
+        const double wmed = n % 2 == 0 ? (w[n / 2 - 1] + w[n / 2]) / 2 : w[n / 2];
+        return bins.findRedshiftBin(wmed / LYA_REST - 1);
+    } catch (std::exception &) {
+        return -1;
+    }
+}
+
+// The same for a spectrum given as arrays (no header, so no S/N cut): the
+// pixels inside the redshift range with the masked ends removed.
+inline int redshiftBinOfSpectrum(const std::vector<double> &wave, const std::vector<double> &ivar,
+                                 const Binning &bins) {
+    const double l1 = LYA_REST * (1 + bins.z_lower()), l2 = LYA_REST * (1 + bins.z_upper());
+    size_t a = std::lower_bound(wave.begin(), wave.end(), l1) - wave.begin();
+    size_t b = std::upper_bound(wave.begin(), wave.end(), l2) - wave.begin();
+    while (a < b && !(ivar[a] >= 1e-15)) ++a;
+    while (b > a && !(ivar[b - 1] >= 1e-15)) --b;
+    int real = 0;
+    for (size_t i = a; i < b; ++i) real += ivar[i] >= 1e-15;
+    if (b <= a || real < MIN_PIXELS_IN_FILE) return -1;
+    const size_t n = b - a;
+    const double wmed = n % 2 == 0 ? (wave[a + n / 2 - 1] + wave[a + n / 2]) / 2 : wave[a + n / 2];
+    return bins.findRedshiftBin(wmed / LYA_REST - 1);
+}
+
+// writeSpectrumEstimates: "Nz Nk", the z-bin counts, then z, k_c, P, error
+// per bin (P = fiducial + theta, error = sqrt of the inverse Fisher diagonal)
+inline void writeSpectrumEstimates(const std::string &fname, const Binning &bins, const std::vector<int> &zcounts,
+                                   const double *theta, const double *pfid, const double *inverse) {
+    std::FILE *f = std::fopen(fname.c_str(), "w");
+    if (!f) throw std::runtime_error("cannot write " + fname);
+    const int nk = bins.nk(), nkz = bins.nkz();
+    std::fprintf(f, "%d %d\n", bins.nz(), nk);
+    for (int c : zcounts) std::fprintf(f, "%d ", c);
+    std::fprintf(f, "\n");
+    for (int i = 0; i < nkz; ++i) {
+        const int kn = i % nk, zm = i / nk;
+        std::fprintf(f, "%.3lf %e %e %e\n", bins.z_centers[zm], (bins.k_edges[kn] + bins.k_edges[kn + 1]) / 2,
+                     theta[i] + pfid[i], std::sqrt(inverse[(size_t) (nkz + 1) * i]));
+    }
+    std::fclose(f);
+}
+
+// writeDetailedSpectrumEstimates: comment lines (the settings, the fiducial
+// parameters, the damping, "Nz Nk" and the z-bin counts), the column names,
+// then per bin z, k1, k2, kc, Pfid, ThetaP, Pest, ErrorP, the Fisher-weighted
+// d, b, t and the d, b, t sums before the weighting.
+inline void writeDetailedSpectrumEstimates(const std::string &fname, const Binning &bins, const Specifics &sp,
+                                           const std::vector<int> &zcounts, bool damped, double damp,
+                                           const double *theta, const double *pfid, const double *inverse,
+                                           const double *const weighted[3], const double *const sums[3],
+                                           bool fisher_optimization) {
+    std::FILE *f = std::fopen(fname.c_str(), "w");
+    if (!f) throw std::runtime_error("cannot write " + fname);
+    std::fprintf(f, "# lyspeq estimate computed by the GB300 engine (lyspeq_gb300)\n");
+    std::fprintf(f, "# Fisher optimization: %s\n", fisher_optimization ? "ON" : "OFF");
+    std::fprintf(f, "# MaximumForestLength %g\n# DynamicChunkNumber %d\n# ContinuumLogLambdaMargOrder %d\n"
+                    "# ContinuumLambdaMargOrder %d\n# TurnOffBaseline %d\n# SmoothNoiseWeights %d\n"
+                    "# RedshiftGrowthOn %d\n# UseResoMatrix %d\n",
+                 sp.max_forest_length, sp.number_of_chunks, sp.cont_logl_order, sp.cont_l_order,
+                 sp.turn_off_sfid ? 1 : 0, sp.smooth_noise_weights, sp.redshift_growth_on ? 1 : 0,
+                 sp.use_reso_matrix ? 1 : 0);
+    std::fprintf(f, "# Fiducial PD13 power (A, n, alpha, B, beta, lambda):\n");
+    for (double v : sp.fiducial) std::fprintf(f, "# %15e\n", v);
+    std::fprintf(f, "# Columns: z bin centre; k band lower edge, upper edge, centre [s/km]; fiducial power,\n"
+                    "# theta = d - b - t, their sum and sqrt(diag F^-1) [km/s]; Fisher-weighted d, b, t;\n"
+                    "# d, b, t before the Fisher weighting.  The counts are of spectra per redshift bin,\n"
+                    "# the first and last out of range.\n");
+    std::fprintf(f, damped ? "# Damped: True\n" : "# Damped: False\n");
+    std::fprintf(f, "# Damping constant: %.3e\n", damp);
+    std::fprintf(f, "# %d %d\n# ", bins.nz(), bins.nk());
+    for (int c : zcounts) std::fprintf(f, "%d ", c);
+    std::fprintf(f, "\n");
+    std::fprintf(f, "%5s %14s %14s %14s %14s %14s %14s %14s %14s %14s %14s %14s %14s %14s\n", "z", "k1", "k2", "kc",
+                 "Pfid", "ThetaP", "Pest", "ErrorP", "d", "b", "t", "Fd", "Fb", "Ft");
+    const int nk = bins.nk(), nkz = bins.nkz();
+    for (int i = 0; i < nkz; ++i) {
+        const int kn = i % nk, zm = i / nk;
+        const double k1 = bins.k_edges[kn], k2 = bins.k_edges[kn + 1];
+        std::fprintf(f, "%5.3lf %14e %14e %14e %14e %14e %14e %14e %14e %14e %14e %14e %14e %14e\n",
+                     bins.z_centers[zm], k1, k2, (k1 + k2) / 2, pfid[i], theta[i], pfid[i] + theta[i],
+                     std::sqrt(inverse[(size_t) (nkz + 1) * i]), weighted[0][i], weighted[1][i], weighted[2][i],
+                     sums[0][i], sums[1][i], sums[2][i]);
+    }
+    std::fclose(f);
+}
+
+}  // namespace output
+
 class OneDQuadraticPowerEstimate;
 
 // One chunk of a spectrum in the estimator's batch (Chunk).
@@ -568,6 +710,7 @@ public:
         fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
         inverse_fisher_matrix_sum.reset(new double[(size_t) nkz_ * nkz_]());
         solver_invfisher_matrix.reset(new double[(size_t) nkz_ * nkz_]());
+        z_bin_counts.assign(bins.nz() + 2, 0);
         current_slot() = this;
     }
     ~OneDQuadraticPowerEstimate() {
@@ -587,6 +730,53 @@ public:
     const Specifics &specifics() const { return sp_; }
     // F-bar(z) of the MeanFluxFile the specifics name (else null)
     const conv::MeanFlux *meanFlux() const { return mean_flux_.get(); }
+
+    // Z_BIN_COUNTS: spectra per redshift bin, index zbin + 1 (0 and
+    // NUMBER_OF_Z_BINS + 1: out of range or dropped), counted as each
+    // OneQSOEstimate is made
+    std::vector<int> z_bin_counts;
+    void countSpectrum(int zbin) { ++z_bin_counts[std::max(-1, std::min(zbin, bins_.nz())) + 1]; }
+
+    std::vector<double> fiducialPowers() const {
+        std::vector<double> p(nkz_);
+        for (int i = 0; i < nkz_; ++i) p[i] = powerSpectrumFiducial(i);
+        return p;
+    }
+    // writeSpectrumEstimates (core/quadratic_estimate.cpp:624-656)
+    void writeSpectrumEstimates(const std::string &fname) const {
+        output::writeSpectrumEstimates(fname, bins_, z_bin_counts, current_power_estimate_vector.get(),
+                                       fiducialPowers().data(), inverse_fisher_matrix_sum.get());
+    }
+    // writeDetailedSpectrumEstimates (:658-751)
+    void writeDetailedSpectrumEstimates(const std::string &fname) const {
+        const double *w[3] = {dbt_estimate_fisher_weighted_vector[0].get(), dbt_estimate_fisher_weighted_vector[1].get(),
+                              dbt_estimate_fisher_weighted_vector[2].get()};
+        const double *d[3] = {dbt_estimate_sum_before_fisher_vector[0].get(),
+                              dbt_estimate_sum_before_fisher_vector[1].get(),
+                              dbt_estimate_sum_before_fisher_vector[2].get()};
+#ifdef FISHER_OPTIMIZATION
+        const bool fopt = true;
+#else
+        const bool fopt = false;
+#endif
+        output::writeDetailedSpectrumEstimates(fname, bins_, sp_, z_bin_counts, damped != 0, damp,
+                                               current_power_estimate_vector.get(), fiducialPowers().data(),
+                                               inverse_fisher_matrix_sum.get(), w, d, fopt);
+    }
+    // writeFisherMatrix (:616-622): the halved, symmetric sum
+    void writeFisherMatrix(const std::string &fname) const {
+        output::fprintfMatrix(fname, fisher_matrix_halved.data(), nkz_, nkz_);
+    }
+    // iterationOutput (:797-830): the detailed estimate and the Fisher, inverse
+    // Fisher and solver matrices of iteration it (1-based), under
+    // OutputDir/OutputFileBase
+    void iterationOutput(int it) const {
+        const std::string base = sp_.output_dir + "/" + sp_.output_file_base + "_it" + std::to_string(it);
+        writeDetailedSpectrumEstimates(base + "_quadratic_power_estimate_detailed.txt");
+        writeFisherMatrix(base + "_fisher_matrix.txt");
+        output::fprintfMatrix(base + "_inversefisher_matrix.txt", inverse_fisher_matrix_sum.get(), nkz_, nkz_);
+        output::fprintfMatrix(base + "_solver_invfishermatrix.txt", solver_invfisher_matrix.get(), nkz_, nkz_);
+    }
     int totalKZBins() const { return nkz_; }
 
     int numberOfChunks() const { return lqg_batch_size(ctx_.get()); }
@@ -600,6 +790,7 @@ public:
         std::vector<double> w = q.wave, d = q.delta, iv = q.ivar;
         const size_t n0 = w.size();
         if (d.size() != n0 || iv.size() != n0) throw std::invalid_argument("QSOSpectrum arrays differ in size");
+        countSpectrum(output::redshiftBinOfSpectrum(w, iv, bins_));
         for (auto &x : iv)
             if (x < 1e-15) x = 0;
         maskOutliers(w, d, iv, 5.0);
@@ -702,21 +893,19 @@ public:
             std::copy(current_power_estimate_vector.get(), current_power_estimate_vector.get() + nkz_,
                       previous_power_estimate_vector.get());
             invertTotalFisherMatrix();
+            if (!sp_.output_file_base.empty()) iterationOutput(it);
             if (hasConverged() || it == number_of_iterations) break;
             smoothPowerSpectra();
         }
         return std::min(it, number_of_iterations);
     }
 
-    // P_fid(k_c, z_c) of bin i_kz (powerSpectrumFiducial; PD13 fit,
-    // core/fiducial_cosmology.cpp:273-282)
+    // P_fid(k_c, z_c) of bin i_kz (powerSpectrumFiducial, core/quadratic_estimate.cpp;
+    // PD13 fit, core/fiducial_cosmology.cpp:273-282), 0 with TurnOffBaseline
     double powerSpectrumFiducial(int i_kz) const {
+        if (sp_.turn_off_sfid) return 0;   // no fiducial signal in C, none in the estimate
         const int kn = i_kz % bins_.nk(), zm = i_kz / bins_.nk();
-        const double k = (bins_.k_edges[kn] + bins_.k_edges[kn + 1]) / 2, z = bins_.z_centers[zm];
-        const double *p = sp_.fiducial;
-        const double q0 = k / 0.009 + 1e-15, x0 = (1. + z) / (1. + 3.0);
-        return (p[0] * 3.14159265358979323846 / 0.009) * std::pow(q0, 2. + p[1] + p[2] * std::log(q0) + p[4] * std::log(x0)) *
-               std::pow(x0, p[3]) / (1. + p[5] * k * k);
+        return fiducialPowerPD13((bins_.k_edges[kn] + bins_.k_edges[kn + 1]) / 2, bins_.z_centers[zm], sp_.fiducial);
     }
 
     // hasConverged (core/quadratic_estimate.cpp:548-614): with
@@ -747,18 +936,7 @@ public:
     // output minus P_fid as the next powerspectra_fits.
     void smoothPowerSpectra() {
         const std::string in = sp_.tmp_folder + "/tmp-power-0.txt", out = sp_.tmp_folder + "/tmp-smooth-0.txt";
-        FILE *f = std::fopen(in.c_str(), "w");
-        if (!f) throw std::runtime_error("cannot write " + in);
-        std::fprintf(f, "%d %d\n", bins_.nz(), bins_.nk());
-        for (int zm = 0; zm < bins_.nz(); ++zm) std::fprintf(f, "%d ", 0);
-        std::fprintf(f, "\n");
-        for (int i = 0; i < nkz_; ++i) {
-            const int kn = i % bins_.nk(), zm = i / bins_.nk();
-            std::fprintf(f, "%.3lf %e %e %e\n", bins_.z_centers[zm], (bins_.k_edges[kn] + bins_.k_edges[kn + 1]) / 2,
-                         current_power_estimate_vector[i] + powerSpectrumFiducial(i),
-                         std::sqrt(inverse_fisher_matrix_sum[(size_t) (nkz_ + 1) * i]));
-        }
-        std::fclose(f);
+        writeSpectrumEstimates(in);
         const std::string cmd = sp_.smoothing_command + " " + in + " " + out + (sp_.smooth_logk_logp ? " --interp_log" : "");
         if (std::system(cmd.c_str()) != 0) throw std::runtime_error("smoothing error: " + cmd);
         FILE *g = std::fopen(out.c_str(), "r");
@@ -1009,6 +1187,8 @@ inline OneQSOEstimate::OneQSOEstimate(const std::string &f_qso) : fname_qso(f_qs
     if (!est) throw std::runtime_error("OneQSOEstimate: no OneDQuadraticPowerEstimate in this process");
     const Specifics &sp = est->specifics();
     const Binning &bins = est->binning();
+    // Z_BIN_COUNTS, from the estimator's own pass over the file (getComputeTimeEst)
+    est->countSpectrum(output::redshiftBinOfFile(f_qso, sp, bins));
     try {
         qio::QSOFile q(f_qso, qio::Binary);
         const int nout = readQsoFile(q, sp, bins.z_lower(), bins.z_upper(), est->meanFlux());
