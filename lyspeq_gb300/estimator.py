@@ -82,17 +82,21 @@ class QuadraticEstimator:
 
     number_of_iterations, chisq_eps and smooth_log are the NumberOfIterations,
     ChiSqConvergence and SmoothLnkLnP settings; fid the fiducial PD13
-    parameters."""
+    parameters; turn_off_sfid TurnOffBaseline (no fiducial power, as the
+    engine's C has no fiducial signal)."""
 
     def __init__(self, engine, bins, fid=synth.PD13_DEFAULT, number_of_iterations=1, chisq_eps=0.01,
-                 smooth_log=False, precision="fp64"):
+                 smooth_log=False, precision="fp64", turn_off_sfid=False):
         self.engine, self.bins = engine, bins
         self.iterations = int(number_of_iterations)
         self.eps = float(chisq_eps)
         self.smooth_log = bool(smooth_log)
         self.precision = precision
-        # powerSpectrumFiducial(kn, zm) for every bin (i_kz = zm nk + kn)
+        # powerSpectrumFiducial(kn, zm) for every bin (i_kz = zm nk + kn); 0
+        # with TurnOffBaseline (core/quadratic_estimate.cpp, powerSpectrumFiducial)
         self.pfid = synth.pd13_power(np.tile(bins.k_centers, bins.nz), np.repeat(bins.z_centers, bins.nk), fid)
+        if turn_off_sfid:
+            self.pfid = np.zeros_like(self.pfid)
 
     def iterate(self) -> NRResult:
         nkz = self.bins.nkz

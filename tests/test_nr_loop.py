@@ -36,6 +36,16 @@ def test_convergence_test_rules():
     assert not ok
 
 
+def test_fiducial_power_is_zero_with_turn_off_baseline():
+    """powerSpectrumFiducial returns 0 under TurnOffBaseline, so the estimate
+    is theta alone and the smoothing fits it without a fiducial offset."""
+    c = G.load("tiny_nosfid")
+    assert c.opts["turn_off_sfid"]
+    on = E.QuadraticEstimator(None, c.bins)
+    off = E.QuadraticEstimator(None, c.bins, turn_off_sfid=True)
+    assert (on.pfid > 0).all() and not off.pfid.any()
+
+
 @pytest.mark.gpu
 def test_nr_loop_matches_reference(engine_lib):
     from lyspeq_gb300 import lqg
