@@ -106,7 +106,8 @@ struct Specifics {
     int cont_logl_order = 1;            // ContinuumLogLambdaMargOrder
     int cont_l_order = -1;              // ContinuumLambdaMargOrder
     bool turn_off_sfid = false;         // TurnOffBaseline
-    bool precomputed_fisher = false;    // PrecomputedFisher given
+    bool precomputed_fisher = false;    // PrecomputedFisher given (no Fisher matrices computed)
+    std::string precomputed_fisher_file;  // PrecomputedFisher: its file, used in place of the sum
     double chisq_convergence = 0.01;    // ChiSqConvergence (CHISQ_CONVERGENCE_EPS)
     bool smooth_logk_logp = true;       // SmoothLnkLnP
     // the six PD13 fiducial parameters (FiducialAmplitude, ...Slope, ...Curvature,
@@ -451,6 +452,22 @@ inline void fprintfMatrix(const std::string &fname, const double *a, int nrows, 
     std::fclose(f);
 }
 
+// mxhelp::fscanfMatrix (mathtools/matrix_helper.cpp:477-501): the format
+// fprintfMatrix writes
+inline std::vector<double> fscanfMatrix(const std::string &fname, int &nrows, int &ncols) {
+    std::FILE *f = std::fopen(fname.c_str(), "r");
+    if (!f) throw std::runtime_error("cannot read " + fname);
+    std::vector<double> a;
+    bool ok = std::fscanf(f, "%d %d", &nrows, &ncols) == 2 && nrows > 0 && ncols > 0;
+    if (ok) {
+        a.resize((size_t) nrows * ncols);
+        for (auto &x : a) ok = ok && std::fscanf(f, "%le", &x) == 1;
+    }
+    std::fclose(f);
+    if (!ok) throw std::runtime_error("cannot read a matrix from " + fname);
+    return a;
+}
+
 // The redshift bin a spectrum counts in, from its median wavelength after the
 // redshift cut (OneQSOEstimate::getComputeTimeEst, core/one_qso_estimate.cpp:
 // 132-174, and QSOFile::readMinMaxMedRedshift, io/qso_file.cpp:293-313); -1
@@ -676,6 +693,13 @@ public:
         if (conv::conversion(sp) == conv::Conversion::MeanFluxFile)
             mean_flux_ = std::make_unique<conv::MeanFlux>(sp.mean_flux_file);
         nkz_ = bins.nkz();
+        // _readPrecomputedFisher (core/quadratic_estimate.cpp:854-863)
+        if (!sp.precomputed_fisher_file.empty()) {
+            int nr = 0, nc = 0;
+            precomputed_fisher_ = output::fscanfMatrix(sp.precomputed_fisher_file, nr, nc);
+            if (nr != nkz_ || nc != nkz_)
+                throw std::invalid_argument("Precomputed Fisher matrix does not have correct number of rows or columns.");
+        }
         std::vector<int> r;
         std::vector<double> dv, deriv, signal;
         for (const auto &t : tables) {
@@ -689,7 +713,8 @@ public:
         lqg_tables tb{(int) tables.size(), r.data(), dv.data(), grid.nv, grid.v_length, grid.nzp,
                       deriv.data(), sp.turn_off_sfid ? nullptr : signal.data()};
         lqg_opts o{sp.max_forest_length_v(), sp.max_mean_pixel_size, sp.cont_logl_order, sp.cont_l_order,
-                   sp.turn_off_sfid ? 1 : 0, sp.precomputed_fisher ? 1 : 0, 0, sp.smooth_noise_weights,
+                   sp.turn_off_sfid ? 1 : 0, sp.precomputed_fisher || !sp.precomputed_fisher_file.empty() ? 1 : 0, 0,
+                   sp.smooth_noise_weights,
                    sp.redshift_growth_on ? 1 : 0, sp.fiducial[3]};
         lqg_ctx *c = nullptr;
         if (lqg_ctx_create(&c, &b, &tb, &o, device) != LQG_OK)
@@ -890,6 +915,9 @@ public:
                                dbt_estimate_sum_before_fisher_vector[1].get(),
                                dbt_estimate_sum_before_fisher_vector[2].get(), fisher_matrix_sum.get(), nullptr),
                   "lqg_download");
+            // PrecomputedFisher in place of the sum (:478-483); as the unhalved
+            // sum the solve takes, which it halves back exactly
+            for (size_t e = 0; e < precomputed_fisher_.size(); ++e) fisher_matrix_sum[e] = 2.0 * precomputed_fisher_[e];
             std::copy(current_power_estimate_vector.get(), current_power_estimate_vector.get() + nkz_,
                       previous_power_estimate_vector.get());
             invertTotalFisherMatrix();
@@ -1062,6 +1090,7 @@ private:
     Binning bins_;
     Specifics sp_;
     std::unique_ptr<conv::MeanFlux> mean_flux_;
+    std::vector<double> precomputed_fisher_;   // PrecomputedFisher (halved, nkz x nkz), else empty
     int nkz_ = 0;
     // the batched iteration behind Chunk::oneQSOiteration: its theta, the
     // batch size it covered and the chunks' statuses

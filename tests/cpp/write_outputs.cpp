@@ -9,7 +9,8 @@
 // z_centers, double dz, vec fiducial (6), double MinimumSnrCut, int64 damped,
 // double damp, vec theta, vec pfid, vec inverse (nkz^2), vec weighted (3 nkz),
 // vec sums (3 nkz), vec fisher (nkz^2), vec solver (nkz^2), int64 number of
-// spectrum files, then per file int64 length and its path.  Prints the
+// spectrum files, then per file int64 length and its path.  Reads the Fisher
+// file back (output::fscanfMatrix; exit 3 if it differs) and prints the
 // fiducial power of every bin (%.17g), one per line.
 #include <cstdint>
 #include <cstdio>
@@ -77,6 +78,11 @@ int main(int argc, char **argv) {
     output::fprintfMatrix(base + "_fisher_matrix.txt", fisher.data(), nkz, nkz);
     output::fprintfMatrix(base + "_inversefisher_matrix.txt", inverse.data(), nkz, nkz);
     output::fprintfMatrix(base + "_solver_invfishermatrix.txt", solver.data(), nkz, nkz);
+    // the matrix reader (PrecomputedFisher) reads the Fisher file back to the
+    // values it was written from
+    int nr = 0, nc = 0;
+    const std::vector<double> back = output::fscanfMatrix(base + "_fisher_matrix.txt", nr, nc);
+    if (nr != nkz || nc != nkz || back != fisher) return 3;
     for (int i = 0; i < nkz; ++i) {
         const int kn = i % bins.nk(), zm = i / bins.nk();
         std::printf("%.17g\n", fiducialPowerPD13((bins.k_edges[kn] + bins.k_edges[kn + 1]) / 2, bins.z_centers[zm],
