@@ -83,10 +83,13 @@ class QuadraticEstimator:
     number_of_iterations, chisq_eps and smooth_log are the NumberOfIterations,
     ChiSqConvergence and SmoothLnkLnP settings; fid the fiducial PD13
     parameters; turn_off_sfid TurnOffBaseline (no fiducial power, as the
-    engine's C has no fiducial signal)."""
+    engine's C has no fiducial signal); precomputed_fisher the matrix of a
+    PrecomputedFisher file (halved, nkz x nkz), used in place of the chunks'
+    sum (core/quadratic_estimate.cpp:478-483; the engine then needs
+    skip_fisher)."""
 
     def __init__(self, engine, bins, fid=synth.PD13_DEFAULT, number_of_iterations=1, chisq_eps=0.01,
-                 smooth_log=False, precision="fp64", turn_off_sfid=False):
+                 smooth_log=False, precision="fp64", turn_off_sfid=False, precomputed_fisher=None):
         self.engine, self.bins = engine, bins
         self.iterations = int(number_of_iterations)
         self.eps = float(chisq_eps)
@@ -97,6 +100,11 @@ class QuadraticEstimator:
         self.pfid = synth.pd13_power(np.tile(bins.k_centers, bins.nz), np.repeat(bins.z_centers, bins.nk), fid)
         if turn_off_sfid:
             self.pfid = np.zeros_like(self.pfid)
+        self.precomputed = None
+        if precomputed_fisher is not None:
+            self.precomputed = np.asarray(precomputed_fisher, dtype=np.float64)
+            if self.precomputed.shape != (bins.nkz, bins.nkz):
+                raise ValueError("Precomputed Fisher matrix does not have correct number of rows or columns.")
 
     def iterate(self) -> NRResult:
         nkz = self.bins.nkz
@@ -108,7 +116,9 @@ class QuadraticEstimator:
             self.engine.iterate(theta=fits, precision=self.precision)
             out = self.engine.download()
             dbt = np.stack([out["d"], out["b"], out["t"]])
-            g = self.engine.fisher_solve(out["fisher"], dbt)
+            # the solve takes the unhalved sum: twice the halved matrix, exactly
+            fsum = out["fisher"] if self.precomputed is None else 2.0 * self.precomputed
+            g = self.engine.fisher_solve(fsum, dbt)
             previous, current = current, g["theta"]
             converged, previous = has_converged(current, previous, g["inverse"], g["fisher"], g["dof"], self.eps)
             if converged or it == self.iterations:

@@ -46,6 +46,41 @@ def test_fiducial_power_is_zero_with_turn_off_baseline():
     assert (on.pfid > 0).all() and not off.pfid.any()
 
 
+def test_precomputed_fisher_shape_is_checked():
+    c = G.load("tiny_nosfid")
+    with pytest.raises(ValueError):
+        E.QuadraticEstimator(None, c.bins, precomputed_fisher=np.eye(3))
+    E.QuadraticEstimator(None, c.bins, precomputed_fisher=np.eye(c.bins.nkz))
+
+
+class _SumsOnly:
+    """Stands in for an engine run with skip_fisher (PrecomputedFisher): the
+    d, b, t sums of a fixture's chunks and a zero Fisher sum; the host solve."""
+
+    def __init__(self, c):
+        self.fsum, self.dbt = G.global_sums(c)
+
+    def iterate(self, theta=None, precision=None):
+        pass
+
+    def download(self):
+        return dict(fisher=np.zeros_like(self.fsum), d=self.dbt[0], b=self.dbt[1], t=self.dbt[2])
+
+    def fisher_solve(self, fsum, dbt):
+        from lyspeq_gb300 import lqg
+        return lqg.fisher_solve(fsum, dbt)
+
+
+def test_precomputed_fisher_replaces_the_sum(engine_lib):
+    """With the reference's own global Fisher matrix (halved) as the
+    PrecomputedFisher file and no Fisher matrices from the chunks, the
+    estimate is the reference's (core/quadratic_estimate.cpp:478-483)."""
+    c = G.load("desi_sub")
+    res = E.QuadraticEstimator(_SumsOnly(c), c.bins, precomputed_fisher=c.g["fisher"]).iterate()
+    assert G.rel_err(res.fisher, c.g["fisher"]) < 1e-15
+    assert G.rel_err(res.theta, c.g["theta"]) < 1e-9
+
+
 @pytest.mark.gpu
 def test_nr_loop_matches_reference(engine_lib):
     from lyspeq_gb300 import lqg
