@@ -159,14 +159,27 @@ class Engine:
         if rc != LQG_OK:
             raise RuntimeError(f"{what} failed ({rc}): {self.lib.lqg_last_error(self.h).decode()}")
 
+    @staticmethod
+    def _pixel_arrays(lam, delta, ivar, offsets):
+        """The concatenated pixel arrays and chunk offsets as the C ABI reads
+        them, checked here: it takes plain pointers and cannot."""
+        lam = np.ascontiguousarray(lam, dtype=np.float64).ravel()
+        delta = np.ascontiguousarray(delta, dtype=np.float64).ravel()
+        ivar = np.ascontiguousarray(ivar, dtype=np.float64).ravel()
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64).ravel()
+        if not (len(lam) == len(delta) == len(ivar)):
+            raise ValueError("lambda, delta and ivar differ in length")
+        if len(offsets) < 1 or offsets[0] < 0 or offsets[-1] > len(lam) or np.any(np.diff(offsets) < 0):
+            raise ValueError("offsets must rise from >= 0 to at most the number of pixels")
+        return lam, delta, ivar, offsets
+
     def add_chunks(self, lam, delta, ivar, offsets, r_fwhm):
         """Add chunks given as concatenated arrays; returns the per-chunk status."""
-        lam = np.ascontiguousarray(lam, dtype=np.float64)
-        delta = np.ascontiguousarray(delta, dtype=np.float64)
-        ivar = np.ascontiguousarray(ivar, dtype=np.float64)
-        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
-        r_fwhm = np.ascontiguousarray(r_fwhm, dtype=np.int32)
+        lam, delta, ivar, offsets = self._pixel_arrays(lam, delta, ivar, offsets)
+        r_fwhm = np.ascontiguousarray(r_fwhm, dtype=np.int32).ravel()
         n = len(offsets) - 1
+        if len(r_fwhm) != n:
+            raise ValueError("one r_fwhm per chunk")
         status = np.zeros(max(n, 1), dtype=np.int32)
         rc = self.lib.lqg_batch_add(self.h, n, offsets.ctypes.data_as(C.POINTER(C.c_int64)),
                                     _dptr(lam), _dptr(delta), _dptr(ivar), _iptr(r_fwhm),
@@ -187,10 +200,7 @@ class Engine:
     def add_chunks_reso(self, lam, delta, ivar, offsets, oversampling, resomat):
         """Add chunks with resolution matrices: resomat has one row of nelem
         values per pixel (see lqg_batch_add_reso); returns the per-chunk status."""
-        lam = np.ascontiguousarray(lam, dtype=np.float64)
-        delta = np.ascontiguousarray(delta, dtype=np.float64)
-        ivar = np.ascontiguousarray(ivar, dtype=np.float64)
-        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        lam, delta, ivar, offsets = self._pixel_arrays(lam, delta, ivar, offsets)
         rm = np.ascontiguousarray(resomat, dtype=np.float64)
         if rm.ndim != 2 or rm.shape[0] != len(lam):
             raise ValueError("resomat must have one row per pixel")
@@ -225,6 +235,8 @@ class Engine:
         cov = np.zeros((nkz, nkz)) if solver is not None else None
         real = np.zeros((nboots, nkz)) if realizations else None
         sv = None if solver is None else np.ascontiguousarray(solver, dtype=np.float64)
+        if sv is not None and sv.shape != (nkz, nkz):
+            raise ValueError(f"solver must be {nkz} x {nkz}")
         rc = self.lib.lqg_bootstrap(self.h, len(off) - 1, _iptr(off), int(nboots), int(seed), _dptr(sv),
                                     _dptr(mean), _dptr(cov), _dptr(fcov), _dptr(real))
         self._check(rc, "lqg_bootstrap")
@@ -256,15 +268,23 @@ class Engine:
                 "input_index")
         return dict(zip(keys, (int(x) for x in info)))
 
+    def _theta(self, theta):
+        if theta is None:
+            return None
+        th = np.ascontiguousarray(theta, dtype=np.float64).ravel()
+        if len(th) != self.nkz:
+            raise ValueError(f"theta must have {self.nkz} values")
+        return th
+
     def iterate(self, theta=None, precision="fp64"):
-        th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+        th = self._theta(theta)
         rc = self.lib.lqg_nr_iteration(self.h, _dptr(th), PRECISION[precision])
         self._check(rc, "lqg_nr_iteration")
 
     def iterate_async(self, theta=None, precision="fp64", stream=None):
         """lqg_nr_iteration_async on a cudaStream_t handle (an int, e.g.
         torch.cuda.Stream.cuda_stream) or None; complete with sync()."""
-        th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+        th = self._theta(theta)
         rc = self.lib.lqg_nr_iteration_async(self.h, _dptr(th), PRECISION[precision],
                                              None if stream is None else C.c_void_p(stream))
         self._check(rc, "lqg_nr_iteration_async")
@@ -309,6 +329,8 @@ class Engine:
         n = self.nkz
         fs = np.ascontiguousarray(fisher_sum, dtype=np.float64)
         db = np.ascontiguousarray(dbt, dtype=np.float64)
+        if fs.shape != (n, n) or db.shape != (3, n):
+            raise ValueError(f"fisher_sum must be {n} x {n} and dbt 3 x {n}")
         out = {k: np.zeros((n, n)) for k in ("fisher", "solver", "inverse")}
         w = np.zeros((3, n))
         th = np.zeros(n)
