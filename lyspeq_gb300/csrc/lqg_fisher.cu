@@ -204,9 +204,19 @@ void spd_inverse(const Mat &L, const Mat &U, int n, Mat &inv) {
     if (nt == 1 || n < 64) {
         columns(0, 1);
     } else {
+        // columns t, t + nt, ... on thread t; a thread the system does not
+        // grant runs its columns here instead
         std::vector<std::thread> pool;
-        for (int t = 1; t < nt; ++t) pool.emplace_back(columns, t, nt);
+        std::vector<int> inline_first;
+        for (int t = 1; t < nt; ++t) {
+            try {
+                pool.emplace_back(columns, t, nt);
+            } catch (...) {
+                inline_first.push_back(t);
+            }
+        }
         columns(0, nt);
+        for (int t : inline_first) columns(t, nt);
         for (auto &th : pool) th.join();
     }
 }
@@ -300,9 +310,14 @@ extern "C" int lqg_fisher_solve_n(int n, const double *fisher_sum, const double 
     const bool spd = spd_factor(S, n, L, U);
     bool possible = true;
     if (spd) {
-        std::thread test([&] { possible = damping_possible(L, U, n); });
+        std::thread test;
+        try {
+            test = std::thread([&] { possible = damping_possible(L, U, n); });
+        } catch (...) {
+            possible = damping_possible(L, U, n);   // no thread granted: in turn
+        }
         spd_inverse(L, U, n, spd_inv);
-        test.join();
+        if (test.joinable()) test.join();
     }
     double damp = 0;
     if (possible) {

@@ -265,7 +265,8 @@ inline bool once_per_device(std::atomic<unsigned long long> &done, Fn fn) {
 
 // fn(i) for i in [0, n) on up to 16 host threads (the calling one included),
 // handed out `grain` at a time; serial when n <= grain.  fn must not throw
-// and must write no state that another i writes.
+// and must write no state that another i writes.  A thread the system does
+// not grant is simply not used: the others take its share.
 template <class Fn>
 inline void host_parallel_for(int n, int grain, Fn fn) {
     if (n <= 0) return;
@@ -282,7 +283,13 @@ inline void host_parallel_for(int n, int grain, Fn fn) {
     };
     std::vector<std::thread> pool;
     pool.reserve(nt - 1);
-    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    for (int t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(worker);
+        } catch (...) {
+            break;
+        }
+    }
     worker();
     for (auto &th : pool) th.join();
 }
