@@ -157,6 +157,32 @@ extern "C" const char *lqg_last_error(const lqg_ctx *ctx) {
     return ctx ? ctx->err.c_str() : "null context";
 }
 
+namespace {
+
+// The context's binning, table list and options: everything Chunk::Chunk
+// reads, all host-side (no CUDA call).
+void set_host_fields(lqg_ctx *ctx, const lqg_bins *bins, const lqg_tables *tables, const lqg_opts *opts) {
+    ctx->nk = bins->nk;
+    ctx->nz = bins->nz;
+    ctx->nkz = bins->nk * bins->nz;
+    ctx->dz = bins->z_bin_width;
+    ctx->triangular = bins->triangular;
+    ctx->k_edges.assign(bins->k_edges, bins->k_edges + bins->nk + 1);
+    ctx->k_centers.clear();
+    for (int k = 0; k < bins->nk; ++k)
+        ctx->k_centers.push_back((ctx->k_edges[k] + ctx->k_edges[k + 1]) / 2.);
+    ctx->z_centers.assign(bins->z_centers, bins->z_centers + bins->nz);
+    ctx->n_tables = tables->n_tables;
+    ctx->nv = tables->nv;
+    ctx->nzp = tables->nzp;
+    ctx->lenv = tables->v_length;
+    ctx->r_fwhm.assign(tables->r_fwhm, tables->r_fwhm + tables->n_tables);
+    ctx->tdv.assign(tables->dv, tables->dv + tables->n_tables);
+    ctx->opts = *opts;
+}
+
+}  // namespace
+
 extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tables *tables,
                               const lqg_opts *opts, int device) {
     cudaGetLastError();   // an error left by earlier work of the process is not this call's
@@ -183,22 +209,7 @@ extern "C" int lqg_ctx_create(lqg_ctx **out, const lqg_bins *bins, const lqg_tab
     if (cudaSetDevice(device) != cudaSuccess) return LQG_ERR_CUDA;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         return LQG_ERR_CUDA;
-    ctx->nk = bins->nk;
-    ctx->nz = bins->nz;
-    ctx->nkz = bins->nk * bins->nz;
-    ctx->dz = bins->z_bin_width;
-    ctx->triangular = bins->triangular;
-    ctx->k_edges.assign(bins->k_edges, bins->k_edges + bins->nk + 1);
-    for (int k = 0; k < bins->nk; ++k)
-        ctx->k_centers.push_back((ctx->k_edges[k] + ctx->k_edges[k + 1]) / 2.);
-    ctx->z_centers.assign(bins->z_centers, bins->z_centers + bins->nz);
-    ctx->n_tables = tables->n_tables;
-    ctx->nv = tables->nv;
-    ctx->nzp = tables->nzp;
-    ctx->lenv = tables->v_length;
-    ctx->r_fwhm.assign(tables->r_fwhm, tables->r_fwhm + tables->n_tables);
-    ctx->tdv.assign(tables->dv, tables->dv + tables->n_tables);
-    ctx->opts = *opts;
+    set_host_fields(ctx.get(), bins, tables, opts);
     // interpolation grids, core/sq_table.cpp:148-175 and :352-362
     ctx->grid.nv = tables->nv;
     ctx->grid.nzp = tables->nzp;
@@ -569,6 +580,36 @@ extern "C" int lqg_batch_add_reso(lqg_ctx *ctx, int n_chunks, const int64_t *off
                                                  "engine's tile (31 oversampling + nelem <= 128, nelem <= 48)");
     return add_chunks(ctx, n_chunks, offsets, lambda, delta, ivar, nullptr, oversampling, nelem, resomat,
                       status_out);
+}
+
+extern "C" int lqg_chunk_plan(const lqg_bins *bins, const lqg_tables *tables, const lqg_opts *opts,
+                              int n_chunks, const int64_t *offsets, const double *lambda, const double *delta,
+                              const double *ivar, const int *r_fwhm, int *status_out, int *info_out) {
+    if (!bins || !tables || !opts || n_chunks < 0 || !status_out || !info_out ||
+        (n_chunks > 0 && (!offsets || !lambda || !delta || !ivar || !r_fwhm)))
+        return LQG_ERR_ARG;
+    if (bins->nk <= 0 || bins->nk > kMaxKBands || bins->nz <= 0 || bins->nz > 64 || !bins->k_edges ||
+        !bins->z_centers || !(bins->z_bin_width > 0) || tables->n_tables <= 0 || !tables->r_fwhm || !tables->dv ||
+        !(opts->max_mean_pixel_size > 0) || !(opts->max_forest_length >= 0))
+        return LQG_ERR_ARG;
+    for (int c = 0; c < n_chunks; ++c)
+        if (offsets[c + 1] < offsets[c]) return LQG_ERR_ARG;
+    lqg_ctx host;   // binning and tables only: nothing on a device
+    set_host_fields(&host, bins, tables, opts);
+    host_parallel_for(n_chunks, 16, [&](int c) {
+        ChunkSetup u;
+        setup_chunk(&host, c, offsets, lambda, delta, ivar, r_fwhm, 0, 0, nullptr, u);
+        status_out[c] = u.st;
+        int *info = info_out + 8 * (size_t) c;
+        if (u.st != LQG_CHUNK_OK) {
+            std::fill(info, info + 8, 0);
+            return;
+        }
+        const auto &h = u.hc;
+        const int v[8] = {h.n, h.fis, h.nq, h.kbin_upp, h.res, h.zlow, h.zupp, c};
+        std::copy(v, v + 8, info);
+    });
+    return LQG_OK;
 }
 
 extern "C" int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info) {

@@ -28,7 +28,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients",
            "lqg_resomat_smooth", "lqg_fisher_solve_n", "lqg_set_wait_limit", "lqg_factor_noalloc",
            "lqg_probe_fp64_rate", "lqg_nr_iteration_async", "lqg_sync", "lqg_autotune", "lqg_tuning_get",
-           "lqg_tuning_set", "lqg_set_fisher_optimization"]
+           "lqg_tuning_set", "lqg_set_fisher_optimization", "lqg_chunk_plan"]
 
 
 class LqgBins(C.Structure):
@@ -86,6 +86,8 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
+    lib.lqg_chunk_plan.argtypes = [C.POINTER(LqgBins), C.POINTER(LqgTables), C.POINTER(LqgOpts), C.c_int,
+                                   C.POINTER(C.c_int64), dp, dp, dp, ip, ip, ip]
     lib.lqg_nr_iteration.argtypes = [vp, dp, C.c_int]
     lib.lqg_download.argtypes = [vp, dp, dp, dp, dp, ip]
     lib.lqg_chunk_result.argtypes = [vp, C.c_int, dp, dp, dp, dp]
@@ -372,6 +374,34 @@ def probe_fp64_rate(device=0):
     if rc != LQG_OK:
         raise RuntimeError(f"lqg_probe_fp64_rate failed ({rc})")
     return out.value
+
+
+def chunk_plan(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_length, max_mean_pixel_size=150.0):
+    """What an Engine's add_chunks would make of the chunks, without a context
+    or a GPU (lqg_chunk_plan): per chunk its status and, when accepted, the
+    chunk_info fields (a dict as Engine.chunk_info returns; None if rejected)."""
+    lib = load_library()
+    lam, delta, ivar, offsets = Engine._pixel_arrays(lam, delta, ivar, offsets)
+    r_fwhm = np.ascontiguousarray(r_fwhm, dtype=np.int32).ravel()
+    n = len(offsets) - 1
+    if len(r_fwhm) != n:
+        raise ValueError("one r_fwhm per chunk")
+    k_edges = np.ascontiguousarray(bins.k_edges, dtype=np.float64)
+    z = np.ascontiguousarray(bins.z_centers, dtype=np.float64)
+    r = np.ascontiguousarray([t.r_fwhm for t in tables], dtype=np.int32)
+    dv = np.ascontiguousarray([t.dv for t in tables], dtype=np.float64)
+    b = LqgBins(bins.nk, bins.nz, _dptr(k_edges), _dptr(z), bins.dz, 1 if bins.triangular else 0)
+    t = LqgTables(len(tables), _iptr(r), _dptr(dv), 2, 1.0, 2, None, None)
+    o = LqgOpts(float(max_forest_length), float(max_mean_pixel_size), -1, -1, 0, 0, 0, -1, 0, 0.0)
+    status = np.zeros(max(n, 1), dtype=np.int32)
+    info = np.zeros(8 * max(n, 1), dtype=np.int32)
+    rc = lib.lqg_chunk_plan(C.byref(b), C.byref(t), C.byref(o), n, offsets.ctypes.data_as(C.POINTER(C.c_int64)),
+                            _dptr(lam), _dptr(delta), _dptr(ivar), _iptr(r_fwhm), _iptr(status), _iptr(info))
+    if rc != LQG_OK:
+        raise RuntimeError(f"lqg_chunk_plan failed ({rc})")
+    keys = ("n", "fisher_index_start", "nq", "kbin_upp", "res_index", "zbin_low", "zbin_upp", "input_index")
+    return status[:n], [dict(zip(keys, (int(x) for x in info[8 * i:8 * i + 8]))) if status[i] == 0 else None
+                        for i in range(n)]
 
 
 def fisher_solve(fisher_sum, dbt):
