@@ -38,6 +38,20 @@ def _free_port():
         return s.getsockname()[1]
 
 
+def test_plan_costs_follow_the_chunks(engine_lib):
+    """Costs from lqg_chunk_plan before any engine: chunk_cost(n, stored
+    matrices) of each golden chunk, 0 for one the engine would reject."""
+    import golden_cases as G
+    c = G.load("desi_sub")
+    chunks = list(c.chunks) + [(c.chunks[0][0], c.chunks[0][1], c.chunks[0][2], 12345)]   # no such table
+    offs = np.cumsum([0] + [len(x[0]) for x in chunks])
+    cat = lambda j: np.concatenate([np.asarray(x[j], dtype=np.float64) for x in chunks])
+    costs = D.plan_costs(c.bins, c.tables, cat(0), cat(1), cat(2), offs, [x[3] for x in chunks],
+                         c.max_forest_length)
+    want = [D.chunk_cost(m[0], m[2] // c.bins.nk * m[3]) for m in c.meta] + [0.0]
+    assert costs == want and all(x > 0 for x in costs[:-1])
+
+
 def _rank_main(rank, world, port, out_path):
     import torch.distributed as dist
     from lyspeq_gb300 import synth
