@@ -85,6 +85,7 @@ def load_library(path: str = LIB_PATH):
                                                C.POINTER(C.c_ubyte)]
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
+    lib.lqg_abi_version.argtypes = []
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
     lib.lqg_chunk_plan.argtypes = [C.POINTER(LqgBins), C.POINTER(LqgTables), C.POINTER(LqgOpts), C.c_int,
                                    C.POINTER(C.c_int64), dp, dp, dp, ip, ip, ip]
