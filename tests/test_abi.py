@@ -35,3 +35,15 @@ def test_tuning_field_count_matches_the_header():
     text = open(HEADER).read()
     m = re.search(r"#define LQG_TUNING_FIELDS (\d+)", text)
     assert m and int(m.group(1)) == lqg.TUNING_FIELDS
+
+
+def test_python_mirror_types_every_entry_point():
+    """lyspeq_gb300/lqg.py declares the argument types of every function of
+    include/lqg.h and lists it among the exports it checks."""
+    import re
+    from lyspeq_gb300 import lqg
+    declared = set(re.findall(r"^(?:int|const char \*|double|void)\s*\*?\s*(lqg_[a-z_0-9]+)\s*\(",
+                              open(HEADER).read(), re.M))
+    typed = set(re.findall(r"lib\.(lqg_[a-z_0-9]+)\.argtypes", open(lqg.__file__).read()))
+    assert declared and declared == typed
+    assert declared == set(lqg.EXPORTS)
