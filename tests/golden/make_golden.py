@@ -62,6 +62,9 @@ CASES = {
     "tiny_tophat": ("tiny", None, (1, -1), 0.0, None),
     # TurnOffBaseline: C without the fiducial signal, no t trace
     "tiny_nosfid": ("tiny", None, (1, -1), 0.0, None),
+    # DESI-size chunks with resolution matrices (11 diagonals deconvolved and
+    # oversampled x3, N 160-634): the resolution path at the sizes it runs at
+    "desi_reso_sub": ("desi_reso", 6, (-1, -1), 0.0, None),
     # the reference built with --enable-fisher-optimization (-DFISHER_OPTIMIZATION):
     # only the Fisher bands |dj| <= 5 and |dj - Nk| <= 2 are computed
     "desi_fopt": ("desi", 6, (1, -1), 0.0, None),

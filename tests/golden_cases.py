@@ -16,6 +16,9 @@ RESO_CASES = ["tiny_reso", "tiny_reso_dia", "tiny_reso_growth", "tiny_reso_smoot
 # from the reference built with FISHER_OPTIMIZATION (banded chunk Fisher
 # matrices); kept out of CASES, whose tests run the full matrices
 FOPT_CASES = ["desi_fopt"]
+# DESI-size chunks with resolution matrices; kept out of CASES and RESO_CASES
+# (their GPU check is tests/test_zzz_reso_sizes.py)
+RESO_SIZE_CASES = ["desi_reso_sub"]
 
 
 @dataclasses.dataclass

@@ -112,7 +112,7 @@ def test_table_builder_reproduces_truth_table():
 TOL = {"tiny_marg3": 1e-7}
 
 
-@pytest.mark.parametrize("name", G.CASES + G.FOPT_CASES)
+@pytest.mark.parametrize("name", G.CASES + G.FOPT_CASES + G.RESO_SIZE_CASES)
 def test_port_matches_reference(name):
     c = G.load(name)
     tol = TOL.get(name, 1e-12)
@@ -143,7 +143,7 @@ def test_port_matches_reference(name):
         assert G.rel_err(g["theta"], c.g["theta"]) < max(tol, 1e-10)
 
 
-@pytest.mark.parametrize("name", G.RESO_CASES)
+@pytest.mark.parametrize("name", G.RESO_CASES + G.RESO_SIZE_CASES)
 def test_port_resolution_preprocessing_matches_reference(name):
     """Deconvolution and oversampling of each spectrum's resolution matrix
     (core/one_qso_estimate.cpp:75-89), cut to a chunk's pixels, give the

@@ -17,7 +17,7 @@ import golden_cases as G
 from oracle import qmle_port as P
 
 
-@pytest.mark.parametrize("name", G.RESO_CASES)
+@pytest.mark.parametrize("name", G.RESO_CASES + G.RESO_SIZE_CASES)
 def test_library_preprocessing_matches_reference(engine_lib, name):
     from lyspeq_gb300 import lqg
     c = G.load(name)
