@@ -22,7 +22,9 @@ theta update.  Steps alternate between the two kinds an NR run is made of:
 the first iteration (theta = 0) and a later one (theta from the previous
 solve, which adds sum theta_k Q_k to C).  `value` times steps with the chunks
 resident on the device; `e2e` times the same through the C ABI from host
-buffers (chunk upload, iteration, result download, solve).
+buffers (chunk upload, iteration, result download, solve), and reports the
+host time of each step's batch add (Chunk::Chunk and the pixel arrays) as
+`batch_add_ms`.
 
 Beside it: the FP64 GPU path on a subset stratified by chunk size (both kinds
 of iteration) with the mixed path's errors against it, a DFMA probe for the
@@ -424,9 +426,12 @@ def main():
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
     e2.record()
+    add_s = 0.0
     for k in range(args.steps):
+        t_add = time.perf_counter()
         eng.clear()
         add_packed(eng, w, packed)
+        add_s += time.perf_counter() - t_add      # host: Chunk::Chunk and the pixel arrays
         nr_step(thetas[(args.warmup + k) % 2])
     e3.record()
     barrier()
@@ -549,7 +554,7 @@ def main():
                    "l2": "working set of tens of GB per iteration (>> 129 MB L2); no flush"},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": ms_e2e},
+                "ms_per_step": ms_e2e, "batch_add_ms": add_s * 1e3 / args.steps},
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
