@@ -427,12 +427,14 @@ def main():
     e3 = torch.cuda.Event(enable_timing=True)
     e2.record()
     add_s = 0.0
+    h2d_sum = 0
     for k in range(args.steps):
         t_add = time.perf_counter()
         eng.clear()
         add_packed(eng, w, packed)
         add_s += time.perf_counter() - t_add      # host: Chunk::Chunk and the pixel arrays
         nr_step(thetas[(args.warmup + k) % 2])
+        h2d_sum += eng.h2d_bytes()                # what the library copied for this step
     e3.record()
     barrier()
     ms_e2e = e2.elapsed_time(e3) / args.steps
@@ -444,8 +446,12 @@ def main():
     for _ in range(5):
         eng.fisher_solve(out["fisher"], dbt)
     solve_ms = (time.perf_counter() - t0) / 5 * 1e3
-    h2d = int(lam.nbytes + delta.nbytes + ivar.nbytes + 8 * nkz + (rr.nbytes if w.reso else 0))
-    d2h = int(8 * (nkz * nkz + 3 * nkz))
+    # bytes copied per e2e step: host to device as the library counts them (the
+    # batch's derived pixel arrays and metadata, theta, the launch plan), device
+    # to host the sums and the chunk statuses the download reads
+    h2d = int(round(h2d_sum / max(args.steps, 1)))
+    input_bytes = int(lam.nbytes + delta.nbytes + ivar.nbytes + 8 * nkz + (rr.nbytes if w.reso else 0))
+    d2h = int(8 * (nkz * nkz + 3 * nkz) + 4 * eng.size)
 
     if rank != 0:
         if world > 1:
@@ -554,7 +560,8 @@ def main():
                    "l2": "working set of tens of GB per iteration (>> 129 MB L2); no flush"},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": ms_e2e, "batch_add_ms": add_s * 1e3 / args.steps},
+                "ms_per_step": ms_e2e, "batch_add_ms": add_s * 1e3 / args.steps,
+                "input_bytes_per_step": input_bytes},
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),

@@ -373,6 +373,10 @@ int lqg_last_launch_count(const lqg_ctx *ctx);
 /* Number of size-bucketed waves of the last iteration: each phase-B kernel
  * (Q build, products, traces, reduction) is launched once per wave. */
 int lqg_last_wave_count(const lqg_ctx *ctx);
+/* Bytes the last iteration copied from host to device: the batch's pixel
+ * arrays and chunk metadata when the batch changed since the previous
+ * iteration, theta, and the launch plan's descriptors. */
+int lqg_last_h2d_bytes(const lqg_ctx *ctx, int64_t *bytes);
 
 /* Limit of every wait inside the tensor-core kernels of later iterations
  * (seconds, at most 60; 0 restores the default of 2 s).  A wait that runs out

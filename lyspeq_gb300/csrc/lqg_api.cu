@@ -47,6 +47,7 @@ struct lqg_ctx {
     lqg_opts opts{};
     uint64_t wait_ns = 0;   // lqg_set_wait_limit; 0: the kernels' 2 s
     int fisher_band = 0;    // lqg_set_fisher_optimization: banded chunk Fisher matrices
+    int64_t h2d_bytes = 0;  // bytes the last iteration copied host to device (lqg_last_h2d_bytes)
     // LQG_PRECISION_MIXED_AUTO: per padded size ld, the mixed form, the drain
     // interval of the products and the Gram's K split (lqg_autotune)
     struct Tune {
@@ -674,6 +675,7 @@ int upload_pixels(lqg_ctx *ctx) {
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_meta.p, meta.data(), meta.size() * sizeof(ChunkDesc),
                                        cudaMemcpyHostToDevice, s));
     LQG_CUDA_CHECK_RET(cudaStreamSynchronize(s));
+    ctx->h2d_bytes += (int64_t) (np * 8 * 10 + nfp * 16 + nrw * 8 + meta.size() * sizeof(ChunkDesc));
     ctx->pix_dirty = false;
     return LQG_OK;
 }
@@ -1021,6 +1023,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     cudaSetDevice(ctx->device);
     int rc = finish_pending(ctx);
     if (rc) return rc;
+    ctx->h2d_bytes = 0;
     if ((rc = upload_pixels(ctx))) return rc;
     cudaStream_t st = ctx->stream;
     if (after && after != st) {
@@ -1034,6 +1037,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
     if (theta) {
         for (int i = 0; i < ctx->nkz; ++i) use_theta |= theta[i] != 0.0;
         LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_theta.p, theta, ctx->nkz * 8, cudaMemcpyHostToDevice, st));
+        ctx->h2d_bytes += (int64_t) ctx->nkz * 8;
     }
     const int nb = (int) ctx->chunks.size();
     ctx->last_status.assign(nb, LQG_CHUNK_OK);
@@ -1126,6 +1130,7 @@ int enqueue_iteration(lqg_ctx *ctx, const double *theta, int precision, cudaStre
                                        cudaMemcpyHostToDevice, st));
     LQG_CUDA_CHECK_RET(cudaMemcpyAsync(ctx->d_scales.p, hs + desc.size() * sizeof(ChunkDesc) + jobs.size() * 4,
                                        scales.size() * 8, cudaMemcpyHostToDevice, st));
+    ctx->h2d_bytes += (int64_t) (desc.size() * sizeof(ChunkDesc) + jobs.size() * 4 + scales.size() * 8);
     LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_status.p, 0, std::max(nb, 1) * 4, st));
     LQG_CUDA_CHECK_RET(cudaMemsetAsync(ctx->d_check.p, 0, 4 * sizeof(unsigned long long), st));
 
@@ -1527,6 +1532,12 @@ extern "C" int lqg_bootstrap_coefficients(int n_qso, int nboots, unsigned long l
 }
 
 extern "C" int lqg_last_wave_count(const lqg_ctx *ctx) { return ctx ? ctx->waves : 0; }
+
+extern "C" int lqg_last_h2d_bytes(const lqg_ctx *ctx, int64_t *bytes) {
+    if (!ctx || !bytes) return LQG_ERR_ARG;
+    *bytes = ctx->h2d_bytes;
+    return LQG_OK;
+}
 
 extern "C" int lqg_set_wait_limit(lqg_ctx *ctx, double seconds) {
     if (!ctx || !(seconds >= 0.0) || seconds > 60.0) return LQG_ERR_ARG;

@@ -28,7 +28,7 @@ EXPORTS = ["lqg_abi_version", "lqg_ctx_create", "lqg_ctx_destroy", "lqg_last_err
            "lqg_bootstrap", "lqg_smooth_ivar", "lqg_bootstrap_complete", "lqg_bootstrap_coefficients",
            "lqg_resomat_smooth", "lqg_fisher_solve_n", "lqg_set_wait_limit", "lqg_factor_noalloc",
            "lqg_probe_fp64_rate", "lqg_nr_iteration_async", "lqg_sync", "lqg_autotune", "lqg_tuning_get",
-           "lqg_tuning_set", "lqg_set_fisher_optimization", "lqg_chunk_plan"]
+           "lqg_tuning_set", "lqg_set_fisher_optimization", "lqg_chunk_plan", "lqg_last_h2d_bytes"]
 
 
 class LqgBins(C.Structure):
@@ -86,6 +86,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_batch_clear.argtypes = [vp]
     lib.lqg_batch_size.argtypes = [vp]
     lib.lqg_abi_version.argtypes = []
+    lib.lqg_last_h2d_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
     lib.lqg_chunk_plan.argtypes = [C.POINTER(LqgBins), C.POINTER(LqgTables), C.POINTER(LqgOpts), C.c_int,
                                    C.POINTER(C.c_int64), dp, dp, dp, ip, ip, ip]
@@ -357,6 +358,12 @@ class Engine:
 
     def wave_count(self):
         return self.lib.lqg_last_wave_count(self.h)
+
+    def h2d_bytes(self):
+        """Bytes the last iteration copied host to device (lqg_last_h2d_bytes)."""
+        v = C.c_int64(0)
+        self._check(self.lib.lqg_last_h2d_bytes(self.h, C.byref(v)), "lqg_last_h2d_bytes")
+        return int(v.value)
 
     def set_wait_limit(self, seconds):
         """Limit of the tensor-core kernels' waits (0: the default 2 s)."""
