@@ -224,9 +224,11 @@ int lqg_batch_size(const lqg_ctx *ctx);
  * zbin_low, zbin_upp, input index (position in the lqg_batch_add call). */
 int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info);
 
-/* What lqg_batch_add would make of each chunk, without a context or a GPU:
- * Chunk::Chunk's checks and numbers (core/chunk_estimate.cpp:141-257) for the
- * same arguments.  status_out[n_chunks] gets LQG_CHUNK_* and
+/* What lqg_batch_add (resomat NULL) or lqg_batch_add_reso (resomat, with its
+ * oversampling and nelem; r_fwhm may then be NULL) would make of each chunk,
+ * without a context or a GPU: Chunk::Chunk's checks and numbers
+ * (core/chunk_estimate.cpp:141-257) for the same arguments, from the same
+ * code.  status_out[n_chunks] gets LQG_CHUNK_* and
  * info_out[8 * n_chunks] the lqg_chunk_info fields of each accepted chunk
  * (input index = its position in this call; zeros for a rejected one).  Of
  * tables only n_tables, r_fwhm and dv are read (deriv and signal may be
@@ -236,7 +238,8 @@ int lqg_chunk_info(const lqg_ctx *ctx, int i, int *info);
  * (n_q_matrices / NUMBER_OF_K_BANDS) * kbin_upp stored matrices. */
 int lqg_chunk_plan(const lqg_bins *bins, const lqg_tables *tables, const lqg_opts *opts, int n_chunks,
                    const int64_t *offsets, const double *lambda, const double *delta, const double *ivar,
-                   const int *r_fwhm, int *status_out, int *info_out);
+                   const int *r_fwhm, int oversampling, int nelem, const double *resomat, int *status_out,
+                   int *info_out);
 
 /* One Newton-Raphson iteration over the whole batch: for every chunk build
  * S and Q_k from the tables, C = S + sum theta_k Q_k + N, invert, continuum

@@ -585,10 +585,18 @@ extern "C" int lqg_batch_add_reso(lqg_ctx *ctx, int n_chunks, const int64_t *off
 
 extern "C" int lqg_chunk_plan(const lqg_bins *bins, const lqg_tables *tables, const lqg_opts *opts,
                               int n_chunks, const int64_t *offsets, const double *lambda, const double *delta,
-                              const double *ivar, const int *r_fwhm, int *status_out, int *info_out) {
+                              const double *ivar, const int *r_fwhm, int oversampling, int nelem,
+                              const double *resomat, int *status_out, int *info_out) {
+    const bool reso = resomat != nullptr;
     if (!bins || !tables || !opts || n_chunks < 0 || !status_out || !info_out ||
-        (n_chunks > 0 && (!offsets || !lambda || !delta || !ivar || !r_fwhm)))
+        (n_chunks > 0 && (!offsets || !lambda || !delta || !ivar || (!reso && !r_fwhm))))
         return LQG_ERR_ARG;
+    if (reso) {
+        // the checks of lqg_batch_add_reso
+        const int os = oversampling > 0 ? oversampling : 1;
+        if (nelem < 1 || nelem % 2 == 0) return LQG_ERR_ARG;
+        if (nelem > kResoMaxElem || (kResoTile - 1) * os + nelem > kResoMaxFine) return LQG_ERR_UNSUPPORTED;
+    }
     if (bins->nk <= 0 || bins->nk > kMaxKBands || bins->nz <= 0 || bins->nz > 64 || !bins->k_edges ||
         !bins->z_centers || !(bins->z_bin_width > 0) || tables->n_tables <= 0 || !tables->r_fwhm || !tables->dv ||
         !(opts->max_mean_pixel_size > 0) || !(opts->max_forest_length >= 0))
@@ -599,7 +607,8 @@ extern "C" int lqg_chunk_plan(const lqg_bins *bins, const lqg_tables *tables, co
     set_host_fields(&host, bins, tables, opts);
     host_parallel_for(n_chunks, 16, [&](int c) {
         ChunkSetup u;
-        setup_chunk(&host, c, offsets, lambda, delta, ivar, r_fwhm, 0, 0, nullptr, u);
+        setup_chunk(&host, c, offsets, lambda, delta, ivar, r_fwhm, reso ? oversampling : 0, reso ? nelem : 0,
+                    resomat, u);
         status_out[c] = u.st;
         int *info = info_out + 8 * (size_t) c;
         if (u.st != LQG_CHUNK_OK) {

@@ -23,13 +23,15 @@ def chunk_cost(n_pix: int, n_stored: int) -> float:
     return (2.0 * (n_stored + 1) + 1.0) * n ** 3
 
 
-def plan_costs(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_length, max_mean_pixel_size=150.0):
-    """chunk_cost of every chunk of an add_chunks call before any engine exists,
-    from lqg_chunk_plan (the pre-pass lyspeq makes for its load balancing,
+def plan_costs(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_length, max_mean_pixel_size=150.0,
+               oversampling=0, resomat=None):
+    """chunk_cost of every chunk of an add_chunks (or, with resomat,
+    add_chunks_reso) call before any engine exists, from lqg_chunk_plan (the
+    pre-pass lyspeq makes for its load balancing,
     OneQSOEstimate::getComputeTimeEst); 0 for a chunk the engine would reject."""
     from . import lqg
     _, info = lqg.chunk_plan(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_length,
-                             max_mean_pixel_size)
+                             max_mean_pixel_size, oversampling=oversampling, resomat=resomat)
     return [0.0 if i is None else chunk_cost(i["n"], i["nq"] // bins.nk * i["kbin_upp"]) for i in info]
 
 

@@ -89,7 +89,7 @@ def load_library(path: str = LIB_PATH):
     lib.lqg_last_h2d_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.lqg_chunk_info.argtypes = [vp, C.c_int, ip]
     lib.lqg_chunk_plan.argtypes = [C.POINTER(LqgBins), C.POINTER(LqgTables), C.POINTER(LqgOpts), C.c_int,
-                                   C.POINTER(C.c_int64), dp, dp, dp, ip, ip, ip]
+                                   C.POINTER(C.c_int64), dp, dp, dp, ip, C.c_int, C.c_int, dp, ip, ip]
     lib.lqg_nr_iteration.argtypes = [vp, dp, C.c_int]
     lib.lqg_download.argtypes = [vp, dp, dp, dp, dp, ip]
     lib.lqg_chunk_result.argtypes = [vp, C.c_int, dp, dp, dp, dp]
@@ -384,14 +384,23 @@ def probe_fp64_rate(device=0):
     return out.value
 
 
-def chunk_plan(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_length, max_mean_pixel_size=150.0):
-    """What an Engine's add_chunks would make of the chunks, without a context
-    or a GPU (lqg_chunk_plan): per chunk its status and, when accepted, the
-    chunk_info fields (a dict as Engine.chunk_info returns; None if rejected)."""
+def chunk_plan(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_length, max_mean_pixel_size=150.0,
+               oversampling=0, resomat=None):
+    """What an Engine's add_chunks (resomat None) or add_chunks_reso (resomat:
+    one row of nelem values per pixel, with oversampling) would make of the
+    chunks, without a context or a GPU (lqg_chunk_plan): per chunk its status
+    and, when accepted, the chunk_info fields (a dict as Engine.chunk_info
+    returns; None if rejected)."""
     lib = load_library()
     lam, delta, ivar, offsets = Engine._pixel_arrays(lam, delta, ivar, offsets)
-    r_fwhm = np.ascontiguousarray(r_fwhm, dtype=np.int32).ravel()
     n = len(offsets) - 1
+    rm = None
+    if resomat is not None:
+        rm = np.ascontiguousarray(resomat, dtype=np.float64)
+        if rm.ndim != 2 or rm.shape[0] != len(lam):
+            raise ValueError("resomat must have one row per pixel")
+        r_fwhm = np.zeros(n, dtype=np.int32)
+    r_fwhm = np.ascontiguousarray(r_fwhm, dtype=np.int32).ravel()
     if len(r_fwhm) != n:
         raise ValueError("one r_fwhm per chunk")
     k_edges = np.ascontiguousarray(bins.k_edges, dtype=np.float64)
@@ -404,7 +413,8 @@ def chunk_plan(bins, tables, lam, delta, ivar, offsets, r_fwhm, max_forest_lengt
     status = np.zeros(max(n, 1), dtype=np.int32)
     info = np.zeros(8 * max(n, 1), dtype=np.int32)
     rc = lib.lqg_chunk_plan(C.byref(b), C.byref(t), C.byref(o), n, offsets.ctypes.data_as(C.POINTER(C.c_int64)),
-                            _dptr(lam), _dptr(delta), _dptr(ivar), _iptr(r_fwhm), _iptr(status), _iptr(info))
+                            _dptr(lam), _dptr(delta), _dptr(ivar), _iptr(r_fwhm), int(oversampling),
+                            0 if rm is None else rm.shape[1], _dptr(rm), _iptr(status), _iptr(info))
     if rc != LQG_OK:
         raise RuntimeError(f"lqg_chunk_plan failed ({rc})")
     keys = ("n", "fisher_index_start", "nq", "kbin_upp", "res_index", "zbin_low", "zbin_upp", "input_index")

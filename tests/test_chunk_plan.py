@@ -84,3 +84,24 @@ def test_raw_spectra_and_planted_faults(engine_lib):
     assert list(status) == [OK, EMPTY, SHORT, SHORT, NO_TABLE, BAD_INPUT]
     assert info[0]["n"] == len(lam) - 10        # the masked ends are cut
     _compare(w.bins, w.tables, planted[:5], w.max_forest_length)
+
+
+@pytest.mark.parametrize("name", G.RESO_CASES + G.RESO_SIZE_CASES)
+def test_resolution_matrix_chunks(engine_lib, name):
+    """Chunks with resolution matrices (lqg_batch_add_reso's rules: RES_INDEX 0,
+    no table lookup), per-pixel rows as add_chunk_list_reso passes them."""
+    from lyspeq_gb300 import lqg
+    c = G.load(name)
+    osamp = c.reso[0]
+    rows = [np.asarray(rm) if osamp > 0 else np.asarray(rm).T for rm in c.rmats]
+    offs = np.cumsum([0] + [len(x[0]) for x in c.chunks])
+    cat = lambda j: np.concatenate([np.asarray(x[j], dtype=np.float64) for x in c.chunks])
+    status, info = lqg.chunk_plan(c.bins, c.tables, cat(0), cat(1), cat(2), offs, None, c.max_forest_length,
+                                  oversampling=osamp, resomat=np.concatenate(rows))
+    assert (status == OK).all()
+    keys = {(t.r_fwhm, round(t.dv, 1)): i for i, t in enumerate(c.tables)}
+    s = c.port_settings(P)
+    for (lam, d, iv, r), rm, m, inf in zip(c.chunks, c.rmats, c.meta, info):
+        ch = P.make_chunk(np.asarray(lam), np.asarray(d), np.asarray(iv), r, c.bins, keys, s, c.reso, rm)
+        got = (inf["n"], inf["fisher_index_start"], inf["nq"], inf["kbin_upp"], inf["res_index"])
+        assert got == (ch.n, ch.fisher_index_start, ch.nq, ch.kbin_upp, ch.res_index) == tuple(m[:4]) + (0,)
